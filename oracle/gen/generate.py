@@ -1,0 +1,92 @@
+"""Run an OpenSBLI problem script through the reference generator and keep its C output.
+
+Test infrastructure (oracle).  Usage, from the repository root:
+
+    python oracle/gen/generate.py --case tgv_central [--ref /root/reference] [--out oracle/_ref]
+
+The reference generator (opensbli, read-only, imported from --ref) runs unmodified under the
+compatibility shims in compat.py.  Its OPSC writer (code_generation/opsc.py:250-282) writes
+opensbli.cpp, opensbliblock00_kernels.h, defdec_data_set.h and bc_exchanges.h into
+<out>/<case>/.  The script's final substitute_simulation_parameters call
+(utilities/helperfunctions.py:130-149) is replaced by one that writes every `X=Input;` as
+`X = osb_param_i/d("X", <script value>);`, so one compiled binary takes its grid size, dt and
+step count from OSB_<X> environment variables at run time (ops_compat/ops_seq.h).
+"""
+import argparse
+import os
+import re
+import runpy
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+
+# case name -> problem script.  "ref:" paths are inside the reference tree, others under cases/.
+CASES = {
+    "tgv_central": "ref:apps/taylor_green_vortex/taylor_green_vortex.py",
+    "tgsym_central": "ref:apps/taylor_green_vortex/TGsym/TGsym.py",
+    "tgv_weno": "tgv_weno.py",
+    "katzer_teno": "katzer_teno.py",
+}
+
+
+def _runtime_substitution(constants, values, simulation_name="opensbli"):
+    path = "./%s.cpp" % simulation_name
+    with open(path) as f:
+        s = f.read()
+    for const, value in zip(constants, values):
+        old = const + "=Input;"
+        if old not in s:
+            continue
+        is_int = re.search(r"^int %s;" % re.escape(const), s, re.M) is not None
+        fn = "osb_param_i" if is_int else "osb_param_d"
+        s = s.replace(old, '%s = %s("%s", %s);' % (const, fn, const, value))
+    left = re.findall(r"(\w+)=Input;", s)
+    if left:
+        raise RuntimeError("constants left without a value: %s" % left)
+    with open(path, "w") as f:
+        f.write(s)
+
+
+def run_case_inproc(case, ref):
+    sys.path.insert(0, HERE)
+    sys.path.insert(0, ref)
+    import compat
+    compat.install()
+    import opensbli.utilities.helperfunctions as hf
+    hf.substitute_simulation_parameters = _runtime_substitution
+    script = CASES[case]
+    if script.startswith("ref:"):
+        script = os.path.join(ref, script[4:])
+    else:
+        script = os.path.join(HERE, "cases", script)
+    runpy.run_path(script, run_name="__main__")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--case", required=True, choices=sorted(CASES) + ["all"])
+    ap.add_argument("--ref", default="/root/reference")
+    ap.add_argument("--out", default=os.path.join(REPO, "oracle", "_ref"))
+    ap.add_argument("--inproc", action="store_true", help=argparse.SUPPRESS)
+    a = ap.parse_args()
+    if a.inproc:
+        run_case_inproc(a.case, a.ref)
+        return
+    cases = sorted(CASES) if a.case == "all" else [a.case]
+    for case in cases:
+        out = os.path.join(os.path.abspath(a.out), case)
+        os.makedirs(out, exist_ok=True)
+        log = os.path.join(out, "generate.log")
+        with open(log, "w") as lf:
+            r = subprocess.run([sys.executable, os.path.abspath(__file__), "--case", case, "--ref", a.ref, "--inproc"],
+                               cwd=out, stdout=lf, stderr=subprocess.STDOUT)
+        if r.returncode != 0:
+            sys.stderr.write(open(log).read()[-4000:])
+            raise SystemExit("generation of %s failed (log: %s)" % (case, log))
+        print("generated %s -> %s" % (case, out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,107 @@
+"""ctypes front-end to the C restatement in oracle/src (test infrastructure only).
+
+build() compiles oracle/src/osb_oracle.c with gcc into oracle/_build/libosb_oracle.so; the
+functions below wrap its entry points with numpy arrays laid out [var][z][y][x].
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "libosb_oracle.so")
+
+CONV = {"central_skew": 0, "weno5js": 1, "teno5": 2}
+VISC = {"none": 0, "const": 1, "sutherland": 2}
+RK = {"rk3": 0, "ls_rk3_ssp": 1}
+BC = {"periodic": 0, "symmetry": 1}
+
+
+class Cfg(ctypes.Structure):
+    _fields_ = [
+        ("ndim", ctypes.c_int),
+        ("n", ctypes.c_int * 3),
+        ("delta", ctypes.c_double * 3),
+        ("gama", ctypes.c_double),
+        ("Minf", ctypes.c_double),
+        ("Re", ctypes.c_double),
+        ("Pr", ctypes.c_double),
+        ("conv", ctypes.c_int),
+        ("visc", ctypes.c_int),
+        ("rk", ctypes.c_int),
+        ("bc", (ctypes.c_int * 2) * 3),
+        ("teno_ct", ctypes.c_double),
+        ("teno_eps", ctypes.c_double),
+        ("dt", ctypes.c_double),
+    ]
+
+
+def build(force=False):
+    src = os.path.join(HERE, "src", "osb_oracle.c")
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-std=c99", "-o", LIB, src, "-lm"])
+    return LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = ctypes.CDLL(build())
+        for name in ("osbo_tgv_init", "osbo_run", "osbo_residual"):
+            getattr(_lib, name).restype = ctypes.c_int
+    return _lib
+
+
+def make_cfg(n, delta, gama=1.4, Minf=0.1, Re=1600.0, Pr=0.71, conv="central_skew", visc="const", rk="rk3",
+             bc="periodic", dt=5e-3, teno_ct=1e-5, teno_eps=1e-15):
+    c = Cfg()
+    c.ndim = len(n) if len(n) == 2 else 3
+    nn = list(n) + [1] * (3 - len(n))
+    dd = list(delta) + [1.0] * (3 - len(delta))
+    for i in range(3):
+        c.n[i] = nn[i]
+        c.delta[i] = dd[i]
+    c.gama, c.Minf, c.Re, c.Pr = gama, Minf, Re, Pr
+    c.conv, c.visc, c.rk = CONV[conv], VISC[visc], RK[rk]
+    for d in range(3):
+        for s in range(2):
+            c.bc[d][s] = BC[bc if isinstance(bc, str) else bc[d][s]]
+    c.teno_ct, c.teno_eps, c.dt = teno_ct, teno_eps, dt
+    return c
+
+
+def _shape(c):
+    nv = 5 if c.ndim == 3 else 4
+    return (nv, c.n[2], c.n[1], c.n[0])
+
+
+def _ptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def tgv_init(c):
+    q = np.zeros(_shape(c), dtype=np.float64)
+    assert lib().osbo_tgv_init(ctypes.byref(c), _ptr(q)) == 0
+    return q
+
+
+def run(c, q0, nsteps, with_ke=False):
+    q = np.ascontiguousarray(q0, dtype=np.float64).copy()
+    ke = np.zeros(nsteps + 1, dtype=np.float64)
+    rc = lib().osbo_run(ctypes.byref(c), _ptr(q), int(nsteps), _ptr(ke) if with_ke else None)
+    assert rc == 0, rc
+    return (q, ke) if with_ke else q
+
+
+def residual(c, q0):
+    q = np.ascontiguousarray(q0, dtype=np.float64)
+    r = np.zeros_like(q)
+    assert lib().osbo_residual(ctypes.byref(c), _ptr(q), _ptr(r)) == 0
+    return r

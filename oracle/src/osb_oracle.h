@@ -1,0 +1,48 @@
+/* osb_oracle.h -- CPU restatement (FP64, plain C) of OpenSBLI's generated per-timestep algorithm.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is the parity oracle for the GB300 backend: tests, smoke() and
+ * bench.py's cpu_baseline leg may call it as the checker; the product never links or calls it.
+ * It is pinned against the reference generator's own C output run here (oracle/_ref, built by
+ * oracle/build_ref.py) and against committed golden fixtures (tests/golden/).
+ *
+ * Layout of every conserved/state array passed in or out: interior points only,
+ * [var][z][y][x], x fastest; var = rho, rhou0, rhou1[, rhou2], rhoE.
+ */
+#ifndef OSB_ORACLE_H
+#define OSB_ORACLE_H
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { OSBO_CONV_CENTRAL_SKEW = 0, OSBO_CONV_WENO5JS = 1, OSBO_CONV_TENO5 = 2 };
+enum { OSBO_VISC_NONE = 0, OSBO_VISC_CONST = 1, OSBO_VISC_SUTHERLAND = 2 };
+enum { OSBO_RK3_2REG = 0, OSBO_RK3_LS_SSP = 1 };
+enum { OSBO_BC_PERIODIC = 0, OSBO_BC_SYMMETRY = 1 };
+
+typedef struct {
+  int ndim;        /* 2 or 3 */
+  int n[3];        /* interior points per axis (n[2] = 1 in 2D) */
+  double delta[3]; /* grid spacing per axis */
+  double gama, Minf, Re, Pr;
+  int conv, visc, rk;
+  int bc[3][2];    /* per axis, per side */
+  double teno_ct, teno_eps;
+  double dt;
+} osbo_cfg;
+
+/* Taylor-Green initial condition (apps/taylor_green_vortex/taylor_green_vortex.py:87-101) on the
+ * interior points, x_i = delta_i * index_i. */
+int osbo_tgv_init(const osbo_cfg *cfg, double *q);
+
+/* Advance q (interior, in/out) by nsteps RK3 steps.  ke (may be NULL) receives nsteps+1 values of
+ * the volume-mean kinetic energy 0.5*rho*|u|^2 before the first and after every step. */
+int osbo_run(const osbo_cfg *cfg, double *q, int nsteps, double *ke);
+
+/* One residual evaluation R(q) on the interior (the right-hand side of one RK stage), for
+ * kernel-level parity tests.  r has the same layout as q. */
+int osbo_residual(const osbo_cfg *cfg, const double *q, double *r);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
