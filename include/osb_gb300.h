@@ -1,0 +1,146 @@
+/* osb_gb300.h -- C ABI of the GB300 backend for OpenSBLI's per-timestep hot path.
+ *
+ * The library replaces what the reference's OPSC writer (code_generation/opsc.py:250-282) emits
+ * and what OPS runs for it: the per-stage kernel list of the generated solver
+ * (code_generation/algorithm/algorithm.py:384-477) -- constituent relations, spatial residual,
+ * Runge-Kutta update and boundary halos -- as hand-written sm_103a CUDA kernels.  A problem script
+ * builds its TraditionalAlgorithmRK as before; opensbli_gb300.GB300Writer(alg) lowers it to an
+ * osb_plan_desc and drives this ABI through ctypes.  Plain C types only; device pointers are
+ * owned by the caller (torch tensors in the Python host) unless stated.
+ *
+ * Return codes: 0 ok, < 0 error (see OSB_E*); osb_get_error gives the message of the last error.
+ * Threading: one context per CUDA stream, not thread-safe on the same context.
+ */
+#ifndef OSB_GB300_H
+#define OSB_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OSB_ABI_VERSION 1
+
+/* error codes */
+#define OSB_OK 0
+#define OSB_EINVAL (-1)      /* bad plan or argument */
+#define OSB_EUNSUPPORTED (-2) /* plan asks for a kernel pattern this backend does not implement */
+#define OSB_ECUDA (-3)       /* CUDA runtime error */
+#define OSB_ENOTBOUND (-4)   /* a field is missing */
+#define OSB_ETIMEOUT (-5)    /* a bounded device wait gave up (device status word) */
+#define OSB_ENONFINITE (-6)  /* NaN/Inf found by osb_reduce(OSB_RED_NANCHECK) */
+
+/* convective schemes: Central(4) skew-symmetric (schemes/spatial/scheme.py:187-271, core/parsing.py:75-111),
+ * LLFWeno(5,'JS') (schemes/spatial/weno.py:474-521), LLFTeno(5) (schemes/spatial/teno.py:489-530) */
+#define OSB_CONV_CENTRAL_SKEW 0
+#define OSB_CONV_WENO5JS 1
+#define OSB_CONV_TENO5 2
+/* viscous terms: none, constant viscosity (taylor_green_vortex.py:18-19), Sutherland (katzer_SBLI.py:25) */
+#define OSB_VISC_NONE 0
+#define OSB_VISC_CONST 1
+#define OSB_VISC_SUTHERLAND 2
+/* time integration: RungeKutta(3) 2-register (schemes/temporal/rk_sbli.py:51-61, 117-124),
+ * RungeKuttaLS(3,'SSP') (schemes/temporal/rk_LS.py:71-101, 155-166) */
+#define OSB_RK3_2REG 0
+#define OSB_RK3_LS 1
+/* boundary conditions (core/boundary_conditions/periodic.py, symmetry.py, isothermal_wall.py ...) */
+#define OSB_BC_PERIODIC 0
+#define OSB_BC_SYMMETRY 1
+/* arithmetic: all FP64 (the reference's Double datatype, core/datatypes.py:2-13), or FP32 state
+ * and flux arithmetic with the RK accumulator in FP64 */
+#define OSB_PREC_FP64 0
+#define OSB_PREC_MIXED 1
+/* reductions */
+#define OSB_RED_KE 0        /* volume mean of 0.5*rho*|u|^2, FP64 */
+#define OSB_RED_ENSTROPHY 1 /* volume mean of 0.5*rho*|curl u|^2, FP64, 4th-order central curl */
+#define OSB_RED_NANCHECK 2  /* 1.0 if any conserved value is NaN/Inf, else 0.0 (apps/check.py:1-27) */
+
+typedef struct osb_plan_desc {
+  int abi_version;   /* OSB_ABI_VERSION */
+  int ndim;          /* 3 (2 reserved for the curvilinear 2D path) */
+  int n[3];          /* interior points per axis: block0np0..2 */
+  double delta[3];   /* Delta0block0..2 */
+  int conv, visc, rk, precision;
+  int bc[3][2];      /* OSB_BC_* per axis and side */
+  double gama, Minf, Re, Pr;
+  double weno_eps;   /* 1e-6 in the reference's WenoJS (weno.py:341-369) */
+  double teno_ct, teno_eps;
+  double rk_a[3];    /* rk_sbli: rkold[]; rk_LS: A[] */
+  double rk_b[3];    /* rk_sbli: rknew[]; rk_LS: B[] */
+  int use_graphs;    /* capture one RK3 step as a CUDA graph */
+} osb_plan_desc;
+
+/* Memory layout of every per-variable array: x fastest, interior point (i,j,k) at element
+ * offset + i + j*stride_y + k*stride_z, halo depths halo[3] on both sides. */
+typedef struct osb_layout {
+  int64_t numel;     /* elements per variable array, halos included */
+  int64_t offset;    /* element offset of interior point (0,0,0) */
+  int64_t stride_y, stride_z;
+  int halo[3];
+  int nvar;          /* 5 in 3D */
+  int state_bytes;   /* 8 (FP64) or 4 (mixed): element size of the bound state arrays */
+} osb_layout;
+
+typedef struct osb_ctx osb_ctx;
+
+/* Validate a plan and report the layout the state arrays must have.
+ * Replaces the dat declarations of defdec_data_set.h (code_generation/opsc.py:693-722). */
+int osb_query_layout(const osb_plan_desc *plan, osb_layout *out);
+
+/* Create a context; allocates the internal work arrays (second state buffer, FP64 RK register,
+ * residual, reduction scratch) on the current device.  Replaces ops_init/ops_decl_* of the
+ * generated main (code_generation/opsc.py:537-553). */
+int osb_create(const osb_plan_desc *plan, osb_ctx **out);
+
+/* Bind conserved variable `var` (0 rho, 1..3 rhou0..2, 4 rhoE) to a caller-owned device array of
+ * the osb_query_layout layout and element size; the library never frees it. */
+int osb_bind_field(osb_ctx *ctx, int var, void *dev_ptr);
+
+/* Stream for all work of this context (cudaStream_t as void*; NULL = legacy default stream). */
+int osb_set_stream(osb_ctx *ctx, void *stream);
+
+/* Taylor-Green initial condition on the interior (apps/taylor_green_vortex/taylor_green_vortex.py:
+ * 87-101, GridBasedInitialisation initialisation/gridbasedinit.py:15-57), computed in FP64 into the
+ * RK register and the bound state. */
+int osb_init_tgv(osb_ctx *ctx);
+
+/* Set / read the FP64 master copy of variable `var` from / into a device array of n0*n1*n2 doubles
+ * laid out [z][y][x] (interior only); setting also refreshes the bound state.  In FP64 mode the
+ * master copy is the state itself; in mixed mode it is the FP64 RK accumulator. */
+int osb_set_state64(osb_ctx *ctx, int var, const double *dev_interior);
+int osb_get_state64(osb_ctx *ctx, int var, double *dev_interior);
+
+/* Advance nsteps RK3 steps of size dt (the generated time loop, algorithm.py:440-474).  Work is
+ * stream-ordered; the call returns without synchronising.  On return the bound arrays hold the
+ * state with valid halos. */
+int osb_step(osb_ctx *ctx, int nsteps, double dt);
+
+/* Evaluate the spatial residual R(q) of the bound state into `var`-major device array out
+ * (5 * n0*n1*n2 values of the state precision, [var][z][y][x] interior) without advancing. */
+int osb_residual(osb_ctx *ctx, void *dev_out);
+
+/* FP64 reduction over the interior (OSB_RED_*); synchronises the context stream. */
+int osb_reduce(osb_ctx *ctx, int what, double *out);
+
+/* Number of kernel launches the last osb_step issued (for launch accounting). */
+int64_t osb_launch_count(osb_ctx *ctx);
+
+/* Per-kernel-family timing, the GPU counterpart of OPS's ops_timing_output (opsc.py:438-439):
+ * while enabled, osb_step runs without graph replay and brackets every launch with CUDA events.
+ * osb_profile(ctx, 1) also clears the totals.  osb_profile_read fills up to n entries of total
+ * milliseconds and launch counts for the families OSB_PF_* and returns the number of families. */
+#define OSB_PF_HALO 0
+#define OSB_PF_WENO_X 1
+#define OSB_PF_WENO_Y 2
+#define OSB_PF_WENO_Z 3
+#define OSB_PF_CENTRAL_RK 4
+int osb_profile(osb_ctx *ctx, int enable);
+int osb_profile_read(osb_ctx *ctx, double *total_ms, int64_t *counts, int n);
+
+int osb_get_error(osb_ctx *ctx, char *buf, int n);
+void osb_destroy(osb_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,579 @@
+// osb_api.cu -- the C ABI (include/osb_gb300.h): contexts, binding, the time loop, reductions.
+//
+// The time loop restates TraditionalAlgorithmRK.generate_solution (algorithm.py:384-477) for one
+// block: every RK stage fills the boundary halos of the current state, evaluates the residual and
+// applies the RK update into the other state buffer; the FP64 RK register is the master copy, so
+// the reference's per-iteration "Save equations" copy (rk_sbli.py:126-133) is needed only before
+// the first step after the caller wrote the state itself.  One step (three stages) can be
+// captured as a CUDA graph and replayed.
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "osb_common.cuh"
+#include "osb_internal.h"
+
+using namespace osb;
+
+struct osb_ctx : public Ctx {};
+
+namespace {
+
+int set_err(osb_ctx *c, int code, const char *msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+int cuda_err(osb_ctx *c, cudaError_t e, const char *where) {
+  if (e == cudaSuccess) return OSB_OK;
+  char buf[256];
+  snprintf(buf, sizeof buf, "%s: %s", where, cudaGetErrorString(e));
+  return set_err(c, OSB_ECUDA, buf);
+}
+
+int validate(const osb_plan_desc *p, char *why, size_t n) {
+  if (!p) { snprintf(why, n, "null plan"); return OSB_EINVAL; }
+  if (p->abi_version != OSB_ABI_VERSION) { snprintf(why, n, "abi_version %d != %d", p->abi_version, OSB_ABI_VERSION); return OSB_EINVAL; }
+  if (p->ndim != 3) { snprintf(why, n, "ndim %d: this library implements 3D blocks", p->ndim); return OSB_EUNSUPPORTED; }
+  for (int d = 0; d < 3; ++d) {
+    if (p->n[d] < 8 || p->n[d] > 4096) { snprintf(why, n, "n[%d] = %d out of range [8, 4096]", d, p->n[d]); return OSB_EINVAL; }
+    if (!(p->delta[d] > 0)) { snprintf(why, n, "delta[%d] must be > 0", d); return OSB_EINVAL; }
+    for (int s = 0; s < 2; ++s)
+      if (p->bc[d][s] != OSB_BC_PERIODIC && p->bc[d][s] != OSB_BC_SYMMETRY) {
+        snprintf(why, n, "bc[%d][%d] = %d not supported on 3D blocks", d, s, p->bc[d][s]);
+        return OSB_EUNSUPPORTED;
+      }
+    if ((p->bc[d][0] == OSB_BC_PERIODIC) != (p->bc[d][1] == OSB_BC_PERIODIC)) {
+      snprintf(why, n, "axis %d: periodic must be set on both sides", d);
+      return OSB_EINVAL;
+    }
+  }
+  if (p->conv != OSB_CONV_CENTRAL_SKEW && p->conv != OSB_CONV_WENO5JS) {
+    snprintf(why, n, "convective scheme %d not supported on 3D blocks", p->conv);
+    return OSB_EUNSUPPORTED;
+  }
+  if (p->visc != OSB_VISC_NONE && p->visc != OSB_VISC_CONST) {
+    snprintf(why, n, "viscosity model %d not supported on 3D blocks", p->visc);
+    return OSB_EUNSUPPORTED;
+  }
+  if (p->rk != OSB_RK3_2REG) { snprintf(why, n, "time scheme %d not supported on 3D blocks", p->rk); return OSB_EUNSUPPORTED; }
+  if (p->precision != OSB_PREC_FP64 && p->precision != OSB_PREC_MIXED) { snprintf(why, n, "precision %d", p->precision); return OSB_EINVAL; }
+  if (!(p->gama > 1.0) || !(p->Minf > 0) || !(p->Re > 0) || !(p->Pr > 0)) { snprintf(why, n, "bad physical constants"); return OSB_EINVAL; }
+  return OSB_OK;
+}
+
+Grid make_grid(const osb_plan_desc *p) {
+  Grid g;
+  g.n0 = p->n[0];
+  g.n1 = p->n[1];
+  g.n2 = p->n[2];
+  int64_t px = p->n[0] + 2 * HX;
+  px = (px + 7) / 8 * 8;  // rows start on 32-byte boundaries for both element sizes
+  const int64_t py = p->n[1] + 2 * HY, pz = p->n[2] + 2 * HZ;
+  g.sy = px;
+  g.sz = px * py;
+  g.off0 = HX + HY * g.sy + HZ * g.sz;
+  g.numel = px * py * pz;
+  return g;
+}
+
+template <typename T> Fields5<T> fields(void *const *a) {
+  Fields5<T> f;
+  for (int v = 0; v < 5; ++v) f.v[v] = static_cast<T *>(a[v]);
+  return f;
+}
+Fields5<double> fields_d(double *const *a) {
+  Fields5<double> f;
+  for (int v = 0; v < 5; ++v) f.v[v] = a[v];
+  return f;
+}
+
+// ---------------------------------------------------------------------------------------------
+// small kernels: initial condition, state copies, packing, reductions
+// ---------------------------------------------------------------------------------------------
+template <typename T>
+__global__ void k_init_tgv(Grid g, Fields5<T> q, Fields5<double> qold, double d0, double d1, double d2, double gama,
+                           double Minf) {
+  const int64_t N = (int64_t)g.n0 * g.n1 * g.n2;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.n0), j = (int)((t / g.n0) % g.n1), k = (int)(t / ((int64_t)g.n0 * g.n1));
+    const double x0 = d0 * i, x1 = d1 * j, x2 = d2 * k;
+    const double u0 = sin(x0) * cos(x1) * cos(x2), u1 = -sin(x1) * cos(x0) * cos(x2), u2 = 0.0;
+    const double p = (0.0625 * cos(2.0 * x0) + 0.0625 * cos(2.0 * x1)) * (cos(2.0 * x2) + 2.0) + 1.0 / (Minf * Minf * gama);
+    const double r = Minf * Minf * gama * p;
+    const double vals[5] = {r, r * u0, r * u1, r * u2, p / (gama - 1) + 0.5 * r * (u0 * u0 + u1 * u1 + u2 * u2)};
+    const int64_t n = gidx(g, i, j, k);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      qold.v[v][n] = vals[v];
+      q.v[v][n] = (T)vals[v];
+    }
+  }
+}
+
+template <typename T> __global__ void k_save(Grid g, Fields5<const T> q, Fields5<double> qold) {
+  const int64_t N = (int64_t)g.n0 * g.n1 * g.n2;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.n0), j = (int)((t / g.n0) % g.n1), k = (int)(t / ((int64_t)g.n0 * g.n1));
+    const int64_t n = gidx(g, i, j, k);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) qold.v[v][n] = (double)q.v[v][n];
+  }
+}
+
+template <typename T> __global__ void k_set64(Grid g, const double *src, T *q, double *qold) {
+  const int64_t N = (int64_t)g.n0 * g.n1 * g.n2;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.n0), j = (int)((t / g.n0) % g.n1), k = (int)(t / ((int64_t)g.n0 * g.n1));
+    const int64_t n = gidx(g, i, j, k);
+    qold[n] = src[t];
+    q[n] = (T)src[t];
+  }
+}
+
+__global__ void k_get64(Grid g, const double *qold, double *dst) {
+  const int64_t N = (int64_t)g.n0 * g.n1 * g.n2;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.n0), j = (int)((t / g.n0) % g.n1), k = (int)(t / ((int64_t)g.n0 * g.n1));
+    dst[t] = qold[gidx(g, i, j, k)];
+  }
+}
+
+template <typename T> __global__ void k_pack(Grid g, Fields5<const T> r, T *dst) {
+  const int64_t N = (int64_t)g.n0 * g.n1 * g.n2;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.n0), j = (int)((t / g.n0) % g.n1), k = (int)(t / ((int64_t)g.n0 * g.n1));
+    const int64_t n = gidx(g, i, j, k);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) dst[v * N + t] = r.v[v][n];
+  }
+}
+
+// Block-partial FP64 sums, then one block adds the partials in a fixed order (deterministic).
+constexpr int RED_THREADS = 256;
+__device__ __forceinline__ double block_sum(double x) {
+  __shared__ double sh[RED_THREADS / 32];
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = x;
+  __syncthreads();
+  x = threadIdx.x < RED_THREADS / 32 ? sh[threadIdx.x] : 0.0;
+  if (threadIdx.x < 32)
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_down_sync(0xffffffffu, x, o);
+  return x;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(RED_THREADS) k_reduce(Grid g, Fields5<const double> qold, Fields5<const T> q, int what,
+                                                        double i0, double i1, double i2, double *partial) {
+  const int64_t N = (int64_t)g.n0 * g.n1 * g.n2;
+  double acc = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.n0), j = (int)((t / g.n0) % g.n1), k = (int)(t / ((int64_t)g.n0 * g.n1));
+    const int64_t n = gidx(g, i, j, k);
+    if (what == OSB_RED_KE) {
+      const double r = qold.v[0][n];
+      acc += 0.5 * (qold.v[1][n] * qold.v[1][n] + qold.v[2][n] * qold.v[2][n] + qold.v[3][n] * qold.v[3][n]) / r;
+    } else if (what == OSB_RED_NANCHECK) {
+      for (int v = 0; v < 5; ++v)
+        if (!isfinite((double)q.v[v][n])) acc = 1.0;
+    } else {  // enstrophy: 0.5 rho |curl u|^2 with 4th-order central first derivatives
+      const double c1[5] = {1.0 / 12.0, -2.0 / 3.0, 0.0, 2.0 / 3.0, -1.0 / 12.0};
+      const int64_t st[3] = {1, g.sy, g.sz};
+      const double id[3] = {i0, i1, i2};
+      double du[3][3];
+      for (int c = 0; c < 3; ++c)
+        for (int d = 0; d < 3; ++d) {
+          double s = 0.0;
+          for (int o = -2; o <= 2; ++o) {
+            if (!o) continue;
+            const int64_t m = n + o * st[d];
+            s += c1[o + 2] * ((double)q.v[1 + c][m] / (double)q.v[0][m]);
+          }
+          du[c][d] = s * id[d];
+        }
+      const double w0 = du[2][1] - du[1][2], w1 = du[0][2] - du[2][0], w2 = du[1][0] - du[0][1];
+      acc += 0.5 * qold.v[0][n] * (w0 * w0 + w1 * w1 + w2 * w2);
+    }
+  }
+  const double s = block_sum(acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = (what == OSB_RED_NANCHECK) ? (s > 0 ? 1.0 : 0.0) : s;
+}
+
+__global__ void k_reduce_final(const double *partial, int nb, int what, double scale, double *out) {
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) acc += partial[b];
+  const double s = block_sum(acc);
+  if (threadIdx.x == 0) out[0] = what == OSB_RED_NANCHECK ? (s > 0 ? 1.0 : 0.0) : s * scale;
+}
+
+int blocks_for(int64_t n) {
+  int64_t b = (n + 255) / 256;
+  if (b > 152 * 8) b = 152 * 8;
+  return (int)(b < 1 ? 1 : b);
+}
+
+// ---------------------------------------------------------------------------------------------
+// per-family event timing (eager path only)
+// ---------------------------------------------------------------------------------------------
+struct ProfScope {
+  osb_ctx *c;
+  int family;
+  cudaStream_t s;
+  cudaEvent_t a = nullptr;
+  ProfScope(osb_ctx *c_, int f, cudaStream_t s_) : c(c_), family(f), s(s_) {
+    if (c->prof_on) {
+      cudaEventCreate(&a);
+      cudaEventRecord(a, s);
+    }
+  }
+  ~ProfScope() {
+    if (c->prof_on) {
+      cudaEvent_t b;
+      cudaEventCreate(&b);
+      cudaEventRecord(b, s);
+      c->prof_pending.push_back({family, a, b});
+    }
+  }
+};
+
+void prof_collect(osb_ctx *c) {
+  for (auto &r : c->prof_pending) {
+    float ms = 0;
+    cudaEventSynchronize(r.b);
+    cudaEventElapsedTime(&ms, r.a, r.b);
+    c->prof_ms[r.family] += ms;
+    c->prof_n[r.family] += 1;
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  c->prof_pending.clear();
+}
+
+// ---------------------------------------------------------------------------------------------
+// time loop
+// ---------------------------------------------------------------------------------------------
+template <typename T> void weno_all(osb_ctx *c, Fields5<const T> qc, Fields5<T> r, cudaStream_t s) {
+  for (int d = 0; d < 3; ++d) {
+    ProfScope ps(c, PF_WENO_X + d, s);
+    launch_weno_dir<T>(*c, qc, r, d, s, &c->launches);
+  }
+}
+
+template <typename T> void residual_into(osb_ctx *c, int cur, cudaStream_t s) {
+  void **qs = cur == 0 ? c->qa : c->qb;
+  Fields5<T> q = fields<T>(qs);
+  Fields5<const T> qc = fields<const T>(qs);
+  Fields5<T> r = fields<T>(c->res);
+  launch_halos<T>(*c, q, s, &c->launches);
+  if (c->plan.conv == OSB_CONV_WENO5JS) {
+    weno_all<T>(c, qc, r, s);
+    const int mode = CRK_RIN | (c->plan.visc == OSB_VISC_CONST ? CRK_VISC : 0);
+    launch_central_rk<T>(*c, qc, r, fields_d(c->qold), r, r, 0.0, 0.0, mode, s, &c->launches);
+  } else {
+    const int mode = CRK_SKEW | (c->plan.visc == OSB_VISC_CONST ? CRK_VISC : 0);
+    launch_central_rk<T>(*c, qc, r, fields_d(c->qold), r, r, 0.0, 0.0, mode, s, &c->launches);
+  }
+}
+
+template <typename T> void one_step(osb_ctx *c, int start, double dt, cudaStream_t s) {
+  int cur = start;
+  for (int st = 0; st < 3; ++st) {
+    void **qs = cur == 0 ? c->qa : c->qb;
+    void **qn = cur == 0 ? c->qb : c->qa;
+    Fields5<T> q = fields<T>(qs);
+    Fields5<const T> qc = fields<const T>(qs);
+    Fields5<T> r = fields<T>(c->res);
+    {
+      ProfScope ps(c, PF_HALO, s);
+      launch_halos<T>(*c, q, s, &c->launches);
+    }
+    const double dtn = dt * c->plan.rk_b[st], dto = dt * c->plan.rk_a[st];
+    const int visc = c->plan.visc == OSB_VISC_CONST ? CRK_VISC : 0;
+    if (c->plan.conv == OSB_CONV_WENO5JS) {
+      weno_all<T>(c, qc, r, s);
+      ProfScope ps(c, PF_CENTRAL_RK, s);
+      launch_central_rk<T>(*c, qc, fields<T>(qn), fields_d(c->qold), r, r, dtn, dto, CRK_RIN | visc | CRK_UPDATE, s,
+                           &c->launches);
+    } else {
+      ProfScope ps(c, PF_CENTRAL_RK, s);
+      launch_central_rk<T>(*c, qc, fields<T>(qn), fields_d(c->qold), r, r, dtn, dto, CRK_SKEW | visc | CRK_UPDATE, s,
+                           &c->launches);
+    }
+    cur ^= 1;
+  }
+}
+
+template <typename T> int step_impl(osb_ctx *c, int nsteps, double dt) {
+  cudaStream_t s = c->stream;
+  c->launches = 0;
+  if (!c->qold_valid) {
+    k_save<T><<<blocks_for((int64_t)c->g.n0 * c->g.n1 * c->g.n2), 256, 0, s>>>(c->g, fields<const T>(c->qa),
+                                                                               fields_d(c->qold));
+    ++c->launches;
+    c->qold_valid = 1;
+  }
+  for (int it = 0; it < nsteps; ++it) {
+    const int start = c->cur;
+    // graphs need a capturable stream: not the legacy default stream
+    if (c->plan.use_graphs && !c->prof_on && c->stream != nullptr) {
+      if (c->graph[start] && c->graph_dt[start] != dt) {
+        cudaGraphExecDestroy(c->graph[start]);
+        c->graph[start] = nullptr;
+      }
+      if (!c->graph[start]) {
+        cudaGraph_t gr;
+        int64_t l0 = c->launches;
+        cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_err(c, e, "cudaStreamBeginCapture");
+        one_step<T>(c, start, dt, s);
+        e = cudaStreamEndCapture(s, &gr);
+        if (e != cudaSuccess) return cuda_err(c, e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&c->graph[start], gr, 0);
+        cudaGraphDestroy(gr);
+        if (e != cudaSuccess) return cuda_err(c, e, "cudaGraphInstantiate");
+        c->graph_dt[start] = dt;
+        c->graph_launches = c->launches - l0;
+        c->launches = l0;
+      }
+      cudaError_t e = cudaGraphLaunch(c->graph[start], s);
+      if (e != cudaSuccess) return cuda_err(c, e, "cudaGraphLaunch");
+      c->launches += c->graph_launches;
+    } else {
+      one_step<T>(c, start, dt, s);
+    }
+    c->cur ^= 1;  // three stages flip the buffer
+  }
+  if (c->cur == 1) {
+    for (int v = 0; v < 5; ++v) {
+      cudaError_t e = cudaMemcpyAsync(c->qa[v], c->qb[v], (size_t)c->g.numel * c->elem, cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return cuda_err(c, e, "copy back");
+    }
+    c->cur = 0;
+  }
+  launch_halos<T>(*c, fields<T>(c->qa), s, &c->launches);
+  if (c->prof_on) prof_collect(c);
+  return cuda_err(c, cudaGetLastError(), "osb_step launch");
+}
+
+}  // namespace
+
+extern "C" {
+
+int osb_query_layout(const osb_plan_desc *plan, osb_layout *out) {
+  char why[256];
+  int rc = validate(plan, why, sizeof why);
+  if (rc) return rc;
+  if (!out) return OSB_EINVAL;
+  Grid g = make_grid(plan);
+  out->numel = g.numel;
+  out->offset = g.off0;
+  out->stride_y = g.sy;
+  out->stride_z = g.sz;
+  out->halo[0] = HX;
+  out->halo[1] = HY;
+  out->halo[2] = HZ;
+  out->nvar = 5;
+  out->state_bytes = plan->precision == OSB_PREC_MIXED ? 4 : 8;
+  return OSB_OK;
+}
+
+int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
+  if (!out) return OSB_EINVAL;
+  *out = nullptr;
+  char why[256];
+  int rc = validate(plan, why, sizeof why);
+  if (rc) {
+    fprintf(stderr, "osb_create: %s\n", why);
+    return rc;
+  }
+  osb_ctx *c = new (std::nothrow) osb_ctx();
+  if (!c) return OSB_EINVAL;
+  c->plan = *plan;
+  c->g = make_grid(plan);
+  c->mixed = plan->precision == OSB_PREC_MIXED;
+  c->elem = c->mixed ? 4 : 8;
+  c->ph.gama = plan->gama;
+  c->ph.Minf = plan->Minf;
+  c->ph.Re = plan->Re;
+  c->ph.Pr = plan->Pr;
+  for (int d = 0; d < 3; ++d) c->ph.inv_delta[d] = 1.0 / plan->delta[d];
+  c->ph.weno_eps = plan->weno_eps > 0 ? plan->weno_eps : 1e-6;
+  const size_t bytes = (size_t)c->g.numel * c->elem;
+  if (c->mixed) { setup_central<float>(); setup_weno<float>(); }
+  else { setup_central<double>(); setup_weno<double>(); }
+  cudaError_t e = cudaGetLastError();
+  for (int v = 0; v < 5 && e == cudaSuccess; ++v) {
+    e = cudaMalloc(&c->qb[v], bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&c->qold[v], (size_t)c->g.numel * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&c->res[v], bytes);
+    if (e == cudaSuccess) e = cudaMemset(c->qb[v], 0, bytes);
+    if (e == cudaSuccess) e = cudaMemset(c->qold[v], 0, (size_t)c->g.numel * sizeof(double));
+    if (e == cudaSuccess) e = cudaMemset(c->res[v], 0, bytes);
+  }
+  c->red_blocks = 152 * 8;
+  if (e == cudaSuccess) e = cudaMalloc(&c->red, (c->red_blocks + 1) * sizeof(double));
+  if (e != cudaSuccess) {
+    fprintf(stderr, "osb_create: %s\n", cudaGetErrorString(e));
+    osb_destroy(c);
+    return OSB_ECUDA;
+  }
+  *out = c;
+  return OSB_OK;
+}
+
+int osb_bind_field(osb_ctx *c, int var, void *dev_ptr) {
+  if (!c) return OSB_EINVAL;
+  if (var < 0 || var >= 5) return set_err(c, OSB_EINVAL, "var out of range");
+  if (!dev_ptr || ((uintptr_t)dev_ptr % 32) != 0) return set_err(c, OSB_EINVAL, "device pointer null or not 32-byte aligned");
+  c->qa[var] = dev_ptr;
+  c->qold_valid = 0;
+  c->cur = 0;
+  for (int s = 0; s < 2; ++s)
+    if (c->graph[s]) { cudaGraphExecDestroy(c->graph[s]); c->graph[s] = nullptr; }
+  return OSB_OK;
+}
+
+int osb_set_stream(osb_ctx *c, void *stream) {
+  if (!c) return OSB_EINVAL;
+  c->stream = (cudaStream_t)stream;
+  for (int s = 0; s < 2; ++s)
+    if (c->graph[s]) { cudaGraphExecDestroy(c->graph[s]); c->graph[s] = nullptr; }
+  return OSB_OK;
+}
+
+static int check_bound(osb_ctx *c) {
+  for (int v = 0; v < 5; ++v)
+    if (!c->qa[v]) return set_err(c, OSB_ENOTBOUND, "a conserved variable is not bound");
+  return OSB_OK;
+}
+
+int osb_init_tgv(osb_ctx *c) {
+  if (!c) return OSB_EINVAL;
+  if (int rc = check_bound(c)) return rc;
+  const int nb = blocks_for((int64_t)c->g.n0 * c->g.n1 * c->g.n2);
+  const osb_plan_desc &p = c->plan;
+  if (c->mixed)
+    k_init_tgv<float><<<nb, 256, 0, c->stream>>>(c->g, fields<float>(c->qa), fields_d(c->qold), p.delta[0], p.delta[1], p.delta[2], p.gama, p.Minf);
+  else
+    k_init_tgv<double><<<nb, 256, 0, c->stream>>>(c->g, fields<double>(c->qa), fields_d(c->qold), p.delta[0], p.delta[1], p.delta[2], p.gama, p.Minf);
+  c->qold_valid = 1;
+  c->cur = 0;
+  int64_t l = 0;
+  if (c->mixed) launch_halos<float>(*c, fields<float>(c->qa), c->stream, &l);
+  else launch_halos<double>(*c, fields<double>(c->qa), c->stream, &l);
+  return cuda_err(c, cudaGetLastError(), "osb_init_tgv");
+}
+
+int osb_set_state64(osb_ctx *c, int var, const double *src) {
+  if (!c) return OSB_EINVAL;
+  if (int rc = check_bound(c)) return rc;
+  if (var < 0 || var >= 5 || !src) return set_err(c, OSB_EINVAL, "bad var or pointer");
+  const int nb = blocks_for((int64_t)c->g.n0 * c->g.n1 * c->g.n2);
+  if (c->mixed) k_set64<float><<<nb, 256, 0, c->stream>>>(c->g, src, (float *)c->qa[var], c->qold[var]);
+  else k_set64<double><<<nb, 256, 0, c->stream>>>(c->g, src, (double *)c->qa[var], c->qold[var]);
+  c->qold_valid = 1;
+  c->cur = 0;
+  if (var == 4) {
+    int64_t l = 0;
+    if (c->mixed) launch_halos<float>(*c, fields<float>(c->qa), c->stream, &l);
+    else launch_halos<double>(*c, fields<double>(c->qa), c->stream, &l);
+  }
+  return cuda_err(c, cudaGetLastError(), "osb_set_state64");
+}
+
+int osb_get_state64(osb_ctx *c, int var, double *dst) {
+  if (!c) return OSB_EINVAL;
+  if (var < 0 || var >= 5 || !dst) return set_err(c, OSB_EINVAL, "bad var or pointer");
+  if (!c->qold_valid) return set_err(c, OSB_EINVAL, "no state yet: call osb_init_tgv, osb_set_state64 or osb_step");
+  const int nb = blocks_for((int64_t)c->g.n0 * c->g.n1 * c->g.n2);
+  k_get64<<<nb, 256, 0, c->stream>>>(c->g, c->qold[var], dst);
+  return cuda_err(c, cudaGetLastError(), "osb_get_state64");
+}
+
+int osb_step(osb_ctx *c, int nsteps, double dt) {
+  if (!c) return OSB_EINVAL;
+  if (int rc = check_bound(c)) return rc;
+  if (nsteps < 0 || !(dt > 0)) return set_err(c, OSB_EINVAL, "nsteps >= 0 and dt > 0 required");
+  return c->mixed ? step_impl<float>(c, nsteps, dt) : step_impl<double>(c, nsteps, dt);
+}
+
+int osb_residual(osb_ctx *c, void *dev_out) {
+  if (!c) return OSB_EINVAL;
+  if (int rc = check_bound(c)) return rc;
+  if (!dev_out) return set_err(c, OSB_EINVAL, "null output");
+  const int nb = blocks_for((int64_t)c->g.n0 * c->g.n1 * c->g.n2);
+  if (c->mixed) {
+    residual_into<float>(c, c->cur, c->stream);
+    k_pack<float><<<nb, 256, 0, c->stream>>>(c->g, fields<const float>(c->res), (float *)dev_out);
+  } else {
+    residual_into<double>(c, c->cur, c->stream);
+    k_pack<double><<<nb, 256, 0, c->stream>>>(c->g, fields<const double>(c->res), (double *)dev_out);
+  }
+  return cuda_err(c, cudaGetLastError(), "osb_residual");
+}
+
+int osb_reduce(osb_ctx *c, int what, double *out) {
+  if (!c || !out) return OSB_EINVAL;
+  if (int rc = check_bound(c)) return rc;
+  if (what < OSB_RED_KE || what > OSB_RED_NANCHECK) return set_err(c, OSB_EINVAL, "unknown reduction");
+  if (!c->qold_valid) return set_err(c, OSB_EINVAL, "no state yet");
+  void **qs = c->cur == 0 ? c->qa : c->qb;
+  const int64_t N = (int64_t)c->g.n0 * c->g.n1 * c->g.n2;
+  int nb = blocks_for(N);
+  if (nb > c->red_blocks) nb = c->red_blocks;
+  Fields5<const double> qo;
+  for (int v = 0; v < 5; ++v) qo.v[v] = c->qold[v];
+  const double *id = c->ph.inv_delta;
+  if (c->mixed) k_reduce<float><<<nb, RED_THREADS, 0, c->stream>>>(c->g, qo, fields<const float>(qs), what, id[0], id[1], id[2], c->red);
+  else k_reduce<double><<<nb, RED_THREADS, 0, c->stream>>>(c->g, qo, fields<const double>(qs), what, id[0], id[1], id[2], c->red);
+  k_reduce_final<<<1, RED_THREADS, 0, c->stream>>>(c->red, nb, what, 1.0 / (double)N, c->red + c->red_blocks);
+  double h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, c->red + c->red_blocks, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) return cuda_err(c, e, "osb_reduce");
+  *out = h;
+  if (what == OSB_RED_NANCHECK && h != 0.0) return set_err(c, OSB_ENONFINITE, "non-finite value in the state");
+  return OSB_OK;
+}
+
+int64_t osb_launch_count(osb_ctx *c) { return c ? c->launches : -1; }
+
+int osb_profile(osb_ctx *c, int enable) {
+  if (!c) return OSB_EINVAL;
+  c->prof_on = enable ? 1 : 0;
+  for (int f = 0; f < PF_COUNT; ++f) {
+    c->prof_ms[f] = 0;
+    c->prof_n[f] = 0;
+  }
+  return OSB_OK;
+}
+
+int osb_profile_read(osb_ctx *c, double *total_ms, int64_t *counts, int n) {
+  if (!c || !total_ms || !counts) return OSB_EINVAL;
+  for (int f = 0; f < n && f < PF_COUNT; ++f) {
+    total_ms[f] = c->prof_ms[f];
+    counts[f] = c->prof_n[f];
+  }
+  return PF_COUNT;
+}
+
+int osb_get_error(osb_ctx *c, char *buf, int n) {
+  if (!c || !buf || n <= 0) return OSB_EINVAL;
+  snprintf(buf, (size_t)n, "%s", c->err.c_str());
+  return OSB_OK;
+}
+
+void osb_destroy(osb_ctx *c) {
+  if (!c) return;
+  for (int s = 0; s < 2; ++s)
+    if (c->graph[s]) cudaGraphExecDestroy(c->graph[s]);
+  for (int v = 0; v < 5; ++v) {
+    cudaFree(c->qb[v]);
+    cudaFree(c->qold[v]);
+    cudaFree(c->res[v]);
+  }
+  cudaFree(c->red);
+  delete c;
+}
+
+}  // extern "C"

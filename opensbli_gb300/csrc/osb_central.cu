@@ -1,0 +1,283 @@
+// osb_central.cu -- fused central-difference RHS and Runge-Kutta update.
+//
+// One kernel evaluates, per interior point, everything the generated solver spreads over its
+// "CR*", "Convective terms group d", "Convective CD ...", "Convective residual", "Viscous CD ...",
+// "Viscous residual", "Sub stage advancement" and "Temporal solution advancement" kernels
+// (algorithm.py:384-477; probe census: ~75 ops_par_loops and ~45 full-grid work arrays per stage),
+// without any intermediate array in HBM:
+//   * constituent relations u_i = rhou_i/rho, p = (gama-1)(rhoE - 1/2 rho |u|^2),
+//     T = gama Minf^2 p/rho (apps/taylor_green_vortex/taylor_green_vortex.py:30-32);
+//   * skew-symmetric convective terms (core/parsing.py:75-111, schemes/spatial/scheme.py:187-271)
+//       mass    -1/2 [ d_j(rho u_j) + u_j d_j rho + rho d_j u_j ]
+//       mom_i   -1/2 [ d_j(rhou_i u_j) + u_j d_j rhou_i + rhou_i d_j u_j ] - d_i p
+//       energy  -1/2 [ d_j(rhoE u_j) + u_j d_j rhoE + rhoE d_j u_j ] - d_j(p u_j);
+//   * viscous and heat-flux terms, constant viscosity (taylor_green_vortex.py:18-19), expanded as
+//     the generated "Viscous residual" kernel: mom_i += (lap u_i + 1/3 d_i div u)/Re,
+//     energy += kT lap T + tau_ij d_j u_i + u_i d_j tau_ij, mixed second derivatives as nested
+//     first derivatives, inner axis the lower one (scheme.py:360-387);
+//   * 4th-order central weights (opensblifunctions.py:485-521, scheme.py:81-85);
+//   * the 2-register RK3 update (schemes/temporal/rk_sbli.py:117-124):
+//       q = qold + dt*rknew[s]*R,  qold = qold + dt*rkold[s]*R   (qold kept in FP64).
+//
+// Tiling: a 32x8 (x,y) tile per block marches through a chunk of z.  A ring of 5 shared-memory
+// planes holds the primitive fields of planes k-2..k+2 with a 2-point x/y halo, so every first,
+// second and mixed derivative of the stencil is read from shared memory; each global point is
+// loaded once per plane visit (coalesced along x).
+#include <cstdio>
+
+#include "osb_common.cuh"
+#include "osb_internal.h"
+
+namespace osb {
+
+namespace {
+constexpr int TX = 32, TY = 8, PX = TX + 4, PY = TY + 4, NF = 7, NP = 5;
+enum { F_RHO = 0, F_U0, F_U1, F_U2, F_P, F_T, F_E };
+
+template <typename T> struct SmemC {
+  T s[NP][NF][PY][PX];
+};
+}  // namespace
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256) k_central_rk(Grid g, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold,
+                                                    Fields5<T> rin, Fields5<T> rout, Phys ph, double dt_new,
+                                                    double dt_old, int zchunk) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  SmemC<T> &sm = *reinterpret_cast<SmemC<T> *>(smem_raw);
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * zchunk;
+  const int k1 = min(k0 + zchunk, g.n2);
+  const T gm1 = T(ph.gama - 1.0);
+  const T gM2 = T(ph.Minf * ph.Minf * ph.gama);
+
+  auto slot = [](int k) { return ((k % NP) + NP) % NP; };
+  auto load_plane = [&](int k) {
+    const int sl = slot(k);
+    for (int e = tid; e < PX * PY; e += TX * TY) {
+      const int px = e % PX, py = e / PX;
+      const int i = i0 - 2 + px, j = j0 - 2 + py;
+      if (i >= g.n0 + 2 || j >= g.n1 + 2) continue;
+      const int64_t n = gidx(g, i, j, k);
+      const T rho = q.v[0][n];
+      const T u0 = q.v[1][n] / rho, u1 = q.v[2][n] / rho, u2 = q.v[3][n] / rho;
+      const T E = q.v[4][n];
+      const T half = T(0.5);
+      const T p = gm1 * (E - half * rho * u0 * u0 - half * rho * u1 * u1 - half * rho * u2 * u2);
+      sm.s[sl][F_RHO][py][px] = rho;
+      sm.s[sl][F_U0][py][px] = u0;
+      sm.s[sl][F_U1][py][px] = u1;
+      sm.s[sl][F_U2][py][px] = u2;
+      sm.s[sl][F_P][py][px] = p;
+      sm.s[sl][F_T][py][px] = gM2 * p / rho;
+      sm.s[sl][F_E][py][px] = E;
+    }
+  };
+
+  const T c1[5] = {T(1.0 / 12.0), T(-2.0 / 3.0), T(0), T(2.0 / 3.0), T(-1.0 / 12.0)};
+  const T c2[5] = {T(-1.0 / 12.0), T(4.0 / 3.0), T(-2.5), T(4.0 / 3.0), T(-1.0 / 12.0)};
+  const T idl[3] = {T(ph.inv_delta[0]), T(ph.inv_delta[1]), T(ph.inv_delta[2])};
+
+  for (int k = k0 - 2; k < k0 + 2; ++k) load_plane(k);
+  for (int k = k0; k < k1; ++k) {
+    load_plane(k + 2);
+    __syncthreads();
+    const int i = i0 + tx, j = j0 + ty;
+    if (i < g.n0 && j < g.n1) {
+      // field f at offset (dz, dy, dx) from the output point
+      auto S = [&](int f, int dz, int dy, int dx) -> T { return sm.s[slot(k + dz)][f][ty + 2 + dy][tx + 2 + dx]; };
+      auto SA = [&](int f, int axis, int o) -> T {
+        return axis == 0 ? S(f, 0, 0, o) : axis == 1 ? S(f, 0, o, 0) : S(f, o, 0, 0);
+      };
+      T R[5] = {T(0), T(0), T(0), T(0), T(0)};
+      // first derivatives of the velocity, shared by both parts: du[c][d] = d_d u_c
+      T du[3][3];
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          T acc = T(0);
+#pragma unroll
+          for (int t = 0; t < 5; ++t)
+            if (t != 2) acc += c1[t] * SA(F_U0 + c, d, t - 2);
+          du[c][d] = acc * idl[d];
+        }
+      const T divu = du[0][0] + du[1][1] + du[2][2];
+      const T rho0 = S(F_RHO, 0, 0, 0), uu[3] = {S(F_U0, 0, 0, 0), S(F_U1, 0, 0, 0), S(F_U2, 0, 0, 0)};
+
+      if (MODE & CRK_SKEW) {
+        const T phi0[5] = {rho0, rho0 * uu[0], rho0 * uu[1], rho0 * uu[2], S(F_E, 0, 0, 0)};
+        T acc[5] = {T(0), T(0), T(0), T(0), T(0)};
+        T dpu = T(0);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          T dphi[5] = {T(0), T(0), T(0), T(0), T(0)}, dphiu[5] = {T(0), T(0), T(0), T(0), T(0)};
+          T dp = T(0), dpud = T(0);
+#pragma unroll
+          for (int t = 0; t < 5; ++t) {
+            if (t == 2) continue;
+            const T r = SA(F_RHO, d, t - 2), ud = SA(F_U0 + d, d, t - 2), p = SA(F_P, d, t - 2);
+            const T phi[5] = {r, r * SA(F_U0, d, t - 2), r * SA(F_U1, d, t - 2), r * SA(F_U2, d, t - 2),
+                              SA(F_E, d, t - 2)};
+#pragma unroll
+            for (int v = 0; v < 5; ++v) {
+              dphi[v] += c1[t] * phi[v];
+              dphiu[v] += c1[t] * (phi[v] * ud);
+            }
+            dp += c1[t] * p;
+            dpud += c1[t] * (p * ud);
+          }
+#pragma unroll
+          for (int v = 0; v < 5; ++v) acc[v] += (dphiu[v] + uu[d] * dphi[v]) * idl[d];
+          R[1 + d] -= dp * idl[d];
+          dpu += dpud * idl[d];
+        }
+#pragma unroll
+        for (int v = 0; v < 5; ++v) R[v] -= T(0.5) * (acc[v] + phi0[v] * divu);
+        R[4] -= dpu;
+      }
+
+      if (MODE & CRK_VISC) {
+        const T invRe = T(1.0 / ph.Re);
+        const T kT = T(1.0 / ((ph.gama - 1.0) * ph.Minf * ph.Minf * ph.Pr * ph.Re));
+        // own-axis second derivatives of u_c and T
+        T d2u[3][3], lapT = T(0);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          const T id2 = idl[d] * idl[d];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            T acc = T(0);
+#pragma unroll
+            for (int t = 0; t < 5; ++t) acc += c2[t] * SA(F_U0 + c, d, t - 2);
+            d2u[c][d] = acc * id2;
+          }
+          T acc = T(0);
+#pragma unroll
+          for (int t = 0; t < 5; ++t) acc += c2[t] * SA(F_T, d, t - 2);
+          lapT += acc * id2;
+        }
+        // mixed derivative d_b(d_a u_c), a < b
+        auto mixed = [&](int c, int a, int b) -> T {
+          T outer = T(0);
+#pragma unroll
+          for (int tb = 0; tb < 5; ++tb) {
+            if (tb == 2) continue;
+            T inner = T(0);
+#pragma unroll
+            for (int ta = 0; ta < 5; ++ta) {
+              if (ta == 2) continue;
+              int o[3] = {0, 0, 0};
+              o[a] = ta - 2;
+              o[b] = tb - 2;
+              inner += c1[ta] * S(F_U0 + c, o[2], o[1], o[0]);
+            }
+            outer += c1[tb] * (inner * idl[a]);
+          }
+          return outer * idl[b];
+        };
+        // d_i(div u) = d_ii u_i + sum_{c != i} d_i d_c u_c
+        const T m01_1 = mixed(1, 0, 1), m02_2 = mixed(2, 0, 2);  // for i = 0
+        const T m01_0 = mixed(0, 0, 1), m12_2 = mixed(2, 1, 2);  // for i = 1
+        const T m02_0 = mixed(0, 0, 2), m12_1 = mixed(1, 1, 2);  // for i = 2
+        const T ddiv[3] = {d2u[0][0] + m01_1 + m02_2, d2u[1][1] + m01_0 + m12_2, d2u[2][2] + m02_0 + m12_1};
+        T mom[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          mom[c] = invRe * (d2u[c][0] + d2u[c][1] + d2u[c][2] + T(1.0 / 3.0) * ddiv[c]);
+          R[1 + c] += mom[c];
+        }
+        T e = kT * lapT;
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+          for (int b = 0; b < 3; ++b) {
+            T tau = du[a][b] + du[b][a];
+            if (a == b) tau -= T(2.0 / 3.0) * divu;
+            e += invRe * tau * du[a][b];
+          }
+        e += uu[0] * mom[0] + uu[1] * mom[1] + uu[2] * mom[2];
+        R[4] += e;
+      }
+
+      const int64_t n = gidx(g, i, j, k);
+      if (MODE & CRK_RIN) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) R[v] += rin.v[v][n];
+      }
+      if (MODE & CRK_UPDATE) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          const double o = qold.v[v][n];
+          const double r = (double)R[v];
+          qnew.v[v][n] = (T)(dt_new * r + o);
+          qold.v[v][n] = dt_old * r + o;
+        }
+      } else {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) rout.v[v][n] = R[v];
+      }
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T, int MODE>
+static void launch_mode(const Ctx &c, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold, Fields5<T> rin,
+                        Fields5<T> rout, double dt_new, double dt_old, cudaStream_t s) {
+  const size_t smem = sizeof(SmemC<T>);
+  const int bx = (c.g.n0 + TX - 1) / TX, by = (c.g.n1 + TY - 1) / TY;
+  // enough blocks to fill 152 SMs about twice, but at least 4 planes per z-chunk
+  int nzc = (2 * 152 + bx * by - 1) / (bx * by);
+  nzc = max(1, min(nzc, (c.g.n2 + 3) / 4));
+  const int zchunk = (c.g.n2 + nzc - 1) / nzc;
+  nzc = (c.g.n2 + zchunk - 1) / zchunk;
+  dim3 grid(bx, by, nzc), block(TX, TY);
+  k_central_rk<T, MODE><<<grid, block, smem, s>>>(c.g, q, qnew, qold, rin, rout, c.ph, dt_new, dt_old, zchunk);
+}
+
+template <typename T>
+void launch_central_rk(const Ctx &c, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold, Fields5<T> rin,
+                       Fields5<T> rout, double dt_new, double dt_old, int mode, cudaStream_t s, int64_t *launches) {
+  ++*launches;
+  switch (mode) {
+#define OSB_CASE(M) \
+  case M: launch_mode<T, M>(c, q, qnew, qold, rin, rout, dt_new, dt_old, s); break;
+    OSB_CASE(CRK_SKEW | CRK_VISC | CRK_UPDATE)
+    OSB_CASE(CRK_SKEW | CRK_VISC)
+    OSB_CASE(CRK_SKEW | CRK_UPDATE)
+    OSB_CASE(CRK_SKEW)
+    OSB_CASE(CRK_VISC | CRK_RIN | CRK_UPDATE)
+    OSB_CASE(CRK_VISC | CRK_RIN)
+    OSB_CASE(CRK_RIN | CRK_UPDATE)
+    OSB_CASE(CRK_RIN)
+#undef OSB_CASE
+    default:
+      --*launches;
+      break;
+  }
+}
+
+template <typename T> void setup_central() {
+  const int smem = (int)sizeof(SmemC<T>);
+#define OSB_ATTR(M) cudaFuncSetAttribute(k_central_rk<T, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  OSB_ATTR(CRK_SKEW | CRK_VISC | CRK_UPDATE)
+  OSB_ATTR(CRK_SKEW | CRK_VISC)
+  OSB_ATTR(CRK_SKEW | CRK_UPDATE)
+  OSB_ATTR(CRK_SKEW)
+  OSB_ATTR(CRK_VISC | CRK_RIN | CRK_UPDATE)
+  OSB_ATTR(CRK_VISC | CRK_RIN)
+  OSB_ATTR(CRK_RIN | CRK_UPDATE)
+  OSB_ATTR(CRK_RIN)
+#undef OSB_ATTR
+}
+template void setup_central<float>();
+template void setup_central<double>();
+
+template void launch_central_rk<float>(const Ctx &, Fields5<const float>, Fields5<float>, Fields5<double>,
+                                       Fields5<float>, Fields5<float>, double, double, int, cudaStream_t, int64_t *);
+template void launch_central_rk<double>(const Ctx &, Fields5<const double>, Fields5<double>, Fields5<double>,
+                                        Fields5<double>, Fields5<double>, double, double, int, cudaStream_t,
+                                        int64_t *);
+
+}  // namespace osb

@@ -1,0 +1,43 @@
+// osb_common.cuh -- shared device-side types for the GB300 kernels.
+//
+// Every per-variable array uses one padded layout: x fastest, interior point (i,j,k) at
+// off0 + i + j*sy + k*sz.  Halos: 4 in x (keeps interior rows 16-byte aligned for both element
+// sizes), 3 in y and z (the WENO5/TENO5 stencil reaches 3 points; central 4th order reaches 2).
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace osb {
+
+constexpr int HX = 4;
+constexpr int HY = 3;
+constexpr int HZ = 3;
+
+struct Grid {
+  int n0, n1, n2;
+  int64_t sy, sz, off0, numel;
+};
+
+__host__ __device__ inline int64_t gidx(const Grid &g, int i, int j, int k) {
+  return g.off0 + (int64_t)i + (int64_t)j * g.sy + (int64_t)k * g.sz;
+}
+
+template <typename T> struct Fields5 {
+  T *v[5];
+};
+
+// Physical and numerical constants of a plan, passed by value to every kernel.
+struct Phys {
+  double gama, Minf, Re, Pr;
+  double inv_delta[3];
+  double weno_eps;
+};
+
+template <typename T> __device__ __forceinline__ T sqrt_t(T x);
+template <> __device__ __forceinline__ float sqrt_t<float>(float x) { return sqrtf(x); }
+template <> __device__ __forceinline__ double sqrt_t<double>(double x) { return sqrt(x); }
+
+template <typename T> __device__ __forceinline__ T abs_t(T x) { return x < T(0) ? -x : x; }
+template <typename T> __device__ __forceinline__ T max_t(T a, T b) { return a > b ? a : b; }
+
+}  // namespace osb

@@ -1,0 +1,65 @@
+// osb_internal.h -- host-side context shared by the translation units of libosbli_gb300.
+#pragma once
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/osb_gb300.h"
+#include "osb_common.cuh"
+
+namespace osb {
+
+struct Ctx {
+  osb_plan_desc plan;
+  Grid g;
+  Phys ph;
+  int mixed;                 // 1: FP32 state, FP64 accumulator
+  int elem;                  // bytes per state element
+  void *qa[5] = {};          // bound state (caller-owned)
+  void *qb[5] = {};          // second state buffer (ping-pong partner), library-owned
+  double *qold[5] = {};      // FP64 RK register (master copy), library-owned
+  void *res[5] = {};         // residual, state precision, library-owned
+  double *red = nullptr;     // reduction scratch (partial sums), library-owned
+  int red_blocks = 0;
+  int cur = 0;               // 0: state in qa, 1: state in qb
+  cudaStream_t stream = nullptr;
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  double graph_dt[2] = {0, 0};
+  int64_t launches = 0;
+  int64_t graph_launches = 0;  // kernel launches recorded in one captured step
+  int qold_valid = 0;          // the FP64 register holds the current state
+  std::string err;
+  // per-kernel-family event timing (osb_profile); only used on the eager (non-graph) path
+  int prof_on = 0;
+  struct ProfRec {
+    int family;
+    cudaEvent_t a, b;
+  };
+  std::vector<ProfRec> prof_pending;
+  double prof_ms[8] = {};
+  int64_t prof_n[8] = {};
+};
+
+// kernel families reported by osb_profile_read
+enum { PF_HALO = 0, PF_WENO_X, PF_WENO_Y, PF_WENO_Z, PF_CENTRAL_RK, PF_OTHER, PF_COUNT };
+
+template <typename T> void setup_central();
+template <typename T> void setup_weno();
+template <typename T> void launch_halos(const Ctx &c, Fields5<T> q, cudaStream_t s, int64_t *launches);
+
+template <typename T>
+void launch_weno_dir(const Ctx &c, Fields5<const T> q, Fields5<T> r, int dir, cudaStream_t s, int64_t *launches);
+
+template <typename T>
+void launch_central_rk(const Ctx &c, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold, Fields5<T> rin,
+                       Fields5<T> rout, double dt_new, double dt_old, int mode, cudaStream_t s, int64_t *launches);
+
+// mode bits for launch_central_rk
+constexpr int CRK_SKEW = 1;      // add skew-symmetric central convective terms
+constexpr int CRK_VISC = 2;      // add viscous / heat-flux terms
+constexpr int CRK_RIN = 4;       // add the residual already in rin (WENO/TENO fluxes)
+constexpr int CRK_UPDATE = 8;    // apply the RK update into qnew/qold (else write R into rout)
+
+}  // namespace osb

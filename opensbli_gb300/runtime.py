@@ -1,0 +1,273 @@
+"""ctypes binding of libosbli_gb300 (include/osb_gb300.h) and a torch-owned solver state.
+
+`Solver(plan)` allocates the conserved-variable arrays as torch tensors on the current CUDA device
+in the layout the library reports, binds them, and exposes the time loop (`step`), reductions,
+residual evaluation and FP64 state access.  There is no CPU fallback: constructing a Solver
+without a CUDA device or without the built library raises.
+"""
+import ctypes
+import os
+
+import torch
+
+from . import build as _build
+
+OSB_ABI_VERSION = 1
+ERRORS = {
+    -1: "invalid plan or argument",
+    -2: "unsupported kernel pattern",
+    -3: "CUDA error",
+    -4: "field not bound",
+    -5: "device wait timed out",
+    -6: "non-finite value in the state",
+}
+
+CONV = {"central_skew": 0, "weno5js": 1, "teno5": 2}
+VISC = {"none": 0, "const": 1, "sutherland": 2}
+RK = {"rk3": 0, "ls_rk3": 1}
+BC = {"periodic": 0, "symmetry": 1}
+PREC = {"fp64": 0, "mixed": 1}
+RED = {"ke": 0, "enstrophy": 1, "nancheck": 2}
+
+
+class PlanDesc(ctypes.Structure):
+    _fields_ = [
+        ("abi_version", ctypes.c_int),
+        ("ndim", ctypes.c_int),
+        ("n", ctypes.c_int * 3),
+        ("delta", ctypes.c_double * 3),
+        ("conv", ctypes.c_int),
+        ("visc", ctypes.c_int),
+        ("rk", ctypes.c_int),
+        ("precision", ctypes.c_int),
+        ("bc", (ctypes.c_int * 2) * 3),
+        ("gama", ctypes.c_double),
+        ("Minf", ctypes.c_double),
+        ("Re", ctypes.c_double),
+        ("Pr", ctypes.c_double),
+        ("weno_eps", ctypes.c_double),
+        ("teno_ct", ctypes.c_double),
+        ("teno_eps", ctypes.c_double),
+        ("rk_a", ctypes.c_double * 3),
+        ("rk_b", ctypes.c_double * 3),
+        ("use_graphs", ctypes.c_int),
+    ]
+
+
+class Layout(ctypes.Structure):
+    _fields_ = [
+        ("numel", ctypes.c_int64),
+        ("offset", ctypes.c_int64),
+        ("stride_y", ctypes.c_int64),
+        ("stride_z", ctypes.c_int64),
+        ("halo", ctypes.c_int * 3),
+        ("nvar", ctypes.c_int),
+        ("state_bytes", ctypes.c_int),
+    ]
+
+
+EXPORTS = (
+    "osb_query_layout", "osb_create", "osb_bind_field", "osb_set_stream", "osb_init_tgv", "osb_set_state64",
+    "osb_get_state64", "osb_step", "osb_residual", "osb_reduce", "osb_launch_count", "osb_profile", "osb_profile_read",
+    "osb_get_error", "osb_destroy",
+)
+PROFILE_FAMILIES = ["halo", "weno_x", "weno_y", "weno_z", "central_rk", "other"]
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load the shared library (building it first if asked and needed)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = _build.LIB
+    if build_if_missing and not _build.up_to_date():
+        _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError("libosbli_gb300.so is not built (run __graft_entry__.build())")
+    lib = ctypes.CDLL(path)
+    vp, ip, dp = ctypes.c_void_p, ctypes.c_int, ctypes.c_double
+    lib.osb_query_layout.argtypes = [ctypes.POINTER(PlanDesc), ctypes.POINTER(Layout)]
+    lib.osb_create.argtypes = [ctypes.POINTER(PlanDesc), ctypes.POINTER(vp)]
+    lib.osb_bind_field.argtypes = [vp, ip, vp]
+    lib.osb_set_stream.argtypes = [vp, vp]
+    lib.osb_init_tgv.argtypes = [vp]
+    lib.osb_set_state64.argtypes = [vp, ip, vp]
+    lib.osb_get_state64.argtypes = [vp, ip, vp]
+    lib.osb_step.argtypes = [vp, ip, dp]
+    lib.osb_residual.argtypes = [vp, vp]
+    lib.osb_reduce.argtypes = [vp, ip, ctypes.POINTER(dp)]
+    lib.osb_launch_count.argtypes = [vp]
+    lib.osb_launch_count.restype = ctypes.c_int64
+    lib.osb_profile.argtypes = [vp, ip]
+    lib.osb_profile_read.argtypes = [vp, ctypes.POINTER(dp), ctypes.POINTER(ctypes.c_int64), ip]
+    lib.osb_get_error.argtypes = [vp, ctypes.c_char_p, ip]
+    lib.osb_destroy.argtypes = [vp]
+    lib.osb_destroy.restype = None
+    for name in EXPORTS:
+        if name not in ("osb_launch_count", "osb_destroy"):
+            getattr(lib, name).restype = ctypes.c_int
+    _lib = lib
+    return lib
+
+
+class OSBError(RuntimeError):
+    pass
+
+
+def make_plan_desc(plan):
+    """Fill the C plan struct from a Plan (opensbli_gb300.plan.Plan)."""
+    d = PlanDesc()
+    d.abi_version = OSB_ABI_VERSION
+    d.ndim = plan.ndim
+    for i in range(3):
+        d.n[i] = plan.n[i]
+        d.delta[i] = plan.delta[i]
+    d.conv = CONV[plan.conv]
+    d.visc = VISC[plan.visc]
+    d.rk = RK[plan.rk]
+    d.precision = PREC[plan.precision]
+    for a in range(3):
+        for s in range(2):
+            d.bc[a][s] = BC[plan.bc[a][s]]
+    d.gama, d.Minf, d.Re, d.Pr = plan.gama, plan.Minf, plan.Re, plan.Pr
+    d.weno_eps = plan.weno_eps
+    d.teno_ct, d.teno_eps = plan.teno_ct, plan.teno_eps
+    for s in range(3):
+        d.rk_a[s] = plan.rk_a[s]
+        d.rk_b[s] = plan.rk_b[s]
+    d.use_graphs = 1 if plan.use_graphs else 0
+    return d
+
+
+class Solver:
+    """One block's flow state on the current CUDA device, advanced by libosbli_gb300."""
+
+    def __init__(self, plan, device=None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("opensbli_gb300 needs a CUDA device; there is no CPU path")
+        self.lib = load()
+        self.plan = plan
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self.desc = make_plan_desc(plan)
+        lay = Layout()
+        self._check(self.lib.osb_query_layout(ctypes.byref(self.desc), ctypes.byref(lay)), ctx=None)
+        self.layout = lay
+        self.dtype = torch.float32 if lay.state_bytes == 4 else torch.float64
+        with torch.cuda.device(self.device):
+            h = ctypes.c_void_p()
+            self._check(self.lib.osb_create(ctypes.byref(self.desc), ctypes.byref(h)), ctx=None)
+            self.ctx = h
+            self.fields = [torch.zeros(lay.numel, dtype=self.dtype, device=self.device) for _ in range(lay.nvar)]
+            for v, t in enumerate(self.fields):
+                self._check(self.lib.osb_bind_field(self.ctx, v, ctypes.c_void_p(t.data_ptr())))
+            # a dedicated stream: CUDA graphs cannot be captured on the legacy default stream
+            self.stream = torch.cuda.Stream(self.device)
+            self._check(self.lib.osb_set_stream(self.ctx, ctypes.c_void_p(self.stream.cuda_stream)))
+            torch.cuda.synchronize(self.device)
+
+    # -- helpers
+    def _check(self, rc, ctx="self"):
+        if rc == 0:
+            return
+        msg = ERRORS.get(rc, "error %d" % rc)
+        c = self.ctx if ctx == "self" else None
+        if c is not None:
+            buf = ctypes.create_string_buffer(512)
+            self.lib.osb_get_error(c, buf, 512)
+            if buf.value:
+                msg += ": " + buf.value.decode()
+        if rc == -2:
+            raise NotImplementedError(msg)
+        raise OSBError(msg)
+
+    @property
+    def shape(self):
+        return (self.plan.n[2], self.plan.n[1], self.plan.n[0])
+
+    def interior(self, var):
+        """View of the interior of bound variable `var` as [z][y][x] (state precision)."""
+        lay = self.layout
+        n0, n1, n2 = self.plan.n
+        return torch.as_strided(self.fields[var], (n2, n1, n0), (lay.stride_z, lay.stride_y, 1), lay.offset)
+
+    # -- stream ordering: library work runs on self.stream; it waits for the caller's current stream
+    # before each call, and the caller's stream waits for it afterwards.
+    def _in(self):
+        self.stream.wait_stream(torch.cuda.current_stream(self.device))
+
+    def _out(self):
+        torch.cuda.current_stream(self.device).wait_stream(self.stream)
+
+    # -- API
+    def init_tgv(self):
+        self._in()
+        self._check(self.lib.osb_init_tgv(self.ctx))
+        self._out()
+
+    def set_state64(self, q):
+        """q: FP64 tensor/array [nvar][z][y][x] (interior)."""
+        q = torch.as_tensor(q, dtype=torch.float64).to(self.device).contiguous()
+        self._in()
+        for v in range(self.layout.nvar):
+            self._check(self.lib.osb_set_state64(self.ctx, v, ctypes.c_void_p(q[v].data_ptr())))
+        q.record_stream(self.stream)
+        self._out()
+
+    def state64(self):
+        self._in()
+        with torch.cuda.stream(self.stream):
+            out = torch.empty((self.layout.nvar,) + self.shape, dtype=torch.float64, device=self.device)
+        for v in range(self.layout.nvar):
+            self._check(self.lib.osb_get_state64(self.ctx, v, ctypes.c_void_p(out[v].data_ptr())))
+        self._out()
+        return out
+
+    def step(self, nsteps, dt):
+        self._in()
+        self._check(self.lib.osb_step(self.ctx, int(nsteps), float(dt)))
+        self._out()
+
+    def residual(self):
+        self._in()
+        with torch.cuda.stream(self.stream):
+            out = torch.empty((self.layout.nvar,) + self.shape, dtype=self.dtype, device=self.device)
+        self._check(self.lib.osb_residual(self.ctx, ctypes.c_void_p(out.data_ptr())))
+        self._out()
+        return out
+
+    def reduce(self, what):
+        v = ctypes.c_double()
+        self._in()
+        self._check(self.lib.osb_reduce(self.ctx, RED[what], ctypes.byref(v)))
+        return v.value
+
+    def profile(self, enable=True):
+        self._check(self.lib.osb_profile(self.ctx, 1 if enable else 0))
+
+    def profile_read(self):
+        """{family: (total_ms, launches)} accumulated since profile(True)."""
+        ms = (ctypes.c_double * 8)()
+        cnt = (ctypes.c_int64 * 8)()
+        n = self.lib.osb_profile_read(self.ctx, ms, cnt, 8)
+        return {PROFILE_FAMILIES[f]: (ms[f], int(cnt[f])) for f in range(min(n, len(PROFILE_FAMILIES))) if cnt[f]}
+
+    def launch_count(self):
+        return int(self.lib.osb_launch_count(self.ctx))
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            torch.cuda.synchronize(self.device)
+            self.lib.osb_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

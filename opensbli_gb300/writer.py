@@ -1,0 +1,238 @@
+"""GB300Writer: the backend seam beside OpenSBLI's OPSC writer.
+
+A problem script builds its algorithm exactly as for OPS:
+
+    alg = TraditionalAlgorithmRK(block)
+    SimulationDataType.set_datatype(Double)
+    OPSC(alg)                                   # reference backend: writes C for OPS
+    GB300Writer(alg, precision='fp64')          # this backend: lowers alg to a Plan
+
+The OPSC writer (code_generation/opsc.py:250-282) walks alg.prg and prints every Kernel as an
+ops_par_loop.  GB300Writer walks the same tree (opsc.py:595-609 traversal) and recognises the
+kernel families of the hot path -- constituent relations, Central skew-symmetric convective terms,
+LLFWeno reconstructions, viscous terms, the RK stage kernels and the boundary exchanges -- and
+lowers them to one Plan that selects the fused GB300 kernels.  Anything it does not recognise
+raises NotImplementedError: there is no generic fallback and no CPU path.
+
+Constants get their values the way the reference's scripts give them: through
+substitute_simulation_parameters(constants, values) (utilities/helperfunctions.py:130-149), here a
+method of the writer taking the same two lists.
+"""
+import math
+import re
+
+from .plan import Plan
+
+_C_NAMES = {"M_PI": math.pi, "pi": math.pi}
+
+
+def _eval_c_expr(expr, env):
+    """Evaluate the small C expressions problem scripts pass as values ('2*M_PI/block0np0')."""
+    if not re.fullmatch(r"[0-9A-Za-z_+\-*/(). eE]+", expr):
+        raise ValueError("unsupported value expression %r" % expr)
+    names = dict(_C_NAMES)
+    names.update(env)
+    return eval(expr, {"__builtins__": {}}, names)
+
+
+def _walk(component, out):
+    for c in getattr(component, "components", []) or []:
+        out.append(c)
+        _walk(c, out)
+    return out
+
+
+class GB300Writer:
+    """Lower an OpenSBLI TraditionalAlgorithmRK to a Plan for libosbli_gb300.
+
+    :arg algorithm: the TraditionalAlgorithmRK of the problem script (same positional argument as
+        OPSC).
+    :arg str precision: 'fp64' (the reference's Double) or 'mixed' (FP32 state and flux arithmetic,
+        FP64 RK accumulator).
+    """
+
+    def __init__(self, algorithm, precision="fp64", use_graphs=True):
+        self.algorithm = algorithm
+        if getattr(algorithm, "MultiBlock", False) or len(algorithm.block_descriptions) != 1:
+            raise NotImplementedError("GB300Writer lowers single-block algorithms")
+        self.block = algorithm.block_descriptions[0]
+        self.components = _walk(algorithm.prg, [])
+        self.kernel_names = [getattr(c, "computation_name", None) for c in self.components
+                             if type(c).__name__ == "Kernel"]
+        self.plan = self._lower(precision, use_graphs)
+        self.ic_kernel = self._find_kernel("Grid_based_initialisation")
+        self.values = {}
+
+    # ------------------------------------------------------------------ recognition
+    def _find_kernel(self, prefix):
+        for c in self.components:
+            if type(c).__name__ == "Kernel" and (c.computation_name or "").startswith(prefix):
+                return c
+        return None
+
+    def _kernels(self, prefix):
+        return [c for c in self.components
+                if type(c).__name__ == "Kernel" and (c.computation_name or "").startswith(prefix)]
+
+    @staticmethod
+    def _max_offset(kernels):
+        from sympy import preorder_traversal
+        m = 0
+        for k in kernels:
+            for e in k.equations:
+                for a in preorder_traversal(e.rhs):
+                    if type(a).__name__ == "DataSet":
+                        m = max([m] + [abs(int(i)) for i in a.indices])
+        return m
+
+    @staticmethod
+    def _lhs_names(kernel):
+        return {str(e.lhs) for e in kernel.equations}
+
+    def _lower(self, precision, use_graphs):
+        """Recognise the kernel families in alg.prg and build the Plan (all information comes from the
+        algorithm tree, as for the OPSC writer)."""
+        names = [n or "" for n in self.kernel_names]
+        ndim = self.block.ndim
+        if ndim != 3:
+            raise NotImplementedError("GB300Writer lowers 3D blocks (got ndim=%d)" % ndim)
+        skew = self._kernels("Convective terms group")
+        weno = self._kernels("LLFWeno_reconstruction_")
+        if self._kernels("LLFTeno_reconstruction_"):
+            raise NotImplementedError("TENO reconstruction on a 3D block is not lowered")
+        visc = self._kernels("Viscous")
+        if bool(skew) == bool(weno):
+            raise NotImplementedError("expected exactly one convective discretisation (Central skew or LLFWeno)")
+        if skew:
+            conv = "central_skew"
+            if len(skew) != 3 or self._max_offset(self._kernels("Convective CD")) != 2:
+                raise NotImplementedError("Central(4) skew-symmetric convective terms expected")
+        else:
+            conv = "weno5js"
+            if len(weno) != 3:
+                raise NotImplementedError("one LLFWeno reconstruction kernel per direction expected")
+            for k in weno:
+                lhs = self._lhs_names(k)
+                if not {"beta_0", "beta_1", "beta_2", "alpha_0", "omega_0", "inv_alpha_sum"} <= lhs:
+                    raise NotImplementedError("WENO5 reconstruction expected in %s" % k.computation_name)
+                if any(n.startswith("tau") for n in lhs):
+                    raise NotImplementedError("WENO-Z is not lowered; WENO-JS only")
+                if self._max_offset([k]) != 3:
+                    raise NotImplementedError("5th-order stencil expected in %s" % k.computation_name)
+                avg = [e for e in k.equations if str(e.lhs).endswith("_rho") and str(e.lhs).startswith("AVG_")]
+                if not avg or "sqrt" not in str(avg[0].rhs):
+                    raise NotImplementedError("Roe averaging expected in %s" % k.computation_name)
+            if not self._kernels("LLFWeno Residual"):
+                raise NotImplementedError("LLFWeno residual kernel missing")
+        if visc and self._max_offset(visc) != 2:
+            raise NotImplementedError("Central(4) viscous terms expected")
+        # constituent relations: u_i, p, T (and a for WENO), constant viscosity
+        base = {re.sub(r"_B0$", "", n) for n in names if n.startswith("CR")}
+        need = {"CRu0", "CRu1", "CRu2", "CRp"} | ({"CRT"} if visc else set()) | ({"CRa"} if weno else set())
+        if not need <= base or base - need - {"CRT", "CRa"}:
+            raise NotImplementedError("unsupported constituent relations: %s" % sorted(base))
+        # RK3 coefficients from the stage kernels (rk_sbli.py:102-124)
+        from sympy import preorder_traversal
+        coeff = {}
+        for kname in ("Sub stage advancement", "Temporal solution advancement"):
+            ks = self._kernels(kname)
+            if len(ks) != 1:
+                raise NotImplementedError("RungeKutta(3) stage kernels expected")
+            for e in ks[0].equations:
+                for a in preorder_traversal(e.rhs):
+                    if type(a).__name__ == "ConstantIndexed":
+                        coeff[str(a.base)] = tuple(float(v) for v in a.value)
+        if set(coeff) != {"rkold", "rknew"} or len(coeff["rkold"]) != 3:
+            raise NotImplementedError("2-register RK3 coefficients rkold/rknew expected")
+        # boundary conditions: periodic exchanges or symmetry boundary kernels, per axis and side
+        bcs = [[None, None] for _ in range(3)]
+        for c in self.components:
+            if type(c).__name__ == "ExchangeSelf":
+                bcs[c.direction][0 if c.side == "left" else 1] = "periodic"
+        for d in range(3):
+            for side in range(2):
+                if self._kernels("Symmetry boundary dir%d side%d" % (d, side)):
+                    bcs[d][side] = "symmetry"
+        other_bc = [n for n in names if "boundary dir" in n and not n.startswith("Symmetry")]
+        if other_bc or any(b is None for pair in bcs for b in pair):
+            raise NotImplementedError("unsupported boundary conditions: %s" % (other_bc or bcs))
+        return Plan(ndim=3, conv=conv, visc="const" if visc else "none", rk="rk3", precision=precision,
+                    bc=tuple(tuple(p) for p in bcs), rk_a=coeff["rkold"], rk_b=coeff["rknew"],
+                    use_graphs=use_graphs, ic="host", kernels=[n for n in names if n])
+
+    # ------------------------------------------------------------------ constants
+    def substitute_simulation_parameters(self, constants, values):
+        """Same arguments as opensbli.utilities.helperfunctions.substitute_simulation_parameters."""
+        env = {}
+        for c, v in zip(constants, values):
+            env[c] = _eval_c_expr(str(v), env) if isinstance(v, str) else v
+        self.values.update(env)
+        p = self.plan
+        n = tuple(int(env.get("block0np%d" % d, p.n[d])) for d in range(3))
+        delta = tuple(float(env.get("Delta%dblock0" % d, p.delta[d])) for d in range(3))
+        self.plan = p.replace(n=n, delta=delta, gama=float(env.get("gama", p.gama)), Minf=float(env.get("Minf", p.Minf)),
+                              Re=float(env.get("Re", p.Re)), Pr=float(env.get("Pr", p.Pr)),
+                              dt=float(env["dt"]) if "dt" in env else p.dt,
+                              niter=int(env["niter"]) if "niter" in env else p.niter)
+        return self.plan
+
+    # ------------------------------------------------------------------ initial condition
+    def initial_state(self):
+        """FP64 initial conserved state [5][z][y][x] from the script's GridBasedInitialisation kernel
+        (initialisation/gridbasedinit.py:15-57), evaluated with numpy in the kernel's equation order."""
+        import numpy as np
+        import sympy
+        k = self.ic_kernel
+        if k is None:
+            raise NotImplementedError("no Grid_based_initialisation kernel in the algorithm")
+        p = self.plan
+        n0, n1, n2 = p.n
+        ii, jj, kk = np.meshgrid(np.arange(n0, dtype=np.float64), np.arange(n1, dtype=np.float64),
+                                 np.arange(n2, dtype=np.float64), indexing="ij")
+        grid_idx = [ii.T, jj.T, kk.T]  # [z][y][x]
+        env = {}
+        consts = dict(self.values)
+        consts.update({"gama": p.gama, "Minf": p.Minf, "Re": p.Re, "Pr": p.Pr})
+        for d in range(3):
+            consts["Delta%dblock0" % d] = p.delta[d]
+        out = {}
+        for eq in k.equations:
+            rhs = eq.rhs
+            gi = {a for a in sympy.preorder_traversal(rhs) if type(a).__name__ == "Grididx"}
+            rhs = rhs.xreplace({a: sympy.Symbol("_osb_gi%d" % int(a.number)) for a in gi})
+            subs_syms, args = [], []
+            for s in rhs.free_symbols:
+                name = str(s)
+                if name.startswith("_osb_gi"):
+                    subs_syms.append(s); args.append(grid_idx[int(name[7:])])
+                elif name in env:
+                    subs_syms.append(s); args.append(env[name])
+                elif name in consts:
+                    subs_syms.append(s); args.append(consts[name])
+                else:
+                    raise NotImplementedError("initial condition symbol %s has no value" % name)
+            f = sympy.lambdify(subs_syms, rhs, "numpy")
+            val = np.broadcast_to(np.asarray(f(*args), dtype=np.float64), (n2, n1, n0)).copy()
+            lhs = eq.lhs
+            name = str(lhs.base) if hasattr(lhs, "base") else str(lhs)
+            name = re.sub(r"_B0$", "", name)
+            env[name] = val
+            out[name] = val
+        order = ["rho", "rhou0", "rhou1", "rhou2", "rhoE"]
+        missing = [v for v in order if v not in out]
+        if missing:
+            raise NotImplementedError("initialisation does not set %s" % missing)
+        return np.stack([out[v] for v in order])
+
+    # ------------------------------------------------------------------ execution
+    def solver(self, device=None):
+        from .runtime import Solver
+        return Solver(self.plan, device=device)
+
+    def run(self, niter=None, dt=None, device=None):
+        """Initialise from the script's initial condition and advance niter steps (defaults: the
+        script's niter and dt).  Returns the Solver, whose state64() gives the FP64 state."""
+        s = self.solver(device)
+        s.set_state64(self.initial_state())
+        s.step(int(niter if niter is not None else self.plan.niter), float(dt if dt is not None else self.plan.dt))
+        return s

@@ -1,0 +1,52 @@
+"""Shared helpers for the tests: golden fixtures and oracle configurations."""
+import json
+import math
+import os
+
+import numpy as np
+
+from oracle import oracle as O
+from opensbli_gb300.plan import Plan
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+VARS = ["rho", "rhou0", "rhou1", "rhou2", "rhoE"]
+
+
+def load_golden(case):
+    d = np.load(os.path.join(GOLDEN, "ref_%s.npz" % case))
+    return d["q"], int(d["n"]), int(d["steps"]), json.loads(str(d["params"]))
+
+
+def golden_plan(case, n=None, **kw):
+    with open(os.path.join(GOLDEN, "plan_%s.json" % case)) as f:
+        p = Plan.from_json(f.read())
+    if n is not None:
+        if p.bc[0][0] == "symmetry":
+            delta = (math.pi / (n - 1),) * 3
+        else:
+            delta = (2 * math.pi / n,) * 3
+        p = p.replace(n=(n, n, n), delta=delta)
+    return p.replace(**kw) if kw else p
+
+
+def oracle_cfg(plan, dt=None):
+    bc = [[plan.bc[d][s] for s in range(2)] for d in range(3)]
+    return O.make_cfg(plan.n, plan.delta, gama=plan.gama, Minf=plan.Minf, Re=plan.Re, Pr=plan.Pr, conv=plan.conv,
+                      visc=plan.visc, rk="rk3", bc=bc, dt=dt if dt is not None else (plan.dt or 1e-3))
+
+
+def rel_err(a, b):
+    """max |a-b| / max |b| per variable."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    out = []
+    for v in range(b.shape[0]):
+        s = np.abs(b[v]).max()
+        out.append(float(np.abs(a[v] - b[v]).max() / (s if s > 0 else 1.0)))
+    return out
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    return [float(np.linalg.norm(a[v] - b[v]) / max(np.linalg.norm(b[v]), 1e-300)) for v in range(b.shape[0])]

@@ -1,0 +1,61 @@
+"""The oracle (C restatement in oracle/src) against the reference's own generated code.
+
+Golden fixtures come from the reference generator's C output run here (tests/golden/make_golden.py);
+where the reference tree and its generated sources are present the oracle is also compared with a
+fresh run of that code at other sizes.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from oracle import refrun
+from helpers import load_golden, golden_plan, oracle_cfg, rel_err
+
+CASES = ["tgv_central", "tgv_weno", "tgsym_central"]
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_matches_reference_golden(case):
+    q_ref, n, steps, params = load_golden(case)
+    plan = golden_plan(case, n=n)
+    plan = plan.replace(Minf=params.get("Minf", plan.Minf))
+    cfg = oracle_cfg(plan, dt=params["dt"])
+    q0 = O.tgv_init(cfg)
+    q = O.run(cfg, q0, steps)
+    err = rel_err(q, q_ref)
+    # rhou2 starts at zero and stays small, so its max-normalised error is the loosest
+    assert max(err) < 1e-12, err
+
+
+def test_oracle_initial_condition_matches_script():
+    # TGV initial condition (taylor_green_vortex.py:87-101): mean density is 1 for rho = gama M^2 p
+    cfg = O.make_cfg((16, 16, 16), (2 * math.pi / 16,) * 3)
+    q = O.tgv_init(cfg)
+    assert abs(q[0].mean() - 1.0) < 1e-14
+    assert abs(q[3]).max() == 0.0
+
+
+def test_oracle_periodic_mass_conservation():
+    cfg = O.make_cfg((16, 16, 16), (2 * math.pi / 16,) * 3, conv="weno5js", Minf=1.25, dt=2e-3)
+    q0 = O.tgv_init(cfg)
+    q = O.run(cfg, q0, 3)
+    assert abs(q[0].sum() - q0[0].sum()) / q0[0].sum() < 1e-13
+
+
+@pytest.mark.parametrize("case,n,steps,extra", [
+    ("tgv_central", 12, 5, {"dt": 4e-3}),
+    ("tgv_weno", 12, 4, {"dt": 3e-3, "Minf": 1.25}),
+])
+def test_oracle_matches_reference_run(case, n, steps, extra):
+    if not refrun.available(case):
+        pytest.skip("generated reference sources for %s not present" % case)
+    params = dict(block0np0=n, block0np1=n, block0np2=n, niter=steps)
+    params.update(extra)
+    fields, _ = refrun.run(case, params, ["rho", "rhou0", "rhou1", "rhou2", "rhoE"], threads=2)
+    q_ref = np.stack([fields[v] for v in ["rho", "rhou0", "rhou1", "rhou2", "rhoE"]])
+    plan = golden_plan(case, n=n).replace(Minf=extra.get("Minf", 0.1))
+    cfg = oracle_cfg(plan, dt=extra["dt"])
+    q = O.run(cfg, O.tgv_init(cfg), steps)
+    assert max(rel_err(q, q_ref)) < 1e-12

@@ -1,0 +1,64 @@
+"""GB300Writer: lowering of the reference's own problem scripts, plan serialisation."""
+import math
+import os
+import subprocess
+import sys
+
+import numpy as np
+import pytest
+
+from opensbli_gb300.plan import Plan, tgv_plan, tgv_cfl_dt
+from opensbli_gb300.writer import _eval_c_expr
+from helpers import GOLDEN, golden_plan
+
+REF = "/root/reference"
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_plan_json_roundtrip():
+    p = tgv_plan(48, conv="weno5js", precision="mixed", Minf=1.25)
+    q = Plan.from_json(p.to_json())
+    assert q == p
+
+
+def test_golden_plans_are_what_the_kernels_implement():
+    c = golden_plan("tgv_central")
+    assert (c.conv, c.visc, c.rk) == ("central_skew", "const", "rk3")
+    assert c.bc == (("periodic", "periodic"),) * 3
+    assert c.rk_a == (0.25, 0.15, 0.6) and abs(c.rk_b[0] - 2 / 3) < 1e-16
+    assert c.n == (64, 64, 64) and abs(c.delta[0] - 2 * math.pi / 64) < 1e-15
+    assert (c.Re, c.Minf, c.Pr, c.gama) == (1600.0, 0.1, 0.71, 1.4)
+    assert c.dt == 0.003385 and c.niter == 5909
+    w = golden_plan("tgv_weno")
+    assert w.conv == "weno5js" and w.visc == "const"
+    s = golden_plan("tgsym_central")
+    assert s.bc == (("symmetry", "symmetry"),) * 3 and s.Re == 800.0
+    assert abs(s.delta[0] - math.pi / 32) < 1e-15
+
+
+def test_value_expressions():
+    env = {"block0np0": 64}
+    assert abs(_eval_c_expr("2*M_PI/block0np0", env) - 2 * math.pi / 64) < 1e-15
+    with pytest.raises(ValueError):
+        _eval_c_expr("__import__('os')", env)
+
+
+def test_cfl_dt_tgv_weno():
+    p = tgv_plan(256, conv="weno5js", Minf=1.25)
+    dt = tgv_cfl_dt(p)
+    assert 1e-3 < dt < 1e-2
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
+@pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgsym_central"])
+def test_writer_lowers_reference_script(case, tmp_path):
+    r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case, "--out",
+                        str(tmp_path), "--ref", REF], capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-3000:]
+    p = Plan.from_json(open(tmp_path / "plan.json").read())
+    g = golden_plan(case)
+    assert p.replace(kernels=[]) == g.replace(kernels=[])
+    assert sorted(p.kernels) == sorted(g.kernels)
+    ic = np.load(tmp_path / "ic.npy")
+    assert ic.shape == (5,) + tuple(reversed(p.n))
+    assert np.isfinite(ic).all()
