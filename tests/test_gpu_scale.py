@@ -26,12 +26,16 @@ def test_weno_256_conservation(precision):
     q = s.state64()
     tot = q.sum(dim=(1, 2, 3))
     assert torch.isfinite(q).all()
-    # periodic flux-difference form: discrete totals of rho, rhou_i, rhoE conserved up to roundoff
+    # periodic grid: the WENO flux difference and the linear central viscous terms telescope, so the
+    # totals of rho and rhou_i are conserved up to roundoff (FP64 register, FP32 or FP64 fluxes); the
+    # energy equation's viscous work is in expanded, non-telescoping form, so its total only
+    # changes by the truncation error
     N = q.shape[1] * q.shape[2] * q.shape[3]
-    assert abs(float(tot[0] - tot0[0])) / float(tot0[0]) < 1e-12
-    assert abs(float(tot[4] - tot0[4])) / float(tot0[4]) < 1e-12
+    tol = 1e-12 if precision == "fp64" else 1e-8
+    assert abs(float(tot[0] - tot0[0])) / float(tot0[0]) < tol
+    assert abs(float(tot[4] - tot0[4])) / float(tot0[4]) < 1e-6
     for v in (1, 2, 3):
-        assert abs(float(tot[v] - tot0[v])) / N < 1e-10
+        assert abs(float(tot[v] - tot0[v])) / N < (1e-12 if precision == "fp64" else 1e-7)
     assert s.reduce("ke") < ke0
     assert s.reduce("nancheck") == 0.0
     s.close()
