@@ -29,6 +29,7 @@ extern "C" {
 #define OSB_ENOTBOUND (-4)   /* a field is missing */
 #define OSB_ETIMEOUT (-5)    /* a bounded device wait gave up (device status word) */
 #define OSB_ENONFINITE (-6)  /* NaN/Inf found by osb_reduce(OSB_RED_NANCHECK) */
+#define OSB_ETOOLARGE (-7)   /* problem larger than a fixed-size scratch array (osb_reduce_noalloc) */
 
 /* convective schemes: Central(4) skew-symmetric (schemes/spatial/scheme.py:187-271, core/parsing.py:75-111),
  * LLFWeno(5,'JS') (schemes/spatial/weno.py:474-521), LLFTeno(5) (schemes/spatial/teno.py:489-530) */
@@ -139,6 +140,21 @@ int osb_profile_read(osb_ctx *ctx, double *total_ms, int64_t *counts, int n);
 
 int osb_get_error(osb_ctx *ctx, char *buf, int n);
 void osb_destroy(osb_ctx *ctx);
+
+/* Allocation-free variant of osb_reduce.  This entry point has no counterpart in the reference; it is
+ * for callers that cannot allocate device memory where they want a diagnostic (a host framework
+ * whose device memory belongs to a pool allocator, a monitoring hook between time steps).  It needs
+ * no context and calls no cudaMalloc/cudaFree: the caller passes the five state arrays (layout and
+ * element size of osb_query_layout for `plan`; for OSB_RED_ENSTROPHY the halos must be filled, as
+ * osb_step leaves them) and `dev_out`, a device pointer to one double that receives the result
+ * (stream-ordered on `stream`, no synchronisation; for OSB_RED_NANCHECK 1.0 means non-finite).
+ * Its only scratch is one FP64 partial sum per z-plane in a fixed device array of
+ * OSB_NOALLOC_MAX_PLANES entries, resident on every device that loads the library until exit;
+ * plans with more z-planes are rejected with OSB_ETOOLARGE.  The first call on a device, with that
+ * device current, looks up the array's device address; make it before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU race and must be serialised. */
+#define OSB_NOALLOC_MAX_PLANES 2048
+int osb_reduce_noalloc(const osb_plan_desc *plan, void *const fields[5], int what, double *dev_out, void *stream);
 
 #ifdef __cplusplus
 }
