@@ -60,7 +60,8 @@ __global__ void __launch_bounds__(256) k_central_rk(Grid g, Fields5<const T> q, 
       if (i >= g.n0 + 2 || j >= g.n1 + 2) continue;
       const int64_t n = gidx(g, i, j, k);
       const T rho = q.v[0][n];
-      const T u0 = q.v[1][n] / rho, u1 = q.v[2][n] / rho, u2 = q.v[3][n] / rho;
+      const T irho = T(1) / rho;
+      const T u0 = q.v[1][n] * irho, u1 = q.v[2][n] * irho, u2 = q.v[3][n] * irho;
       const T E = q.v[4][n];
       const T half = T(0.5);
       const T p = gm1 * (E - half * rho * u0 * u0 - half * rho * u1 * u1 - half * rho * u2 * u2);
@@ -69,7 +70,7 @@ __global__ void __launch_bounds__(256) k_central_rk(Grid g, Fields5<const T> q, 
       sm.s[sl][F_U1][py][px] = u1;
       sm.s[sl][F_U2][py][px] = u2;
       sm.s[sl][F_P][py][px] = p;
-      sm.s[sl][F_T][py][px] = gM2 * p / rho;
+      sm.s[sl][F_T][py][px] = gM2 * p * irho;
       sm.s[sl][F_E][py][px] = E;
     }
   };
@@ -227,9 +228,12 @@ static void launch_mode(const Ctx &c, Fields5<const T> q, Fields5<T> qnew, Field
                         Fields5<T> rout, double dt_new, double dt_old, cudaStream_t s) {
   const size_t smem = sizeof(SmemC<T>);
   const int bx = (c.g.n0 + TX - 1) / TX, by = (c.g.n1 + TY - 1) / TY;
-  // enough blocks to fill 152 SMs about twice, but at least 4 planes per z-chunk
-  int nzc = (2 * 152 + bx * by - 1) / (bx * by);
-  nzc = max(1, min(nzc, (c.g.n2 + 3) / 4));
+  // z-chunks: about four waves of resident blocks (each SM holds 3 FP32 / 1 FP64 block of this
+  // shared-memory footprint) so the last wave's tail is short; at least 8 planes per chunk so the
+  // 4 halo planes of each chunk cost at most half a chunk's loads
+  const int resident = 152 * (sizeof(T) == 4 ? 3 : 1);
+  int nzc = (4 * resident + bx * by - 1) / (bx * by);
+  nzc = max(1, min(nzc, (c.g.n2 + 7) / 8));
   const int zchunk = (c.g.n2 + nzc - 1) / nzc;
   nzc = (c.g.n2 + zchunk - 1) / zchunk;
   dim3 grid(bx, by, nzc), block(TX, TY);

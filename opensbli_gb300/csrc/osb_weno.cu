@@ -11,16 +11,26 @@
 //     (physical_models/euler_eigensystem.py:107-135): eigenvalues (u_d,u_d,u_d,u_d+a,u_d-a);
 //   * LLF splitting (shock_capturing.py:357-398, 464-536): CF = LEV.F, CS = LEV.Q at i-2..i+3,
 //     lambda_r = max over those six points of |ev_r| from the point values, f+- = CF +- lambda CS;
-//   * WENO5-JS (weno.py:70-205, 341-369) in the reference's own form: smoothness indicators and
-//     candidate stencils carry the splitting's factor 1/2, alpha_r = d_r/(eps + beta_r)^2;
+//   * WENO5-JS (weno.py:70-205, 341-369): the reference keeps the splitting's factor 1/2 out of f
+//     and puts it into the smoothness indicators (1/4 of Jiang-Shu's) and the candidate stencils
+//     (1/2 of the usual ones); alpha_r = d_r/(eps + beta_r)^2, omega_r = alpha_r / sum alpha;
 //   * flux = REV.(fhat+ + fhat-) (shock_capturing.py:418-448);
 //   * residual R -= (flux_{i+1/2} - flux_{i-1/2}) / delta_d.
 //
+// Arithmetic is rearranged for fewer instructions, not changed in meaning: sqrt(rho_L) u_L is formed
+// as rhou_L / sqrt(rho_L); the three dense LEV rows (entropy and both acoustic waves) share one
+// dot product g = (phi, -(g-1)u, g-1).X and h = X_{1+d} - u_d X_0 (the flux vector F is never
+// stored: its projections are formed from Q, u_d and p):
+//     acoustic+- . X = bt (g +- a h),   entropy . X = X_0 - g / a^2;
+// the smoothness indicators use Jiang and Shu's sum-of-squares form; the weights take reciprocals
+// of (eps+beta)^2 instead of divisions.  In FP32 the reciprocals are the fast hardware ones
+// (2 ulp); in FP64 every division is exact.
+//
 // Tiling: a block covers TA lines along d and computes TI consecutive interfaces per line, giving
 // the flux difference of TI-1 cells.  The primitive fields of the TI+5 points of every line sit in
-// shared memory (loaded once, coalesced along x); each thread owns whole interfaces, keeps the six
-// stencil points' conserved and flux vectors in registers and projects them one characteristic
-// field at a time.
+// shared memory (loaded once, coalesced along x).  For y and z each thread owns four consecutive
+// interfaces of one line and slides a six-point register window along it, so a point's conserved
+// and flux vectors are loaded and formed once per thread instead of six times.
 #include "osb_common.cuh"
 #include "osb_internal.h"
 
@@ -33,165 +43,172 @@ template <int DIR> struct WTile;
 template <> struct WTile<0> {  // x: 64 interfaces x 4 rows, one interface per thread
   static constexpr int TI = 64, TA = 4, IPT = 1;
 };
-template <> struct WTile<1> {  // y: 32 x-lanes x 32 interfaces, four interfaces per thread
+template <> struct WTile<1> {  // y: 32 x-lanes x 32 interfaces, four consecutive interfaces per thread
   static constexpr int TI = 32, TA = 32, IPT = 4;
 };
 template <> struct WTile<2> {
   static constexpr int TI = 32, TA = 32, IPT = 4;
 };
+
+template <typename T> __device__ __forceinline__ T rcp_t(T x);
+template <> __device__ __forceinline__ float rcp_t<float>(float x) { return __fdividef(1.0f, x); }
+template <> __device__ __forceinline__ double rcp_t<double>(double x) { return 1.0 / x; }
+template <typename T> __device__ __forceinline__ T rsqrt_t(T x);
+template <> __device__ __forceinline__ float rsqrt_t<float>(float x) { return rsqrtf(x); }
+template <> __device__ __forceinline__ double rsqrt_t<double>(double x) { return 1.0 / sqrt(x); }
 }  // namespace
 
-// WENO5-JS on f = CF + lambda CS at points i-2..i+2 (upwind side of i+1/2), reference form.
-template <typename T> __device__ __forceinline__ T weno_plus(T f0, T f1, T f2, T f3, T f4, T eps) {
-  const T h = T(0.5);
-  const T b0 = h * f2 * (T(5.0 / 3.0) * f2 - T(31.0 / 6.0) * f3 + T(11.0 / 6.0) * f4) +
-               h * f3 * (T(25.0 / 6.0) * f3 - T(19.0 / 6.0) * f4) + T(1.0 / 3.0) * f4 * f4;
-  const T b1 = h * f1 * (T(2.0 / 3.0) * f1 - T(13.0 / 6.0) * f2 + T(5.0 / 6.0) * f3) +
-               h * f2 * (T(13.0 / 6.0) * f2 - T(13.0 / 6.0) * f3) + T(1.0 / 3.0) * f3 * f3;
-  const T b2 = h * f0 * (T(2.0 / 3.0) * f0 + T(11.0 / 6.0) * f2) +
-               h * f1 * (T(-19.0 / 6.0) * f0 + T(25.0 / 6.0) * f1 - T(31.0 / 6.0) * f2) + T(5.0 / 6.0) * f2 * f2;
-  const T a0 = T(3.0 / 10.0) / ((b0 + eps) * (b0 + eps));
-  const T a1 = T(3.0 / 5.0) / ((b1 + eps) * (b1 + eps));
-  const T a2 = T(1.0 / 10.0) / ((b2 + eps) * (b2 + eps));
-  const T inv = T(1) / (a0 + a1 + a2);
-  return a0 * inv * (T(1.0 / 6.0) * f2 + T(5.0 / 12.0) * f3 - T(1.0 / 12.0) * f4) +
-         a1 * inv * (T(-1.0 / 12.0) * f1 + T(5.0 / 12.0) * f2 + T(1.0 / 6.0) * f3) +
-         a2 * inv * (T(1.0 / 6.0) * f0 - T(7.0 / 12.0) * f1 + T(11.0 / 12.0) * f2);
-}
-// f = CF - lambda CS at points i-1..i+3 (f1..f5), reconstruct at i+1/2 from the right.
-template <typename T> __device__ __forceinline__ T weno_minus(T f1, T f2, T f3, T f4, T f5, T eps) {
-  const T h = T(0.5);
-  const T b0 = h * f3 * (T(5.0 / 3.0) * f3 - T(31.0 / 6.0) * f4 + T(11.0 / 6.0) * f5) +
-               h * f4 * (T(25.0 / 6.0) * f4 - T(19.0 / 6.0) * f5) + T(1.0 / 3.0) * f5 * f5;
-  const T b1 = h * f2 * (T(2.0 / 3.0) * f2 - T(13.0 / 6.0) * f3 + T(5.0 / 6.0) * f4) +
-               h * f3 * (T(13.0 / 6.0) * f3 - T(13.0 / 6.0) * f4) + T(1.0 / 3.0) * f4 * f4;
-  const T b2 = h * f1 * (T(2.0 / 3.0) * f1 - T(19.0 / 6.0) * f2 + T(11.0 / 6.0) * f3) +
-               h * f2 * (T(25.0 / 6.0) * f2 - T(31.0 / 6.0) * f3) + T(5.0 / 6.0) * f3 * f3;
-  const T a0 = T(1.0 / 10.0) / ((b0 + eps) * (b0 + eps));
-  const T a1 = T(3.0 / 5.0) / ((b1 + eps) * (b1 + eps));
-  const T a2 = T(3.0 / 10.0) / ((b2 + eps) * (b2 + eps));
-  const T inv = T(1) / (a0 + a1 + a2);
-  return a0 * inv * (T(11.0 / 12.0) * f3 - T(7.0 / 12.0) * f4 + T(1.0 / 6.0) * f5) +
-         a1 * inv * (T(1.0 / 6.0) * f2 + T(5.0 / 12.0) * f3 - T(1.0 / 12.0) * f4) +
-         a2 * inv * (T(-1.0 / 12.0) * f1 + T(5.0 / 12.0) * f2 + T(1.0 / 6.0) * f3);
+// One WENO5-JS side.  f0..f4 are the five stencil values ordered from the far upwind point to the
+// far downwind one (for the right-going side: points i-2..i+2; for the left-going side the caller
+// passes points i+3..i-1).  d0 weights the most downwind candidate (3/10), d2 the most upwind (1/10).
+template <typename T> __device__ __forceinline__ T weno5_side(T f0, T f1, T f2, T f3, T f4, T eps) {
+  const T c13 = T(13.0 / 48.0), c14 = T(1.0 / 16.0);
+  const T t0 = f2 - T(2) * f3 + f4, s0 = T(3) * f2 - T(4) * f3 + f4;
+  const T t1 = f1 - T(2) * f2 + f3, s1 = f1 - f3;
+  const T t2 = f0 - T(2) * f1 + f2, s2 = f0 - T(4) * f1 + T(3) * f2;
+  const T b0 = c13 * t0 * t0 + c14 * s0 * s0;
+  const T b1 = c13 * t1 * t1 + c14 * s1 * s1;
+  const T b2 = c13 * t2 * t2 + c14 * s2 * s2;
+  const T e0 = b0 + eps, e1 = b1 + eps, e2 = b2 + eps;
+  const T a0 = T(3.0 / 10.0) * rcp_t(e0 * e0);
+  const T a1 = T(3.0 / 5.0) * rcp_t(e1 * e1);
+  const T a2 = T(1.0 / 10.0) * rcp_t(e2 * e2);
+  const T p0 = T(1.0 / 6.0) * f2 + T(5.0 / 12.0) * f3 - T(1.0 / 12.0) * f4;
+  const T p1 = T(-1.0 / 12.0) * f1 + T(5.0 / 12.0) * f2 + T(1.0 / 6.0) * f3;
+  const T p2 = T(1.0 / 6.0) * f0 - T(7.0 / 12.0) * f1 + T(11.0 / 12.0) * f2;
+  return (a0 * p0 + a1 * p1 + a2 * p2) * rcp_t(a0 + a1 + a2);
 }
 
-// Characteristic flux at one interface.  P(f, t) reads field f of stencil point t = 0..5 (points
-// i-2..i+3); returns the five components of the interface flux.
-template <typename T, int D, typename Pt>
-__device__ __forceinline__ void interface_flux(const Pt &P, const T gama, const T eps, T out[5]) {
-  constexpr int E1 = (D + 1) % 3, E2 = (D + 2) % 3;  // the two tangential axes
+// Per-point window entry: conserved vector Q, u_D, a, p.  The physical flux along D,
+// F = (Q_{1+D}, Q_{1+c} u_D + delta_cD p, (p + Q_4) u_D), is folded into the projections below.
+template <typename T> struct WPt {
+  T Q[5], ud, a, p;
+};
+
+template <typename T, int D, typename Pt> __device__ __forceinline__ void load_point(const Pt &P, int t, WPt<T> &w) {
+  w.Q[0] = P(W_RHO, t);
+  w.Q[1] = P(W_RU0, t);
+  w.Q[2] = P(W_RU1, t);
+  w.Q[3] = P(W_RU2, t);
+  w.Q[4] = P(W_E, t);
+  w.ud = P(W_UD, t);
+  w.p = P(W_P, t);
+  w.a = P(W_A, t);
+}
+
+// Characteristic flux at the interface between window points 2 and 3 (points i and i+1).
+template <typename T, int D>
+__device__ __forceinline__ void interface_flux(const WPt<T> (&W)[6], const T gama, const T eps, T out[5]) {
+  constexpr int E1 = (D + 1) % 3, E2 = (D + 2) % 3;  // the two tangential axes (shear rows)
+  constexpr int e1 = 3 - E1 - D, e2 = 3 - E2 - D;    // third axis of each shear row
   const T gm1 = gama - T(1);
-  // ---- Roe average of points 2 (i) and 3 (i+1)
-  const T rl = P(W_RHO, 2), rr = P(W_RHO, 3);
-  const T sl = sqrt_t(rl), sr = sqrt_t(rr);
-  const T rho = sqrt_t(rl * rr);
-  const T inv_s = T(1) / (sl + sr);
+  // ---- Roe average of points 2 and 3
+  const T rl = W[2].Q[0], rr = W[3].Q[0];
+  const T isl = rsqrt_t(rl), isr = rsqrt_t(rr);  // 1/sqrt(rho)
+  const T sl = rl * isl, sr = rr * isr;          // sqrt(rho)
+  const T rho = sl * sr;
+  const T inv_s = rcp_t(sl + sr);
   T u[3];
 #pragma unroll
-  for (int c = 0; c < 3; ++c) u[c] = inv_s * (sl * (P(W_RU0 + c, 2) / rl) + sr * (P(W_RU0 + c, 3) / rr));
-  const T Hh = inv_s * ((P(W_P, 2) + P(W_E, 2)) / sl + (P(W_P, 3) + P(W_E, 3)) / sr);
+  for (int c = 0; c < 3; ++c) u[c] = inv_s * (W[2].Q[1 + c] * isl + W[3].Q[1 + c] * isr);
+  const T Hh = inv_s * ((W[2].p + W[2].Q[4]) * isl + (W[3].p + W[3].Q[4]) * isr);
   const T usq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
   const T a = sqrt_t(gm1 * (Hh - T(0.5) * usq));
-  const T ia = T(1) / a, irho = T(1) / rho;
-  const T ia2 = ia * ia;
+  const T ia = rcp_t(a), irho = rcp_t(rho);
   const T phi = gm1 * T(0.5) * usq;
   const T bt = T(0.70710678118654752440) * irho * ia;  // 1/(sqrt(2) rho a)
   const T al = T(0.70710678118654752440) * rho * ia;   // rho/(sqrt(2) a)
+  const T ia2 = ia * ia;
+  const T btA = bt * a;
 
-  // ---- stencil vectors in registers
-  T Q[6][5], F[6][5];
   T lam_u = T(0), lam_p = T(0), lam_m = T(0);
 #pragma unroll
   for (int t = 0; t < 6; ++t) {
-    const T ud = P(W_UD, t), p = P(W_P, t), at = P(W_A, t);
-    Q[t][0] = P(W_RHO, t);
-    Q[t][1] = P(W_RU0, t);
-    Q[t][2] = P(W_RU1, t);
-    Q[t][3] = P(W_RU2, t);
-    Q[t][4] = P(W_E, t);
-    F[t][0] = Q[t][1 + D];
+    lam_u = max_t(lam_u, abs_t(W[t].ud));
+    lam_p = max_t(lam_p, abs_t(W[t].ud + W[t].a));
+    lam_m = max_t(lam_m, abs_t(W[t].a - W[t].ud));
+  }
+  auto recon = [&](const T (&cf)[6], const T (&cs)[6], T lam) -> T {
+    T fp[6], fm[6];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) F[t][1 + c] = Q[t][1 + c] * ud + (c == D ? p : T(0));
-    F[t][4] = (p + Q[t][4]) * ud;
-    lam_u = max_t(lam_u, abs_t(ud));
-    lam_p = max_t(lam_p, abs_t(ud + at));
-    lam_m = max_t(lam_m, abs_t(at - ud));
+    for (int t = 0; t < 6; ++t) {
+      fp[t] = cf[t] + lam * cs[t];
+      fm[t] = cf[t] - lam * cs[t];
+    }
+    return weno5_side(fp[0], fp[1], fp[2], fp[3], fp[4], eps) + weno5_side(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
+  };
+
+  // ---- shear rows: LEV_r . X = (s/rho)(u_e X_0 - X_{1+e}); for X = F: X_0 = Q_{1+D}, X_{1+e} = Q_{1+e} u_D
+  const T se1 = (D == (E1 + 1) % 3) ? T(1) : T(-1), se2 = (D == (E2 + 1) % 3) ? T(1) : T(-1);
+  T rE1, rE2;
+  {
+    T cf[6], cs[6];
+    const T sr1 = se1 * irho;
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = sr1 * (u[e1] * W[t].Q[1 + D] - W[t].Q[1 + e1] * W[t].ud);
+      cs[t] = sr1 * (u[e1] * W[t].Q[0] - W[t].Q[1 + e1]);
+    }
+    rE1 = recon(cf, cs, lam_u);
+    const T sr2 = se2 * irho;
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = sr2 * (u[e2] * W[t].Q[1 + D] - W[t].Q[1 + e2] * W[t].ud);
+      cs[t] = sr2 * (u[e2] * W[t].Q[0] - W[t].Q[1 + e2]);
+    }
+    rE2 = recon(cf, cs, lam_u);
+  }
+  // ---- dense rows share g = phi X_0 - (g-1) u.X_{1..3} + (g-1) X_4 and h = X_{1+D} - u_D X_0
+  T gQ[6], gF[6], hQ[6], hF[6];
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    const WPt<T> &w = W[t];
+    const T dq = u[0] * w.Q[1] + u[1] * w.Q[2] + u[2] * w.Q[3];
+    gQ[t] = phi * w.Q[0] - gm1 * dq + gm1 * w.Q[4];
+    hQ[t] = w.Q[1 + D] - u[D] * w.Q[0];
+    gF[t] = phi * w.Q[1 + D] - gm1 * (w.ud * dq + u[D] * w.p) + gm1 * (w.p + w.Q[4]) * w.ud;
+    hF[t] = w.Q[1 + D] * w.ud + w.p - u[D] * w.Q[1 + D];
+  }
+  T rD, r3, r4;
+  {
+    T cf[6], cs[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = W[t].Q[1 + D] - gF[t] * ia2;
+      cs[t] = W[t].Q[0] - gQ[t] * ia2;
+    }
+    rD = recon(cf, cs, lam_u);
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = bt * gF[t] + btA * hF[t];
+      cs[t] = bt * gQ[t] + btA * hQ[t];
+    }
+    r3 = recon(cf, cs, lam_p);
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = bt * gF[t] - btA * hF[t];
+      cs[t] = bt * gQ[t] - btA * hQ[t];
+    }
+    r4 = recon(cf, cs, lam_m);
   }
 
-  T rec[5];
-  // ---- row D: entropy wave, LEV_D = (1 - phi/a^2, (g-1)u_c/a^2, -(g-1)/a^2)
-  {
-    const T l0 = T(1) - phi * ia2, l1 = gm1 * u[0] * ia2, l2 = gm1 * u[1] * ia2, l3 = gm1 * u[2] * ia2,
-            l4 = -gm1 * ia2;
-    T fp[6], fm[6];
-#pragma unroll
-    for (int t = 0; t < 6; ++t) {
-      const T cf = l0 * F[t][0] + l1 * F[t][1] + l2 * F[t][2] + l3 * F[t][3] + l4 * F[t][4];
-      const T cs = l0 * Q[t][0] + l1 * Q[t][1] + l2 * Q[t][2] + l3 * Q[t][3] + l4 * Q[t][4];
-      fp[t] = cf + lam_u * cs;
-      fm[t] = cf - lam_u * cs;
-    }
-    rec[D] = weno_plus(fp[0], fp[1], fp[2], fp[3], fp[4], eps) + weno_minus(fm[1], fm[2], fm[3], fm[4], fm[5], eps);
-  }
-  // ---- rows E1, E2: shear waves.  Row r (r != D), third axis e = 3 - r - D:
-  //      LEV_r = (s u_e/rho) e_0 - (s/rho) e_{1+e}, s = +1 if D == (r+1)%3 else -1
-#pragma unroll
-  for (int w = 0; w < 2; ++w) {
-    const int r = w == 0 ? E1 : E2;
-    const int e = 3 - r - D;
-    const T s = (D == (r + 1) % 3) ? T(1) : T(-1);
-    const T l0 = s * u[e] * irho, le = -s * irho;
-    T fp[6], fm[6];
-#pragma unroll
-    for (int t = 0; t < 6; ++t) {
-      const T cf = l0 * F[t][0] + le * F[t][1 + e];
-      const T cs = l0 * Q[t][0] + le * Q[t][1 + e];
-      fp[t] = cf + lam_u * cs;
-      fm[t] = cf - lam_u * cs;
-    }
-    rec[r] = weno_plus(fp[0], fp[1], fp[2], fp[3], fp[4], eps) + weno_minus(fm[1], fm[2], fm[3], fm[4], fm[5], eps);
-  }
-  // ---- rows 3, 4: acoustic waves u_d + a, u_d - a
-#pragma unroll
-  for (int w = 0; w < 2; ++w) {
-    const T sg = w == 0 ? T(-1) : T(1);  // row 3: phi - u_d a ; row 4: phi + u_d a
-    const T lam = w == 0 ? lam_p : lam_m;
-    T l[5];
-    l[0] = bt * (phi + sg * u[D] * a);
-#pragma unroll
-    for (int c = 0; c < 3; ++c) l[1 + c] = -bt * (gm1 * u[c] + (c == D ? sg * a : T(0)));
-    l[4] = bt * gm1;
-    T fp[6], fm[6];
-#pragma unroll
-    for (int t = 0; t < 6; ++t) {
-      const T cf = l[0] * F[t][0] + l[1] * F[t][1] + l[2] * F[t][2] + l[3] * F[t][3] + l[4] * F[t][4];
-      const T cs = l[0] * Q[t][0] + l[1] * Q[t][1] + l[2] * Q[t][2] + l[3] * Q[t][3] + l[4] * Q[t][4];
-      fp[t] = cf + lam * cs;
-      fm[t] = cf - lam * cs;
-    }
-    rec[3 + w] = weno_plus(fp[0], fp[1], fp[2], fp[3], fp[4], eps) + weno_minus(fm[1], fm[2], fm[3], fm[4], fm[5], eps);
-  }
   // ---- back to conserved space: flux = REV . rec
-  const T sac = rec[3] + rec[4], dac = rec[3] - rec[4];
-  const T hh = (phi + a * a) / gm1;
-  out[0] = rec[D] + al * sac;
+  const T sac = r3 + r4, dac = r3 - r4;
+  const T igm1 = rcp_t(gm1);
+  const T hh = (phi + a * a) * igm1;
+  out[0] = rD + al * sac;
 #pragma unroll
-  for (int c = 0; c < 3; ++c) out[1 + c] = u[c] * rec[D] + al * (u[c] * sac + (c == D ? a * dac : T(0)));
-  out[4] = (phi / gm1) * rec[D] + al * (hh * sac + u[D] * a * dac);
+  for (int c = 0; c < 3; ++c) out[1 + c] = u[c] * rD + al * (u[c] * sac + (c == D ? a * dac : T(0)));
+  out[4] = (phi * igm1) * rD + al * (hh * sac + u[D] * a * dac);
   // shear columns: REV[1+e][r] = -s rho, REV[4][r] = -s rho u_e
-#pragma unroll
-  for (int w = 0; w < 2; ++w) {
-    const int r = w == 0 ? E1 : E2;
-    const int e = 3 - r - D;
-    const T s = (D == (r + 1) % 3) ? T(1) : T(-1);
-    out[1 + e] += -s * rho * rec[r];
-    out[4] += -s * rho * u[e] * rec[r];
-  }
+  out[1 + e1] -= se1 * rho * rE1;
+  out[4] -= se1 * rho * u[e1] * rE1;
+  out[1 + e2] -= se2 * rho * rE2;
+  out[4] -= se2 * rho * u[e2] * rE2;
 }
 
 template <typename T, int DIR, bool ACCUM>
-__global__ void __launch_bounds__(256) k_weno(Grid g, Fields5<const T> q, Fields5<T> res, Phys ph) {
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fields5<const T> q, Fields5<T> res, Phys ph) {
   using Tl = WTile<DIR>;
   constexpr int TI = Tl::TI, TA = Tl::TA, NPT = TI + 5;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -203,7 +220,7 @@ __global__ void __launch_bounds__(256) k_weno(Grid g, Fields5<const T> q, Fields
   const T eps = T(ph.weno_eps);
 
   // tile origin: first cell whose flux difference this block writes (d0), across-line origin
-  int d0, a0, o1, o2;  // o1/o2: the remaining coordinates
+  int d0, a0, o1, o2;
   if (DIR == 0) { d0 = blockIdx.x * (TI - 1); a0 = blockIdx.y * TA; o2 = blockIdx.z; o1 = 0; }
   else if (DIR == 1) { a0 = blockIdx.x * TA; d0 = blockIdx.y * (TI - 1); o2 = blockIdx.z; o1 = 0; }
   else { a0 = blockIdx.x * TA; o1 = blockIdx.y; d0 = blockIdx.z * (TI - 1); o2 = 0; }
@@ -245,19 +262,41 @@ __global__ void __launch_bounds__(256) k_weno(Grid g, Fields5<const T> q, Fields
   }
   __syncthreads();
 
-  // ---- interface fluxes: interface m of a line sits between cells d0-1+m and d0+m
-#pragma unroll 1
-  for (int w = 0; w < Tl::IPT; ++w) {
-    int m, a;
-    if (DIR == 0) { m = tid % TI; a = tid / TI; }
-    else { a = tid % TA; m = tid / TA + w * (256 / TA); }
-    const int left = d0 - 1 + m;
-    if (left <= nd - 1 && a0 + a < na) {
-      auto P = [&](int f, int t) -> T { return sf[sidx(f, m + t, a)]; };
-      T fl[5];
-      interface_flux<T, DIR>(P, gama, eps, fl);
+  // ---- interface fluxes: interface m of a line sits between cells d0-1+m and d0+m and uses the
+  //      points at positions m..m+5
+  auto flux_store = [&](int m, int a, const T (&fl)[5]) {
 #pragma unroll
-      for (int v = 0; v < 5; ++v) sflux[DIR == 0 ? (v * TA + a) * TI + m : (v * TI + m) * TA + a] = fl[v];
+    for (int v = 0; v < 5; ++v) sflux[DIR == 0 ? (v * TA + a) * TI + m : (v * TI + m) * TA + a] = fl[v];
+  };
+  if (DIR == 0) {
+    const int m = tid % TI, a = tid / TI;
+    if (d0 - 1 + m <= nd - 1 && a0 + a < na) {
+      auto P = [&](int f, int t) -> T { return sf[sidx(f, m + t, a)]; };
+      WPt<T> W[6];
+#pragma unroll
+      for (int t = 0; t < 6; ++t) load_point<T, DIR>(P, t, W[t]);
+      T fl[5];
+      interface_flux<T, DIR>(W, gama, eps, fl);
+      flux_store(m, a, fl);
+    }
+  } else {
+    const int a = tid % TA, m0 = (tid / TA) * Tl::IPT;
+    auto P = [&](int f, int t) -> T { return sf[sidx(f, m0 + t, a)]; };
+    if (a0 + a < na && d0 - 1 + m0 <= nd - 1) {
+      WPt<T> W[6];
+#pragma unroll
+      for (int t = 0; t < 5; ++t) load_point<T, DIR>(P, t, W[t]);
+#pragma unroll 1
+      for (int w = 0; w < Tl::IPT; ++w) {
+        if (d0 - 1 + m0 + w <= nd - 1) {
+          load_point<T, DIR>(P, w + 5, W[5]);
+          T fl[5];
+          interface_flux<T, DIR>(W, gama, eps, fl);
+          flux_store(m0 + w, a, fl);
+        }
+#pragma unroll
+        for (int t = 0; t < 5; ++t) W[t] = W[t + 1];
+      }
     }
   }
   __syncthreads();
