@@ -30,6 +30,7 @@ def install():
     if "matplotlib" not in sys.modules:
         mpl = _stub_module("matplotlib")
         plt = _stub_module("matplotlib.pyplot")
+        plt.style = types.SimpleNamespace(use=lambda *a, **k: None)  # katzer_init.py:16 sets a style
         mpl.pyplot = plt
 
     import sympy
@@ -117,3 +118,24 @@ def install():
             out.append(OpenSBLIEq(v, factor(rhs_matrix[no])) if rhs_matrix[no] != 0 else S.Zero)
         return out
     _sc.EigenSystem.generate_equations_from_matrices = _eqs_from_matrices
+
+    # (9) MetricsEquation.generate_sd_metrics_equations zips two N-d arrays (equation_types/metric.py:
+    # 207-212); SymPy 1.1 iterated them element by element, current SymPy iterates sub-arrays.
+    from sympy import flatten as _flatten, Equality
+    from opensbli.equation_types import metric as _metric
+    from opensbli.equation_types.opensbliequations import OpenSBLIEquation
+
+    def _sd_eqns(cls):
+        def elems(a):
+            return list(a.reshape(len(a)) if hasattr(a, "reshape") and hasattr(a, "shape") else _flatten(a))
+        eqns = [OpenSBLIEq(x, y) for x, y in zip(elems(cls.SD_metrics), elems(cls.SD_evaluations))]
+        eqns = [e for e in eqns if isinstance(e, Equality)]
+        cls.sdequations = [OpenSBLIEquation(e.lhs, e.rhs) for e in eqns]
+        return
+    _metric.MetricsEquation.generate_sd_metrics_equations = _sd_eqns
+
+    # (10) a GroupedPiecewise nested in an expression is printed as a Piecewise
+    # (code_generation/opsc.py:48 OPSCCodePrinter; SymPy 1.1 found _print_Piecewise through the MRO).
+    from opensbli.code_generation.opsc import OPSCCodePrinter
+    if not hasattr(OPSCCodePrinter, "_print_GroupedPiecewise"):
+        OPSCCodePrinter._print_GroupedPiecewise = OPSCCodePrinter._print_Piecewise

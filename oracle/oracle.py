@@ -39,11 +39,14 @@ class Cfg(ctypes.Structure):
 
 
 def build(force=False):
-    src = os.path.join(HERE, "src", "osb_oracle.c")
-    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+    srcs = [os.path.join(HERE, "src", f) for f in ("osb_oracle.c", "osb_oracle2d.c")]
+    deps = srcs + [os.path.join(HERE, "src", "osb_oracle.h")]
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(f) for f in deps):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
-    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-std=c99", "-o", LIB, src, "-lm"])
+    tmp = LIB + ".tmp"
+    subprocess.check_call(["gcc", "-O2", "-fPIC", "-shared", "-std=c99", "-o", tmp] + srcs + ["-lm"])
+    os.replace(tmp, LIB)
     return LIB
 
 
@@ -54,7 +57,7 @@ def lib():
     global _lib
     if _lib is None:
         _lib = ctypes.CDLL(build())
-        for name in ("osbo_tgv_init", "osbo_run", "osbo_residual"):
+        for name in ("osbo_tgv_init", "osbo_run", "osbo_residual", "osbo2d_run", "osbo2d_metrics"):
             getattr(_lib, name).restype = ctypes.c_int
     return _lib
 
@@ -105,3 +108,58 @@ def residual(c, q0):
     r = np.zeros_like(q)
     assert lib().osbo_residual(ctypes.byref(c), _ptr(q), _ptr(r)) == 0
     return r
+
+
+class Cfg2D(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_int * 2),
+        ("delta", ctypes.c_double * 2),
+        ("gama", ctypes.c_double),
+        ("Minf", ctypes.c_double),
+        ("Re", ctypes.c_double),
+        ("Pr", ctypes.c_double),
+        ("Twall", ctypes.c_double),
+        ("SuthT", ctypes.c_double),
+        ("RefT", ctypes.c_double),
+        ("teno_eps", ctypes.c_double),
+        ("teno_ct", ctypes.c_double),
+        ("Lx1", ctypes.c_double),
+        ("by", ctypes.c_double),
+        ("rkA", ctypes.c_double * 3),
+        ("rkB", ctypes.c_double * 3),
+        ("dt", ctypes.c_double),
+    ]
+
+
+def make_cfg2d(plan):
+    """Oracle configuration from a 2D Plan (opensbli_gb300.plan.Plan with ndim=2)."""
+    c = Cfg2D()
+    for d in range(2):
+        c.n[d] = plan.n[d]
+        c.delta[d] = plan.delta[d]
+    c.gama, c.Minf, c.Re, c.Pr = plan.gama, plan.Minf, plan.Re, plan.Pr
+    c.Twall, c.SuthT, c.RefT = plan.Twall, plan.SuthT, plan.RefT
+    c.teno_eps, c.teno_ct = plan.teno_eps, plan.teno_ct
+    c.Lx1, c.by = plan.Lx1, plan.by
+    for s in range(3):
+        c.rkA[s] = plan.rk_a[s]
+        c.rkB[s] = plan.rk_b[s]
+    c.dt = plan.dt
+    return c
+
+
+def run2d(plan, q0_padded, nsteps):
+    """q0_padded: FP64 [4][n1+8][n0+8] with a 4-point halo.  Returns the state after nsteps."""
+    c = make_cfg2d(plan)
+    q = np.ascontiguousarray(q0_padded, dtype=np.float64).copy()
+    assert q.shape == (4, plan.n[1] + 8, plan.n[0] + 8)
+    assert lib().osbo2d_run(ctypes.byref(c), _ptr(q), int(nsteps)) == 0
+    return q
+
+
+def metrics2d(plan):
+    c = make_cfg2d(plan)
+    D = np.zeros((plan.n[1], plan.n[0]))
+    S = np.zeros_like(D)
+    assert lib().osbo2d_metrics(ctypes.byref(c), _ptr(D), _ptr(S)) == 0
+    return D, S

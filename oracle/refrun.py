@@ -42,8 +42,9 @@ def load_dump(path, interior=True):
     pad = size - dm + dp
     a = np.fromfile(path, dtype=np.float64, offset=48).reshape(pad[2], pad[1], pad[0])
     if not interior:
-        return a
-    return a[-dm[2]:-dm[2] + size[2], -dm[1]:-dm[1] + size[1], -dm[0]:-dm[0] + size[0]]
+        return a[0] if size[2] == 1 and pad[2] == 1 else a
+    a = a[-dm[2]:-dm[2] + size[2], -dm[1]:-dm[1] + size[1], -dm[0]:-dm[0] + size[0]]
+    return a[0] if size[2] == 1 and pad[2] == 1 else a
 
 
 def run(case, params, variables, threads=None, outdir=None, timeout=3600):
@@ -55,6 +56,7 @@ def run(case, params, variables, threads=None, outdir=None, timeout=3600):
     if threads:
         env["OMP_NUM_THREADS"] = str(threads)
     tmp = outdir or tempfile.mkdtemp(prefix="osbref_")
+    os.makedirs(tmp, exist_ok=True)
     env["OSB_DUMP_DIR"] = tmp
     out = subprocess.run([exe], env=env, cwd=tmp, capture_output=True, text=True, timeout=timeout)
     if out.returncode != 0:

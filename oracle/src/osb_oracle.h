@@ -42,6 +42,24 @@ int osbo_run(const osbo_cfg *cfg, double *q, int nsteps, double *ke);
  * kernel-level parity tests.  r has the same layout as q. */
 int osbo_residual(const osbo_cfg *cfg, const double *q, double *r);
 
+/* ---- 2D curvilinear shock/boundary-layer path (TENO5, metrics, Sutherland, walls, LS-RK3) ---- */
+typedef struct {
+  int n[2];          /* interior points in x0, x1 */
+  double delta[2];   /* computational spacing: Delta0block0, Delta1block0 */
+  double gama, Minf, Re, Pr, Twall, SuthT, RefT;
+  double teno_eps, teno_ct;
+  double Lx1, by;    /* x1 = Lx1 sinh(by delta1 j / Lx1) / sinh(by) */
+  double rkA[3], rkB[3];
+  double dt;
+} osbo2d_cfg;
+
+/* Advance q by nsteps LS-RK3 steps.  q holds [4][n1+8][n0+8]: rho, rhou0, rhou1, rhoE with a
+ * 4-point halo on every side (the initial state must fill the halos as the script's
+ * initialisation kernel does); it is overwritten with the final state, halos included. */
+int osbo2d_run(const osbo2d_cfg *cfg, double *q, int nsteps);
+/* Metric terms D11 and SD111 on the interior, [n1][n0]. */
+int osbo2d_metrics(const osbo2d_cfg *cfg, double *D11, double *SD111);
+
 #ifdef __cplusplus
 }
 #endif
