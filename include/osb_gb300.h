@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-#define OSB_ABI_VERSION 1
+#define OSB_ABI_VERSION 2
 
 /* error codes */
 #define OSB_OK 0
@@ -47,6 +47,10 @@ extern "C" {
 /* boundary conditions (core/boundary_conditions/periodic.py, symmetry.py, isothermal_wall.py ...) */
 #define OSB_BC_PERIODIC 0
 #define OSB_BC_SYMMETRY 1
+#define OSB_BC_INLET_PRESSURE_EXTRAPOLATE 2 /* inlet_pressure_extrapolate.py:11-66 (x0 side 0) */
+#define OSB_BC_EXTRAPOLATION 3             /* extrapolation.py:8-58, order 0 (x0 side 1) */
+#define OSB_BC_ISOTHERMAL_WALL 4           /* isothermal_wall.py:11-88 (x1 side 0) */
+#define OSB_BC_DIRICHLET 5                 /* dirichlet.py:6-41 with a state switched at x0 (x1 side 1) */
 /* arithmetic: all FP64 (the reference's Double datatype, core/datatypes.py:2-13), or FP32 state
  * and flux arithmetic with the RK accumulator in FP64 */
 #define OSB_PREC_FP64 0
@@ -69,6 +73,13 @@ typedef struct osb_plan_desc {
   double rk_a[3];    /* rk_sbli: rkold[]; rk_LS: A[] */
   double rk_b[3];    /* rk_sbli: rknew[]; rk_LS: B[] */
   int use_graphs;    /* capture one RK3 step as a CUDA graph */
+  /* 2D wall-bounded blocks (apps/katzer_SBLI/katzer_SBLI.py): isothermal wall temperature,
+   * Sutherland constants (mu = T^1.5 (1 + SuthT/RefT)/(T + SuthT/RefT)), and the Dirichlet face's
+   * two states: dirichlet_state[0] where x0 <= dirichlet_x_switch, [1] where x0 > it; rho, rhou0,
+   * rhou1, rhoE. */
+  double Twall, SuthT, RefT;
+  double dirichlet_state[2][4];
+  double dirichlet_x_switch;
 } osb_plan_desc;
 
 /* Memory layout of every per-variable array: x fastest, interior point (i,j,k) at element
@@ -105,6 +116,17 @@ int osb_set_stream(osb_ctx *ctx, void *stream);
  * RK register and the bound state. */
 int osb_init_tgv(osb_ctx *ctx);
 
+/* Set variable `var` from a device array that includes a halo of width h (1 <= h <= the layout's halo)
+ * on every side: [n1+2h][n0+2h] in 2D, [n2+2h][n1+2h][n0+2h] in 3D, FP64.  Initial conditions whose
+ * kernel also fills halos (GridBasedInitialisation ranges, initialisation/gridbasedinit.py:15-57)
+ * use this. */
+int osb_set_state64_padded(osb_ctx *ctx, int var, const double *dev_padded, int h);
+
+/* 2D blocks stretched in x1: set the x1 coordinate (device FP64, [n1+2h][n0+2h] with halo h) and
+ * evaluate the metric terms once: detJ = dx1/dxi1 with the boundary closures, D11 = 1/detJ with
+ * mirrored halos, SD111 = dD11/dxi1 (equation_types/metric.py:37-234, 315-332). */
+int osb_set_coordinate(osb_ctx *ctx, int axis, const double *dev_padded, int h);
+
 /* Set / read the FP64 master copy of variable `var` from / into a device array of n0*n1*n2 doubles
  * laid out [z][y][x] (interior only); setting also refreshes the bound state.  In FP64 mode the
  * master copy is the state itself; in mixed mode it is the FP64 RK accumulator. */
@@ -117,7 +139,8 @@ int osb_get_state64(osb_ctx *ctx, int var, double *dev_interior);
 int osb_step(osb_ctx *ctx, int nsteps, double dt);
 
 /* Evaluate the spatial residual R(q) of the bound state into `var`-major device array out
- * (5 * n0*n1*n2 values of the state precision, [var][z][y][x] interior) without advancing. */
+ * (nvar * n0*n1*n2 values of the state precision, [var][z][y][x] interior) without advancing.
+ * On 2D blocks the LS-RK register is used as scratch (its next use multiplies it by A[0] = 0). */
 int osb_residual(osb_ctx *ctx, void *dev_out);
 
 /* FP64 reduction over the interior (OSB_RED_*); synchronises the context stream. */

@@ -1,0 +1,581 @@
+// osb_2d.cu -- the 2D curvilinear wall-bounded path: metrics stretched in x1, TENO5 (or WENO5-JS)
+// characteristic fluxes, Sutherland viscous terms with one-sided boundary closures, the
+// low-storage RK3 update and the four face conditions of the shock/boundary-layer problem.
+//
+// Kernel list per RK stage (the generated loop, algorithm.py:384-477, for
+// apps/katzer_SBLI/katzer_SBLI.py with fixed-C_T TENO):
+//   k2_bc_* (inlet, outlet, wall, top, in that order) on the FP64 master state
+//   k2_to_state (mixed only: FP64 master -> FP32 working state, halos included)
+//   k2_prims   constituent relations u0, u1, p, a, T, mu (Sutherland)
+//   k2_flux<T, D, SCHEME> for D = x0, x1: interface fluxes + flux difference into R
+//   k2_visc_rk viscous/heat-flux terms + LS-RK3: du = A du + dt R, q += B du (FP64)
+// Metrics (once, k2_metric_*): detJ = dx1/dxi1 with the closures, D11 = 1/detJ, halos mirrored about
+// the boundary points, SD111 = dD11/dxi1 (equation_types/metric.py:37-234, 315-332).
+#include "osb_common.cuh"
+#include "osb_internal.h"
+
+namespace osb {
+
+namespace {
+
+template <typename T> __device__ __forceinline__ T rcp2(T x);
+template <> __device__ __forceinline__ float rcp2<float>(float x) { return __fdividef(1.0f, x); }
+template <> __device__ __forceinline__ double rcp2<double>(double x) { return 1.0 / x; }
+
+// ---- one-sided closures of the ReducedAccess boundary scheme (reduced_access_scheme.py:34-83):
+// G(o) reads the function at offset o along the axis, k is the point's index, n the axis size.
+template <typename T, typename Gf> __device__ __forceinline__ T d1c(const Gf &G, int k, int n) {
+  if (k == 0) return T(-25.0 / 12.0) * G(0) + T(4) * G(1) - T(3) * G(2) + T(4.0 / 3.0) * G(3) - T(0.25) * G(4);
+  if (k == 1) return T(-0.25) * G(-1) - T(5.0 / 6.0) * G(0) + T(1.5) * G(1) - T(0.5) * G(2) + T(1.0 / 12.0) * G(3);
+  if (k == n - 1) return T(25.0 / 12.0) * G(0) - T(4) * G(-1) + T(3) * G(-2) - T(4.0 / 3.0) * G(-3) + T(0.25) * G(-4);
+  if (k == n - 2) return T(0.25) * G(1) + T(5.0 / 6.0) * G(0) - T(1.5) * G(-1) + T(0.5) * G(-2) - T(1.0 / 12.0) * G(-3);
+  return T(1.0 / 12.0) * G(-2) - T(2.0 / 3.0) * G(-1) + T(2.0 / 3.0) * G(1) - T(1.0 / 12.0) * G(2);
+}
+template <typename T, typename Gf> __device__ __forceinline__ T d2c(const Gf &G, int k, int n) {
+  if (k == 0)
+    return T(35.0 / 12.0) * G(0) - T(26.0 / 3.0) * G(1) + T(9.5) * G(2) - T(14.0 / 3.0) * G(3) + T(11.0 / 12.0) * G(4);
+  if (k == 1)
+    return T(11.0 / 12.0) * G(-1) - T(5.0 / 3.0) * G(0) + T(0.5) * G(1) + T(1.0 / 3.0) * G(2) - T(1.0 / 12.0) * G(3);
+  if (k == n - 1)
+    return T(35.0 / 12.0) * G(0) - T(26.0 / 3.0) * G(-1) + T(9.5) * G(-2) - T(14.0 / 3.0) * G(-3) + T(11.0 / 12.0) * G(-4);
+  if (k == n - 2)
+    return T(11.0 / 12.0) * G(1) - T(5.0 / 3.0) * G(0) + T(0.5) * G(-1) + T(1.0 / 3.0) * G(-2) - T(1.0 / 12.0) * G(-3);
+  return T(-1.0 / 12.0) * G(-2) + T(4.0 / 3.0) * G(-1) - T(2.5) * G(0) + T(4.0 / 3.0) * G(1) - T(1.0 / 12.0) * G(2);
+}
+
+__device__ __forceinline__ int64_t g2(const Grid &g, int i, int j) { return g.off0 + (int64_t)i + (int64_t)j * g.sy; }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------------------------
+// metrics
+// ---------------------------------------------------------------------------------------------
+__global__ void k2_metric_d11(Grid g, const double *x1, double *D11, double inv_d1) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.n0 || j >= g.n1) return;
+  auto G = [&](int o) { return x1[g2(g, i, j + o)]; };
+  const double detJ = inv_d1 * d1c<double>(G, j, g.n1);
+  D11[g2(g, i, j)] = 1.0 / detJ;
+}
+
+// mirror D11 into the halos: axis 0 then axis 1, sides 0 and 1 (3 points on side 0, 4 on side 1)
+__global__ void k2_metric_halo(Grid g, double *D11, int axis, int hx, int hy) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (axis == 0) {
+    const int j = t - hy;
+    if (j >= g.n1 + hy) return;
+    for (int k = 1; k <= 3; ++k) D11[g2(g, -k, j)] = D11[g2(g, k, j)];
+    for (int k = 1; k <= 4 && k <= hx; ++k) D11[g2(g, g.n0 - 1 + k, j)] = D11[g2(g, g.n0 - 1 - k, j)];
+  } else {
+    const int i = t - hx;
+    if (i >= g.n0 + hx) return;
+    for (int k = 1; k <= 3; ++k) D11[g2(g, i, -k)] = D11[g2(g, i, k)];
+    for (int k = 1; k <= 4 && k <= hy; ++k) D11[g2(g, i, g.n1 - 1 + k)] = D11[g2(g, i, g.n1 - 1 - k)];
+  }
+}
+
+__global__ void k2_metric_sd(Grid g, const double *D11, double *SD111, double inv_d1) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.n0 || j >= g.n1) return;
+  auto G = [&](int o) { return D11[g2(g, i, j + o)]; };
+  SD111[g2(g, i, j)] = inv_d1 * d1c<double>(G, j, g.n1);
+}
+
+// ---------------------------------------------------------------------------------------------
+// boundary conditions on the FP64 master state, x0 side 0, x0 side 1, x1 side 0, x1 side 1
+// ---------------------------------------------------------------------------------------------
+struct Q4 {
+  double *v[4];
+};
+
+// InletPressureExtrapolateBC (core/boundary_conditions/inlet_pressure_extrapolate.py:11-66):
+// supersonic points at i = 0 take the halo state at i = -1; subsonic points keep their state and the
+// energy halos take rhoE(0).
+__global__ void k2_bc_inlet(Grid g, Q4 q, double gama, int h) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x - 3;
+  if (j >= g.n1 + h) return;
+  const int64_t b = g2(g, 0, j), m1 = g2(g, -1, j);
+  const double rhob = q.v[0][b];
+  const double ub0 = fabs(q.v[1][b] / rhob), ub1 = fabs(q.v[2][b] / rhob);
+  const double pb = (gama - 1) * (-0.5 * rhob * (ub0 * ub0 + ub1 * ub1) + q.v[3][b]);
+  const double ab = sqrt(gama * pb / rhob);
+  if (ub0 >= ab) {
+    for (int v = 0; v < 4; ++v) q.v[v][b] = q.v[v][m1];
+  } else {
+    const double e = q.v[3][b];
+    for (int t = 1; t <= 3; ++t) q.v[3][g2(g, -t, j)] = e;
+  }
+}
+
+// ExtrapolationBC, order 0 (core/boundary_conditions/extrapolation.py:8-58): the last point and the
+// halo points take the state of point n0-2.
+__global__ void k2_bc_outlet(Grid g, Q4 q, int hx, int hy) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x - 3;
+  if (j >= g.n1 + hy) return;
+  for (int v = 0; v < 4; ++v) {
+    const double val = q.v[v][g2(g, g.n0 - 2, j)];
+    for (int t = 0; t <= hx; ++t) q.v[v][g2(g, g.n0 - 1 + t, j)] = val;
+  }
+}
+
+// IsothermalWallBC (core/boundary_conditions/isothermal_wall.py:32-88)
+__global__ void k2_bc_wall(Grid g, Q4 q, double gama, double Minf, double Twall, int hx) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x - 3;
+  if (i >= g.n0 + hx) return;
+  const double M2 = Minf * Minf;
+  const int64_t w = g2(g, i, 0), a1 = g2(g, i, 1);
+  q.v[1][w] = 0.0;
+  q.v[2][w] = 0.0;
+  q.v[3][w] = Twall * (1.0 / M2) * q.v[0][w] / (gama * (gama - 1.0));
+  const double Pw = (gama - 1) * (-(0.5 * q.v[1][w] * q.v[1][w] + 0.5 * q.v[2][w] * q.v[2][w]) / q.v[0][w] + q.v[3][w]);
+  const double Ta = M2 * gama * (gama - 1) *
+                    (-(0.5 * q.v[1][a1] * q.v[1][a1] + 0.5 * q.v[2][a1] * q.v[2][a1]) / q.v[0][a1] + q.v[3][a1]) /
+                    q.v[0][a1];
+  for (int t = 1; t <= 3; ++t) {
+    const int64_t m = g2(g, i, t), hh = g2(g, i, -t);
+    const double um0 = q.v[1][m] / q.v[0][m], um1 = q.v[2][m] / q.v[0][m];
+    const double Tt = (t + 1) * Twall - t * Ta;
+    const double rh = M2 * gama * Pw / Tt;
+    q.v[0][hh] = rh;
+    q.v[1][hh] = -rh * um0;
+    q.v[2][hh] = -rh * um1;
+    q.v[3][hh] = (1.0 / (gama - 1)) * Pw + 0.5 * rh * (um0 * um0 + um1 * um1);
+  }
+}
+
+// DirichletBC with a piecewise state in x0 (katzer_SBLI.py:108-114): points j >= n1-1 take
+// state[1] where x0 = delta0 * i > x_switch and state[0] elsewhere.
+struct Dir2 {
+  double lo[4], hi[4];
+};
+__global__ void k2_bc_top(Grid g, Q4 q, Dir2 st, double delta0, double xs, int hx, int hy) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x - 3;
+  if (i >= g.n0 + hx) return;
+  const double x0 = delta0 * i;
+  for (int j = g.n1 - 1; j < g.n1 + hy; ++j)
+    for (int v = 0; v < 4; ++v) q.v[v][g2(g, i, j)] = x0 > xs ? st.hi[v] : st.lo[v];
+}
+
+template <typename T> struct Q4T {
+  T *v[4];
+};
+
+// FP64 master -> working state (mixed path), every padded point.
+__global__ void k2_to_state(int64_t numel, Q4 src, Q4T<float> dst) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < numel; t += (int64_t)gridDim.x * blockDim.x)
+    for (int v = 0; v < 4; ++v) dst.v[v][t] = (float)src.v[v][t];
+}
+
+// ---------------------------------------------------------------------------------------------
+// constituent relations over -3..n+3 (u, p, a) with T and Sutherland mu
+// ---------------------------------------------------------------------------------------------
+template <typename T> struct Prims {
+  T *u0, *u1, *p, *a, *T_, *mu;
+};
+
+template <typename T>
+__global__ void k2_prims(Grid g, Q4T<const T> q, Prims<T> pr, double gama, double Minf, double suth) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x - 3, j = blockIdx.y * blockDim.y + threadIdx.y - 3;
+  if (i >= g.n0 + 4 || j >= g.n1 + 4) return;
+  const int64_t n = g2(g, i, j);
+  const T r = q.v[0][n];
+  const T ir = T(1) / r;
+  const T u0 = q.v[1][n] * ir, u1 = q.v[2][n] * ir;
+  const T gm = T(gama);
+  const T p = (gm - T(1)) * (q.v[3][n] - T(0.5) * r * u0 * u0 - T(0.5) * r * u1 * u1);
+  pr.u0[n] = u0;
+  pr.u1[n] = u1;
+  pr.p[n] = p;
+  pr.a[n] = sqrt_t(gm * p * ir);
+  const T Tt = T(Minf * Minf * gama) * p * ir;
+  const T S = T(suth);
+  pr.T_[n] = Tt;
+  pr.mu[n] = (S + T(1)) * Tt * sqrt_t(Tt) / (S + Tt);
+}
+
+// ---------------------------------------------------------------------------------------------
+// characteristic fluxes (4 conserved variables) with WENO5-JS or TENO5
+// ---------------------------------------------------------------------------------------------
+template <typename T> __device__ __forceinline__ T w5_side(T f0, T f1, T f2, T f3, T f4, T eps) {
+  const T c13 = T(13.0 / 48.0), c14 = T(1.0 / 16.0);
+  const T t0 = f2 - T(2) * f3 + f4, s0 = T(3) * f2 - T(4) * f3 + f4;
+  const T t1 = f1 - T(2) * f2 + f3, s1 = f1 - f3;
+  const T t2 = f0 - T(2) * f1 + f2, s2 = f0 - T(4) * f1 + T(3) * f2;
+  const T e0 = c13 * t0 * t0 + c14 * s0 * s0 + eps, e1 = c13 * t1 * t1 + c14 * s1 * s1 + eps,
+          e2 = c13 * t2 * t2 + c14 * s2 * s2 + eps;
+  const T a0 = T(3.0 / 10.0) * rcp2(e0 * e0), a1 = T(3.0 / 5.0) * rcp2(e1 * e1), a2 = T(1.0 / 10.0) * rcp2(e2 * e2);
+  const T p0 = T(1.0 / 6.0) * f2 + T(5.0 / 12.0) * f3 - T(1.0 / 12.0) * f4;
+  const T p1 = T(-1.0 / 12.0) * f1 + T(5.0 / 12.0) * f2 + T(1.0 / 6.0) * f3;
+  const T p2 = T(1.0 / 6.0) * f0 - T(7.0 / 12.0) * f1 + T(11.0 / 12.0) * f2;
+  return (a0 * p0 + a1 * p1 + a2 * p2) * rcp2(a0 + a1 + a2);
+}
+
+// TENO5 with a fixed cut-off (schemes/spatial/teno.py:57-213, 407-465) on f = CF +- lambda CS,
+// ordered from the far upwind point to the far downwind one.  Smoothness indicators of the halved
+// values; alpha_r = (1 + |b0 - b2| / (eps + b_r))^6 for the central (0), downwind (1) and upwind (2)
+// candidates; delta_r = 0 where alpha_r / sum < C_T; weights d = (11/20, 2/5, 1/20).  The
+// normalised weights are formed from the ratios m_r / max m so that (.)^6 cannot overflow.
+template <typename T> __device__ __forceinline__ T t5_side(T f0, T f1, T f2, T f3, T f4, T eps, T ct) {
+  const T h0 = T(0.5) * f0, h1 = T(0.5) * f1, h2 = T(0.5) * f2, h3 = T(0.5) * f3, h4 = T(0.5) * f4;
+  const T c13 = T(13.0 / 12.0), c14 = T(0.25);
+  const T x0 = h1 - h3, y0 = h1 - T(2) * h2 + h3;
+  const T x1 = h2 - T(2) * h3 + h4, y1 = T(3) * h2 - T(4) * h3 + h4;
+  const T x2 = h0 - T(4) * h1 + T(3) * h2, y2 = h0 - T(2) * h1 + h2;
+  const T b0 = c14 * x0 * x0 + c13 * y0 * y0;
+  const T b1 = c13 * x1 * x1 + c14 * y1 * y1;
+  const T b2 = c14 * x2 * x2 + c13 * y2 * y2;
+  const T tau = abs_t(b0 - b2);
+  const T m0 = T(1) + tau / (eps + b0), m1 = T(1) + tau / (eps + b1), m2 = T(1) + tau / (eps + b2);
+  const T mm = max_t(m0, max_t(m1, m2));
+  const T n0 = m0 / mm, n1 = m1 / mm, n2 = m2 / mm;
+  const T q0 = (n0 * n0) * (n0 * n0) * (n0 * n0), q1 = (n1 * n1) * (n1 * n1) * (n1 * n1),
+          q2 = (n2 * n2) * (n2 * n2) * (n2 * n2);
+  const T iq = T(1) / (q0 + q1 + q2);
+  const T d0 = ct > q0 * iq ? T(0) : T(1), d1 = ct > q1 * iq ? T(0) : T(1), d2 = ct > q2 * iq ? T(0) : T(1);
+  const T w0 = T(0.55) * d0, w1 = T(0.4) * d1, w2 = T(0.05) * d2;
+  const T iw = T(1) / (w0 + w1 + w2);
+  return (w0 * (T(-1.0 / 12.0) * f1 + T(5.0 / 12.0) * f2 + T(1.0 / 6.0) * f3) +
+          w1 * (T(1.0 / 6.0) * f2 + T(5.0 / 12.0) * f3 - T(1.0 / 12.0) * f4) +
+          w2 * (T(1.0 / 6.0) * f0 - T(7.0 / 12.0) * f1 + T(11.0 / 12.0) * f2)) *
+         iw;
+}
+
+enum { S2_RHO = 0, S2_RU0, S2_RU1, S2_E, S2_P, S2_A, S2_UD, S2_NF };
+
+template <typename T> struct W2 {
+  T Q[4], ud, a, p;
+};
+
+// Characteristic flux between window points 2 and 3 along D (2D Euler eigensystem for a unit
+// normal, physical_models/euler_eigensystem.py:77-105; the block's metric is diagonal so the
+// eigensystem is Cartesian).  Dense rows share g = phi X0 - (g-1) u.X + (g-1) X3, h = X_{1+D} - u_D X0.
+template <typename T, int D, bool TENO>
+__device__ __forceinline__ void flux2(const W2<T> (&W)[6], T gama, T eps, T ct, T out[4]) {
+  constexpr int E = 1 - D;
+  const T s = D == 0 ? T(1) : T(-1);
+  const T gm1 = gama - T(1);
+  const T rl = W[2].Q[0], rr = W[3].Q[0];
+  const T sl = sqrt_t(rl), sr = sqrt_t(rr);
+  const T rho = sqrt_t(rl * rr);
+  const T inv_s = T(1) / (sl + sr);
+  T u[2];
+#pragma unroll
+  for (int c = 0; c < 2; ++c) u[c] = inv_s * (sl * (W[2].Q[1 + c] / rl) + sr * (W[3].Q[1 + c] / rr));
+  const T Hh = inv_s * ((W[2].p + W[2].Q[3]) / sl + (W[3].p + W[3].Q[3]) / sr);
+  const T usq = u[0] * u[0] + u[1] * u[1];
+  const T a = sqrt_t(gm1 * (Hh - T(0.5) * usq));
+  const T ia = T(1) / a, irho = T(1) / rho;
+  const T phi = gm1 * T(0.5) * usq;
+  const T bt = T(0.70710678118654752440) * irho * ia, al = T(0.70710678118654752440) * rho * ia;
+  const T ia2 = ia * ia, btA = bt * a;
+  T lu = T(0), lp = T(0), lm = T(0);
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    lu = max_t(lu, abs_t(W[t].ud));
+    lp = max_t(lp, abs_t(W[t].ud + W[t].a));
+    lm = max_t(lm, abs_t(W[t].a - W[t].ud));
+  }
+  auto recon = [&](const T (&cf)[6], const T (&cs)[6], T lam) -> T {
+    T fp[6], fm[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      fp[t] = cf[t] + lam * cs[t];
+      fm[t] = cf[t] - lam * cs[t];
+    }
+    if (TENO)
+      return t5_side(fp[0], fp[1], fp[2], fp[3], fp[4], eps, ct) + t5_side(fm[5], fm[4], fm[3], fm[2], fm[1], eps, ct);
+    return w5_side(fp[0], fp[1], fp[2], fp[3], fp[4], eps) + w5_side(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
+  };
+  T r0, r1, r2, r3;
+  {
+    T cf[6], cs[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {  // shear row: (s/rho)(u_E X0 - X_{1+E})
+      cf[t] = s * irho * (u[E] * W[t].Q[1 + D] - W[t].Q[1 + E] * W[t].ud);
+      cs[t] = s * irho * (u[E] * W[t].Q[0] - W[t].Q[1 + E]);
+    }
+    r1 = recon(cf, cs, lu);
+    T gQ[6], gF[6], hQ[6], hF[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      const W2<T> &w = W[t];
+      const T dq = u[0] * w.Q[1] + u[1] * w.Q[2];
+      gQ[t] = phi * w.Q[0] - gm1 * dq + gm1 * w.Q[3];
+      hQ[t] = w.Q[1 + D] - u[D] * w.Q[0];
+      gF[t] = phi * w.Q[1 + D] - gm1 * (w.ud * dq + u[D] * w.p) + gm1 * (w.p + w.Q[3]) * w.ud;
+      hF[t] = w.Q[1 + D] * w.ud + w.p - u[D] * w.Q[1 + D];
+    }
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = W[t].Q[1 + D] - gF[t] * ia2;
+      cs[t] = W[t].Q[0] - gQ[t] * ia2;
+    }
+    r0 = recon(cf, cs, lu);
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = bt * gF[t] + btA * hF[t];
+      cs[t] = bt * gQ[t] + btA * hQ[t];
+    }
+    r2 = recon(cf, cs, lp);
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = bt * gF[t] - btA * hF[t];
+      cs[t] = bt * gQ[t] - btA * hQ[t];
+    }
+    r3 = recon(cf, cs, lm);
+  }
+  const T sac = r2 + r3, dac = r2 - r3;
+  const T hh = (phi + a * a) / gm1;
+  out[0] = r0 + al * sac;
+#pragma unroll
+  for (int c = 0; c < 2; ++c) out[1 + c] = u[c] * r0 + al * (u[c] * sac + (c == D ? a * dac : T(0)));
+  out[3] = (phi / gm1) * r0 + al * (hh * sac + u[D] * a * dac);
+  out[1 + E] -= s * rho * r1;
+  out[3] -= s * rho * u[E] * r1;
+}
+
+template <int D> struct T2Tile;
+template <> struct T2Tile<0> { static constexpr int TI = 64, TA = 4; };
+template <> struct T2Tile<1> { static constexpr int TI = 24, TA = 16; };  // static smem < 48 KB in FP64
+
+// Interface fluxes along D for a tile and the flux difference -(F_i - F_{i-1})/delta (times D11 for
+// x1), written (D = 0) or accumulated (D = 1) into R.
+template <typename T, int D, bool TENO>
+__global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<const T> pr, const double *D11,
+                                               Q4T<T> res, double gama_d, double eps_d, double ct_d, double inv_dd) {
+  using Tl = T2Tile<D>;
+  constexpr int TI = Tl::TI, TA = Tl::TA, NPT = TI + 5;
+  __shared__ T sf[S2_NF][NPT][TA];
+  __shared__ T sfl[4][TI][TA];
+  const int tid = threadIdx.x;
+  const int nd = D == 0 ? g.n0 : g.n1, na = D == 0 ? g.n1 : g.n0;
+  const int d0 = (D == 0 ? blockIdx.x : blockIdx.y) * (TI - 1);
+  const int a0 = (D == 0 ? blockIdx.y : blockIdx.x) * TA;
+  auto coord = [&](int c, int a, int &i, int &j) {
+    if (D == 0) { i = c; j = a0 + a; }
+    else { i = a0 + a; j = c; }
+  };
+  for (int t = tid; t < NPT * TA; t += 256) {
+    int pos, a;
+    if (D == 0) { a = t / NPT; pos = t % NPT; }
+    else { pos = t / TA; a = t % TA; }
+    const int c = d0 - 3 + pos;
+    if (c > nd + 2 || a0 + a >= na) continue;
+    int i, j;
+    coord(c, a, i, j);
+    const int64_t m = g2(g, i, j);
+    sf[S2_RHO][pos][a] = q.v[0][m];
+    sf[S2_RU0][pos][a] = q.v[1][m];
+    sf[S2_RU1][pos][a] = q.v[2][m];
+    sf[S2_E][pos][a] = q.v[3][m];
+    sf[S2_P][pos][a] = pr.p[m];
+    sf[S2_A][pos][a] = pr.a[m];
+    sf[S2_UD][pos][a] = D == 0 ? pr.u0[m] : pr.u1[m];
+  }
+  __syncthreads();
+  const T gama = T(gama_d), eps = T(eps_d), ct = T(ct_d);
+  for (int t = tid; t < TI * TA; t += 256) {
+    int m, a;
+    if (D == 0) { a = t / TI; m = t % TI; }
+    else { m = t / TA; a = t % TA; }
+    if (d0 - 1 + m > nd - 1 || a0 + a >= na) continue;
+    W2<T> W[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+      W[k].Q[0] = sf[S2_RHO][m + k][a];
+      W[k].Q[1] = sf[S2_RU0][m + k][a];
+      W[k].Q[2] = sf[S2_RU1][m + k][a];
+      W[k].Q[3] = sf[S2_E][m + k][a];
+      W[k].p = sf[S2_P][m + k][a];
+      W[k].a = sf[S2_A][m + k][a];
+      W[k].ud = sf[S2_UD][m + k][a];
+    }
+    T fl[4];
+    flux2<T, D, TENO>(W, gama, eps, ct, fl);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) sfl[v][m][a] = fl[v];
+  }
+  __syncthreads();
+  for (int t = tid; t < (TI - 1) * TA; t += 256) {
+    int m, a;
+    if (D == 0) { a = t / (TI - 1); m = t % (TI - 1); }
+    else { m = t / TA; a = t % TA; }
+    const int c = d0 + m;
+    if (c >= nd || a0 + a >= na) continue;
+    int i, j;
+    coord(c, a, i, j);
+    const int64_t gi = g2(g, i, j);
+    const T scale = D == 0 ? T(inv_dd) : T(inv_dd) * T(D11[gi]);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const T d = -(sfl[v][m + 1][a] - sfl[v][m][a]) * scale;
+      if (D == 0) res.v[v][gi] = d;
+      else res.v[v][gi] += d;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// viscous terms (stretched metric, closures) + LS-RK3 update
+// ---------------------------------------------------------------------------------------------
+struct Visc2Args {
+  double Re, kappa, inv_d0, inv_d1, dt, A, B;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k2_visc_rk(Grid g, Prims<const T> pr, const double *D11, const double *SD111,
+                                                  Q4T<const T> res, Q4 du, Q4 q64, Visc2Args va, int update) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.n0 || j >= g.n1) return;
+  const int64_t c = g2(g, i, j);
+  const T id0 = T(va.inv_d0), id1 = T(va.inv_d1), iRe = T(1.0 / va.Re);
+  const T Dm = T(D11[c]), S = T(SD111[c]), mu = pr.mu[c];
+  const T *uc[2] = {pr.u0, pr.u1};
+  auto X = [&](const T *f, int o) { return f[g2(g, i + o, j)]; };
+  auto Y = [&](const T *f, int o) { return f[g2(g, i, j + o)]; };
+  T gr[2][2], h[2][2][2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const T *f = uc[k];
+    gr[k][0] = id0 * d1c<T>([&](int o) { return X(f, o); }, i, g.n0);
+    const T fy = id1 * d1c<T>([&](int o) { return Y(f, o); }, j, g.n1);
+    gr[k][1] = Dm * fy;
+    h[k][0][0] = id0 * id0 * d2c<T>([&](int o) { return X(f, o); }, i, g.n0);
+    h[k][1][1] = Dm * Dm * (id1 * id1 * d2c<T>([&](int o) { return Y(f, o); }, j, g.n1)) + Dm * S * fy;
+    // d/dx0 of the row j+o, then d/dxi1 of that column (inner axis x0 over the extended x1 range)
+    auto inner = [&](int o) {
+      return id0 * d1c<T>([&](int p) { return f[g2(g, i + p, j + o)]; }, i, g.n0);
+    };
+    h[k][0][1] = h[k][1][0] = Dm * (id1 * d1c<T>(inner, j, g.n1));
+  }
+  const T mux = id0 * d1c<T>([&](int o) { return X(pr.mu, o); }, i, g.n0);
+  const T muy = Dm * id1 * d1c<T>([&](int o) { return Y(pr.mu, o); }, j, g.n1);
+  const T Tx = id0 * d1c<T>([&](int o) { return X(pr.T_, o); }, i, g.n0);
+  const T Tyx = id1 * d1c<T>([&](int o) { return Y(pr.T_, o); }, j, g.n1);
+  const T Ty = Dm * Tyx;
+  const T Txx = id0 * id0 * d2c<T>([&](int o) { return X(pr.T_, o); }, i, g.n0);
+  const T Tyy = Dm * Dm * (id1 * id1 * d2c<T>([&](int o) { return Y(pr.T_, o); }, j, g.n1)) + Dm * S * Tyx;
+  const T div = gr[0][0] + gr[1][1];
+  const T mug[2] = {mux, muy};
+  const T uu[2] = {pr.u0[c], pr.u1[c]};
+  T R[4] = {res.v[0][c], res.v[1][c], res.v[2][c], res.v[3][c]};
+  T e = T(va.kappa) * (mu * (Txx + Tyy) + mux * Tx + muy * Ty);
+#pragma unroll
+  for (int a = 0; a < 2; ++a) {
+    T v = T(0);
+#pragma unroll
+    for (int b = 0; b < 2; ++b) v += mug[b] * (gr[a][b] + gr[b][a] - (a == b ? T(2.0 / 3.0) * div : T(0))) * iRe;
+    const T lap = h[a][0][0] + h[a][1][1];
+    const T ddiv = h[0][a][0] + h[1][a][1];
+    v += mu * iRe * (lap + ddiv * T(1.0 / 3.0));
+    R[1 + a] += v;
+    e += uu[a] * v;
+#pragma unroll
+    for (int b = 0; b < 2; ++b) e += mu * iRe * (gr[a][b] + gr[b][a] - (a == b ? T(2.0 / 3.0) * div : T(0))) * gr[a][b];
+  }
+  R[3] += e;
+  if (update) {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      const double d = va.dt * (double)R[v] + va.A * du.v[v][c];
+      du.v[v][c] = d;
+      q64.v[v][c] = va.B * d + q64.v[v][c];
+    }
+  } else {
+#pragma unroll
+    for (int v = 0; v < 4; ++v) du.v[v][c] = (double)R[v];  // residual output mode: du holds R
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------------------------
+static Q4 q4(double *const *a) {
+  Q4 r;
+  for (int v = 0; v < 4; ++v) r.v[v] = a[v];
+  return r;
+}
+template <typename T> static Q4T<T> q4t(void *const *a) {
+  Q4T<T> r;
+  for (int v = 0; v < 4; ++v) r.v[v] = static_cast<T *>(a[v]);
+  return r;
+}
+
+void launch2_metrics(const Ctx &c, const double *x1, cudaStream_t s, int64_t *launches) {
+  dim3 b(32, 8), gr((c.g.n0 + 31) / 32, (c.g.n1 + 7) / 8);
+  const double inv_d1 = 1.0 / c.plan.delta[1];
+  k2_metric_d11<<<gr, b, 0, s>>>(c.g, x1, c.d11, inv_d1);
+  k2_metric_halo<<<(c.g.n1 + 2 * c.hy2 + 127) / 128, 128, 0, s>>>(c.g, c.d11, 0, c.hx2, c.hy2);
+  k2_metric_halo<<<(c.g.n0 + 2 * c.hx2 + 127) / 128, 128, 0, s>>>(c.g, c.d11, 1, c.hx2, c.hy2);
+  k2_metric_sd<<<gr, b, 0, s>>>(c.g, c.d11, c.sd111, inv_d1);
+  *launches += 4;
+}
+
+void launch2_bcs(const Ctx &c, cudaStream_t s, int64_t *launches) {
+  const osb_plan_desc &p = c.plan;
+  Q4 q = q4(c.q64_2d);
+  const int ny = c.g.n1 + 3 + c.hy2, nx = c.g.n0 + 3 + c.hx2;
+  k2_bc_inlet<<<(ny + 127) / 128, 128, 0, s>>>(c.g, q, p.gama, c.hy2);
+  k2_bc_outlet<<<(ny + 127) / 128, 128, 0, s>>>(c.g, q, c.hx2, c.hy2);
+  k2_bc_wall<<<(nx + 127) / 128, 128, 0, s>>>(c.g, q, p.gama, p.Minf, p.Twall, c.hx2);
+  Dir2 st;
+  for (int v = 0; v < 4; ++v) {
+    st.lo[v] = p.dirichlet_state[0][v];
+    st.hi[v] = p.dirichlet_state[1][v];
+  }
+  k2_bc_top<<<(nx + 127) / 128, 128, 0, s>>>(c.g, q, st, p.delta[0], p.dirichlet_x_switch, c.hx2, c.hy2);
+  *launches += 4;
+  if (c.mixed) {
+    int nb = (int)((c.g.numel + 255) / 256);
+    if (nb > 152 * 8) nb = 152 * 8;
+    k2_to_state<<<nb, 256, 0, s>>>(c.g.numel, q, q4t<float>(c.qa));
+    ++*launches;
+  }
+}
+
+template <typename T> void launch2_rhs(const Ctx &c, int update, double A, double B, double dt, cudaStream_t s,
+                                       int64_t *launches) {
+  const osb_plan_desc &p = c.plan;
+  Prims<T> pr;
+  pr.u0 = static_cast<T *>(c.prim2[0]);
+  pr.u1 = static_cast<T *>(c.prim2[1]);
+  pr.p = static_cast<T *>(c.prim2[2]);
+  pr.a = static_cast<T *>(c.prim2[3]);
+  pr.T_ = static_cast<T *>(c.prim2[4]);
+  pr.mu = static_cast<T *>(c.prim2[5]);
+  Prims<const T> prc{pr.u0, pr.u1, pr.p, pr.a, pr.T_, pr.mu};
+  Q4T<const T> q = q4t<const T>(c.qa);
+  dim3 b(32, 8), gp((c.g.n0 + 7 + 31) / 32, (c.g.n1 + 7 + 7) / 8);
+  k2_prims<T><<<gp, b, 0, s>>>(c.g, q, pr, p.gama, p.Minf, p.SuthT / p.RefT);
+  Q4T<T> r = q4t<T>(c.res);
+  const bool teno = p.conv == OSB_CONV_TENO5;
+  const double eps = teno ? p.teno_eps : p.weno_eps;
+  {
+    using Tl = T2Tile<0>;
+    dim3 gx((c.g.n0 + Tl::TI - 2) / (Tl::TI - 1), (c.g.n1 + Tl::TA - 1) / Tl::TA);
+    if (teno) k2_flux<T, 0, true><<<gx, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, 1.0 / p.delta[0]);
+    else k2_flux<T, 0, false><<<gx, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, 1.0 / p.delta[0]);
+  }
+  {
+    using Tl = T2Tile<1>;
+    dim3 gy((c.g.n0 + Tl::TA - 1) / Tl::TA, (c.g.n1 + Tl::TI - 2) / (Tl::TI - 1));
+    if (teno) k2_flux<T, 1, true><<<gy, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, 1.0 / p.delta[1]);
+    else k2_flux<T, 1, false><<<gy, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, 1.0 / p.delta[1]);
+  }
+  Visc2Args va;
+  va.Re = p.Re;
+  va.kappa = 1.0 / ((p.gama - 1) * p.Minf * p.Minf * p.Pr * p.Re);
+  va.inv_d0 = 1.0 / p.delta[0];
+  va.inv_d1 = 1.0 / p.delta[1];
+  va.dt = dt;
+  va.A = A;
+  va.B = B;
+  dim3 gv((c.g.n0 + 31) / 32, (c.g.n1 + 7) / 8);
+  k2_visc_rk<T><<<gv, b, 0, s>>>(c.g, prc, c.d11, c.sd111, q4t<const T>(c.res), q4(c.du2), q4(c.q64_2d), va, update);
+  *launches += 4;
+}
+
+template void launch2_rhs<float>(const Ctx &, int, double, double, double, cudaStream_t, int64_t *);
+template void launch2_rhs<double>(const Ctx &, int, double, double, double, cudaStream_t, int64_t *);
+
+}  // namespace osb

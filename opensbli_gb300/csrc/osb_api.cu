@@ -34,7 +34,27 @@ int cuda_err(osb_ctx *c, cudaError_t e, const char *where) {
 int validate(const osb_plan_desc *p, char *why, size_t n) {
   if (!p) { snprintf(why, n, "null plan"); return OSB_EINVAL; }
   if (p->abi_version != OSB_ABI_VERSION) { snprintf(why, n, "abi_version %d != %d", p->abi_version, OSB_ABI_VERSION); return OSB_EINVAL; }
-  if (p->ndim != 3) { snprintf(why, n, "ndim %d: this library implements 3D blocks", p->ndim); return OSB_EUNSUPPORTED; }
+  if (p->ndim == 2) {
+    for (int d = 0; d < 2; ++d) {
+      if (p->n[d] < 8 || p->n[d] > 16384) { snprintf(why, n, "n[%d] = %d out of range [8, 16384]", d, p->n[d]); return OSB_EINVAL; }
+      if (!(p->delta[d] > 0)) { snprintf(why, n, "delta[%d] must be > 0", d); return OSB_EINVAL; }
+    }
+    if (p->bc[0][0] != OSB_BC_INLET_PRESSURE_EXTRAPOLATE || p->bc[0][1] != OSB_BC_EXTRAPOLATION ||
+        p->bc[1][0] != OSB_BC_ISOTHERMAL_WALL || p->bc[1][1] != OSB_BC_DIRICHLET) {
+      snprintf(why, n, "2D blocks: boundary conditions must be inlet/extrapolation (x0) and isothermal wall/Dirichlet (x1)");
+      return OSB_EUNSUPPORTED;
+    }
+    if (p->conv != OSB_CONV_TENO5 && p->conv != OSB_CONV_WENO5JS) { snprintf(why, n, "2D blocks: TENO5 or WENO5-JS fluxes"); return OSB_EUNSUPPORTED; }
+    if (p->visc != OSB_VISC_SUTHERLAND) { snprintf(why, n, "2D blocks: Sutherland viscosity"); return OSB_EUNSUPPORTED; }
+    if (p->rk != OSB_RK3_LS) { snprintf(why, n, "2D blocks: low-storage RK3"); return OSB_EUNSUPPORTED; }
+    if (p->precision != OSB_PREC_FP64 && p->precision != OSB_PREC_MIXED) { snprintf(why, n, "precision %d", p->precision); return OSB_EINVAL; }
+    if (!(p->gama > 1.0) || !(p->Minf > 0) || !(p->Re > 0) || !(p->Pr > 0) || !(p->Twall > 0) || !(p->RefT > 0)) {
+      snprintf(why, n, "bad physical constants");
+      return OSB_EINVAL;
+    }
+    return OSB_OK;
+  }
+  if (p->ndim != 3) { snprintf(why, n, "ndim %d: this library implements 2D and 3D blocks", p->ndim); return OSB_EUNSUPPORTED; }
   for (int d = 0; d < 3; ++d) {
     if (p->n[d] < 8 || p->n[d] > 4096) { snprintf(why, n, "n[%d] = %d out of range [8, 4096]", d, p->n[d]); return OSB_EINVAL; }
     if (!(p->delta[d] > 0)) { snprintf(why, n, "delta[%d] must be > 0", d); return OSB_EINVAL; }
@@ -64,6 +84,18 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
 
 Grid make_grid(const osb_plan_desc *p) {
   Grid g;
+  if (p->ndim == 2) {  // x fastest, 4-point halo on every side, one plane
+    g.n0 = p->n[0];
+    g.n1 = p->n[1];
+    g.n2 = 1;
+    int64_t px = p->n[0] + 8;
+    px = (px + 7) / 8 * 8;
+    g.sy = px;
+    g.sz = px * (p->n[1] + 8);
+    g.off0 = 4 + 4 * g.sy;
+    g.numel = g.sz;
+    return g;
+  }
   g.n0 = p->n[0];
   g.n1 = p->n[1];
   g.n2 = p->n[2];
@@ -355,9 +387,140 @@ template <typename T> int step_impl(osb_ctx *c, int nsteps, double dt) {
   return cuda_err(c, cudaGetLastError(), "osb_step launch");
 }
 
+// One LS-RK3 step on a 2D block: boundary conditions, then per stage the right-hand side with the
+// update du = A du + dt R, q += B du, and the boundary conditions again (algorithm.py:384-477).
+template <typename T> void one_step2(osb_ctx *c, double dt, cudaStream_t s) {
+  {
+    ProfScope ps(c, PF_HALO, s);
+    launch2_bcs(*c, s, &c->launches);
+  }
+  for (int st = 0; st < 3; ++st) {
+    {
+      ProfScope ps(c, PF_CENTRAL_RK, s);
+      launch2_rhs<T>(*c, 1, c->plan.rk_a[st], c->plan.rk_b[st], dt, s, &c->launches);
+    }
+    ProfScope ps(c, PF_HALO, s);
+    launch2_bcs(*c, s, &c->launches);
+  }
+}
+
+template <typename T> int step2_impl(osb_ctx *c, int nsteps, double dt) {
+  cudaStream_t s = c->stream;
+  c->launches = 0;
+  for (int it = 0; it < nsteps; ++it) {
+    if (c->plan.use_graphs && !c->prof_on && s != nullptr) {
+      if (c->graph[0] && c->graph_dt[0] != dt) {
+        cudaGraphExecDestroy(c->graph[0]);
+        c->graph[0] = nullptr;
+      }
+      if (!c->graph[0]) {
+        cudaGraph_t gr;
+        const int64_t l0 = c->launches;
+        cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_err(c, e, "cudaStreamBeginCapture");
+        one_step2<T>(c, dt, s);
+        e = cudaStreamEndCapture(s, &gr);
+        if (e != cudaSuccess) return cuda_err(c, e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&c->graph[0], gr, 0);
+        cudaGraphDestroy(gr);
+        if (e != cudaSuccess) return cuda_err(c, e, "cudaGraphInstantiate");
+        c->graph_dt[0] = dt;
+        c->graph_launches = c->launches - l0;
+        c->launches = l0;
+      }
+      cudaError_t e = cudaGraphLaunch(c->graph[0], s);
+      if (e != cudaSuccess) return cuda_err(c, e, "cudaGraphLaunch");
+      c->launches += c->graph_launches;
+    } else {
+      one_step2<T>(c, dt, s);
+    }
+  }
+  if (c->prof_on) prof_collect(c);
+  return cuda_err(c, cudaGetLastError(), "osb_step launch");
+}
+
+template <typename T> __global__ void k_set64_padded(Grid g, const double *src, int h, T *q, double *q64) {
+  const int w = g.n0 + 2 * h, hgt = g.n1 + 2 * h, dep = g.n2 == 1 ? 1 : g.n2 + 2 * h;
+  const int64_t N = (int64_t)w * hgt * dep;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % w) - h, j = (int)((t / w) % hgt) - h;
+    const int k = g.n2 == 1 ? 0 : (int)(t / ((int64_t)w * hgt)) - h;
+    const int64_t n = gidx(g, i, j, k);
+    q64[n] = src[t];
+    q[n] = (T)src[t];
+  }
+}
+
+__global__ void k_copy_padded(Grid g, const double *src, int h, double *dst) {
+  const int w = g.n0 + 2 * h, hgt = g.n1 + 2 * h;
+  const int64_t N = (int64_t)w * hgt;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % w) - h, j = (int)(t / w) - h;
+    dst[gidx(g, i, j, 0)] = src[t];
+  }
+}
+
+struct P4 {
+  const double *v[4];
+};
+template <typename T> __global__ void k_pack_d(Grid g, P4 src4, T *dst, int nvar) {
+  const int64_t N = (int64_t)g.n0 * g.n1 * g.n2;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.n0), j = (int)((t / g.n0) % g.n1), k = (int)(t / ((int64_t)g.n0 * g.n1));
+    for (int v = 0; v < nvar; ++v) dst[v * N + t] = (T)src4.v[v][gidx(g, i, j, k)];
+  }
+}
+
+struct D4 {
+  const double *v[4];
+};
+__global__ void k_reduce2(Grid g, D4 q, int what, double *partial) {
+  const int64_t N = (int64_t)g.n0 * g.n1;
+  double acc = 0.0;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.n0), j = (int)(t / g.n0);
+    const int64_t n = gidx(g, i, j, 0);
+    if (what == OSB_RED_KE) acc += 0.5 * (q.v[1][n] * q.v[1][n] + q.v[2][n] * q.v[2][n]) / q.v[0][n];
+    else
+      for (int v = 0; v < 4; ++v)
+        if (!isfinite(q.v[v][n])) acc = 1.0;
+  }
+  const double s = block_sum(acc);
+  if (threadIdx.x == 0) partial[blockIdx.x] = (what == OSB_RED_NANCHECK) ? (s > 0 ? 1.0 : 0.0) : s;
+}
+
 }  // namespace
 
 extern "C" {
+
+static int check_bound(osb_ctx *c);
+
+int osb_set_state64_padded(osb_ctx *c, int var, const double *src, int h) {
+  if (!c) return OSB_EINVAL;
+  if (int rc = check_bound(c)) return rc;
+  const int hmax = c->plan.ndim == 2 ? 4 : HY;
+  if (var < 0 || var >= c->nvar || !src || h < 1 || h > hmax) return set_err(c, OSB_EINVAL, "bad var, pointer or halo");
+  double *m = c->plan.ndim == 2 ? c->q64_2d[var] : c->qold[var];
+  const int64_t N = (int64_t)(c->g.n0 + 2 * h) * (c->g.n1 + 2 * h) * (c->plan.ndim == 2 ? 1 : c->g.n2 + 2 * h);
+  const int nb = blocks_for(N);
+  if (c->mixed) k_set64_padded<float><<<nb, 256, 0, c->stream>>>(c->g, src, h, (float *)c->qa[var], m);
+  else k_set64_padded<double><<<nb, 256, 0, c->stream>>>(c->g, src, h, (double *)c->qa[var], m);
+  c->qold_valid = 1;
+  c->cur = 0;
+  return cuda_err(c, cudaGetLastError(), "osb_set_state64_padded");
+}
+
+int osb_set_coordinate(osb_ctx *c, int axis, const double *src, int h) {
+  if (!c) return OSB_EINVAL;
+  if (c->plan.ndim != 2 || axis != 1) return set_err(c, OSB_EUNSUPPORTED, "coordinates: 2D blocks stretched in x1 only");
+  if (!src || h < 4 || h > 4) return set_err(c, OSB_EINVAL, "coordinate array needs a 4-point halo");
+  const int nb = blocks_for((int64_t)(c->g.n0 + 2 * h) * (c->g.n1 + 2 * h));
+  k_copy_padded<<<nb, 256, 0, c->stream>>>(c->g, src, h, c->x1);
+  int64_t l = 0;
+  launch2_metrics(*c, c->x1, c->stream, &l);
+  c->metrics_valid = 1;
+  return cuda_err(c, cudaGetLastError(), "osb_set_coordinate");
+}
 
 int osb_query_layout(const osb_plan_desc *plan, osb_layout *out) {
   char why[256];
@@ -370,9 +533,9 @@ int osb_query_layout(const osb_plan_desc *plan, osb_layout *out) {
   out->stride_y = g.sy;
   out->stride_z = g.sz;
   out->halo[0] = HX;
-  out->halo[1] = HY;
-  out->halo[2] = HZ;
-  out->nvar = 5;
+  out->halo[1] = plan->ndim == 2 ? 4 : HY;
+  out->halo[2] = plan->ndim == 2 ? 0 : HZ;
+  out->nvar = plan->ndim == 2 ? 4 : 5;
   out->state_bytes = plan->precision == OSB_PREC_MIXED ? 4 : 8;
   return OSB_OK;
 }
@@ -399,9 +562,42 @@ int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
   for (int d = 0; d < 3; ++d) c->ph.inv_delta[d] = 1.0 / plan->delta[d];
   c->ph.weno_eps = plan->weno_eps > 0 ? plan->weno_eps : 1e-6;
   const size_t bytes = (size_t)c->g.numel * c->elem;
+  cudaError_t e = cudaSuccess;
+  if (plan->ndim == 2) {
+    c->nvar = 4;
+    const size_t b64 = (size_t)c->g.numel * sizeof(double);
+    for (int v = 0; v < 4 && e == cudaSuccess; ++v) {
+      if (c->mixed) {
+        e = cudaMalloc(&c->q64_2d[v], b64);
+        if (e == cudaSuccess) e = cudaMemset(c->q64_2d[v], 0, b64);
+      }
+      if (e == cudaSuccess) e = cudaMalloc(&c->du2[v], b64);
+      if (e == cudaSuccess) e = cudaMemset(c->du2[v], 0, b64);
+      if (e == cudaSuccess) e = cudaMalloc(&c->res[v], bytes);
+      if (e == cudaSuccess) e = cudaMemset(c->res[v], 0, bytes);
+    }
+    for (int k = 0; k < 6 && e == cudaSuccess; ++k) {
+      e = cudaMalloc(&c->prim2[k], bytes);
+      if (e == cudaSuccess) e = cudaMemset(c->prim2[k], 0, bytes);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&c->x1, b64);
+    if (e == cudaSuccess) e = cudaMalloc(&c->d11, b64);
+    if (e == cudaSuccess) e = cudaMalloc(&c->sd111, b64);
+    if (e == cudaSuccess) e = cudaMemset(c->d11, 0, b64);
+    if (e == cudaSuccess) e = cudaMemset(c->sd111, 0, b64);
+    c->red_blocks = 152 * 8;
+    if (e == cudaSuccess) e = cudaMalloc(&c->red, (c->red_blocks + 1) * sizeof(double));
+    if (e != cudaSuccess) {
+      fprintf(stderr, "osb_create: %s\n", cudaGetErrorString(e));
+      osb_destroy(c);
+      return OSB_ECUDA;
+    }
+    *out = c;
+    return OSB_OK;
+  }
   if (c->mixed) { setup_central<float>(); setup_weno<float>(); }
   else { setup_central<double>(); setup_weno<double>(); }
-  cudaError_t e = cudaGetLastError();
+  e = cudaGetLastError();
   for (int v = 0; v < 5 && e == cudaSuccess; ++v) {
     e = cudaMalloc(&c->qb[v], bytes);
     if (e == cudaSuccess) e = cudaMalloc(&c->qold[v], (size_t)c->g.numel * sizeof(double));
@@ -423,9 +619,10 @@ int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
 
 int osb_bind_field(osb_ctx *c, int var, void *dev_ptr) {
   if (!c) return OSB_EINVAL;
-  if (var < 0 || var >= 5) return set_err(c, OSB_EINVAL, "var out of range");
+  if (var < 0 || var >= c->nvar) return set_err(c, OSB_EINVAL, "var out of range");
   if (!dev_ptr || ((uintptr_t)dev_ptr % 32) != 0) return set_err(c, OSB_EINVAL, "device pointer null or not 32-byte aligned");
   c->qa[var] = dev_ptr;
+  if (c->plan.ndim == 2 && !c->mixed) c->q64_2d[var] = static_cast<double *>(dev_ptr);
   c->qold_valid = 0;
   c->cur = 0;
   for (int s = 0; s < 2; ++s)
@@ -442,7 +639,7 @@ int osb_set_stream(osb_ctx *c, void *stream) {
 }
 
 static int check_bound(osb_ctx *c) {
-  for (int v = 0; v < 5; ++v)
+  for (int v = 0; v < c->nvar; ++v)
     if (!c->qa[v]) return set_err(c, OSB_ENOTBOUND, "a conserved variable is not bound");
   return OSB_OK;
 }
@@ -450,6 +647,7 @@ static int check_bound(osb_ctx *c) {
 int osb_init_tgv(osb_ctx *c) {
   if (!c) return OSB_EINVAL;
   if (int rc = check_bound(c)) return rc;
+  if (c->plan.ndim != 3) return set_err(c, OSB_EUNSUPPORTED, "the Taylor-Green initial condition is 3D");
   const int nb = blocks_for((int64_t)c->g.n0 * c->g.n1 * c->g.n2);
   const osb_plan_desc &p = c->plan;
   if (c->mixed)
@@ -467,8 +665,14 @@ int osb_init_tgv(osb_ctx *c) {
 int osb_set_state64(osb_ctx *c, int var, const double *src) {
   if (!c) return OSB_EINVAL;
   if (int rc = check_bound(c)) return rc;
-  if (var < 0 || var >= 5 || !src) return set_err(c, OSB_EINVAL, "bad var or pointer");
+  if (var < 0 || var >= c->nvar || !src) return set_err(c, OSB_EINVAL, "bad var or pointer");
   const int nb = blocks_for((int64_t)c->g.n0 * c->g.n1 * c->g.n2);
+  if (c->plan.ndim == 2) {
+    if (c->mixed) k_set64<float><<<nb, 256, 0, c->stream>>>(c->g, src, (float *)c->qa[var], c->q64_2d[var]);
+    else k_set64<double><<<nb, 256, 0, c->stream>>>(c->g, src, (double *)c->qa[var], c->q64_2d[var]);
+    c->qold_valid = 1;
+    return cuda_err(c, cudaGetLastError(), "osb_set_state64");
+  }
   if (c->mixed) k_set64<float><<<nb, 256, 0, c->stream>>>(c->g, src, (float *)c->qa[var], c->qold[var]);
   else k_set64<double><<<nb, 256, 0, c->stream>>>(c->g, src, (double *)c->qa[var], c->qold[var]);
   c->qold_valid = 1;
@@ -483,10 +687,10 @@ int osb_set_state64(osb_ctx *c, int var, const double *src) {
 
 int osb_get_state64(osb_ctx *c, int var, double *dst) {
   if (!c) return OSB_EINVAL;
-  if (var < 0 || var >= 5 || !dst) return set_err(c, OSB_EINVAL, "bad var or pointer");
+  if (var < 0 || var >= c->nvar || !dst) return set_err(c, OSB_EINVAL, "bad var or pointer");
   if (!c->qold_valid) return set_err(c, OSB_EINVAL, "no state yet: call osb_init_tgv, osb_set_state64 or osb_step");
   const int nb = blocks_for((int64_t)c->g.n0 * c->g.n1 * c->g.n2);
-  k_get64<<<nb, 256, 0, c->stream>>>(c->g, c->qold[var], dst);
+  k_get64<<<nb, 256, 0, c->stream>>>(c->g, c->plan.ndim == 2 ? c->q64_2d[var] : c->qold[var], dst);
   return cuda_err(c, cudaGetLastError(), "osb_get_state64");
 }
 
@@ -494,6 +698,11 @@ int osb_step(osb_ctx *c, int nsteps, double dt) {
   if (!c) return OSB_EINVAL;
   if (int rc = check_bound(c)) return rc;
   if (nsteps < 0 || !(dt > 0)) return set_err(c, OSB_EINVAL, "nsteps >= 0 and dt > 0 required");
+  if (c->plan.ndim == 2) {
+    if (!c->metrics_valid) return set_err(c, OSB_EINVAL, "2D block: call osb_set_coordinate first");
+    if (!c->qold_valid) return set_err(c, OSB_EINVAL, "2D block: set the state first");
+    return c->mixed ? step2_impl<float>(c, nsteps, dt) : step2_impl<double>(c, nsteps, dt);
+  }
   return c->mixed ? step_impl<float>(c, nsteps, dt) : step_impl<double>(c, nsteps, dt);
 }
 
@@ -502,6 +711,21 @@ int osb_residual(osb_ctx *c, void *dev_out) {
   if (int rc = check_bound(c)) return rc;
   if (!dev_out) return set_err(c, OSB_EINVAL, "null output");
   const int nb = blocks_for((int64_t)c->g.n0 * c->g.n1 * c->g.n2);
+  if (c->plan.ndim == 2) {
+    if (!c->metrics_valid) return set_err(c, OSB_EINVAL, "2D block: call osb_set_coordinate first");
+    int64_t l = 0;
+    launch2_bcs(*c, c->stream, &l);
+    P4 d;
+    for (int v = 0; v < 4; ++v) d.v[v] = c->du2[v];
+    if (c->mixed) {
+      launch2_rhs<float>(*c, 0, 0.0, 0.0, 0.0, c->stream, &l);
+      k_pack_d<float><<<nb, 256, 0, c->stream>>>(c->g, d, (float *)dev_out, 4);
+    } else {
+      launch2_rhs<double>(*c, 0, 0.0, 0.0, 0.0, c->stream, &l);
+      k_pack_d<double><<<nb, 256, 0, c->stream>>>(c->g, d, (double *)dev_out, 4);
+    }
+    return cuda_err(c, cudaGetLastError(), "osb_residual");
+  }
   if (c->mixed) {
     residual_into<float>(c, c->cur, c->stream);
     k_pack<float><<<nb, 256, 0, c->stream>>>(c->g, fields<const float>(c->res), (float *)dev_out);
@@ -521,6 +745,20 @@ int osb_reduce(osb_ctx *c, int what, double *out) {
   const int64_t N = (int64_t)c->g.n0 * c->g.n1 * c->g.n2;
   int nb = blocks_for(N);
   if (nb > c->red_blocks) nb = c->red_blocks;
+  if (c->plan.ndim == 2) {
+    if (what == OSB_RED_ENSTROPHY) return set_err(c, OSB_EUNSUPPORTED, "enstrophy: 3D blocks");
+    D4 q2;
+    for (int v = 0; v < 4; ++v) q2.v[v] = c->q64_2d[v];
+    k_reduce2<<<nb, RED_THREADS, 0, c->stream>>>(c->g, q2, what, c->red);
+    k_reduce_final<<<1, RED_THREADS, 0, c->stream>>>(c->red, nb, what, 1.0 / (double)N, c->red + c->red_blocks);
+    double h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, c->red + c->red_blocks, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "osb_reduce");
+    *out = h;
+    if (what == OSB_RED_NANCHECK && h != 0.0) return set_err(c, OSB_ENONFINITE, "non-finite value in the state");
+    return OSB_OK;
+  }
   Fields5<const double> qo;
   for (int v = 0; v < 5; ++v) qo.v[v] = c->qold[v];
   const double *id = c->ph.inv_delta;
@@ -573,6 +811,14 @@ void osb_destroy(osb_ctx *c) {
     cudaFree(c->res[v]);
   }
   cudaFree(c->red);
+  for (int v = 0; v < 4; ++v) {
+    if (c->mixed) cudaFree(c->q64_2d[v]);
+    cudaFree(c->du2[v]);
+  }
+  for (int k = 0; k < 6; ++k) cudaFree(c->prim2[k]);
+  cudaFree(c->x1);
+  cudaFree(c->d11);
+  cudaFree(c->sd111);
   delete c;
 }
 

@@ -30,6 +30,14 @@ struct Ctx {
   int64_t launches = 0;
   int64_t graph_launches = 0;  // kernel launches recorded in one captured step
   int qold_valid = 0;          // the FP64 register holds the current state
+  // 2D wall-bounded path
+  int nvar = 5;
+  int hx2 = 4, hy2 = 4;           // halos of the 2D layout
+  double *q64_2d[4] = {};         // FP64 master state, padded (the bound arrays in FP64 mode)
+  double *du2[4] = {};            // LS-RK register
+  void *prim2[6] = {};            // u0, u1, p, a, T, mu (state precision, padded)
+  double *x1 = nullptr, *d11 = nullptr, *sd111 = nullptr;
+  int metrics_valid = 0;
   std::string err;
   // per-kernel-family event timing (osb_profile); only used on the eager (non-graph) path
   int prof_on = 0;
@@ -55,6 +63,11 @@ void launch_weno_dir(const Ctx &c, Fields5<const T> q, Fields5<T> r, int dir, cu
 template <typename T>
 void launch_central_rk(const Ctx &c, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold, Fields5<T> rin,
                        Fields5<T> rout, double dt_new, double dt_old, int mode, cudaStream_t s, int64_t *launches);
+
+void launch2_metrics(const Ctx &c, const double *x1, cudaStream_t s, int64_t *launches);
+void launch2_bcs(const Ctx &c, cudaStream_t s, int64_t *launches);
+template <typename T>
+void launch2_rhs(const Ctx &c, int update, double A, double B, double dt, cudaStream_t s, int64_t *launches);
 
 // mode bits for launch_central_rk
 constexpr int CRK_SKEW = 1;      // add skew-symmetric central convective terms

@@ -15,6 +15,26 @@ RK3_RKOLD = (1.0 / 4.0, 3.0 / 20.0, 3.0 / 5.0)
 RK3_RKNEW = (2.0 / 3.0, 5.0 / 12.0, 3.0 / 5.0)
 
 
+def ls_rk3_ssp_coefficients(c=0.924574):
+    """A and B of the 3-stage, 2-register (Williamson form) strong-stability-preserving RK3 with free
+    parameter c = B1, as RungeKuttaLS(3, 'SSP') defines them (schemes/temporal/rk_LS.py:75-89, after
+    Gottlieb, Shu and Tadmor, SIAM Review 43 (2001)).  Returns (A, B), A[0] = 0."""
+    c2, c3, c4, c5, c6 = c ** 2, c ** 3, c ** 4, c ** 5, c ** 6
+    z1 = math.sqrt(36 * c4 + 36 * c3 - 135 * c2 + 84 * c - 12)
+    z2 = 2 * c2 + c - 2
+    z3 = 12 * c4 - 18 * c3 + 18 * c2 - 11 * c + 2
+    z4 = 36 * c4 - 36 * c3 + 13 * c2 - 8 * c + 4
+    z5 = 69 * c3 - 62 * c2 + 28 * c - 8
+    z6 = 34 * c4 - 46 * c3 + 34 * c2 - 13 * c + 2
+    w = 3 * z2 - z1
+    B = (c, (12 * c * (c - 1) * w - w ** 2) / (144 * c * (3 * c - 2) * (c - 1) ** 2),
+         (-24 * (3 * c - 2) * (c - 1) ** 2) / (w ** 2 - 12 * c * (c - 1) * w))
+    A = (0.0, (-z1 * (6 * c2 - 4 * c + 1) + 3 * z3) / ((2 * c + 1) * z1 - 3 * (c + 2) * (2 * c - 1) ** 2),
+         (-z1 * z4 + 108 * (2 * c - 1) * c5 - 3 * (2 * c - 1) * z5) /
+         (24 * z1 * c * (c - 1) ** 4 + 72 * c * z6 + 72 * c6 * (2 * c - 13)))
+    return A, B
+
+
 @dataclasses.dataclass
 class Plan:
     ndim: int = 3
@@ -38,12 +58,22 @@ class Plan:
     dt: Optional[float] = None
     niter: Optional[int] = None
     ic: str = "tgv"                 # tgv | host (evaluated from the script's initialisation kernel)
+    # 2D wall-bounded blocks: wall temperature, Sutherland constants, Dirichlet face states switched
+    # at x0 = dirichlet_x_switch, x1 stretching (used by the oracle; the GPU takes coordinates)
+    Twall: float = 1.67619431
+    SuthT: float = 110.4
+    RefT: float = 288.0
+    dirichlet_lo: Tuple[float, ...] = (1.00000596004, 1.00000268202, 0.00565001630205, 0.94644428042)
+    dirichlet_hi: Tuple[float, ...] = (1.129734572, 1.0921171, -0.058866065, 1.0590824)
+    dirichlet_x_switch: float = 40.0
+    Lx1: float = 115.0
+    by: float = 5.0
     name: str = ""
     kernels: List[str] = dataclasses.field(default_factory=list)  # the reference kernel names lowered
 
     @property
     def cells(self):
-        return self.n[0] * self.n[1] * self.n[2]
+        return self.n[0] * self.n[1] * (self.n[2] if self.ndim == 3 else 1)
 
     def replace(self, **kw):
         return dataclasses.replace(self, **kw)
@@ -54,11 +84,10 @@ class Plan:
     @classmethod
     def from_json(cls, s):
         d = json.loads(s)
-        d["n"] = tuple(d["n"])
-        d["delta"] = tuple(d["delta"])
+        for k in ("n", "delta", "rk_a", "rk_b", "dirichlet_lo", "dirichlet_hi"):
+            if k in d:
+                d[k] = tuple(d[k])
         d["bc"] = tuple(tuple(x) for x in d["bc"])
-        d["rk_a"] = tuple(d["rk_a"])
-        d["rk_b"] = tuple(d["rk_b"])
         return cls(**d)
 
 
@@ -87,3 +116,16 @@ def tgv_cfl_dt(plan, cfl=0.5):
     a = np.sqrt(g * p / r)
     s = np.sqrt(u0 ** 2 + u1 ** 2) + a
     return cfl * min(plan.delta) / float(s.max())
+
+
+def katzer_plan(n0=512, n1=256, precision="fp64", conv="teno5", dt=0.04, use_graphs=True):
+    """2D laminar shock-wave/boundary-layer interaction (apps/katzer_SBLI/katzer_SBLI.py constants):
+    Mach 2, Re = 950, Pr = 0.72, Twall = 1.67619431, Sutherland 110.4/288, TENO5 with C_T = 1e-5 and
+    eps = 1e-15, domain [0, 400] x [0, 115] with x1 = 115 sinh(5 eta)/sinh(5), LS-RK3 (SSP)."""
+    A, B = ls_rk3_ssp_coefficients()
+    return Plan(ndim=2, n=(n0, n1, 1), delta=(400.0 / (n0 - 1), 115.0 / (n1 - 1), 1.0), conv=conv, visc="sutherland",
+                rk="ls_rk3", precision=precision,
+                bc=(("inlet_pressure_extrapolate", "extrapolation"), ("isothermal_wall", "dirichlet"),
+                    ("periodic", "periodic")),
+                gama=1.4, Minf=2.0, Re=950.0, Pr=0.72, teno_ct=1e-5, teno_eps=1e-15, rk_a=A, rk_b=B, dt=dt,
+                use_graphs=use_graphs, ic="host", name="katzer_%s_%dx%d" % (conv, n0, n1))

@@ -12,7 +12,7 @@ import torch
 
 from . import build as _build
 
-OSB_ABI_VERSION = 1
+OSB_ABI_VERSION = 2
 ERRORS = {
     -1: "invalid plan or argument",
     -2: "unsupported kernel pattern",
@@ -20,12 +20,14 @@ ERRORS = {
     -4: "field not bound",
     -5: "device wait timed out",
     -6: "non-finite value in the state",
+    -7: "problem larger than a fixed-size scratch array",
 }
 
 CONV = {"central_skew": 0, "weno5js": 1, "teno5": 2}
 VISC = {"none": 0, "const": 1, "sutherland": 2}
 RK = {"rk3": 0, "ls_rk3": 1}
-BC = {"periodic": 0, "symmetry": 1}
+BC = {"periodic": 0, "symmetry": 1, "inlet_pressure_extrapolate": 2, "extrapolation": 3, "isothermal_wall": 4,
+      "dirichlet": 5}
 PREC = {"fp64": 0, "mixed": 1}
 RED = {"ke": 0, "enstrophy": 1, "nancheck": 2}
 
@@ -51,6 +53,11 @@ class PlanDesc(ctypes.Structure):
         ("rk_a", ctypes.c_double * 3),
         ("rk_b", ctypes.c_double * 3),
         ("use_graphs", ctypes.c_int),
+        ("Twall", ctypes.c_double),
+        ("SuthT", ctypes.c_double),
+        ("RefT", ctypes.c_double),
+        ("dirichlet_state", (ctypes.c_double * 4) * 2),
+        ("dirichlet_x_switch", ctypes.c_double),
     ]
 
 
@@ -68,6 +75,7 @@ class Layout(ctypes.Structure):
 
 EXPORTS = (
     "osb_query_layout", "osb_create", "osb_bind_field", "osb_set_stream", "osb_init_tgv", "osb_set_state64",
+    "osb_set_state64_padded", "osb_set_coordinate",
     "osb_get_state64", "osb_step", "osb_residual", "osb_reduce", "osb_launch_count", "osb_profile", "osb_profile_read",
     "osb_get_error", "osb_destroy",
 )
@@ -98,6 +106,8 @@ def load(build_if_missing=True):
     lib.osb_set_stream.argtypes = [vp, vp]
     lib.osb_init_tgv.argtypes = [vp]
     lib.osb_set_state64.argtypes = [vp, ip, vp]
+    lib.osb_set_state64_padded.argtypes = [vp, ip, vp, ip]
+    lib.osb_set_coordinate.argtypes = [vp, ip, vp, ip]
     lib.osb_get_state64.argtypes = [vp, ip, vp]
     lib.osb_step.argtypes = [vp, ip, dp]
     lib.osb_residual.argtypes = [vp, vp]
@@ -142,6 +152,11 @@ def make_plan_desc(plan):
         d.rk_a[s] = plan.rk_a[s]
         d.rk_b[s] = plan.rk_b[s]
     d.use_graphs = 1 if plan.use_graphs else 0
+    d.Twall, d.SuthT, d.RefT = plan.Twall, plan.SuthT, plan.RefT
+    for v in range(4):
+        d.dirichlet_state[0][v] = plan.dirichlet_lo[v]
+        d.dirichlet_state[1][v] = plan.dirichlet_hi[v]
+    d.dirichlet_x_switch = plan.dirichlet_x_switch
     return d
 
 
@@ -188,11 +203,15 @@ class Solver:
 
     @property
     def shape(self):
+        if self.plan.ndim == 2:
+            return (self.plan.n[1], self.plan.n[0])
         return (self.plan.n[2], self.plan.n[1], self.plan.n[0])
 
     def interior(self, var):
-        """View of the interior of bound variable `var` as [z][y][x] (state precision)."""
+        """View of the interior of bound variable `var` as [z][y][x] ([y][x] in 2D), state precision."""
         lay = self.layout
+        if self.plan.ndim == 2:
+            return torch.as_strided(self.fields[var], self.shape, (lay.stride_y, 1), lay.offset)
         n0, n1, n2 = self.plan.n
         return torch.as_strided(self.fields[var], (n2, n1, n0), (lay.stride_z, lay.stride_y, 1), lay.offset)
 
@@ -217,6 +236,24 @@ class Solver:
         for v in range(self.layout.nvar):
             self._check(self.lib.osb_set_state64(self.ctx, v, ctypes.c_void_p(q[v].data_ptr())))
         q.record_stream(self.stream)
+        self._out()
+
+    def set_state64_padded(self, q, h):
+        """q: FP64 [nvar][...] including a halo of width h on every side (the initialisation kernel's
+        range)."""
+        q = torch.as_tensor(q, dtype=torch.float64).to(self.device).contiguous()
+        self._in()
+        for v in range(self.layout.nvar):
+            self._check(self.lib.osb_set_state64_padded(self.ctx, v, ctypes.c_void_p(q[v].data_ptr()), int(h)))
+        q.record_stream(self.stream)
+        self._out()
+
+    def set_coordinate(self, x1, h=4):
+        """2D blocks stretched in x1: the x1 coordinate, FP64 [n1+2h][n0+2h]; evaluates the metrics."""
+        x = torch.as_tensor(x1, dtype=torch.float64).to(self.device).contiguous()
+        self._in()
+        self._check(self.lib.osb_set_coordinate(self.ctx, 1, ctypes.c_void_p(x.data_ptr()), int(h)))
+        x.record_stream(self.stream)
         self._out()
 
     def state64(self):

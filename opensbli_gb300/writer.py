@@ -21,6 +21,8 @@ method of the writer taking the same two lists.
 import math
 import re
 
+import numpy as np
+
 from .plan import Plan
 
 _C_NAMES = {"M_PI": math.pi, "pi": math.pi}
@@ -94,8 +96,10 @@ class GB300Writer:
         algorithm tree, as for the OPSC writer)."""
         names = [n or "" for n in self.kernel_names]
         ndim = self.block.ndim
+        if ndim == 2:
+            return self._lower_2d(precision, use_graphs)
         if ndim != 3:
-            raise NotImplementedError("GB300Writer lowers 3D blocks (got ndim=%d)" % ndim)
+            raise NotImplementedError("GB300Writer lowers 2D and 3D blocks (got ndim=%d)" % ndim)
         skew = self._kernels("Convective terms group")
         weno = self._kernels("LLFWeno_reconstruction_")
         if self._kernels("LLFTeno_reconstruction_"):
@@ -160,6 +164,81 @@ class GB300Writer:
                     bc=tuple(tuple(p) for p in bcs), rk_a=coeff["rkold"], rk_b=coeff["rknew"],
                     use_graphs=use_graphs, ic="host", kernels=[n for n in names if n])
 
+    def _rk_coefficients(self, names_expected):
+        from sympy import preorder_traversal
+        coeff = {}
+        for kname in names_expected:
+            ks = self._kernels(kname)
+            if len(ks) != 1:
+                raise NotImplementedError("RK stage kernel %r expected" % kname)
+            for e in ks[0].equations:
+                for a in preorder_traversal(e.rhs):
+                    if type(a).__name__ == "ConstantIndexed":
+                        coeff[str(a.base)] = tuple(float(v) for v in a.value)
+        return coeff
+
+    def _lower_2d(self, precision, use_graphs):
+        """2D wall-bounded blocks (apps/katzer_SBLI/katzer_SBLI.py with a fixed TENO cut-off): metrics
+        stretched in x1, LLFTeno(5) or LLFWeno(5), Central(4) viscous terms with Sutherland viscosity,
+        RungeKuttaLS(3), inlet/extrapolation faces in x0, isothermal wall/Dirichlet faces in x1."""
+        import sympy
+        names = [n or "" for n in self.kernel_names]
+        teno = self._kernels("LLFTeno_reconstruction_")
+        weno = self._kernels("LLFWeno_reconstruction_")
+        if bool(teno) == bool(weno) or len(teno or weno) != 2:
+            raise NotImplementedError("2D blocks: one LLFTeno or LLFWeno reconstruction per direction expected")
+        for k in teno:
+            lhs = self._lhs_names(k)
+            if not {"delta_0", "delta_1", "delta_2", "inv_omega_sum"} <= lhs:
+                raise NotImplementedError("TENO5 with a cut-off expected in %s" % k.computation_name)
+            if any("TENO" in str(e.rhs) and "TENO_CT" not in str(e.rhs) for e in k.equations):
+                raise NotImplementedError("adaptive TENO (shock sensor) is not lowered; use a fixed C_T")
+        if self._max_offset(teno or weno) != 3:
+            raise NotImplementedError("5th-order reconstruction stencil expected")
+        if not self._kernels("MetricsEquation") or not self._kernels("Metric boundary"):
+            raise NotImplementedError("2D blocks: metric terms expected")
+        if not any(n.startswith("CRmu") for n in names):
+            raise NotImplementedError("2D blocks: Sutherland viscosity (CRmu) expected")
+        coeff = self._rk_coefficients(["Temporal solution advancement"])
+        if set(coeff) != {"rkA", "rkB"}:
+            raise NotImplementedError("RungeKuttaLS(3) coefficients rkA/rkB expected")
+        faces = {
+            "InletPressureExtrapolate boundary dir0 side0": ("inlet_pressure_extrapolate", 0, 0),
+            "Extrapolation boundary dir0 side1": ("extrapolation", 0, 1),
+            "IsothermalWall boundary dir1 side0": ("isothermal_wall", 1, 0),
+            "Dirichlet boundary dir1 side1": ("dirichlet", 1, 1),
+        }
+        bcs = [[None, None], [None, None]]
+        for kname, (kind, d, side) in faces.items():
+            if self._kernels(kname):
+                bcs[d][side] = kind
+        if any(b is None for pair in bcs for b in pair):
+            found = sorted(n for n in names if "boundary dir" in n)
+            raise NotImplementedError("2D boundary conditions: %s" % found)
+        # the Dirichlet face: rho, rhou0, rhou1, rhoE = Piecewise((hi, x0 > xs), (lo, True))
+        dk = self._kernels("Dirichlet boundary dir1 side1")[0]
+        lo, hi, xs = {}, {}, None
+        for e in dk.equations:
+            name = re.sub(r"_B0$", "", str(getattr(e.lhs, "base", e.lhs)))
+            rhs = e.rhs
+            if isinstance(rhs, sympy.Piecewise) and len(rhs.args) == 2:
+                (vhi, cond), (vlo, _) = rhs.args
+                if not isinstance(cond, sympy.core.relational.StrictGreaterThan):
+                    raise NotImplementedError("Dirichlet face: state switched by x0 > value expected")
+                xs = float(cond.rhs)
+                hi[name], lo[name] = float(vhi), float(vlo)
+            elif name in ("rho", "rhou0", "rhou1", "rhoE"):
+                hi[name] = lo[name] = float(rhs)
+        order = ["rho", "rhou0", "rhou1", "rhoE"]
+        if any(v not in lo for v in order):
+            raise NotImplementedError("Dirichlet face must set rho, rhou0, rhou1, rhoE")
+        return Plan(ndim=2, n=(64, 32, 1), delta=(1.0, 1.0, 1.0), conv="teno5" if teno else "weno5js",
+                    visc="sutherland", rk="ls_rk3", precision=precision,
+                    bc=(tuple(bcs[0]), tuple(bcs[1]), ("periodic", "periodic")),
+                    rk_a=coeff["rkA"], rk_b=coeff["rkB"], use_graphs=use_graphs, ic="host",
+                    dirichlet_lo=tuple(lo[v] for v in order), dirichlet_hi=tuple(hi[v] for v in order),
+                    dirichlet_x_switch=xs if xs is not None else 1e300, kernels=[n for n in names if n])
+
     # ------------------------------------------------------------------ constants
     def substitute_simulation_parameters(self, constants, values):
         """Same arguments as opensbli.utilities.helperfunctions.substitute_simulation_parameters."""
@@ -168,57 +247,84 @@ class GB300Writer:
             env[c] = _eval_c_expr(str(v), env) if isinstance(v, str) else v
         self.values.update(env)
         p = self.plan
-        n = tuple(int(env.get("block0np%d" % d, p.n[d])) for d in range(3))
-        delta = tuple(float(env.get("Delta%dblock0" % d, p.delta[d])) for d in range(3))
-        self.plan = p.replace(n=n, delta=delta, gama=float(env.get("gama", p.gama)), Minf=float(env.get("Minf", p.Minf)),
-                              Re=float(env.get("Re", p.Re)), Pr=float(env.get("Pr", p.Pr)),
-                              dt=float(env["dt"]) if "dt" in env else p.dt,
-                              niter=int(env["niter"]) if "niter" in env else p.niter)
+        nd = p.ndim
+        n = tuple(int(env.get("block0np%d" % d, p.n[d])) if d < nd else 1 for d in range(3))
+        delta = tuple(float(env.get("Delta%dblock0" % d, p.delta[d])) if d < nd else 1.0 for d in range(3))
+        kw = dict(n=n, delta=delta, gama=float(env.get("gama", p.gama)), Minf=float(env.get("Minf", p.Minf)),
+                  Re=float(env.get("Re", p.Re)), Pr=float(env.get("Pr", p.Pr)),
+                  dt=float(env["dt"]) if "dt" in env else p.dt,
+                  niter=int(env["niter"]) if "niter" in env else p.niter)
+        if nd == 2:
+            kw.update(Twall=float(env.get("Twall", p.Twall)), SuthT=float(env.get("SuthT", p.SuthT)),
+                      RefT=float(env.get("RefT", p.RefT)), teno_eps=float(env.get("eps", p.teno_eps)),
+                      teno_ct=float(env.get("TENO_CT", p.teno_ct)), Lx1=float(env.get("Lx1", p.Lx1)),
+                      by=float(env.get("by", p.by)))
+        self.plan = p.replace(**kw)
         return self.plan
 
     # ------------------------------------------------------------------ initial condition
-    def initial_state(self):
-        """FP64 initial conserved state [5][z][y][x] from the script's GridBasedInitialisation kernel
-        (initialisation/gridbasedinit.py:15-57), evaluated with numpy in the kernel's equation order."""
+    def initial_fields(self, halo=0):
+        """Evaluate the script's GridBasedInitialisation kernel (initialisation/gridbasedinit.py:15-57)
+        with numpy, in the kernel's equation order, on the interior plus `halo` points on every side.
+        Returns {name: FP64 array [z][y][x] (2D: [y][x])} for every array the kernel assigns."""
         import numpy as np
         import sympy
         k = self.ic_kernel
         if k is None:
             raise NotImplementedError("no Grid_based_initialisation kernel in the algorithm")
         p = self.plan
-        n0, n1, n2 = p.n
-        ii, jj, kk = np.meshgrid(np.arange(n0, dtype=np.float64), np.arange(n1, dtype=np.float64),
-                                 np.arange(n2, dtype=np.float64), indexing="ij")
-        grid_idx = [ii.T, jj.T, kk.T]  # [z][y][x]
+        nd = p.ndim
+        ranges = [np.arange(-halo, p.n[d] + halo, dtype=np.float64) for d in range(nd)]
+        grids = np.meshgrid(*ranges[::-1], indexing="ij")  # [z][y][x] order
+        grid_idx = grids[::-1]                               # grid_idx[d] varies along axis d
+        shape = grids[0].shape
         env = {}
         consts = dict(self.values)
         consts.update({"gama": p.gama, "Minf": p.Minf, "Re": p.Re, "Pr": p.Pr})
         for d in range(3):
             consts["Delta%dblock0" % d] = p.delta[d]
+        if nd == 2:
+            consts.update({"Lx1": p.Lx1, "by": p.by, "Twall": p.Twall, "SuthT": p.SuthT, "RefT": p.RefT})
         out = {}
         for eq in k.equations:
             rhs = eq.rhs
-            gi = {a for a in sympy.preorder_traversal(rhs) if type(a).__name__ == "Grididx"}
-            rhs = rhs.xreplace({a: sympy.Symbol("_osb_gi%d" % int(a.number)) for a in gi})
+            reps = {}
+            for a in sympy.preorder_traversal(rhs):
+                t = type(a).__name__
+                if t == "Grididx":
+                    reps[a] = sympy.Symbol("_osb_gi%d" % int(a.number))
+                elif t == "DataSet":
+                    reps[a] = sympy.Symbol("_osb_ds_" + re.sub(r"_B0$", "", str(a.base)))
+            rhs = rhs.xreplace(reps)
             subs_syms, args = [], []
-            for s in rhs.free_symbols:
-                name = str(s)
+            for sym in rhs.free_symbols:
+                name = str(sym)
                 if name.startswith("_osb_gi"):
-                    subs_syms.append(s); args.append(grid_idx[int(name[7:])])
+                    subs_syms.append(sym); args.append(grid_idx[int(name[7:])])
+                elif name.startswith("_osb_ds_"):
+                    subs_syms.append(sym); args.append(env[name[8:]])
                 elif name in env:
-                    subs_syms.append(s); args.append(env[name])
+                    subs_syms.append(sym); args.append(env[name])
                 elif name in consts:
-                    subs_syms.append(s); args.append(consts[name])
+                    subs_syms.append(sym); args.append(consts[name])
                 else:
                     raise NotImplementedError("initial condition symbol %s has no value" % name)
             f = sympy.lambdify(subs_syms, rhs, "numpy")
-            val = np.broadcast_to(np.asarray(f(*args), dtype=np.float64), (n2, n1, n0)).copy()
+            val = np.broadcast_to(np.asarray(f(*args), dtype=np.float64), shape).copy()
             lhs = eq.lhs
-            name = str(lhs.base) if hasattr(lhs, "base") else str(lhs)
-            name = re.sub(r"_B0$", "", name)
+            name = re.sub(r"_B0$", "", str(lhs.base) if hasattr(lhs, "base") else str(lhs))
             env[name] = val
             out[name] = val
-        order = ["rho", "rhou0", "rhou1", "rhou2", "rhoE"]
+        return out
+
+    def state_names(self):
+        return ["rho", "rhou0", "rhou1", "rhoE"] if self.plan.ndim == 2 else ["rho", "rhou0", "rhou1", "rhou2", "rhoE"]
+
+    def initial_state(self, halo=0):
+        """FP64 initial conserved state [nvar][...] from the script's initialisation kernel."""
+        import numpy as np
+        out = self.initial_fields(halo)
+        order = self.state_names()
         missing = [v for v in order if v not in out]
         if missing:
             raise NotImplementedError("initialisation does not set %s" % missing)
@@ -233,6 +339,11 @@ class GB300Writer:
         """Initialise from the script's initial condition and advance niter steps (defaults: the
         script's niter and dt).  Returns the Solver, whose state64() gives the FP64 state."""
         s = self.solver(device)
-        s.set_state64(self.initial_state())
+        if self.plan.ndim == 2:
+            f = self.initial_fields(halo=4)
+            s.set_coordinate(f["x1"], 4)
+            s.set_state64_padded(np.stack([f[v] for v in self.state_names()]), 4)
+        else:
+            s.set_state64(self.initial_state())
         s.step(int(niter if niter is not None else self.plan.niter), float(dt if dt is not None else self.plan.dt))
         return s

@@ -62,11 +62,16 @@ def lower(case, ref, out, n=None):
     if n is not None:
         for d in range(3):
             if "block0np%d" % d in consts:
-                vals[consts.index("block0np%d" % d)] = str(n)
+                vals[consts.index("block0np%d" % d)] = str(n if d == 0 else (n // 2 if w.plan.ndim == 2 else n))
     w.substitute_simulation_parameters(consts, vals)
     with open(os.path.join(out, "plan.json"), "w") as f:
         f.write(w.plan.to_json())
-    np.save(os.path.join(out, "ic.npy"), w.initial_state())
+    if w.plan.ndim == 2:
+        f = w.initial_fields(halo=4)
+        np.save(os.path.join(out, "ic.npy"), np.stack([f[v] for v in w.state_names()]))
+        np.save(os.path.join(out, "x1.npy"), f["x1"])
+    else:
+        np.save(os.path.join(out, "ic.npy"), w.initial_state())
     with open(os.path.join(out, "constants.json"), "w") as f:
         json.dump({"constants": consts, "values": vals}, f)
     return w.plan

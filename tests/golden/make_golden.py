@@ -35,7 +35,50 @@ CASES = {
 }
 
 
+# 2D case: grid (n0, n1), steps, overrides.  The fixture keeps the reference's initial state and
+# final state with a 4-point halo (its initialisation kernel fills halos that the inlet reads) and
+# the x1 coordinate the metrics are computed from.
+CASES_2D = {
+    "katzer_teno": ((64, 32), 20, {"dt": 0.01}),
+}
+VARS_2D = ["rho", "rhou0", "rhou1", "rhoE"]
+
+
+def padded4(d, names):
+    # dumps carry a 5-point halo; keep 4
+    return {v: refrun.load_dump(os.path.join(d, "opensbli_output.%s_B0.bin" % v), interior=False)[1:-1, 1:-1]
+            for v in names}
+
+
+def main2d(ref):
+    import tempfile
+    for case, ((n0, n1), steps, extra) in CASES_2D.items():
+        if not refrun.available(case):
+            subprocess.check_call([sys.executable, os.path.join(REPO, "oracle", "gen", "generate.py"), "--case", case,
+                                   "--ref", ref])
+        base = dict(block0np0=n0, block0np1=n1)
+        base.update(extra)
+        d0 = tempfile.mkdtemp(prefix="osb_g0_")
+        refrun.run(case, dict(base, niter=0), VARS_2D + ["x1"], threads=4, outdir=d0)
+        ic = padded4(d0, VARS_2D + ["x1"])
+        d1 = tempfile.mkdtemp(prefix="osb_g1_")
+        refrun.run(case, dict(base, niter=steps), VARS_2D, threads=4, outdir=d1)
+        fin = padded4(d1, VARS_2D)
+        np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % case), q0=np.stack([ic[v] for v in VARS_2D]),
+                            x1=ic["x1"], q=np.stack([fin[v] for v in VARS_2D]), n=np.array([n0, n1]), steps=steps,
+                            params=json.dumps(dict(base, niter=steps)))
+        out = os.path.join("/tmp", "osb_lower_%s" % case)
+        subprocess.check_call([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case,
+                               "--out", out, "--ref", ref], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        with open(os.path.join(out, "plan.json")) as f:
+            plan = json.load(f)
+        with open(os.path.join(HERE, "plan_%s.json" % case), "w") as f:
+            json.dump(plan, f, indent=1)
+        print("wrote", case, fin["rho"].shape)
+
+
 def main(ref="/root/reference"):
+    main2d(ref)
     for case, (n, steps, extra) in CASES.items():
         if not refrun.available(case):
             subprocess.check_call([sys.executable, os.path.join(REPO, "oracle", "gen", "generate.py"), "--case", case,

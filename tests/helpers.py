@@ -50,3 +50,31 @@ def rel_l2(a, b):
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
     return [float(np.linalg.norm(a[v] - b[v]) / max(np.linalg.norm(b[v]), 1e-300)) for v in range(b.shape[0])]
+
+
+def load_golden_2d(case="katzer_teno"):
+    d = np.load(os.path.join(GOLDEN, "ref_%s.npz" % case))
+    return d["q0"], d["x1"], d["q"], tuple(int(v) for v in d["n"]), int(d["steps"]), json.loads(str(d["params"]))
+
+
+def golden_plan_2d(case="katzer_teno", n=None, **kw):
+    with open(os.path.join(GOLDEN, "plan_%s.json" % case)) as f:
+        p = Plan.from_json(f.read())
+    if n is not None:
+        n0, n1 = n
+        p = p.replace(n=(n0, n1, 1), delta=(400.0 / (n0 - 1), 115.0 / (n1 - 1), 1.0))
+    return p.replace(**kw) if kw else p
+
+
+def widen_2d(q_pad, n0_new):
+    """A padded 2D state whose rows depend on x1 only, widened to n0_new interior columns by repeating
+    its first interior column (the Katzer initial state is independent of x0)."""
+    h = 4
+    col = q_pad[..., :, h:h + 1]
+    return np.repeat(col, n0_new + 2 * h, axis=-1)
+
+
+def rel_err_2d(a, b, h=4):
+    """max-normalised error over the interior of padded 2D states."""
+    sl = (slice(h, -h), slice(h, -h))
+    return [float(np.abs(a[v][sl] - b[v][sl]).max() / np.abs(b[v][sl]).max()) for v in range(b.shape[0])]

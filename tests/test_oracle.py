@@ -59,3 +59,32 @@ def test_oracle_matches_reference_run(case, n, steps, extra):
     cfg = oracle_cfg(plan, dt=extra["dt"])
     q = O.run(cfg, O.tgv_init(cfg), steps)
     assert max(rel_err(q, q_ref)) < 1e-12
+
+
+def test_oracle_2d_matches_reference_golden():
+    from helpers import load_golden_2d, golden_plan_2d, rel_err_2d
+    q0, x1, q_ref, n, steps, params = load_golden_2d()
+    plan = golden_plan_2d(n=n).replace(dt=params["dt"])
+    q = O.run2d(plan, q0, steps)
+    assert max(rel_err_2d(q, q_ref)) < 1e-12
+    # halos too (the outlet and wall faces write them)
+    assert float(np.abs(q - q_ref).max()) < 1e-10
+
+
+def test_oracle_2d_metrics_match_reference_coordinates():
+    from helpers import load_golden_2d, golden_plan_2d
+    q0, x1, q_ref, n, steps, params = load_golden_2d()
+    plan = golden_plan_2d(n=n)
+    D, S = O.metrics2d(plan)
+    # D11 = 1/(dx1/dxi1): compare with a second-order estimate from the reference's own x1
+    dx = np.gradient(x1[4:-4, 4], plan.delta[1])
+    assert np.allclose(D[2:-2, 0], 1.0 / dx[2:-2], rtol=5e-2)
+    assert np.all(D > 0) and np.all(np.isfinite(S))
+
+
+def test_ls_rk3_coefficients_match_the_lowered_plan():
+    from opensbli_gb300.plan import ls_rk3_ssp_coefficients
+    from helpers import golden_plan_2d
+    A, B = ls_rk3_ssp_coefficients()
+    p = golden_plan_2d()
+    assert np.allclose(A, p.rk_a, rtol=0, atol=1e-15) and np.allclose(B, p.rk_b, rtol=1e-15)

@@ -43,6 +43,17 @@ def test_value_expressions():
         _eval_c_expr("__import__('os')", env)
 
 
+def test_katzer_plan_matches_lowered_script():
+    from opensbli_gb300.plan import katzer_plan
+    k = katzer_plan()
+    g = golden_plan("katzer_teno")
+    for f in ("ndim", "n", "conv", "visc", "rk", "bc", "gama", "Minf", "Re", "Pr", "Twall", "SuthT", "RefT", "teno_eps",
+              "teno_ct", "dirichlet_lo", "dirichlet_hi", "dirichlet_x_switch", "Lx1", "by"):
+        assert getattr(k, f) == getattr(g, f), f
+    assert np.allclose(k.rk_a, g.rk_a, atol=1e-15) and np.allclose(k.rk_b, g.rk_b, rtol=1e-15)
+    assert np.allclose(k.delta[:2], g.delta[:2], rtol=1e-15)
+
+
 def test_cfl_dt_tgv_weno():
     p = tgv_plan(256, conv="weno5js", Minf=1.25)
     dt = tgv_cfl_dt(p)
@@ -50,7 +61,7 @@ def test_cfl_dt_tgv_weno():
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
-@pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgsym_central"])
+@pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgsym_central", "katzer_teno"])
 def test_writer_lowers_reference_script(case, tmp_path):
     r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case, "--out",
                         str(tmp_path), "--ref", REF], capture_output=True, text=True, timeout=900)
@@ -60,5 +71,8 @@ def test_writer_lowers_reference_script(case, tmp_path):
     assert p.replace(kernels=[]) == g.replace(kernels=[])
     assert sorted(p.kernels) == sorted(g.kernels)
     ic = np.load(tmp_path / "ic.npy")
-    assert ic.shape == (5,) + tuple(reversed(p.n))
+    if p.ndim == 2:
+        assert ic.shape == (4, p.n[1] + 8, p.n[0] + 8)  # 4-point halo: the initialisation kernel fills halos
+    else:
+        assert ic.shape == (5,) + tuple(reversed(p.n))
     assert np.isfinite(ic).all()
