@@ -118,21 +118,19 @@ def max_over_ranks(x, world):
 # ------------------------------------------------------------------------------------------------
 # reference arm
 # ------------------------------------------------------------------------------------------------
-def reference_cpu(n, steps, warmup, dt, Minf, threads=None, allow_port=True):
-    """Time the reference's generated C for the WENO TGV (or, if its generated sources are absent,
+def reference_cpu(wl, steps, warmup, threads=None, allow_port=True):
+    """Time the reference generator's C for the workload (or, if its generated sources are absent,
     the oracle's C restatement) on the host cores.  Returns a dict with cell-updates/s."""
     from oracle import refrun
     threads = threads or os.cpu_count()
-    case = "tgv_weno"
+    case = wl.cpu_case
     if refrun.available(case):
-        refrun.build(case)
-        params = dict(block0np0=n, block0np1=n, block0np2=n, dt=dt, Minf=Minf)
         import tempfile
+        exe = refrun.build(case)
         tmp = tempfile.mkdtemp(prefix="osb_bench_ref_")
         env = dict(os.environ, OMP_NUM_THREADS=str(threads))
-        for k, v in params.items():
+        for k, v in wl.cpu_params.items():
             env["OSB_" + k] = repr(v) if isinstance(v, float) else str(v)
-        exe = refrun.build(case)
 
         def run(niter):
             env["OSB_niter"] = str(niter)
@@ -147,37 +145,34 @@ def reference_cpu(n, steps, warmup, dt, Minf, threads=None, allow_port=True):
         if warmup > 0:
             run(warmup)
         wall = run(steps)
-        return {"value": n ** 3 * steps / wall, "wall_s": wall, "kind": "reference", "cores": threads,
-                "sample": "reference generator's C for the WENO5-JS TGV (opensbli.cpp from LLFWeno(5,'JS'), "
-                          "compiled with the OPS-API stand-in, OpenMP), %d^3, %d timed RK3 steps after a "
-                          "%d-step warm-up run" % (n, steps, warmup)}
-    if not allow_port:
+        return {"value": wl.cells * steps / wall, "wall_s": wall, "kind": "reference", "cores": threads,
+                "sample": "the reference generator's C for this problem (oracle/_ref/%s: opensbli.cpp and kernels "
+                          "from the reference's OPSC writer, compiled with the OPS-API stand-in and OpenMP), full "
+                          "grid, %d timed RK3 steps after a %d-step warm-up run" % (case, steps, warmup)}
+    if not allow_port or wl.plan.ndim != 3:
         raise RuntimeError("reference sources not present")
     from oracle import oracle as O
-    import math
-    cfg = O.make_cfg((n, n, n), (2 * math.pi / n,) * 3, Minf=Minf, conv="weno5js", dt=dt)
+    p = wl.plan
+    cfg = O.make_cfg(p.n, p.delta, Minf=p.Minf, conv=p.conv, dt=wl.dt)
     q0 = O.tgv_init(cfg)
     t0 = time.perf_counter()
     O.run(cfg, q0, steps)
     wall = time.perf_counter() - t0
-    return {"value": n ** 3 * steps / wall, "wall_s": wall, "kind": "port", "cores": 1,
-            "sample": "oracle C restatement (single thread), %d^3, %d RK3 steps" % (n, steps)}
+    return {"value": wl.cells * steps / wall, "wall_s": wall, "kind": "port", "cores": 1,
+            "sample": "oracle C restatement (single thread), full grid, %d RK3 steps" % steps}
 
 
 def ref_arm(args, world, rank):
     if rank != 0:
         return
-    from opensbli_gb300.plan import tgv_plan, tgv_cfl_dt
-    plan = tgv_plan(args.n, conv="weno5js", Minf=1.25)
-    dt = tgv_cfl_dt(plan)
-    # a bounded sample: the full grid, a few steps (each 256^3 WENO step takes seconds on the host)
+    wl = workload(args.config, args.n)
     steps = max(1, min(args.steps, args.ref_steps))
     warm = max(0, min(args.warmup, 1))
-    r = reference_cpu(args.n, steps, warm, dt, 1.25)
+    r = reference_cpu(wl, steps, warm)
     line = {"metric": METRIC, "value": r["value"], "unit": UNIT, "n_gpus": args.gpus, "steps": steps,
             "warmup": warm, "ms_per_step": 1e3 * r["wall_s"] / steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic: analytic Taylor-Green initial condition",
-            "config": config_block(args.n, dt, "fp64"), "impl": "reference",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic: the problem's analytic initial condition",
+            "config": dict(wl.config, precision="fp64"), "impl": "reference",
             "cpu_baseline": {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": r["kind"],
                              "sample": r["sample"]},
             "e2e": {"value": r["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -192,6 +187,65 @@ def config_block(n, dt, precision):
             "grid": [n, n, n], "dt": dt, "precision": precision,
             "l2": "inputs larger than L2 (state %.0f MB FP32 + %.0f MB FP64 register)" % (
                 5 * n ** 3 * 4 / 1e6, 5 * n ** 3 * 8 / 1e6)}
+
+
+class Workload:
+    """One benchmark configuration: how to build an initialised solver, its size and dt."""
+
+    def __init__(self, name, plan, dt, init, config, cpu_case, cpu_params, alg_bytes):
+        self.name, self.plan, self.dt, self.init = name, plan, dt, init
+        self.config, self.cpu_case, self.cpu_params, self.alg_bytes = config, cpu_case, cpu_params, alg_bytes
+
+    @property
+    def cells(self):
+        return self.plan.cells
+
+    def solver(self, precision):
+        from opensbli_gb300.runtime import Solver
+        s = Solver(self.plan.replace(precision=precision))
+        self.init(s)
+        return s
+
+
+def workload(name, n=None):
+    import numpy as np
+    from opensbli_gb300.plan import tgv_plan, tgv_cfl_dt, katzer_plan
+    if name == "tgv_weno256":
+        n = n or 256
+        plan = tgv_plan(n, conv="weno5js", Minf=1.25)
+        dt = tgv_cfl_dt(plan)
+        return Workload(name, plan, dt, lambda s: s.init_tgv(), config_block(n, dt, "mixed"), "tgv_weno",
+                        dict(block0np0=n, block0np1=n, block0np2=n, dt=dt, Minf=1.25),
+                        {"mixed": 5 * (2 * 4 + 2 * 8), "fp64": 5 * (2 * 8 + 2 * 8)})
+    if name == "tgv_central64":
+        n = n or 64
+        plan = tgv_plan(n, conv="central_skew", Minf=0.1)
+        dt = 5e-3
+        cfg = {"workload": "Taylor-Green vortex %d^3 on [0,2pi)^3, 4th-order central skew-symmetric convective and "
+                           "viscous terms, RK3 (2-register), Minf=0.1, Re=1600, Pr=0.71, dt=5e-3" % n,
+               "grid": [n, n, n], "dt": dt, "precision": "fp64",
+               "l2": "inputs smaller than L2 (%.0f MB state); a step reads and writes every array" % (5 * n ** 3 * 8 / 1e6)}
+        return Workload(name, plan, dt, lambda s: s.init_tgv(), cfg, "tgv_central",
+                        dict(block0np0=n, block0np1=n, block0np2=n, dt=dt, Minf=0.1),
+                        {"mixed": 5 * (2 * 4 + 2 * 8), "fp64": 5 * (2 * 8 + 2 * 8)})
+    if name == "katzer512":
+        n0, n1 = (n or 512), 256
+        plan = katzer_plan(n0, n1, dt=0.04)
+        d = np.load(os.path.join(REPO, "tests", "golden", "katzer_ic_n%d.npz" % n1))
+        q = np.repeat(d["q_col"][:, :, None], n0 + 8, axis=2)
+        x1 = np.repeat(d["x1_col"][:, None], n0 + 8, axis=1)
+
+        def init(s):
+            s.set_coordinate(x1, 4)
+            s.set_state64_padded(q, 4)
+        cfg = {"workload": "2D shock/boundary-layer interaction %dx%d (Katzer): TENO5 (C_T=1e-5, eps=1e-15), "
+                           "metrics stretched in x1 (sinh, factor 5), Sutherland viscosity, isothermal wall "
+                           "Tw=1.676, shock-generator top face, LS-RK3 SSP, Mach 2, Re=950, dt=0.04" % (n0, n1),
+               "grid": [n0, n1], "dt": 0.04, "precision": "mixed",
+               "l2": "inputs smaller than L2 (%.0f MB state)" % (4 * n0 * n1 * 8 / 1e6)}
+        return Workload(name, plan, 0.04, init, cfg, "katzer_teno", dict(block0np0=n0, block0np1=n1, dt=0.04),
+                        {"mixed": 4 * (2 * 4 + 2 * 8) + 4, "fp64": 4 * (2 * 8 + 2 * 8) + 8})
+    raise SystemExit("unknown config %s" % name)
 
 
 # ------------------------------------------------------------------------------------------------
@@ -210,21 +264,17 @@ def time_steps(solver, steps, dt, torch):
 
 
 def own_arm(args, world, rank, local):
-    import numpy as np
     import torch
-    from opensbli_gb300.plan import tgv_plan, tgv_cfl_dt
-    from opensbli_gb300.runtime import Solver
 
     torch.cuda.set_device(local)
-    n = args.n
-    plan = tgv_plan(n, conv="weno5js", Minf=1.25, precision="mixed")
-    dt = tgv_cfl_dt(plan)
-    cells = n ** 3
+    wl = workload(args.config, args.n)
+    dt, cells = wl.dt, wl.cells
     K, W = args.steps, args.warmup
+    head = "mixed" if wl.config["precision"] == "mixed" else "fp64"
+    other = "fp64" if head == "mixed" else "mixed"
 
-    # ---- mixed path: device-resident timing
-    s = Solver(plan)
-    s.init_tgv()
+    # ---- headline precision: device-resident timing
+    s = wl.solver(head)
     s.step(W, dt)
     barrier(world)
     with ClockSampler(local) as clk:
@@ -232,17 +282,19 @@ def own_arm(args, world, rank, local):
     launches = s.launch_count()
     t = max_over_ranks(t, world)
     value = world * cells * K / t
-    q_mixed = s.state64()
+    q_head = s.state64()
 
     # ---- per-kernel-family timing (eager launches bracketed by CUDA events on the solver stream)
+    steps_prof = max(2, min(K, 5))
     s.profile(True)
-    s.step(max(2, min(K, 5)), dt)
+    s.step(steps_prof, dt)
     torch.cuda.synchronize()
     prof = s.profile_read()
     s.profile(False)
 
     # ---- e2e through the public API: pinned host state in, host state out, every step
-    s.init_tgv()
+    s.close()
+    s = wl.solver(head)
     host_in = s.state64().cpu().pin_memory()
     host_out = torch.empty_like(host_in).pin_memory()
     e2e_steps = max(1, min(K, 5))
@@ -256,70 +308,78 @@ def own_arm(args, world, rank, local):
         torch.cuda.synchronize()
     t_e2e = max_over_ranks(time.perf_counter() - t0, world)
     e2e_value = world * cells * e2e_steps / t_e2e
-    bytes_io = 5 * cells * 8
+    bytes_io = host_in.numel() * 8
     s.close()
     del s
 
-    # ---- FP64 path on the same workload and error of the mixed run against it
-    K64 = max(1, min(K, args.fp64_steps))
-    s64 = Solver(plan.replace(precision="fp64"))
-    s64.init_tgv()
-    s64.step(min(W, 1), dt)
-    t64 = time_steps(s64, K64, dt, torch)
-    # FP64 reference state after W+K steps for the error of the mixed run
-    s64.init_tgv()
-    s64.step(W + K, dt)
-    q64 = s64.state64()
-    s64.close()
-    del s64
-    diff = (q_mixed - q64)
-    l2 = [float(torch.linalg.vector_norm(diff[v]) / torch.linalg.vector_norm(q64[v])) for v in range(5)]
-    linf = [float(diff[v].abs().max() / q64[v].abs().max()) for v in range(5)]
+    # ---- the other precision on the same workload; error of the mixed run against the FP64 run
+    K2 = max(1, min(K, args.fp64_steps if other == "fp64" else K))
+    s2 = wl.solver(other)
+    s2.step(min(W, 1), dt)
+    t2 = time_steps(s2, K2, dt, torch)
+    s2.close()
+    s2 = wl.solver(other)
+    s2.step(W + K, dt)
+    q_other = s2.state64()
+    s2.close()
+    del s2
+    q_mixed, q64 = (q_head, q_other) if head == "mixed" else (q_other, q_head)
+    diff = q_mixed - q64
+    nv = q64.shape[0]
+    l2 = [float(torch.linalg.vector_norm(diff[v]) / torch.linalg.vector_norm(q64[v])) for v in range(nv)]
+    linf = [float(diff[v].abs().max() / q64[v].abs().max()) for v in range(nv)]
 
-    # ---- roofline of the whole RK3 step and of the dominant kernel family
+    # ---- roofline: the whole RK3 step and the dominant kernel family
     peak, peak_kind = load_peaks()
     t_step = t / K
-    achieved_step = cells * 3 * ALG_BYTES_STAGE["mixed"] / t_step / 1e9
-    fam_bytes = {"weno_x": 5 * 4 * 2, "weno_y": 5 * 4 * 3, "weno_z": 5 * 4 * 3, "central_rk": 5 * (4 + 4 + 8 + 8 + 4),
-                 "halo": 0}
-    dom = max((f for f in prof if f in fam_bytes and fam_bytes[f] > 0), key=lambda f: prof[f][0], default=None)
+    bstage = wl.alg_bytes[head]
+    achieved_step = cells * 3 * bstage / t_step / 1e9
+    if wl.plan.ndim == 3:
+        e = 4 if head == "mixed" else 8
+        fam_bytes = {"weno_x": 5 * e * 2, "weno_y": 5 * e * 3, "weno_z": 5 * e * 3,
+                     "central_rk": 5 * (e + e + 8 + 8 + e) if wl.plan.conv == "weno5js" else 5 * (e + 8 + 8 + e),
+                     "halo": 0}
+    else:
+        e = 4 if head == "mixed" else 8
+        fam_bytes = {"central_rk": 4 * (e + 8 + 8 + 8 + 8) + 8 * 2, "halo": 0}
+    dom = max((f for f in prof if fam_bytes.get(f, 0) > 0), key=lambda f: prof[f][0], default=None)
     roof = None
     if dom:
         ms, cnt = prof[dom]
         per_launch = ms / cnt / 1e3
         ach = cells * fam_bytes[dom] / per_launch / 1e9
-        roof = {"bound": "hbm", "kernel": "k_weno<float,%d>" % "xyz".index(dom[-1]) if dom.startswith("weno") else dom,
-                "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak, "peak_kind": peak_kind,
-                "traffic": None, "alg_bytes_per_cell": fam_bytes[dom],
+        roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "peak_kind": peak_kind, "traffic": None, "alg_bytes_per_cell": fam_bytes[dom],
                 "avg_launch_ms": per_launch * 1e3,
                 "step": {"achieved": achieved_step, "frac": achieved_step / peak,
-                         "alg_bytes_per_cell_per_stage": ALG_BYTES_STAGE["mixed"]}}
-        steps_prof = max(2, min(K, 5))
-        roof["families_ms_per_step"] = {f: prof[f][0] / steps_prof for f in prof}
+                         "alg_bytes_per_cell_per_stage": bstage},
+                "families_ms_per_step": {f: prof[f][0] / steps_prof for f in prof}}
 
     # ---- CPU baseline (rank 0, N=1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         try:
-            r = reference_cpu(n, args.ref_steps, 0, dt, 1.25)
+            r = reference_cpu(wl, args.ref_steps, 0)
             cpu = {"value": r["value"], "unit": UNIT, "cores": r["cores"], "kind": r["kind"], "sample": r["sample"]}
-        except Exception as e:
-            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "unavailable", "sample": str(e)[:200]}
+        except Exception as ex:
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "unavailable", "sample": str(ex)[:200]}
 
     if rank == 0:
+        vars_ = ["rho", "rhou0", "rhou1", "rhou2", "rhoE"] if nv == 5 else ["rho", "rhou0", "rhou1", "rhoE"]
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
                 "ms_per_step": 1e3 * t / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f32 (RK accumulator f64)", "data": "synthetic: analytic Taylor-Green initial condition",
-                "config": dict(config_block(n, dt, "mixed"), parallelism="replicas" if world > 1 else "single"),
+                "dtype": "f32 (RK accumulator f64)" if head == "mixed" else "f64",
+                "data": "synthetic: the problem's analytic initial condition",
+                "config": dict(wl.config, parallelism="replicas" if world > 1 else "single"),
                 "roofline": roof, "cpu_baseline": cpu,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": bytes_io,
                         "d2h_bytes_per_step": bytes_io, "steps": e2e_steps,
                         "path": "Solver.set_state64 (pinned host -> device) + Solver.step(1) + state64 -> pinned host"},
                 "gpu_launches": launches, "clocks": clk.summary(),
-                "fp64": {"value": world * cells * K64 / t64, "ms_per_step": 1e3 * t64 / K64, "steps": K64,
-                         "mixed_speedup": (value / world) / (cells * K64 / t64)},
-                "error_vs_fp64": {"steps": W + K, "l2": l2, "linf": linf,
-                                  "vars": ["rho", "rhou0", "rhou1", "rhou2", "rhoE"]}}
+                other: {"value": world * cells * K2 / t2, "ms_per_step": 1e3 * t2 / K2, "steps": K2},
+                "mixed_vs_fp64_speedup": ((value / world) / (cells * K2 / t2)) if head == "mixed" else
+                ((cells * K2 / t2) / (value / world)),
+                "error_vs_fp64": {"steps": W + K, "l2": l2, "linf": linf, "vars": vars_}}
         print(json.dumps(line), flush=True)
 
 
@@ -329,11 +389,15 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
-    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--config", default="tgv_weno256", choices=["tgv_weno256", "tgv_central64", "katzer512"])
+    ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--fp64-steps", type=int, default=3)
-    ap.add_argument("--ref-steps", type=int, default=2)
+    ap.add_argument("--ref-steps", type=int, default=None,
+                    help="timed steps of the host-core reference sample (default: 2 at 256^3, 40 otherwise)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
+    if args.ref_steps is None:
+        args.ref_steps = 2 if args.config == "tgv_weno256" else 40
     world, rank, local = dist_init()
     if args.impl == "reference":
         ref_arm(args, world, rank)

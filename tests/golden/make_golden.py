@@ -79,6 +79,7 @@ def main2d(ref):
 
 def main(ref="/root/reference"):
     main2d(ref)
+    katzer_profile(ref)
     for case, (n, steps, extra) in CASES.items():
         if not refrun.available(case):
             subprocess.check_call([sys.executable, os.path.join(REPO, "oracle", "gen", "generate.py"), "--case", case,
@@ -97,6 +98,21 @@ def main(ref="/root/reference"):
         with open(os.path.join(HERE, "plan_%s.json" % case), "w") as f:
             json.dump(plan, f, indent=1)
         print("wrote", case, q.shape)
+
+
+def katzer_profile(ref="/root/reference", n1=256, n0=512):
+    """The reference's Katzer initial state on n1 = 256 rows (it is independent of x0): one padded
+    column of rho, rhou0, rhou1, rhoE and x1 with a 4-point halo, for the 512 x 256 benchmark."""
+    import tempfile
+    case = "katzer_teno"
+    if not refrun.available(case):
+        subprocess.check_call([sys.executable, os.path.join(REPO, "oracle", "gen", "generate.py"), "--case", case,
+                               "--ref", ref])
+    d = tempfile.mkdtemp(prefix="osb_kic_")
+    refrun.run(case, dict(block0np0=n0, block0np1=n1, niter=0), VARS_2D + ["x1"], threads=8, outdir=d)
+    p = padded4(d, VARS_2D + ["x1"])
+    np.savez_compressed(os.path.join(HERE, "katzer_ic_n%d.npz" % n1),
+                        q_col=np.stack([p[v][:, 4] for v in VARS_2D]), x1_col=p["x1"][:, 4], n1=n1)
 
 
 if __name__ == "__main__":
