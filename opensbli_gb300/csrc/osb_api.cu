@@ -561,6 +561,17 @@ int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
   c->ph.Pr = plan->Pr;
   for (int d = 0; d < 3; ++d) c->ph.inv_delta[d] = 1.0 / plan->delta[d];
   c->ph.weno_eps = plan->weno_eps > 0 ? plan->weno_eps : 1e-6;
+  c->ph.gm1 = plan->gama - 1.0;
+  c->ph.gM2 = plan->Minf * plan->Minf * plan->gama;
+  c->ph.invRe = 1.0 / plan->Re;
+  c->ph.kT = 1.0 / ((plan->gama - 1.0) * plan->Minf * plan->Minf * plan->Pr * plan->Re);
+  c->ph.f_gama = (float)c->ph.gama;
+  c->ph.f_gm1 = (float)c->ph.gm1;
+  c->ph.f_gM2 = (float)c->ph.gM2;
+  c->ph.f_invRe = (float)c->ph.invRe;
+  c->ph.f_kT = (float)c->ph.kT;
+  c->ph.f_eps = (float)c->ph.weno_eps;
+  for (int d = 0; d < 3; ++d) c->ph.f_inv_delta[d] = (float)c->ph.inv_delta[d];
   const size_t bytes = (size_t)c->g.numel * c->elem;
   cudaError_t e = cudaSuccess;
   if (plan->ndim == 2) {

@@ -48,43 +48,82 @@ __global__ void __launch_bounds__(256) k_central_rk(Grid g, Fields5<const T> q, 
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * zchunk;
   const int k1 = min(k0 + zchunk, g.n2);
-  const T gm1 = T(ph.gama - 1.0);
-  const T gM2 = T(ph.Minf * ph.Minf * ph.gama);
+  const T gm1 = pick<T>(ph.gm1, ph.f_gm1);
+  const T gM2 = pick<T>(ph.gM2, ph.f_gM2);
 
   auto slot = [](int k) { return ((k % NP) + NP) % NP; };
-  auto load_plane = [&](int k) {
-    const int sl = slot(k);
-    for (int e = tid; e < PX * PY; e += TX * TY) {
+  // Plane loads are software-pipelined: the global loads of plane k+3 are issued into registers
+  // before the stencil work on plane k and written (as primitives) into the ring after it.
+  constexpr int PPT = (PX * PY + TX * TY - 1) / (TX * TY);  // points per thread per plane
+  T pre[PPT][5];
+  auto fetch = [&](int k) {
+#pragma unroll
+    for (int r = 0; r < PPT; ++r) {
+      const int e = tid + r * TX * TY;
       const int px = e % PX, py = e / PX;
       const int i = i0 - 2 + px, j = j0 - 2 + py;
-      if (i >= g.n0 + 2 || j >= g.n1 + 2) continue;
-      const int64_t n = gidx(g, i, j, k);
-      const T rho = q.v[0][n];
-      const T irho = T(1) / rho;
-      const T u0 = q.v[1][n] * irho, u1 = q.v[2][n] * irho, u2 = q.v[3][n] * irho;
-      const T E = q.v[4][n];
-      const T half = T(0.5);
-      const T p = gm1 * (E - half * rho * u0 * u0 - half * rho * u1 * u1 - half * rho * u2 * u2);
-      sm.s[sl][F_RHO][py][px] = rho;
-      sm.s[sl][F_U0][py][px] = u0;
-      sm.s[sl][F_U1][py][px] = u1;
-      sm.s[sl][F_U2][py][px] = u2;
-      sm.s[sl][F_P][py][px] = p;
-      sm.s[sl][F_T][py][px] = gM2 * p * irho;
-      sm.s[sl][F_E][py][px] = E;
+      if (e < PX * PY && i < g.n0 + 2 && j < g.n1 + 2 && k < g.n2 + 2) {
+        const int64_t n = gidx(g, i, j, k);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) pre[r][v] = q.v[v][n];
+      }
+    }
+  };
+  auto store = [&](int k) {
+    const int sl = slot(k);
+#pragma unroll
+    for (int r = 0; r < PPT; ++r) {
+      const int e = tid + r * TX * TY;
+      const int px = e % PX, py = e / PX;
+      const int i = i0 - 2 + px, j = j0 - 2 + py;
+      if (e < PX * PY && i < g.n0 + 2 && j < g.n1 + 2 && k < g.n2 + 2) {
+        const T rho = pre[r][0];
+        const T irho = T(1) / rho;
+        const T u0 = pre[r][1] * irho, u1 = pre[r][2] * irho, u2 = pre[r][3] * irho;
+        const T E = pre[r][4];
+        const T half = T(0.5);
+        const T p = gm1 * (E - half * rho * u0 * u0 - half * rho * u1 * u1 - half * rho * u2 * u2);
+        sm.s[sl][F_RHO][py][px] = rho;
+        sm.s[sl][F_U0][py][px] = u0;
+        sm.s[sl][F_U1][py][px] = u1;
+        sm.s[sl][F_U2][py][px] = u2;
+        sm.s[sl][F_P][py][px] = p;
+        sm.s[sl][F_T][py][px] = gM2 * p * irho;
+        sm.s[sl][F_E][py][px] = E;
+      }
     }
   };
 
   const T c1[5] = {T(1.0 / 12.0), T(-2.0 / 3.0), T(0), T(2.0 / 3.0), T(-1.0 / 12.0)};
   const T c2[5] = {T(-1.0 / 12.0), T(4.0 / 3.0), T(-2.5), T(4.0 / 3.0), T(-1.0 / 12.0)};
-  const T idl[3] = {T(ph.inv_delta[0]), T(ph.inv_delta[1]), T(ph.inv_delta[2])};
+  const T idl[3] = {pick<T>(ph.inv_delta[0], ph.f_inv_delta[0]), pick<T>(ph.inv_delta[1], ph.f_inv_delta[1]),
+                    pick<T>(ph.inv_delta[2], ph.f_inv_delta[2])};
 
-  for (int k = k0 - 2; k < k0 + 2; ++k) load_plane(k);
+  for (int k = k0 - 2; k < k0 + 3; ++k) {
+    fetch(k);
+    store(k);
+  }
   for (int k = k0; k < k1; ++k) {
-    load_plane(k + 2);
     __syncthreads();
+    if (k + 3 < k1 + 2) fetch(k + 3);
     const int i = i0 + tx, j = j0 + ty;
-    if (i < g.n0 && j < g.n1) {
+    const bool active = i < g.n0 && j < g.n1;
+    // the residual already in rin and the FP64 register at the output point, loaded early
+    T rpre[5];
+    double opre[5];
+    int64_t nout = 0;
+    if (active) {
+      nout = gidx(g, i, j, k);
+      if (MODE & CRK_RIN) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) rpre[v] = rin.v[v][nout];
+      }
+      if (MODE & CRK_UPDATE) {
+#pragma unroll
+        for (int v = 0; v < 5; ++v) opre[v] = qold.v[v][nout];
+      }
+    }
+    if (active) {
       // field f at offset (dz, dy, dx) from the output point
       auto S = [&](int f, int dz, int dy, int dx) -> T { return sm.s[slot(k + dz)][f][ty + 2 + dy][tx + 2 + dx]; };
       auto SA = [&](int f, int axis, int o) -> T {
@@ -139,8 +178,8 @@ __global__ void __launch_bounds__(256) k_central_rk(Grid g, Fields5<const T> q, 
       }
 
       if (MODE & CRK_VISC) {
-        const T invRe = T(1.0 / ph.Re);
-        const T kT = T(1.0 / ((ph.gama - 1.0) * ph.Minf * ph.Minf * ph.Pr * ph.Re));
+        const T invRe = pick<T>(ph.invRe, ph.f_invRe);
+        const T kT = pick<T>(ph.kT, ph.f_kT);
         // own-axis second derivatives of u_c and T
         T d2u[3][3], lapT = T(0);
 #pragma unroll
@@ -201,18 +240,25 @@ __global__ void __launch_bounds__(256) k_central_rk(Grid g, Fields5<const T> q, 
         R[4] += e;
       }
 
-      const int64_t n = gidx(g, i, j, k);
+      const int64_t n = nout;
       if (MODE & CRK_RIN) {
 #pragma unroll
-        for (int v = 0; v < 5; ++v) R[v] += rin.v[v][n];
+        for (int v = 0; v < 5; ++v) R[v] += rpre[v];
       }
       if (MODE & CRK_UPDATE) {
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
-          const double o = qold.v[v][n];
+          const double o = opre[v];
           const double r = (double)R[v];
-          qnew.v[v][n] = (T)(dt_new * r + o);
-          qold.v[v][n] = dt_old * r + o;
+          const double o2 = dt_old * r + o;
+          qold.v[v][n] = o2;
+          if (sizeof(T) == 8) {
+            qnew.v[v][n] = (T)(dt_new * r + o);
+          } else {
+            // FP32 state: the stage value q = qold + dt_new R equals qold' + (dt_new - dt_old) R;
+            // rounding qold' and adding the small FP32 correction keeps FP64 work to one FMA per var
+            qnew.v[v][n] = (T)o2 + (T)(dt_new - dt_old) * R[v];
+          }
         }
       } else {
 #pragma unroll
@@ -220,6 +266,7 @@ __global__ void __launch_bounds__(256) k_central_rk(Grid g, Fields5<const T> q, 
       }
     }
     __syncthreads();
+    if (k + 3 < k1 + 2) store(k + 3);
   }
 }
 

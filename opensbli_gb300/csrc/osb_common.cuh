@@ -31,7 +31,16 @@ struct Phys {
   double gama, Minf, Re, Pr;
   double inv_delta[3];
   double weno_eps;
+  // derived constants, filled on the host in both precisions so kernels do no FP64 set-up work:
+  // gama-1, gama*Minf^2, 1/Re, kT = 1/((gama-1) Minf^2 Pr Re)
+  double gm1, gM2, invRe, kT;
+  float f_gama, f_gm1, f_gM2, f_invRe, f_kT, f_eps, f_inv_delta[3];
 };
+
+// the FP64 or FP32 copy of a plan constant
+template <typename T> __host__ __device__ __forceinline__ T pick(double d, float f);
+template <> __host__ __device__ __forceinline__ double pick<double>(double d, float) { return d; }
+template <> __host__ __device__ __forceinline__ float pick<float>(double, float f) { return f; }
 
 template <typename T> __device__ __forceinline__ T sqrt_t(T x);
 template <> __device__ __forceinline__ float sqrt_t<float>(float x) { return sqrtf(x); }

@@ -216,8 +216,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
   T *sflux = sf + W_NF * NPT * TA;           // [5][TI][TA] or [5][TA][TI]
   const int tid = threadIdx.x;
   const int n[3] = {g.n0, g.n1, g.n2};
-  const T gm1 = T(ph.gama - 1.0), gama = T(ph.gama);
-  const T eps = T(ph.weno_eps);
+  const T gm1 = pick<T>(ph.gm1, ph.f_gm1), gama = pick<T>(ph.gama, ph.f_gama);
+  const T eps = pick<T>(ph.weno_eps, ph.f_eps);
 
   // tile origin: first cell whose flux difference this block writes (d0), across-line origin
   int d0, a0, o1, o2;
@@ -248,7 +248,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
     coords(pos, a, i, j, k);
     const int64_t m = gidx(g, i, j, k);
     const T rho = q.v[0][m], r0 = q.v[1][m], r1 = q.v[2][m], r2 = q.v[3][m], E = q.v[4][m];
-    const T u0 = r0 / rho, u1 = r1 / rho, u2 = r2 / rho;
+    const T irho = T(1) / rho;
+    const T u0 = r0 * irho, u1 = r1 * irho, u2 = r2 * irho;
     const T half = T(0.5);
     const T p = gm1 * (E - half * rho * u0 * u0 - half * rho * u1 * u1 - half * rho * u2 * u2);
     sf[sidx(W_RHO, pos, a)] = rho;
@@ -257,7 +258,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
     sf[sidx(W_RU2, pos, a)] = r2;
     sf[sidx(W_E, pos, a)] = E;
     sf[sidx(W_P, pos, a)] = p;
-    sf[sidx(W_A, pos, a)] = sqrt_t(gama * p / rho);
+    sf[sidx(W_A, pos, a)] = sqrt_t(gama * p * irho);
     sf[sidx(W_UD, pos, a)] = DIR == 0 ? u0 : DIR == 1 ? u1 : u2;
   }
   __syncthreads();
@@ -302,7 +303,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
   __syncthreads();
 
   // ---- flux difference for cells d0 .. d0+TI-2
-  const T idd = T(ph.inv_delta[DIR]);
+  const T idd = pick<T>(ph.inv_delta[DIR], ph.f_inv_delta[DIR]);
   for (int t = tid; t < (TI - 1) * TA; t += 256) {
     int m, a;
     if (DIR == 0) { a = t / (TI - 1); m = t % (TI - 1); }
