@@ -201,9 +201,12 @@ class Workload:
         return self.plan.cells
 
     def solver(self, precision):
+        """A solver holding the initial state, its kernel launch shapes autotuned on that state
+        (untimed set-up)."""
         from opensbli_gb300.runtime import Solver
         s = Solver(self.plan.replace(precision=precision))
         self.init(s)
+        s.autotune(reps=3)
         return s
 
 

@@ -161,6 +161,23 @@ int64_t osb_launch_count(osb_ctx *ctx);
 int osb_profile(osb_ctx *ctx, int enable);
 int osb_profile_read(osb_ctx *ctx, double *total_ms, int64_t *counts, int n);
 
+/* Launch shapes of the WENO5-JS flux kernels.  No counterpart in the reference (the generated OPS code
+ * launches every kernel with one fixed block shape).  Direction 0 (x) always runs the tiled kernel;
+ * directions 1 and 2 run tiled or line-marching with 4 or 8 transverse lines per block and `seg`
+ * cells per line segment (4 <= seg <= 4096).  All shapes compute the same interface fluxes.
+ * osb_set_weno_shape / osb_autotune drop captured step graphs (re-captured at the next osb_step).
+ * osb_autotune times every candidate shape of each direction (`reps` launches each, CUDA events on
+ * the context stream, after one warm-up launch) on the bound state, keeps the fastest, and writes
+ * its time per launch in ms to best_ms[dir] when best_ms is not NULL.  It synchronises the stream,
+ * overwrites the residual scratch, and must not be called during stream capture.  On plans without
+ * WENO fluxes it does nothing and returns 0. */
+#define OSB_WENO_TILE 0
+#define OSB_WENO_MARCH4 1
+#define OSB_WENO_MARCH8 2
+int osb_set_weno_shape(osb_ctx *ctx, int dir, int kind, int seg);
+int osb_get_weno_shape(osb_ctx *ctx, int dir, int *kind, int *seg);
+int osb_autotune(osb_ctx *ctx, int reps, double *best_ms);
+
 int osb_get_error(osb_ctx *ctx, char *buf, int n);
 void osb_destroy(osb_ctx *ctx);
 

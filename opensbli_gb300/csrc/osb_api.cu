@@ -562,11 +562,13 @@ int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
   for (int d = 0; d < 3; ++d) c->ph.inv_delta[d] = 1.0 / plan->delta[d];
   c->ph.weno_eps = plan->weno_eps > 0 ? plan->weno_eps : 1e-6;
   c->ph.gm1 = plan->gama - 1.0;
+  c->ph.igm1 = 1.0 / c->ph.gm1;
   c->ph.gM2 = plan->Minf * plan->Minf * plan->gama;
   c->ph.invRe = 1.0 / plan->Re;
   c->ph.kT = 1.0 / ((plan->gama - 1.0) * plan->Minf * plan->Minf * plan->Pr * plan->Re);
   c->ph.f_gama = (float)c->ph.gama;
   c->ph.f_gm1 = (float)c->ph.gm1;
+  c->ph.f_igm1 = (float)c->ph.igm1;
   c->ph.f_gM2 = (float)c->ph.gM2;
   c->ph.f_invRe = (float)c->ph.invRe;
   c->ph.f_kT = (float)c->ph.kT;
@@ -804,6 +806,93 @@ int osb_profile_read(osb_ctx *c, double *total_ms, int64_t *counts, int n) {
     counts[f] = c->prof_n[f];
   }
   return PF_COUNT;
+}
+
+static void drop_graphs(osb_ctx *c) {
+  for (int s = 0; s < 2; ++s)
+    if (c->graph[s]) {
+      cudaGraphExecDestroy(c->graph[s]);
+      c->graph[s] = nullptr;
+    }
+}
+
+int osb_set_weno_shape(osb_ctx *c, int dir, int kind, int seg) {
+  if (!c) return OSB_EINVAL;
+  if (dir < 0 || dir > 2) return set_err(c, OSB_EINVAL, "osb_set_weno_shape: dir must be 0, 1 or 2");
+  if (kind != OSB_WENO_TILE && kind != OSB_WENO_MARCH4 && kind != OSB_WENO_MARCH8)
+    return set_err(c, OSB_EINVAL, "osb_set_weno_shape: unknown kind");
+  if (dir == 0 && kind != OSB_WENO_TILE)
+    return set_err(c, OSB_EUNSUPPORTED, "osb_set_weno_shape: the x direction runs the tiled kernel only");
+  if (seg < 4 || seg > 4096) return set_err(c, OSB_EINVAL, "osb_set_weno_shape: seg must lie in [4, 4096]");
+  c->wcfg[dir] = WenoCfg{kind, seg};
+  drop_graphs(c);
+  return OSB_OK;
+}
+
+int osb_get_weno_shape(osb_ctx *c, int dir, int *kind, int *seg) {
+  if (!c || dir < 0 || dir > 2 || !kind || !seg) return OSB_EINVAL;
+  *kind = c->wcfg[dir].kind;
+  *seg = c->wcfg[dir].seg;
+  return OSB_OK;
+}
+
+}  // extern "C"
+
+template <typename T> static int autotune_impl(osb_ctx *c, int reps, double *best_ms) {
+  cudaStream_t s = c->stream;
+  void **qs = c->cur == 0 ? c->qa : c->qb;
+  Fields5<const T> qc = fields<const T>(qs);
+  Fields5<T> r = fields<T>(c->res);
+  launch_halos<T>(*c, fields<T>(qs), s, &c->launches);
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  const int n[3] = {c->g.n0, c->g.n1, c->g.n2};
+  cudaError_t err = cudaSuccess;
+  for (int d = 0; d < 3 && err == cudaSuccess; ++d) {
+    std::vector<WenoCfg> cand{{WENO_TILE, 32}};
+    if (d > 0) {
+      for (int kind : {WENO_MARCH4, WENO_MARCH8}) {
+        for (int seg : {16, 24, 32, 48, 64, 96, 128, 192, 256})
+          if (seg < n[d]) cand.push_back({kind, seg});
+        cand.push_back({kind, n[d]});
+      }
+    }
+    float best = 1e30f;
+    WenoCfg pick_cfg = c->wcfg[d];
+    for (const WenoCfg &w : cand) {
+      launch_weno_cfg<T>(*c, qc, r, d, w, s);
+      cudaEventRecord(e0, s);
+      for (int k = 0; k < reps; ++k) launch_weno_cfg<T>(*c, qc, r, d, w, s);
+      cudaEventRecord(e1, s);
+      err = cudaEventSynchronize(e1);
+      if (err == cudaSuccess) err = cudaGetLastError();
+      if (err != cudaSuccess) break;
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) {
+        best = ms;
+        pick_cfg = w;
+      }
+    }
+    c->wcfg[d] = pick_cfg;
+    if (best_ms) best_ms[d] = best / reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  drop_graphs(c);
+  return cuda_err(c, err, "osb_autotune");
+}
+
+extern "C" {
+
+int osb_autotune(osb_ctx *c, int reps, double *best_ms) {
+  if (!c) return OSB_EINVAL;
+  if (reps < 1) return set_err(c, OSB_EINVAL, "osb_autotune: reps must be >= 1");
+  if (c->plan.ndim != 3 || c->plan.conv != OSB_CONV_WENO5JS) return OSB_OK;
+  int rc = check_bound(c);
+  if (rc) return rc;
+  return c->mixed ? autotune_impl<float>(c, reps, best_ms) : autotune_impl<double>(c, reps, best_ms);
 }
 
 int osb_get_error(osb_ctx *c, char *buf, int n) {

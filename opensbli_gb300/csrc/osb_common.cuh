@@ -32,9 +32,9 @@ struct Phys {
   double inv_delta[3];
   double weno_eps;
   // derived constants, filled on the host in both precisions so kernels do no FP64 set-up work:
-  // gama-1, gama*Minf^2, 1/Re, kT = 1/((gama-1) Minf^2 Pr Re)
-  double gm1, gM2, invRe, kT;
-  float f_gama, f_gm1, f_gM2, f_invRe, f_kT, f_eps, f_inv_delta[3];
+  // gama-1, 1/(gama-1), gama*Minf^2, 1/Re, kT = 1/((gama-1) Minf^2 Pr Re)
+  double gm1, igm1, gM2, invRe, kT;
+  float f_gama, f_gm1, f_igm1, f_gM2, f_invRe, f_kT, f_eps, f_inv_delta[3];
 };
 
 // the FP64 or FP32 copy of a plan constant

@@ -11,6 +11,13 @@
 
 namespace osb {
 
+// launch shape of one direction's WENO flux kernel
+enum { WENO_TILE = 0, WENO_MARCH4 = 1, WENO_MARCH8 = 2 };
+struct WenoCfg {
+  int kind;  // WENO_TILE, or line-marching with 4 or 8 transverse lines per block (y and z only)
+  int seg;   // line-marching: cells per segment
+};
+
 struct Ctx {
   osb_plan_desc plan;
   Grid g;
@@ -28,6 +35,7 @@ struct Ctx {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   double graph_dt[2] = {0, 0};
   int64_t launches = 0;
+  WenoCfg wcfg[3] = {{WENO_TILE, 32}, {WENO_TILE, 32}, {WENO_TILE, 32}};
   int64_t graph_launches = 0;  // kernel launches recorded in one captured step
   int qold_valid = 0;          // the FP64 register holds the current state
   // 2D wall-bounded path
@@ -59,6 +67,8 @@ template <typename T> void launch_halos(const Ctx &c, Fields5<T> q, cudaStream_t
 
 template <typename T>
 void launch_weno_dir(const Ctx &c, Fields5<const T> q, Fields5<T> r, int dir, cudaStream_t s, int64_t *launches);
+template <typename T>
+void launch_weno_cfg(const Ctx &c, Fields5<const T> q, Fields5<T> r, int dir, WenoCfg w, cudaStream_t s);
 
 template <typename T>
 void launch_central_rk(const Ctx &c, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold, Fields5<T> rin,

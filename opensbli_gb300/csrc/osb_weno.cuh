@@ -1,0 +1,207 @@
+// osb_weno.cuh -- the per-interface arithmetic of the characteristic WENO5-JS flux, shared by the
+// tiled and the line-marching flux kernels.
+//
+// Restates the generated "LLFWeno_reconstruction_d_direction" kernels (shock_capturing.py:146-155,
+// 257-265) for one interface of a Cartesian block:
+//   * Roe average at i+1/2 (schemes/spatial/averaging.py:70-114):
+//       rho^ = sqrt(rho_L rho_R), u^ = (sqrt(rho_L) u_L + sqrt(rho_R) u_R)/(sqrt(rho_L)+sqrt(rho_R)),
+//       H^ likewise from (p+rhoE)/rho, a^ = sqrt((gama-1)(H^ - |u^|^2/2));
+//   * Euler eigensystem for the unit normal of direction d
+//     (physical_models/euler_eigensystem.py:107-135): eigenvalues (u_d,u_d,u_d,u_d+a,u_d-a);
+//   * LLF splitting (shock_capturing.py:357-398, 464-536): CF = LEV.F, CS = LEV.Q at i-2..i+3,
+//     lambda_r = max over those six points of |ev_r| from the point values, f+- = CF +- lambda CS;
+//   * WENO5-JS (weno.py:70-205, 341-369): the reference keeps the splitting's factor 1/2 out of f
+//     and puts it into the smoothness indicators (1/4 of Jiang-Shu's) and the candidate stencils
+//     (1/2 of the usual ones); alpha_r = d_r/(eps + beta_r)^2, omega_r = alpha_r / sum alpha;
+//   * flux = REV.(fhat+ + fhat-) (shock_capturing.py:418-448).
+//
+// Arithmetic is rearranged for fewer instructions, not changed in meaning: sqrt(rho_L) u_L is formed
+// as rhou_L / sqrt(rho_L); the three dense LEV rows (entropy and both acoustic waves) share one
+// dot product g = (phi, -(g-1)u, g-1).X and h = X_{1+d} - u_d X_0 (the flux vector F is never
+// stored: its projections are formed from Q, u_d and p):
+//     acoustic+- . X = bt (g +- a h),   entropy . X = X_0 - g / a^2;
+// the smoothness indicators use Jiang and Shu's sum-of-squares form.  The nonlinear weights:
+// in FP32 alpha_r = d_r * rcp((eps+beta_r)^2) with the fast hardware reciprocal (2 ulp); in FP64,
+// where every division costs a Newton sequence on the slow FP64 pipe, the three alphas are scaled
+// by the common factor prod_s (eps+beta_s)^2, alpha_0 ~ d_0 (eps+beta_1)^2 (eps+beta_2)^2 etc., so
+// one exact division per side remains (the products stay far inside the FP64 range).
+#pragma once
+#include "osb_common.cuh"
+
+namespace osb {
+
+template <typename T> __device__ __forceinline__ T rcp_t(T x);
+template <> __device__ __forceinline__ float rcp_t<float>(float x) { return __fdividef(1.0f, x); }
+template <> __device__ __forceinline__ double rcp_t<double>(double x) { return 1.0 / x; }
+
+// sqrt(x) and 1/sqrt(x) of a positive x: FP32 from the hardware reciprocal square root (one SFU
+// operation), FP64 from the correctly rounded square root and one exact division
+__device__ __forceinline__ void sqrt_rsqrt(float x, float &s, float &is) {
+  is = rsqrtf(x);
+  s = x * is;
+}
+__device__ __forceinline__ void sqrt_rsqrt(double x, double &s, double &is) {
+  s = sqrt(x);
+  is = 1.0 / s;
+}
+
+// One WENO5-JS side.  f0..f4 are the five stencil values ordered from the far upwind point to the
+// far downwind one (for the right-going side: points i-2..i+2; for the left-going side the caller
+// passes points i+3..i-1).  d0 weights the most downwind candidate (3/10), d2 the most upwind (1/10).
+template <typename T> __device__ __forceinline__ T weno5_side(T f0, T f1, T f2, T f3, T f4, T eps) {
+  const T c13 = T(13.0 / 48.0), c14 = T(1.0 / 16.0);
+  const T t0 = f2 - T(2) * f3 + f4, s0 = T(3) * f2 - T(4) * f3 + f4;
+  const T t1 = f1 - T(2) * f2 + f3, s1 = f1 - f3;
+  const T t2 = f0 - T(2) * f1 + f2, s2 = f0 - T(4) * f1 + T(3) * f2;
+  const T b0 = c13 * t0 * t0 + c14 * s0 * s0;
+  const T b1 = c13 * t1 * t1 + c14 * s1 * s1;
+  const T b2 = c13 * t2 * t2 + c14 * s2 * s2;
+  const T e0 = b0 + eps, e1 = b1 + eps, e2 = b2 + eps;
+  const T p0 = T(1.0 / 6.0) * f2 + T(5.0 / 12.0) * f3 - T(1.0 / 12.0) * f4;
+  const T p1 = T(-1.0 / 12.0) * f1 + T(5.0 / 12.0) * f2 + T(1.0 / 6.0) * f3;
+  const T p2 = T(1.0 / 6.0) * f0 - T(7.0 / 12.0) * f1 + T(11.0 / 12.0) * f2;
+  if (sizeof(T) == 8) {
+    const T q0 = e0 * e0, q1 = e1 * e1, q2 = e2 * e2;
+    const T a0 = T(3.0 / 10.0) * (q1 * q2), a1 = T(3.0 / 5.0) * (q0 * q2), a2 = T(1.0 / 10.0) * (q0 * q1);
+    return (a0 * p0 + a1 * p1 + a2 * p2) / (a0 + a1 + a2);
+  } else {
+    const T a0 = T(3.0 / 10.0) * rcp_t(e0 * e0);
+    const T a1 = T(3.0 / 5.0) * rcp_t(e1 * e1);
+    const T a2 = T(1.0 / 10.0) * rcp_t(e2 * e2);
+    return (a0 * p0 + a1 * p1 + a2 * p2) * rcp_t(a0 + a1 + a2);
+  }
+}
+
+// Per-point window entry: conserved vector Q, u_D, a, p.  The physical flux along D,
+// F = (Q_{1+D}, Q_{1+c} u_D + delta_cD p, (p + Q_4) u_D), is folded into the projections below.
+template <typename T> struct WPt {
+  T Q[5], ud, a, p;
+};
+
+// Primitive quantities of one point from its conserved vector (1/rho by the fast reciprocal in FP32).
+template <typename T, int D>
+__device__ __forceinline__ void point_prims(const T (&r)[5], T gm1, T gama, WPt<T> &w) {
+  const T irho = rcp_t(r[0]);
+  const T u0 = r[1] * irho, u1 = r[2] * irho, u2 = r[3] * irho;
+  const T p = gm1 * (r[4] - T(0.5) * (r[1] * u0 + r[2] * u1 + r[3] * u2));
+#pragma unroll
+  for (int v = 0; v < 5; ++v) w.Q[v] = r[v];
+  w.p = p;
+  T ia;
+  sqrt_rsqrt(gama * p * irho, w.a, ia);
+  w.ud = D == 0 ? u0 : D == 1 ? u1 : u2;
+}
+
+// Characteristic flux at the interface between window points 2 and 3 (points i and i+1).
+template <typename T, int D>
+__device__ __forceinline__ void interface_flux(const WPt<T> (&W)[6], const T gm1, const T igm1, const T eps,
+                                               T out[5]) {
+  constexpr int E1 = (D + 1) % 3, E2 = (D + 2) % 3;  // the two tangential axes (shear rows)
+  constexpr int e1 = 3 - E1 - D, e2 = 3 - E2 - D;    // third axis of each shear row
+  // ---- Roe average of points 2 and 3
+  const T rl = W[2].Q[0], rr = W[3].Q[0];
+  T sl, sr, isl, isr;  // sqrt(rho) and 1/sqrt(rho) of both sides
+  sqrt_rsqrt(rl, sl, isl);
+  sqrt_rsqrt(rr, sr, isr);
+  const T rho = sl * sr;
+  const T inv_s = rcp_t(sl + sr);
+  T u[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) u[c] = inv_s * (W[2].Q[1 + c] * isl + W[3].Q[1 + c] * isr);
+  const T Hh = inv_s * ((W[2].p + W[2].Q[4]) * isl + (W[3].p + W[3].Q[4]) * isr);
+  const T usq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+  T a, ia;
+  sqrt_rsqrt(gm1 * (Hh - T(0.5) * usq), a, ia);
+  const T irho = isl * isr;
+  const T phi = gm1 * T(0.5) * usq;
+  const T bt = T(0.70710678118654752440) * irho * ia;  // 1/(sqrt(2) rho a)
+  const T al = T(0.70710678118654752440) * rho * ia;   // rho/(sqrt(2) a)
+  const T ia2 = ia * ia;
+  const T btA = bt * a;
+
+  T lam_u = T(0), lam_p = T(0), lam_m = T(0);
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    lam_u = max_t(lam_u, abs_t(W[t].ud));
+    lam_p = max_t(lam_p, abs_t(W[t].ud + W[t].a));
+    lam_m = max_t(lam_m, abs_t(W[t].a - W[t].ud));
+  }
+  auto recon = [&](const T (&cf)[6], const T (&cs)[6], T lam) -> T {
+    T fp[6], fm[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      fp[t] = cf[t] + lam * cs[t];
+      fm[t] = cf[t] - lam * cs[t];
+    }
+    return weno5_side(fp[0], fp[1], fp[2], fp[3], fp[4], eps) + weno5_side(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
+  };
+
+  // ---- shear rows: LEV_r . X = (s/rho)(u_e X_0 - X_{1+e}); for X = F: X_0 = Q_{1+D}, X_{1+e} = Q_{1+e} u_D
+  const T se1 = (D == (E1 + 1) % 3) ? T(1) : T(-1), se2 = (D == (E2 + 1) % 3) ? T(1) : T(-1);
+  T rE1, rE2;
+  {
+    T cf[6], cs[6];
+    const T sr1 = se1 * irho;
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = sr1 * (u[e1] * W[t].Q[1 + D] - W[t].Q[1 + e1] * W[t].ud);
+      cs[t] = sr1 * (u[e1] * W[t].Q[0] - W[t].Q[1 + e1]);
+    }
+    rE1 = recon(cf, cs, lam_u);
+    const T sr2 = se2 * irho;
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = sr2 * (u[e2] * W[t].Q[1 + D] - W[t].Q[1 + e2] * W[t].ud);
+      cs[t] = sr2 * (u[e2] * W[t].Q[0] - W[t].Q[1 + e2]);
+    }
+    rE2 = recon(cf, cs, lam_u);
+  }
+  // ---- dense rows share g = phi X_0 - (g-1) u.X_{1..3} + (g-1) X_4 and h = X_{1+D} - u_D X_0
+  T gQ[6], gF[6], hQ[6], hF[6];
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    const WPt<T> &w = W[t];
+    const T dq = u[0] * w.Q[1] + u[1] * w.Q[2] + u[2] * w.Q[3];
+    gQ[t] = phi * w.Q[0] - gm1 * dq + gm1 * w.Q[4];
+    hQ[t] = w.Q[1 + D] - u[D] * w.Q[0];
+    gF[t] = phi * w.Q[1 + D] - gm1 * (w.ud * dq + u[D] * w.p) + gm1 * (w.p + w.Q[4]) * w.ud;
+    hF[t] = w.Q[1 + D] * w.ud + w.p - u[D] * w.Q[1 + D];
+  }
+  T rD, r3, r4;
+  {
+    T cf[6], cs[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = W[t].Q[1 + D] - gF[t] * ia2;
+      cs[t] = W[t].Q[0] - gQ[t] * ia2;
+    }
+    rD = recon(cf, cs, lam_u);
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = bt * gF[t] + btA * hF[t];
+      cs[t] = bt * gQ[t] + btA * hQ[t];
+    }
+    r3 = recon(cf, cs, lam_p);
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = bt * gF[t] - btA * hF[t];
+      cs[t] = bt * gQ[t] - btA * hQ[t];
+    }
+    r4 = recon(cf, cs, lam_m);
+  }
+
+  // ---- back to conserved space: flux = REV . rec
+  const T sac = r3 + r4, dac = r3 - r4;
+  const T hh = (phi + a * a) * igm1;
+  out[0] = rD + al * sac;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) out[1 + c] = u[c] * rD + al * (u[c] * sac + (c == D ? a * dac : T(0)));
+  out[4] = (phi * igm1) * rD + al * (hh * sac + u[D] * a * dac);
+  // shear columns: REV[1+e][r] = -s rho, REV[4][r] = -s rho u_e
+  out[1 + e1] -= se1 * rho * rE1;
+  out[4] -= se1 * rho * u[e1] * rE1;
+  out[1 + e2] -= se2 * rho * rE2;
+  out[4] -= se2 * rho * u[e2] * rE2;
+}
+
+}  // namespace osb

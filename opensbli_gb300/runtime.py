@@ -77,8 +77,10 @@ EXPORTS = (
     "osb_query_layout", "osb_create", "osb_bind_field", "osb_set_stream", "osb_init_tgv", "osb_set_state64",
     "osb_set_state64_padded", "osb_set_coordinate",
     "osb_get_state64", "osb_step", "osb_residual", "osb_reduce", "osb_launch_count", "osb_profile", "osb_profile_read",
-    "osb_get_error", "osb_destroy",
+    "osb_set_weno_shape", "osb_get_weno_shape", "osb_autotune", "osb_get_error", "osb_destroy",
 )
+# launch shapes of the WENO flux kernels (osb_set_weno_shape)
+WENO_SHAPES = {"tile": 0, "march4": 1, "march8": 2}
 PROFILE_FAMILIES = ["halo", "weno_x", "weno_y", "weno_z", "central_rk", "other"]
 
 _lib = None
@@ -116,6 +118,9 @@ def load(build_if_missing=True):
     lib.osb_launch_count.restype = ctypes.c_int64
     lib.osb_profile.argtypes = [vp, ip]
     lib.osb_profile_read.argtypes = [vp, ctypes.POINTER(dp), ctypes.POINTER(ctypes.c_int64), ip]
+    lib.osb_set_weno_shape.argtypes = [vp, ip, ip, ip]
+    lib.osb_get_weno_shape.argtypes = [vp, ip, ctypes.POINTER(ip), ctypes.POINTER(ip)]
+    lib.osb_autotune.argtypes = [vp, ip, ctypes.POINTER(dp)]
     lib.osb_get_error.argtypes = [vp, ctypes.c_char_p, ip]
     lib.osb_destroy.argtypes = [vp]
     lib.osb_destroy.restype = None
@@ -296,6 +301,27 @@ class Solver:
 
     def launch_count(self):
         return int(self.lib.osb_launch_count(self.ctx))
+
+    def set_weno_shape(self, d, kind, seg=32):
+        """Launch shape of the direction-d WENO flux kernel: kind in WENO_SHAPES, seg cells per line
+        segment for the line-marching shapes."""
+        self._check(self.lib.osb_set_weno_shape(self.ctx, int(d), WENO_SHAPES[kind], int(seg)))
+
+    def weno_shape(self, d):
+        k, sg = ctypes.c_int(), ctypes.c_int()
+        self._check(self.lib.osb_get_weno_shape(self.ctx, int(d), ctypes.byref(k), ctypes.byref(sg)))
+        return {v: n for n, v in WENO_SHAPES.items()}[k.value], sg.value
+
+    def autotune(self, reps=5):
+        """Time the candidate launch shapes on the bound state and keep the fastest per direction;
+        returns {dir: (kind, seg, ms per launch)} (empty for plans without WENO fluxes)."""
+        best = (ctypes.c_double * 3)()
+        self._in()
+        self._check(self.lib.osb_autotune(self.ctx, int(reps), best))
+        self._out()
+        if self.plan.ndim != 3 or self.plan.conv != "weno5js":
+            return {}
+        return {d: self.weno_shape(d) + (best[d],) for d in range(3)}
 
     def close(self):
         if getattr(self, "ctx", None):
