@@ -161,21 +161,27 @@ int64_t osb_launch_count(osb_ctx *ctx);
 int osb_profile(osb_ctx *ctx, int enable);
 int osb_profile_read(osb_ctx *ctx, double *total_ms, int64_t *counts, int n);
 
-/* Launch shapes of the WENO5-JS flux kernels.  No counterpart in the reference (the generated OPS code
- * launches every kernel with one fixed block shape).  Direction 0 (x) always runs the tiled kernel;
- * directions 1 and 2 run tiled or line-marching with 4 or 8 transverse lines per block and `seg`
- * cells per line segment (4 <= seg <= 4096).  All shapes compute the same interface fluxes.
- * osb_set_weno_shape / osb_autotune drop captured step graphs (re-captured at the next osb_step).
- * osb_autotune times every candidate shape of each direction (`reps` launches each, CUDA events on
- * the context stream, after one warm-up launch) on the bound state, keeps the fastest, and writes
- * its time per launch in ms to best_ms[dir] when best_ms is not NULL.  It synchronises the stream,
- * overwrites the residual scratch, and must not be called during stream capture.  On plans without
- * WENO fluxes it does nothing and returns 0. */
+/* Launch shapes of the 3D kernels.  No counterpart in the reference (the generated OPS code launches
+ * every kernel with one fixed block shape).
+ * WENO5-JS flux kernels: tiled, or line-marching with `seg` cells per line segment (4 <= seg <= 4096)
+ * and 4 or 8 warps per block (x: each warp walks 32 y-lines; y and z: each thread walks one line,
+ * 32 x-lanes by 4 or 8 lines per block).  Fused central/RK kernel: tiles of 32 x ty points (ty 8 or 16).  All shapes
+ * compute the same values.  Setting a shape drops captured step graphs (re-captured at the next
+ * osb_step).
+ * osb_autotune times every candidate shape (`reps` launches each, CUDA events on the context
+ * stream, after one warm-up launch) on the bound state, keeps the fastest, and writes the time per
+ * launch in ms of the chosen shapes to best_ms[0..3] (WENO x, y, z, central; 0 for kernels the plan
+ * does not use) when best_ms is not NULL.  The central kernel is timed in its residual-only form.
+ * It synchronises the stream, overwrites the residual scratch (never the state or the RK register),
+ * and must not be called during stream capture.  On 2D plans it does nothing and returns 0. */
 #define OSB_WENO_TILE 0
 #define OSB_WENO_MARCH4 1
 #define OSB_WENO_MARCH8 2
+#define OSB_TUNE_SLOTS 4
 int osb_set_weno_shape(osb_ctx *ctx, int dir, int kind, int seg);
 int osb_get_weno_shape(osb_ctx *ctx, int dir, int *kind, int *seg);
+int osb_set_central_shape(osb_ctx *ctx, int ty);
+int osb_get_central_shape(osb_ctx *ctx, int *ty);
 int osb_autotune(osb_ctx *ctx, int reps, double *best_ms);
 
 int osb_get_error(osb_ctx *ctx, char *buf, int n);

@@ -12,6 +12,7 @@
 // Metrics (once, k2_metric_*): detJ = dx1/dxi1 with the closures, D11 = 1/detJ, halos mirrored about
 // the boundary points, SD111 = dD11/dxi1 (equation_types/metric.py:37-234, 315-332).
 #include "osb_common.cuh"
+#include "osb_cvt.cuh"
 #include "osb_internal.h"
 
 namespace osb {
@@ -163,7 +164,7 @@ template <typename T> struct Q4T {
 // FP64 master -> working state (mixed path), every padded point.
 __global__ void k2_to_state(int64_t numel, Q4 src, Q4T<float> dst) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < numel; t += (int64_t)gridDim.x * blockDim.x)
-    for (int v = 0; v < 4; ++v) dst.v[v][t] = (float)src.v[v][t];
+    for (int v = 0; v < 4; ++v) dst.v[v][t] = cvt_f64_f32(src.v[v][t]);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -477,13 +478,13 @@ __global__ void __launch_bounds__(256) k2_visc_rk(Grid g, Prims<const T> pr, con
   if (update) {
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      const double d = va.dt * (double)R[v] + va.A * du.v[v][c];
+      const double d = va.dt * to_f64(R[v]) + va.A * du.v[v][c];
       du.v[v][c] = d;
       q64.v[v][c] = va.B * d + q64.v[v][c];
     }
   } else {
 #pragma unroll
-    for (int v = 0; v < 4; ++v) du.v[v][c] = (double)R[v];  // residual output mode: du holds R
+    for (int v = 0; v < 4; ++v) du.v[v][c] = to_f64(R[v]);  // residual output mode: du holds R
   }
 }
 

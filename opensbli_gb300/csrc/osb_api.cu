@@ -608,6 +608,12 @@ int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
     *out = c;
     return OSB_OK;
   }
+  {
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && nsm > 0)
+      c->num_sms = nsm;
+  }
   if (c->mixed) { setup_central<float>(); setup_weno<float>(); }
   else { setup_central<double>(); setup_weno<double>(); }
   e = cudaGetLastError();
@@ -821,8 +827,6 @@ int osb_set_weno_shape(osb_ctx *c, int dir, int kind, int seg) {
   if (dir < 0 || dir > 2) return set_err(c, OSB_EINVAL, "osb_set_weno_shape: dir must be 0, 1 or 2");
   if (kind != OSB_WENO_TILE && kind != OSB_WENO_MARCH4 && kind != OSB_WENO_MARCH8)
     return set_err(c, OSB_EINVAL, "osb_set_weno_shape: unknown kind");
-  if (dir == 0 && kind != OSB_WENO_TILE)
-    return set_err(c, OSB_EUNSUPPORTED, "osb_set_weno_shape: the x direction runs the tiled kernel only");
   if (seg < 4 || seg > 4096) return set_err(c, OSB_EINVAL, "osb_set_weno_shape: seg must lie in [4, 4096]");
   c->wcfg[dir] = WenoCfg{kind, seg};
   drop_graphs(c);
@@ -847,36 +851,64 @@ template <typename T> static int autotune_impl(osb_ctx *c, int reps, double *bes
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
-  const int n[3] = {c->g.n0, c->g.n1, c->g.n2};
   cudaError_t err = cudaSuccess;
-  for (int d = 0; d < 3 && err == cudaSuccess; ++d) {
+  // time `launch` (one warm-up, then reps launches); returns ms per launch, or -1 on error
+  auto timeit = [&](auto &&launch) -> float {
+    launch();
+    cudaEventRecord(e0, s);
+    for (int k = 0; k < reps; ++k) launch();
+    cudaEventRecord(e1, s);
+    err = cudaEventSynchronize(e1);
+    if (err == cudaSuccess) err = cudaGetLastError();
+    if (err != cudaSuccess) return -1.0f;
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    return ms / reps;
+  };
+  for (int t = 0; t < OSB_TUNE_SLOTS && best_ms; ++t) best_ms[t] = 0.0;
+  const int n[3] = {c->g.n0, c->g.n1, c->g.n2};
+  const bool weno = c->plan.conv == OSB_CONV_WENO5JS;
+  for (int d = 0; d < 3 && weno && err == cudaSuccess; ++d) {
     std::vector<WenoCfg> cand{{WENO_TILE, 32}};
-    if (d > 0) {
-      for (int kind : {WENO_MARCH4, WENO_MARCH8}) {
-        for (int seg : {16, 24, 32, 48, 64, 96, 128, 192, 256})
-          if (seg < n[d]) cand.push_back({kind, seg});
-        cand.push_back({kind, n[d]});
-      }
+    for (int kind : {WENO_MARCH4, WENO_MARCH8}) {
+      for (int seg : {16, 24, 32, 48, 64, 96, 128, 192, 256})
+        if (seg < n[d]) cand.push_back({kind, seg});
+      cand.push_back({kind, n[d]});
     }
     float best = 1e30f;
-    WenoCfg pick_cfg = c->wcfg[d];
+    WenoCfg choice = c->wcfg[d];
     for (const WenoCfg &w : cand) {
-      launch_weno_cfg<T>(*c, qc, r, d, w, s);
-      cudaEventRecord(e0, s);
-      for (int k = 0; k < reps; ++k) launch_weno_cfg<T>(*c, qc, r, d, w, s);
-      cudaEventRecord(e1, s);
-      err = cudaEventSynchronize(e1);
-      if (err == cudaSuccess) err = cudaGetLastError();
-      if (err != cudaSuccess) break;
-      float ms = 0;
-      cudaEventElapsedTime(&ms, e0, e1);
+      const float ms = timeit([&] { launch_weno_cfg<T>(*c, qc, r, d, w, s); });
+      if (ms < 0) break;
       if (ms < best) {
         best = ms;
-        pick_cfg = w;
+        choice = w;
       }
     }
-    c->wcfg[d] = pick_cfg;
-    if (best_ms) best_ms[d] = best / reps;
+    c->wcfg[d] = choice;
+    if (best_ms) best_ms[d] = best;
+  }
+  if (err == cudaSuccess) {
+    // residual-only form of the step's central kernel: same stencils and loads, writes R into the
+    // residual scratch instead of touching the state and the RK register
+    const int visc = c->plan.visc == OSB_VISC_CONST ? CRK_VISC : 0;
+    const int mode = (weno ? CRK_RIN : CRK_SKEW) | visc;
+    float best = 1e30f;
+    int choice = c->crk_ty;
+    for (int ty : {8, 16}) {
+      c->crk_ty = ty;
+      int64_t dummy = 0;
+      const float ms = timeit([&] {
+        launch_central_rk<T>(*c, qc, r, fields_d(c->qold), r, r, 0.0, 0.0, mode, s, &dummy);
+      });
+      if (ms < 0) break;
+      if (ms < best) {
+        best = ms;
+        choice = ty;
+      }
+    }
+    c->crk_ty = choice;
+    if (best_ms) best_ms[3] = best;
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
@@ -886,10 +918,27 @@ template <typename T> static int autotune_impl(osb_ctx *c, int reps, double *bes
 
 extern "C" {
 
+int osb_set_central_shape(osb_ctx *c, int ty) {
+  if (!c) return OSB_EINVAL;
+  if (ty != 8 && ty != 16) return set_err(c, OSB_EINVAL, "osb_set_central_shape: ty must be 8 or 16");
+  c->crk_ty = ty;
+  drop_graphs(c);
+  return OSB_OK;
+}
+
+int osb_get_central_shape(osb_ctx *c, int *ty) {
+  if (!c || !ty) return OSB_EINVAL;
+  *ty = c->crk_ty;
+  return OSB_OK;
+}
+
 int osb_autotune(osb_ctx *c, int reps, double *best_ms) {
   if (!c) return OSB_EINVAL;
   if (reps < 1) return set_err(c, OSB_EINVAL, "osb_autotune: reps must be >= 1");
-  if (c->plan.ndim != 3 || c->plan.conv != OSB_CONV_WENO5JS) return OSB_OK;
+  if (c->plan.ndim != 3) {
+    for (int t = 0; t < OSB_TUNE_SLOTS && best_ms; ++t) best_ms[t] = 0.0;
+    return OSB_OK;
+  }
   int rc = check_bound(c);
   if (rc) return rc;
   return c->mixed ? autotune_impl<float>(c, reps, best_ms) : autotune_impl<double>(c, reps, best_ms);

@@ -19,39 +19,50 @@
 //   * the 2-register RK3 update (schemes/temporal/rk_sbli.py:117-124):
 //       q = qold + dt*rknew[s]*R,  qold = qold + dt*rkold[s]*R   (qold kept in FP64).
 //
-// Tiling: a 32x8 (x,y) tile per block marches through a chunk of z.  A ring of 5 shared-memory
+// Tiling: a 32 x TY (x,y) tile per block marches through a chunk of z.  A ring of 5 shared-memory
 // planes holds the primitive fields of planes k-2..k+2 with a 2-point x/y halo, so every first,
 // second and mixed derivative of the stencil is read from shared memory; each global point is
-// loaded once per plane visit (coalesced along x).
+// loaded once per plane visit (coalesced along x).  The ring holds u0, u1, u2, T and, when the
+// skew-symmetric convective terms are evaluated, rho, p and rhoE as well (with WENO fluxes the
+// kernel needs only the viscous stencils: 4 fields, so more blocks fit on an SM).
 #include <cstdio>
 
 #include "osb_common.cuh"
+#include "osb_cvt.cuh"
 #include "osb_internal.h"
 
 namespace osb {
 
 namespace {
-constexpr int TX = 32, TY = 8, PX = TX + 4, PY = TY + 4, NF = 7, NP = 5;
-enum { F_RHO = 0, F_U0, F_U1, F_U2, F_P, F_T, F_E };
-
-template <typename T> struct SmemC {
-  T s[NP][NF][PY][PX];
-};
+constexpr int TX = 32, PX = TX + 4, NP = 5;
+enum { F_U0 = 0, F_U1, F_U2, F_T, F_RHO, F_P, F_E };
+template <int MODE> __host__ __device__ constexpr int ring_fields() { return (MODE & CRK_SKEW) ? 7 : 4; }
+// FP32: the 4-field ring allows 1024 resident threads per SM (64 registers); the 7-field ring is
+// limited by shared memory to 3 blocks of 32x8 or 1 of 32x16.  FP64 runs on the FP64 pipe's rate.
+template <typename T, int MODE, int TY> __host__ __device__ constexpr int central_min_blocks() {
+  return sizeof(T) != 4 ? 1 : (MODE & CRK_SKEW) ? (TY == 8 ? 3 : 1) : 1024 / (TX * TY);
+}
+template <typename T, int MODE, int TY> constexpr size_t ring_bytes() {
+  return sizeof(T) * (size_t)NP * ring_fields<MODE>() * (TY + 4) * PX;
+}
 }  // namespace
 
-template <typename T, int MODE>
-__global__ void __launch_bounds__(256) k_central_rk(Grid g, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold,
-                                                    Fields5<T> rin, Fields5<T> rout, Phys ph, double dt_new,
-                                                    double dt_old, int zchunk) {
+template <typename T, int MODE, int TY>
+__global__ void __launch_bounds__(TX * TY, central_min_blocks<T, MODE, TY>()) k_central_rk(Grid g, Fields5<const T> q, Fields5<T> qnew,
+                                                        Fields5<double> qold, Fields5<T> rin, Fields5<T> rout, Phys ph,
+                                                        double dt_new, double dt_old, int zchunk) {
+  constexpr int NF = ring_fields<MODE>(), PY = TY + 4;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  SmemC<T> &sm = *reinterpret_cast<SmemC<T> *>(smem_raw);
+  T *ring = reinterpret_cast<T *>(smem_raw);  // [NP][NF][PY][PX]
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * zchunk;
   const int k1 = min(k0 + zchunk, g.n2);
   const T gm1 = pick<T>(ph.gm1, ph.f_gm1);
   const T gM2 = pick<T>(ph.gM2, ph.f_gM2);
+  const T ddt = (T)(dt_new - dt_old);
 
   auto slot = [](int k) { return ((k % NP) + NP) % NP; };
+  auto at = [&](int sl, int f, int py, int px) -> T & { return ring[((sl * NF + f) * PY + py) * PX + px]; };
   // Plane loads are software-pipelined: the global loads of plane k+3 are issued into registers
   // before the stencil work on plane k and written (as primitives) into the ring after it.
   constexpr int PPT = (PX * PY + TX * TY - 1) / (TX * TY);  // points per thread per plane
@@ -78,18 +89,20 @@ __global__ void __launch_bounds__(256) k_central_rk(Grid g, Fields5<const T> q, 
       const int i = i0 - 2 + px, j = j0 - 2 + py;
       if (e < PX * PY && i < g.n0 + 2 && j < g.n1 + 2 && k < g.n2 + 2) {
         const T rho = pre[r][0];
-        const T irho = T(1) / rho;
+        const T irho = rcp_t(rho);
         const T u0 = pre[r][1] * irho, u1 = pre[r][2] * irho, u2 = pre[r][3] * irho;
         const T E = pre[r][4];
         const T half = T(0.5);
         const T p = gm1 * (E - half * rho * u0 * u0 - half * rho * u1 * u1 - half * rho * u2 * u2);
-        sm.s[sl][F_RHO][py][px] = rho;
-        sm.s[sl][F_U0][py][px] = u0;
-        sm.s[sl][F_U1][py][px] = u1;
-        sm.s[sl][F_U2][py][px] = u2;
-        sm.s[sl][F_P][py][px] = p;
-        sm.s[sl][F_T][py][px] = gM2 * p * irho;
-        sm.s[sl][F_E][py][px] = E;
+        at(sl, F_U0, py, px) = u0;
+        at(sl, F_U1, py, px) = u1;
+        at(sl, F_U2, py, px) = u2;
+        at(sl, F_T, py, px) = gM2 * p * irho;
+        if (NF == 7) {
+          at(sl, F_RHO, py, px) = rho;
+          at(sl, F_P, py, px) = p;
+          at(sl, F_E, py, px) = E;
+        }
       }
     }
   };
@@ -125,7 +138,7 @@ __global__ void __launch_bounds__(256) k_central_rk(Grid g, Fields5<const T> q, 
     }
     if (active) {
       // field f at offset (dz, dy, dx) from the output point
-      auto S = [&](int f, int dz, int dy, int dx) -> T { return sm.s[slot(k + dz)][f][ty + 2 + dy][tx + 2 + dx]; };
+      auto S = [&](int f, int dz, int dy, int dx) -> T { return at(slot(k + dz), f, ty + 2 + dy, tx + 2 + dx); };
       auto SA = [&](int f, int axis, int o) -> T {
         return axis == 0 ? S(f, 0, 0, o) : axis == 1 ? S(f, 0, o, 0) : S(f, o, 0, 0);
       };
@@ -143,9 +156,10 @@ __global__ void __launch_bounds__(256) k_central_rk(Grid g, Fields5<const T> q, 
           du[c][d] = acc * idl[d];
         }
       const T divu = du[0][0] + du[1][1] + du[2][2];
-      const T rho0 = S(F_RHO, 0, 0, 0), uu[3] = {S(F_U0, 0, 0, 0), S(F_U1, 0, 0, 0), S(F_U2, 0, 0, 0)};
+      const T uu[3] = {S(F_U0, 0, 0, 0), S(F_U1, 0, 0, 0), S(F_U2, 0, 0, 0)};
 
-      if (MODE & CRK_SKEW) {
+      if constexpr ((MODE & CRK_SKEW) != 0) {
+        const T rho0 = S(F_RHO, 0, 0, 0);
         const T phi0[5] = {rho0, rho0 * uu[0], rho0 * uu[1], rho0 * uu[2], S(F_E, 0, 0, 0)};
         T acc[5] = {T(0), T(0), T(0), T(0), T(0)};
         T dpu = T(0);
@@ -249,15 +263,17 @@ __global__ void __launch_bounds__(256) k_central_rk(Grid g, Fields5<const T> q, 
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
           const double o = opre[v];
-          const double r = (double)R[v];
-          const double o2 = dt_old * r + o;
-          qold.v[v][n] = o2;
-          if (sizeof(T) == 8) {
+          if constexpr (sizeof(T) == 8) {
+            const double r = (double)R[v];
+            qold.v[v][n] = dt_old * r + o;
             qnew.v[v][n] = (T)(dt_new * r + o);
           } else {
             // FP32 state: the stage value q = qold + dt_new R equals qold' + (dt_new - dt_old) R;
-            // rounding qold' and adding the small FP32 correction keeps FP64 work to one FMA per var
-            qnew.v[v][n] = (T)o2 + (T)(dt_new - dt_old) * R[v];
+            // rounding qold' and adding the small FP32 correction leaves one FP64 FMA per variable
+            // on the FP64 pipe, the conversions run on the integer pipes (osb_cvt.cuh)
+            const double o2 = fma(dt_old, cvt_f32_f64(R[v]), o);
+            qold.v[v][n] = o2;
+            qnew.v[v][n] = cvt_f64_f32(o2) + ddt * R[v];
           }
         }
       } else {
@@ -270,21 +286,39 @@ __global__ void __launch_bounds__(256) k_central_rk(Grid g, Fields5<const T> q, 
   }
 }
 
-template <typename T, int MODE>
+// resident blocks per SM of one kernel instance (occupancy calculator, cached per instance)
+template <typename T, int MODE, int TY> static int resident_per_sm() {
+  static int nb = [] {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_central_rk<T, MODE, TY>, TX * TY,
+                                                      ring_bytes<T, MODE, TY>()) != cudaSuccess || b < 1)
+      b = 1;
+    return b;
+  }();
+  return nb;
+}
+
+template <typename T, int MODE, int TY>
 static void launch_mode(const Ctx &c, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold, Fields5<T> rin,
                         Fields5<T> rout, double dt_new, double dt_old, cudaStream_t s) {
-  const size_t smem = sizeof(SmemC<T>);
   const int bx = (c.g.n0 + TX - 1) / TX, by = (c.g.n1 + TY - 1) / TY;
-  // z-chunks: about four waves of resident blocks (each SM holds 3 FP32 / 1 FP64 block of this
-  // shared-memory footprint) so the last wave's tail is short; at least 8 planes per chunk so the
-  // 4 halo planes of each chunk cost at most half a chunk's loads
-  const int resident = 152 * (sizeof(T) == 4 ? 3 : 1);
+  // z-chunks: about four waves of resident blocks so the last wave's tail is short; at least 8
+  // planes per chunk so the 4 halo planes of each chunk cost at most half a chunk's loads
+  const int resident = c.num_sms * resident_per_sm<T, MODE, TY>();
   int nzc = (4 * resident + bx * by - 1) / (bx * by);
   nzc = max(1, min(nzc, (c.g.n2 + 7) / 8));
   const int zchunk = (c.g.n2 + nzc - 1) / nzc;
   nzc = (c.g.n2 + zchunk - 1) / zchunk;
   dim3 grid(bx, by, nzc), block(TX, TY);
-  k_central_rk<T, MODE><<<grid, block, smem, s>>>(c.g, q, qnew, qold, rin, rout, c.ph, dt_new, dt_old, zchunk);
+  k_central_rk<T, MODE, TY><<<grid, block, ring_bytes<T, MODE, TY>(), s>>>(c.g, q, qnew, qold, rin, rout, c.ph, dt_new,
+                                                                          dt_old, zchunk);
+}
+
+template <typename T, int MODE>
+static void launch_ty(const Ctx &c, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold, Fields5<T> rin,
+                      Fields5<T> rout, double dt_new, double dt_old, cudaStream_t s) {
+  if (c.crk_ty == 16) launch_mode<T, MODE, 16>(c, q, qnew, qold, rin, rout, dt_new, dt_old, s);
+  else launch_mode<T, MODE, 8>(c, q, qnew, qold, rin, rout, dt_new, dt_old, s);
 }
 
 template <typename T>
@@ -293,7 +327,7 @@ void launch_central_rk(const Ctx &c, Fields5<const T> q, Fields5<T> qnew, Fields
   ++*launches;
   switch (mode) {
 #define OSB_CASE(M) \
-  case M: launch_mode<T, M>(c, q, qnew, qold, rin, rout, dt_new, dt_old, s); break;
+  case M: launch_ty<T, M>(c, q, qnew, qold, rin, rout, dt_new, dt_old, s); break;
     OSB_CASE(CRK_SKEW | CRK_VISC | CRK_UPDATE)
     OSB_CASE(CRK_SKEW | CRK_VISC)
     OSB_CASE(CRK_SKEW | CRK_UPDATE)
@@ -309,18 +343,21 @@ void launch_central_rk(const Ctx &c, Fields5<const T> q, Fields5<T> qnew, Fields
   }
 }
 
+template <typename T, int MODE> static void attr_mode() {
+  cudaFuncSetAttribute(k_central_rk<T, MODE, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)ring_bytes<T, MODE, 8>());
+  cudaFuncSetAttribute(k_central_rk<T, MODE, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)ring_bytes<T, MODE, 16>());
+}
 template <typename T> void setup_central() {
-  const int smem = (int)sizeof(SmemC<T>);
-#define OSB_ATTR(M) cudaFuncSetAttribute(k_central_rk<T, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  OSB_ATTR(CRK_SKEW | CRK_VISC | CRK_UPDATE)
-  OSB_ATTR(CRK_SKEW | CRK_VISC)
-  OSB_ATTR(CRK_SKEW | CRK_UPDATE)
-  OSB_ATTR(CRK_SKEW)
-  OSB_ATTR(CRK_VISC | CRK_RIN | CRK_UPDATE)
-  OSB_ATTR(CRK_VISC | CRK_RIN)
-  OSB_ATTR(CRK_RIN | CRK_UPDATE)
-  OSB_ATTR(CRK_RIN)
-#undef OSB_ATTR
+  attr_mode<T, CRK_SKEW | CRK_VISC | CRK_UPDATE>();
+  attr_mode<T, CRK_SKEW | CRK_VISC>();
+  attr_mode<T, CRK_SKEW | CRK_UPDATE>();
+  attr_mode<T, CRK_SKEW>();
+  attr_mode<T, CRK_VISC | CRK_RIN | CRK_UPDATE>();
+  attr_mode<T, CRK_VISC | CRK_RIN>();
+  attr_mode<T, CRK_RIN | CRK_UPDATE>();
+  attr_mode<T, CRK_RIN>();
 }
 template void setup_central<float>();
 template void setup_central<double>();

@@ -46,6 +46,11 @@ template <typename T> __device__ __forceinline__ T sqrt_t(T x);
 template <> __device__ __forceinline__ float sqrt_t<float>(float x) { return sqrtf(x); }
 template <> __device__ __forceinline__ double sqrt_t<double>(double x) { return sqrt(x); }
 
+// 1/x: the fast hardware reciprocal in FP32 (2 ulp), the exact quotient in FP64
+template <typename T> __device__ __forceinline__ T rcp_t(T x);
+template <> __device__ __forceinline__ float rcp_t<float>(float x) { return __fdividef(1.0f, x); }
+template <> __device__ __forceinline__ double rcp_t<double>(double x) { return 1.0 / x; }
+
 template <typename T> __device__ __forceinline__ T abs_t(T x) { return x < T(0) ? -x : x; }
 template <typename T> __device__ __forceinline__ T max_t(T a, T b) { return a > b ? a : b; }
 

@@ -36,6 +36,8 @@ struct Ctx {
   double graph_dt[2] = {0, 0};
   int64_t launches = 0;
   WenoCfg wcfg[3] = {{WENO_TILE, 32}, {WENO_TILE, 32}, {WENO_TILE, 32}};
+  int crk_ty = 8;             // tile height of the fused central/RK kernel (8 or 16)
+  int num_sms = 152;          // multiprocessors of the device (set at creation)
   int64_t graph_launches = 0;  // kernel launches recorded in one captured step
   int qold_valid = 0;          // the FP64 register holds the current state
   // 2D wall-bounded path

@@ -19,6 +19,8 @@
 //    cell being finished are loaded one interface ahead, the previous interface flux stays in
 //    registers, and no shared memory or barrier is used.  Each segment re-reads the 5 points of
 //    its stencil halo and recomputes one interface flux.
+//  * line-marching (x): a warp owns 32 y-lines and walks along x; conserved vectors and residuals
+//    pass through a per-warp shared-memory transpose so global accesses stay row-contiguous.
 // Which shape runs, and the segment length, is chosen per direction by osb_autotune.
 #include "osb_common.cuh"
 #include "osb_internal.h"
@@ -246,6 +248,115 @@ __global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 512 : 256) / (32 * 
   }
 }
 
+// Line-marching flux kernel for x.  A warp owns 32 consecutive y-lines of one z-plane and walks a
+// segment of L cells along x; lane l computes line j0+l.  The conserved vectors arrive in chunks of
+// XC points of all 32 lines, loaded with the lanes spread along x (each row's XC values are
+// contiguous) and transposed through a per-warp shared-memory tile; the next chunk's loads are in
+// flight while the current one is consumed.  Residuals are staged the same way and written back in
+// row pieces aligned with the 32-byte sectors of the padded layout (interior x = 0 sits 4 elements
+// into a row).  Only __syncwarp orders the per-warp tiles; the x sweep writes R (no accumulation).
+template <typename T> struct MX {
+  static constexpr int XC = 4;            // points per load chunk
+  static constexpr int RG = 8;            // cells per residual group
+  static constexpr int QP = XC + 1;       // row pitch of the staged conserved tile
+  static constexpr int RP = RG + 1;       // row pitch of the staged residual tile
+  static constexpr int WARP_ELEMS = 5 * 32 * QP + 5 * 32 * RP;
+};
+
+template <typename T, int BY>
+__global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 512 : 256) / (32 * BY))
+    k_weno_march_x(Grid g, Fields5<const T> q, Fields5<T> res, Phys ph, int L) {
+  using M = MX<T>;
+  constexpr int XC = M::XC, RG = M::RG, QP = M::QP, RP = M::RP;
+  constexpr int RPI = 32 / XC;  // rows covered by one load instruction
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x, w = threadIdx.y;
+  T *qs = reinterpret_cast<T *>(smem_raw) + (size_t)w * M::WARP_ELEMS;  // [5][32][QP]
+  T *rs = qs + 5 * 32 * QP;                                              // [5][32][RP]
+  const int j0 = blockIdx.y * 32, k = blockIdx.z * BY + w;
+  if (k >= g.n2) return;  // uniform per warp
+  const int n0 = g.n0, n1 = g.n1;
+  const int c0 = blockIdx.x * L, c1 = min(c0 + L, n0);  // cells c0 .. c1-1
+  const int pfirst = c0 - 3, plast = c1 + 2;            // points of the segment's stencils
+  const T gm1 = pick<T>(ph.gm1, ph.f_gm1), gama = pick<T>(ph.gama, ph.f_gama);
+  const T igm1 = pick<T>(ph.igm1, ph.f_igm1), eps = pick<T>(ph.weno_eps, ph.f_eps);
+  const T idd = pick<T>(ph.inv_delta[0], ph.f_inv_delta[0]);
+  const int lrow = lane / XC, lcol = lane % XC;  // loader position inside a chunk
+  const bool row_ok = j0 + lane < n1;
+
+  T buf[5][XC];  // this lane's share of a chunk: XC rows (lrow + RPI*it), one point each
+  auto load_chunk = [&](int xs) {
+#pragma unroll
+    for (int it = 0; it < XC; ++it) {
+      const int row = lrow + RPI * it, x = xs + lcol;
+      if (j0 + row < n1 && x <= n0 + 3) {
+        const int64_t m = gidx(g, x, j0 + row, k);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) buf[v][it] = __ldg(q.v[v] + m);
+      }
+    }
+  };
+  auto stage_chunk = [&]() {
+#pragma unroll
+    for (int it = 0; it < XC; ++it) {
+      const int row = lrow + RPI * it;
+#pragma unroll
+      for (int v = 0; v < 5; ++v) qs[(v * 32 + row) * QP + lcol] = buf[v][it];
+    }
+  };
+  // residual groups: cells [gs, gs+RG) with gs = 8m - 4, i.e. whole 32-byte sectors of a row
+  auto flush = [&](int gs, int lo, int hi) {
+    __syncwarp();
+    constexpr int RR = 32 / RG;  // rows per store instruction
+#pragma unroll
+    for (int it = 0; it < RG; ++it) {
+      const int row = lane / RG + RR * it, col = lane % RG, x = gs + col;
+      if (j0 + row < n1 && x >= lo && x <= hi) {
+        const int64_t m = gidx(g, x, j0 + row, k);
+#pragma unroll
+        for (int v = 0; v < 5; ++v) res.v[v][m] = rs[(v * 32 + row) * RP + col];
+      }
+    }
+    __syncwarp();
+  };
+
+  WPt<T> W[6];
+  T Fp[5];
+  int xc = ((pfirst + 4) / XC) * XC - 4;  // chunk containing pfirst (pfirst + 4 >= 1)
+  load_chunk(xc);
+#pragma unroll 1
+  for (; xc <= plast; xc += XC) {
+    __syncwarp();
+    stage_chunk();
+    __syncwarp();
+    if (xc + XC <= plast) load_chunk(xc + XC);
+    const int pa = max(xc, pfirst), pb = min(xc + XC - 1, plast);
+#pragma unroll 1
+    for (int p = pa; p <= pb; ++p) {
+#pragma unroll
+      for (int t = 0; t < 5; ++t) W[t] = W[t + 1];
+      T r[5];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) r[v] = qs[(v * 32 + lane) * QP + (p - xc)];
+      point_prims<T, 0>(r, gm1, gama, W[5]);
+      if (p >= c0 + 2) {  // window holds points c-3 .. c+2 of interface c = p - 2
+        const int c = p - 2;
+        T F[5];
+        if (row_ok) interface_flux<T, 0>(W, gm1, igm1, eps, F);
+        if (c > c0) {
+          const int cc = c - 1;  // cell finished by this interface
+          const int gs = ((cc + 4) / RG) * RG - 4, col = cc - gs;
+#pragma unroll
+          for (int v = 0; v < 5; ++v) rs[(v * 32 + lane) * RP + col] = -(F[v] - Fp[v]) * idd;
+          if (col == RG - 1 || cc == c1 - 1) flush(gs, c0, c1 - 1);
+        }
+#pragma unroll
+        for (int v = 0; v < 5; ++v) Fp[v] = F[v];
+      }
+    }
+  }
+}
+
 template <typename T, int DIR> constexpr size_t tile_smem() {
   using Tl = WTile<DIR>;
   return sizeof(T) * ((size_t)W_NF * (Tl::TI + 5) * Tl::TA + 5 * (DIR == 0 ? Tl::TA * Tl::FS : Tl::TI * Tl::TA));
@@ -270,10 +381,21 @@ static void launch_march(const Ctx &c, Fields5<const T> q, Fields5<T> r, int L, 
   k_weno_march<T, DIR, ACCUM, BY><<<grid, dim3(32, BY), 0, s>>>(c.g, q, r, c.ph, L);
 }
 
+template <typename T, int BY> constexpr size_t march_x_smem() { return sizeof(T) * (size_t)BY * MX<T>::WARP_ELEMS; }
+
+template <typename T, int BY>
+static void launch_march_x(const Ctx &c, Fields5<const T> q, Fields5<T> r, int L, cudaStream_t s) {
+  dim3 grid((c.g.n0 + L - 1) / L, (c.g.n1 + 31) / 32, (c.g.n2 + BY - 1) / BY);
+  k_weno_march_x<T, BY><<<grid, dim3(32, BY), march_x_smem<T, BY>(), s>>>(c.g, q, r, c.ph, L);
+}
+
 template <typename T, int DIR, bool ACCUM>
 static void launch_variant(const Ctx &c, Fields5<const T> q, Fields5<T> r, WenoCfg w, cudaStream_t s) {
   if constexpr (DIR == 0) {
-    launch_tile<T, DIR, ACCUM>(c, q, r, s);
+    static_assert(!ACCUM, "the x sweep writes the residual");
+    if (w.kind == WENO_TILE) launch_tile<T, DIR, ACCUM>(c, q, r, s);
+    else if (w.kind == WENO_MARCH4) launch_march_x<T, 4>(c, q, r, w.seg, s);
+    else launch_march_x<T, 8>(c, q, r, w.seg, s);
   } else {
     if (w.kind == WENO_TILE) launch_tile<T, DIR, ACCUM>(c, q, r, s);
     else if (w.kind == WENO_MARCH4) launch_march<T, DIR, ACCUM, 4>(c, q, r, w.seg, s);
@@ -298,6 +420,8 @@ template <typename T, int DIR, bool ACCUM> static void attr_dir() {
   cudaFuncSetAttribute(k_weno<T, DIR, ACCUM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem<T, DIR>());
 }
 template <typename T> void setup_weno() {
+  cudaFuncSetAttribute(k_weno_march_x<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_x_smem<T, 4>());
+  cudaFuncSetAttribute(k_weno_march_x<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_x_smem<T, 8>());
   attr_dir<T, 0, false>();
   attr_dir<T, 1, true>();
   attr_dir<T, 2, true>();

@@ -30,10 +30,6 @@
 
 namespace osb {
 
-template <typename T> __device__ __forceinline__ T rcp_t(T x);
-template <> __device__ __forceinline__ float rcp_t<float>(float x) { return __fdividef(1.0f, x); }
-template <> __device__ __forceinline__ double rcp_t<double>(double x) { return 1.0 / x; }
-
 // sqrt(x) and 1/sqrt(x) of a positive x: FP32 from the hardware reciprocal square root (one SFU
 // operation), FP64 from the correctly rounded square root and one exact division
 __device__ __forceinline__ void sqrt_rsqrt(float x, float &s, float &is) {

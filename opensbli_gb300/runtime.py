@@ -77,7 +77,8 @@ EXPORTS = (
     "osb_query_layout", "osb_create", "osb_bind_field", "osb_set_stream", "osb_init_tgv", "osb_set_state64",
     "osb_set_state64_padded", "osb_set_coordinate",
     "osb_get_state64", "osb_step", "osb_residual", "osb_reduce", "osb_launch_count", "osb_profile", "osb_profile_read",
-    "osb_set_weno_shape", "osb_get_weno_shape", "osb_autotune", "osb_get_error", "osb_destroy",
+    "osb_set_weno_shape", "osb_get_weno_shape", "osb_set_central_shape", "osb_get_central_shape", "osb_autotune",
+    "osb_get_error", "osb_destroy",
 )
 # launch shapes of the WENO flux kernels (osb_set_weno_shape)
 WENO_SHAPES = {"tile": 0, "march4": 1, "march8": 2}
@@ -120,6 +121,8 @@ def load(build_if_missing=True):
     lib.osb_profile_read.argtypes = [vp, ctypes.POINTER(dp), ctypes.POINTER(ctypes.c_int64), ip]
     lib.osb_set_weno_shape.argtypes = [vp, ip, ip, ip]
     lib.osb_get_weno_shape.argtypes = [vp, ip, ctypes.POINTER(ip), ctypes.POINTER(ip)]
+    lib.osb_set_central_shape.argtypes = [vp, ip]
+    lib.osb_get_central_shape.argtypes = [vp, ctypes.POINTER(ip)]
     lib.osb_autotune.argtypes = [vp, ip, ctypes.POINTER(dp)]
     lib.osb_get_error.argtypes = [vp, ctypes.c_char_p, ip]
     lib.osb_destroy.argtypes = [vp]
@@ -312,16 +315,30 @@ class Solver:
         self._check(self.lib.osb_get_weno_shape(self.ctx, int(d), ctypes.byref(k), ctypes.byref(sg)))
         return {v: n for n, v in WENO_SHAPES.items()}[k.value], sg.value
 
+    def set_central_shape(self, ty):
+        """Tile height (8 or 16) of the fused central/RK kernel."""
+        self._check(self.lib.osb_set_central_shape(self.ctx, int(ty)))
+
+    def central_shape(self):
+        ty = ctypes.c_int()
+        self._check(self.lib.osb_get_central_shape(self.ctx, ctypes.byref(ty)))
+        return ty.value
+
     def autotune(self, reps=5):
-        """Time the candidate launch shapes on the bound state and keep the fastest per direction;
-        returns {dir: (kind, seg, ms per launch)} (empty for plans without WENO fluxes)."""
-        best = (ctypes.c_double * 3)()
+        """Time the candidate launch shapes on the bound state and keep the fastest; returns
+        {"weno_x"|"weno_y"|"weno_z": (kind, seg, ms per launch), "central": (ty, ms per launch)}
+        for the kernels the plan uses (empty for 2D plans)."""
+        best = (ctypes.c_double * 4)()
         self._in()
         self._check(self.lib.osb_autotune(self.ctx, int(reps), best))
         self._out()
-        if self.plan.ndim != 3 or self.plan.conv != "weno5js":
+        if self.plan.ndim != 3:
             return {}
-        return {d: self.weno_shape(d) + (best[d],) for d in range(3)}
+        out = {"central": (self.central_shape(), best[3])}
+        if self.plan.conv == "weno5js":
+            for d, name in enumerate(("weno_x", "weno_y", "weno_z")):
+                out[name] = self.weno_shape(d) + (best[d],)
+        return out
 
     def close(self):
         if getattr(self, "ctx", None):
