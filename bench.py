@@ -386,13 +386,89 @@ def own_arm(args, world, rank, local):
         print(json.dumps(line), flush=True)
 
 
+def adjoint_arm(args, world, rank, local):
+    """Gradient of the volume-integrated kinetic energy at T = 2 with respect to the initial velocity
+    field, 3D Taylor-Green 128^3, Re = 1600, Mach 0.1, central scheme, FP64, checkpoints every 20
+    steps.  dt = 2.5e-3 (800 steps): the stated 400 steps of 5e-3 exceed the acoustic stability
+    limit of the scheme at 128^3 (|lambda|_max dt ~ 2.7 > sqrt(3)).  Reports gradient throughput
+    (cell-steps per second of forward + checkpointed adjoint) and directional derivatives against
+    central finite differences (h = 1e-6) along seeded random directions."""
+    import torch
+    from opensbli_gb300.adjoint import Rollout, kinetic_energy, state_from_velocity, tgv_base
+    from opensbli_gb300.plan import tgv_plan
+    from opensbli_gb300.runtime import Solver
+
+    torch.cuda.set_device(local)
+    n = args.n or 128
+    T_end, every = 2.0, 20
+    nsteps = args.adj_steps or 800
+    dt = T_end / nsteps
+    plan = tgv_plan(n, conv="central_skew", precision="fp64", Minf=0.1, Re=1600.0)
+    s = Solver(plan)
+    p, rho, base = tgv_base(plan, s.device)
+    cells = plan.cells
+
+    def J_of(vel):
+        s.set_state64(state_from_velocity(vel, p, rho, plan.gama))
+        s.step(nsteps, dt)
+        return float(kinetic_energy(s.state64(), plan.delta))
+
+    J_of(base)  # warm-up (graph capture, scratch allocation)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J0 = J_of(base)
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+
+    def grad():
+        v = base.clone().requires_grad_(True)
+        qT = Rollout.apply(state_from_velocity(v, p, rho, plan.gama), s, nsteps, dt, every)
+        J = kinetic_energy(qT, plan.delta)
+        J.backward()
+        return float(J.detach()), v.grad.detach()
+
+    grad()  # warm-up of the adjoint scratch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J, g = grad()
+    torch.cuda.synchronize()
+    t_grad = time.perf_counter() - t0
+    fd = []
+    for seed in range(args.fd_dirs):
+        d = torch.randn(base.shape, generator=torch.Generator(device=s.device).manual_seed(seed), device=s.device,
+                        dtype=torch.float64)
+        h = 1e-6
+        f = (J_of(base + h * d) - J_of(base - h * d)) / (2 * h)
+        a = float((g * d).sum())
+        fd.append({"seed": seed, "fd": f, "adjoint": a, "rel_err": abs(f - a) / abs(a)})
+    s.close()
+    if rank == 0:
+        line = {"metric": "gradient cell-steps/s (forward + checkpointed adjoint)", "value": cells * nsteps / t_grad,
+                "unit": "cell-steps/s", "n_gpus": world, "steps": nsteps, "warmup": 1,
+                "ms_per_step": 1e3 * t_grad / nsteps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic: the problem's analytic initial condition",
+                "config": {"workload": "adjoint of 3D Taylor-Green %d^3, Re=1600, Mach 0.1, central 4th-order, RK3, "
+                                       "J = volume-integrated kinetic energy at T=2, gradient w.r.t. the initial "
+                                       "velocity field, checkpoints every %d steps" % (n, every),
+                           "grid": [n, n, n], "dt": dt, "nsteps": nsteps, "T": T_end,
+                           "dt_note": "400 steps of 5e-3 exceed the scheme's acoustic stability limit at 128^3"},
+                "J": J, "J_forward_only": J0, "forward_ms_per_step": 1e3 * t_fwd / nsteps,
+                "gradient_over_forward": t_grad / t_fwd,
+                "fd_check": {"h": 1e-6, "directions": len(fd),
+                             "max_rel_err": max((r["rel_err"] for r in fd), default=None), "dirs": fd}}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
-    ap.add_argument("--config", default="tgv_weno256", choices=["tgv_weno256", "tgv_central64", "katzer512"])
+    ap.add_argument("--config", default="tgv_weno256",
+                    choices=["tgv_weno256", "tgv_central64", "katzer512", "tgv_adjoint128"])
+    ap.add_argument("--adj-steps", type=int, default=None, help="tgv_adjoint128: RK3 steps to T=2 (default 800)")
+    ap.add_argument("--fd-dirs", type=int, default=16, help="tgv_adjoint128: finite-difference directions")
     ap.add_argument("--n", type=int, default=None)
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--ref-steps", type=int, default=None,
@@ -402,7 +478,13 @@ def main():
     if args.ref_steps is None:
         args.ref_steps = 2 if args.config == "tgv_weno256" else 40
     world, rank, local = dist_init()
-    if args.impl == "reference":
+    if args.config == "tgv_adjoint128":
+        if args.impl == "reference":
+            if rank == 0:
+                print(json.dumps({"impl": "reference", "unavailable": "the reference has no adjoint of its time loop"}))
+        else:
+            adjoint_arm(args, world, rank, local)
+    elif args.impl == "reference":
         ref_arm(args, world, rank)
     else:
         own_arm(args, world, rank, local)

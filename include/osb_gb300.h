@@ -184,6 +184,16 @@ int osb_set_central_shape(osb_ctx *ctx, int ty);
 int osb_get_central_shape(osb_ctx *ctx, int *ty);
 int osb_autotune(osb_ctx *ctx, int reps, double *best_ms);
 
+/* Discrete adjoint of the time loop.  No counterpart in the reference.  FP64 3D plans with central
+ * skew-symmetric fluxes and periodic boundaries (viscous terms as the plan says); other plans get
+ * OSB_EUNSUPPORTED.  Arrays are device FP64, dense interior [5][n2][n1][n0].
+ * osb_adjoint_residual: out = (dR/dq)^T lam at the bound state.
+ * osb_adjoint_step: lam_out = (dPhi/dq)^T lam_in, Phi = one 2-register RK3 step of size dt from the
+ * bound state, whose stage states are recomputed; the bound state itself is left unchanged.
+ * The first call allocates the adjoint scratch (about 57 padded fields + 15 interior fields). */
+int osb_adjoint_residual(osb_ctx *ctx, const double *lam, double *out);
+int osb_adjoint_step(osb_ctx *ctx, double dt, const double *lam_in, double *lam_out);
+
 int osb_get_error(osb_ctx *ctx, char *buf, int n);
 void osb_destroy(osb_ctx *ctx);
 

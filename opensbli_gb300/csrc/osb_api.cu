@@ -918,6 +918,34 @@ template <typename T> static int autotune_impl(osb_ctx *c, int reps, double *bes
 
 extern "C" {
 
+static int adjoint_check(osb_ctx *c) {
+  if (!c) return OSB_EINVAL;
+  const osb_plan_desc &p = c->plan;
+  if (p.ndim != 3 || c->mixed || p.conv != OSB_CONV_CENTRAL_SKEW)
+    return set_err(c, OSB_EUNSUPPORTED, "adjoint: FP64 3D plans with central skew-symmetric fluxes only");
+  for (int d = 0; d < 3; ++d)
+    if (p.bc[d][0] != OSB_BC_PERIODIC || p.bc[d][1] != OSB_BC_PERIODIC)
+      return set_err(c, OSB_EUNSUPPORTED, "adjoint: periodic boundaries only");
+  int rc = check_bound(c);
+  if (rc) return rc;
+  return cuda_err(c, adj_ensure(*c), "adjoint scratch allocation");
+}
+
+int osb_adjoint_residual(osb_ctx *c, const double *lam, double *out) {
+  int rc = adjoint_check(c);
+  if (rc) return rc;
+  if (!lam || !out) return set_err(c, OSB_EINVAL, "osb_adjoint_residual: null array");
+  return cuda_err(c, adj_residual(*c, fields<double>(c->cur == 0 ? c->qa : c->qb), lam, out), "osb_adjoint_residual");
+}
+
+int osb_adjoint_step(osb_ctx *c, double dt, const double *lam_in, double *lam_out) {
+  int rc = adjoint_check(c);
+  if (rc) return rc;
+  if (!lam_in || !lam_out) return set_err(c, OSB_EINVAL, "osb_adjoint_step: null array");
+  return cuda_err(c, adj_step(*c, fields<double>(c->cur == 0 ? c->qa : c->qb), dt, lam_in, lam_out),
+                  "osb_adjoint_step");
+}
+
 int osb_set_central_shape(osb_ctx *c, int ty) {
   if (!c) return OSB_EINVAL;
   if (ty != 8 && ty != 16) return set_err(c, OSB_EINVAL, "osb_set_central_shape: ty must be 8 or 16");
@@ -960,6 +988,7 @@ void osb_destroy(osb_ctx *c) {
     cudaFree(c->res[v]);
   }
   cudaFree(c->red);
+  cudaFree(c->adj);
   for (int v = 0; v < 4; ++v) {
     if (c->mixed) cudaFree(c->q64_2d[v]);
     cudaFree(c->du2[v]);

@@ -37,6 +37,7 @@ struct Ctx {
   int64_t launches = 0;
   WenoCfg wcfg[3] = {{WENO_TILE, 32}, {WENO_TILE, 32}, {WENO_TILE, 32}};
   int crk_ty = 8;             // tile height of the fused central/RK kernel (8 or 16)
+  double *adj = nullptr;      // adjoint scratch (stage states, primitives, sensitivity fields)
   int num_sms = 152;          // multiprocessors of the device (set at creation)
   int64_t graph_launches = 0;  // kernel launches recorded in one captured step
   int qold_valid = 0;          // the FP64 register holds the current state
@@ -80,6 +81,12 @@ void launch2_metrics(const Ctx &c, const double *x1, cudaStream_t s, int64_t *la
 void launch2_bcs(const Ctx &c, cudaStream_t s, int64_t *launches);
 template <typename T>
 void launch2_rhs(const Ctx &c, int update, double A, double B, double dt, cudaStream_t s, int64_t *launches);
+
+// discrete adjoint of the periodic central scheme (FP64 plans)
+cudaError_t adj_ensure(Ctx &c);
+cudaError_t adj_residual(Ctx &c, Fields5<double> q, const double *lam, double *out);
+cudaError_t adj_step(Ctx &c, Fields5<double> q, double dt, const double *lam_in, double *lam_out);
+void adj_halos(const Ctx &c, double *const *f, int nf, cudaStream_t s, int64_t *launches);
 
 // mode bits for launch_central_rk
 constexpr int CRK_SKEW = 1;      // add skew-symmetric central convective terms

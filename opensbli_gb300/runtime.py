@@ -78,7 +78,7 @@ EXPORTS = (
     "osb_set_state64_padded", "osb_set_coordinate",
     "osb_get_state64", "osb_step", "osb_residual", "osb_reduce", "osb_launch_count", "osb_profile", "osb_profile_read",
     "osb_set_weno_shape", "osb_get_weno_shape", "osb_set_central_shape", "osb_get_central_shape", "osb_autotune",
-    "osb_get_error", "osb_destroy",
+    "osb_adjoint_residual", "osb_adjoint_step", "osb_get_error", "osb_destroy",
 )
 # launch shapes of the WENO flux kernels (osb_set_weno_shape)
 WENO_SHAPES = {"tile": 0, "march4": 1, "march8": 2}
@@ -124,6 +124,8 @@ def load(build_if_missing=True):
     lib.osb_set_central_shape.argtypes = [vp, ip]
     lib.osb_get_central_shape.argtypes = [vp, ctypes.POINTER(ip)]
     lib.osb_autotune.argtypes = [vp, ip, ctypes.POINTER(dp)]
+    lib.osb_adjoint_residual.argtypes = [vp, vp, vp]
+    lib.osb_adjoint_step.argtypes = [vp, dp, vp, vp]
     lib.osb_get_error.argtypes = [vp, ctypes.c_char_p, ip]
     lib.osb_destroy.argtypes = [vp]
     lib.osb_destroy.restype = None
@@ -338,6 +340,36 @@ class Solver:
         if self.plan.conv == "weno5js":
             for d, name in enumerate(("weno_x", "weno_y", "weno_z")):
                 out[name] = self.weno_shape(d) + (best[d],)
+        return out
+
+    # -- discrete adjoint (FP64 periodic central plans)
+    def _dense64(self, a):
+        shape = (self.layout.nvar,) + self.shape
+        t = torch.as_tensor(a, dtype=torch.float64).to(self.device).reshape(shape).contiguous()
+        return t
+
+    def adjoint_residual(self, lam):
+        """(dR/dq)^T lam at the bound state; lam FP64 [5][z][y][x]."""
+        lam = self._dense64(lam)
+        self._in()
+        with torch.cuda.stream(self.stream):
+            out = torch.empty_like(lam)
+        self._check(self.lib.osb_adjoint_residual(self.ctx, ctypes.c_void_p(lam.data_ptr()),
+                                                  ctypes.c_void_p(out.data_ptr())))
+        lam.record_stream(self.stream)
+        self._out()
+        return out
+
+    def adjoint_step(self, lam, dt):
+        """(dPhi/dq)^T lam for one RK3 step Phi of size dt from the bound state (left unchanged)."""
+        lam = self._dense64(lam)
+        self._in()
+        with torch.cuda.stream(self.stream):
+            out = torch.empty_like(lam)
+        self._check(self.lib.osb_adjoint_step(self.ctx, float(dt), ctypes.c_void_p(lam.data_ptr()),
+                                              ctypes.c_void_p(out.data_ptr())))
+        lam.record_stream(self.stream)
+        self._out()
         return out
 
     def close(self):

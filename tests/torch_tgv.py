@@ -34,7 +34,7 @@ def d2(f, d, idl):
 
 
 class Params:
-    def __init__(self, n, gama=1.4, Minf=0.1, Re=1600.0, Pr=0.71):
+    def __init__(self, n, gama=1.4, Minf=0.1, Re=1600.0, Pr=0.71, viscous=True):
         self.n = n
         self.delta = tuple(2 * math.pi / k for k in n)
         self.idl = tuple(1.0 / dd for dd in self.delta)
@@ -43,6 +43,8 @@ class Params:
         self.gM2 = gama * Minf * Minf
         self.invRe = 1.0 / Re
         self.kT = 1.0 / ((gama - 1.0) * Minf * Minf * Pr * Re)
+        if not viscous:
+            self.invRe = self.kT = 0.0
 
 
 def rhs(q, P):
