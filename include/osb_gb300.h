@@ -197,6 +197,32 @@ int osb_adjoint_step(osb_ctx *ctx, double dt, const double *lam_in, double *lam_
 int osb_get_error(osb_ctx *ctx, char *buf, int n);
 void osb_destroy(osb_ctx *ctx);
 
+/* Batched ensembles.  No counterpart in the reference (one block per process there).  n independent
+ * 3D periodic plans (central skew-symmetric or WENO5-JS fluxes, RK3, one precision for all, sizes
+ * free) stepped together: per RK3 stage, one launch per halo axis and persistent tile-queue launches
+ * for the WENO directions and the fused central/RK update, all instances at once; each step is one
+ * CUDA graph on the batch's stream (osb_batch_set_stream).  The batch owns its device memory.
+ * States are FP64 dense interior [5][n2][n1][n0] device arrays; every instance has its own dt
+ * (osb_batch_set_dt, a host array of n values, before the first step).  Batches whose steps overlap
+ * in time must use the same stream (the kernels share one constant-memory descriptor table).
+ * osb_batch_autotune times the WENO line-marching shapes (4 or 8 lines per block, segment length)
+ * and the central tile (height 8/16, z-planes per tile) over the whole batch; best_ms[0..3] (may be
+ * NULL) receives the chosen shapes' times per launch (WENO x, y, z, central).  osb_batch_get_shape
+ * fills out[0..7] = {kind_x, seg_x, kind_y, seg_y, kind_z, seg_z, central ty, central z-planes}.
+ * More instances than the descriptor table holds give OSB_ETOOLARGE. */
+typedef struct osb_batch osb_batch;
+int osb_batch_create(const osb_plan_desc *plans, int n, osb_batch **out);
+int osb_batch_set_stream(osb_batch *batch, void *stream);
+int osb_batch_set_dt(osb_batch *batch, const double *dt);
+int osb_batch_set_state64(osb_batch *batch, int inst, const double *dev_interior);
+int osb_batch_get_state64(osb_batch *batch, int inst, double *dev_interior);
+int osb_batch_step(osb_batch *batch, int nsteps);
+int osb_batch_autotune(osb_batch *batch, int reps, double *best_ms);
+int osb_batch_get_shape(osb_batch *batch, int *out, int n);
+int64_t osb_batch_launch_count(osb_batch *batch);
+int osb_batch_get_error(osb_batch *batch, char *buf, int n);
+void osb_batch_destroy(osb_batch *batch);
+
 /* Allocation-free variant of osb_reduce.  This entry point has no counterpart in the reference; it is
  * for callers that cannot allocate device memory where they want a diagnostic (a host framework
  * whose device memory belongs to a pool allocator, a monitoring hook between time steps).  It needs

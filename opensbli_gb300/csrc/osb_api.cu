@@ -491,6 +491,34 @@ __global__ void k_reduce2(Grid g, D4 q, int what, double *partial) {
 
 }  // namespace
 
+namespace osb {
+int plan_validate(const osb_plan_desc *p, char *why, size_t n) { return validate(p, why, n); }
+Grid plan_grid(const osb_plan_desc *p) { return make_grid(p); }
+Phys plan_phys(const osb_plan_desc *plan) {
+  Phys ph{};
+  ph.gama = plan->gama;
+  ph.Minf = plan->Minf;
+  ph.Re = plan->Re;
+  ph.Pr = plan->Pr;
+  for (int d = 0; d < 3; ++d) ph.inv_delta[d] = 1.0 / plan->delta[d];
+  ph.weno_eps = plan->weno_eps > 0 ? plan->weno_eps : 1e-6;
+  ph.gm1 = plan->gama - 1.0;
+  ph.igm1 = 1.0 / ph.gm1;
+  ph.gM2 = plan->Minf * plan->Minf * plan->gama;
+  ph.invRe = 1.0 / plan->Re;
+  ph.kT = 1.0 / ((plan->gama - 1.0) * plan->Minf * plan->Minf * plan->Pr * plan->Re);
+  ph.f_gama = (float)ph.gama;
+  ph.f_gm1 = (float)ph.gm1;
+  ph.f_igm1 = (float)ph.igm1;
+  ph.f_gM2 = (float)ph.gM2;
+  ph.f_invRe = (float)ph.invRe;
+  ph.f_kT = (float)ph.kT;
+  ph.f_eps = (float)ph.weno_eps;
+  for (int d = 0; d < 3; ++d) ph.f_inv_delta[d] = (float)ph.inv_delta[d];
+  return ph;
+}
+}  // namespace osb
+
 extern "C" {
 
 static int check_bound(osb_ctx *c);
@@ -555,25 +583,7 @@ int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
   c->g = make_grid(plan);
   c->mixed = plan->precision == OSB_PREC_MIXED;
   c->elem = c->mixed ? 4 : 8;
-  c->ph.gama = plan->gama;
-  c->ph.Minf = plan->Minf;
-  c->ph.Re = plan->Re;
-  c->ph.Pr = plan->Pr;
-  for (int d = 0; d < 3; ++d) c->ph.inv_delta[d] = 1.0 / plan->delta[d];
-  c->ph.weno_eps = plan->weno_eps > 0 ? plan->weno_eps : 1e-6;
-  c->ph.gm1 = plan->gama - 1.0;
-  c->ph.igm1 = 1.0 / c->ph.gm1;
-  c->ph.gM2 = plan->Minf * plan->Minf * plan->gama;
-  c->ph.invRe = 1.0 / plan->Re;
-  c->ph.kT = 1.0 / ((plan->gama - 1.0) * plan->Minf * plan->Minf * plan->Pr * plan->Re);
-  c->ph.f_gama = (float)c->ph.gama;
-  c->ph.f_gm1 = (float)c->ph.gm1;
-  c->ph.f_igm1 = (float)c->ph.igm1;
-  c->ph.f_gM2 = (float)c->ph.gM2;
-  c->ph.f_invRe = (float)c->ph.invRe;
-  c->ph.f_kT = (float)c->ph.kT;
-  c->ph.f_eps = (float)c->ph.weno_eps;
-  for (int d = 0; d < 3; ++d) c->ph.f_inv_delta[d] = (float)c->ph.inv_delta[d];
+  c->ph = plan_phys(plan);
   const size_t bytes = (size_t)c->g.numel * c->elem;
   cudaError_t e = cudaSuccess;
   if (plan->ndim == 2) {

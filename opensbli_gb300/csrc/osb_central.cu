@@ -47,15 +47,17 @@ template <typename T, int MODE, int TY> constexpr size_t ring_bytes() {
 }
 }  // namespace
 
+// One tile: output points (bx*32 .. +31, by*TY .. +TY-1) for the z-planes of chunk bz.  Called by
+// the per-block kernel below and by the batched persistent kernel (osb_batch.cu).
 template <typename T, int MODE, int TY>
-__global__ void __launch_bounds__(TX * TY, central_min_blocks<T, MODE, TY>()) k_central_rk(Grid g, Fields5<const T> q, Fields5<T> qnew,
-                                                        Fields5<double> qold, Fields5<T> rin, Fields5<T> rout, Phys ph,
-                                                        double dt_new, double dt_old, int zchunk) {
+__device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold,
+                                             Fields5<T> rin, Fields5<T> rout, const Phys &ph, double dt_new,
+                                             double dt_old, int zchunk, int bx, int by, int bz,
+                                             unsigned char *smem_raw) {
   constexpr int NF = ring_fields<MODE>(), PY = TY + 4;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   T *ring = reinterpret_cast<T *>(smem_raw);  // [NP][NF][PY][PX]
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
-  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, k0 = blockIdx.z * zchunk;
+  const int i0 = bx * TX, j0 = by * TY, k0 = bz * zchunk;
   const int k1 = min(k0 + zchunk, g.n2);
   const T gm1 = pick<T>(ph.gm1, ph.f_gm1);
   const T gM2 = pick<T>(ph.gM2, ph.f_gM2);
@@ -286,6 +288,15 @@ __global__ void __launch_bounds__(TX * TY, central_min_blocks<T, MODE, TY>()) k_
   }
 }
 
+template <typename T, int MODE, int TY>
+__global__ void __launch_bounds__(TX * TY, central_min_blocks<T, MODE, TY>())
+    k_central_rk(Grid g, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold, Fields5<T> rin, Fields5<T> rout,
+                 Phys ph, double dt_new, double dt_old, int zchunk) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  central_tile<T, MODE, TY>(g, q, qnew, qold, rin, rout, ph, dt_new, dt_old, zchunk, blockIdx.x, blockIdx.y, blockIdx.z,
+                            smem_raw);
+}
+
 // resident blocks per SM of one kernel instance (occupancy calculator, cached per instance)
 template <typename T, int MODE, int TY> static int resident_per_sm() {
   static int nb = [] {
@@ -349,6 +360,7 @@ template <typename T, int MODE> static void attr_mode() {
   cudaFuncSetAttribute(k_central_rk<T, MODE, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)ring_bytes<T, MODE, 16>());
 }
+template <typename T> static void attr_batch();
 template <typename T> void setup_central() {
   attr_mode<T, CRK_SKEW | CRK_VISC | CRK_UPDATE>();
   attr_mode<T, CRK_SKEW | CRK_VISC>();
@@ -358,9 +370,122 @@ template <typename T> void setup_central() {
   attr_mode<T, CRK_VISC | CRK_RIN>();
   attr_mode<T, CRK_RIN | CRK_UPDATE>();
   attr_mode<T, CRK_RIN>();
+  attr_batch<T>();
 }
+// Descriptor table of the batch being stepped, in this module's constant memory: the persistent
+// kernels read an instance's grid, constants and pointers through the constant cache (uniform per
+// block), so they cost no registers.  batch_table_upload_central copies a device-resident table here,
+// stream-ordered (capturable); batches stepping at the same time must share one stream.
+static __constant__ __align__(16) unsigned char c_batch_table[BATCH_TABLE_BYTES];
+
+cudaError_t batch_table_upload_central(const void *src_dev, size_t bytes, cudaStream_t s) {
+  if (bytes > BATCH_TABLE_BYTES) return cudaErrorInvalidValue;
+  return cudaMemcpyToSymbolAsync(c_batch_table, src_dev, bytes, 0, cudaMemcpyDeviceToDevice, s);
+}
+
+// ---------------------------------------------------------------------------------------------
+// batched ensemble: one persistent launch per kernel mode over the tiles of every instance that
+// uses that mode (items {instance, bx, by, bz} taken from a tile queue)
+// ---------------------------------------------------------------------------------------------
+template <typename T, int MODE, int TY>
+__global__ void __launch_bounds__(TX * TY, central_min_blocks<T, MODE, TY>())
+    k_batch_central(const int4 *items, int nitems, int *counter, int parity, double ca,
+                    double cb) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int slot;
+  for (;;) {
+    const int it = next_item(counter, &slot);
+    if (it >= nitems) return;
+    const int4 w = items[it];
+    const BatchInst<T> &d = reinterpret_cast<const BatchInst<T> *>(c_batch_table)[w.x];
+    Fields5<const T> q;
+    Fields5<T> qn, r;
+    Fields5<double> qo;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      q.v[v] = d.q[parity][v];
+      qn.v[v] = d.q[parity ^ 1][v];
+      r.v[v] = d.res[v];
+      qo.v[v] = d.qold[v];
+    }
+    central_tile<T, MODE, TY>(d.g, q, qn, qo, r, r, d.ph, d.dt * cb, d.dt * ca, d.zchunk, w.y, w.z, w.w, smem_raw);
+  }
+}
+
+template <typename T, int MODE, int TY> static int occ_batch() {
+  int b = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_central<T, MODE, TY>, TX * TY,
+                                                    ring_bytes<T, MODE, TY>()) != cudaSuccess || b < 1)
+    b = 1;
+  return b;
+}
+
+// mode: CRK_SKEW or CRK_RIN, with CRK_VISC as the plan says; CRK_UPDATE is implied
+template <typename T> int batch_central_blocks_per_sm(int mode, int ty) {
+  const int m = mode | CRK_UPDATE;
+#define OSB_OCC(M) \
+  if (m == (M)) return ty == 16 ? occ_batch<T, M, 16>() : occ_batch<T, M, 8>();
+  OSB_OCC(CRK_SKEW | CRK_VISC | CRK_UPDATE)
+  OSB_OCC(CRK_SKEW | CRK_UPDATE)
+  OSB_OCC(CRK_RIN | CRK_VISC | CRK_UPDATE)
+  OSB_OCC(CRK_RIN | CRK_UPDATE)
+#undef OSB_OCC
+  return 1;
+}
+
+template <typename T, int MODE>
+static void batch_mode(const int4 *items, int nitems, int *counter, int parity, double ca,
+                       double cb, int ty, int nblocks, cudaStream_t s) {
+  if (ty == 16)
+    k_batch_central<T, MODE, 16><<<nblocks, dim3(TX, 16), ring_bytes<T, MODE, 16>(), s>>>(items, nitems, counter,
+                                                                                          parity, ca, cb);
+  else
+    k_batch_central<T, MODE, 8><<<nblocks, dim3(TX, 8), ring_bytes<T, MODE, 8>(), s>>>(items, nitems, counter,
+                                                                                        parity, ca, cb);
+}
+
+template <typename T>
+void launch_batch_central(const int4 *items, int nitems, int *counter, int parity, double ca,
+                          double cb, int mode, int ty, int nblocks, cudaStream_t s) {
+  switch (mode | CRK_UPDATE) {
+    case CRK_SKEW | CRK_VISC | CRK_UPDATE:
+      batch_mode<T, CRK_SKEW | CRK_VISC | CRK_UPDATE>(items, nitems, counter, parity, ca, cb, ty, nblocks, s);
+      break;
+    case CRK_SKEW | CRK_UPDATE:
+      batch_mode<T, CRK_SKEW | CRK_UPDATE>(items, nitems, counter, parity, ca, cb, ty, nblocks, s);
+      break;
+    case CRK_RIN | CRK_VISC | CRK_UPDATE:
+      batch_mode<T, CRK_RIN | CRK_VISC | CRK_UPDATE>(items, nitems, counter, parity, ca, cb, ty, nblocks, s);
+      break;
+    case CRK_RIN | CRK_UPDATE:
+      batch_mode<T, CRK_RIN | CRK_UPDATE>(items, nitems, counter, parity, ca, cb, ty, nblocks, s);
+      break;
+    default:
+      break;
+  }
+}
+
+template <typename T, int MODE> static void attr_batch_mode() {
+  cudaFuncSetAttribute(k_batch_central<T, MODE, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)ring_bytes<T, MODE, 8>());
+  cudaFuncSetAttribute(k_batch_central<T, MODE, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)ring_bytes<T, MODE, 16>());
+}
+template <typename T> static void attr_batch() {
+  attr_batch_mode<T, CRK_SKEW | CRK_VISC | CRK_UPDATE>();
+  attr_batch_mode<T, CRK_SKEW | CRK_UPDATE>();
+  attr_batch_mode<T, CRK_RIN | CRK_VISC | CRK_UPDATE>();
+  attr_batch_mode<T, CRK_RIN | CRK_UPDATE>();
+}
+
 template void setup_central<float>();
 template void setup_central<double>();
+template int batch_central_blocks_per_sm<float>(int, int);
+template int batch_central_blocks_per_sm<double>(int, int);
+template void launch_batch_central<float>(const int4 *, int, int *, int, double, double, int,
+                                          int, int, cudaStream_t);
+template void launch_batch_central<double>(const int4 *, int, int *, int, double, double,
+                                           int, int, int, cudaStream_t);
 
 template void launch_central_rk<float>(const Ctx &, Fields5<const float>, Fields5<float>, Fields5<double>,
                                        Fields5<float>, Fields5<float>, double, double, int, cudaStream_t, int64_t *);

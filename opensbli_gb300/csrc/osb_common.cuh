@@ -54,4 +54,31 @@ template <> __device__ __forceinline__ double rcp_t<double>(double x) { return 1
 template <typename T> __device__ __forceinline__ T abs_t(T x) { return x < T(0) ? -x : x; }
 template <typename T> __device__ __forceinline__ T max_t(T a, T b) { return a > b ? a : b; }
 
+// Tile queue of the persistent batched kernels: one thread of the block takes the next item index
+// from a global counter (atomicAdd, never waits); all threads then read it.
+__device__ __forceinline__ int next_item(int *counter, int *slot) {
+  __syncthreads();  // every thread is done with the previous item index
+  if (threadIdx.x == 0 && threadIdx.y == 0) *slot = atomicAdd(counter, 1);
+  __syncthreads();
+  return *slot;
+}
+
+// bytes of the constant-memory descriptor table of a batch (BatchInst entries)
+constexpr size_t BATCH_TABLE_BYTES = 56 * 1024;
+
+// One instance of a batched ensemble: its grid, constants, ping-pong state buffers, residual and
+// FP64 RK register (all padded, as for a single plan), time step and scheme.
+template <typename T> struct BatchInst {
+  Grid g;
+  Phys ph;
+  T *q[2][5];
+  T *res[5];
+  double *qold[5];
+  double dt;
+  int conv;    // OSB_CONV_CENTRAL_SKEW or OSB_CONV_WENO5JS
+  int visc;    // 1: constant-viscosity viscous terms
+  int zchunk;  // z-planes per central-kernel tile
+  int pad;
+};
+
 }  // namespace osb

@@ -61,6 +61,11 @@ struct Ctx {
   int64_t prof_n[8] = {};
 };
 
+// plan checks and derived layout/constants (osb_api.cu)
+int plan_validate(const osb_plan_desc *p, char *why, size_t n);
+Grid plan_grid(const osb_plan_desc *p);
+Phys plan_phys(const osb_plan_desc *p);
+
 // kernel families reported by osb_profile_read
 enum { PF_HALO = 0, PF_WENO_X, PF_WENO_Y, PF_WENO_Z, PF_CENTRAL_RK, PF_OTHER, PF_COUNT };
 
@@ -81,6 +86,18 @@ void launch2_metrics(const Ctx &c, const double *x1, cudaStream_t s, int64_t *la
 void launch2_bcs(const Ctx &c, cudaStream_t s, int64_t *launches);
 template <typename T>
 void launch2_rhs(const Ctx &c, int update, double A, double B, double dt, cudaStream_t s, int64_t *launches);
+
+// batched ensemble kernels (persistent, tile queue): items are int4 {instance, bx, by, bz}
+cudaError_t batch_table_upload_central(const void *src_dev, size_t bytes, cudaStream_t s);
+cudaError_t batch_table_upload_weno(const void *src_dev, size_t bytes, cudaStream_t s);
+template <typename T>
+void launch_batch_central(const int4 *items, int nitems, int *counter, int parity, double ca,
+                          double cb, int mode, int ty, int nblocks, cudaStream_t s);
+template <typename T> int batch_central_blocks_per_sm(int mode, int ty);
+template <typename T>
+void launch_batch_weno(const int4 *items, int nitems, int *counter, int parity, int dir,
+                       int kind, int seg, int nblocks, cudaStream_t s);
+template <typename T> int batch_weno_blocks_per_sm(int dir, int kind);
 
 // discrete adjoint of the periodic central scheme (FP64 plans)
 cudaError_t adj_ensure(Ctx &c);

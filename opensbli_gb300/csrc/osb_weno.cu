@@ -188,14 +188,14 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
 // Line-marching flux kernel for DIR 1 (y) and 2 (z); block = 32 x-lanes by BY transverse lines,
 // blockIdx.z = segment of L cells along DIR.
 template <typename T, int DIR, bool ACCUM, int BY>
-__global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 512 : 256) / (32 * BY))
-    k_weno_march(Grid g, Fields5<const T> q, Fields5<T> res, Phys ph, int L) {
+__device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> q, Fields5<T> res, const Phys &ph,
+                                                int L, int bx, int by, int bz) {
   static_assert(DIR == 1 || DIR == 2, "marching runs along y or z");
-  const int i = blockIdx.x * 32 + threadIdx.x;
-  const int o = blockIdx.y * BY + threadIdx.y;  // k for DIR 1, j for DIR 2
+  const int i = bx * 32 + threadIdx.x;
+  const int o = by * BY + threadIdx.y;  // k for DIR 1, j for DIR 2
   const int nd = DIR == 1 ? g.n1 : g.n2, no = DIR == 1 ? g.n2 : g.n1;
   if (i >= g.n0 || o >= no) return;
-  const int c0 = blockIdx.z * L;
+  const int c0 = bz * L;
   const int c1 = min(c0 + L, nd);  // this thread finishes cells c0 .. c1-1
   const int64_t sd = DIR == 1 ? g.sy : g.sz;
   const int64_t mline = DIR == 1 ? gidx(g, i, 0, o) : gidx(g, i, o, 0);  // cell 0 of the line
@@ -248,6 +248,12 @@ __global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 512 : 256) / (32 * 
   }
 }
 
+template <typename T, int DIR, bool ACCUM, int BY>
+__global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 512 : 256) / (32 * BY))
+    k_weno_march(Grid g, Fields5<const T> q, Fields5<T> res, Phys ph, int L) {
+  weno_march_tile<T, DIR, ACCUM, BY>(g, q, res, ph, L, blockIdx.x, blockIdx.y, blockIdx.z);
+}
+
 // Line-marching flux kernel for x.  A warp owns 32 consecutive y-lines of one z-plane and walks a
 // segment of L cells along x; lane l computes line j0+l.  The conserved vectors arrive in chunks of
 // XC points of all 32 lines, loaded with the lanes spread along x (each row's XC values are
@@ -264,19 +270,18 @@ template <typename T> struct MX {
 };
 
 template <typename T, int BY>
-__global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 512 : 256) / (32 * BY))
-    k_weno_march_x(Grid g, Fields5<const T> q, Fields5<T> res, Phys ph, int L) {
+__device__ __forceinline__ void weno_march_x_tile(const Grid &g, Fields5<const T> q, Fields5<T> res, const Phys &ph,
+                                                  int L, int bx, int by, int bz, unsigned char *smem_raw) {
   using M = MX<T>;
   constexpr int XC = M::XC, RG = M::RG, QP = M::QP, RP = M::RP;
   constexpr int RPI = 32 / XC;  // rows covered by one load instruction
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x, w = threadIdx.y;
   T *qs = reinterpret_cast<T *>(smem_raw) + (size_t)w * M::WARP_ELEMS;  // [5][32][QP]
   T *rs = qs + 5 * 32 * QP;                                              // [5][32][RP]
-  const int j0 = blockIdx.y * 32, k = blockIdx.z * BY + w;
+  const int j0 = by * 32, k = bz * BY + w;
   if (k >= g.n2) return;  // uniform per warp
   const int n0 = g.n0, n1 = g.n1;
-  const int c0 = blockIdx.x * L, c1 = min(c0 + L, n0);  // cells c0 .. c1-1
+  const int c0 = bx * L, c1 = min(c0 + L, n0);  // cells c0 .. c1-1
   const int pfirst = c0 - 3, plast = c1 + 2;            // points of the segment's stencils
   const T gm1 = pick<T>(ph.gm1, ph.f_gm1), gama = pick<T>(ph.gama, ph.f_gama);
   const T igm1 = pick<T>(ph.igm1, ph.f_igm1), eps = pick<T>(ph.weno_eps, ph.f_eps);
@@ -357,6 +362,13 @@ __global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 512 : 256) / (32 * 
   }
 }
 
+template <typename T, int BY>
+__global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 512 : 256) / (32 * BY))
+    k_weno_march_x(Grid g, Fields5<const T> q, Fields5<T> res, Phys ph, int L) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  weno_march_x_tile<T, BY>(g, q, res, ph, L, blockIdx.x, blockIdx.y, blockIdx.z, smem_raw);
+}
+
 template <typename T, int DIR> constexpr size_t tile_smem() {
   using Tl = WTile<DIR>;
   return sizeof(T) * ((size_t)W_NF * (Tl::TI + 5) * Tl::TA + 5 * (DIR == 0 ? Tl::TA * Tl::FS : Tl::TI * Tl::TA));
@@ -416,10 +428,102 @@ void launch_weno_cfg(const Ctx &c, Fields5<const T> q, Fields5<T> r, int dir, We
   else launch_variant<T, 2, true>(c, q, r, w, s);
 }
 
+// Descriptor table of the batch being stepped, in this module's constant memory: the persistent
+// kernels read an instance's grid, constants and pointers through the constant cache (uniform per
+// block), so they cost no registers.  batch_table_upload_weno copies a device-resident table here,
+// stream-ordered (capturable); batches stepping at the same time must share one stream.
+static __constant__ __align__(16) unsigned char c_batch_table[BATCH_TABLE_BYTES];
+
+cudaError_t batch_table_upload_weno(const void *src_dev, size_t bytes, cudaStream_t s) {
+  if (bytes > BATCH_TABLE_BYTES) return cudaErrorInvalidValue;
+  return cudaMemcpyToSymbolAsync(c_batch_table, src_dev, bytes, 0, cudaMemcpyDeviceToDevice, s);
+}
+
+// ---------------------------------------------------------------------------------------------
+// batched ensemble: persistent launches over the line-marching tiles of every WENO instance
+// (items {instance, bx, by, bz} from a tile queue; segment length common to the batch)
+// ---------------------------------------------------------------------------------------------
+// The tile loop and the descriptor reads add live values to the line-marching bodies: these
+// kernels allow 3/4 of the single-plan kernels' resident threads (more registers, no spills).
+template <typename T, int BY>
+__global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 384 : 192) / (32 * BY))
+    k_batch_weno_x(const int4 *items, int nitems, int *counter, int parity, int L) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ int slot;
+  for (;;) {
+    const int it = next_item(counter, &slot);
+    if (it >= nitems) return;
+    const int4 w = items[it];
+    const BatchInst<T> &d = reinterpret_cast<const BatchInst<T> *>(c_batch_table)[w.x];
+    Fields5<const T> q;
+    Fields5<T> r;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      q.v[v] = d.q[parity][v];
+      r.v[v] = d.res[v];
+    }
+    weno_march_x_tile<T, BY>(d.g, q, r, d.ph, L, w.y, w.z, w.w, smem_raw);
+  }
+}
+
+template <typename T, int DIR, int BY>
+__global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 384 : 192) / (32 * BY))
+    k_batch_weno_yz(const int4 *items, int nitems, int *counter, int parity, int L) {
+  __shared__ int slot;
+  for (;;) {
+    const int it = next_item(counter, &slot);
+    if (it >= nitems) return;
+    const int4 w = items[it];
+    const BatchInst<T> &d = reinterpret_cast<const BatchInst<T> *>(c_batch_table)[w.x];
+    Fields5<const T> q;
+    Fields5<T> r;
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      q.v[v] = d.q[parity][v];
+      r.v[v] = d.res[v];
+    }
+    weno_march_tile<T, DIR, true, BY>(d.g, q, r, d.ph, L, w.y, w.z, w.w);
+  }
+}
+
+template <typename T> int batch_weno_blocks_per_sm(int dir, int kind) {
+  int b = 0;
+  cudaError_t e;
+  if (dir == 0)
+    e = kind == WENO_MARCH8
+            ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_weno_x<T, 8>, 256, march_x_smem<T, 8>())
+            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_weno_x<T, 4>, 128, march_x_smem<T, 4>());
+  else if (dir == 1)
+    e = kind == WENO_MARCH8 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_weno_yz<T, 1, 8>, 256, 0)
+                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_weno_yz<T, 1, 4>, 128, 0);
+  else
+    e = kind == WENO_MARCH8 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_weno_yz<T, 2, 8>, 256, 0)
+                            : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_batch_weno_yz<T, 2, 4>, 128, 0);
+  return (e != cudaSuccess || b < 1) ? 1 : b;
+}
+
+template <typename T>
+void launch_batch_weno(const int4 *items, int nitems, int *counter, int parity, int dir,
+                       int kind, int seg, int nblocks, cudaStream_t s) {
+  const bool by8 = kind == WENO_MARCH8;
+  if (dir == 0) {
+    if (by8) k_batch_weno_x<T, 8><<<nblocks, dim3(32, 8), march_x_smem<T, 8>(), s>>>(items, nitems, counter, parity, seg);
+    else k_batch_weno_x<T, 4><<<nblocks, dim3(32, 4), march_x_smem<T, 4>(), s>>>(items, nitems, counter, parity, seg);
+  } else if (dir == 1) {
+    if (by8) k_batch_weno_yz<T, 1, 8><<<nblocks, dim3(32, 8), 0, s>>>(items, nitems, counter, parity, seg);
+    else k_batch_weno_yz<T, 1, 4><<<nblocks, dim3(32, 4), 0, s>>>(items, nitems, counter, parity, seg);
+  } else {
+    if (by8) k_batch_weno_yz<T, 2, 8><<<nblocks, dim3(32, 8), 0, s>>>(items, nitems, counter, parity, seg);
+    else k_batch_weno_yz<T, 2, 4><<<nblocks, dim3(32, 4), 0, s>>>(items, nitems, counter, parity, seg);
+  }
+}
+
 template <typename T, int DIR, bool ACCUM> static void attr_dir() {
   cudaFuncSetAttribute(k_weno<T, DIR, ACCUM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem<T, DIR>());
 }
 template <typename T> void setup_weno() {
+  cudaFuncSetAttribute(k_batch_weno_x<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_x_smem<T, 4>());
+  cudaFuncSetAttribute(k_batch_weno_x<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_x_smem<T, 8>());
   cudaFuncSetAttribute(k_weno_march_x<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_x_smem<T, 4>());
   cudaFuncSetAttribute(k_weno_march_x<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_x_smem<T, 8>());
   attr_dir<T, 0, false>();
@@ -432,6 +536,12 @@ template void setup_weno<double>();
 template void launch_weno_dir<float>(const Ctx &, Fields5<const float>, Fields5<float>, int, cudaStream_t, int64_t *);
 template void launch_weno_dir<double>(const Ctx &, Fields5<const double>, Fields5<double>, int, cudaStream_t,
                                       int64_t *);
+template int batch_weno_blocks_per_sm<float>(int, int);
+template int batch_weno_blocks_per_sm<double>(int, int);
+template void launch_batch_weno<float>(const int4 *, int, int *, int, int, int, int, int,
+                                       cudaStream_t);
+template void launch_batch_weno<double>(const int4 *, int, int *, int, int, int, int, int,
+                                        cudaStream_t);
 template void launch_weno_cfg<float>(const Ctx &, Fields5<const float>, Fields5<float>, int, WenoCfg, cudaStream_t);
 template void launch_weno_cfg<double>(const Ctx &, Fields5<const double>, Fields5<double>, int, WenoCfg,
                                       cudaStream_t);

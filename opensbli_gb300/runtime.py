@@ -79,6 +79,9 @@ EXPORTS = (
     "osb_get_state64", "osb_step", "osb_residual", "osb_reduce", "osb_launch_count", "osb_profile", "osb_profile_read",
     "osb_set_weno_shape", "osb_get_weno_shape", "osb_set_central_shape", "osb_get_central_shape", "osb_autotune",
     "osb_adjoint_residual", "osb_adjoint_step", "osb_get_error", "osb_destroy",
+    "osb_batch_create", "osb_batch_set_stream", "osb_batch_set_dt", "osb_batch_set_state64", "osb_batch_get_state64",
+    "osb_batch_step", "osb_batch_autotune", "osb_batch_get_shape", "osb_batch_launch_count", "osb_batch_get_error",
+    "osb_batch_destroy",
 )
 # launch shapes of the WENO flux kernels (osb_set_weno_shape)
 WENO_SHAPES = {"tile": 0, "march4": 1, "march8": 2}
@@ -127,10 +130,23 @@ def load(build_if_missing=True):
     lib.osb_adjoint_residual.argtypes = [vp, vp, vp]
     lib.osb_adjoint_step.argtypes = [vp, dp, vp, vp]
     lib.osb_get_error.argtypes = [vp, ctypes.c_char_p, ip]
+    lib.osb_batch_create.argtypes = [ctypes.POINTER(PlanDesc), ip, ctypes.POINTER(vp)]
+    lib.osb_batch_set_stream.argtypes = [vp, vp]
+    lib.osb_batch_set_dt.argtypes = [vp, ctypes.POINTER(dp)]
+    lib.osb_batch_set_state64.argtypes = [vp, ip, vp]
+    lib.osb_batch_get_state64.argtypes = [vp, ip, vp]
+    lib.osb_batch_step.argtypes = [vp, ip]
+    lib.osb_batch_autotune.argtypes = [vp, ip, ctypes.POINTER(dp)]
+    lib.osb_batch_get_shape.argtypes = [vp, ctypes.POINTER(ip), ip]
+    lib.osb_batch_launch_count.argtypes = [vp]
+    lib.osb_batch_launch_count.restype = ctypes.c_int64
+    lib.osb_batch_get_error.argtypes = [vp, ctypes.c_char_p, ip]
+    lib.osb_batch_destroy.argtypes = [vp]
+    lib.osb_batch_destroy.restype = None
     lib.osb_destroy.argtypes = [vp]
     lib.osb_destroy.restype = None
     for name in EXPORTS:
-        if name not in ("osb_launch_count", "osb_destroy"):
+        if name not in ("osb_launch_count", "osb_destroy", "osb_batch_launch_count", "osb_batch_destroy"):
             getattr(lib, name).restype = ctypes.c_int
     _lib = lib
     return lib
