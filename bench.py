@@ -331,6 +331,22 @@ def own_arm(args, world, rank, local):
     nv = q64.shape[0]
     l2 = [float(torch.linalg.vector_norm(diff[v]) / torch.linalg.vector_norm(q64[v])) for v in range(nv)]
     linf = [float(diff[v].abs().max() / q64[v].abs().max()) for v in range(nv)]
+    long_err = None
+    if args.error_steps:
+        # the configuration's own run length: both precisions from the initial state
+        runs = {}
+        for prec in ("mixed", "fp64"):
+            s3 = wl.solver(prec)
+            s3.step(args.error_steps, dt)
+            runs[prec] = s3.state64()
+            s3.close()
+        d3 = runs["mixed"] - runs["fp64"]
+        long_err = {"steps": args.error_steps,
+                    "l2": [float(torch.linalg.vector_norm(d3[v]) / torch.linalg.vector_norm(runs["fp64"][v]))
+                           for v in range(nv)],
+                    "linf": [float(d3[v].abs().max() / runs["fp64"][v].abs().max()) for v in range(nv)],
+                    "finite": bool(torch.isfinite(runs["mixed"]).all() and torch.isfinite(runs["fp64"]).all())}
+        del runs, d3
 
     # ---- roofline: the whole RK3 step and the dominant kernel family
     peak, peak_kind = load_peaks()
@@ -383,6 +399,8 @@ def own_arm(args, world, rank, local):
                 "mixed_vs_fp64_speedup": ((value / world) / (cells * K2 / t2)) if head == "mixed" else
                 ((cells * K2 / t2) / (value / world)),
                 "error_vs_fp64": {"steps": W + K, "l2": l2, "linf": linf, "vars": vars_}}
+        if long_err:
+            line["error_vs_fp64_long"] = long_err
         print(json.dumps(line), flush=True)
 
 
@@ -562,6 +580,8 @@ def main():
     ap.add_argument("--ref-steps", type=int, default=None,
                     help="timed steps of the host-core reference sample (default: 2 at 256^3, 40 otherwise)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--error-steps", type=int, default=0,
+                    help="also run both precisions this many steps from the initial state and report the error")
     args = ap.parse_args()
     if args.ref_steps is None:
         args.ref_steps = 2 if args.config == "tgv_weno256" else 40

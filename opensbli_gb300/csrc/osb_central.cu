@@ -91,7 +91,7 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
       const int i = i0 - 2 + px, j = j0 - 2 + py;
       if (e < PX * PY && i < g.n0 + 2 && j < g.n1 + 2 && k < g.n2 + 2) {
         const T rho = pre[r][0];
-        const T irho = rcp_t(rho);
+        const T irho = T(1) / rho;  // correctly rounded: u and T feed the viscous terms
         const T u0 = pre[r][1] * irho, u1 = pre[r][2] * irho, u2 = pre[r][3] * irho;
         const T E = pre[r][4];
         const T half = T(0.5);

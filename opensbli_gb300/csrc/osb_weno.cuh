@@ -21,7 +21,8 @@
 // stored: its projections are formed from Q, u_d and p):
 //     acoustic+- . X = bt (g +- a h),   entropy . X = X_0 - g / a^2;
 // the smoothness indicators use Jiang and Shu's sum-of-squares form.  The nonlinear weights:
-// in FP32 alpha_r = d_r * rcp((eps+beta_r)^2) with the fast hardware reciprocal (2 ulp); in FP64,
+// in FP32 alpha_r = d_r * rcp((eps+beta_r)^2) with the fast hardware reciprocal (2 ulp), applied to
+// the candidate differences (p_r - p_1) only; in FP64,
 // where every division costs a Newton sequence on the slow FP64 pipe, the three alphas are scaled
 // by the common factor prod_s (eps+beta_s)^2, alpha_0 ~ d_0 (eps+beta_1)^2 (eps+beta_2)^2 etc., so
 // one exact division per side remains (the products stay far inside the FP64 range).
@@ -61,10 +62,12 @@ template <typename T> __device__ __forceinline__ T weno5_side(T f0, T f1, T f2, 
     const T a0 = T(3.0 / 10.0) * (q1 * q2), a1 = T(3.0 / 5.0) * (q0 * q2), a2 = T(1.0 / 10.0) * (q0 * q1);
     return (a0 * p0 + a1 * p1 + a2 * p2) / (a0 + a1 + a2);
   } else {
+    // sum_r omega_r p_r written as p1 + omega_0 (p0 - p1) + omega_2 (p2 - p1): the weights' rounding
+    // (fast reciprocals) then scales only the small candidate differences, not the flux itself
     const T a0 = T(3.0 / 10.0) * rcp_t(e0 * e0);
     const T a1 = T(3.0 / 5.0) * rcp_t(e1 * e1);
     const T a2 = T(1.0 / 10.0) * rcp_t(e2 * e2);
-    return (a0 * p0 + a1 * p1 + a2 * p2) * rcp_t(a0 + a1 + a2);
+    return p1 + (a0 * (p0 - p1) + a2 * (p2 - p1)) * rcp_t(a0 + a1 + a2);
   }
 }
 
@@ -74,10 +77,12 @@ template <typename T> struct WPt {
   T Q[5], ud, a, p;
 };
 
-// Primitive quantities of one point from its conserved vector (1/rho by the fast reciprocal in FP32).
+// Primitive quantities of one point from its conserved vector.  1/rho is a correctly rounded
+// division: the velocity enters the physical flux directly, and a biased reciprocal would bias
+// every flux difference by the same relative amount, step after step.
 template <typename T, int D>
 __device__ __forceinline__ void point_prims(const T (&r)[5], T gm1, T gama, WPt<T> &w) {
-  const T irho = rcp_t(r[0]);
+  const T irho = T(1) / r[0];
   const T u0 = r[1] * irho, u1 = r[2] * irho, u2 = r[3] * irho;
   const T p = gm1 * (r[4] - T(0.5) * (r[1] * u0 + r[2] * u1 + r[3] * u2));
 #pragma unroll
