@@ -34,6 +34,11 @@ UNIT = "cell-updates/s"
 ALG_BYTES_STAGE = {"mixed": 5 * (2 * 4 + 2 * 8), "fp64": 5 * (2 * 8 + 2 * 8)}
 
 
+# DRAM bytes per cell per launch measured by ncu for the mixed WENO TGV kernels at 192^3 (state larger
+# than L2), used to scale the roofline's traffic figure to the benchmark's grid
+DRAM_BYTES_PER_CELL_WENO_MIXED = {"weno_x": 56.1, "weno_y": 57.8, "weno_z": 57.7, "central_rk": 144.8}
+
+
 def load_peaks():
     p = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -367,8 +372,14 @@ def own_arm(args, world, rank, local):
         ms, cnt = prof[dom]
         per_launch = ms / cnt / 1e3
         ach = cells * fam_bytes[dom] / per_launch / 1e9
+        traffic, tsrc = None, None
+        if wl.name == "tgv_weno256" and head == "mixed" and dom in DRAM_BYTES_PER_CELL_WENO_MIXED:
+            traffic = DRAM_BYTES_PER_CELL_WENO_MIXED[dom] * cells / 1e9
+            tsrc = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the same kernel at 192^3 "
+                    "(profiles/weno_central_tgv192_mixed_kernels.md), per cell, times this launch's cells")
         roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "peak_kind": peak_kind, "traffic": None, "alg_bytes_per_cell": fam_bytes[dom],
+                "peak_kind": peak_kind, "traffic": traffic, "traffic_unit": "GB per launch",
+                "traffic_source": tsrc, "alg_bytes_per_cell": fam_bytes[dom],
                 "avg_launch_ms": per_launch * 1e3,
                 "step": {"achieved": achieved_step, "frac": achieved_step / peak,
                          "alg_bytes_per_cell_per_stage": bstage},

@@ -184,6 +184,19 @@ int osb_set_central_shape(osb_ctx *ctx, int ty);
 int osb_get_central_shape(osb_ctx *ctx, int *ty);
 int osb_autotune(osb_ctx *ctx, int reps, double *best_ms);
 
+/* Point probes, the counterpart of SimulationMonitor's per-point reductions
+ * (core/diagnostics/simulation_monitors.py:66-108): n requests {what, i, j, k} (interior indices, k = 0
+ * on 2D blocks); what = a conserved variable 0..nvar-1 or a derived quantity OSB_PROBE_*.  Values come
+ * from the FP64 state (exact in both precisions) into host_out[n]; the call synchronises the stream.
+ * At most OSB_PROBE_MAX requests per call. */
+#define OSB_PROBE_U0 16
+#define OSB_PROBE_U1 17
+#define OSB_PROBE_U2 18
+#define OSB_PROBE_P 19
+#define OSB_PROBE_T 20
+#define OSB_PROBE_MAX 4096
+int osb_probe(osb_ctx *ctx, int n, const int *what_ijk, double *host_out);
+
 /* Discrete adjoint of the time loop.  No counterpart in the reference.  FP64 3D plans with central
  * skew-symmetric fluxes and periodic boundaries (viscous terms as the plan says); other plans get
  * OSB_EUNSUPPORTED.  Arrays are device FP64, dense interior [5][n2][n1][n0].

@@ -714,6 +714,65 @@ int osb_set_state64(osb_ctx *c, int var, const double *src) {
   return cuda_err(c, cudaGetLastError(), "osb_set_state64");
 }
 
+}  // extern "C"
+
+// point probes: what = 0..nvar-1 conserved variable, OSB_PROBE_U0.. derived (FP64 master state)
+__global__ void k_probe(Grid g, Fields5<double> m, int nvar, int n, const int *req, double *out, double gm1, double gM2) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int what = req[4 * t], i = req[4 * t + 1], j = req[4 * t + 2], k = req[4 * t + 3];
+  const int64_t idx = gidx(g, i, j, k);
+  if (what < nvar) {
+    out[t] = m.v[what][idx];
+    return;
+  }
+  const double rho = m.v[0][idx], E = m.v[nvar - 1][idx];
+  const int ndim = nvar - 2;
+  double ke = 0.0, u[3] = {0.0, 0.0, 0.0};
+  for (int c = 0; c < ndim; ++c) {
+    u[c] = m.v[1 + c][idx] / rho;
+    ke += 0.5 * rho * u[c] * u[c];
+  }
+  const double p = gm1 * (E - ke);
+  double v = 0.0;
+  if (what <= OSB_PROBE_U2) v = u[what - OSB_PROBE_U0];
+  else if (what == OSB_PROBE_P) v = p;
+  else v = gM2 * p / rho;
+  out[t] = v;
+}
+
+extern "C" {
+
+int osb_probe(osb_ctx *c, int n, const int *what_ijk, double *host_out) {
+  if (!c || n < 0 || (n > 0 && (!what_ijk || !host_out))) return OSB_EINVAL;
+  if (n == 0) return OSB_OK;
+  if (n > OSB_PROBE_MAX) return set_err(c, OSB_ETOOLARGE, "osb_probe: too many probes");
+  if (!c->qold_valid) return set_err(c, OSB_EINVAL, "no state yet: call osb_init_tgv, osb_set_state64 or osb_step");
+  const int n2 = c->plan.ndim == 2 ? 1 : c->g.n2;
+  for (int t = 0; t < n; ++t) {
+    const int w = what_ijk[4 * t], i = what_ijk[4 * t + 1], j = what_ijk[4 * t + 2], k = what_ijk[4 * t + 3];
+    const bool ok_w = (w >= 0 && w < c->nvar) || (w >= OSB_PROBE_U0 && w <= OSB_PROBE_T &&
+                                                   (w != OSB_PROBE_U2 || c->plan.ndim == 3));
+    if (!ok_w || i < 0 || i >= c->g.n0 || j < 0 || j >= c->g.n1 || k < 0 || k >= n2)
+      return set_err(c, OSB_EINVAL, "osb_probe: quantity or index out of range");
+  }
+  cudaError_t e = cudaSuccess;
+  if (!c->probe_buf) e = cudaMalloc(&c->probe_buf, OSB_PROBE_MAX * (4 * sizeof(int) + sizeof(double)));
+  if (e != cudaSuccess) return cuda_err(c, e, "osb_probe allocation");
+  int *req = reinterpret_cast<int *>(c->probe_buf);
+  double *out = reinterpret_cast<double *>(req + 4 * OSB_PROBE_MAX);
+  e = cudaMemcpyAsync(req, what_ijk, sizeof(int) * 4 * n, cudaMemcpyHostToDevice, c->stream);
+  Fields5<double> m;
+  for (int v = 0; v < 5; ++v) m.v[v] = v < c->nvar ? (c->plan.ndim == 2 ? c->q64_2d[v] : c->qold[v]) : nullptr;
+  if (e == cudaSuccess) {
+    k_probe<<<(n + 127) / 128, 128, 0, c->stream>>>(c->g, m, c->nvar, n, req, out, c->ph.gm1, c->ph.gM2);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host_out, out, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  return cuda_err(c, e, "osb_probe");
+}
+
 int osb_get_state64(osb_ctx *c, int var, double *dst) {
   if (!c) return OSB_EINVAL;
   if (var < 0 || var >= c->nvar || !dst) return set_err(c, OSB_EINVAL, "bad var or pointer");
@@ -999,6 +1058,7 @@ void osb_destroy(osb_ctx *c) {
   }
   cudaFree(c->red);
   cudaFree(c->adj);
+  cudaFree(c->probe_buf);
   for (int v = 0; v < 4; ++v) {
     if (c->mixed) cudaFree(c->q64_2d[v]);
     cudaFree(c->du2[v]);

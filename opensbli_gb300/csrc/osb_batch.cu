@@ -233,9 +233,9 @@ template <typename T> void launch_weno_b(osb_batch *b, int q, int parity, cudaSt
   ++b->launches;
 }
 
-template <typename T> void launch_central_b(osb_batch *b, int q, int parity, double ca, double cb, cudaStream_t s) {
+template <typename T> void launch_central_b(osb_batch *b, int q, int parity, int stage, cudaStream_t s) {
   if (!b->item_cnt[q]) return;
-  launch_batch_central<T>(b->d_items + b->item_off[q], b->item_cnt[q], b->d_counters + q, parity, ca, cb,
+  launch_batch_central<T>(b->d_items + b->item_off[q], b->item_cnt[q], b->d_counters + q, parity, stage,
                           CENTRAL_MODES[q - Q_C0], b->crk_ty, b->nblocks[q], s);
   ++b->launches;
 }
@@ -248,7 +248,7 @@ template <typename T> void one_step_b(osb_batch *b, int start, cudaStream_t s) {
     cudaMemsetAsync(b->d_counters, 0, sizeof(int) * Q_COUNT, s);
     launch_halos_b<T>(b, par, s);
     for (int q = Q_WX; q <= Q_WZ; ++q) launch_weno_b<T>(b, q, par, s);
-    for (int q = Q_C0; q < Q_COUNT; ++q) launch_central_b<T>(b, q, par, b->rk_a[st], b->rk_b[st], s);
+    for (int q = Q_C0; q < Q_COUNT; ++q) launch_central_b<T>(b, q, par, st, s);
   }
 }
 
@@ -342,7 +342,7 @@ template <typename T> int autotune_b(osb_batch *b, int reps, double *best_ms) {
         b->zchunk = zc;
         if ((err = build_items<T>(b)) != cudaSuccess) break;
         const float ms = timeit([&] {
-          for (int q = Q_C0; q < Q_COUNT; ++q) launch_central_b<T>(b, q, par, b->rk_a[0], b->rk_b[0], s);
+          for (int q = Q_C0; q < Q_COUNT; ++q) launch_central_b<T>(b, q, par, 0, s);
         });
         if (ms < 0) break;
         if (ms < best) {
@@ -365,6 +365,15 @@ template <typename T> int autotune_b(osb_batch *b, int reps, double *best_ms) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   return bcuda(b, err, "osb_batch_autotune");
+}
+
+template <typename T> void set_inst_dt(BatchInst<T> &d, double dt, const double *a, const double *b) {
+  d.dt = dt;
+  for (int s = 0; s < 3; ++s) {
+    d.dtn[s] = dt * b[s];
+    d.dto[s] = dt * a[s];
+    d.ddt[s] = (float)(dt * b[s] - dt * a[s]);
+  }
 }
 
 // the state arrays of stage-start parity `par` hold FP32 copies: re-derive them from the register
@@ -492,8 +501,8 @@ int osb_batch_set_dt(osb_batch *b, const double *dt) {
   if (!b || !dt) return OSB_EINVAL;
   for (int i = 0; i < b->nb; ++i) {
     if (!(dt[i] > 0)) return berr(b, OSB_EINVAL, "osb_batch_set_dt: every dt must be > 0");
-    if (b->mixed) inst<float>(b, i).dt = dt[i];
-    else inst<double>(b, i).dt = dt[i];
+    if (b->mixed) set_inst_dt(inst<float>(b, i), dt[i], b->rk_a, b->rk_b);
+    else set_inst_dt(inst<double>(b, i), dt[i], b->rk_a, b->rk_b);
   }
   // stream-ordered, so steps already queued keep their time steps; the graphs copy the device table
   return bcuda(b, cudaMemcpyAsync(b->d_table, b->table.data(), b->table.size(), cudaMemcpyHostToDevice, b->stream),

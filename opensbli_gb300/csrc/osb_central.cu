@@ -52,7 +52,7 @@ template <typename T, int MODE, int TY> constexpr size_t ring_bytes() {
 template <typename T, int MODE, int TY>
 __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold,
                                              Fields5<T> rin, Fields5<T> rout, const Phys &ph, double dt_new,
-                                             double dt_old, int zchunk, int bx, int by, int bz,
+                                             double dt_old, T ddt, int zchunk, int bx, int by, int bz,
                                              unsigned char *smem_raw) {
   constexpr int NF = ring_fields<MODE>(), PY = TY + 4;
   T *ring = reinterpret_cast<T *>(smem_raw);  // [NP][NF][PY][PX]
@@ -61,7 +61,6 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
   const int k1 = min(k0 + zchunk, g.n2);
   const T gm1 = pick<T>(ph.gm1, ph.f_gm1);
   const T gM2 = pick<T>(ph.gM2, ph.f_gM2);
-  const T ddt = (T)(dt_new - dt_old);
 
   auto slot = [](int k) { return ((k % NP) + NP) % NP; };
   auto at = [&](int sl, int f, int py, int px) -> T & { return ring[((sl * NF + f) * PY + py) * PX + px]; };
@@ -129,6 +128,15 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
     int64_t nout = 0;
     if (active) {
       nout = gidx(g, i, j, k);
+      if (k + 2 < k1) {
+        // L2 prefetch of the output-point arrays two planes ahead (no registers held)
+        const int64_t np = nout + 2 * g.sz;
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          if (MODE & CRK_RIN) prefetch_l2(rin.v[v] + np);
+          if (MODE & CRK_UPDATE) prefetch_l2(qold.v[v] + np);
+        }
+      }
       if (MODE & CRK_RIN) {
 #pragma unroll
         for (int v = 0; v < 5; ++v) rpre[v] = rin.v[v][nout];
@@ -291,9 +299,10 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
 template <typename T, int MODE, int TY>
 __global__ void __launch_bounds__(TX * TY, central_min_blocks<T, MODE, TY>())
     k_central_rk(Grid g, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold, Fields5<T> rin, Fields5<T> rout,
-                 Phys ph, double dt_new, double dt_old, int zchunk) {
+                 Phys ph, double dt_new, double dt_old, T ddt, int zchunk) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  central_tile<T, MODE, TY>(g, q, qnew, qold, rin, rout, ph, dt_new, dt_old, zchunk, blockIdx.x, blockIdx.y, blockIdx.z,
+  central_tile<T, MODE, TY>(g, q, qnew, qold, rin, rout, ph, dt_new, dt_old, ddt, zchunk, blockIdx.x, blockIdx.y,
+                            blockIdx.z,
                             smem_raw);
 }
 
@@ -321,8 +330,10 @@ static void launch_mode(const Ctx &c, Fields5<const T> q, Fields5<T> qnew, Field
   const int zchunk = (c.g.n2 + nzc - 1) / nzc;
   nzc = (c.g.n2 + zchunk - 1) / zchunk;
   dim3 grid(bx, by, nzc), block(TX, TY);
+  // (dt_new - dt_old) in the state precision, formed once here: the FP32 stage update adds it times R
+  const T ddt = (T)(dt_new - dt_old);
   k_central_rk<T, MODE, TY><<<grid, block, ring_bytes<T, MODE, TY>(), s>>>(c.g, q, qnew, qold, rin, rout, c.ph, dt_new,
-                                                                          dt_old, zchunk);
+                                                                          dt_old, ddt, zchunk);
 }
 
 template <typename T, int MODE>
@@ -389,8 +400,7 @@ cudaError_t batch_table_upload_central(const void *src_dev, size_t bytes, cudaSt
 // ---------------------------------------------------------------------------------------------
 template <typename T, int MODE, int TY>
 __global__ void __launch_bounds__(TX * TY, central_min_blocks<T, MODE, TY>())
-    k_batch_central(const int4 *items, int nitems, int *counter, int parity, double ca,
-                    double cb) {
+    k_batch_central(const int4 *items, int nitems, int *counter, int parity, int stage) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ int slot;
   for (;;) {
@@ -408,7 +418,8 @@ __global__ void __launch_bounds__(TX * TY, central_min_blocks<T, MODE, TY>())
       r.v[v] = d.res[v];
       qo.v[v] = d.qold[v];
     }
-    central_tile<T, MODE, TY>(d.g, q, qn, qo, r, r, d.ph, d.dt * cb, d.dt * ca, d.zchunk, w.y, w.z, w.w, smem_raw);
+    central_tile<T, MODE, TY>(d.g, q, qn, qo, r, r, d.ph, d.dtn[stage], d.dto[stage], (T)d.ddt[stage], d.zchunk, w.y,
+                              w.z, w.w, smem_raw);
   }
 }
 
@@ -434,31 +445,31 @@ template <typename T> int batch_central_blocks_per_sm(int mode, int ty) {
 }
 
 template <typename T, int MODE>
-static void batch_mode(const int4 *items, int nitems, int *counter, int parity, double ca,
-                       double cb, int ty, int nblocks, cudaStream_t s) {
+static void batch_mode(const int4 *items, int nitems, int *counter, int parity, int stage, int ty,
+                       int nblocks, cudaStream_t s) {
   if (ty == 16)
     k_batch_central<T, MODE, 16><<<nblocks, dim3(TX, 16), ring_bytes<T, MODE, 16>(), s>>>(items, nitems, counter,
-                                                                                          parity, ca, cb);
+                                                                                          parity, stage);
   else
     k_batch_central<T, MODE, 8><<<nblocks, dim3(TX, 8), ring_bytes<T, MODE, 8>(), s>>>(items, nitems, counter,
-                                                                                        parity, ca, cb);
+                                                                                        parity, stage);
 }
 
 template <typename T>
-void launch_batch_central(const int4 *items, int nitems, int *counter, int parity, double ca,
-                          double cb, int mode, int ty, int nblocks, cudaStream_t s) {
+void launch_batch_central(const int4 *items, int nitems, int *counter, int parity, int stage, int mode, int ty,
+                          int nblocks, cudaStream_t s) {
   switch (mode | CRK_UPDATE) {
     case CRK_SKEW | CRK_VISC | CRK_UPDATE:
-      batch_mode<T, CRK_SKEW | CRK_VISC | CRK_UPDATE>(items, nitems, counter, parity, ca, cb, ty, nblocks, s);
+      batch_mode<T, CRK_SKEW | CRK_VISC | CRK_UPDATE>(items, nitems, counter, parity, stage, ty, nblocks, s);
       break;
     case CRK_SKEW | CRK_UPDATE:
-      batch_mode<T, CRK_SKEW | CRK_UPDATE>(items, nitems, counter, parity, ca, cb, ty, nblocks, s);
+      batch_mode<T, CRK_SKEW | CRK_UPDATE>(items, nitems, counter, parity, stage, ty, nblocks, s);
       break;
     case CRK_RIN | CRK_VISC | CRK_UPDATE:
-      batch_mode<T, CRK_RIN | CRK_VISC | CRK_UPDATE>(items, nitems, counter, parity, ca, cb, ty, nblocks, s);
+      batch_mode<T, CRK_RIN | CRK_VISC | CRK_UPDATE>(items, nitems, counter, parity, stage, ty, nblocks, s);
       break;
     case CRK_RIN | CRK_UPDATE:
-      batch_mode<T, CRK_RIN | CRK_UPDATE>(items, nitems, counter, parity, ca, cb, ty, nblocks, s);
+      batch_mode<T, CRK_RIN | CRK_UPDATE>(items, nitems, counter, parity, stage, ty, nblocks, s);
       break;
     default:
       break;
@@ -482,10 +493,8 @@ template void setup_central<float>();
 template void setup_central<double>();
 template int batch_central_blocks_per_sm<float>(int, int);
 template int batch_central_blocks_per_sm<double>(int, int);
-template void launch_batch_central<float>(const int4 *, int, int *, int, double, double, int,
-                                          int, int, cudaStream_t);
-template void launch_batch_central<double>(const int4 *, int, int *, int, double, double,
-                                           int, int, int, cudaStream_t);
+template void launch_batch_central<float>(const int4 *, int, int *, int, int, int, int, int, cudaStream_t);
+template void launch_batch_central<double>(const int4 *, int, int *, int, int, int, int, int, cudaStream_t);
 
 template void launch_central_rk<float>(const Ctx &, Fields5<const float>, Fields5<float>, Fields5<double>,
                                        Fields5<float>, Fields5<float>, double, double, int, cudaStream_t, int64_t *);

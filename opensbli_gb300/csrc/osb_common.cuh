@@ -46,6 +46,11 @@ template <typename T> __device__ __forceinline__ T sqrt_t(T x);
 template <> __device__ __forceinline__ float sqrt_t<float>(float x) { return sqrtf(x); }
 template <> __device__ __forceinline__ double sqrt_t<double>(double x) { return sqrt(x); }
 
+// bring the line holding *p into L2 (a hint: no register is written, nothing waits for it)
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // 1/x: the fast hardware reciprocal in FP32 (2 ulp), the exact quotient in FP64
 template <typename T> __device__ __forceinline__ T rcp_t(T x);
 template <> __device__ __forceinline__ float rcp_t<float>(float x) { return __fdividef(1.0f, x); }
@@ -75,6 +80,8 @@ template <typename T> struct BatchInst {
   T *res[5];
   double *qold[5];
   double dt;
+  double dtn[3], dto[3];  // dt * rknew[s], dt * rkold[s] of the three stages
+  float ddt[3];           // dt * (rknew[s] - rkold[s]), the FP32 stage increment factor
   int conv;    // OSB_CONV_CENTRAL_SKEW or OSB_CONV_WENO5JS
   int visc;    // 1: constant-viscosity viscous terms
   int zchunk;  // z-planes per central-kernel tile

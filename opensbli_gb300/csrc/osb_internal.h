@@ -38,6 +38,7 @@ struct Ctx {
   WenoCfg wcfg[3] = {{WENO_TILE, 32}, {WENO_TILE, 32}, {WENO_TILE, 32}};
   int crk_ty = 8;             // tile height of the fused central/RK kernel (8 or 16)
   double *adj = nullptr;      // adjoint scratch (stage states, primitives, sensitivity fields)
+  void *probe_buf = nullptr;  // point-probe requests and results (osb_probe)
   int num_sms = 152;          // multiprocessors of the device (set at creation)
   int64_t graph_launches = 0;  // kernel launches recorded in one captured step
   int qold_valid = 0;          // the FP64 register holds the current state
@@ -91,8 +92,8 @@ void launch2_rhs(const Ctx &c, int update, double A, double B, double dt, cudaSt
 cudaError_t batch_table_upload_central(const void *src_dev, size_t bytes, cudaStream_t s);
 cudaError_t batch_table_upload_weno(const void *src_dev, size_t bytes, cudaStream_t s);
 template <typename T>
-void launch_batch_central(const int4 *items, int nitems, int *counter, int parity, double ca,
-                          double cb, int mode, int ty, int nblocks, cudaStream_t s);
+void launch_batch_central(const int4 *items, int nitems, int *counter, int parity, int stage, int mode, int ty,
+                          int nblocks, cudaStream_t s);
 template <typename T> int batch_central_blocks_per_sm(int mode, int ty);
 template <typename T>
 void launch_batch_weno(const int4 *items, int nitems, int *counter, int parity, int dir,

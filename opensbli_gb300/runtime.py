@@ -78,7 +78,7 @@ EXPORTS = (
     "osb_set_state64_padded", "osb_set_coordinate",
     "osb_get_state64", "osb_step", "osb_residual", "osb_reduce", "osb_launch_count", "osb_profile", "osb_profile_read",
     "osb_set_weno_shape", "osb_get_weno_shape", "osb_set_central_shape", "osb_get_central_shape", "osb_autotune",
-    "osb_adjoint_residual", "osb_adjoint_step", "osb_get_error", "osb_destroy",
+    "osb_adjoint_residual", "osb_adjoint_step", "osb_probe", "osb_get_error", "osb_destroy",
     "osb_batch_create", "osb_batch_set_stream", "osb_batch_set_dt", "osb_batch_set_state64", "osb_batch_get_state64",
     "osb_batch_step", "osb_batch_autotune", "osb_batch_get_shape", "osb_batch_launch_count", "osb_batch_get_error",
     "osb_batch_destroy",
@@ -128,6 +128,7 @@ def load(build_if_missing=True):
     lib.osb_get_central_shape.argtypes = [vp, ctypes.POINTER(ip)]
     lib.osb_autotune.argtypes = [vp, ip, ctypes.POINTER(dp)]
     lib.osb_adjoint_residual.argtypes = [vp, vp, vp]
+    lib.osb_probe.argtypes = [vp, ip, ctypes.POINTER(ip), ctypes.POINTER(dp)]
     lib.osb_adjoint_step.argtypes = [vp, dp, vp, vp]
     lib.osb_get_error.argtypes = [vp, ctypes.c_char_p, ip]
     lib.osb_batch_create.argtypes = [ctypes.POINTER(PlanDesc), ip, ctypes.POINTER(vp)]
@@ -322,6 +323,18 @@ class Solver:
 
     def launch_count(self):
         return int(self.lib.osb_launch_count(self.ctx))
+
+    def probe(self, requests):
+        """Point values from the FP64 state: requests = [(what, i, j, k), ...] with what a conserved
+        variable index or one of opensbli_gb300.monitor.DERIVED's codes; returns a list of floats."""
+        n = len(requests)
+        if n == 0:
+            return []
+        flat = (ctypes.c_int * (4 * n))(*[int(x) for r in requests for x in r])
+        out = (ctypes.c_double * n)()
+        self._in()
+        self._check(self.lib.osb_probe(self.ctx, n, flat, out))
+        return list(out)
 
     def set_weno_shape(self, d, kind, seg=32):
         """Launch shape of the direction-d WENO flux kernel: kind in WENO_SHAPES, seg cells per line

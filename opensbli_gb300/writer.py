@@ -335,9 +335,12 @@ class GB300Writer:
         from .runtime import Solver
         return Solver(self.plan, device=device)
 
-    def run(self, niter=None, dt=None, device=None):
+    def run(self, niter=None, dt=None, device=None, monitor=None):
         """Initialise from the script's initial condition and advance niter steps (defaults: the
-        script's niter and dt).  Returns the Solver, whose state64() gives the FP64 state."""
+        script's niter and dt).  The algorithm's SimulationMonitor, if it has one (or `monitor`, an
+        opensbli_gb300.monitor.SimulationMonitor), samples and prints where the generated code would.
+        Returns the Solver, whose state64() gives the FP64 state."""
+        from . import monitor as mon
         s = self.solver(device)
         if self.plan.ndim == 2:
             f = self.initial_fields(halo=4)
@@ -345,5 +348,10 @@ class GB300Writer:
             s.set_state64_padded(np.stack([f[v] for v in self.state_names()]), 4)
         else:
             s.set_state64(self.initial_state())
-        s.step(int(niter if niter is not None else self.plan.niter), float(dt if dt is not None else self.plan.dt))
+        if monitor is None and getattr(self.algorithm, "simulation_monitor", None) is not None:
+            monitor = mon.SimulationMonitor.from_reference(self.algorithm.simulation_monitor)
+        mon.run(s, int(niter if niter is not None else self.plan.niter), float(dt if dt is not None else self.plan.dt),
+                monitor)
+        if monitor is not None:
+            monitor.close()
         return s
