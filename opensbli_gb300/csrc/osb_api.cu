@@ -68,7 +68,7 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
       return OSB_EINVAL;
     }
   }
-  if (p->conv != OSB_CONV_CENTRAL_SKEW && p->conv != OSB_CONV_WENO5JS) {
+  if (p->conv != OSB_CONV_CENTRAL_SKEW && p->conv != OSB_CONV_WENO5JS && p->conv != OSB_CONV_WENO5Z) {
     snprintf(why, n, "convective scheme %d not supported on 3D blocks", p->conv);
     return OSB_EUNSUPPORTED;
   }
@@ -297,7 +297,7 @@ template <typename T> void residual_into(osb_ctx *c, int cur, cudaStream_t s) {
   Fields5<const T> qc = fields<const T>(qs);
   Fields5<T> r = fields<T>(c->res);
   launch_halos<T>(*c, q, s, &c->launches);
-  if (c->plan.conv == OSB_CONV_WENO5JS) {
+  if (c->plan.conv == OSB_CONV_WENO5JS || c->plan.conv == OSB_CONV_WENO5Z) {
     weno_all<T>(c, qc, r, s);
     const int mode = CRK_RIN | (c->plan.visc == OSB_VISC_CONST ? CRK_VISC : 0);
     launch_central_rk<T>(*c, qc, r, fields_d(c->qold), r, r, 0.0, 0.0, mode, s, &c->launches);
@@ -321,7 +321,7 @@ template <typename T> void one_step(osb_ctx *c, int start, double dt, cudaStream
     }
     const double dtn = dt * c->plan.rk_b[st], dto = dt * c->plan.rk_a[st];
     const int visc = c->plan.visc == OSB_VISC_CONST ? CRK_VISC : 0;
-    if (c->plan.conv == OSB_CONV_WENO5JS) {
+    if (c->plan.conv == OSB_CONV_WENO5JS || c->plan.conv == OSB_CONV_WENO5Z) {
       weno_all<T>(c, qc, r, s);
       ProfScope ps(c, PF_CENTRAL_RK, s);
       launch_central_rk<T>(*c, qc, fields<T>(qn), fields_d(c->qold), r, r, dtn, dto, CRK_RIN | visc | CRK_UPDATE, s,
@@ -936,7 +936,7 @@ template <typename T> static int autotune_impl(osb_ctx *c, int reps, double *bes
   };
   for (int t = 0; t < OSB_TUNE_SLOTS && best_ms; ++t) best_ms[t] = 0.0;
   const int n[3] = {c->g.n0, c->g.n1, c->g.n2};
-  const bool weno = c->plan.conv == OSB_CONV_WENO5JS;
+  const bool weno = c->plan.conv == OSB_CONV_WENO5JS || c->plan.conv == OSB_CONV_WENO5Z;
   for (int d = 0; d < 3 && weno && err == cudaSuccess; ++d) {
     std::vector<WenoCfg> cand{{WENO_TILE, 32}};
     for (int kind : {WENO_MARCH4, WENO_MARCH8}) {

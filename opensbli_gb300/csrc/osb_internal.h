@@ -35,7 +35,8 @@ struct Ctx {
   cudaGraphExec_t graph[2] = {nullptr, nullptr};
   double graph_dt[2] = {0, 0};
   int64_t launches = 0;
-  WenoCfg wcfg[3] = {{WENO_TILE, 32}, {WENO_TILE, 32}, {WENO_TILE, 32}};
+  // WENO launch shapes: the autotuner's choice at 256^3 as the default (osb_autotune refines it)
+  WenoCfg wcfg[3] = {{WENO_MARCH4, 32}, {WENO_MARCH4, 48}, {WENO_MARCH4, 48}};
   int crk_ty = 8;             // tile height of the fused central/RK kernel (8 or 16)
   double *adj = nullptr;      // adjoint scratch (stage states, primitives, sensitivity fields)
   void *probe_buf = nullptr;  // point-probe requests and results (osb_probe)

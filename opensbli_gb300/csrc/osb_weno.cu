@@ -51,7 +51,7 @@ template <typename T, int D, typename Pt> __device__ __forceinline__ void load_p
 }
 }  // namespace
 
-template <typename T, int DIR, bool ACCUM>
+template <typename T, int DIR, bool ACCUM, int SCH>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fields5<const T> q, Fields5<T> res, Phys ph) {
   using Tl = WTile<DIR>;
   constexpr int TI = Tl::TI, TA = Tl::TA, NPT = TI + 5, FS = Tl::FS;
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
         if (d0 - 1 + m0 + w <= nd - 1) {
           load_point<T, DIR>(P, w + 5, W[5]);
           T fl[5];
-          interface_flux<T, DIR>(W, gm1, igm1, eps, fl);
+          interface_flux<T, DIR, SCH>(W, gm1, igm1, eps, fl);
 #pragma unroll
           for (int v = 0; v < 5; ++v) sflux[fidx(v, m0 + w, a)] = fl[v];
         }
@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
 
 // Line-marching flux kernel for DIR 1 (y) and 2 (z); block = 32 x-lanes by BY transverse lines,
 // blockIdx.z = segment of L cells along DIR.
-template <typename T, int DIR, bool ACCUM, int BY>
+template <typename T, int DIR, bool ACCUM, int BY, int SCH>
 __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> q, Fields5<T> res, const Phys &ph,
                                                 int L, int bx, int by, int bz) {
   static_assert(DIR == 1 || DIR == 2, "marching runs along y or z");
@@ -233,7 +233,7 @@ __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> 
       for (int v = 0; v < 5; ++v) rv[v] = res.v[v][mc];
     }
     T F[5];
-    interface_flux<T, DIR>(W, gm1, igm1, eps, F);
+    interface_flux<T, DIR, SCH>(W, gm1, igm1, eps, F);
     if (c > c0) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
@@ -248,10 +248,10 @@ __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> 
   }
 }
 
-template <typename T, int DIR, bool ACCUM, int BY>
+template <typename T, int DIR, bool ACCUM, int BY, int SCH>
 __global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 512 : 256) / (32 * BY))
     k_weno_march(Grid g, Fields5<const T> q, Fields5<T> res, Phys ph, int L) {
-  weno_march_tile<T, DIR, ACCUM, BY>(g, q, res, ph, L, blockIdx.x, blockIdx.y, blockIdx.z);
+  weno_march_tile<T, DIR, ACCUM, BY, SCH>(g, q, res, ph, L, blockIdx.x, blockIdx.y, blockIdx.z);
 }
 
 // Line-marching flux kernel for x.  A warp owns 32 consecutive y-lines of one z-plane and walks a
@@ -269,7 +269,7 @@ template <typename T> struct MX {
   static constexpr int WARP_ELEMS = 5 * 32 * QP + 5 * 32 * RP;
 };
 
-template <typename T, int BY>
+template <typename T, int BY, int SCH>
 __device__ __forceinline__ void weno_march_x_tile(const Grid &g, Fields5<const T> q, Fields5<T> res, const Phys &ph,
                                                   int L, int bx, int by, int bz, unsigned char *smem_raw) {
   using M = MX<T>;
@@ -347,7 +347,7 @@ __device__ __forceinline__ void weno_march_x_tile(const Grid &g, Fields5<const T
       if (p >= c0 + 2) {  // window holds points c-3 .. c+2 of interface c = p - 2
         const int c = p - 2;
         T F[5];
-        if (row_ok) interface_flux<T, 0>(W, gm1, igm1, eps, F);
+        if (row_ok) interface_flux<T, 0, SCH>(W, gm1, igm1, eps, F);
         if (c > c0) {
           const int cc = c - 1;  // cell finished by this interface
           const int gs = ((cc + 4) / RG) * RG - 4, col = cc - gs;
@@ -362,11 +362,11 @@ __device__ __forceinline__ void weno_march_x_tile(const Grid &g, Fields5<const T
   }
 }
 
-template <typename T, int BY>
+template <typename T, int BY, int SCH>
 __global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 512 : 256) / (32 * BY))
     k_weno_march_x(Grid g, Fields5<const T> q, Fields5<T> res, Phys ph, int L) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  weno_march_x_tile<T, BY>(g, q, res, ph, L, blockIdx.x, blockIdx.y, blockIdx.z, smem_raw);
+  weno_march_x_tile<T, BY, SCH>(g, q, res, ph, L, blockIdx.x, blockIdx.y, blockIdx.z, smem_raw);
 }
 
 template <typename T, int DIR> constexpr size_t tile_smem() {
@@ -374,8 +374,8 @@ template <typename T, int DIR> constexpr size_t tile_smem() {
   return sizeof(T) * ((size_t)W_NF * (Tl::TI + 5) * Tl::TA + 5 * (DIR == 0 ? Tl::TA * Tl::FS : Tl::TI * Tl::TA));
 }
 
-template <typename T, int DIR, bool ACCUM> static void launch_tile(const Ctx &c, Fields5<const T> q, Fields5<T> r,
-                                                                    cudaStream_t s) {
+template <typename T, int DIR, bool ACCUM, int SCH>
+static void launch_tile(const Ctx &c, Fields5<const T> q, Fields5<T> r, cudaStream_t s) {
   using Tl = WTile<DIR>;
   const int n[3] = {c.g.n0, c.g.n1, c.g.n2};
   const int nt = (n[DIR] + Tl::TI - 2) / (Tl::TI - 1);
@@ -383,36 +383,42 @@ template <typename T, int DIR, bool ACCUM> static void launch_tile(const Ctx &c,
   if (DIR == 0) grid = dim3(nt, (n[1] + Tl::TA - 1) / Tl::TA, n[2]);
   else if (DIR == 1) grid = dim3((n[0] + Tl::TA - 1) / Tl::TA, nt, n[2]);
   else grid = dim3((n[0] + Tl::TA - 1) / Tl::TA, n[1], nt);
-  k_weno<T, DIR, ACCUM><<<grid, 256, tile_smem<T, DIR>(), s>>>(c.g, q, r, c.ph);
+  k_weno<T, DIR, ACCUM, SCH><<<grid, 256, tile_smem<T, DIR>(), s>>>(c.g, q, r, c.ph);
 }
 
-template <typename T, int DIR, bool ACCUM, int BY>
+template <typename T, int DIR, bool ACCUM, int BY, int SCH>
 static void launch_march(const Ctx &c, Fields5<const T> q, Fields5<T> r, int L, cudaStream_t s) {
   const int nd = DIR == 1 ? c.g.n1 : c.g.n2, no = DIR == 1 ? c.g.n2 : c.g.n1;
   dim3 grid((c.g.n0 + 31) / 32, (no + BY - 1) / BY, (nd + L - 1) / L);
-  k_weno_march<T, DIR, ACCUM, BY><<<grid, dim3(32, BY), 0, s>>>(c.g, q, r, c.ph, L);
+  k_weno_march<T, DIR, ACCUM, BY, SCH><<<grid, dim3(32, BY), 0, s>>>(c.g, q, r, c.ph, L);
 }
 
 template <typename T, int BY> constexpr size_t march_x_smem() { return sizeof(T) * (size_t)BY * MX<T>::WARP_ELEMS; }
 
-template <typename T, int BY>
+template <typename T, int BY, int SCH>
 static void launch_march_x(const Ctx &c, Fields5<const T> q, Fields5<T> r, int L, cudaStream_t s) {
   dim3 grid((c.g.n0 + L - 1) / L, (c.g.n1 + 31) / 32, (c.g.n2 + BY - 1) / BY);
-  k_weno_march_x<T, BY><<<grid, dim3(32, BY), march_x_smem<T, BY>(), s>>>(c.g, q, r, c.ph, L);
+  k_weno_march_x<T, BY, SCH><<<grid, dim3(32, BY), march_x_smem<T, BY>(), s>>>(c.g, q, r, c.ph, L);
+}
+
+template <typename T, int DIR, bool ACCUM, int SCH>
+static void launch_shape(const Ctx &c, Fields5<const T> q, Fields5<T> r, WenoCfg w, cudaStream_t s) {
+  if constexpr (DIR == 0) {
+    static_assert(!ACCUM, "the x sweep writes the residual");
+    if (w.kind == WENO_TILE) launch_tile<T, DIR, ACCUM, SCH>(c, q, r, s);
+    else if (w.kind == WENO_MARCH4) launch_march_x<T, 4, SCH>(c, q, r, w.seg, s);
+    else launch_march_x<T, 8, SCH>(c, q, r, w.seg, s);
+  } else {
+    if (w.kind == WENO_TILE) launch_tile<T, DIR, ACCUM, SCH>(c, q, r, s);
+    else if (w.kind == WENO_MARCH4) launch_march<T, DIR, ACCUM, 4, SCH>(c, q, r, w.seg, s);
+    else launch_march<T, DIR, ACCUM, 8, SCH>(c, q, r, w.seg, s);
+  }
 }
 
 template <typename T, int DIR, bool ACCUM>
 static void launch_variant(const Ctx &c, Fields5<const T> q, Fields5<T> r, WenoCfg w, cudaStream_t s) {
-  if constexpr (DIR == 0) {
-    static_assert(!ACCUM, "the x sweep writes the residual");
-    if (w.kind == WENO_TILE) launch_tile<T, DIR, ACCUM>(c, q, r, s);
-    else if (w.kind == WENO_MARCH4) launch_march_x<T, 4>(c, q, r, w.seg, s);
-    else launch_march_x<T, 8>(c, q, r, w.seg, s);
-  } else {
-    if (w.kind == WENO_TILE) launch_tile<T, DIR, ACCUM>(c, q, r, s);
-    else if (w.kind == WENO_MARCH4) launch_march<T, DIR, ACCUM, 4>(c, q, r, w.seg, s);
-    else launch_march<T, DIR, ACCUM, 8>(c, q, r, w.seg, s);
-  }
+  if (c.plan.conv == OSB_CONV_WENO5Z) launch_shape<T, DIR, ACCUM, SCH_Z>(c, q, r, w, s);
+  else launch_shape<T, DIR, ACCUM, SCH_JS>(c, q, r, w, s);
 }
 
 template <typename T>
@@ -462,7 +468,7 @@ __global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 384 : 192) / (32 * 
       q.v[v] = d.q[parity][v];
       r.v[v] = d.res[v];
     }
-    weno_march_x_tile<T, BY>(d.g, q, r, d.ph, L, w.y, w.z, w.w, smem_raw);
+    weno_march_x_tile<T, BY, SCH_JS>(d.g, q, r, d.ph, L, w.y, w.z, w.w, smem_raw);
   }
 }
 
@@ -482,7 +488,7 @@ __global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 384 : 192) / (32 * 
       q.v[v] = d.q[parity][v];
       r.v[v] = d.res[v];
     }
-    weno_march_tile<T, DIR, true, BY>(d.g, q, r, d.ph, L, w.y, w.z, w.w);
+    weno_march_tile<T, DIR, true, BY, SCH_JS>(d.g, q, r, d.ph, L, w.y, w.z, w.w);
   }
 }
 
@@ -519,13 +525,22 @@ void launch_batch_weno(const int4 *items, int nitems, int *counter, int parity, 
 }
 
 template <typename T, int DIR, bool ACCUM> static void attr_dir() {
-  cudaFuncSetAttribute(k_weno<T, DIR, ACCUM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tile_smem<T, DIR>());
+  cudaFuncSetAttribute(k_weno<T, DIR, ACCUM, SCH_JS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)tile_smem<T, DIR>());
+  cudaFuncSetAttribute(k_weno<T, DIR, ACCUM, SCH_Z>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)tile_smem<T, DIR>());
 }
 template <typename T> void setup_weno() {
   cudaFuncSetAttribute(k_batch_weno_x<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_x_smem<T, 4>());
   cudaFuncSetAttribute(k_batch_weno_x<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_x_smem<T, 8>());
-  cudaFuncSetAttribute(k_weno_march_x<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_x_smem<T, 4>());
-  cudaFuncSetAttribute(k_weno_march_x<T, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_x_smem<T, 8>());
+  cudaFuncSetAttribute(k_weno_march_x<T, 4, SCH_JS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)march_x_smem<T, 4>());
+  cudaFuncSetAttribute(k_weno_march_x<T, 8, SCH_JS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)march_x_smem<T, 8>());
+  cudaFuncSetAttribute(k_weno_march_x<T, 4, SCH_Z>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)march_x_smem<T, 4>());
+  cudaFuncSetAttribute(k_weno_march_x<T, 8, SCH_Z>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)march_x_smem<T, 8>());
   attr_dir<T, 0, false>();
   attr_dir<T, 1, true>();
   attr_dir<T, 2, true>();

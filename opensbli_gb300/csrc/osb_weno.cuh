@@ -20,7 +20,8 @@
 // dot product g = (phi, -(g-1)u, g-1).X and h = X_{1+d} - u_d X_0 (the flux vector F is never
 // stored: its projections are formed from Q, u_d and p):
 //     acoustic+- . X = bt (g +- a h),   entropy . X = X_0 - g / a^2;
-// the smoothness indicators use Jiang and Shu's sum-of-squares form.  The nonlinear weights:
+// the smoothness indicators use Jiang and Shu's sum-of-squares form built from first and second
+// differences, and the candidates enter as p1 plus weighted third differences.  The nonlinear weights:
 // in FP32 alpha_r = d_r * rcp((eps+beta_r)^2) with the fast hardware reciprocal (2 ulp), applied to
 // the candidate differences (p_r - p_1) only; in FP64,
 // where every division costs a Newton sequence on the slow FP64 pipe, the three alphas are scaled
@@ -42,32 +43,60 @@ __device__ __forceinline__ void sqrt_rsqrt(double x, double &s, double &is) {
   is = 1.0 / s;
 }
 
-// One WENO5-JS side.  f0..f4 are the five stencil values ordered from the far upwind point to the
+// Schemes of the nonlinear weights
+enum { SCH_JS = 0, SCH_Z = 1 };
+
+// One WENO5 side.  f0..f4 are the five stencil values ordered from the far upwind point to the
 // far downwind one (for the right-going side: points i-2..i+2; for the left-going side the caller
 // passes points i+3..i-1).  d0 weights the most downwind candidate (3/10), d2 the most upwind (1/10).
-template <typename T> __device__ __forceinline__ T weno5_side(T f0, T f1, T f2, T f3, T f4, T eps) {
+// JS: alpha_r = d_r / (eps + beta_r)^2.  Z (weno.py:283-331, Borges et al.): alpha_r =
+// d_r (1 + (tau / (eps + beta_r))^2) with tau = |beta_0 - beta_2| (eps 1e-14 in the reference).
+template <typename T, int SCH> __device__ __forceinline__ T weno5_side(T f0, T f1, T f2, T f3, T f4, T eps) {
+  // first differences d_i = f_{i+1} - f_i; second differences t_r (the Jiang-Shu curvature terms);
+  // s_r the one-sided slopes of each candidate stencil
+  const T d0 = f1 - f0, d1 = f2 - f1, d2 = f3 - f2, d3 = f4 - f3;
+  const T t0 = d3 - d2, t1 = d2 - d1, t2 = d1 - d0;
+  const T s0 = d3 - T(3) * d2, s1 = d1 + d2, s2 = T(3) * d1 - d0;
   const T c13 = T(13.0 / 48.0), c14 = T(1.0 / 16.0);
-  const T t0 = f2 - T(2) * f3 + f4, s0 = T(3) * f2 - T(4) * f3 + f4;
-  const T t1 = f1 - T(2) * f2 + f3, s1 = f1 - f3;
-  const T t2 = f0 - T(2) * f1 + f2, s2 = f0 - T(4) * f1 + T(3) * f2;
   const T b0 = c13 * t0 * t0 + c14 * s0 * s0;
   const T b1 = c13 * t1 * t1 + c14 * s1 * s1;
   const T b2 = c13 * t2 * t2 + c14 * s2 * s2;
   const T e0 = b0 + eps, e1 = b1 + eps, e2 = b2 + eps;
-  const T p0 = T(1.0 / 6.0) * f2 + T(5.0 / 12.0) * f3 - T(1.0 / 12.0) * f4;
-  const T p1 = T(-1.0 / 12.0) * f1 + T(5.0 / 12.0) * f2 + T(1.0 / 6.0) * f3;
-  const T p2 = T(1.0 / 6.0) * f0 - T(7.0 / 12.0) * f1 + T(11.0 / 12.0) * f2;
+  const T q0 = e0 * e0, q1 = e1 * e1, q2 = e2 * e2;
+  // candidates (with the reference's factor 1/2): p1 = f2/2 + d1/12 + d2/6, and the other two
+  // through third differences, p0 - p1 = -(t0 - t1)/12, p2 - p1 = (t2 - t1)/6; the result
+  // sum_r omega_r p_r = p1 + omega_0 (p0 - p1) + omega_2 (p2 - p1) scales only those differences by
+  // the weights
+  const T p1 = T(0.5) * f2 + T(1.0 / 12.0) * d1 + T(1.0 / 6.0) * d2;
+  const T D0 = t0 - t1, D2 = t2 - t1;
   if (sizeof(T) == 8) {
-    const T q0 = e0 * e0, q1 = e1 * e1, q2 = e2 * e2;
-    const T a0 = T(3.0 / 10.0) * (q1 * q2), a1 = T(3.0 / 5.0) * (q0 * q2), a2 = T(1.0 / 10.0) * (q0 * q1);
-    return (a0 * p0 + a1 * p1 + a2 * p2) / (a0 + a1 + a2);
+    // alphas scaled by q0 q1 q2: one exact division per side
+    T a0, a1, a2;
+    if (SCH == SCH_Z) {
+      const T tt = (b0 - b2) * (b0 - b2);
+      a0 = T(3.0 / 10.0) * (q0 + tt) * (q1 * q2);
+      a1 = T(3.0 / 5.0) * (q1 + tt) * (q0 * q2);
+      a2 = T(1.0 / 10.0) * (q2 + tt) * (q0 * q1);
+    } else {
+      a0 = T(3.0 / 10.0) * (q1 * q2);
+      a1 = T(3.0 / 5.0) * (q0 * q2);
+      a2 = T(1.0 / 10.0) * (q0 * q1);
+    }
+    return p1 + (T(-1.0 / 12.0) * a0 * D0 + T(1.0 / 6.0) * a2 * D2) / (a0 + a1 + a2);
   } else {
-    // sum_r omega_r p_r written as p1 + omega_0 (p0 - p1) + omega_2 (p2 - p1): the weights' rounding
-    // (fast reciprocals) then scales only the small candidate differences, not the flux itself
-    const T a0 = T(3.0 / 10.0) * rcp_t(e0 * e0);
-    const T a1 = T(3.0 / 5.0) * rcp_t(e1 * e1);
-    const T a2 = T(1.0 / 10.0) * rcp_t(e2 * e2);
-    return p1 + (a0 * (p0 - p1) + a2 * (p2 - p1)) * rcp_t(a0 + a1 + a2);
+    // fast hardware reciprocals: their rounding scales only the small third differences
+    T a0, a1, a2;
+    if (SCH == SCH_Z) {
+      const T tt = (b0 - b2) * (b0 - b2);
+      a0 = T(3.0 / 10.0) + T(3.0 / 10.0) * tt * rcp_t(q0);
+      a1 = T(3.0 / 5.0) + T(3.0 / 5.0) * tt * rcp_t(q1);
+      a2 = T(1.0 / 10.0) + T(1.0 / 10.0) * tt * rcp_t(q2);
+    } else {
+      a0 = T(3.0 / 10.0) * rcp_t(q0);
+      a1 = T(3.0 / 5.0) * rcp_t(q1);
+      a2 = T(1.0 / 10.0) * rcp_t(q2);
+    }
+    return p1 + (T(-1.0 / 12.0) * a0 * D0 + T(1.0 / 6.0) * a2 * D2) * rcp_t(a0 + a1 + a2);
   }
 }
 
@@ -94,7 +123,7 @@ __device__ __forceinline__ void point_prims(const T (&r)[5], T gm1, T gama, WPt<
 }
 
 // Characteristic flux at the interface between window points 2 and 3 (points i and i+1).
-template <typename T, int D>
+template <typename T, int D, int SCH>
 __device__ __forceinline__ void interface_flux(const WPt<T> (&W)[6], const T gm1, const T igm1, const T eps,
                                                T out[5]) {
   constexpr int E1 = (D + 1) % 3, E2 = (D + 2) % 3;  // the two tangential axes (shear rows)
@@ -134,7 +163,8 @@ __device__ __forceinline__ void interface_flux(const WPt<T> (&W)[6], const T gm1
       fp[t] = cf[t] + lam * cs[t];
       fm[t] = cf[t] - lam * cs[t];
     }
-    return weno5_side(fp[0], fp[1], fp[2], fp[3], fp[4], eps) + weno5_side(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
+    return weno5_side<T, SCH>(fp[0], fp[1], fp[2], fp[3], fp[4], eps) +
+           weno5_side<T, SCH>(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
   };
 
   // ---- shear rows: LEV_r . X = (s/rho)(u_e X_0 - X_{1+e}); for X = F: X_0 = Q_{1+D}, X_{1+e} = Q_{1+e} u_D

@@ -40,7 +40,7 @@ class Plan:
     ndim: int = 3
     n: Tuple[int, int, int] = (64, 64, 64)
     delta: Tuple[float, float, float] = (2 * math.pi / 64,) * 3
-    conv: str = "central_skew"      # central_skew | weno5js | teno5
+    conv: str = "central_skew"      # central_skew | weno5js | weno5z | teno5
     visc: str = "const"             # none | const | sutherland
     rk: str = "rk3"                 # rk3 (2-register) | ls_rk3
     precision: str = "fp64"         # fp64 | mixed
@@ -95,10 +95,11 @@ def tgv_plan(n=64, conv="central_skew", precision="fp64", Minf=0.1, Re=1600.0, P
              dt=None, use_graphs=True):
     """3D Taylor-Green vortex on the periodic box [0, 2 pi)^3 with n^3 points (delta = 2 pi / n), the
     configuration of apps/taylor_green_vortex/taylor_green_vortex.py (conv='central_skew') and of the
-    WENO5-JS variant (conv='weno5js')."""
+    WENO5-JS and WENO5-Z variants (conv='weno5js', 'weno5z')."""
     ns = (n, n, n) if isinstance(n, int) else tuple(n)
     return Plan(n=ns, delta=tuple(2 * math.pi / k for k in ns), conv=conv, visc=visc, precision=precision, Minf=Minf,
                 Re=Re, Pr=Pr, gama=gama, dt=dt, use_graphs=use_graphs, ic="tgv",
+                weno_eps=1e-14 if conv == "weno5z" else 1e-6,  # WenoZ.eps / WenoJS.eps (weno.py)
                 name="tgv_%s_%d" % (conv, ns[0]))
 
 

@@ -13,7 +13,7 @@ import time
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--n", type=int, default=192)
-    ap.add_argument("--conv", default="weno5js", choices=["weno5js", "central_skew"])
+    ap.add_argument("--conv", default="weno5js", choices=["weno5js", "weno5z", "central_skew"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=0)
@@ -25,7 +25,7 @@ def main():
     import torch
     from .plan import tgv_plan, tgv_cfl_dt
     from .runtime import Solver
-    M = 1.25 if a.conv == "weno5js" else 0.1
+    M = 1.25 if a.conv.startswith("weno") else 0.1
     plan = tgv_plan(a.n, conv=a.conv, Minf=M, precision=a.precision, use_graphs=not a.no_graphs)
     dt = tgv_cfl_dt(plan)
     s = Solver(plan)

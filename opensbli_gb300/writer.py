@@ -112,15 +112,19 @@ class GB300Writer:
             if len(skew) != 3 or self._max_offset(self._kernels("Convective CD")) != 2:
                 raise NotImplementedError("Central(4) skew-symmetric convective terms expected")
         else:
-            conv = "weno5js"
+            conv = None
             if len(weno) != 3:
                 raise NotImplementedError("one LLFWeno reconstruction kernel per direction expected")
             for k in weno:
                 lhs = self._lhs_names(k)
                 if not {"beta_0", "beta_1", "beta_2", "alpha_0", "omega_0", "inv_alpha_sum"} <= lhs:
                     raise NotImplementedError("WENO5 reconstruction expected in %s" % k.computation_name)
-                if any(n.startswith("tau") for n in lhs):
-                    raise NotImplementedError("WENO-Z is not lowered; WENO-JS only")
+                # WenoZ's alphas carry the global indicator |beta_0 - beta_2| (weno.py:283-331)
+                alpha0 = [e for e in k.equations if str(e.lhs) == "alpha_0"]
+                kconv = "weno5z" if alpha0 and "Abs(" in str(alpha0[0].rhs) else "weno5js"
+                if conv not in (None, kconv):
+                    raise NotImplementedError("mixed WENO formulations across directions")
+                conv = kconv
                 if self._max_offset([k]) != 3:
                     raise NotImplementedError("5th-order stencil expected in %s" % k.computation_name)
                 avg = [e for e in k.equations if str(e.lhs).endswith("_rho") and str(e.lhs).startswith("AVG_")]
@@ -162,6 +166,7 @@ class GB300Writer:
             raise NotImplementedError("unsupported boundary conditions: %s" % (other_bc or bcs))
         return Plan(ndim=3, conv=conv, visc="const" if visc else "none", rk="rk3", precision=precision,
                     bc=tuple(tuple(p) for p in bcs), rk_a=coeff["rkold"], rk_b=coeff["rknew"],
+                    weno_eps=1e-14 if conv == "weno5z" else 1e-6,  # WenoZ.eps / WenoJS.eps (weno.py)
                     use_graphs=use_graphs, ic="host", kernels=[n for n in names if n])
 
     def _rk_coefficients(self, names_expected):

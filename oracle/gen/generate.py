@@ -27,6 +27,7 @@ CASES = {
     "tgv_central": "ref:apps/taylor_green_vortex/taylor_green_vortex.py",
     "tgsym_central": "ref:apps/taylor_green_vortex/TGsym/TGsym.py",
     "tgv_weno": "tgv_weno.py",
+    "tgv_wenoz": "tgv_wenoz.py",
     "katzer_teno": "katzer_teno.py",
 }
 

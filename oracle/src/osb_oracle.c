@@ -298,6 +298,7 @@ static void residual_viscous(st_t *s) {
  *   464-495); lambda_r = max over the six points of |ev_r| from the point values (u, a) (:512-536);
  *   F+- = 1/2 (CF +- lambda CS).
  *   WENO5-JS (weno.py:70-205, 341-369): alpha_r = d_r/(1e-6 + beta_r)^2, omega_r = alpha_r/sum,
+ *   or WENO5-Z (weno.py:283-331): alpha_r = d_r (1 + (tau/(1e-14 + beta_r))^2), tau = |beta_0 - beta_2|,
  *   candidate polynomials c_rj, optimal weights d = (3/10, 3/5, 1/10).
  *   Flux at i+1/2 = REV.(Fhat+ + Fhat-) (shock_capturing.py:418-448).
  * ------------------------------------------------------------------------------------------- */
@@ -305,7 +306,7 @@ static void residual_viscous(st_t *s) {
  * folds the 1/2 into the smoothness indicators (1/4 of Jiang-Shu's, expanded as products) and into
  * the candidate stencils (1/2 of the usual c_rj).  The expressions below keep that form and term
  * order.  fp = f at points i-2..i+2 (upwind side), fm = f at points i-1..i+3. */
-static double weno5js_plus(const double f[5]) {
+static double weno5_plus(const double f[5], int z) {
   const double b0 = 0.5 * f[2] * ((5.0 / 3.0) * f[2] - (31.0 / 6.0) * f[3] + (11.0 / 6.0) * f[4]) +
                     0.5 * f[3] * ((25.0 / 6.0) * f[3] - (19.0 / 6.0) * f[4]) + (1.0 / 3.0) * f[4] * f[4];
   const double b1 = 0.5 * f[1] * ((2.0 / 3.0) * f[1] - (13.0 / 6.0) * f[2] + (5.0 / 6.0) * f[3]) +
@@ -313,15 +314,23 @@ static double weno5js_plus(const double f[5]) {
   const double b2 = 0.5 * f[0] * ((2.0 / 3.0) * f[0] + (11.0 / 6.0) * f[2]) +
                     0.5 * f[1] * (-(19.0 / 6.0) * f[0] + (25.0 / 6.0) * f[1] - (31.0 / 6.0) * f[2]) +
                     (5.0 / 6.0) * f[2] * f[2];
-  const double a0 = (3.0 / 10.0) / ((b0 + 1e-6) * (b0 + 1e-6));
-  const double a1 = (3.0 / 5.0) / ((b1 + 1e-6) * (b1 + 1e-6));
-  const double a2 = (1.0 / 10.0) / ((b2 + 1e-6) * (b2 + 1e-6));
+  double a0, a1, a2;
+  if (z) {  /* WENO-Z (weno.py:283-331): d_r + d_r tau^2 / (beta_r + 1e-14)^2, tau = |beta_0 - beta_2| */
+    const double t = fabs(b0 - b2);
+    a0 = (3.0 / 10.0) + (3.0 / 10.0) * (t * t) / ((b0 + 1.0e-14) * (b0 + 1.0e-14));
+    a1 = (3.0 / 5.0) + (3.0 / 5.0) * (t * t) / ((b1 + 1.0e-14) * (b1 + 1.0e-14));
+    a2 = (1.0 / 10.0) + (1.0 / 10.0) * (t * t) / ((b2 + 1.0e-14) * (b2 + 1.0e-14));
+  } else {
+    a0 = (3.0 / 10.0) / ((b0 + 1e-6) * (b0 + 1e-6));
+    a1 = (3.0 / 5.0) / ((b1 + 1e-6) * (b1 + 1e-6));
+    a2 = (1.0 / 10.0) / ((b2 + 1e-6) * (b2 + 1e-6));
+  }
   const double inv = 1.0 / (a0 + a1 + a2);
   return a0 * inv * ((1.0 / 6.0) * f[2] + (5.0 / 12.0) * f[3] - (1.0 / 12.0) * f[4]) +
          a1 * inv * (-(1.0 / 12.0) * f[1] + (5.0 / 12.0) * f[2] + (1.0 / 6.0) * f[3]) +
          a2 * inv * ((1.0 / 6.0) * f[0] - (7.0 / 12.0) * f[1] + (11.0 / 12.0) * f[2]);
 }
-static double weno5js_minus(const double g[5]) {
+static double weno5_minus(const double g[5], int z) {
   /* g[0..4] = f at points i-1..i+3 (f1..f5 in the six-point numbering) */
   const double f1 = g[0], f2 = g[1], f3 = g[2], f4 = g[3], f5 = g[4];
   const double b0 = 0.5 * f3 * ((5.0 / 3.0) * f3 - (31.0 / 6.0) * f4 + (11.0 / 6.0) * f5) +
@@ -330,9 +339,17 @@ static double weno5js_minus(const double g[5]) {
                     0.5 * f3 * ((13.0 / 6.0) * f3 - (13.0 / 6.0) * f4) + (1.0 / 3.0) * f4 * f4;
   const double b2 = 0.5 * f1 * ((2.0 / 3.0) * f1 - (19.0 / 6.0) * f2 + (11.0 / 6.0) * f3) +
                     0.5 * f2 * ((25.0 / 6.0) * f2 - (31.0 / 6.0) * f3) + (5.0 / 6.0) * f3 * f3;
-  const double a0 = (1.0 / 10.0) / ((b0 + 1e-6) * (b0 + 1e-6));
-  const double a1 = (3.0 / 5.0) / ((b1 + 1e-6) * (b1 + 1e-6));
-  const double a2 = (3.0 / 10.0) / ((b2 + 1e-6) * (b2 + 1e-6));
+  double a0, a1, a2;
+  if (z) {
+    const double t = fabs(b0 - b2);
+    a0 = (1.0 / 10.0) + (1.0 / 10.0) * (t * t) / ((b0 + 1.0e-14) * (b0 + 1.0e-14));
+    a1 = (3.0 / 5.0) + (3.0 / 5.0) * (t * t) / ((b1 + 1.0e-14) * (b1 + 1.0e-14));
+    a2 = (3.0 / 10.0) + (3.0 / 10.0) * (t * t) / ((b2 + 1.0e-14) * (b2 + 1.0e-14));
+  } else {
+    a0 = (1.0 / 10.0) / ((b0 + 1e-6) * (b0 + 1e-6));
+    a1 = (3.0 / 5.0) / ((b1 + 1e-6) * (b1 + 1e-6));
+    a2 = (3.0 / 10.0) / ((b2 + 1e-6) * (b2 + 1e-6));
+  }
   const double inv = 1.0 / (a0 + a1 + a2);
   return a0 * inv * ((11.0 / 12.0) * f3 - (7.0 / 12.0) * f4 + (1.0 / 6.0) * f5) +
          a1 * inv * ((1.0 / 6.0) * f2 + (5.0 / 12.0) * f3 - (1.0 / 12.0) * f4) +
@@ -444,7 +461,7 @@ static void residual_weno(st_t *s) {
           fp[t] = CF[r][t] + lam[r] * CS[r][t];
           fm[t] = CF[r][t + 1] - lam[r] * CS[r][t + 1];
         }
-        rec[r] = weno5js_plus(fp) + weno5js_minus(fm);
+        rec[r] = weno5_plus(fp, s->c.conv == OSBO_CONV_WENO5Z) + weno5_minus(fm, s->c.conv == OSBO_CONV_WENO5Z);
       }
       for (int v = 0; v < 5; ++v) {
         double fl = 0;

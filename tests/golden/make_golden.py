@@ -31,6 +31,7 @@ VARS = ["rho", "rhou0", "rhou1", "rhou2", "rhoE"]
 CASES = {
     "tgv_central": (16, 20, {"dt": 5e-3}),
     "tgv_weno": (16, 10, {"dt": 2e-3, "Minf": 1.25}),
+    "tgv_wenoz": (16, 10, {"dt": 2e-3, "Minf": 1.25}),
     "tgsym_central": (17, 10, {"dt": 5e-3}),
 }
 
@@ -77,10 +78,14 @@ def main2d(ref):
         print("wrote", case, fin["rho"].shape)
 
 
-def main(ref="/root/reference"):
-    main2d(ref)
-    katzer_profile(ref)
+def main(ref="/root/reference", only=None):
+    """Regenerate every fixture, or only the 3D case `only`."""
+    if only is None:
+        main2d(ref)
+        katzer_profile(ref)
     for case, (n, steps, extra) in CASES.items():
+        if only is not None and case != only:
+            continue
         if not refrun.available(case):
             subprocess.check_call([sys.executable, os.path.join(REPO, "oracle", "gen", "generate.py"), "--case", case,
                                    "--ref", ref])

