@@ -182,6 +182,13 @@ int osb_profile_read(osb_ctx *ctx, double *total_ms, int64_t *counts, int n);
 int osb_set_weno_shape(osb_ctx *ctx, int dir, int kind, int seg);
 int osb_get_weno_shape(osb_ctx *ctx, int dir, int *kind, int *seg);
 int osb_set_central_shape(osb_ctx *ctx, int ty);
+/* The fused central/RK kernel of FP32 plans with WENO fluxes brings its conserved planes into shared
+ * memory with TMA (cp.async.bulk.tensor, mbarrier-completed, two planes ahead).  osb_set_tma(ctx, 0)
+ * selects the register-staged loads instead (same results); osb_tma_active reports 1 when the TMA
+ * path serves the bound state.  A TMA wait that gives up sets a device status word, reported as
+ * OSB_ETIMEOUT by the next osb_reduce. */
+int osb_set_tma(osb_ctx *ctx, int enable);
+int osb_tma_active(osb_ctx *ctx);
 int osb_get_central_shape(osb_ctx *ctx, int *ty);
 int osb_autotune(osb_ctx *ctx, int reps, double *best_ms);
 

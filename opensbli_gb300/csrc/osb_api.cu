@@ -492,6 +492,49 @@ __global__ void k_reduce2(Grid g, D4 q, int what, double *partial) {
 }  // namespace
 
 namespace osb {
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link against libcuda)
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+static EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      p = nullptr;
+    return reinterpret_cast<EncodeTiledFn>(p);
+  }();
+  return fn;
+}
+
+// Boxes of 40 x (TY+4) x 1 elements of one padded conserved array: x from interior i0-4 (a multiple
+// of 32 in padded coordinates, so every copy starts on a 16-byte boundary), all rows of the plane's
+// tile and its 2-point halo.  Out-of-range parts of a box read as zeros (never used).
+int encode_state_maps(Ctx &c, int buf) {
+  c.tma_ok[buf] = 0;
+  EncodeTiledFn fn = encode_tiled();
+  if (!fn || c.plan.ndim != 3 || !c.mixed) return OSB_OK;  // the TMA path serves FP32 3D states
+  void *const *arrays = buf == 0 ? c.qa : c.qb;
+  for (int v = 0; v < 5; ++v)
+    if (!arrays[v] || (reinterpret_cast<uintptr_t>(arrays[v]) & 15)) return OSB_OK;
+  const size_t e = (size_t)c.elem;
+  const cuuint64_t dims[3] = {(cuuint64_t)c.g.sy, (cuuint64_t)(c.g.n1 + 2 * HY), (cuuint64_t)(c.g.n2 + 2 * HZ)};
+  const cuuint64_t strides[2] = {(cuuint64_t)(c.g.sy * e), (cuuint64_t)(c.g.sz * e)};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  for (int t = 0; t < 2; ++t) {
+    const cuuint32_t box[3] = {40, (cuuint32_t)((t == 0 ? 8 : 16) + 4), 1};
+    for (int v = 0; v < 5; ++v) {
+      CUresult r = fn(&c.tma[buf][t].m[v], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, arrays[v], dims, strides, box, estr,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+      if (r != CUDA_SUCCESS) return OSB_OK;  // keep the register path
+    }
+  }
+  c.tma_ok[buf] = 1;
+  return OSB_OK;
+}
+
 int plan_validate(const osb_plan_desc *p, char *why, size_t n) { return validate(p, why, n); }
 Grid plan_grid(const osb_plan_desc *p) { return make_grid(p); }
 Phys plan_phys(const osb_plan_desc *plan) {
@@ -637,11 +680,14 @@ int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
   }
   c->red_blocks = 152 * 8;
   if (e == cudaSuccess) e = cudaMalloc(&c->red, (c->red_blocks + 1) * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(c->d_status, 0, sizeof(int));
   if (e != cudaSuccess) {
     fprintf(stderr, "osb_create: %s\n", cudaGetErrorString(e));
     osb_destroy(c);
     return OSB_ECUDA;
   }
+  if (plan->ndim == 3) encode_state_maps(*c, 1);
   *out = c;
   return OSB_OK;
 }
@@ -654,6 +700,7 @@ int osb_bind_field(osb_ctx *c, int var, void *dev_ptr) {
   if (c->plan.ndim == 2 && !c->mixed) c->q64_2d[var] = static_cast<double *>(dev_ptr);
   c->qold_valid = 0;
   c->cur = 0;
+  if (c->plan.ndim == 3) encode_state_maps(*c, 0);
   for (int s = 0; s < 2; ++s)
     if (c->graph[s]) { cudaGraphExecDestroy(c->graph[s]); c->graph[s] = nullptr; }
   return OSB_OK;
@@ -855,9 +902,13 @@ int osb_reduce(osb_ctx *c, int what, double *out) {
   k_reduce_final<<<1, RED_THREADS, 0, c->stream>>>(c->red, nb, what, 1.0 / (double)N, c->red + c->red_blocks);
   double h = 0;
   cudaError_t e = cudaMemcpyAsync(&h, c->red + c->red_blocks, sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+  int status = 0;
+  if (e == cudaSuccess && c->d_status)
+    e = cudaMemcpyAsync(&status, c->d_status, sizeof(int), cudaMemcpyDeviceToHost, c->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
   if (e != cudaSuccess) return cuda_err(c, e, "osb_reduce");
   *out = h;
+  if (status) return set_err(c, OSB_ETIMEOUT, "a bounded device wait gave up in an earlier step (status word set)");
   if (what == OSB_RED_NANCHECK && h != 0.0) return set_err(c, OSB_ENONFINITE, "non-finite value in the state");
   return OSB_OK;
 }
@@ -1023,6 +1074,20 @@ int osb_set_central_shape(osb_ctx *c, int ty) {
   return OSB_OK;
 }
 
+int osb_set_tma(osb_ctx *c, int enable) {
+  if (!c) return OSB_EINVAL;
+  c->tma_enabled = enable ? 1 : 0;
+  drop_graphs(c);
+  return OSB_OK;
+}
+
+int osb_tma_active(osb_ctx *c) {
+  if (!c) return OSB_EINVAL;
+  const int buf_ok = c->cur == 0 ? c->tma_ok[0] : c->tma_ok[1];
+  return (c->tma_enabled && buf_ok && c->plan.ndim == 3 && c->mixed &&
+          (c->plan.conv == OSB_CONV_WENO5JS || c->plan.conv == OSB_CONV_WENO5Z)) ? 1 : 0;
+}
+
 int osb_get_central_shape(osb_ctx *c, int *ty) {
   if (!c || !ty) return OSB_EINVAL;
   *ty = c->crk_ty;
@@ -1057,6 +1122,7 @@ void osb_destroy(osb_ctx *c) {
     cudaFree(c->res[v]);
   }
   cudaFree(c->red);
+  cudaFree(c->d_status);
   cudaFree(c->adj);
   cudaFree(c->probe_buf);
   for (int v = 0; v < 4; ++v) {

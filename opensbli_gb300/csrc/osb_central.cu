@@ -42,18 +42,19 @@ template <int MODE> __host__ __device__ constexpr int ring_fields() { return (MO
 template <typename T, int MODE, int TY> __host__ __device__ constexpr int central_min_blocks() {
   return sizeof(T) != 4 ? 1 : (MODE & CRK_SKEW) ? (TY == 8 ? 3 : 1) : 1024 / (TX * TY);
 }
-template <typename T, int MODE, int TY> constexpr size_t ring_bytes() {
+template <typename T, int MODE, int TY> __host__ __device__ constexpr size_t ring_bytes() {
   return sizeof(T) * (size_t)NP * ring_fields<MODE>() * (TY + 4) * PX;
 }
 }  // namespace
 
 // One tile: output points (bx*32 .. +31, by*TY .. +TY-1) for the z-planes of chunk bz.  Called by
 // the per-block kernel below and by the batched persistent kernel (osb_batch.cu).
-template <typename T, int MODE, int TY>
+template <typename T, int MODE, int TY, bool TMA = false>
 __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold,
                                              Fields5<T> rin, Fields5<T> rout, const Phys &ph, double dt_new,
                                              double dt_old, T ddt, int zchunk, int bx, int by, int bz,
-                                             unsigned char *smem_raw) {
+                                             unsigned char *smem_raw, const TmaPlanes *tp = nullptr,
+                                             int *status = nullptr) {
   constexpr int NF = ring_fields<MODE>(), PY = TY + 4;
   T *ring = reinterpret_cast<T *>(smem_raw);  // [NP][NF][PY][PX]
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
@@ -81,6 +82,22 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
       }
     }
   };
+  // primitives of one point into ring slot sl at (py, px)
+  auto put = [&](int sl, int py, int px, T rho, T r0, T r1, T r2, T E) {
+    const T irho = T(1) / rho;  // correctly rounded: u and T feed the viscous terms
+    const T u0 = r0 * irho, u1 = r1 * irho, u2 = r2 * irho;
+    const T half = T(0.5);
+    const T p = gm1 * (E - half * rho * u0 * u0 - half * rho * u1 * u1 - half * rho * u2 * u2);
+    at(sl, F_U0, py, px) = u0;
+    at(sl, F_U1, py, px) = u1;
+    at(sl, F_U2, py, px) = u2;
+    at(sl, F_T, py, px) = gM2 * p * irho;
+    if (NF == 7) {
+      at(sl, F_RHO, py, px) = rho;
+      at(sl, F_P, py, px) = p;
+      at(sl, F_E, py, px) = E;
+    }
+  };
   auto store = [&](int k) {
     const int sl = slot(k);
 #pragma unroll
@@ -88,22 +105,50 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
       const int e = tid + r * TX * TY;
       const int px = e % PX, py = e / PX;
       const int i = i0 - 2 + px, j = j0 - 2 + py;
-      if (e < PX * PY && i < g.n0 + 2 && j < g.n1 + 2 && k < g.n2 + 2) {
-        const T rho = pre[r][0];
-        const T irho = T(1) / rho;  // correctly rounded: u and T feed the viscous terms
-        const T u0 = pre[r][1] * irho, u1 = pre[r][2] * irho, u2 = pre[r][3] * irho;
-        const T E = pre[r][4];
-        const T half = T(0.5);
-        const T p = gm1 * (E - half * rho * u0 * u0 - half * rho * u1 * u1 - half * rho * u2 * u2);
-        at(sl, F_U0, py, px) = u0;
-        at(sl, F_U1, py, px) = u1;
-        at(sl, F_U2, py, px) = u2;
-        at(sl, F_T, py, px) = gM2 * p * irho;
-        if (NF == 7) {
-          at(sl, F_RHO, py, px) = rho;
-          at(sl, F_P, py, px) = p;
-          at(sl, F_E, py, px) = E;
-        }
+      if (e < PX * PY && i < g.n0 + 2 && j < g.n1 + 2 && k < g.n2 + 2)
+        put(sl, py, px, pre[r][0], pre[r][1], pre[r][2], pre[r][3], pre[r][4]);
+    }
+  };
+
+  // TMA path: the conserved planes arrive as boxes of RX x PY points per field (x from i0-4, so the
+  // copy starts on a 16-byte boundary), NS planes ahead, each completing on its own mbarrier
+  constexpr int NS = 2, RX = 40;
+  constexpr uint32_t PLANE_BYTES = 5u * RX * PY * sizeof(T);
+  __shared__ __align__(8) uint64_t bars[NS];
+  __shared__ int failed;
+  T *raw = reinterpret_cast<T *>(smem_raw + ((ring_bytes<T, MODE, TY>() + 127) / 128) * 128);  // [NS][5][PY][RX]
+  const int zfirst = k0 - 2, zlast = min(k1 + 1, g.n2 + 1);
+  auto issue = [&](int z) {  // one thread
+    const int st = (z - zfirst) % NS;
+    mbar_expect_tx(&bars[st], PLANE_BYTES);
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+      tma_load_3d(raw + (st * 5 + v) * PY * RX, &tp->m[v], i0, j0 - 2 + HY, z + HZ, &bars[st]);
+  };
+  auto wait_plane = [&](int z) {
+    const int st = (z - zfirst) % NS;
+    const uint32_t par = ((z - zfirst) / NS) & 1u;
+    if (failed) return;
+    for (uint32_t it = 0;; ++it) {
+      if (mbar_try_wait(&bars[st], par)) return;
+      if (it > (1u << 22)) {  // bounded: report through the status word and carry on
+        failed = 1;
+        if (status) atomicExch(status, 1);
+        return;
+      }
+    }
+  };
+  auto convert = [&](int z) {  // raw plane z -> ring
+    const int st = (z - zfirst) % NS, sl = slot(z);
+    const T *b = raw + st * 5 * PY * RX;
+#pragma unroll
+    for (int r = 0; r < PPT; ++r) {
+      const int e = tid + r * TX * TY;
+      const int px = e % PX, py = e / PX;
+      const int i = i0 - 2 + px, j = j0 - 2 + py;
+      if (e < PX * PY && i < g.n0 + 2 && j < g.n1 + 2) {
+        const int o = py * RX + px + 2;
+        put(sl, py, px, b[o], b[PY * RX + o], b[2 * PY * RX + o], b[3 * PY * RX + o], b[4 * PY * RX + o]);
       }
     }
   };
@@ -113,13 +158,40 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
   const T idl[3] = {pick<T>(ph.inv_delta[0], ph.f_inv_delta[0]), pick<T>(ph.inv_delta[1], ph.f_inv_delta[1]),
                     pick<T>(ph.inv_delta[2], ph.f_inv_delta[2])};
 
-  for (int k = k0 - 2; k < k0 + 3; ++k) {
-    fetch(k);
-    store(k);
+  if constexpr (TMA) {
+    // every TMA destination must sit on a 128-byte boundary: refuse (status 2) rather than copy
+    if ((smem_u32(raw) & 127u) != 0u) {
+      if (tid == 0 && status) atomicExch(status, 2);
+      return;
+    }
+    if (tid == 0) {
+      for (int s = 0; s < NS; ++s) mbar_init(&bars[s], 1);
+      failed = 0;
+      fence_async_smem();
+    }
+    __syncthreads();
+    if (tid == 0)
+      for (int z = zfirst; z < zfirst + NS && z <= zlast; ++z) issue(z);
+    for (int z = k0 - 2; z < k0 + 3; ++z) {
+      wait_plane(z);
+      convert(z);
+      __syncthreads();  // ring visible; the raw stage of z may be refilled
+      if (tid == 0 && z + NS <= zlast) issue(z + NS);
+    }
+  } else {
+    for (int k = k0 - 2; k < k0 + 3; ++k) {
+      fetch(k);
+      store(k);
+    }
   }
   for (int k = k0; k < k1; ++k) {
     __syncthreads();
-    if (k + 3 < k1 + 2) fetch(k + 3);
+    if constexpr (TMA) {
+      // the raw stage of plane k+2 (converted at the end of the previous iteration) is free now
+      if (k > k0 && tid == 0 && k + 2 + NS <= zlast) issue(k + 2 + NS);
+    } else {
+      if (k + 3 < k1 + 2) fetch(k + 3);
+    }
     const int i = i0 + tx, j = j0 + ty;
     const bool active = i < g.n0 && j < g.n1;
     // the residual already in rin and the FP64 register at the output point, loaded early
@@ -292,7 +364,22 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
       }
     }
     __syncthreads();
-    if (k + 3 < k1 + 2) store(k + 3);
+    if (k + 3 < k1 + 2) {
+      if constexpr (TMA) {
+        wait_plane(k + 3);
+        convert(k + 3);
+      } else {
+        store(k + 3);
+      }
+    }
+  }
+  if constexpr (TMA) {
+    // after a timed-out wait, give copies still in flight a bounded chance to land before the
+    // block's shared memory is released
+    if (failed && tid == 0)
+      for (int s = 0; s < NS; ++s)
+        for (uint32_t it = 0; it < (1u << 20); ++it)
+          if (mbar_try_wait(&bars[s], 0u) || mbar_try_wait(&bars[s], 1u)) break;
   }
 }
 
@@ -304,6 +391,26 @@ __global__ void __launch_bounds__(TX * TY, central_min_blocks<T, MODE, TY>())
   central_tile<T, MODE, TY>(g, q, qnew, qold, rin, rout, ph, dt_new, dt_old, ddt, zchunk, blockIdx.x, blockIdx.y,
                             blockIdx.z,
                             smem_raw);
+}
+
+// the same kernel with the conserved planes brought in by TMA (FP32 state, residual-input modes)
+template <typename T, int MODE, int TY>
+__global__ void __launch_bounds__(TX * TY, central_min_blocks<T, MODE, TY>())
+    k_central_rk_tma(const __grid_constant__ TmaPlanes maps, Grid g, Fields5<T> qnew, Fields5<double> qold,
+                     Fields5<T> rin, Fields5<T> rout, Phys ph, double dt_new, double dt_old, T ddt, int zchunk,
+                     int *status) {
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  // TMA destinations must start on 128-byte boundaries of the shared window; the dynamic region
+  // follows the static shared variables, so align its base explicitly (128 bytes are reserved)
+  unsigned char *base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+  Fields5<const T> qnull{};
+  central_tile<T, MODE, TY, true>(g, qnull, qnew, qold, rin, rout, ph, dt_new, dt_old, ddt, zchunk, blockIdx.x,
+                                  blockIdx.y, blockIdx.z, base, &maps, status);
+}
+
+template <typename T, int MODE, int TY> constexpr size_t tma_smem_bytes() {
+  // 128 bytes of slack for aligning the region's base, the ring rounded to 128, two raw planes
+  return 128 + ((ring_bytes<T, MODE, TY>() + 127) / 128) * 128 + 2 * 5 * 40 * (TY + 4) * sizeof(T);
 }
 
 // resident blocks per SM of one kernel instance (occupancy calculator, cached per instance)
@@ -318,9 +425,39 @@ template <typename T, int MODE, int TY> static int resident_per_sm() {
   return nb;
 }
 
+template <typename T, int MODE, int TY> static int resident_per_sm_tma() {
+  static int nb = [] {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_central_rk_tma<T, MODE, TY>, TX * TY,
+                                                      tma_smem_bytes<T, MODE, TY>()) != cudaSuccess || b < 1)
+      b = 1;
+    return b;
+  }();
+  return nb;
+}
+
 template <typename T, int MODE, int TY>
 static void launch_mode(const Ctx &c, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold, Fields5<T> rin,
                         Fields5<T> rout, double dt_new, double dt_old, cudaStream_t s) {
+  // TMA plane loads: FP32 state with the residual-input modes (the skew modes' 7-field ring leaves no
+  // shared memory for the staging buffers without losing resident blocks)
+  constexpr bool tma_mode = sizeof(T) == 4 && (MODE & CRK_RIN) && !(MODE & CRK_SKEW);
+  if constexpr (tma_mode) {
+    const int buf = q.v[0] == static_cast<const T *>(c.qa[0]) ? 0 : q.v[0] == static_cast<const T *>(c.qb[0]) ? 1 : -1;
+    if (buf >= 0 && c.tma_enabled && c.tma_ok[buf] && c.d_status) {
+      const TmaPlanes &maps = c.tma[buf][TY == 16 ? 1 : 0];
+      const int bx = (c.g.n0 + TX - 1) / TX, by = (c.g.n1 + TY - 1) / TY;
+      const int resident = c.num_sms * resident_per_sm_tma<T, MODE, TY>();
+      int nzc = (4 * resident + bx * by - 1) / (bx * by);
+      nzc = max(1, min(nzc, (c.g.n2 + 7) / 8));
+      const int zchunk = (c.g.n2 + nzc - 1) / nzc;
+      nzc = (c.g.n2 + zchunk - 1) / zchunk;
+      const T ddt = (T)(dt_new - dt_old);
+      k_central_rk_tma<T, MODE, TY><<<dim3(bx, by, nzc), dim3(TX, TY), tma_smem_bytes<T, MODE, TY>(), s>>>(
+          maps, c.g, qnew, qold, rin, rout, c.ph, dt_new, dt_old, ddt, zchunk, c.d_status);
+      return;
+    }
+  }
   const int bx = (c.g.n0 + TX - 1) / TX, by = (c.g.n1 + TY - 1) / TY;
   // z-chunks: about four waves of resident blocks so the last wave's tail is short; at least 8
   // planes per chunk so the 4 halo planes of each chunk cost at most half a chunk's loads
@@ -365,6 +502,13 @@ void launch_central_rk(const Ctx &c, Fields5<const T> q, Fields5<T> qnew, Fields
   }
 }
 
+template <typename T, int MODE> static void attr_tma() {
+  cudaFuncSetAttribute(k_central_rk_tma<T, MODE, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)tma_smem_bytes<T, MODE, 8>());
+  cudaFuncSetAttribute(k_central_rk_tma<T, MODE, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)tma_smem_bytes<T, MODE, 16>());
+}
+
 template <typename T, int MODE> static void attr_mode() {
   cudaFuncSetAttribute(k_central_rk<T, MODE, 8>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)ring_bytes<T, MODE, 8>());
@@ -382,6 +526,12 @@ template <typename T> void setup_central() {
   attr_mode<T, CRK_RIN | CRK_UPDATE>();
   attr_mode<T, CRK_RIN>();
   attr_batch<T>();
+  if constexpr (sizeof(T) == 4) {
+    attr_tma<T, CRK_VISC | CRK_RIN | CRK_UPDATE>();
+    attr_tma<T, CRK_VISC | CRK_RIN>();
+    attr_tma<T, CRK_RIN | CRK_UPDATE>();
+    attr_tma<T, CRK_RIN>();
+  }
 }
 // Descriptor table of the batch being stepped, in this module's constant memory: the persistent
 // kernels read an instance's grid, constants and pointers through the constant cache (uniform per

@@ -5,6 +5,7 @@
 // sizes), 3 in y and z (the WENO5/TENO5 stencil reaches 3 points; central 4th order reaches 2).
 #pragma once
 #include <cstdint>
+#include <cuda.h>  // CUtensorMap (the type only; maps are encoded through the runtime's driver entry point)
 #include <cuda_runtime.h>
 
 namespace osb {
@@ -45,6 +46,41 @@ template <> __host__ __device__ __forceinline__ float pick<float>(double, float 
 template <typename T> __device__ __forceinline__ T sqrt_t(T x);
 template <> __device__ __forceinline__ float sqrt_t<float>(float x) { return sqrtf(x); }
 template <> __device__ __forceinline__ double sqrt_t<double>(double x) { return sqrt(x); }
+
+// tensor maps of the five conserved arrays of one state buffer (for one box shape)
+struct TmaPlanes {
+  CUtensorMap m[5];
+};
+
+// ---- TMA (cp.async.bulk.tensor) and mbarrier helpers
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+// make the initialised barriers visible to the asynchronous (TMA) proxy
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// 3D tiled bulk copy global -> shared of the box at (x, y, z) described by *map, completing on *bar
+__device__ __forceinline__ void tma_load_3d(void *dst, const void *map, int x, int y, int z, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(smem_u32(dst)),
+      "l"(map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
 
 // bring the line holding *p into L2 (a hint: no register is written, nothing waits for it)
 __device__ __forceinline__ void prefetch_l2(const void *p) {

@@ -39,6 +39,12 @@ struct Ctx {
   WenoCfg wcfg[3] = {{WENO_MARCH4, 32}, {WENO_MARCH4, 48}, {WENO_MARCH4, 48}};
   int crk_ty = 8;             // tile height of the fused central/RK kernel (8 or 16)
   double *adj = nullptr;      // adjoint scratch (stage states, primitives, sensitivity fields)
+  // TMA tensor maps of the two state buffers (qa, qb) for the central kernel's plane boxes, tile
+  // heights 8 and 16; a device status word that bounded device waits set when they give up
+  TmaPlanes tma[2][2];
+  int tma_ok[2] = {0, 0};
+  int tma_enabled = 1;
+  int *d_status = nullptr;
   void *probe_buf = nullptr;  // point-probe requests and results (osb_probe)
   int num_sms = 152;          // multiprocessors of the device (set at creation)
   int64_t graph_launches = 0;  // kernel launches recorded in one captured step
@@ -62,6 +68,9 @@ struct Ctx {
   double prof_ms[8] = {};
   int64_t prof_n[8] = {};
 };
+
+// encode the central kernel's tensor maps for state buffer `buf` (0: bound arrays, 1: partner)
+int encode_state_maps(Ctx &c, int buf);
 
 // plan checks and derived layout/constants (osb_api.cu)
 int plan_validate(const osb_plan_desc *p, char *why, size_t n);

@@ -78,7 +78,8 @@ EXPORTS = (
     "osb_set_state64_padded", "osb_set_coordinate",
     "osb_get_state64", "osb_step", "osb_residual", "osb_reduce", "osb_launch_count", "osb_profile", "osb_profile_read",
     "osb_set_weno_shape", "osb_get_weno_shape", "osb_set_central_shape", "osb_get_central_shape", "osb_autotune",
-    "osb_adjoint_residual", "osb_adjoint_step", "osb_probe", "osb_get_error", "osb_destroy",
+    "osb_adjoint_residual", "osb_adjoint_step", "osb_probe", "osb_set_tma", "osb_tma_active", "osb_get_error",
+    "osb_destroy",
     "osb_batch_create", "osb_batch_set_stream", "osb_batch_set_dt", "osb_batch_set_state64", "osb_batch_get_state64",
     "osb_batch_step", "osb_batch_autotune", "osb_batch_get_shape", "osb_batch_launch_count", "osb_batch_get_error",
     "osb_batch_destroy",
@@ -129,6 +130,8 @@ def load(build_if_missing=True):
     lib.osb_autotune.argtypes = [vp, ip, ctypes.POINTER(dp)]
     lib.osb_adjoint_residual.argtypes = [vp, vp, vp]
     lib.osb_probe.argtypes = [vp, ip, ctypes.POINTER(ip), ctypes.POINTER(dp)]
+    lib.osb_set_tma.argtypes = [vp, ip]
+    lib.osb_tma_active.argtypes = [vp]
     lib.osb_adjoint_step.argtypes = [vp, dp, vp, vp]
     lib.osb_get_error.argtypes = [vp, ctypes.c_char_p, ip]
     lib.osb_batch_create.argtypes = [ctypes.POINTER(PlanDesc), ip, ctypes.POINTER(vp)]
@@ -349,6 +352,13 @@ class Solver:
     def set_central_shape(self, ty):
         """Tile height (8 or 16) of the fused central/RK kernel."""
         self._check(self.lib.osb_set_central_shape(self.ctx, int(ty)))
+
+    def set_tma(self, enable=True):
+        """Select TMA plane loads (default) or register-staged loads in the fused central/RK kernel."""
+        self._check(self.lib.osb_set_tma(self.ctx, 1 if enable else 0))
+
+    def tma_active(self):
+        return bool(self.lib.osb_tma_active(self.ctx))
 
     def central_shape(self):
         ty = ctypes.c_int()
