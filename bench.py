@@ -236,9 +236,10 @@ def workload(name, n=None):
         return Workload(name, plan, dt, lambda s: s.init_tgv(), cfg, "tgv_central",
                         dict(block0np0=n, block0np1=n, block0np2=n, dt=dt, Minf=0.1),
                         {"mixed": 5 * (2 * 4 + 2 * 8), "fp64": 5 * (2 * 8 + 2 * 8)})
-    if name == "katzer512":
+    if name in ("katzer512", "katzer512_adaptive"):
+        adaptive = name.endswith("_adaptive")
         n0, n1 = (n or 512), 256
-        plan = katzer_plan(n0, n1, dt=0.04)
+        plan = katzer_plan(n0, n1, dt=0.04, adaptive=adaptive)
         d = np.load(os.path.join(REPO, "tests", "golden", "katzer_ic_n%d.npz" % n1))
         q = np.repeat(d["q_col"][:, :, None], n0 + 8, axis=2)
         x1 = np.repeat(d["x1_col"][:, None], n0 + 8, axis=1)
@@ -246,12 +247,15 @@ def workload(name, n=None):
         def init(s):
             s.set_coordinate(x1, 4)
             s.set_state64_padded(q, 4)
-        cfg = {"workload": "2D shock/boundary-layer interaction %dx%d (Katzer): TENO5 (C_T=1e-5, eps=1e-15), "
+        cut = ("C_T adapted per interface by the modified Ducros sensor (a1=10.5, a2=4.5)" if adaptive
+               else "C_T=1e-5")
+        cfg = {"workload": "2D shock/boundary-layer interaction %dx%d (Katzer): TENO5 (%s, eps=1e-15), "
                            "metrics stretched in x1 (sinh, factor 5), Sutherland viscosity, isothermal wall "
-                           "Tw=1.676, shock-generator top face, LS-RK3 SSP, Mach 2, Re=950, dt=0.04" % (n0, n1),
+                           "Tw=1.676, shock-generator top face, LS-RK3 SSP, Mach 2, Re=950, dt=0.04" % (n0, n1, cut),
                "grid": [n0, n1], "dt": 0.04, "precision": "mixed",
                "l2": "inputs smaller than L2 (%.0f MB state)" % (4 * n0 * n1 * 8 / 1e6)}
-        return Workload(name, plan, 0.04, init, cfg, "katzer_teno", dict(block0np0=n0, block0np1=n1, dt=0.04),
+        return Workload(name, plan, 0.04, init, cfg, "katzer_adaptive" if adaptive else "katzer_teno",
+                        dict(block0np0=n0, block0np1=n1, dt=0.04),
                         {"mixed": 4 * (2 * 4 + 2 * 8) + 4, "fp64": 4 * (2 * 8 + 2 * 8) + 8})
     raise SystemExit("unknown config %s" % name)
 
@@ -582,7 +586,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
     ap.add_argument("--config", default="tgv_weno256",
-                    choices=["tgv_weno256", "tgv_central64", "katzer512", "tgv_adjoint128", "tgv_batch96"])
+                    choices=["tgv_weno256", "tgv_central64", "katzer512", "katzer512_adaptive", "tgv_adjoint128",
+                             "tgv_batch96"])
     ap.add_argument("--precision", default=None, choices=["mixed", "fp64"], help="tgv_batch96: precision")
     ap.add_argument("--adj-steps", type=int, default=None, help="tgv_adjoint128: RK3 steps to T=2 (default 800)")
     ap.add_argument("--fd-dirs", type=int, default=16, help="tgv_adjoint128: finite-difference directions")

@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-#define OSB_ABI_VERSION 2
+#define OSB_ABI_VERSION 3
 
 /* error codes */
 #define OSB_OK 0
@@ -81,6 +81,13 @@ typedef struct osb_plan_desc {
   double Twall, SuthT, RefT;
   double dirichlet_state[2][4];
   double dirichlet_x_switch;
+  /* TENO5 with the cut-off adapted per interface by the modified Ducros sensor (2D blocks;
+   * schemes/spatial/teno.py:430-443, schemes/spatial/shock_sensors.py:12-49): at the interface whose
+   * left point is P, C_T = 10^-floor(teno_a1 - teno_a2 (1 - (1 - theta)^4 (1 + 4 theta))) with
+   * theta(P) = (1/2 - 1/2 tanh(2.5 + 250 div u)) (div u)^2 / (sensor_eps + (div u)^2 + |curl u|^2)
+   * on the interior (0 elsewhere).  teno_adaptive = 0 keeps the fixed teno_ct. */
+  int teno_adaptive;
+  double teno_a1, teno_a2, sensor_eps;
 } osb_plan_desc;
 
 /* Memory layout of every per-variable array: x fastest, interior point (i,j,k) at element
@@ -133,6 +140,12 @@ int osb_set_coordinate(osb_ctx *ctx, int axis, const double *dev_padded, int h);
  * master copy is the state itself; in mixed mode it is the FP64 RK accumulator. */
 int osb_set_state64(osb_ctx *ctx, int var, const double *dev_interior);
 int osb_get_state64(osb_ctx *ctx, int var, double *dev_interior);
+
+/* Plans with teno_adaptive: evaluate the TENO cut-off C_T of the current state (after applying the
+ * boundary conditions) into a device array of n0*n1 doubles laid out [x1][x0].  The reference
+ * stores the same field, TENO_B0, for output (StoreSome in apps/katzer_SBLI/katzer_SBLI.py);
+ * values are 10^-k with k an integer. */
+int osb_teno_cutoff(osb_ctx *ctx, double *dev_out);
 
 /* Advance nsteps RK3 steps of size dt (the generated time loop, algorithm.py:440-474).  Work is
  * stream-ordered; the call returns without synchronising.  On return the bound arrays hold the

@@ -7,6 +7,7 @@
 //   k2_bc_* (inlet, outlet, wall, top, in that order) on the FP64 master state
 //   k2_to_state (mixed only: FP64 master -> FP32 working state, halos included)
 //   k2_prims   constituent relations u0, u1, p, a, T, mu (Sutherland)
+//   k2_sensor_ct (adaptive TENO only): modified Ducros sensor theta and the cut-off C_T per point
 //   k2_flux<T, D, SCHEME> for D = x0, x1: interface fluxes + flux difference into R
 //   k2_visc_rk viscous/heat-flux terms + LS-RK3: du = A du + dt R, q += B du (FP64)
 // Metrics (once, k2_metric_*): detJ = dx1/dxi1 with the closures, D11 = 1/detJ, halos mirrored about
@@ -195,6 +196,54 @@ __global__ void k2_prims(Grid g, Q4T<const T> q, Prims<T> pr, double gama, doubl
 }
 
 // ---------------------------------------------------------------------------------------------
+// adaptive TENO cut-off (schemes/spatial/teno.py:430-443) from the modified Ducros sensor
+// (schemes/spatial/shock_sensors.py:12-49), one value per interface left point
+// ---------------------------------------------------------------------------------------------
+// 10^-k for k = 0..22, as decimal literals (the correctly rounded values pow(10, -k) returns)
+__constant__ double c_p10n[23] = {1e0,   1e-1,  1e-2,  1e-3,  1e-4,  1e-5,  1e-6,  1e-7,
+                                  1e-8,  1e-9,  1e-10, 1e-11, 1e-12, 1e-13, 1e-14, 1e-15,
+                                  1e-16, 1e-17, 1e-18, 1e-19, 1e-20, 1e-21, 1e-22};
+
+struct Sensor2Args {
+  double inv_d0, inv_d1, a1, a2, eps;
+};
+
+__device__ __forceinline__ float tanh_t(float x) { return tanhf(x); }
+__device__ __forceinline__ double tanh_t(double x) { return tanh(x); }
+
+// Over i in [-1, n0], j in [-1, n1] (every interface's left point along either axis).  On the
+// interior, with the derivatives' one-sided closures and the x1 metric (d/dx1 = D11 d/dxi1):
+//   theta = (1/2 - 1/2 tanh(2.5 + 250 div)) div^2 / (eps + div^2 + om^2),
+//   div = du0/dx0 + du1/dx1, om = du1/dx0 - du0/dx1;
+// theta = 0 on the other points (the sensor's range is the interior).  The cut-off is
+// C_T = 10^-floor(a1 - a2 (1 - (1 - theta)^4 (1 + 4 theta))), formed in FP64 in both precisions.
+template <typename T>
+__global__ void k2_sensor_ct(Grid g, Prims<const T> pr, const double *D11, T *ct, Sensor2Args sa) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x - 1, j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+  if (i > g.n0 || j > g.n1) return;
+  const int64_t n = g2(g, i, j);
+  double th = 0.0;
+  if (i >= 0 && i < g.n0 && j >= 0 && j < g.n1) {
+    const int64_t sy = g.sy;
+    auto U0x = [&](int o) { return pr.u0[n + o]; };
+    auto U1x = [&](int o) { return pr.u1[n + o]; };
+    auto U0y = [&](int o) { return pr.u0[n + o * sy]; };
+    auto U1y = [&](int o) { return pr.u1[n + o * sy]; };
+    const T id0 = T(sa.inv_d0), id1 = T(sa.inv_d1);
+    const T l0 = id0 * d1c<T>(U0x, i, g.n0), l1 = id0 * d1c<T>(U1x, i, g.n0);
+    const T l2 = id1 * d1c<T>(U0y, j, g.n1), l3 = id1 * d1c<T>(U1y, j, g.n1);
+    const T D = T(D11[n]);
+    const T div = l0 + l3 * D, om = l1 - l2 * D;
+    const T sw = T(0.5) - T(0.5) * tanh_t(T(250) * l0 + T(250) * l3 * D + T(2.5));
+    th = (double)(sw * (div * div) / (T(sa.eps) + div * div + om * om));
+  }
+  const double w = 1.0 - th;
+  const double k = floor(sa.a1 - sa.a2 * (1.0 - (w * w) * (w * w) * (4.0 * th + 1.0)));
+  const double c = (k >= 0.0 && k <= 22.0) ? c_p10n[(int)k] : pow(10.0, -k);
+  ct[n] = T(c);
+}
+
+// ---------------------------------------------------------------------------------------------
 // characteristic fluxes (4 conserved variables) with WENO5-JS or TENO5
 // ---------------------------------------------------------------------------------------------
 template <typename T> __device__ __forceinline__ T w5_side(T f0, T f1, T f2, T f3, T f4, T eps) {
@@ -340,10 +389,12 @@ template <> struct T2Tile<0> { static constexpr int TI = 64, TA = 4; };
 template <> struct T2Tile<1> { static constexpr int TI = 24, TA = 16; };  // static smem < 48 KB in FP64
 
 // Interface fluxes along D for a tile and the flux difference -(F_i - F_{i-1})/delta (times D11 for
-// x1), written (D = 0) or accumulated (D = 1) into R.
+// x1), written (D = 0) or accumulated (D = 1) into R.  TENO's cut-off is ct_d, or with ctp set the
+// per-point value at the interface's left point.
 template <typename T, int D, bool TENO>
 __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<const T> pr, const double *D11,
-                                               Q4T<T> res, double gama_d, double eps_d, double ct_d, double inv_dd) {
+                                               Q4T<T> res, double gama_d, double eps_d, double ct_d, double inv_dd,
+                                               const T *ctp) {
   using Tl = T2Tile<D>;
   constexpr int TI = Tl::TI, TA = Tl::TA, NPT = TI + 5;
   __shared__ T sf[S2_NF][NPT][TA];
@@ -391,8 +442,14 @@ __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<con
       W[k].a = sf[S2_A][m + k][a];
       W[k].ud = sf[S2_UD][m + k][a];
     }
+    T ctl = ct;
+    if (TENO && ctp) {
+      int i, j;
+      coord(d0 - 1 + m, a, i, j);
+      ctl = ctp[g2(g, i, j)];
+    }
     T fl[4];
-    flux2<T, D, TENO>(W, gama, eps, ct, fl);
+    flux2<T, D, TENO>(W, gama, eps, ctl, fl);
 #pragma unroll
     for (int v = 0; v < 4; ++v) sfl[v][m][a] = fl[v];
   }
@@ -551,17 +608,29 @@ template <typename T> void launch2_rhs(const Ctx &c, int update, double A, doubl
   Q4T<T> r = q4t<T>(c.res);
   const bool teno = p.conv == OSB_CONV_TENO5;
   const double eps = teno ? p.teno_eps : p.weno_eps;
+  const T *ctp = nullptr;
+  if (teno && p.teno_adaptive) {
+    Sensor2Args sa{1.0 / p.delta[0], 1.0 / p.delta[1], p.teno_a1, p.teno_a2, p.sensor_eps};
+    dim3 gs((c.g.n0 + 2 + 31) / 32, (c.g.n1 + 2 + 7) / 8);
+    k2_sensor_ct<T><<<gs, b, 0, s>>>(c.g, prc, c.d11, static_cast<T *>(c.ct2), sa);
+    ctp = static_cast<const T *>(c.ct2);
+    ++*launches;
+  }
   {
     using Tl = T2Tile<0>;
     dim3 gx((c.g.n0 + Tl::TI - 2) / (Tl::TI - 1), (c.g.n1 + Tl::TA - 1) / Tl::TA);
-    if (teno) k2_flux<T, 0, true><<<gx, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, 1.0 / p.delta[0]);
-    else k2_flux<T, 0, false><<<gx, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, 1.0 / p.delta[0]);
+    if (teno)
+      k2_flux<T, 0, true><<<gx, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, 1.0 / p.delta[0], ctp);
+    else
+      k2_flux<T, 0, false><<<gx, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, 1.0 / p.delta[0], ctp);
   }
   {
     using Tl = T2Tile<1>;
     dim3 gy((c.g.n0 + Tl::TA - 1) / Tl::TA, (c.g.n1 + Tl::TI - 2) / (Tl::TI - 1));
-    if (teno) k2_flux<T, 1, true><<<gy, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, 1.0 / p.delta[1]);
-    else k2_flux<T, 1, false><<<gy, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, 1.0 / p.delta[1]);
+    if (teno)
+      k2_flux<T, 1, true><<<gy, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, 1.0 / p.delta[1], ctp);
+    else
+      k2_flux<T, 1, false><<<gy, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, 1.0 / p.delta[1], ctp);
   }
   Visc2Args va;
   va.Re = p.Re;
@@ -575,6 +644,37 @@ template <typename T> void launch2_rhs(const Ctx &c, int update, double A, doubl
   k2_visc_rk<T><<<gv, b, 0, s>>>(c.g, prc, c.d11, c.sd111, q4t<const T>(c.res), q4(c.du2), q4(c.q64_2d), va, update);
   *launches += 4;
 }
+
+// The adaptive TENO cut-off of the current working state over the interior, as FP64 [n1][n0]
+// (the reference stores this field as TENO_B0 for output).
+template <typename T> __global__ void k2_pack_ct(Grid g, const T *ct, double *out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.n0 || j >= g.n1) return;
+  out[(int64_t)j * g.n0 + i] = (double)ct[g2(g, i, j)];
+}
+
+template <typename T> void launch2_cutoff(const Ctx &c, double *out, cudaStream_t s, int64_t *launches) {
+  const osb_plan_desc &p = c.plan;
+  Prims<T> pr;
+  pr.u0 = static_cast<T *>(c.prim2[0]);
+  pr.u1 = static_cast<T *>(c.prim2[1]);
+  pr.p = static_cast<T *>(c.prim2[2]);
+  pr.a = static_cast<T *>(c.prim2[3]);
+  pr.T_ = static_cast<T *>(c.prim2[4]);
+  pr.mu = static_cast<T *>(c.prim2[5]);
+  Prims<const T> prc{pr.u0, pr.u1, pr.p, pr.a, pr.T_, pr.mu};
+  dim3 b(32, 8), gp((c.g.n0 + 7 + 31) / 32, (c.g.n1 + 7 + 7) / 8);
+  k2_prims<T><<<gp, b, 0, s>>>(c.g, q4t<const T>(c.qa), pr, p.gama, p.Minf, p.SuthT / p.RefT);
+  Sensor2Args sa{1.0 / p.delta[0], 1.0 / p.delta[1], p.teno_a1, p.teno_a2, p.sensor_eps};
+  dim3 gs((c.g.n0 + 2 + 31) / 32, (c.g.n1 + 2 + 7) / 8);
+  k2_sensor_ct<T><<<gs, b, 0, s>>>(c.g, prc, c.d11, static_cast<T *>(c.ct2), sa);
+  dim3 gi((c.g.n0 + 31) / 32, (c.g.n1 + 7) / 8);
+  k2_pack_ct<T><<<gi, b, 0, s>>>(c.g, static_cast<const T *>(c.ct2), out);
+  *launches += 3;
+}
+
+template void launch2_cutoff<float>(const Ctx &, double *, cudaStream_t, int64_t *);
+template void launch2_cutoff<double>(const Ctx &, double *, cudaStream_t, int64_t *);
 
 template void launch2_rhs<float>(const Ctx &, int, double, double, double, cudaStream_t, int64_t *);
 template void launch2_rhs<double>(const Ctx &, int, double, double, double, cudaStream_t, int64_t *);

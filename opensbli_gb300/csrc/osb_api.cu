@@ -6,6 +6,7 @@
 // the reference's per-iteration "Save equations" copy (rk_sbli.py:126-133) is needed only before
 // the first step after the caller wrote the state itself.  One step (three stages) can be
 // captured as a CUDA graph and replayed.
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <new>
@@ -45,6 +46,13 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
       return OSB_EUNSUPPORTED;
     }
     if (p->conv != OSB_CONV_TENO5 && p->conv != OSB_CONV_WENO5JS) { snprintf(why, n, "2D blocks: TENO5 or WENO5-JS fluxes"); return OSB_EUNSUPPORTED; }
+    if (p->teno_adaptive) {
+      if (p->conv != OSB_CONV_TENO5) { snprintf(why, n, "teno_adaptive needs TENO5 fluxes"); return OSB_EINVAL; }
+      if (!(p->sensor_eps >= 0) || !std::isfinite(p->teno_a1) || !std::isfinite(p->teno_a2)) {
+        snprintf(why, n, "adaptive TENO: sensor_eps >= 0 and finite teno_a1, teno_a2");
+        return OSB_EINVAL;
+      }
+    }
     if (p->visc != OSB_VISC_SUTHERLAND) { snprintf(why, n, "2D blocks: Sutherland viscosity"); return OSB_EUNSUPPORTED; }
     if (p->rk != OSB_RK3_LS) { snprintf(why, n, "2D blocks: low-storage RK3"); return OSB_EUNSUPPORTED; }
     if (p->precision != OSB_PREC_FP64 && p->precision != OSB_PREC_MIXED) { snprintf(why, n, "precision %d", p->precision); return OSB_EINVAL; }
@@ -55,6 +63,7 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
     return OSB_OK;
   }
   if (p->ndim != 3) { snprintf(why, n, "ndim %d: this library implements 2D and 3D blocks", p->ndim); return OSB_EUNSUPPORTED; }
+  if (p->teno_adaptive) { snprintf(why, n, "adaptive TENO is implemented on 2D blocks"); return OSB_EUNSUPPORTED; }
   for (int d = 0; d < 3; ++d) {
     if (p->n[d] < 8 || p->n[d] > 4096) { snprintf(why, n, "n[%d] = %d out of range [8, 4096]", d, p->n[d]); return OSB_EINVAL; }
     if (!(p->delta[d] > 0)) { snprintf(why, n, "delta[%d] must be > 0", d); return OSB_EINVAL; }
@@ -646,6 +655,10 @@ int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
       e = cudaMalloc(&c->prim2[k], bytes);
       if (e == cudaSuccess) e = cudaMemset(c->prim2[k], 0, bytes);
     }
+    if (e == cudaSuccess && plan->teno_adaptive) {
+      e = cudaMalloc(&c->ct2, bytes);
+      if (e == cudaSuccess) e = cudaMemset(c->ct2, 0, bytes);
+    }
     if (e == cudaSuccess) e = cudaMalloc(&c->x1, b64);
     if (e == cudaSuccess) e = cudaMalloc(&c->d11, b64);
     if (e == cudaSuccess) e = cudaMalloc(&c->sd111, b64);
@@ -827,6 +840,20 @@ int osb_get_state64(osb_ctx *c, int var, double *dst) {
   const int nb = blocks_for((int64_t)c->g.n0 * c->g.n1 * c->g.n2);
   k_get64<<<nb, 256, 0, c->stream>>>(c->g, c->plan.ndim == 2 ? c->q64_2d[var] : c->qold[var], dst);
   return cuda_err(c, cudaGetLastError(), "osb_get_state64");
+}
+
+int osb_teno_cutoff(osb_ctx *c, double *dev_out) {
+  if (!c) return OSB_EINVAL;
+  if (!dev_out) return set_err(c, OSB_EINVAL, "null output");
+  if (c->plan.ndim != 2 || !c->plan.teno_adaptive) return set_err(c, OSB_EINVAL, "plan has no adaptive TENO");
+  if (int rc = check_bound(c)) return rc;
+  if (!c->metrics_valid) return set_err(c, OSB_EINVAL, "2D block: call osb_set_coordinate first");
+  if (!c->qold_valid) return set_err(c, OSB_EINVAL, "2D block: set the state first");
+  int64_t l = 0;
+  launch2_bcs(*c, c->stream, &l);
+  if (c->mixed) launch2_cutoff<float>(*c, dev_out, c->stream, &l);
+  else launch2_cutoff<double>(*c, dev_out, c->stream, &l);
+  return cuda_err(c, cudaGetLastError(), "osb_teno_cutoff");
 }
 
 int osb_step(osb_ctx *c, int nsteps, double dt) {
@@ -1130,6 +1157,7 @@ void osb_destroy(osb_ctx *c) {
     cudaFree(c->du2[v]);
   }
   for (int k = 0; k < 6; ++k) cudaFree(c->prim2[k]);
+  cudaFree(c->ct2);
   cudaFree(c->x1);
   cudaFree(c->d11);
   cudaFree(c->sd111);

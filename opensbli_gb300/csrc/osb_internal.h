@@ -55,6 +55,7 @@ struct Ctx {
   double *q64_2d[4] = {};         // FP64 master state, padded (the bound arrays in FP64 mode)
   double *du2[4] = {};            // LS-RK register
   void *prim2[6] = {};            // u0, u1, p, a, T, mu (state precision, padded)
+  void *ct2 = nullptr;            // adaptive TENO: cut-off C_T per point (state precision, padded)
   double *x1 = nullptr, *d11 = nullptr, *sd111 = nullptr;
   int metrics_valid = 0;
   std::string err;
@@ -95,6 +96,7 @@ void launch_central_rk(const Ctx &c, Fields5<const T> q, Fields5<T> qnew, Fields
 
 void launch2_metrics(const Ctx &c, const double *x1, cudaStream_t s, int64_t *launches);
 void launch2_bcs(const Ctx &c, cudaStream_t s, int64_t *launches);
+template <typename T> void launch2_cutoff(const Ctx &c, double *out, cudaStream_t s, int64_t *launches);
 template <typename T>
 void launch2_rhs(const Ctx &c, int update, double A, double B, double dt, cudaStream_t s, int64_t *launches);
 

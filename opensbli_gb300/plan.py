@@ -52,6 +52,12 @@ class Plan:
     weno_eps: float = 1e-6
     teno_ct: float = 1e-5
     teno_eps: float = 1e-15
+    # adaptive TENO cut-off from the modified Ducros sensor (teno.py:430-443, shock_sensors.py:12-49):
+    # C_T = 10^-floor(a1 - a2 g(theta)) per interface; sensor_eps regularises theta's denominator
+    teno_adaptive: bool = False
+    teno_a1: float = 10.5
+    teno_a2: float = 4.5
+    sensor_eps: float = 1e-12
     rk_a: Tuple[float, float, float] = RK3_RKOLD
     rk_b: Tuple[float, float, float] = RK3_RKNEW
     use_graphs: bool = True
@@ -119,14 +125,17 @@ def tgv_cfl_dt(plan, cfl=0.5):
     return cfl * min(plan.delta) / float(s.max())
 
 
-def katzer_plan(n0=512, n1=256, precision="fp64", conv="teno5", dt=0.04, use_graphs=True):
+def katzer_plan(n0=512, n1=256, precision="fp64", conv="teno5", dt=0.04, use_graphs=True, adaptive=False):
     """2D laminar shock-wave/boundary-layer interaction (apps/katzer_SBLI/katzer_SBLI.py constants):
     Mach 2, Re = 950, Pr = 0.72, Twall = 1.67619431, Sutherland 110.4/288, TENO5 with C_T = 1e-5 and
-    eps = 1e-15, domain [0, 400] x [0, 115] with x1 = 115 sinh(5 eta)/sinh(5), LS-RK3 (SSP)."""
+    eps = 1e-15, domain [0, 400] x [0, 115] with x1 = 115 sinh(5 eta)/sinh(5), LS-RK3 (SSP).
+    adaptive=True gives the script as published: the TENO cut-off adapted per interface by the
+    modified Ducros sensor (a1 = 10.5, a2 = 4.5, sensor epsilon 1e-12)."""
     A, B = ls_rk3_ssp_coefficients()
     return Plan(ndim=2, n=(n0, n1, 1), delta=(400.0 / (n0 - 1), 115.0 / (n1 - 1), 1.0), conv=conv, visc="sutherland",
                 rk="ls_rk3", precision=precision,
                 bc=(("inlet_pressure_extrapolate", "extrapolation"), ("isothermal_wall", "dirichlet"),
                     ("periodic", "periodic")),
                 gama=1.4, Minf=2.0, Re=950.0, Pr=0.72, teno_ct=1e-5, teno_eps=1e-15, rk_a=A, rk_b=B, dt=dt,
-                use_graphs=use_graphs, ic="host", name="katzer_%s_%dx%d" % (conv, n0, n1))
+                use_graphs=use_graphs, ic="host", teno_adaptive=adaptive,
+                name="katzer_%s%s_%dx%d" % (conv, "_adaptive" if adaptive else "", n0, n1))

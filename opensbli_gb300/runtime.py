@@ -12,7 +12,7 @@ import torch
 
 from . import build as _build
 
-OSB_ABI_VERSION = 2
+OSB_ABI_VERSION = 3
 ERRORS = {
     -1: "invalid plan or argument",
     -2: "unsupported kernel pattern",
@@ -58,6 +58,10 @@ class PlanDesc(ctypes.Structure):
         ("RefT", ctypes.c_double),
         ("dirichlet_state", (ctypes.c_double * 4) * 2),
         ("dirichlet_x_switch", ctypes.c_double),
+        ("teno_adaptive", ctypes.c_int),
+        ("teno_a1", ctypes.c_double),
+        ("teno_a2", ctypes.c_double),
+        ("sensor_eps", ctypes.c_double),
     ]
 
 
@@ -76,7 +80,7 @@ class Layout(ctypes.Structure):
 EXPORTS = (
     "osb_query_layout", "osb_create", "osb_bind_field", "osb_set_stream", "osb_init_tgv", "osb_set_state64",
     "osb_set_state64_padded", "osb_set_coordinate",
-    "osb_get_state64", "osb_step", "osb_residual", "osb_reduce", "osb_launch_count", "osb_profile", "osb_profile_read",
+    "osb_get_state64", "osb_teno_cutoff", "osb_step", "osb_residual", "osb_reduce", "osb_launch_count", "osb_profile", "osb_profile_read",
     "osb_set_weno_shape", "osb_get_weno_shape", "osb_set_central_shape", "osb_get_central_shape", "osb_autotune",
     "osb_adjoint_residual", "osb_adjoint_step", "osb_probe", "osb_set_tma", "osb_tma_active", "osb_get_error",
     "osb_destroy",
@@ -116,6 +120,7 @@ def load(build_if_missing=True):
     lib.osb_set_state64_padded.argtypes = [vp, ip, vp, ip]
     lib.osb_set_coordinate.argtypes = [vp, ip, vp, ip]
     lib.osb_get_state64.argtypes = [vp, ip, vp]
+    lib.osb_teno_cutoff.argtypes = [vp, vp]
     lib.osb_step.argtypes = [vp, ip, dp]
     lib.osb_residual.argtypes = [vp, vp]
     lib.osb_reduce.argtypes = [vp, ip, ctypes.POINTER(dp)]
@@ -187,6 +192,8 @@ def make_plan_desc(plan):
         d.dirichlet_state[0][v] = plan.dirichlet_lo[v]
         d.dirichlet_state[1][v] = plan.dirichlet_hi[v]
     d.dirichlet_x_switch = plan.dirichlet_x_switch
+    d.teno_adaptive = 1 if plan.teno_adaptive else 0
+    d.teno_a1, d.teno_a2, d.sensor_eps = plan.teno_a1, plan.teno_a2, plan.sensor_eps
     return d
 
 
@@ -292,6 +299,16 @@ class Solver:
             out = torch.empty((self.layout.nvar,) + self.shape, dtype=torch.float64, device=self.device)
         for v in range(self.layout.nvar):
             self._check(self.lib.osb_get_state64(self.ctx, v, ctypes.c_void_p(out[v].data_ptr())))
+        self._out()
+        return out
+
+    def teno_cutoff(self):
+        """The adaptive TENO cut-off C_T of the current state, FP64 [n1][n0] (2D plans with
+        teno_adaptive; the reference's TENO_B0 output field)."""
+        self._in()
+        with torch.cuda.stream(self.stream):
+            out = torch.empty(self.shape, dtype=torch.float64, device=self.device)
+        self._check(self.lib.osb_teno_cutoff(self.ctx, ctypes.c_void_p(out.data_ptr())))
         self._out()
         return out
 

@@ -196,8 +196,7 @@ class GB300Writer:
             lhs = self._lhs_names(k)
             if not {"delta_0", "delta_1", "delta_2", "inv_omega_sum"} <= lhs:
                 raise NotImplementedError("TENO5 with a cut-off expected in %s" % k.computation_name)
-            if any("TENO" in str(e.rhs) and "TENO_CT" not in str(e.rhs) for e in k.equations):
-                raise NotImplementedError("adaptive TENO (shock sensor) is not lowered; use a fixed C_T")
+        adaptive = self._adaptive_teno(teno) if teno else None
         if self._max_offset(teno or weno) != 3:
             raise NotImplementedError("5th-order reconstruction stencil expected")
         if not self._kernels("MetricsEquation") or not self._kernels("Metric boundary"):
@@ -242,7 +241,110 @@ class GB300Writer:
                     bc=(tuple(bcs[0]), tuple(bcs[1]), ("periodic", "periodic")),
                     rk_a=coeff["rkA"], rk_b=coeff["rkB"], use_graphs=use_graphs, ic="host",
                     dirichlet_lo=tuple(lo[v] for v in order), dirichlet_hi=tuple(hi[v] for v in order),
-                    dirichlet_x_switch=xs if xs is not None else 1e300, kernels=[n for n in names if n])
+                    dirichlet_x_switch=xs if xs is not None else 1e300, kernels=[n for n in names if n],
+                    teno_adaptive=adaptive is not None,
+                    sensor_eps=adaptive if adaptive is not None else Plan.sensor_eps)
+
+    def _adaptive_teno(self, teno):
+        """Recognise the adaptive TENO cut-off (LLFTeno(formulation='adaptive'), schemes/spatial/
+        teno.py:430-443) and the modified Ducros sensor it reads (schemes/spatial/shock_sensors.py:
+        12-49, added to the constituent relations).  Returns None for a fixed C_T, else the sensor's
+        epsilon (the value the generator gives the constant; a value substituted for it as a
+        simulation parameter does not reach the generated code, whose line is not `epsilon=Input;`).
+        Both formulas are checked numerically against the forms the GPU kernel implements."""
+        import math
+        import random
+        import sympy
+        ct = [e for k in teno for e in k.equations if str(e.lhs) == "TENO_CT"]
+        if not ct:
+            if any("TENO" in str(e.rhs) and "TENO_CT" not in str(e.rhs) for k in teno for e in k.equations):
+                raise NotImplementedError("TENO cut-off form not recognised")
+            return None
+        sensor = None
+        for e in ct:
+            ds = [a for a in sympy.preorder_traversal(e.rhs) if type(a).__name__ == "DataSet"]
+            names = {str(a.base) for a in ds}
+            if len(names) != 1 or any(int(i) != 0 for a in ds for i in a.indices):
+                raise NotImplementedError("adaptive TENO: C_T must read one sensor array at the interface's left point")
+            name = names.pop()
+            if sensor not in (None, name):
+                raise NotImplementedError("adaptive TENO: one sensor array for both directions expected")
+            sensor = name
+            th, a1, a2 = sympy.symbols("_osb_th _osb_a1 _osb_a2")
+            reps = {a: th for a in ds}
+            for a in sympy.preorder_traversal(e.rhs):
+                if str(a) == "teno_a1":
+                    reps[a] = a1
+                elif str(a) == "teno_a2":
+                    reps[a] = a2
+            f = e.rhs.xreplace(reps)
+            if f.free_symbols - {th, a1, a2}:
+                raise NotImplementedError("adaptive TENO: unexpected symbols in C_T: %s" % (f.free_symbols - {th, a1, a2}))
+            for t in (0.0, 0.013, 0.31, 0.5, 0.77, 0.999, 1.0):
+                want = 10.0 ** (-math.floor(10.5 - 4.5 * (1 - (1 - t) ** 4 * (4 * t + 1))))
+                got = float(f.subs({th: t, a1: 10.5, a2: 4.5}))
+                if abs(got - want) > 1e-12 * want:
+                    raise NotImplementedError("adaptive TENO: C_T formula not recognised")
+        # the sensor equation, with its derivative locals (GridVariables) classified by the variable
+        # and direction of their interior (default-branch) central stencil
+        locs, theta_eq = {}, None
+        for k in self.components:
+            if type(k).__name__ != "Kernel":
+                continue
+            for e in k.equations:
+                if str(e.lhs) == sensor or str(getattr(e.lhs, "base", "")) == sensor:
+                    if theta_eq is not None:
+                        raise NotImplementedError("adaptive TENO: sensor written more than once")
+                    theta_eq, kern = e, k
+        if theta_eq is None:
+            raise NotImplementedError("adaptive TENO: no kernel evaluates the sensor %s" % sensor)
+        for e in kern.equations:
+            if type(e.lhs).__name__ != "GridVariable" or not isinstance(e.rhs, sympy.Piecewise):
+                continue
+            body = e.rhs.args[-1][0]
+            ds = [a for a in sympy.preorder_traversal(body) if type(a).__name__ == "DataSet"]
+            var = {str(a.base) for a in ds}
+            dirs = {d for a in ds for d, i in enumerate(a.indices) if int(i) != 0}
+            offs = sorted({int(i) for a in ds for i in a.indices if int(i) != 0})
+            if len(var) != 1 or len(dirs) != 1 or offs != [-2, -1, 1, 2]:
+                raise NotImplementedError("adaptive TENO: sensor derivative %s not recognised" % e.lhs)
+            locs[e.lhs] = (var.pop(), dirs.pop())
+        sym = {}
+        for v in ("u0_B0", "u1_B0"):
+            for d in (0, 1):
+                sym[(v, d)] = sympy.Symbol("_osb_d_%s_%d" % (v, d))
+        D = sympy.Symbol("_osb_D11")
+        reps, eps = {}, None
+        for a in sympy.preorder_traversal(theta_eq.rhs):
+            t = type(a).__name__
+            if t == "GridVariable":
+                if a not in locs:
+                    raise NotImplementedError("adaptive TENO: sensor local %s not recognised" % a)
+                reps[a] = sym[locs[a]]
+            elif t == "DataSet" and str(a.base) == "D11_B0" and all(int(i) == 0 for i in a.indices):
+                reps[a] = D
+            elif t == "ConstantObject" and str(a) == "epsilon":
+                eps = float(a.value)
+                reps[a] = sympy.Float(eps)
+        g = theta_eq.rhs.xreplace(reps)
+        # the derivatives carry inv_0/inv_1 = 1/Delta; take Delta = 1 for the check
+        g = g.subs({s_: 1 for s_ in g.free_symbols if str(s_) in ("inv_0", "inv_1")})
+        if eps is None or g.free_symbols - set(sym.values()) - {D}:
+            raise NotImplementedError("adaptive TENO: sensor formula not recognised")
+        # derivative locals are (f(+1)*8 - f(-1)*8 + f(-2) - f(+2))/12 etc.: the symbols stand for
+        # the stencil values, so compare against the reference form on random derivative values
+        rnd = random.Random(7)
+        for _ in range(8):
+            vals = {k_: rnd.uniform(-0.02, 0.02) for k_ in sym}
+            Dv = rnd.uniform(0.5, 2.0)
+            a_, b_ = vals[("u0_B0", 0)], vals[("u1_B0", 0)]
+            c_, d_ = vals[("u0_B0", 1)], vals[("u1_B0", 1)]
+            div, om = a_ + d_ * Dv, b_ - c_ * Dv
+            want = (0.5 - 0.5 * math.tanh(2.5 + 250.0 * div)) * div * div / (eps + div * div + om * om)
+            got = float(g.subs({**{sym[k_]: vals[k_] for k_ in sym}, D: Dv}))
+            if abs(got - want) > 1e-12 * max(abs(want), 1e-300):
+                raise NotImplementedError("adaptive TENO: sensor formula not recognised")
+        return eps
 
     # ------------------------------------------------------------------ constants
     def substitute_simulation_parameters(self, constants, values):
@@ -263,7 +365,8 @@ class GB300Writer:
             kw.update(Twall=float(env.get("Twall", p.Twall)), SuthT=float(env.get("SuthT", p.SuthT)),
                       RefT=float(env.get("RefT", p.RefT)), teno_eps=float(env.get("eps", p.teno_eps)),
                       teno_ct=float(env.get("TENO_CT", p.teno_ct)), Lx1=float(env.get("Lx1", p.Lx1)),
-                      by=float(env.get("by", p.by)))
+                      by=float(env.get("by", p.by)), teno_a1=float(env.get("teno_a1", p.teno_a1)),
+                      teno_a2=float(env.get("teno_a2", p.teno_a2)))
         self.plan = p.replace(**kw)
         return self.plan
 

@@ -57,7 +57,7 @@ def lib():
     global _lib
     if _lib is None:
         _lib = ctypes.CDLL(build())
-        for name in ("osbo_tgv_init", "osbo_run", "osbo_residual", "osbo2d_run", "osbo2d_metrics"):
+        for name in ("osbo_tgv_init", "osbo_run", "osbo_residual", "osbo2d_run", "osbo2d_metrics", "osbo2d_cutoff"):
             getattr(_lib, name).restype = ctypes.c_int
     return _lib
 
@@ -128,6 +128,10 @@ class Cfg2D(ctypes.Structure):
         ("rkA", ctypes.c_double * 3),
         ("rkB", ctypes.c_double * 3),
         ("dt", ctypes.c_double),
+        ("teno_adaptive", ctypes.c_int),
+        ("teno_a1", ctypes.c_double),
+        ("teno_a2", ctypes.c_double),
+        ("sensor_eps", ctypes.c_double),
     ]
 
 
@@ -145,6 +149,10 @@ def make_cfg2d(plan):
         c.rkA[s] = plan.rk_a[s]
         c.rkB[s] = plan.rk_b[s]
     c.dt = plan.dt
+    c.teno_adaptive = 1 if getattr(plan, "teno_adaptive", False) else 0
+    c.teno_a1 = getattr(plan, "teno_a1", 10.5)
+    c.teno_a2 = getattr(plan, "teno_a2", 4.5)
+    c.sensor_eps = getattr(plan, "sensor_eps", 1e-30)
     return c
 
 
@@ -155,6 +163,16 @@ def run2d(plan, q0_padded, nsteps):
     assert q.shape == (4, plan.n[1] + 8, plan.n[0] + 8)
     assert lib().osbo2d_run(ctypes.byref(c), _ptr(q), int(nsteps)) == 0
     return q
+
+
+def cutoff2d(plan, q0_padded):
+    """The adaptive TENO cut-off [n1][n0] of a padded FP64 state (boundary conditions applied)."""
+    c = make_cfg2d(plan)
+    q = np.ascontiguousarray(q0_padded, dtype=np.float64)
+    assert q.shape == (4, plan.n[1] + 8, plan.n[0] + 8)
+    ct = np.zeros((plan.n[1], plan.n[0]))
+    assert lib().osbo2d_cutoff(ctypes.byref(c), _ptr(q), _ptr(ct)) == 0
+    return ct
 
 
 def metrics2d(plan):

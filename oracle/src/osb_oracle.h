@@ -51,6 +51,10 @@ typedef struct {
   double Lx1, by;    /* x1 = Lx1 sinh(by delta1 j / Lx1) / sinh(by) */
   double rkA[3], rkB[3];
   double dt;
+  /* adaptive TENO (teno.py:430-443) driven by the modified Ducros sensor (shock_sensors.py:12-49):
+   * C_T = 10^-floor(a1 - a2 (1 - (1-theta)^4 (1+4 theta))) per interface; 0 selects the fixed teno_ct */
+  int teno_adaptive;
+  double teno_a1, teno_a2, sensor_eps;
 } osbo2d_cfg;
 
 /* Advance q by nsteps LS-RK3 steps.  q holds [4][n1+8][n0+8]: rho, rhou0, rhou1, rhoE with a
@@ -58,6 +62,7 @@ typedef struct {
  * initialisation kernel does); it is overwritten with the final state, halos included. */
 int osbo2d_run(const osbo2d_cfg *cfg, double *q, int nsteps);
 /* Metric terms D11 and SD111 on the interior, [n1][n0]. */
+int osbo2d_cutoff(const osbo2d_cfg *cfg, const double *q, double *ct);
 int osbo2d_metrics(const osbo2d_cfg *cfg, double *D11, double *SD111);
 
 #ifdef __cplusplus

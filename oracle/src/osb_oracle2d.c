@@ -25,7 +25,7 @@ typedef struct {
   int px, py;
   size_t np;
   double *q[4], *du[4], *res[4];
-  double *u0, *u1, *p, *a, *T, *mu;
+  double *u0, *u1, *p, *a, *T, *mu, *theta;
   double *x1, *D11, *SD111, *flux[4];
 } s2_t;
 
@@ -49,12 +49,13 @@ static void s2_init(s2_t *s, const osbo2d_cfg *cfg) {
     s->flux[v] = alloc2(s);
   }
   s->u0 = alloc2(s); s->u1 = alloc2(s); s->p = alloc2(s); s->a = alloc2(s); s->T = alloc2(s); s->mu = alloc2(s);
+  s->theta = alloc2(s); /* written on the interior only; the rest stays 0, as the generated code leaves it */
   s->x1 = alloc2(s); s->D11 = alloc2(s); s->SD111 = alloc2(s);
 }
 
 static void s2_free(s2_t *s) {
   for (int v = 0; v < 4; ++v) { free(s->q[v]); free(s->du[v]); free(s->res[v]); free(s->flux[v]); }
-  free(s->u0); free(s->u1); free(s->p); free(s->a); free(s->T); free(s->mu);
+  free(s->u0); free(s->u1); free(s->p); free(s->a); free(s->T); free(s->mu); free(s->theta);
   free(s->x1); free(s->D11); free(s->SD111);
 }
 
@@ -223,14 +224,37 @@ static void constituent(s2_t *s) {
   }
 }
 
+/* Modified Ducros sensor (shock_sensors.py:12-49, metric-transformed: d/dx0 = d/dxi0, d/dx1 =
+ * D11 d/dxi1), evaluated on the interior with the one-sided closures of the derivatives:
+ *   theta = (1/2 - 1/2 tanh(2.5 (1 + 100 div))) div^2 / (eps + div^2 + omega^2),
+ *   div = du0/dx0 + du1/dx1, omega = du1/dx0 - du0/dx1. */
+static void sensor(s2_t *s) {
+  FOR2(0, N0, 0, N1) {
+    const size_t n = I2(s, i, j);
+    const double l0 = d1c(s, s->u0, i, j, 0), l1 = d1c(s, s->u1, i, j, 0);
+    const double l2 = d1c(s, s->u0, i, j, 1), l3 = d1c(s, s->u1, i, j, 1);
+    const double D = s->D11[n];
+    const double div = l0 + l3 * D, om = l1 - l2 * D;
+    s->theta[n] = (0.5 - 0.5 * tanh(250.0 * l0 + 250.0 * l3 * D + 2.5)) * (div * div) /
+                  (s->c.sensor_eps + div * div + om * om);
+  }
+}
+
+/* TENO cut-off at the interface whose left point is n: fixed, or from the sensor there */
+static double teno_cutoff(const s2_t *s, size_t n) {
+  if (!s->c.teno_adaptive) return s->c.teno_ct;
+  const double th = s->theta[n];
+  return pow(10.0, -floor(s->c.teno_a1 - s->c.teno_a2 * (-pow(1 - th, 4) * (4 * th + 1) + 1)));
+}
+
 /* ---------------------------------------------------------------------------------------------
  * TENO5 with fixed cut-off (schemes/spatial/teno.py:57-213, 407-465): smoothness indicators of the
  * half-split fluxes, alpha_r = (1 + |b0 - b2|/(eps + b_r))^6, delta_r = 0 if alpha_r/sum < C_T,
  * omega_r = d_r delta_r / sum(d delta), d = (11/20, 2/5, 1/20) for the central, downwind and
  * upwind candidates.  f = CF +- lambda CS at points i-2..i+2 (right-going side).
  * ------------------------------------------------------------------------------------------- */
-static double teno5_plus(const s2_t *s, const double f[5]) {
-  const double eps = s->c.teno_eps, CT = s->c.teno_ct;
+static double teno5_plus(const s2_t *s, const double f[5], double CT) {
+  const double eps = s->c.teno_eps;
   const double h0 = 0.5 * f[0], h1 = 0.5 * f[1], h2 = 0.5 * f[2], h3 = 0.5 * f[3], h4 = 0.5 * f[4];
   const double b0 = 0.25 * (h1 - h3) * (h1 - h3) + (13.0 / 12.0) * (h1 - 2 * h2 + h3) * (h1 - 2 * h2 + h3);
   const double b1 = (13.0 / 12.0) * (h2 - 2 * h3 + h4) * (h2 - 2 * h3 + h4) + 0.25 * (3 * h2 - 4 * h3 + h4) * (3 * h2 - 4 * h3 + h4);
@@ -301,13 +325,14 @@ static void teno_fluxes(s2_t *s, int dir) {
       for (int r = 0; r < 4; ++r) lam[r] = fmax(lam[r], ev[r]);
     }
     double rec[4];
+    const double CT = teno_cutoff(s, c);
     for (int r = 0; r < 4; ++r) {
       double fp[5], fm[5];
       for (int t = 0; t < 5; ++t) {
         fp[t] = CF[r][t] + lam[r] * CS[r][t];
         fm[t] = CF[r][5 - t] - lam[r] * CS[r][5 - t];
       }
-      rec[r] = teno5_plus(s, fp) + teno5_plus(s, fm);
+      rec[r] = teno5_plus(s, fp, CT) + teno5_plus(s, fm, CT);
     }
     /* REV columns (euler_eigensystem.py:90-92) */
     const double hh = (phi + a * a) / (g - 1);
@@ -410,6 +435,7 @@ int osbo2d_run(const osbo2d_cfg *cfg, double *q, int nsteps) {
     apply_bcs(&s);
     for (int st = 0; st < 3; ++st) {
       constituent(&s);
+      if (cfg->teno_adaptive) sensor(&s);
       residual_teno(&s);
       residual_viscous(&s);
       /* RungeKuttaLS (rk_LS.py:155-166): du = A du + dt R; q = q + B du */
@@ -427,6 +453,26 @@ int osbo2d_run(const osbo2d_cfg *cfg, double *q, int nsteps) {
     for (int j = -hp; j < cfg->n[1] + hp; ++j)
       for (int i = -hp; i < cfg->n[0] + hp; ++i)
         q[((size_t)v * pyo + (size_t)(j + hp)) * pxo + (size_t)(i + hp)] = s.q[v][I2(&s, i, j)];
+  s2_free(&s);
+  return 0;
+}
+
+/* The adaptive TENO cut-off of a padded state (the boundary conditions applied first) over the
+ * interior, [n1][n0]: the field the reference stores as TENO_B0. */
+int osbo2d_cutoff(const osbo2d_cfg *cfg, const double *q, double *ct) {
+  s2_t s;
+  s2_init(&s, cfg);
+  const int hp = 4, pxo = cfg->n[0] + 2 * hp, pyo = cfg->n[1] + 2 * hp;
+  for (int v = 0; v < 4; ++v)
+    for (int j = -hp; j < cfg->n[1] + hp; ++j)
+      for (int i = -hp; i < cfg->n[0] + hp; ++i)
+        s.q[v][I2(&s, i, j)] = q[((size_t)v * pyo + (size_t)(j + hp)) * pxo + (size_t)(i + hp)];
+  metrics(&s);
+  apply_bcs(&s);
+  constituent(&s);
+  sensor(&s);
+  for (int j = 0; j < cfg->n[1]; ++j)
+    for (int i = 0; i < cfg->n[0]; ++i) ct[(size_t)j * cfg->n[0] + i] = teno_cutoff(&s, I2(&s, i, j));
   s2_free(&s);
   return 0;
 }

@@ -41,6 +41,8 @@ CASES = {
 # the x1 coordinate the metrics are computed from.
 CASES_2D = {
     "katzer_teno": ((64, 32), 20, {"dt": 0.01}),
+    # the published script: TENO cut-off adapted by the modified Ducros sensor
+    "katzer_adaptive": ((64, 32), 20, {"dt": 0.01}),
 }
 VARS_2D = ["rho", "rhou0", "rhou1", "rhoE"]
 
@@ -51,9 +53,11 @@ def padded4(d, names):
             for v in names}
 
 
-def main2d(ref):
+def main2d(ref, only=None):
     import tempfile
     for case, ((n0, n1), steps, extra) in CASES_2D.items():
+        if only is not None and case != only:
+            continue
         if not refrun.available(case):
             subprocess.check_call([sys.executable, os.path.join(REPO, "oracle", "gen", "generate.py"), "--case", case,
                                    "--ref", ref])
@@ -79,10 +83,13 @@ def main2d(ref):
 
 
 def main(ref="/root/reference", only=None):
-    """Regenerate every fixture, or only the 3D case `only`."""
+    """Regenerate every fixture, or only the case `only`."""
     if only is None:
         main2d(ref)
         katzer_profile(ref)
+    elif only in CASES_2D:
+        main2d(ref, only)
+        return
     for case, (n, steps, extra) in CASES.items():
         if only is not None and case != only:
             continue

@@ -72,3 +72,86 @@ def test_gpu_2d_reductions():
     with pytest.raises(NotImplementedError):
         s.reduce("enstrophy")
     s.close()
+
+
+# ---- the published Katzer script: TENO cut-off adapted per interface by the Ducros sensor ----
+
+def test_gpu_2d_adaptive_fp64_matches_reference_golden():
+    q0, x1, q_ref, n, steps, params = load_golden_2d("katzer_adaptive")
+    plan = golden_plan_2d("katzer_adaptive", n=n).replace(dt=params["dt"])
+    assert plan.teno_adaptive
+    q = run_gpu_2d(plan, q0, x1, steps, params["dt"])
+    ref = q_ref[:, 4:-4, 4:-4]
+    err = [float(np.abs(q[v] - ref[v]).max() / np.abs(ref[v]).max()) for v in range(4)]
+    assert max(err) <= 1e-12, err
+
+
+def perturbed_state(n0, amp=0.03, seed=3):
+    """The Katzer initial state widened to n0 columns with seeded noise on both momenta: the sensor
+    then takes all five cut-off levels 1e-10 .. 1e-6 somewhere (the laminar state alone keeps
+    C_T = 1e-10 almost everywhere)."""
+    q0, x1, _, n, _, _ = load_golden_2d("katzer_adaptive")
+    q, x1w = widen_2d(q0, n0), widen_2d(x1[None], n0)[0]
+    rng = np.random.default_rng(seed)
+    q[1] *= 1 + amp * rng.standard_normal(q[1].shape)
+    q[2] += amp * rng.standard_normal(q[2].shape)
+    return q, x1w, n
+
+
+@pytest.mark.parametrize("n0,steps,perturb", [(130, 20, False), (96, 10, True)])
+def test_gpu_2d_adaptive_fp64_matches_oracle(n0, steps, perturb):
+    dt = 0.01
+    if perturb:
+        q0w, x1w, n = perturbed_state(n0)
+    else:
+        q0, x1, _, n, _, _ = load_golden_2d("katzer_adaptive")
+        q0w, x1w = widen_2d(q0, n0), widen_2d(x1[None], n0)[0]
+    plan = golden_plan_2d("katzer_adaptive", n=(n0, n[1])).replace(dt=dt)
+    q_or = O.run2d(plan, q0w, steps)
+    q = run_gpu_2d(plan, q0w, x1w, steps, dt)
+    ref = q_or[:, 4:-4, 4:-4]
+    err = [float(np.abs(q[v] - ref[v]).max() / np.abs(ref[v]).max()) for v in range(4)]
+    assert max(err) <= 1e-11, err
+
+
+def test_gpu_2d_adaptive_cutoff_field_matches_oracle():
+    """The per-point cut-off (the reference's TENO_B0 field), bit for bit, on a state where the
+    sensor takes every level."""
+    q, x1w, n = perturbed_state(96)
+    plan = golden_plan_2d("katzer_adaptive", n=(96, n[1])).replace(dt=0.01)
+    ct_or = O.cutoff2d(plan, q)
+    s = Solver(plan)
+    s.set_coordinate(x1w, 4)
+    s.set_state64_padded(q, 4)
+    ct = s.teno_cutoff().cpu().numpy()
+    s.close()
+    assert len(np.unique(ct_or)) == 5
+    assert np.array_equal(ct, ct_or), int((ct != ct_or).sum())
+
+
+def test_gpu_2d_adaptive_mixed_close_to_fp64():
+    q0, x1, q_ref, n, steps, params = load_golden_2d("katzer_adaptive")
+    plan = golden_plan_2d("katzer_adaptive", n=n).replace(dt=params["dt"])
+    qm = run_gpu_2d(plan.replace(precision="mixed"), q0, x1, steps, params["dt"])
+    ref = q_ref[:, 4:-4, 4:-4]
+    l2 = [float(np.linalg.norm(qm[v] - ref[v]) / np.linalg.norm(ref[v])) for v in range(4)]
+    assert max(l2) < 1e-5, l2
+
+
+def test_gpu_2d_adaptive_graph_and_eager_identical():
+    q0, x1, _, n, _, params = load_golden_2d("katzer_adaptive")
+    plan = golden_plan_2d("katzer_adaptive", n=n).replace(dt=params["dt"])
+    a = run_gpu_2d(plan.replace(use_graphs=True), q0, x1, 4, params["dt"])
+    b = run_gpu_2d(plan.replace(use_graphs=False), q0, x1, 4, params["dt"])
+    assert np.array_equal(a, b)
+
+
+def test_gpu_2d_cutoff_needs_an_adaptive_plan():
+    q0, x1, _, n, _, params = load_golden_2d("katzer_teno")
+    plan = golden_plan_2d("katzer_teno", n=n).replace(dt=params["dt"])
+    s = Solver(plan)
+    s.set_coordinate(x1, 4)
+    s.set_state64_padded(q0, 4)
+    with pytest.raises(Exception):
+        s.teno_cutoff()
+    s.close()

@@ -69,14 +69,26 @@ def test_oracle_matches_reference_run(case, n, steps, extra):
     assert max(rel_err(q, q_ref)) < 1e-12
 
 
-def test_oracle_2d_matches_reference_golden():
+@pytest.mark.parametrize("case", ["katzer_teno", "katzer_adaptive"])
+def test_oracle_2d_matches_reference_golden(case):
     from helpers import load_golden_2d, golden_plan_2d, rel_err_2d
-    q0, x1, q_ref, n, steps, params = load_golden_2d()
-    plan = golden_plan_2d(n=n).replace(dt=params["dt"])
+    q0, x1, q_ref, n, steps, params = load_golden_2d(case)
+    plan = golden_plan_2d(case, n=n).replace(dt=params["dt"])
+    assert plan.teno_adaptive == (case == "katzer_adaptive")
     q = O.run2d(plan, q0, steps)
     assert max(rel_err_2d(q, q_ref)) < 1e-12
     # halos too (the outlet and wall faces write them)
     assert float(np.abs(q - q_ref).max()) < 1e-10
+
+
+def test_oracle_adaptive_cutoff_changes_the_solution():
+    """The sensor-driven cut-off is not the fixed C_T = 1e-5: running the published script's
+    fixture with the fixed cut-off leaves a visible difference, so the golden case pins the sensor."""
+    from helpers import load_golden_2d, golden_plan_2d, rel_err_2d
+    q0, x1, q_ref, n, steps, params = load_golden_2d("katzer_adaptive")
+    plan = golden_plan_2d("katzer_adaptive", n=n).replace(dt=params["dt"], teno_adaptive=False)
+    q = O.run2d(plan, q0, steps)
+    assert max(rel_err_2d(q, q_ref)) > 1e-6
 
 
 def test_oracle_2d_metrics_match_reference_coordinates():

@@ -54,6 +54,19 @@ def test_katzer_plan_matches_lowered_script():
     assert np.allclose(k.delta[:2], g.delta[:2], rtol=1e-15)
 
 
+def test_published_katzer_script_lowers_to_adaptive_teno():
+    from opensbli_gb300.plan import katzer_plan
+    k = katzer_plan(adaptive=True)
+    g = golden_plan("katzer_adaptive")
+    assert g.teno_adaptive and not golden_plan("katzer_teno").teno_adaptive
+    for f in ("conv", "teno_adaptive", "teno_a1", "teno_a2", "teno_eps", "bc", "Twall"):
+        assert getattr(k, f) == getattr(g, f), f
+    # the script substitutes epsilon = 1e-30, but the generated code keeps the value the sensor gives
+    # its constant (the line is not `epsilon=Input;`), so the lowered plan does too
+    assert g.sensor_eps == 1e-12 == k.sensor_eps
+    assert "ConstituentRelations evaluation" in g.kernels
+
+
 def test_cfl_dt_tgv_weno():
     p = tgv_plan(256, conv="weno5js", Minf=1.25)
     dt = tgv_cfl_dt(p)
@@ -61,7 +74,8 @@ def test_cfl_dt_tgv_weno():
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
-@pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgv_wenoz", "tgsym_central", "katzer_teno"])
+@pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgv_wenoz", "tgsym_central", "katzer_teno",
+                                  "katzer_adaptive"])
 def test_writer_lowers_reference_script(case, tmp_path):
     r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case, "--out",
                         str(tmp_path), "--ref", REF], capture_output=True, text=True, timeout=900)
