@@ -83,15 +83,30 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
     }
   };
   // primitives of one point into ring slot sl at (py, px)
+  // (FP32: u, p and T rounded once from their exact values, prims_f32, so the first- and second-
+  // derivative stencils see no extra rounding noise in them)
   auto put = [&](int sl, int py, int px, T rho, T r0, T r1, T r2, T E) {
-    const T irho = T(1) / rho;  // correctly rounded: u and T feed the viscous terms
-    const T u0 = r0 * irho, u1 = r1 * irho, u2 = r2 * irho;
-    const T half = T(0.5);
-    const T p = gm1 * (E - half * rho * u0 * u0 - half * rho * u1 * u1 - half * rho * u2 * u2);
+    T u0, u1, u2, p, Tt;
+    if constexpr (sizeof(T) == 4) {
+      float irho, u[3], p_lo;
+      prims_f32(rho, r0, r1, r2, E, gm1, irho, u, p, p_lo);
+      u0 = u[0];
+      u1 = u[1];
+      u2 = u[2];
+      Tt = scaled_ratio_f32(gM2, p, p_lo, rho, irho);
+    } else {
+      const T irho = T(1) / rho;  // correctly rounded: u and T feed the viscous terms
+      u0 = r0 * irho;
+      u1 = r1 * irho;
+      u2 = r2 * irho;
+      const T half = T(0.5);
+      p = gm1 * (E - half * rho * u0 * u0 - half * rho * u1 * u1 - half * rho * u2 * u2);
+      Tt = gM2 * p * irho;
+    }
     at(sl, F_U0, py, px) = u0;
     at(sl, F_U1, py, px) = u1;
     at(sl, F_U2, py, px) = u2;
-    at(sl, F_T, py, px) = gM2 * p * irho;
+    at(sl, F_T, py, px) = Tt;
     if (NF == 7) {
       at(sl, F_RHO, py, px) = rho;
       at(sl, F_P, py, px) = p;
@@ -153,8 +168,17 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
     }
   };
 
-  const T c1[5] = {T(1.0 / 12.0), T(-2.0 / 3.0), T(0), T(2.0 / 3.0), T(-1.0 / 12.0)};
   const T c2[5] = {T(-1.0 / 12.0), T(4.0 / 3.0), T(-2.5), T(4.0 / 3.0), T(-1.0 / 12.0)};
+  // 4th-order first derivative (times delta) from the values at offsets -2, -1, +1, +2, written on the
+  // differences of opposite points: rounding then scales with those differences, not with |f|
+  auto d1 = [](T fm2, T fm1, T fp1, T fp2) -> T { return T(2.0 / 3.0) * (fp1 - fm1) - T(1.0 / 12.0) * (fp2 - fm2); };
+  // 4th-order second derivative (times delta^2): FP32 on the differences from the centre value, FP64
+  // as the weighted sum
+  auto d2 = [&](T fm2, T fm1, T f0, T fp1, T fp2) -> T {
+    if constexpr (sizeof(T) == 4)
+      return T(4.0 / 3.0) * ((fp1 - f0) + (fm1 - f0)) - T(1.0 / 12.0) * ((fp2 - f0) + (fm2 - f0));
+    return c2[0] * fm2 + c2[1] * fm1 + c2[2] * f0 + c2[3] * fp1 + c2[4] * fp2;
+  };
   const T idl[3] = {pick<T>(ph.inv_delta[0], ph.f_inv_delta[0]), pick<T>(ph.inv_delta[1], ph.f_inv_delta[1]),
                     pick<T>(ph.inv_delta[2], ph.f_inv_delta[2])};
 
@@ -231,11 +255,7 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
       for (int c = 0; c < 3; ++c)
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-          T acc = T(0);
-#pragma unroll
-          for (int t = 0; t < 5; ++t)
-            if (t != 2) acc += c1[t] * SA(F_U0 + c, d, t - 2);
-          du[c][d] = acc * idl[d];
+          du[c][d] = d1(SA(F_U0 + c, d, -2), SA(F_U0 + c, d, -1), SA(F_U0 + c, d, 1), SA(F_U0 + c, d, 2)) * idl[d];
         }
       const T divu = du[0][0] + du[1][1] + du[2][2];
       const T uu[3] = {S(F_U0, 0, 0, 0), S(F_U1, 0, 0, 0), S(F_U2, 0, 0, 0)};
@@ -247,22 +267,29 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
         T dpu = T(0);
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-          T dphi[5] = {T(0), T(0), T(0), T(0), T(0)}, dphiu[5] = {T(0), T(0), T(0), T(0), T(0)};
-          T dp = T(0), dpud = T(0);
+          // the five conserved quantities phi, phi u_d, p and p u_d at offsets -2, -1, +1, +2 along d
+          T phi[4][5], phu[4][5], pp[4], ppu[4];
 #pragma unroll
-          for (int t = 0; t < 5; ++t) {
-            if (t == 2) continue;
-            const T r = SA(F_RHO, d, t - 2), ud = SA(F_U0 + d, d, t - 2), p = SA(F_P, d, t - 2);
-            const T phi[5] = {r, r * SA(F_U0, d, t - 2), r * SA(F_U1, d, t - 2), r * SA(F_U2, d, t - 2),
-                              SA(F_E, d, t - 2)};
+          for (int s4 = 0; s4 < 4; ++s4) {
+            const int o = s4 < 2 ? s4 - 2 : s4 - 1;
+            const T r = SA(F_RHO, d, o), ud = SA(F_U0 + d, d, o);
+            phi[s4][0] = r;
+            phi[s4][1] = r * SA(F_U0, d, o);
+            phi[s4][2] = r * SA(F_U1, d, o);
+            phi[s4][3] = r * SA(F_U2, d, o);
+            phi[s4][4] = SA(F_E, d, o);
 #pragma unroll
-            for (int v = 0; v < 5; ++v) {
-              dphi[v] += c1[t] * phi[v];
-              dphiu[v] += c1[t] * (phi[v] * ud);
-            }
-            dp += c1[t] * p;
-            dpud += c1[t] * (p * ud);
+            for (int v = 0; v < 5; ++v) phu[s4][v] = phi[s4][v] * ud;
+            pp[s4] = SA(F_P, d, o);
+            ppu[s4] = pp[s4] * ud;
           }
+          T dphi[5], dphiu[5];
+#pragma unroll
+          for (int v = 0; v < 5; ++v) {
+            dphi[v] = d1(phi[0][v], phi[1][v], phi[2][v], phi[3][v]);
+            dphiu[v] = d1(phu[0][v], phu[1][v], phu[2][v], phu[3][v]);
+          }
+          const T dp = d1(pp[0], pp[1], pp[2], pp[3]), dpud = d1(ppu[0], ppu[1], ppu[2], ppu[3]);
 #pragma unroll
           for (int v = 0; v < 5; ++v) acc[v] += (dphiu[v] + uu[d] * dphi[v]) * idl[d];
           R[1 + d] -= dp * idl[d];
@@ -282,35 +309,28 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
         for (int d = 0; d < 3; ++d) {
           const T id2 = idl[d] * idl[d];
 #pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            T acc = T(0);
-#pragma unroll
-            for (int t = 0; t < 5; ++t) acc += c2[t] * SA(F_U0 + c, d, t - 2);
-            d2u[c][d] = acc * id2;
-          }
-          T acc = T(0);
-#pragma unroll
-          for (int t = 0; t < 5; ++t) acc += c2[t] * SA(F_T, d, t - 2);
-          lapT += acc * id2;
+          for (int c = 0; c < 3; ++c)
+            d2u[c][d] = d2(SA(F_U0 + c, d, -2), SA(F_U0 + c, d, -1), SA(F_U0 + c, d, 0), SA(F_U0 + c, d, 1),
+                           SA(F_U0 + c, d, 2)) * id2;
+          lapT += d2(SA(F_T, d, -2), SA(F_T, d, -1), SA(F_T, d, 0), SA(F_T, d, 1), SA(F_T, d, 2)) * id2;
         }
         // mixed derivative d_b(d_a u_c), a < b
         auto mixed = [&](int c, int a, int b) -> T {
-          T outer = T(0);
+          T inner[4];
 #pragma unroll
-          for (int tb = 0; tb < 5; ++tb) {
-            if (tb == 2) continue;
-            T inner = T(0);
+          for (int sb = 0; sb < 4; ++sb) {
+            const int ob = sb < 2 ? sb - 2 : sb - 1;
+            T f[4];
 #pragma unroll
-            for (int ta = 0; ta < 5; ++ta) {
-              if (ta == 2) continue;
+            for (int sa = 0; sa < 4; ++sa) {
               int o[3] = {0, 0, 0};
-              o[a] = ta - 2;
-              o[b] = tb - 2;
-              inner += c1[ta] * S(F_U0 + c, o[2], o[1], o[0]);
+              o[a] = sa < 2 ? sa - 2 : sa - 1;
+              o[b] = ob;
+              f[sa] = S(F_U0 + c, o[2], o[1], o[0]);
             }
-            outer += c1[tb] * (inner * idl[a]);
+            inner[sb] = d1(f[0], f[1], f[2], f[3]) * idl[a];
           }
-          return outer * idl[b];
+          return d1(inner[0], inner[1], inner[2], inner[3]) * idl[b];
         };
         // d_i(div u) = d_ii u_i + sum_{c != i} d_i d_c u_c
         const T m01_1 = mixed(1, 0, 1), m02_2 = mixed(2, 0, 2);  // for i = 0

@@ -92,6 +92,49 @@ template <typename T> __device__ __forceinline__ T rcp_t(T x);
 template <> __device__ __forceinline__ float rcp_t<float>(float x) { return __fdividef(1.0f, x); }
 template <> __device__ __forceinline__ double rcp_t<double>(double x) { return 1.0 / x; }
 
+// ---- FP32 primitives rounded once.  The FP32 state is exact input; what the mixed path must avoid is
+// extra rounding noise in u, p and T, which the derivative stencils and flux differences amplify by
+// 1/delta or 1/delta^2 (p = (g-1)(E - |m|^2/(2 rho)) also loses bits to cancellation).  Error-free
+// transformations (the exact division residual from one FMA, Dekker/Knuth two-product and two-sum)
+// carry the discarded parts: u_c comes out correctly rounded in almost every case, p within about one
+// ulp of (g-1)_f32 (E - |m|^2/(2 rho)) evaluated exactly.  p_lo is the part of p below p_hi.
+__device__ __forceinline__ void prims_f32(float rho, float m0, float m1, float m2, float E, float gm1, float &irho,
+                                          float (&u)[3], float &p_hi, float &p_lo) {
+  // __fmul_rn/__fadd_rn are never contracted into FMAs: the two-sum identities need the rounded
+  // sums and products they are written with
+  irho = 1.0f / rho;
+  const float m[3] = {m0, m1, m2};
+  float k_hi = 0.0f, k_lo = 0.0f;  // |m|^2 / rho as an unevaluated sum
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float q = __fmul_rn(m[c], irho);
+    const float e = fmaf(-q, rho, m[c]);  // m - q rho, exact
+    u[c] = fmaf(e, irho, q);
+    // m (m / rho) = m q + m e / rho
+    const float ph = __fmul_rn(m[c], q);
+    const float pl = fmaf(m[c], q, -ph) + m[c] * (e * irho);
+    const float s = __fadd_rn(k_hi, ph), bv = __fsub_rn(s, k_hi);
+    k_lo += __fadd_rn(__fsub_rn(k_hi, __fsub_rn(s, bv)), __fsub_rn(ph, bv)) + pl;
+    k_hi = s;
+  }
+  const float h = -0.5f * k_hi;  // exact
+  const float d = __fadd_rn(E, h), bv = __fsub_rn(d, E);
+  const float d_lo = __fadd_rn(__fsub_rn(E, __fsub_rn(d, bv)), __fsub_rn(h, bv)) - 0.5f * k_lo;
+  const float ph = __fmul_rn(gm1, d);
+  const float pl = fmaf(gm1, d, -ph) + gm1 * d_lo;
+  p_hi = __fadd_rn(ph, pl);  // renormalise
+  p_lo = __fsub_rn(pl, __fsub_rn(p_hi, ph));
+}
+
+// c (p_hi + p_lo) / rho rounded once (T = gama Minf^2 p / rho)
+__device__ __forceinline__ float scaled_ratio_f32(float c, float p_hi, float p_lo, float rho, float irho) {
+  const float n_hi = __fmul_rn(c, p_hi);
+  const float n_lo = fmaf(c, p_hi, -n_hi) + c * p_lo;
+  const float q = __fmul_rn(n_hi, irho);
+  const float e = fmaf(-q, rho, n_hi) + n_lo;
+  return fmaf(e, irho, q);
+}
+
 template <typename T> __device__ __forceinline__ T abs_t(T x) { return x < T(0) ? -x : x; }
 template <typename T> __device__ __forceinline__ T max_t(T a, T b) { return a > b ? a : b; }
 

@@ -346,7 +346,7 @@ __device__ __forceinline__ void weno_march_x_tile(const Grid &g, Fields5<const T
       point_prims<T, 0>(r, gm1, gama, W[5]);
       if (p >= c0 + 2) {  // window holds points c-3 .. c+2 of interface c = p - 2
         const int c = p - 2;
-        T F[5];
+        T F[5] = {T(0), T(0), T(0), T(0), T(0)};  // rows past n1: defined, never stored
         if (row_ok) interface_flux<T, 0, SCH>(W, gm1, igm1, eps, F);
         if (c > c0) {
           const int cc = c - 1;  // cell finished by this interface
@@ -362,8 +362,9 @@ __device__ __forceinline__ void weno_march_x_tile(const Grid &g, Fields5<const T
   }
 }
 
+// FP32: 384 resident threads per SM, so the difference-form flux fits in registers without spills
 template <typename T, int BY, int SCH>
-__global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 512 : 256) / (32 * BY))
+__global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 384 : 256) / (32 * BY))
     k_weno_march_x(Grid g, Fields5<const T> q, Fields5<T> res, Phys ph, int L) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   weno_march_x_tile<T, BY, SCH>(g, q, res, ph, L, blockIdx.x, blockIdx.y, blockIdx.z, smem_raw);

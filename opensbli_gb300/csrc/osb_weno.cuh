@@ -109,23 +109,164 @@ template <typename T> struct WPt {
 // Primitive quantities of one point from its conserved vector.  1/rho is a correctly rounded
 // division: the velocity enters the physical flux directly, and a biased reciprocal would bias
 // every flux difference by the same relative amount, step after step.
+// In FP32, u_D and p are rounded once from their exact values (prims_f32).
 template <typename T, int D>
 __device__ __forceinline__ void point_prims(const T (&r)[5], T gm1, T gama, WPt<T> &w) {
-  const T irho = T(1) / r[0];
-  const T u0 = r[1] * irho, u1 = r[2] * irho, u2 = r[3] * irho;
-  const T p = gm1 * (r[4] - T(0.5) * (r[1] * u0 + r[2] * u1 + r[3] * u2));
+  T irho, p;
+  if constexpr (sizeof(T) == 4) {
+    float u[3], p_lo;
+    prims_f32(r[0], r[1], r[2], r[3], r[4], gm1, irho, u, p, p_lo);
+    w.ud = u[D];
+  } else {
+    irho = T(1) / r[0];
+    const T u0 = r[1] * irho, u1 = r[2] * irho, u2 = r[3] * irho;
+    p = gm1 * (r[4] - T(0.5) * (r[1] * u0 + r[2] * u1 + r[3] * u2));
+    w.ud = D == 0 ? u0 : D == 1 ? u1 : u2;
+  }
 #pragma unroll
   for (int v = 0; v < 5; ++v) w.Q[v] = r[v];
   w.p = p;
   T ia;
   sqrt_rsqrt(gama * p * irho, w.a, ia);
-  w.ud = D == 0 ? u0 : D == 1 ? u1 : u2;
+}
+
+// FP32: the same flux in difference form about window point 2 (point i).  The reconstruction
+// reproduces constants (candidates are consistent, weights sum to one) and the splitting is linear,
+// so replacing every point's conserved vector Q_t and physical flux F_t by Q_t - Q_i and F_t - F_i
+// makes it return LEV.(F^ - F_i), and REV maps that to F_{i+1/2} - F_i (REV LEV = I).  The projections
+// then act on differences of neighbouring points instead of O(1) values: their FP32 rounding, which
+// otherwise dominates the flux differences that form the residual, shrinks with the differences.
+// F_{i+1/2} = F_i + (F_{i+1/2} - F_i) is rounded once.
+template <int D, int SCH>
+__device__ __forceinline__ void interface_flux_delta(const WPt<float> (&W)[6], const float gm1, const float igm1,
+                                                     const float eps, float out[5]) {
+  using T = float;
+  constexpr int E1 = (D + 1) % 3, E2 = (D + 2) % 3;
+  constexpr int e1 = 3 - E1 - D, e2 = 3 - E2 - D;
+  // ---- Roe average of points 2 and 3 (as below)
+  const T rl = W[2].Q[0], rr = W[3].Q[0];
+  T sl, sr, isl, isr;
+  sqrt_rsqrt(rl, sl, isl);
+  sqrt_rsqrt(rr, sr, isr);
+  const T rho = sl * sr;
+  const T inv_s = rcp_t(sl + sr);
+  T u[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) u[c] = inv_s * (W[2].Q[1 + c] * isl + W[3].Q[1 + c] * isr);
+  const T Hh = inv_s * ((W[2].p + W[2].Q[4]) * isl + (W[3].p + W[3].Q[4]) * isr);
+  const T usq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+  T a, ia;
+  sqrt_rsqrt(gm1 * (Hh - T(0.5) * usq), a, ia);
+  const T irho = isl * isr;
+  const T phi = gm1 * T(0.5) * usq;
+  const T bt = T(0.70710678118654752440) * irho * ia;
+  const T al = T(0.70710678118654752440) * rho * ia;
+  const T ia2 = ia * ia;
+  const T btA = bt * a;
+  T lam_u = T(0), lam_p = T(0), lam_m = T(0);
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    lam_u = max_t(lam_u, abs_t(W[t].ud));
+    lam_p = max_t(lam_p, abs_t(W[t].ud + W[t].a));
+    lam_m = max_t(lam_m, abs_t(W[t].a - W[t].ud));
+  }
+  auto recon = [&](const T (&cf)[6], const T (&cs)[6], T lam) -> T {
+    T fp[6], fm[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      fp[t] = cf[t] + lam * cs[t];
+      fm[t] = cf[t] - lam * cs[t];
+    }
+    return weno5_side<T, SCH>(fp[0], fp[1], fp[2], fp[3], fp[4], eps) +
+           weno5_side<T, SCH>(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
+  };
+  // physical flux component v of point t: (Q_{1+D}, Q_{1+c} u_D + delta_cD p, (Q_4 + p) u_D)
+  auto flux = [&](int t, int v) -> T {
+    const WPt<T> &w = W[t];
+    if (v == 0) return w.Q[1 + D];
+    if (v == 4) return (w.Q[4] + w.p) * w.ud;
+    return v - 1 == D ? fmaf(w.Q[v], w.ud, w.p) : w.Q[v] * w.ud;
+  };
+  T F2[5];
+#pragma unroll
+  for (int v = 0; v < 5; ++v) F2[v] = flux(2, v);
+  auto dQ = [&](int t, int v) -> T { return t == 2 ? T(0) : W[t].Q[v] - W[2].Q[v]; };
+  auto dF = [&](int t, int v) -> T { return t == 2 ? T(0) : flux(t, v) - F2[v]; };
+
+  const T se1 = (D == (E1 + 1) % 3) ? T(1) : T(-1), se2 = (D == (E2 + 1) % 3) ? T(1) : T(-1);
+  T rE1, rE2;
+  {
+    T cf[6], cs[6];
+    const T sr1 = se1 * irho;
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = sr1 * (u[e1] * dF(t, 0) - dF(t, 1 + e1));
+      cs[t] = sr1 * (u[e1] * dQ(t, 0) - dQ(t, 1 + e1));
+    }
+    rE1 = recon(cf, cs, lam_u);
+    const T sr2 = se2 * irho;
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = sr2 * (u[e2] * dF(t, 0) - dF(t, 1 + e2));
+      cs[t] = sr2 * (u[e2] * dQ(t, 0) - dQ(t, 1 + e2));
+    }
+    rE2 = recon(cf, cs, lam_u);
+  }
+  T gQ[6], gF[6], hQ[6], hF[6];
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    const T uq = u[0] * dQ(t, 1) + u[1] * dQ(t, 2) + u[2] * dQ(t, 3);
+    const T uf = u[0] * dF(t, 1) + u[1] * dF(t, 2) + u[2] * dF(t, 3);
+    gQ[t] = phi * dQ(t, 0) - gm1 * uq + gm1 * dQ(t, 4);
+    hQ[t] = dQ(t, 1 + D) - u[D] * dQ(t, 0);
+    gF[t] = phi * dF(t, 0) - gm1 * uf + gm1 * dF(t, 4);
+    hF[t] = dF(t, 1 + D) - u[D] * dF(t, 0);
+  }
+  T rD, r3, r4;
+  {
+    T cf[6], cs[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = dF(t, 0) - gF[t] * ia2;
+      cs[t] = dQ(t, 0) - gQ[t] * ia2;
+    }
+    rD = recon(cf, cs, lam_u);
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = bt * gF[t] + btA * hF[t];
+      cs[t] = bt * gQ[t] + btA * hQ[t];
+    }
+    r3 = recon(cf, cs, lam_p);
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = bt * gF[t] - btA * hF[t];
+      cs[t] = bt * gQ[t] - btA * hQ[t];
+    }
+    r4 = recon(cf, cs, lam_m);
+  }
+  const T sac = r3 + r4, dac = r3 - r4;
+  const T hh = (phi + a * a) * igm1;
+  T G[5];
+  G[0] = rD + al * sac;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) G[1 + c] = u[c] * rD + al * (u[c] * sac + (c == D ? a * dac : T(0)));
+  G[4] = (phi * igm1) * rD + al * (hh * sac + u[D] * a * dac);
+  G[1 + e1] -= se1 * rho * rE1;
+  G[4] -= se1 * rho * u[e1] * rE1;
+  G[1 + e2] -= se2 * rho * rE2;
+  G[4] -= se2 * rho * u[e2] * rE2;
+#pragma unroll
+  for (int v = 0; v < 5; ++v) out[v] = F2[v] + G[v];
 }
 
 // Characteristic flux at the interface between window points 2 and 3 (points i and i+1).
 template <typename T, int D, int SCH>
 __device__ __forceinline__ void interface_flux(const WPt<T> (&W)[6], const T gm1, const T igm1, const T eps,
                                                T out[5]) {
+  if constexpr (sizeof(T) == 4) {
+    interface_flux_delta<D, SCH>(W, gm1, igm1, eps, out);
+    return;
+  }
   constexpr int E1 = (D + 1) % 3, E2 = (D + 2) % 3;  // the two tangential axes (shear rows)
   constexpr int e1 = 3 - E1 - D, e2 = 3 - E2 - D;    // third axis of each shear row
   // ---- Roe average of points 2 and 3
