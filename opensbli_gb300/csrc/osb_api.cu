@@ -567,6 +567,8 @@ Phys plan_phys(const osb_plan_desc *plan) {
   ph.f_kT = (float)ph.kT;
   ph.f_eps = (float)ph.weno_eps;
   for (int d = 0; d < 3; ++d) ph.f_inv_delta[d] = (float)ph.inv_delta[d];
+  ph.f_gm1_lo = (float)(ph.gm1 - (double)ph.f_gm1);
+  for (int d = 0; d < 3; ++d) ph.f_inv_delta_lo[d] = (float)(ph.inv_delta[d] - (double)ph.f_inv_delta[d]);
   return ph;
 }
 }  // namespace osb

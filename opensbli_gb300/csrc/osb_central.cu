@@ -60,7 +60,7 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * TX + tx;
   const int i0 = bx * TX, j0 = by * TY, k0 = bz * zchunk;
   const int k1 = min(k0 + zchunk, g.n2);
-  const T gm1 = pick<T>(ph.gm1, ph.f_gm1);
+  const T gm1 = pick<T>(ph.gm1, ph.f_gm1), gm1_lo = pick<T>(0.0, ph.f_gm1_lo);
   const T gM2 = pick<T>(ph.gM2, ph.f_gM2);
 
   auto slot = [](int k) { return ((k % NP) + NP) % NP; };
@@ -89,7 +89,7 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
     T u0, u1, u2, p, Tt;
     if constexpr (sizeof(T) == 4) {
       float irho, u[3], p_lo;
-      prims_f32(rho, r0, r1, r2, E, gm1, irho, u, p, p_lo);
+      prims_f32(rho, r0, r1, r2, E, gm1, gm1_lo, irho, u, p, p_lo);
       u0 = u[0];
       u1 = u[1];
       u2 = u[2];
@@ -181,6 +181,8 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
   };
   const T idl[3] = {pick<T>(ph.inv_delta[0], ph.f_inv_delta[0]), pick<T>(ph.inv_delta[1], ph.f_inv_delta[1]),
                     pick<T>(ph.inv_delta[2], ph.f_inv_delta[2])};
+  const T idl_lo[3] = {pick<T>(0.0, ph.f_inv_delta_lo[0]), pick<T>(0.0, ph.f_inv_delta_lo[1]),
+                       pick<T>(0.0, ph.f_inv_delta_lo[2])};
 
   if constexpr (TMA) {
     // every TMA destination must sit on a 128-byte boundary: refuse (status 2) rather than copy
@@ -255,7 +257,8 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
       for (int c = 0; c < 3; ++c)
 #pragma unroll
         for (int d = 0; d < 3; ++d) {
-          du[c][d] = d1(SA(F_U0 + c, d, -2), SA(F_U0 + c, d, -1), SA(F_U0 + c, d, 1), SA(F_U0 + c, d, 2)) * idl[d];
+          du[c][d] = mul_hl(d1(SA(F_U0 + c, d, -2), SA(F_U0 + c, d, -1), SA(F_U0 + c, d, 1), SA(F_U0 + c, d, 2)),
+                            idl[d], idl_lo[d]);
         }
       const T divu = du[0][0] + du[1][1] + du[2][2];
       const T uu[3] = {S(F_U0, 0, 0, 0), S(F_U1, 0, 0, 0), S(F_U2, 0, 0, 0)};
@@ -291,9 +294,9 @@ __device__ __forceinline__ void central_tile(const Grid &g, Fields5<const T> q, 
           }
           const T dp = d1(pp[0], pp[1], pp[2], pp[3]), dpud = d1(ppu[0], ppu[1], ppu[2], ppu[3]);
 #pragma unroll
-          for (int v = 0; v < 5; ++v) acc[v] += (dphiu[v] + uu[d] * dphi[v]) * idl[d];
-          R[1 + d] -= dp * idl[d];
-          dpu += dpud * idl[d];
+          for (int v = 0; v < 5; ++v) acc[v] += mul_hl(dphiu[v] + uu[d] * dphi[v], idl[d], idl_lo[d]);
+          R[1 + d] -= mul_hl(dp, idl[d], idl_lo[d]);
+          dpu += mul_hl(dpud, idl[d], idl_lo[d]);
         }
 #pragma unroll
         for (int v = 0; v < 5; ++v) R[v] -= T(0.5) * (acc[v] + phi0[v] * divu);

@@ -36,6 +36,10 @@ struct Phys {
   // gama-1, 1/(gama-1), gama*Minf^2, 1/Re, kT = 1/((gama-1) Minf^2 Pr Re)
   double gm1, igm1, gM2, invRe, kT;
   float f_gama, f_gm1, f_igm1, f_gM2, f_invRe, f_kT, f_eps, f_inv_delta[3];
+  // FP32 remainders: gama-1 = f_gm1 + f_gm1_lo, 1/delta_d = f_inv_delta[d] + f_inv_delta_lo[d].  A
+  // constant rounded to FP32 alone would scale every pressure or every flux difference by the same
+  // factor (1/delta: up to 6e-8), a bias that grows linearly in time instead of averaging out.
+  float f_gm1_lo, f_inv_delta_lo[3];
 };
 
 // the FP64 or FP32 copy of a plan constant
@@ -98,8 +102,8 @@ template <> __device__ __forceinline__ double rcp_t<double>(double x) { return 1
 // transformations (the exact division residual from one FMA, Dekker/Knuth two-product and two-sum)
 // carry the discarded parts: u_c comes out correctly rounded in almost every case, p within about one
 // ulp of (g-1)_f32 (E - |m|^2/(2 rho)) evaluated exactly.  p_lo is the part of p below p_hi.
-__device__ __forceinline__ void prims_f32(float rho, float m0, float m1, float m2, float E, float gm1, float &irho,
-                                          float (&u)[3], float &p_hi, float &p_lo) {
+__device__ __forceinline__ void prims_f32(float rho, float m0, float m1, float m2, float E, float gm1, float gm1_lo,
+                                          float &irho, float (&u)[3], float &p_hi, float &p_lo) {
   // __fmul_rn/__fadd_rn are never contracted into FMAs: the two-sum identities need the rounded
   // sums and products they are written with
   irho = 1.0f / rho;
@@ -121,7 +125,7 @@ __device__ __forceinline__ void prims_f32(float rho, float m0, float m1, float m
   const float d = __fadd_rn(E, h), bv = __fsub_rn(d, E);
   const float d_lo = __fadd_rn(__fsub_rn(E, __fsub_rn(d, bv)), __fsub_rn(h, bv)) - 0.5f * k_lo;
   const float ph = __fmul_rn(gm1, d);
-  const float pl = fmaf(gm1, d, -ph) + gm1 * d_lo;
+  const float pl = fmaf(gm1, d, -ph) + fmaf(gm1, d_lo, gm1_lo * d);
   p_hi = __fadd_rn(ph, pl);  // renormalise
   p_lo = __fsub_rn(pl, __fsub_rn(p_hi, ph));
 }
@@ -134,6 +138,10 @@ __device__ __forceinline__ float scaled_ratio_f32(float c, float p_hi, float p_l
   const float e = fmaf(-q, rho, n_hi) + n_lo;
   return fmaf(e, irho, q);
 }
+
+// x * (hi + lo) for a constant carried as an FP32 pair; FP64 ignores lo
+__device__ __forceinline__ float mul_hl(float x, float hi, float lo) { return fmaf(x, hi, x * lo); }
+__device__ __forceinline__ double mul_hl(double x, double hi, double) { return x * hi; }
 
 template <typename T> __device__ __forceinline__ T abs_t(T x) { return x < T(0) ? -x : x; }
 template <typename T> __device__ __forceinline__ T max_t(T a, T b) { return a > b ? a : b; }

@@ -62,6 +62,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
   const int n[3] = {g.n0, g.n1, g.n2};
   const T gm1 = pick<T>(ph.gm1, ph.f_gm1), gama = pick<T>(ph.gama, ph.f_gama);
   const T igm1 = pick<T>(ph.igm1, ph.f_igm1), eps = pick<T>(ph.weno_eps, ph.f_eps);
+  const T gm1_lo = pick<T>(0.0, ph.f_gm1_lo);
 
   // tile origin: first cell whose flux difference this block writes (d0), across-line origin
   int d0, a0, o1, o2;
@@ -110,7 +111,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
       if (DIR == 0) { a = t / NPT; pos = t % NPT; }
       else { pos = t / TA; a = t % TA; }
       WPt<T> w;
-      point_prims<T, DIR>(r[l], gm1, gama, w);
+      point_prims<T, DIR>(r[l], gm1, gm1_lo, gama, w);
       sf[sidx(W_RHO, pos, a)] = w.Q[0];
       sf[sidx(W_RU0, pos, a)] = w.Q[1];
       sf[sidx(W_RU1, pos, a)] = w.Q[2];
@@ -150,6 +151,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
 
   // ---- flux difference for cells d0 .. d0+TI-2 (residual loads issued before the stores)
   const T idd = pick<T>(ph.inv_delta[DIR], ph.f_inv_delta[DIR]);
+  const T idd_lo = pick<T>(0.0, ph.f_inv_delta_lo[DIR]);
   constexpr int NST = ((TI - 1) * TA + 255) / 256;
   T rv[NST][5];
   int64_t gi[NST];
@@ -179,7 +181,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
     else { m = t / TA; a = t % TA; }
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
-      const T d = -(sflux[fidx(v, m + 1, a)] - sflux[fidx(v, m, a)]) * idd;
+      const T d = -mul_hl(sflux[fidx(v, m + 1, a)] - sflux[fidx(v, m, a)], idd, idd_lo);
       res.v[v][gi[l]] = ACCUM ? rv[l][v] + d : d;
     }
   }
@@ -202,6 +204,7 @@ __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> 
   const T gm1 = pick<T>(ph.gm1, ph.f_gm1), gama = pick<T>(ph.gama, ph.f_gama);
   const T igm1 = pick<T>(ph.igm1, ph.f_igm1), eps = pick<T>(ph.weno_eps, ph.f_eps);
   const T idd = pick<T>(ph.inv_delta[DIR], ph.f_inv_delta[DIR]);
+  const T idd_lo = pick<T>(0.0, ph.f_inv_delta_lo[DIR]), gm1_lo = pick<T>(0.0, ph.f_gm1_lo);
 
   // points c0-3 .. c0+1 fill the window; point c0+2 is the first one streamed in
   WPt<T> W[6];
@@ -212,7 +215,7 @@ __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> 
 #pragma unroll
       for (int v = 0; v < 5; ++v) r[t][v] = __ldg(q.v[v] + mline + (int64_t)(c0 - 3 + t) * sd);
 #pragma unroll
-    for (int t = 0; t < 5; ++t) point_prims<T, DIR>(r[t], gm1, gama, W[t]);
+    for (int t = 0; t < 5; ++t) point_prims<T, DIR>(r[t], gm1, gm1_lo, gama, W[t]);
   }
   T nq[5];
 #pragma unroll
@@ -221,7 +224,7 @@ __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> 
   // interface c lies between cells c-1 and c and uses points c-3 .. c+2
 #pragma unroll 1
   for (int c = c0; c <= c1; ++c) {
-    point_prims<T, DIR>(nq, gm1, gama, W[5]);
+    point_prims<T, DIR>(nq, gm1, gm1_lo, gama, W[5]);
     if (c < c1) {  // point c+3 <= nd+2 lies inside the halo
 #pragma unroll
       for (int v = 0; v < 5; ++v) nq[v] = __ldg(q.v[v] + mline + (int64_t)(c + 3) * sd);
@@ -237,7 +240,7 @@ __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> 
     if (c > c0) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        const T d = -(F[v] - Fp[v]) * idd;
+        const T d = -mul_hl(F[v] - Fp[v], idd, idd_lo);
         res.v[v][mc] = ACCUM ? rv[v] + d : d;
       }
     }
@@ -286,6 +289,7 @@ __device__ __forceinline__ void weno_march_x_tile(const Grid &g, Fields5<const T
   const T gm1 = pick<T>(ph.gm1, ph.f_gm1), gama = pick<T>(ph.gama, ph.f_gama);
   const T igm1 = pick<T>(ph.igm1, ph.f_igm1), eps = pick<T>(ph.weno_eps, ph.f_eps);
   const T idd = pick<T>(ph.inv_delta[0], ph.f_inv_delta[0]);
+  const T idd_lo = pick<T>(0.0, ph.f_inv_delta_lo[0]), gm1_lo = pick<T>(0.0, ph.f_gm1_lo);
   const int lrow = lane / XC, lcol = lane % XC;  // loader position inside a chunk
   const bool row_ok = j0 + lane < n1;
 
@@ -343,7 +347,7 @@ __device__ __forceinline__ void weno_march_x_tile(const Grid &g, Fields5<const T
       T r[5];
 #pragma unroll
       for (int v = 0; v < 5; ++v) r[v] = qs[(v * 32 + lane) * QP + (p - xc)];
-      point_prims<T, 0>(r, gm1, gama, W[5]);
+      point_prims<T, 0>(r, gm1, gm1_lo, gama, W[5]);
       if (p >= c0 + 2) {  // window holds points c-3 .. c+2 of interface c = p - 2
         const int c = p - 2;
         T F[5] = {T(0), T(0), T(0), T(0), T(0)};  // rows past n1: defined, never stored
@@ -352,7 +356,7 @@ __device__ __forceinline__ void weno_march_x_tile(const Grid &g, Fields5<const T
           const int cc = c - 1;  // cell finished by this interface
           const int gs = ((cc + 4) / RG) * RG - 4, col = cc - gs;
 #pragma unroll
-          for (int v = 0; v < 5; ++v) rs[(v * 32 + lane) * RP + col] = -(F[v] - Fp[v]) * idd;
+          for (int v = 0; v < 5; ++v) rs[(v * 32 + lane) * RP + col] = -mul_hl(F[v] - Fp[v], idd, idd_lo);
           if (col == RG - 1 || cc == c1 - 1) flush(gs, c0, c1 - 1);
         }
 #pragma unroll

@@ -111,11 +111,11 @@ template <typename T> struct WPt {
 // every flux difference by the same relative amount, step after step.
 // In FP32, u_D and p are rounded once from their exact values (prims_f32).
 template <typename T, int D>
-__device__ __forceinline__ void point_prims(const T (&r)[5], T gm1, T gama, WPt<T> &w) {
+__device__ __forceinline__ void point_prims(const T (&r)[5], T gm1, T gm1_lo, T gama, WPt<T> &w) {
   T irho, p;
   if constexpr (sizeof(T) == 4) {
     float u[3], p_lo;
-    prims_f32(r[0], r[1], r[2], r[3], r[4], gm1, irho, u, p, p_lo);
+    prims_f32(r[0], r[1], r[2], r[3], r[4], gm1, gm1_lo, irho, u, p, p_lo);
     w.ud = u[D];
   } else {
     irho = T(1) / r[0];
