@@ -32,6 +32,11 @@ int cuda_err(osb_ctx *c, cudaError_t e, const char *where) {
   return set_err(c, OSB_ECUDA, buf);
 }
 
+// the characteristic-flux schemes of the 3D kernels (WENO5-JS, WENO5-Z, TENO5)
+bool char_fluxes(const osb_plan_desc &p) {
+  return p.conv == OSB_CONV_WENO5JS || p.conv == OSB_CONV_WENO5Z || p.conv == OSB_CONV_TENO5;
+}
+
 int validate(const osb_plan_desc *p, char *why, size_t n) {
   if (!p) { snprintf(why, n, "null plan"); return OSB_EINVAL; }
   if (p->abi_version != OSB_ABI_VERSION) { snprintf(why, n, "abi_version %d != %d", p->abi_version, OSB_ABI_VERSION); return OSB_EINVAL; }
@@ -77,7 +82,8 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
       return OSB_EINVAL;
     }
   }
-  if (p->conv != OSB_CONV_CENTRAL_SKEW && p->conv != OSB_CONV_WENO5JS && p->conv != OSB_CONV_WENO5Z) {
+  if (p->conv != OSB_CONV_CENTRAL_SKEW && p->conv != OSB_CONV_WENO5JS && p->conv != OSB_CONV_WENO5Z &&
+      p->conv != OSB_CONV_TENO5) {
     snprintf(why, n, "convective scheme %d not supported on 3D blocks", p->conv);
     return OSB_EUNSUPPORTED;
   }
@@ -306,7 +312,7 @@ template <typename T> void residual_into(osb_ctx *c, int cur, cudaStream_t s) {
   Fields5<const T> qc = fields<const T>(qs);
   Fields5<T> r = fields<T>(c->res);
   launch_halos<T>(*c, q, s, &c->launches);
-  if (c->plan.conv == OSB_CONV_WENO5JS || c->plan.conv == OSB_CONV_WENO5Z) {
+  if (char_fluxes(c->plan)) {
     weno_all<T>(c, qc, r, s);
     const int mode = CRK_RIN | (c->plan.visc == OSB_VISC_CONST ? CRK_VISC : 0);
     launch_central_rk<T>(*c, qc, r, fields_d(c->qold), r, r, 0.0, 0.0, mode, s, &c->launches);
@@ -330,7 +336,7 @@ template <typename T> void one_step(osb_ctx *c, int start, double dt, cudaStream
     }
     const double dtn = dt * c->plan.rk_b[st], dto = dt * c->plan.rk_a[st];
     const int visc = c->plan.visc == OSB_VISC_CONST ? CRK_VISC : 0;
-    if (c->plan.conv == OSB_CONV_WENO5JS || c->plan.conv == OSB_CONV_WENO5Z) {
+    if (char_fluxes(c->plan)) {
       weno_all<T>(c, qc, r, s);
       ProfScope ps(c, PF_CENTRAL_RK, s);
       launch_central_rk<T>(*c, qc, fields<T>(qn), fields_d(c->qold), r, r, dtn, dto, CRK_RIN | visc | CRK_UPDATE, s,
@@ -553,7 +559,9 @@ Phys plan_phys(const osb_plan_desc *plan) {
   ph.Re = plan->Re;
   ph.Pr = plan->Pr;
   for (int d = 0; d < 3; ++d) ph.inv_delta[d] = 1.0 / plan->delta[d];
-  ph.weno_eps = plan->weno_eps > 0 ? plan->weno_eps : 1e-6;
+  ph.weno_eps = plan->conv == OSB_CONV_TENO5 ? plan->teno_eps : plan->weno_eps > 0 ? plan->weno_eps : 1e-6;
+  ph.teno_ct = plan->teno_ct;
+  ph.f_teno_ct = (float)plan->teno_ct;
   ph.gm1 = plan->gama - 1.0;
   ph.igm1 = 1.0 / ph.gm1;
   ph.gM2 = plan->Minf * plan->Minf * plan->gama;
@@ -1016,7 +1024,7 @@ template <typename T> static int autotune_impl(osb_ctx *c, int reps, double *bes
   };
   for (int t = 0; t < OSB_TUNE_SLOTS && best_ms; ++t) best_ms[t] = 0.0;
   const int n[3] = {c->g.n0, c->g.n1, c->g.n2};
-  const bool weno = c->plan.conv == OSB_CONV_WENO5JS || c->plan.conv == OSB_CONV_WENO5Z;
+  const bool weno = char_fluxes(c->plan);
   for (int d = 0; d < 3 && weno && err == cudaSuccess; ++d) {
     std::vector<WenoCfg> cand{{WENO_TILE, 32}};
     for (int kind : {WENO_MARCH4, WENO_MARCH8}) {
@@ -1114,7 +1122,7 @@ int osb_tma_active(osb_ctx *c) {
   if (!c) return OSB_EINVAL;
   const int buf_ok = c->cur == 0 ? c->tma_ok[0] : c->tma_ok[1];
   return (c->tma_enabled && buf_ok && c->plan.ndim == 3 && c->mixed &&
-          (c->plan.conv == OSB_CONV_WENO5JS || c->plan.conv == OSB_CONV_WENO5Z)) ? 1 : 0;
+          (char_fluxes(c->plan))) ? 1 : 0;
 }
 
 int osb_get_central_shape(osb_ctx *c, int *ty) {

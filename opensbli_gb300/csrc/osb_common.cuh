@@ -40,6 +40,9 @@ struct Phys {
   // constant rounded to FP32 alone would scale every pressure or every flux difference by the same
   // factor (1/delta: up to 6e-8), a bias that grows linearly in time instead of averaging out.
   float f_gm1_lo, f_inv_delta_lo[3];
+  // TENO cut-off C_T (weno_eps holds TENO's eps for TENO plans)
+  double teno_ct;
+  float f_teno_ct;
 };
 
 // the FP64 or FP32 copy of a plan constant

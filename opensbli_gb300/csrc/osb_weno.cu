@@ -62,6 +62,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
   const int n[3] = {g.n0, g.n1, g.n2};
   const T gm1 = pick<T>(ph.gm1, ph.f_gm1), gama = pick<T>(ph.gama, ph.f_gama);
   const T igm1 = pick<T>(ph.igm1, ph.f_igm1), eps = pick<T>(ph.weno_eps, ph.f_eps);
+  const T ct = pick<T>(ph.teno_ct, ph.f_teno_ct);
   const T gm1_lo = pick<T>(0.0, ph.f_gm1_lo);
 
   // tile origin: first cell whose flux difference this block writes (d0), across-line origin
@@ -138,7 +139,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
         if (d0 - 1 + m0 + w <= nd - 1) {
           load_point<T, DIR>(P, w + 5, W[5]);
           T fl[5];
-          interface_flux<T, DIR, SCH>(W, gm1, igm1, eps, fl);
+          interface_flux<T, DIR, SCH>(W, gm1, igm1, eps, ct, fl);
 #pragma unroll
           for (int v = 0; v < 5; ++v) sflux[fidx(v, m0 + w, a)] = fl[v];
         }
@@ -203,6 +204,7 @@ __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> 
   const int64_t mline = DIR == 1 ? gidx(g, i, 0, o) : gidx(g, i, o, 0);  // cell 0 of the line
   const T gm1 = pick<T>(ph.gm1, ph.f_gm1), gama = pick<T>(ph.gama, ph.f_gama);
   const T igm1 = pick<T>(ph.igm1, ph.f_igm1), eps = pick<T>(ph.weno_eps, ph.f_eps);
+  const T ct = pick<T>(ph.teno_ct, ph.f_teno_ct);
   const T idd = pick<T>(ph.inv_delta[DIR], ph.f_inv_delta[DIR]);
   const T idd_lo = pick<T>(0.0, ph.f_inv_delta_lo[DIR]), gm1_lo = pick<T>(0.0, ph.f_gm1_lo);
 
@@ -236,7 +238,7 @@ __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> 
       for (int v = 0; v < 5; ++v) rv[v] = res.v[v][mc];
     }
     T F[5];
-    interface_flux<T, DIR, SCH>(W, gm1, igm1, eps, F);
+    interface_flux<T, DIR, SCH>(W, gm1, igm1, eps, ct, F);
     if (c > c0) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
@@ -288,6 +290,7 @@ __device__ __forceinline__ void weno_march_x_tile(const Grid &g, Fields5<const T
   const int pfirst = c0 - 3, plast = c1 + 2;            // points of the segment's stencils
   const T gm1 = pick<T>(ph.gm1, ph.f_gm1), gama = pick<T>(ph.gama, ph.f_gama);
   const T igm1 = pick<T>(ph.igm1, ph.f_igm1), eps = pick<T>(ph.weno_eps, ph.f_eps);
+  const T ct = pick<T>(ph.teno_ct, ph.f_teno_ct);
   const T idd = pick<T>(ph.inv_delta[0], ph.f_inv_delta[0]);
   const T idd_lo = pick<T>(0.0, ph.f_inv_delta_lo[0]), gm1_lo = pick<T>(0.0, ph.f_gm1_lo);
   const int lrow = lane / XC, lcol = lane % XC;  // loader position inside a chunk
@@ -351,7 +354,7 @@ __device__ __forceinline__ void weno_march_x_tile(const Grid &g, Fields5<const T
       if (p >= c0 + 2) {  // window holds points c-3 .. c+2 of interface c = p - 2
         const int c = p - 2;
         T F[5] = {T(0), T(0), T(0), T(0), T(0)};  // rows past n1: defined, never stored
-        if (row_ok) interface_flux<T, 0, SCH>(W, gm1, igm1, eps, F);
+        if (row_ok) interface_flux<T, 0, SCH>(W, gm1, igm1, eps, ct, F);
         if (c > c0) {
           const int cc = c - 1;  // cell finished by this interface
           const int gs = ((cc + 4) / RG) * RG - 4, col = cc - gs;
@@ -423,6 +426,7 @@ static void launch_shape(const Ctx &c, Fields5<const T> q, Fields5<T> r, WenoCfg
 template <typename T, int DIR, bool ACCUM>
 static void launch_variant(const Ctx &c, Fields5<const T> q, Fields5<T> r, WenoCfg w, cudaStream_t s) {
   if (c.plan.conv == OSB_CONV_WENO5Z) launch_shape<T, DIR, ACCUM, SCH_Z>(c, q, r, w, s);
+  else if (c.plan.conv == OSB_CONV_TENO5) launch_shape<T, DIR, ACCUM, SCH_TENO>(c, q, r, w, s);
   else launch_shape<T, DIR, ACCUM, SCH_JS>(c, q, r, w, s);
 }
 
@@ -534,6 +538,8 @@ template <typename T, int DIR, bool ACCUM> static void attr_dir() {
                        (int)tile_smem<T, DIR>());
   cudaFuncSetAttribute(k_weno<T, DIR, ACCUM, SCH_Z>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)tile_smem<T, DIR>());
+  cudaFuncSetAttribute(k_weno<T, DIR, ACCUM, SCH_TENO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)tile_smem<T, DIR>());
 }
 template <typename T> void setup_weno() {
   cudaFuncSetAttribute(k_batch_weno_x<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_x_smem<T, 4>());
@@ -545,6 +551,10 @@ template <typename T> void setup_weno() {
   cudaFuncSetAttribute(k_weno_march_x<T, 4, SCH_Z>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)march_x_smem<T, 4>());
   cudaFuncSetAttribute(k_weno_march_x<T, 8, SCH_Z>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)march_x_smem<T, 8>());
+  cudaFuncSetAttribute(k_weno_march_x<T, 4, SCH_TENO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)march_x_smem<T, 4>());
+  cudaFuncSetAttribute(k_weno_march_x<T, 8, SCH_TENO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)march_x_smem<T, 8>());
   attr_dir<T, 0, false>();
   attr_dir<T, 1, true>();

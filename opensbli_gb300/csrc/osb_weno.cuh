@@ -44,7 +44,7 @@ __device__ __forceinline__ void sqrt_rsqrt(double x, double &s, double &is) {
 }
 
 // Schemes of the nonlinear weights
-enum { SCH_JS = 0, SCH_Z = 1 };
+enum { SCH_JS = 0, SCH_Z = 1, SCH_TENO = 2 };
 
 // One WENO5 side.  f0..f4 are the five stencil values ordered from the far upwind point to the
 // far downwind one (for the right-going side: points i-2..i+2; for the left-going side the caller
@@ -100,6 +100,35 @@ template <typename T, int SCH> __device__ __forceinline__ T weno5_side(T f0, T f
   }
 }
 
+// One TENO5 side with a fixed cut-off (schemes/spatial/teno.py:57-213, 407-465), the same stencil
+// order as weno5_side.  The indicators of the halved values are weno5_side's b1 (central stencil),
+// b0 (downwind) and b2 (upwind); tau = |beta_central - beta_upwind| (the reference's tau5 = |b0 - b2|
+// in its own numbering); alpha_r = (1 + tau/(eps + beta_r))^6, formed as ratios to the largest base
+// so that the sixth power cannot overflow; delta_r = 0 where alpha_r / sum alpha < ct; weights
+// d = 11/20 (central), 2/5 (downwind), 1/20 (upwind), normalised over the kept candidates and applied
+// to the candidate differences from the central one (as weno5_side does).
+template <typename T> __device__ __forceinline__ T teno5_side(T f0, T f1, T f2, T f3, T f4, T eps, T ct) {
+  const T d0 = f1 - f0, d1 = f2 - f1, d2 = f3 - f2, d3 = f4 - f3;
+  const T t0 = d3 - d2, t1 = d2 - d1, t2 = d1 - d0;
+  const T s0 = d3 - T(3) * d2, s1 = d1 + d2, s2 = T(3) * d1 - d0;
+  const T c13 = T(13.0 / 48.0), c14 = T(1.0 / 16.0);
+  const T bd = c13 * t0 * t0 + c14 * s0 * s0;  // downwind
+  const T bc = c13 * t1 * t1 + c14 * s1 * s1;  // central
+  const T bu = c13 * t2 * t2 + c14 * s2 * s2;  // upwind
+  const T tau = abs_t(bc - bu);
+  const T mc = T(1) + tau * rcp_t(eps + bc), md = T(1) + tau * rcp_t(eps + bd), mu = T(1) + tau * rcp_t(eps + bu);
+  const T im = rcp_t(max_t(mc, max_t(md, mu)));
+  const T nc = mc * im, nd = md * im, nu = mu * im;
+  const T qc = (nc * nc) * (nc * nc) * (nc * nc), qd = (nd * nd) * (nd * nd) * (nd * nd),
+          qu = (nu * nu) * (nu * nu) * (nu * nu);
+  const T iq = rcp_t(qc + qd + qu);
+  const T wc = ct > qc * iq ? T(0) : T(11.0 / 20.0);
+  const T wd = ct > qd * iq ? T(0) : T(2.0 / 5.0);
+  const T wu = ct > qu * iq ? T(0) : T(1.0 / 20.0);
+  const T p1 = T(0.5) * f2 + T(1.0 / 12.0) * d1 + T(1.0 / 6.0) * d2;
+  return p1 + (T(-1.0 / 12.0) * wd * (t0 - t1) + T(1.0 / 6.0) * wu * (t2 - t1)) * rcp_t(wc + wd + wu);
+}
+
 // Per-point window entry: conserved vector Q, u_D, a, p.  The physical flux along D,
 // F = (Q_{1+D}, Q_{1+c} u_D + delta_cD p, (p + Q_4) u_D), is folded into the projections below.
 template <typename T> struct WPt {
@@ -139,7 +168,7 @@ __device__ __forceinline__ void point_prims(const T (&r)[5], T gm1, T gm1_lo, T 
 // F_{i+1/2} = F_i + (F_{i+1/2} - F_i) is rounded once.
 template <int D, int SCH>
 __device__ __forceinline__ void interface_flux_delta(const WPt<float> (&W)[6], const float gm1, const float igm1,
-                                                     const float eps, float out[5]) {
+                                                     const float eps, const float ct, float out[5]) {
   using T = float;
   constexpr int E1 = (D + 1) % 3, E2 = (D + 2) % 3;
   constexpr int e1 = 3 - E1 - D, e2 = 3 - E2 - D;
@@ -177,8 +206,12 @@ __device__ __forceinline__ void interface_flux_delta(const WPt<float> (&W)[6], c
       fp[t] = cf[t] + lam * cs[t];
       fm[t] = cf[t] - lam * cs[t];
     }
-    return weno5_side<T, SCH>(fp[0], fp[1], fp[2], fp[3], fp[4], eps) +
-           weno5_side<T, SCH>(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
+    if constexpr (SCH == SCH_TENO)
+      return teno5_side<T>(fp[0], fp[1], fp[2], fp[3], fp[4], eps, ct) +
+             teno5_side<T>(fm[5], fm[4], fm[3], fm[2], fm[1], eps, ct);
+    else
+      return weno5_side<T, SCH>(fp[0], fp[1], fp[2], fp[3], fp[4], eps) +
+             weno5_side<T, SCH>(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
   };
   // physical flux component v of point t: (Q_{1+D}, Q_{1+c} u_D + delta_cD p, (Q_4 + p) u_D)
   auto flux = [&](int t, int v) -> T {
@@ -260,11 +293,12 @@ __device__ __forceinline__ void interface_flux_delta(const WPt<float> (&W)[6], c
 }
 
 // Characteristic flux at the interface between window points 2 and 3 (points i and i+1).
+// ct: the TENO cut-off (unused by the WENO schemes).
 template <typename T, int D, int SCH>
 __device__ __forceinline__ void interface_flux(const WPt<T> (&W)[6], const T gm1, const T igm1, const T eps,
-                                               T out[5]) {
+                                               const T ct, T out[5]) {
   if constexpr (sizeof(T) == 4) {
-    interface_flux_delta<D, SCH>(W, gm1, igm1, eps, out);
+    interface_flux_delta<D, SCH>(W, gm1, igm1, eps, ct, out);
     return;
   }
   constexpr int E1 = (D + 1) % 3, E2 = (D + 2) % 3;  // the two tangential axes (shear rows)
@@ -304,8 +338,12 @@ __device__ __forceinline__ void interface_flux(const WPt<T> (&W)[6], const T gm1
       fp[t] = cf[t] + lam * cs[t];
       fm[t] = cf[t] - lam * cs[t];
     }
-    return weno5_side<T, SCH>(fp[0], fp[1], fp[2], fp[3], fp[4], eps) +
-           weno5_side<T, SCH>(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
+    if constexpr (SCH == SCH_TENO)
+      return teno5_side<T>(fp[0], fp[1], fp[2], fp[3], fp[4], eps, ct) +
+             teno5_side<T>(fm[5], fm[4], fm[3], fm[2], fm[1], eps, ct);
+    else
+      return weno5_side<T, SCH>(fp[0], fp[1], fp[2], fp[3], fp[4], eps) +
+             weno5_side<T, SCH>(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
   };
 
   // ---- shear rows: LEV_r . X = (s/rho)(u_e X_0 - X_{1+e}); for X = F: X_0 = Q_{1+D}, X_{1+e} = Q_{1+e} u_D

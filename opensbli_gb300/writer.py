@@ -102,12 +102,31 @@ class GB300Writer:
             raise NotImplementedError("GB300Writer lowers 2D and 3D blocks (got ndim=%d)" % ndim)
         skew = self._kernels("Convective terms group")
         weno = self._kernels("LLFWeno_reconstruction_")
-        if self._kernels("LLFTeno_reconstruction_"):
-            raise NotImplementedError("TENO reconstruction on a 3D block is not lowered")
+        teno = self._kernels("LLFTeno_reconstruction_")
         visc = self._kernels("Viscous")
-        if bool(skew) == bool(weno):
-            raise NotImplementedError("expected exactly one convective discretisation (Central skew or LLFWeno)")
-        if skew:
+        if [bool(skew), bool(weno), bool(teno)].count(True) != 1:
+            raise NotImplementedError("expected exactly one convective discretisation (Central skew, LLFWeno or "
+                                      "LLFTeno)")
+        if teno:
+            # LLFTeno(5) with a fixed cut-off TENO_CT (teno.py:407-465); the adaptive cut-off needs the
+            # Ducros sensor, which this build evaluates on 2D blocks only
+            conv = "teno5"
+            if len(teno) != 3:
+                raise NotImplementedError("one LLFTeno reconstruction kernel per direction expected")
+            for k in teno:
+                lhs = self._lhs_names(k)
+                if not {"delta_0", "delta_1", "delta_2", "inv_omega_sum"} <= lhs:
+                    raise NotImplementedError("TENO5 with a cut-off expected in %s" % k.computation_name)
+                if "TENO_CT" in lhs:
+                    raise NotImplementedError("adaptive TENO (Ducros sensor) on a 3D block is not lowered")
+                if self._max_offset([k]) != 3:
+                    raise NotImplementedError("5th-order stencil expected in %s" % k.computation_name)
+                avg = [e for e in k.equations if str(e.lhs).endswith("_rho") and str(e.lhs).startswith("AVG_")]
+                if not avg or "sqrt" not in str(avg[0].rhs):
+                    raise NotImplementedError("Roe averaging expected in %s" % k.computation_name)
+            if not self._kernels("LLFTeno Residual"):
+                raise NotImplementedError("LLFTeno residual kernel missing")
+        elif skew:
             conv = "central_skew"
             if len(skew) != 3 or self._max_offset(self._kernels("Convective CD")) != 2:
                 raise NotImplementedError("Central(4) skew-symmetric convective terms expected")
@@ -136,7 +155,7 @@ class GB300Writer:
             raise NotImplementedError("Central(4) viscous terms expected")
         # constituent relations: u_i, p, T (and a for WENO), constant viscosity
         base = {re.sub(r"_B0$", "", n) for n in names if n.startswith("CR")}
-        need = {"CRu0", "CRu1", "CRu2", "CRp"} | ({"CRT"} if visc else set()) | ({"CRa"} if weno else set())
+        need = {"CRu0", "CRu1", "CRu2", "CRp"} | ({"CRT"} if visc else set()) | ({"CRa"} if weno or teno else set())
         if not need <= base or base - need - {"CRT", "CRa"}:
             raise NotImplementedError("unsupported constituent relations: %s" % sorted(base))
         # RK3 coefficients from the stage kernels (rk_sbli.py:102-124)
@@ -361,6 +380,8 @@ class GB300Writer:
                   Re=float(env.get("Re", p.Re)), Pr=float(env.get("Pr", p.Pr)),
                   dt=float(env["dt"]) if "dt" in env else p.dt,
                   niter=int(env["niter"]) if "niter" in env else p.niter)
+        if nd == 3 and p.conv == "teno5":
+            kw.update(teno_eps=float(env.get("eps", p.teno_eps)), teno_ct=float(env.get("TENO_CT", p.teno_ct)))
         if nd == 2:
             kw.update(Twall=float(env.get("Twall", p.Twall)), SuthT=float(env.get("SuthT", p.SuthT)),
                       RefT=float(env.get("RefT", p.RefT)), teno_eps=float(env.get("eps", p.teno_eps)),

@@ -28,6 +28,7 @@ CASES = {
     "tgsym_central": "ref:apps/taylor_green_vortex/TGsym/TGsym.py",
     "tgv_weno": "tgv_weno.py",
     "tgv_wenoz": "tgv_wenoz.py",
+    "tgv_teno": "tgv_teno.py",
     "katzer_teno": "katzer_teno.py",
     "katzer_adaptive": "ref:apps/katzer_SBLI/katzer_SBLI.py",
 }

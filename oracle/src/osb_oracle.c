@@ -356,10 +356,26 @@ static double weno5_minus(const double g[5], int z) {
          a2 * inv * (-(1.0 / 12.0) * f1 + (5.0 / 12.0) * f2 + (1.0 / 6.0) * f3);
 }
 
-/* TENO5 (schemes/spatial/teno.py:57-213, 407-465) with fixed cut-off C_T: smoothness indicators
- * as for WENO5 (full Jiang-Shu form, teno.py:159-173), alpha_r = (1 + tau5/(eps + beta_r))^6 with
- * tau5 = |beta_0 - beta_2|, delta_r = 0 if alpha_r/sum(alpha) < C_T else 1,
- * omega_r = d_r delta_r / sum(d delta), d = (0.55, 0.4, 0.05)... (restated in the 2D path). */
+/* TENO5 (schemes/spatial/teno.py:57-213, 407-465) with fixed cut-off C_T on one side of the split
+ * flux, f[0..4] ordered from the far upwind point to the far downwind one: smoothness indicators of
+ * the halved values (the splitting's 1/2, full Jiang-Shu form, teno.py:159-173), alpha_r =
+ * (1 + tau5/(eps + beta_r))^6 with tau5 = |beta_0 - beta_2|, delta_r = 0 if alpha_r/sum(alpha) < C_T
+ * else 1, omega_r = d_r delta_r / sum(d delta) with d = (0.55, 0.4, 0.05) for the central, downwind
+ * and upwind candidates (teno.py:133; the same restatement as the 2D path's teno5_plus). */
+static double teno5_side(const double f[5], double eps, double CT) {
+  const double h0 = 0.5 * f[0], h1 = 0.5 * f[1], h2 = 0.5 * f[2], h3 = 0.5 * f[3], h4 = 0.5 * f[4];
+  const double b0 = 0.25 * (h1 - h3) * (h1 - h3) + (13.0 / 12.0) * (h1 - 2 * h2 + h3) * (h1 - 2 * h2 + h3);
+  const double b1 = (13.0 / 12.0) * (h2 - 2 * h3 + h4) * (h2 - 2 * h3 + h4) + 0.25 * (3 * h2 - 4 * h3 + h4) * (3 * h2 - 4 * h3 + h4);
+  const double b2 = 0.25 * (h0 - 4 * h1 + 3 * h2) * (h0 - 4 * h1 + 3 * h2) + (13.0 / 12.0) * (h0 - 2 * h1 + h2) * (h0 - 2 * h1 + h2);
+  const double tau = fabs(b0 - b2);
+  const double a0 = pow(1 + tau / (eps + b0), 6), a1 = pow(1 + tau / (eps + b1), 6), a2 = pow(1 + tau / (eps + b2), 6);
+  const double inv = 1.0 / (a0 + a1 + a2);
+  const double d0 = CT > a0 * inv ? 0.0 : 1.0, d1 = CT > a1 * inv ? 0.0 : 1.0, d2 = CT > a2 * inv ? 0.0 : 1.0;
+  const double iw = 1.0 / (0.55 * d0 + 0.4 * d1 + 0.05 * d2);
+  return 0.55 * d0 * iw * (-(1.0 / 12.0) * f[1] + (5.0 / 12.0) * f[2] + (1.0 / 6.0) * f[3]) +
+         0.4 * d1 * iw * ((1.0 / 6.0) * f[2] + (5.0 / 12.0) * f[3] - (1.0 / 12.0) * f[4]) +
+         0.05 * d2 * iw * ((1.0 / 6.0) * f[0] - (7.0 / 12.0) * f[1] + (11.0 / 12.0) * f[2]);
+}
 
 static void eigensystem(int dir, double rho, double u0, double u1, double u2, double a, double g, double L[5][5],
                         double R[5][5]) {
@@ -461,7 +477,12 @@ static void residual_weno(st_t *s) {
           fp[t] = CF[r][t] + lam[r] * CS[r][t];
           fm[t] = CF[r][t + 1] - lam[r] * CS[r][t + 1];
         }
-        rec[r] = weno5_plus(fp, s->c.conv == OSBO_CONV_WENO5Z) + weno5_minus(fm, s->c.conv == OSBO_CONV_WENO5Z);
+        if (s->c.conv == OSBO_CONV_TENO5) {
+          const double fmr[5] = {fm[4], fm[3], fm[2], fm[1], fm[0]};  /* points i+3 .. i-1 */
+          rec[r] = teno5_side(fp, s->c.teno_eps, s->c.teno_ct) + teno5_side(fmr, s->c.teno_eps, s->c.teno_ct);
+        } else {
+          rec[r] = weno5_plus(fp, s->c.conv == OSBO_CONV_WENO5Z) + weno5_minus(fm, s->c.conv == OSBO_CONV_WENO5Z);
+        }
       }
       for (int v = 0; v < 5; ++v) {
         double fl = 0;

@@ -37,10 +37,11 @@ def residual_with(plan, q0, kind, seg):
     return r
 
 
+@pytest.mark.parametrize("conv", ["weno5js", "teno5"])
 @pytest.mark.parametrize("n", [(24, 24, 24), (40, 37, 29)])
 @pytest.mark.parametrize("kind,seg", SHAPES)
-def test_weno_shapes_fp64_match_oracle(n, kind, seg):
-    plan = tgv_plan(n, conv="weno5js", Minf=1.25)
+def test_weno_shapes_fp64_match_oracle(n, kind, seg, conv):
+    plan = tgv_plan(n, conv=conv, Minf=1.25)
     cfg = oracle_cfg(plan)
     q0 = O.tgv_init(cfg)
     r_or = O.residual(cfg, q0)
