@@ -50,7 +50,7 @@ def test_query_layout_fp64_and_mixed():
 
 @pytest.mark.parametrize("change,code", [
     (dict(n=(4, 64, 64)), -1),                    # too small
-    (dict(conv="teno5"), -2),                     # TENO on a 3D block
+    (dict(conv="teno5", teno_adaptive=True), -2),  # adaptive TENO on a 3D block
     (dict(visc="sutherland"), -2),
     (dict(rk="ls_rk3"), -2),
     (dict(bc=(("periodic", "symmetry"),) + (("periodic", "periodic"),) * 2), -1),
