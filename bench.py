@@ -36,7 +36,7 @@ ALG_BYTES_STAGE = {"mixed": 5 * (2 * 4 + 2 * 8), "fp64": 5 * (2 * 8 + 2 * 8)}
 
 # DRAM bytes per cell per launch measured by ncu for the mixed WENO TGV kernels at 192^3 (state larger
 # than L2), used to scale the roofline's traffic figure to the benchmark's grid
-DRAM_BYTES_PER_CELL_WENO_MIXED = {"weno_x": 56.1, "weno_y": 57.8, "weno_z": 57.7, "central_rk": 144.8}
+DRAM_BYTES_PER_CELL_WENO_MIXED = {"weno_x": 45.7, "weno_y": 57.9, "weno_z": 57.8, "central_rk": 147.3}
 
 
 def load_peaks():
