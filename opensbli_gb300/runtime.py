@@ -285,6 +285,48 @@ class Solver:
         q.record_stream(self.stream)
         self._out()
 
+    def state_names(self):
+        """OPS dat names of the conserved variables on block 0 (rho_B0, rhou0_B0, ...)."""
+        nv = self.layout.nvar
+        return ["rho_B0", "rhou0_B0", "rhou1_B0", "rhoE_B0"] if nv == 4 else \
+            ["rho_B0", "rhou0_B0", "rhou1_B0", "rhou2_B0", "rhoE_B0"]
+
+    def write_ops_hdf5(self, path, extra=None, halo=5, block_name="opensbliblock00"):
+        """Write the FP64 state as an OPS block file (the layout of the generated code's
+        ops_fetch_block_hdf5_file / ops_fetch_dat_hdf5_file calls): one dat per conserved variable, plus
+        `extra` = {dat name: FP64 interior array} (coordinates, sensors).  Halos are `halo` deep on
+        every side: periodic axes carry the periodic images, other axes zeros (the boundary kernels
+        recompute halos on restart)."""
+        import numpy as np
+        from . import hdf5
+        q = self.state64().cpu().numpy()
+        arrays = {n: q[v] for v, n in enumerate(self.state_names())}
+        for k, a in (extra or {}).items():
+            arrays[k] = np.asarray(a, dtype=np.float64)
+        nd = self.plan.ndim
+        modes = [("wrap" if self.plan.bc[d][0] == "periodic" else "constant") for d in range(nd)][::-1]
+        padded = []
+        for a in arrays.values():
+            if a.shape != self.shape:
+                raise ValueError("extra dat of shape %s, the block is %s" % (a.shape, self.shape))
+            for ax, m in enumerate(modes):
+                w = [(0, 0)] * nd
+                w[ax] = (halo, halo)
+                a = np.pad(a, w, mode=m)
+            padded.append(a)
+        hdf5.write_ops_state(path, list(arrays), padded, tuple(self.plan.n[:nd]), halo, block_name)
+
+    def read_ops_hdf5(self, path, block_name="opensbliblock00"):
+        """Set the state from an OPS block file holding the conserved dats (as written by
+        write_ops_hdf5 or by the generated code); the halos in the file are not used."""
+        import numpy as np
+        from . import hdf5
+        arrays, halo, npts = hdf5.read_ops_state(path, self.state_names(), block_name)
+        if tuple(npts) != tuple(self.plan.n[:self.plan.ndim]):
+            raise ValueError("%s holds a %s block, the plan is %s" % (path, npts, self.plan.n[:self.plan.ndim]))
+        sl = (slice(halo, -halo),) * self.plan.ndim if halo else (slice(None),) * self.plan.ndim
+        self.set_state64(np.stack([a[sl] for a in arrays]))
+
     def set_coordinate(self, x1, h=4):
         """2D blocks stretched in x1: the x1 coordinate, FP64 [n1+2h][n0+2h]; evaluates the metrics."""
         x = torch.as_tensor(x1, dtype=torch.float64).to(self.device).contiguous()

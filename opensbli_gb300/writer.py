@@ -464,23 +464,96 @@ class GB300Writer:
         from .runtime import Solver
         return Solver(self.plan, device=device)
 
-    def run(self, niter=None, dt=None, device=None, monitor=None):
+    def io_requests(self):
+        """The block's HDF5 IO objects (core/io_hdf5.py:19-132) as plain data: a list of
+        {"kind": "write"|"read", "arrays": [dat names], "every": N or None, "at_end": bool,
+        "name": file name or None}."""
+        out, seen = [], set()
+        # the IO objects sit in the algorithm's program where the generated code calls them
+        for io in self.components:
+            if type(io).__name__ != "iohdf5" or id(io) in seen:
+                continue
+            seen.add(id(io))
+            kw = getattr(io, "kwargs", {}) or {}
+            places = getattr(io, "algorithm_place", []) or []
+            every = [getattr(p, "frequency", None) for p in places if type(p).__name__ == "InTheSimulation"]
+            r = {"kind": kw.get("iotype", "write"), "arrays": [str(a) for a in io.arrays],
+                 "every": int(every[0]) if every and every[0] else None,
+                 "at_end": any(type(p).__name__ == "AfterSimulationEnds" for p in places),
+                 "name": kw.get("name") if kw.get("iotype", "write") == "write" else kw.get("filename", "data.h5")}
+            if r not in out:  # the program lists an IO object once per place it acts at
+                out.append(r)
+        return out
+
+    def _output_dats(self, s, names, coords):
+        """The dats of `names` this library can produce, as FP64 interior arrays: conserved variables
+        (written by Solver.write_ops_hdf5 itself), x0/x1 of the grid, and on 2D blocks with adaptive TENO
+        the cut-off field TENO_B0.  Returns (extra dats, names it cannot produce)."""
+        extra, skipped = {}, []
+        conserved = set(s.state_names())
+        for n in names:
+            if n in conserved:
+                continue
+            base = n[:-3] if n.endswith("_B0") else n
+            if base in coords:
+                extra[n] = coords[base]
+            elif n == "TENO_B0" and self.plan.teno_adaptive:
+                extra[n] = s.teno_cutoff().cpu().numpy()
+            else:
+                skipped.append(n)
+        return extra, skipped
+
+    def run(self, niter=None, dt=None, device=None, monitor=None, output_dir=None):
         """Initialise from the script's initial condition and advance niter steps (defaults: the
         script's niter and dt).  The algorithm's SimulationMonitor, if it has one (or `monitor`, an
         opensbli_gb300.monitor.SimulationMonitor), samples and prints where the generated code would.
+        With `output_dir`, the script's HDF5 IO is carried out there as the generated code does it:
+        read requests (iotype "read") set the state from their file before the first step; write
+        requests write opensbli_output_%06d.h5 every `save_every` steps and opensbli_output.h5 (or the
+        requested name) after the last, in the OPS block layout (opensbli_gb300.hdf5).  Dats the
+        library does not hold are left out and listed in `self.skipped_output`.
         Returns the Solver, whose state64() gives the FP64 state."""
+        import os
         from . import monitor as mon
         s = self.solver(device)
+        coords = {}
         if self.plan.ndim == 2:
             f = self.initial_fields(halo=4)
             s.set_coordinate(f["x1"], 4)
             s.set_state64_padded(np.stack([f[v] for v in self.state_names()]), 4)
+            coords = {k: f[k][4:-4, 4:-4] for k in ("x0", "x1") if k in f}
         else:
             s.set_state64(self.initial_state())
+        ios = self.io_requests() if output_dir is not None else []
+        for r in ios:
+            if r["kind"] == "read":
+                s.read_ops_hdf5(os.path.join(output_dir, r["name"]))
         if monitor is None and getattr(self.algorithm, "simulation_monitor", None) is not None:
             monitor = mon.SimulationMonitor.from_reference(self.algorithm.simulation_monitor)
-        mon.run(s, int(niter if niter is not None else self.plan.niter), float(dt if dt is not None else self.plan.dt),
-                monitor)
+        n = int(niter if niter is not None else self.plan.niter)
+        step = float(dt if dt is not None else self.plan.dt)
+        writes = [r for r in ios if r["kind"] == "write"]
+        self.skipped_output = []
+
+        def write(r, fname):
+            extra, skipped = self._output_dats(s, r["arrays"], coords)
+            self.skipped_output += [x for x in skipped if x not in self.skipped_output]
+            s.write_ops_hdf5(os.path.join(output_dir, fname), extra=extra)
+
+        # chunks end where a periodic write is due (generated code: fmod(iter + 1, save_every) == 0)
+        ends = sorted({k for r in writes if r["every"] for k in range(r["every"], n + 1, r["every"])} | {n})
+        it = 0
+        for e in ends:
+            if e > it:
+                mon.run(s, e - it, step, monitor, t0_iteration=it)
+                it = e
+            for r in writes:
+                if r["every"] and e % r["every"] == 0 and e > 0:
+                    write(r, "opensbli_output_%06d.h5" % e)
+        for r in writes:
+            if r["at_end"]:
+                name = r["name"] or "opensbli_output"
+                write(r, name if name.endswith(".h5") else name + ".h5")
         if monitor is not None:
             monitor.close()
         return s

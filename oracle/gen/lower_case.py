@@ -74,6 +74,8 @@ def lower(case, ref, out, n=None):
         np.save(os.path.join(out, "ic.npy"), w.initial_state())
     with open(os.path.join(out, "constants.json"), "w") as f:
         json.dump({"constants": consts, "values": vals}, f)
+    with open(os.path.join(out, "io.json"), "w") as f:
+        json.dump(w.io_requests(), f)
     return w.plan
 
 

@@ -84,6 +84,15 @@ def test_writer_lowers_reference_script(case, tmp_path):
     g = golden_plan(case)
     assert p.replace(kernels=[]) == g.replace(kernels=[])
     assert sorted(p.kernels) == sorted(g.kernels)
+    # the script's HDF5 output requests, as GB300Writer.run carries them out
+    import json
+    io = json.load(open(tmp_path / "io.json"))
+    writes = [r for r in io if r["kind"] == "write"]
+    assert len(writes) == 1 and writes[0]["at_end"]
+    conserved = ["rho_B0", "rhou0_B0", "rhou1_B0"] + (["rhou2_B0"] if p.ndim == 3 else []) + ["rhoE_B0"]
+    assert writes[0]["arrays"][:len(conserved)] == conserved
+    if case == "katzer_adaptive":
+        assert writes[0]["arrays"][len(conserved):] == ["x0_B0", "x1_B0", "D11_B0", "TENO_B0"]
     ic = np.load(tmp_path / "ic.npy")
     if p.ndim == 2:
         assert ic.shape == (4, p.n[1] + 8, p.n[0] + 8)  # 4-point halo: the initialisation kernel fills halos
