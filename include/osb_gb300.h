@@ -37,6 +37,7 @@ extern "C" {
 #define OSB_CONV_WENO5JS 1
 #define OSB_CONV_TENO5 2
 #define OSB_CONV_WENO5Z 3   /* WENO5-Z weights (weno.py:283-331), 3D blocks */
+#define OSB_CONV_TENO6 4    /* LLFTeno(6), fixed cut-off (teno.py:94-192, 216-234), 3D blocks */
 /* viscous terms: none, constant viscosity (taylor_green_vortex.py:18-19), Sutherland (katzer_SBLI.py:25) */
 #define OSB_VISC_NONE 0
 #define OSB_VISC_CONST 1

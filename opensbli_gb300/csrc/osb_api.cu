@@ -34,7 +34,8 @@ int cuda_err(osb_ctx *c, cudaError_t e, const char *where) {
 
 // the characteristic-flux schemes of the 3D kernels (WENO5-JS, WENO5-Z, TENO5)
 bool char_fluxes(const osb_plan_desc &p) {
-  return p.conv == OSB_CONV_WENO5JS || p.conv == OSB_CONV_WENO5Z || p.conv == OSB_CONV_TENO5;
+  return p.conv == OSB_CONV_WENO5JS || p.conv == OSB_CONV_WENO5Z || p.conv == OSB_CONV_TENO5 ||
+         p.conv == OSB_CONV_TENO6;
 }
 
 int validate(const osb_plan_desc *p, char *why, size_t n) {
@@ -83,7 +84,7 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
     }
   }
   if (p->conv != OSB_CONV_CENTRAL_SKEW && p->conv != OSB_CONV_WENO5JS && p->conv != OSB_CONV_WENO5Z &&
-      p->conv != OSB_CONV_TENO5) {
+      p->conv != OSB_CONV_TENO5 && p->conv != OSB_CONV_TENO6) {
     snprintf(why, n, "convective scheme %d not supported on 3D blocks", p->conv);
     return OSB_EUNSUPPORTED;
   }
@@ -559,7 +560,8 @@ Phys plan_phys(const osb_plan_desc *plan) {
   ph.Re = plan->Re;
   ph.Pr = plan->Pr;
   for (int d = 0; d < 3; ++d) ph.inv_delta[d] = 1.0 / plan->delta[d];
-  ph.weno_eps = plan->conv == OSB_CONV_TENO5 ? plan->teno_eps : plan->weno_eps > 0 ? plan->weno_eps : 1e-6;
+  ph.weno_eps = (plan->conv == OSB_CONV_TENO5 || plan->conv == OSB_CONV_TENO6) ? plan->teno_eps
+                : plan->weno_eps > 0 ? plan->weno_eps : 1e-6;
   ph.teno_ct = plan->teno_ct;
   ph.f_teno_ct = (float)plan->teno_ct;
   ph.gm1 = plan->gama - 1.0;

@@ -427,6 +427,7 @@ template <typename T, int DIR, bool ACCUM>
 static void launch_variant(const Ctx &c, Fields5<const T> q, Fields5<T> r, WenoCfg w, cudaStream_t s) {
   if (c.plan.conv == OSB_CONV_WENO5Z) launch_shape<T, DIR, ACCUM, SCH_Z>(c, q, r, w, s);
   else if (c.plan.conv == OSB_CONV_TENO5) launch_shape<T, DIR, ACCUM, SCH_TENO>(c, q, r, w, s);
+  else if (c.plan.conv == OSB_CONV_TENO6) launch_shape<T, DIR, ACCUM, SCH_TENO6>(c, q, r, w, s);
   else launch_shape<T, DIR, ACCUM, SCH_JS>(c, q, r, w, s);
 }
 
@@ -540,6 +541,8 @@ template <typename T, int DIR, bool ACCUM> static void attr_dir() {
                        (int)tile_smem<T, DIR>());
   cudaFuncSetAttribute(k_weno<T, DIR, ACCUM, SCH_TENO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)tile_smem<T, DIR>());
+  cudaFuncSetAttribute(k_weno<T, DIR, ACCUM, SCH_TENO6>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)tile_smem<T, DIR>());
 }
 template <typename T> void setup_weno() {
   cudaFuncSetAttribute(k_batch_weno_x<T, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)march_x_smem<T, 4>());
@@ -555,6 +558,10 @@ template <typename T> void setup_weno() {
   cudaFuncSetAttribute(k_weno_march_x<T, 4, SCH_TENO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)march_x_smem<T, 4>());
   cudaFuncSetAttribute(k_weno_march_x<T, 8, SCH_TENO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)march_x_smem<T, 8>());
+  cudaFuncSetAttribute(k_weno_march_x<T, 4, SCH_TENO6>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)march_x_smem<T, 4>());
+  cudaFuncSetAttribute(k_weno_march_x<T, 8, SCH_TENO6>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)march_x_smem<T, 8>());
   attr_dir<T, 0, false>();
   attr_dir<T, 1, true>();

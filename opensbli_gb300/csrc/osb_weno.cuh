@@ -44,7 +44,7 @@ __device__ __forceinline__ void sqrt_rsqrt(double x, double &s, double &is) {
 }
 
 // Schemes of the nonlinear weights
-enum { SCH_JS = 0, SCH_Z = 1, SCH_TENO = 2 };
+enum { SCH_JS = 0, SCH_Z = 1, SCH_TENO = 2, SCH_TENO6 = 3 };
 
 // One WENO5 side.  f0..f4 are the five stencil values ordered from the far upwind point to the
 // far downwind one (for the right-going side: points i-2..i+2; for the left-going side the caller
@@ -129,6 +129,44 @@ template <typename T> __device__ __forceinline__ T teno5_side(T f0, T f1, T f2, 
   return p1 + (T(-1.0 / 12.0) * wd * (t0 - t1) + T(1.0 / 6.0) * wu * (t2 - t1)) * rcp_t(wc + wd + wu);
 }
 
+// One TENO6 side with a fixed cut-off (schemes/spatial/teno.py:94-192, 216-234, 407-465).  f0..f5
+// run from the far upwind point to one past the far downwind one (+ side: points i-2..i+3; - side:
+// i+3..i-2).  Candidates: the three TENO5 stencils and f2..f5; indicators of the halved values, the
+// fourth one (f2..f5) as the reference generates it: 1/36 A^2 + 13/12 B^2 plus, on the + side, the linear
+// third-difference term 781/720 C and on the - side 781/720 C^2 (teno.py:175-176 vs 183-185), with A, B,
+// C its first-, second- and third-derivative combinations; tau6 = |b_c/6 - 2 b_d/3 + b_u/6 - b_4|;
+// alpha_r = (1 + tau6/(eps + beta_r))^6 as ratios to the largest base (in magnitude: the + side's
+// fourth indicator may be negative); weights 231/500, 3/10, 27/500, 23/125 for the central, downwind,
+// upwind and four-point candidates, applied to candidate differences from the central one.
+template <typename T>
+__device__ __forceinline__ T teno6_side(T f0, T f1, T f2, T f3, T f4, T f5, bool plus, T eps, T ct) {
+  const T d0 = f1 - f0, d1 = f2 - f1, d2 = f3 - f2, d3 = f4 - f3, d4 = f5 - f4;
+  const T t0 = d3 - d2, t1 = d2 - d1, t2 = d1 - d0;
+  const T s0 = d3 - T(3) * d2, s1 = d1 + d2, s2 = T(3) * d1 - d0;
+  const T c13 = T(13.0 / 48.0), c14 = T(1.0 / 16.0);
+  const T bd = c13 * t0 * t0 + c14 * s0 * s0;
+  const T bc = c13 * t1 * t1 + c14 * s1 * s1;
+  const T bu = c13 * t2 * t2 + c14 * s2 * s2;
+  const T A = T(11) * d2 - T(7) * d3 + T(2) * d4, B = T(3) * d3 - T(2) * d2 - d4, C = d2 - T(2) * d3 + d4;
+  const T b4 = T(1.0 / 144.0) * A * A + c13 * B * B + (plus ? T(781.0 / 1440.0) * C : T(781.0 / 2880.0) * C * C);
+  const T tau = abs_t(T(1.0 / 6.0) * (bc + bu) - T(2.0 / 3.0) * bd - b4);
+  const T mc = T(1) + tau * rcp_t(eps + bc), md = T(1) + tau * rcp_t(eps + bd), mu = T(1) + tau * rcp_t(eps + bu),
+          m4 = T(1) + tau * rcp_t(eps + b4);
+  const T im = rcp_t(max_t(max_t(abs_t(mc), abs_t(md)), max_t(abs_t(mu), abs_t(m4))));
+  const T nc = mc * im, nd = md * im, nu = mu * im, n4 = m4 * im;
+  const T qc = (nc * nc) * (nc * nc) * (nc * nc), qd = (nd * nd) * (nd * nd) * (nd * nd),
+          qu = (nu * nu) * (nu * nu) * (nu * nu), q4 = (n4 * n4) * (n4 * n4) * (n4 * n4);
+  const T iq = rcp_t((qc + qd) + (qu + q4));
+  const T wc = ct > qc * iq ? T(0) : T(231.0 / 500.0);
+  const T wd = ct > qd * iq ? T(0) : T(3.0 / 10.0);
+  const T wu = ct > qu * iq ? T(0) : T(27.0 / 500.0);
+  const T w4 = ct > q4 * iq ? T(0) : T(23.0 / 125.0);
+  const T p1 = T(0.5) * f2 + T(1.0 / 12.0) * d1 + T(1.0 / 6.0) * d2;
+  const T num = T(-1.0 / 12.0) * wd * (t0 - t1) + T(1.0 / 6.0) * wu * (t2 - t1) +
+                T(1.0 / 24.0) * w4 * (T(5) * d2 - T(2) * d1 - T(4) * d3 + d4);
+  return p1 + num * rcp_t((wc + wd) + (wu + w4));
+}
+
 // Per-point window entry: conserved vector Q, u_D, a, p.  The physical flux along D,
 // F = (Q_{1+D}, Q_{1+c} u_D + delta_cD p, (p + Q_4) u_D), is folded into the projections below.
 template <typename T> struct WPt {
@@ -206,7 +244,10 @@ __device__ __forceinline__ void interface_flux_delta(const WPt<float> (&W)[6], c
       fp[t] = cf[t] + lam * cs[t];
       fm[t] = cf[t] - lam * cs[t];
     }
-    if constexpr (SCH == SCH_TENO)
+    if constexpr (SCH == SCH_TENO6)
+      return teno6_side<T>(fp[0], fp[1], fp[2], fp[3], fp[4], fp[5], true, eps, ct) +
+             teno6_side<T>(fm[5], fm[4], fm[3], fm[2], fm[1], fm[0], false, eps, ct);
+    else if constexpr (SCH == SCH_TENO)
       return teno5_side<T>(fp[0], fp[1], fp[2], fp[3], fp[4], eps, ct) +
              teno5_side<T>(fm[5], fm[4], fm[3], fm[2], fm[1], eps, ct);
     else
@@ -338,7 +379,10 @@ __device__ __forceinline__ void interface_flux(const WPt<T> (&W)[6], const T gm1
       fp[t] = cf[t] + lam * cs[t];
       fm[t] = cf[t] - lam * cs[t];
     }
-    if constexpr (SCH == SCH_TENO)
+    if constexpr (SCH == SCH_TENO6)
+      return teno6_side<T>(fp[0], fp[1], fp[2], fp[3], fp[4], fp[5], true, eps, ct) +
+             teno6_side<T>(fm[5], fm[4], fm[3], fm[2], fm[1], fm[0], false, eps, ct);
+    else if constexpr (SCH == SCH_TENO)
       return teno5_side<T>(fp[0], fp[1], fp[2], fp[3], fp[4], eps, ct) +
              teno5_side<T>(fm[5], fm[4], fm[3], fm[2], fm[1], eps, ct);
     else

@@ -40,7 +40,7 @@ class Plan:
     ndim: int = 3
     n: Tuple[int, int, int] = (64, 64, 64)
     delta: Tuple[float, float, float] = (2 * math.pi / 64,) * 3
-    conv: str = "central_skew"      # central_skew | weno5js | weno5z | teno5
+    conv: str = "central_skew"      # central_skew | weno5js | weno5z | teno5 | teno6
     visc: str = "const"             # none | const | sutherland
     rk: str = "rk3"                 # rk3 (2-register) | ls_rk3
     precision: str = "fp64"         # fp64 | mixed
@@ -101,8 +101,8 @@ def tgv_plan(n=64, conv="central_skew", precision="fp64", Minf=0.1, Re=1600.0, P
              dt=None, use_graphs=True):
     """3D Taylor-Green vortex on the periodic box [0, 2 pi)^3 with n^3 points (delta = 2 pi / n), the
     configuration of apps/taylor_green_vortex/taylor_green_vortex.py (conv='central_skew') and of the
-    WENO5-JS, WENO5-Z and TENO5 variants (conv='weno5js', 'weno5z', 'teno5'; TENO5 with the fixed
-    cut-off C_T = 1e-5 and eps = 1e-15)."""
+    WENO5-JS, WENO5-Z, TENO5 and TENO6 variants (conv='weno5js', 'weno5z', 'teno5', 'teno6'; TENO with
+    the fixed cut-off C_T = 1e-5 and eps = 1e-15)."""
     ns = (n, n, n) if isinstance(n, int) else tuple(n)
     return Plan(n=ns, delta=tuple(2 * math.pi / k for k in ns), conv=conv, visc=visc, precision=precision, Minf=Minf,
                 Re=Re, Pr=Pr, gama=gama, dt=dt, use_graphs=use_graphs, ic="tgv",

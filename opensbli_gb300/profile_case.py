@@ -13,7 +13,7 @@ import time
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--n", type=int, default=192)
-    ap.add_argument("--conv", default="weno5js", choices=["weno5js", "weno5z", "teno5", "central_skew"])
+    ap.add_argument("--conv", default="weno5js", choices=["weno5js", "weno5z", "teno5", "teno6", "central_skew"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--steps", type=int, default=1)
     ap.add_argument("--warmup", type=int, default=0)

@@ -23,7 +23,7 @@ ERRORS = {
     -7: "problem larger than a fixed-size scratch array",
 }
 
-CONV = {"central_skew": 0, "weno5js": 1, "teno5": 2, "weno5z": 3}
+CONV = {"central_skew": 0, "weno5js": 1, "teno5": 2, "weno5z": 3, "teno6": 4}
 VISC = {"none": 0, "const": 1, "sutherland": 2}
 RK = {"rk3": 0, "ls_rk3": 1}
 BC = {"periodic": 0, "symmetry": 1, "inlet_pressure_extrapolate": 2, "extrapolation": 3, "isothermal_wall": 4,

@@ -110,7 +110,8 @@ class GB300Writer:
         if teno:
             # LLFTeno(5) with a fixed cut-off TENO_CT (teno.py:407-465); the adaptive cut-off needs the
             # Ducros sensor, which this build evaluates on 2D blocks only
-            conv = "teno5"
+            # LLFTeno(6) adds a fourth candidate stencil (delta_3, teno.py:94-105)
+            conv = "teno6" if all("delta_3" in self._lhs_names(k) for k in teno) else "teno5"
             if len(teno) != 3:
                 raise NotImplementedError("one LLFTeno reconstruction kernel per direction expected")
             for k in teno:
@@ -215,6 +216,8 @@ class GB300Writer:
             lhs = self._lhs_names(k)
             if not {"delta_0", "delta_1", "delta_2", "inv_omega_sum"} <= lhs:
                 raise NotImplementedError("TENO5 with a cut-off expected in %s" % k.computation_name)
+            if "delta_3" in lhs:
+                raise NotImplementedError("TENO6 on a 2D block is not lowered (3D blocks only)")
         adaptive = self._adaptive_teno(teno) if teno else None
         if self._max_offset(teno or weno) != 3:
             raise NotImplementedError("5th-order reconstruction stencil expected")
@@ -380,7 +383,7 @@ class GB300Writer:
                   Re=float(env.get("Re", p.Re)), Pr=float(env.get("Pr", p.Pr)),
                   dt=float(env["dt"]) if "dt" in env else p.dt,
                   niter=int(env["niter"]) if "niter" in env else p.niter)
-        if nd == 3 and p.conv == "teno5":
+        if nd == 3 and p.conv in ("teno5", "teno6"):
             kw.update(teno_eps=float(env.get("eps", p.teno_eps)), teno_ct=float(env.get("TENO_CT", p.teno_ct)))
         if nd == 2:
             kw.update(Twall=float(env.get("Twall", p.Twall)), SuthT=float(env.get("SuthT", p.SuthT)),

@@ -29,6 +29,7 @@ CASES = {
     "tgv_weno": "tgv_weno.py",
     "tgv_wenoz": "tgv_wenoz.py",
     "tgv_teno": "tgv_teno.py",
+    "tgv_teno6": "tgv_teno6.py",
     "katzer_teno": "katzer_teno.py",
     "katzer_adaptive": "ref:apps/katzer_SBLI/katzer_SBLI.py",
 }

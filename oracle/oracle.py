@@ -13,7 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libosb_oracle.so")
 
-CONV = {"central_skew": 0, "weno5js": 1, "teno5": 2, "weno5z": 3}
+CONV = {"central_skew": 0, "weno5js": 1, "teno5": 2, "weno5z": 3, "teno6": 4}
 VISC = {"none": 0, "const": 1, "sutherland": 2}
 RK = {"rk3": 0, "ls_rk3_ssp": 1}
 BC = {"periodic": 0, "symmetry": 1}

@@ -377,6 +377,57 @@ static double teno5_side(const double f[5], double eps, double CT) {
          0.05 * d2 * iw * ((1.0 / 6.0) * f[0] - (7.0 / 12.0) * f[1] + (11.0 / 12.0) * f[2]);
 }
 
+/* TENO6 (schemes/spatial/teno.py:94-192, 216-234, 407-465) with fixed cut-off on one side of the
+ * split flux.  g[0..5] are the split-flux values at points i-2 .. i+3 for either side; the four
+ * stencils of the + side (fn_points, teno.py:100-105) are i-1..i+1, i..i+2, i-2..i and i..i+3, those of
+ * the - side i..i+2, i-1..i+1, i+1..i+3 and i-2..i+1.  Indicators and candidates act on the halved values
+ * (the splitting's 1/2, as the generated code writes them); the + side's fourth indicator carries the
+ * reference's linear (unsquared) third-difference term (teno.py:175-176), the - side's the squared one.
+ * tau6 = |beta_0/6 - 2 beta_1/3 + beta_2/6 - beta_3| (teno.py:229), alpha_r = (1 + tau6/(eps+beta_r))^6,
+ * d = (231/500, 3/10, 27/500, 23/125). */
+static double teno6_side(const double g[6], int plus, double eps, double CT) {
+  double h[6];
+  for (int t = 0; t < 6; ++t) h[t] = 0.5 * g[t];
+  double b[4], p[4];
+  if (plus) {
+    b[0] = 0.25 * pow(h[1] - h[3], 2) + (13.0 / 12.0) * pow(h[1] - 2 * h[2] + h[3], 2);
+    b[1] = (13.0 / 12.0) * pow(h[2] - 2 * h[3] + h[4], 2) + 0.25 * pow(3 * h[2] - 4 * h[3] + h[4], 2);
+    b[2] = 0.25 * pow(h[0] - 4 * h[1] + 3 * h[2], 2) + (13.0 / 12.0) * pow(h[0] - 2 * h[1] + h[2], 2);
+    b[3] = (1.0 / 36.0) * pow(-11 * h[2] + 18 * h[3] - 9 * h[4] + 2 * h[5], 2) +
+           (13.0 / 12.0) * pow(2 * h[2] - 5 * h[3] + 4 * h[4] - h[5], 2) +
+           (781.0 / 720.0) * (-h[2] + 3 * h[3] - 3 * h[4] + h[5]);
+    p[0] = -(1.0 / 6.0) * h[1] + (5.0 / 6.0) * h[2] + (2.0 / 6.0) * h[3];
+    p[1] = (2.0 / 6.0) * h[2] + (5.0 / 6.0) * h[3] - (1.0 / 6.0) * h[4];
+    p[2] = (2.0 / 6.0) * h[0] - (7.0 / 6.0) * h[1] + (11.0 / 6.0) * h[2];
+    p[3] = (3.0 / 12.0) * h[2] + (13.0 / 12.0) * h[3] - (5.0 / 12.0) * h[4] + (1.0 / 12.0) * h[5];
+  } else {
+    b[0] = 0.25 * pow(h[2] - h[4], 2) + (13.0 / 12.0) * pow(h[2] - 2 * h[3] + h[4], 2);
+    b[1] = 0.25 * pow(h[1] - 4 * h[2] + 3 * h[3], 2) + (13.0 / 12.0) * pow(h[1] - 2 * h[2] + h[3], 2);
+    b[2] = 0.25 * pow(3 * h[3] - 4 * h[4] + h[5], 2) + (13.0 / 12.0) * pow(h[3] - 2 * h[4] + h[5], 2);
+    b[3] = (1.0 / 36.0) * pow(-2 * h[0] + 9 * h[1] - 18 * h[2] + 11 * h[3], 2) +
+           (13.0 / 12.0) * pow(-h[0] + 4 * h[1] - 5 * h[2] + 2 * h[3], 2) +
+           (781.0 / 720.0) * pow(-h[0] + 3 * h[1] - 3 * h[2] + h[3], 2);
+    p[0] = (2.0 / 6.0) * h[2] + (5.0 / 6.0) * h[3] - (1.0 / 6.0) * h[4];
+    p[1] = -(1.0 / 6.0) * h[1] + (5.0 / 6.0) * h[2] + (2.0 / 6.0) * h[3];
+    p[2] = (11.0 / 6.0) * h[3] - (7.0 / 6.0) * h[4] + (2.0 / 6.0) * h[5];
+    p[3] = (1.0 / 12.0) * h[0] - (5.0 / 12.0) * h[1] + (13.0 / 12.0) * h[2] + (3.0 / 12.0) * h[3];
+  }
+  const double tau = fabs(b[0] / 6.0 - 2.0 * b[1] / 3.0 + b[2] / 6.0 - b[3]);
+  const double dw[4] = {231.0 / 500.0, 3.0 / 10.0, 27.0 / 500.0, 23.0 / 125.0};
+  double a[4], sa = 0.0;
+  for (int r = 0; r < 4; ++r) {
+    a[r] = pow(1 + tau / (eps + b[r]), 6);
+    sa += a[r];
+  }
+  double num = 0.0, den = 0.0;
+  for (int r = 0; r < 4; ++r) {
+    const double dl = CT > a[r] / sa ? 0.0 : 1.0;
+    num += dw[r] * dl * p[r];
+    den += dw[r] * dl;
+  }
+  return num / den;
+}
+
 static void eigensystem(int dir, double rho, double u0, double u1, double u2, double a, double g, double L[5][5],
                         double R[5][5]) {
   double k[3] = {0, 0, 0};
@@ -477,7 +528,14 @@ static void residual_weno(st_t *s) {
           fp[t] = CF[r][t] + lam[r] * CS[r][t];
           fm[t] = CF[r][t + 1] - lam[r] * CS[r][t + 1];
         }
-        if (s->c.conv == OSBO_CONV_TENO5) {
+        if (s->c.conv == OSBO_CONV_TENO6) {
+          double gp[6], gm[6];
+          for (int t = 0; t < 6; ++t) {
+            gp[t] = CF[r][t] + lam[r] * CS[r][t];
+            gm[t] = CF[r][t] - lam[r] * CS[r][t];
+          }
+          rec[r] = teno6_side(gp, 1, s->c.teno_eps, s->c.teno_ct) + teno6_side(gm, 0, s->c.teno_eps, s->c.teno_ct);
+        } else if (s->c.conv == OSBO_CONV_TENO5) {
           const double fmr[5] = {fm[4], fm[3], fm[2], fm[1], fm[0]};  /* points i+3 .. i-1 */
           rec[r] = teno5_side(fp, s->c.teno_eps, s->c.teno_ct) + teno5_side(fmr, s->c.teno_eps, s->c.teno_ct);
         } else {

@@ -14,7 +14,7 @@
 extern "C" {
 #endif
 
-enum { OSBO_CONV_CENTRAL_SKEW = 0, OSBO_CONV_WENO5JS = 1, OSBO_CONV_TENO5 = 2, OSBO_CONV_WENO5Z = 3 };
+enum { OSBO_CONV_CENTRAL_SKEW = 0, OSBO_CONV_WENO5JS = 1, OSBO_CONV_TENO5 = 2, OSBO_CONV_WENO5Z = 3, OSBO_CONV_TENO6 = 4 };
 enum { OSBO_VISC_NONE = 0, OSBO_VISC_CONST = 1, OSBO_VISC_SUTHERLAND = 2 };
 enum { OSBO_RK3_2REG = 0, OSBO_RK3_LS_SSP = 1 };
 enum { OSBO_BC_PERIODIC = 0, OSBO_BC_SYMMETRY = 1 };

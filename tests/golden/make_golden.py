@@ -33,6 +33,7 @@ CASES = {
     "tgv_weno": (16, 10, {"dt": 2e-3, "Minf": 1.25}),
     "tgv_wenoz": (16, 10, {"dt": 2e-3, "Minf": 1.25}),
     "tgv_teno": (16, 10, {"dt": 2e-3, "Minf": 1.25}),
+    "tgv_teno6": (16, 10, {"dt": 2e-3, "Minf": 1.25}),
     "tgsym_central": (17, 10, {"dt": 5e-3}),
 }
 

@@ -30,7 +30,7 @@ def run_gpu(plan, q0, steps, dt):
     return out
 
 
-@pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgsym_central"])
+@pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central"])
 def test_gpu_fp64_matches_reference_golden(case):
     """The writer-lowered plan of the reference's own script reproduces the reference's output."""
     q_ref, n, steps, params = load_golden(case)
@@ -53,6 +53,8 @@ def test_gpu_fp64_matches_reference_golden(case):
     ("weno5z", (33, 40, 17), 4, 2e-3, 1.25),
     ("teno5", (20, 20, 20), 8, 2e-3, 1.25),
     ("teno5", (33, 40, 17), 4, 2e-3, 1.25),
+    ("teno6", (20, 20, 20), 8, 2e-3, 1.25),
+    ("teno6", (33, 40, 17), 4, 2e-3, 1.25),
 ])
 def test_gpu_fp64_matches_oracle(conv, n, steps, dt, M):
     plan = tgv_plan(n, conv=conv, Minf=M)
@@ -67,7 +69,7 @@ def test_gpu_fp64_matches_oracle(conv, n, steps, dt, M):
     assert max(err) <= FP64_TOL, err
 
 
-@pytest.mark.parametrize("conv,M", [("central_skew", 0.1), ("weno5js", 1.25), ("teno5", 1.25)])
+@pytest.mark.parametrize("conv,M", [("central_skew", 0.1), ("weno5js", 1.25), ("teno5", 1.25), ("teno6", 1.25)])
 def test_gpu_residual_matches_oracle(conv, M):
     plan = tgv_plan(24, conv=conv, Minf=M)
     cfg = oracle_cfg(plan)
@@ -82,7 +84,8 @@ def test_gpu_residual_matches_oracle(conv, M):
         assert np.abs(r[v] - r_or[v]).max() / scale <= FP64_TOL
 
 
-@pytest.mark.parametrize("conv,M,tol", [("central_skew", 0.1, 2e-6), ("weno5js", 1.25, 2e-6), ("teno5", 1.25, 2e-6)])
+@pytest.mark.parametrize("conv,M,tol", [("central_skew", 0.1, 2e-6), ("weno5js", 1.25, 2e-6), ("teno5", 1.25, 2e-6),
+                                        ("teno6", 1.25, 2e-6)])
 def test_gpu_mixed_close_to_fp64(conv, M, tol):
     plan = tgv_plan(32, conv=conv, Minf=M)
     cfg = oracle_cfg(plan, dt=2e-3)

@@ -37,7 +37,7 @@ def residual_with(plan, q0, kind, seg):
     return r
 
 
-@pytest.mark.parametrize("conv", ["weno5js", "teno5"])
+@pytest.mark.parametrize("conv", ["weno5js", "teno5", "teno6"])
 @pytest.mark.parametrize("n", [(24, 24, 24), (40, 37, 29)])
 @pytest.mark.parametrize("kind,seg", SHAPES)
 def test_weno_shapes_fp64_match_oracle(n, kind, seg, conv):

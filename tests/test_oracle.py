@@ -13,7 +13,7 @@ from oracle import oracle as O
 from oracle import refrun
 from helpers import load_golden, golden_plan, oracle_cfg, rel_err, rel_err_mom, WENOZ_TOL
 
-CASES = ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgsym_central"]
+CASES = ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central"]
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -53,6 +53,7 @@ def test_oracle_periodic_mass_conservation():
     ("tgv_weno", 12, 4, {"dt": 3e-3, "Minf": 1.25}),
     ("tgv_wenoz", 12, 4, {"dt": 3e-3, "Minf": 1.25}),
     ("tgv_teno", 12, 4, {"dt": 3e-3, "Minf": 1.25}),
+    ("tgv_teno6", 12, 4, {"dt": 3e-3, "Minf": 1.25}),
 ])
 def test_oracle_matches_reference_run(case, n, steps, extra):
     if not refrun.available(case):
