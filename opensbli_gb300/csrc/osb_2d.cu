@@ -3,13 +3,16 @@
 // low-storage RK3 update and the four face conditions of the shock/boundary-layer problem.
 //
 // Kernel list per RK stage (the generated loop, algorithm.py:384-477, for
-// apps/katzer_SBLI/katzer_SBLI.py with fixed-C_T TENO):
-//   k2_bc_* (inlet, outlet, wall, top, in that order) on the FP64 master state
-//   k2_to_state (mixed only: FP64 master -> FP32 working state, halos included)
-//   k2_prims   constituent relations u0, u1, p, a, T, mu (Sutherland)
+// apps/katzer_SBLI/katzer_SBLI.py):
+//   k2_prims   constituent relations u0, u1, p, a, T, mu (Sutherland) from the FP64 master; mixed:
+//              also the FP32 working state
 //   k2_sensor_ct (adaptive TENO only): modified Ducros sensor theta and the cut-off C_T per point
 //   k2_flux<T, D, SCHEME> for D = x0, x1: interface fluxes + flux difference into R
 //   k2_visc_rk viscous/heat-flux terms + LS-RK3: du = A du + dt R, q += B du (FP64)
+//   k2_bc_x, k2_bc_y  the four face conditions on the FP64 master (inlet and outlet, then wall and
+//              top: the generated order where it matters)
+// A step starts with the face conditions and, mixed, ends with k2_to_state (the bound FP32 arrays
+// current).
 // Metrics (once, k2_metric_*): detJ = dx1/dxi1 with the closures, D11 = 1/detJ, halos mirrored about
 // the boundary points, SD111 = dD11/dxi1 (equation_types/metric.py:37-234, 315-332).
 #include "osb_common.cuh"
@@ -90,73 +93,81 @@ struct Q4 {
   double *v[4];
 };
 
-// InletPressureExtrapolateBC (core/boundary_conditions/inlet_pressure_extrapolate.py:11-66):
-// supersonic points at i = 0 take the halo state at i = -1; subsonic points keep their state and the
-// energy halos take rhoE(0).
-__global__ void k2_bc_inlet(Grid g, Q4 q, double gama, int h) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x - 3;
-  if (j >= g.n1 + h) return;
-  const int64_t b = g2(g, 0, j), m1 = g2(g, -1, j);
-  const double rhob = q.v[0][b];
-  const double ub0 = fabs(q.v[1][b] / rhob), ub1 = fabs(q.v[2][b] / rhob);
-  const double pb = (gama - 1) * (-0.5 * rhob * (ub0 * ub0 + ub1 * ub1) + q.v[3][b]);
-  const double ab = sqrt(gama * pb / rhob);
-  if (ub0 >= ab) {
-    for (int v = 0; v < 4; ++v) q.v[v][b] = q.v[v][m1];
-  } else {
-    const double e = q.v[3][b];
-    for (int t = 1; t <= 3; ++t) q.v[3][g2(g, -t, j)] = e;
-  }
-}
-
-// ExtrapolationBC, order 0 (core/boundary_conditions/extrapolation.py:8-58): the last point and the
-// halo points take the state of point n0-2.
-__global__ void k2_bc_outlet(Grid g, Q4 q, int hx, int hy) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x - 3;
-  if (j >= g.n1 + hy) return;
-  for (int v = 0; v < 4; ++v) {
-    const double val = q.v[v][g2(g, g.n0 - 2, j)];
-    for (int t = 0; t <= hx; ++t) q.v[v][g2(g, g.n0 - 1 + t, j)] = val;
-  }
-}
-
-// IsothermalWallBC (core/boundary_conditions/isothermal_wall.py:32-88)
-__global__ void k2_bc_wall(Grid g, Q4 q, double gama, double Minf, double Twall, int hx) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x - 3;
-  if (i >= g.n0 + hx) return;
-  const double M2 = Minf * Minf;
-  const int64_t w = g2(g, i, 0), a1 = g2(g, i, 1);
-  q.v[1][w] = 0.0;
-  q.v[2][w] = 0.0;
-  q.v[3][w] = Twall * (1.0 / M2) * q.v[0][w] / (gama * (gama - 1.0));
-  const double Pw = (gama - 1) * (-(0.5 * q.v[1][w] * q.v[1][w] + 0.5 * q.v[2][w] * q.v[2][w]) / q.v[0][w] + q.v[3][w]);
-  const double Ta = M2 * gama * (gama - 1) *
-                    (-(0.5 * q.v[1][a1] * q.v[1][a1] + 0.5 * q.v[2][a1] * q.v[2][a1]) / q.v[0][a1] + q.v[3][a1]) /
-                    q.v[0][a1];
-  for (int t = 1; t <= 3; ++t) {
-    const int64_t m = g2(g, i, t), hh = g2(g, i, -t);
-    const double um0 = q.v[1][m] / q.v[0][m], um1 = q.v[2][m] / q.v[0][m];
-    const double Tt = (t + 1) * Twall - t * Ta;
-    const double rh = M2 * gama * Pw / Tt;
-    q.v[0][hh] = rh;
-    q.v[1][hh] = -rh * um0;
-    q.v[2][hh] = -rh * um1;
-    q.v[3][hh] = (1.0 / (gama - 1)) * Pw + 0.5 * rh * (um0 * um0 + um1 * um1);
-  }
-}
-
-// DirichletBC with a piecewise state in x0 (katzer_SBLI.py:108-114): points j >= n1-1 take
-// state[1] where x0 = delta0 * i > x_switch and state[0] elsewhere.
+// Face conditions of the shock/boundary-layer block:
+//  * InletPressureExtrapolateBC (core/boundary_conditions/inlet_pressure_extrapolate.py:11-66):
+//    supersonic points at i = 0 take the halo state at i = -1; subsonic points keep their state and
+//    the energy halos take rhoE(0);
+//  * ExtrapolationBC, order 0 (core/boundary_conditions/extrapolation.py:8-58): the last point and
+//    the halo points take the state of point n0-2;
+//  * IsothermalWallBC (core/boundary_conditions/isothermal_wall.py:32-88): zero momentum at the
+//    wall, wall energy from Twall, halo states mirrored with a linearly extrapolated temperature;
+//  * DirichletBC with a piecewise state in x0 (katzer_SBLI.py:108-114): points j >= n1-1 take
+//    state[1] where x0 = delta0 * i > x_switch and state[0] elsewhere.
 struct Dir2 {
   double lo[4], hi[4];
 };
-__global__ void k2_bc_top(Grid g, Q4 q, Dir2 st, double delta0, double xs, int hx, int hy) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x - 3;
-  if (i >= g.n0 + hx) return;
-  const double x0 = delta0 * i;
-  for (int j = g.n1 - 1; j < g.n1 + hy; ++j)
-    for (int v = 0; v < 4; ++v) q.v[v][g2(g, i, j)] = x0 > xs ? st.hi[v] : st.lo[v];
+
+// The four faces in two launches.  The inlet and outlet touch disjoint columns (0, -1..-3 and
+// n0-2..n0+hx), the wall and the top face disjoint rows (-3..0 and n1-1..n1+hy); the generated order
+// (inlet, outlet, wall, top) only matters between the pairs: the wall reads the x-halo columns the
+// inlet and outlet wrote, and at the corners the later face wins.  One thread per row (x faces) or
+// column (y faces); small blocks spread the FP64 divisions over many SMs.
+struct BC2Args {
+  double gama, Minf, Twall, delta0, xs;
+  int hx, hy;
+  Dir2 st;
+};
+__global__ void __launch_bounds__(64) k2_bc_x(Grid g, Q4 q, BC2Args a) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x - 3;
+  if (j >= g.n1 + a.hy) return;
+  {  // inlet
+    const int64_t b = g2(g, 0, j), m1 = g2(g, -1, j);
+    const double rhob = q.v[0][b];
+    const double ub0 = fabs(q.v[1][b] / rhob), ub1 = fabs(q.v[2][b] / rhob);
+    const double pb = (a.gama - 1) * (-0.5 * rhob * (ub0 * ub0 + ub1 * ub1) + q.v[3][b]);
+    const double ab = sqrt(a.gama * pb / rhob);
+    if (ub0 >= ab) {
+      for (int v = 0; v < 4; ++v) q.v[v][b] = q.v[v][m1];
+    } else {
+      const double e = q.v[3][b];
+      for (int t = 1; t <= 3; ++t) q.v[3][g2(g, -t, j)] = e;
+    }
+  }
+  for (int v = 0; v < 4; ++v) {  // outlet
+    const double val = q.v[v][g2(g, g.n0 - 2, j)];
+    for (int t = 0; t <= a.hx; ++t) q.v[v][g2(g, g.n0 - 1 + t, j)] = val;
+  }
 }
+
+__global__ void __launch_bounds__(64) k2_bc_y(Grid g, Q4 q, BC2Args a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x - 3;
+  if (i >= g.n0 + a.hx) return;
+  const double M2 = a.Minf * a.Minf, gama = a.gama;
+  {  // isothermal wall
+    const int64_t w = g2(g, i, 0), a1 = g2(g, i, 1);
+    q.v[1][w] = 0.0;
+    q.v[2][w] = 0.0;
+    q.v[3][w] = a.Twall * (1.0 / M2) * q.v[0][w] / (gama * (gama - 1.0));
+    const double Pw = (gama - 1) * (-(0.5 * q.v[1][w] * q.v[1][w] + 0.5 * q.v[2][w] * q.v[2][w]) / q.v[0][w] + q.v[3][w]);
+    const double Ta = M2 * gama * (gama - 1) *
+                      (-(0.5 * q.v[1][a1] * q.v[1][a1] + 0.5 * q.v[2][a1] * q.v[2][a1]) / q.v[0][a1] + q.v[3][a1]) /
+                      q.v[0][a1];
+    for (int t = 1; t <= 3; ++t) {
+      const int64_t m = g2(g, i, t), hh = g2(g, i, -t);
+      const double um0 = q.v[1][m] / q.v[0][m], um1 = q.v[2][m] / q.v[0][m];
+      const double Tt = (t + 1) * a.Twall - t * Ta;
+      const double rh = M2 * gama * Pw / Tt;
+      q.v[0][hh] = rh;
+      q.v[1][hh] = -rh * um0;
+      q.v[2][hh] = -rh * um1;
+      q.v[3][hh] = (1.0 / (gama - 1)) * Pw + 0.5 * rh * (um0 * um0 + um1 * um1);
+    }
+  }
+  const double x0 = a.delta0 * i;  // Dirichlet top face
+  for (int j = g.n1 - 1; j < g.n1 + a.hy; ++j)
+    for (int v = 0; v < 4; ++v) q.v[v][g2(g, i, j)] = x0 > a.xs ? a.st.hi[v] : a.st.lo[v];
+}
+
 
 template <typename T> struct Q4T {
   T *v[4];
@@ -175,21 +186,42 @@ template <typename T> struct Prims {
   T *u0, *u1, *p, *a, *T_, *mu;
 };
 
+// Over every padded point (-4 .. n+3) from the FP64 master state.  Mixed: the FP32 working state is
+// written here (the FP64 -> FP32 rounding of the stage), and u, p, T come out rounded once from the
+// FP32 values (prims_f32).  FP64: the master is the state.
 template <typename T>
-__global__ void k2_prims(Grid g, Q4T<const T> q, Prims<T> pr, double gama, double Minf, double suth) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x - 3, j = blockIdx.y * blockDim.y + threadIdx.y - 3;
+__global__ void k2_prims(Grid g, Q4 q64, Q4T<float> qs, Prims<T> pr, double gama, double Minf, double suth) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x - 4, j = blockIdx.y * blockDim.y + threadIdx.y - 4;
   if (i >= g.n0 + 4 || j >= g.n1 + 4) return;
   const int64_t n = g2(g, i, j);
-  const T r = q.v[0][n];
-  const T ir = T(1) / r;
-  const T u0 = q.v[1][n] * ir, u1 = q.v[2][n] * ir;
+  T r, u0, u1, p, Tt, ir;
   const T gm = T(gama);
-  const T p = (gm - T(1)) * (q.v[3][n] - T(0.5) * r * u0 * u0 - T(0.5) * r * u1 * u1);
+  if constexpr (sizeof(T) == 4) {
+    float qv[4];
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+      qv[v] = cvt_f64_f32(q64.v[v][n]);
+      qs.v[v][n] = qv[v];
+    }
+    const float gm1 = (float)(gama - 1.0), gm1_lo = (float)((gama - 1.0) - (double)gm1);
+    float u[3], p_lo;
+    r = qv[0];
+    prims_f32(qv[0], qv[1], qv[2], 0.0f, qv[3], gm1, gm1_lo, ir, u, p, p_lo);
+    u0 = u[0];
+    u1 = u[1];
+    Tt = scaled_ratio_f32((float)(Minf * Minf * gama), p, p_lo, r, ir);
+  } else {
+    r = q64.v[0][n];
+    ir = T(1) / r;
+    u0 = q64.v[1][n] * ir;
+    u1 = q64.v[2][n] * ir;
+    p = (gm - T(1)) * (q64.v[3][n] - T(0.5) * r * u0 * u0 - T(0.5) * r * u1 * u1);
+    Tt = T(Minf * Minf * gama) * p * ir;
+  }
   pr.u0[n] = u0;
   pr.u1[n] = u1;
   pr.p[n] = p;
   pr.a[n] = sqrt_t(gm * p * ir);
-  const T Tt = T(Minf * Minf * gama) * p * ir;
   const T S = T(suth);
   pr.T_[n] = Tt;
   pr.mu[n] = (S + T(1)) * Tt * sqrt_t(Tt) / (S + Tt);
@@ -463,10 +495,13 @@ __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<con
     int i, j;
     coord(c, a, i, j);
     const int64_t gi = g2(g, i, j);
-    const T scale = D == 0 ? T(inv_dd) : T(inv_dd) * T(D11[gi]);
+    // 1/delta (times D11 along x1) formed in FP64 and carried as an FP32 pair in mixed precision: one
+    // rounding of it would scale every flux difference of the point the same way, step after step
+    const double sc = D == 0 ? inv_dd : inv_dd * D11[gi];
+    const T sc_hi = T(sc), sc_lo = T(sc - (double)sc_hi);
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      const T d = -(sfl[v][m + 1][a] - sfl[v][m][a]) * scale;
+      const T d = -mul_hl(sfl[v][m + 1][a] - sfl[v][m][a], sc_hi, sc_lo);
       if (D == 0) res.v[v][gi] = d;
       else res.v[v][gi] += d;
     }
@@ -571,24 +606,32 @@ void launch2_metrics(const Ctx &c, const double *x1, cudaStream_t s, int64_t *la
 
 void launch2_bcs(const Ctx &c, cudaStream_t s, int64_t *launches) {
   const osb_plan_desc &p = c.plan;
-  Q4 q = q4(c.q64_2d);
-  const int ny = c.g.n1 + 3 + c.hy2, nx = c.g.n0 + 3 + c.hx2;
-  k2_bc_inlet<<<(ny + 127) / 128, 128, 0, s>>>(c.g, q, p.gama, c.hy2);
-  k2_bc_outlet<<<(ny + 127) / 128, 128, 0, s>>>(c.g, q, c.hx2, c.hy2);
-  k2_bc_wall<<<(nx + 127) / 128, 128, 0, s>>>(c.g, q, p.gama, p.Minf, p.Twall, c.hx2);
-  Dir2 st;
+  BC2Args a;
+  a.gama = p.gama;
+  a.Minf = p.Minf;
+  a.Twall = p.Twall;
+  a.delta0 = p.delta[0];
+  a.xs = p.dirichlet_x_switch;
+  a.hx = c.hx2;
+  a.hy = c.hy2;
   for (int v = 0; v < 4; ++v) {
-    st.lo[v] = p.dirichlet_state[0][v];
-    st.hi[v] = p.dirichlet_state[1][v];
+    a.st.lo[v] = p.dirichlet_state[0][v];
+    a.st.hi[v] = p.dirichlet_state[1][v];
   }
-  k2_bc_top<<<(nx + 127) / 128, 128, 0, s>>>(c.g, q, st, p.delta[0], p.dirichlet_x_switch, c.hx2, c.hy2);
-  *launches += 4;
-  if (c.mixed) {
-    int nb = (int)((c.g.numel + 255) / 256);
-    if (nb > 152 * 8) nb = 152 * 8;
-    k2_to_state<<<nb, 256, 0, s>>>(c.g.numel, q, q4t<float>(c.qa));
-    ++*launches;
-  }
+  const int ny = c.g.n1 + 3 + c.hy2, nx = c.g.n0 + 3 + c.hx2;
+  k2_bc_x<<<(ny + 63) / 64, 64, 0, s>>>(c.g, q4(c.q64_2d), a);
+  k2_bc_y<<<(nx + 63) / 64, 64, 0, s>>>(c.g, q4(c.q64_2d), a);
+  *launches += 2;
+}
+
+// Mixed: the FP32 working state from the FP64 master at every padded point (the right-hand side's
+// k2_prims does this for its own stage; this one leaves the bound arrays current after a step).
+void launch2_to_state(const Ctx &c, cudaStream_t s, int64_t *launches) {
+  if (!c.mixed) return;
+  int nb = (int)((c.g.numel + 255) / 256);
+  if (nb > 152 * 8) nb = 152 * 8;
+  k2_to_state<<<nb, 256, 0, s>>>(c.g.numel, q4(c.q64_2d), q4t<float>(c.qa));
+  ++*launches;
 }
 
 template <typename T> void launch2_rhs(const Ctx &c, int update, double A, double B, double dt, cudaStream_t s,
@@ -603,8 +646,8 @@ template <typename T> void launch2_rhs(const Ctx &c, int update, double A, doubl
   pr.mu = static_cast<T *>(c.prim2[5]);
   Prims<const T> prc{pr.u0, pr.u1, pr.p, pr.a, pr.T_, pr.mu};
   Q4T<const T> q = q4t<const T>(c.qa);
-  dim3 b(32, 8), gp((c.g.n0 + 7 + 31) / 32, (c.g.n1 + 7 + 7) / 8);
-  k2_prims<T><<<gp, b, 0, s>>>(c.g, q, pr, p.gama, p.Minf, p.SuthT / p.RefT);
+  dim3 b(32, 8), gp((c.g.n0 + 8 + 31) / 32, (c.g.n1 + 8 + 7) / 8);
+  k2_prims<T><<<gp, b, 0, s>>>(c.g, q4(c.q64_2d), q4t<float>(c.qa), pr, p.gama, p.Minf, p.SuthT / p.RefT);
   Q4T<T> r = q4t<T>(c.res);
   const bool teno = p.conv == OSB_CONV_TENO5;
   const double eps = teno ? p.teno_eps : p.weno_eps;
@@ -663,8 +706,8 @@ template <typename T> void launch2_cutoff(const Ctx &c, double *out, cudaStream_
   pr.T_ = static_cast<T *>(c.prim2[4]);
   pr.mu = static_cast<T *>(c.prim2[5]);
   Prims<const T> prc{pr.u0, pr.u1, pr.p, pr.a, pr.T_, pr.mu};
-  dim3 b(32, 8), gp((c.g.n0 + 7 + 31) / 32, (c.g.n1 + 7 + 7) / 8);
-  k2_prims<T><<<gp, b, 0, s>>>(c.g, q4t<const T>(c.qa), pr, p.gama, p.Minf, p.SuthT / p.RefT);
+  dim3 b(32, 8), gp((c.g.n0 + 8 + 31) / 32, (c.g.n1 + 8 + 7) / 8);
+  k2_prims<T><<<gp, b, 0, s>>>(c.g, q4(c.q64_2d), q4t<float>(c.qa), pr, p.gama, p.Minf, p.SuthT / p.RefT);
   Sensor2Args sa{1.0 / p.delta[0], 1.0 / p.delta[1], p.teno_a1, p.teno_a2, p.sensor_eps};
   dim3 gs((c.g.n0 + 2 + 31) / 32, (c.g.n1 + 2 + 7) / 8);
   k2_sensor_ct<T><<<gs, b, 0, s>>>(c.g, prc, c.d11, static_cast<T *>(c.ct2), sa);

@@ -418,6 +418,9 @@ template <typename T> void one_step2(osb_ctx *c, double dt, cudaStream_t s) {
     ProfScope ps(c, PF_HALO, s);
     launch2_bcs(*c, s, &c->launches);
   }
+  // mixed: each stage's right-hand side rounds the master into the FP32 state itself; this leaves
+  // the bound FP32 arrays holding the step's final state
+  launch2_to_state(*c, s, &c->launches);
 }
 
 template <typename T> int step2_impl(osb_ctx *c, int nsteps, double dt) {
