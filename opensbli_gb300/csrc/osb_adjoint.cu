@@ -1,4 +1,5 @@
-// osb_adjoint.cu -- discrete adjoint of the periodic central scheme and of its RK3 step (FP64).
+// osb_adjoint.cu -- discrete adjoint of the periodic central and WENO5-JS schemes and of their RK3
+// step (FP64).
 //
 // The forward residual (osb_central.cu; the generated Taylor-Green solver's convective
 // skew-symmetric and constant-viscosity viscous terms) is, at every point, a function of point
@@ -18,9 +19,12 @@
 //   s[D2_d u_c] = kappa_c (1 + delta_cd / 3) / Re,   s[D_{min(c,e)} D_{max(c,e)} u_e] = kappa_c / (3 Re),
 //   kappa_c = lambda_{1+c} + lambda_4 u_c.
 // The 2-register RK3 step (schemes/temporal/rk_sbli.py:117-124) is reversed stage by stage from the
-// recomputed stage states.  Only periodic FP64 central plans are accepted.
+// recomputed stage states.  With WENO5-JS fluxes the convective part is replaced by the transpose of
+// the characteristic flux difference (k_adj_weno, the reverse mode of osb_adjoint_weno.cuh) and the
+// passes above carry the viscous and heat-flux terms only.  Periodic FP64 plans are accepted.
 #include <cstdio>
 
+#include "osb_adjoint_weno.cuh"
 #include "osb_common.cuh"
 #include "osb_internal.h"
 
@@ -70,7 +74,9 @@ __global__ void k_adj_prims(int64_t numel, Fields5<const double> q, Prim5 pr, do
   }
 }
 
-__global__ void k_adj_pass1(Grid g, Fields5<const double> q, Prim5 pr, FieldSet A, Phys ph) {
+// conv = 0 (characteristic-flux plans): the skew-symmetric convective sensitivities are zero and only
+// the viscous and heat-flux ones are formed; the flux adjoint comes from k_adj_weno.
+__global__ void k_adj_pass1(Grid g, Fields5<const double> q, Prim5 pr, FieldSet A, Phys ph, int conv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
   if (i >= g.n0) return;
   const int64_t n = gidx(g, i, j, k);
@@ -127,6 +133,7 @@ __global__ void k_adj_pass1(Grid g, Fields5<const double> q, Prim5 pr, FieldSet 
     mom[c] = invRe * (d2u[c][0] + d2u[c][1] + d2u[c][2] + ddiv / 3.0);
   }
   double L[5], phi[5], u[3];
+  const double cv = conv ? 1.0 : 0.0;
 #pragma unroll
   for (int v = 0; v < 5; ++v) {
     L[v] = A.f[A_LAM + v][n];
@@ -137,13 +144,13 @@ __global__ void k_adj_pass1(Grid g, Fields5<const double> q, Prim5 pr, FieldSet 
 #pragma unroll
   for (int v = 0; v < 5; ++v)
 #pragma unroll
-    for (int d = 0; d < 3; ++d) A.f[A_LU + 3 * v + d][n] = L[v] * u[d];
+    for (int d = 0; d < 3; ++d) A.f[A_LU + 3 * v + d][n] = cv * L[v] * u[d];
 #pragma unroll
   for (int c = 0; c < 3; ++c) A.f[A_KAP + c][n] = L[1 + c] + L[4] * u[c];
   double sigma = 0;
 #pragma unroll
   for (int v = 0; v < 5; ++v) sigma += L[v] * phi[v];
-  sigma *= -0.5;
+  sigma *= -0.5 * cv;
 #pragma unroll
   for (int a = 0; a < 3; ++a)
 #pragma unroll
@@ -157,13 +164,14 @@ __global__ void k_adj_pass1(Grid g, Fields5<const double> q, Prim5 pr, FieldSet 
     double s = 0;
 #pragma unroll
     for (int v = 0; v < 5; ++v) s += L[v] * dphi[v][c];
-    A.f[A_LOCU + c][n] = -0.5 * s + L[4] * mom[c];
+    A.f[A_LOCU + c][n] = -0.5 * cv * s + L[4] * mom[c];
   }
 #pragma unroll
-  for (int v = 0; v < 5; ++v) A.f[A_LOCPHI + v][n] = -0.5 * L[v] * divu;
+  for (int v = 0; v < 5; ++v) A.f[A_LOCPHI + v][n] = -0.5 * cv * L[v] * divu;
 }
 
-__global__ void k_adj_pass2(Grid g, Fields5<const double> q, Prim5 pr, FieldSet A, Phys ph, double *out, double scale) {
+__global__ void k_adj_pass2(Grid g, Fields5<const double> q, Prim5 pr, FieldSet A, Phys ph, double *out, double scale,
+                            int conv) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y, k = blockIdx.z;
   if (i >= g.n0) return;
   const int64_t n = gidx(g, i, j, k);
@@ -218,7 +226,7 @@ __global__ void k_adj_pass2(Grid g, Fields5<const double> q, Prim5 pr, FieldSet 
       a += D1(A.f[A_LU + 3 * v + d], d);
       b += u[d] * DL[v][d];
     }
-    Gphi[v] = 0.5 * a + 0.5 * b + A.f[A_LOCPHI + v][n];
+    Gphi[v] = conv ? 0.5 * a + 0.5 * b + A.f[A_LOCPHI + v][n] : 0.0;
   }
   double Gu[3];
 #pragma unroll
@@ -234,13 +242,13 @@ __global__ void k_adj_pass2(Grid g, Fields5<const double> q, Prim5 pr, FieldSet 
     double s = 0;
 #pragma unroll
     for (int v = 0; v < 5; ++v) s += phi[v] * DL[v][c];
-    g += A.f[A_LOCU + c][n] + 0.5 * s + p * DL[4][c];
+    g += A.f[A_LOCU + c][n] + (conv ? 0.5 * s + p * DL[4][c] : 0.0);
     Gu[c] = g;
   }
   double Gp = 0, GT = 0;
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
-    Gp += DL[1 + d][d] + u[d] * DL[4][d];
+    if (conv) Gp += DL[1 + d][d] + u[d] * DL[4][d];
     GT += D2(A.f[A_LAM + 4], d);
   }
   GT *= kT;
@@ -261,6 +269,57 @@ __global__ void k_adj_pass2(Grid g, Fields5<const double> q, Prim5 pr, FieldSet 
 #pragma unroll
   for (int c = 0; c < 3; ++c) out[(1 + c) * N + m] = scale * Gut[c] * ir;
   out[4 * N + m] = scale * GE;
+}
+
+// The characteristic WENO5-JS flux along D, transposed.  The forward residual of cell c is
+// -(F_{c+1/2} - F_{c-1/2}) / delta_D with the interface fluxes of left points L = -1 .. n-1 computed
+// on the periodically filled state, so an interface's flux adjoint is
+//   F_bar(L) = (lambda_{L+1} [L+1 < n] - lambda_L [L >= 0]) / delta_D,
+// and its window's six points receive (dF/dQ)^T F_bar, folded back onto their periodic images.  One
+// thread per interface; the contributions of the six interfaces sharing a point meet in FP64 atomics.
+template <int D>
+__global__ void k_adj_weno(Grid g, Fields5<const double> q, FieldSet A, Phys ph, double *out, double scale) {
+  const int nd = D == 0 ? g.n0 : D == 1 ? g.n1 : g.n2;
+  const int na = D == 0 ? g.n1 : g.n0, nb = D == 2 ? g.n1 : g.n2;  // transverse extents
+  const int64_t total = (int64_t)(nd + 1) * na * nb;
+  const int64_t N = (int64_t)g.n0 * g.n1 * g.n2;
+  const int64_t sd = D == 0 ? 1 : D == 1 ? g.sy : g.sz;
+  for (int64_t w = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; w < total; w += (int64_t)gridDim.x * blockDim.x) {
+    const int L = (int)(w % (nd + 1)) - 1;
+    const int64_t rest = w / (nd + 1);
+    const int ia = (int)(rest % na), ib = (int)(rest / na);
+    int i = 0, j = 0, k = 0;  // coordinates of the left point
+    if (D == 0) { i = L; j = ia; k = ib; }
+    else if (D == 1) { i = ia; j = L; k = ib; }
+    else { i = ia; j = ib; k = L; }
+    const int64_t nL = gidx(g, i, j, k);
+    double Fb[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      double f = 0.0;
+      if (L >= 0) f -= A.f[A_LAM + v][nL];
+      if (L + 1 < nd) f += A.f[A_LAM + v][nL + sd];
+      Fb[v] = f * ph.inv_delta[D];
+    }
+    double Q[6][5], Qb[6][5];
+#pragma unroll
+    for (int t = 0; t < 6; ++t)
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        Q[t][v] = q.v[v][nL + (int64_t)(t - 2) * sd];
+        Qb[t][v] = 0.0;
+      }
+    adjw::interface_flux_adj<D>(Q, Fb, ph.gama, Qb, nullptr, ph.weno_eps);
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      const int c = ((L - 2 + t) % nd + nd) % nd;
+      const int64_t m = D == 0 ? (int64_t)c + (int64_t)g.n0 * (j + (int64_t)g.n1 * k)
+                        : D == 1 ? (int64_t)i + (int64_t)g.n0 * (c + (int64_t)g.n1 * k)
+                                 : (int64_t)i + (int64_t)g.n0 * (j + (int64_t)g.n1 * c);
+#pragma unroll
+      for (int v = 0; v < 5; ++v) atomicAdd(out + v * N + m, scale * Qb[t][v]);
+    }
+  }
 }
 
 }  // namespace osb
@@ -393,10 +452,32 @@ void adj_rhs(Ctx &c, const AdjView &v, Fields5<double> qs, double *out, double s
   adj_halos(c, v.A.f + A_LAM, 5, s, &c.launches);
   k_adj_prims<<<grid_blocks(c.g.numel), 256, 0, s>>>(c.g.numel, cq(qs), v.pr, ph.gm1, ph.gM2);
   const dim3 grid((c.g.n0 + 127) / 128, c.g.n1, c.g.n2);
-  k_adj_pass1<<<grid, 128, 0, s>>>(c.g, cq(qs), v.pr, v.A, ph);
+  const int conv = c.plan.conv == OSB_CONV_CENTRAL_SKEW ? 1 : 0;
+  k_adj_pass1<<<grid, 128, 0, s>>>(c.g, cq(qs), v.pr, v.A, ph, conv);
   adj_halos(c, v.A.f, NA_HALO, s, &c.launches);
-  k_adj_pass2<<<grid, 128, 0, s>>>(c.g, cq(qs), v.pr, v.A, ph, out, scale);
+  k_adj_pass2<<<grid, 128, 0, s>>>(c.g, cq(qs), v.pr, v.A, ph, out, scale, conv);
   c.launches += 3;
+  if (!conv) {  // WENO5-JS fluxes: their transposes, added into out
+    const int64_t per = (int64_t)c.g.n0 * c.g.n1 * c.g.n2;
+    const int nb = grid_blocks(per + per / 8 + 1);
+    k_adj_weno<0><<<nb, 128, 0, s>>>(c.g, cq(qs), v.A, ph, out, scale);
+    k_adj_weno<1><<<nb, 128, 0, s>>>(c.g, cq(qs), v.A, ph, out, scale);
+    k_adj_weno<2><<<nb, 128, 0, s>>>(c.g, cq(qs), v.A, ph, out, scale);
+    c.launches += 3;
+  }
+}
+
+// one forward RK3 stage of the plan from qs into qn (the FP64 register o updated): the same kernels as
+// the solver's step
+void fwd_stage(Ctx &c, Fields5<double> qs, Fields5<double> qn, Fields5<double> o, Fields5<double> res, double dtn,
+               double dto, cudaStream_t s) {
+  const int visc = c.plan.visc == OSB_VISC_CONST ? CRK_VISC : 0;
+  if (c.plan.conv == OSB_CONV_CENTRAL_SKEW) {
+    launch_central_rk<double>(c, cq(qs), qn, o, res, res, dtn, dto, CRK_SKEW | visc | CRK_UPDATE, s, &c.launches);
+    return;
+  }
+  for (int d = 0; d < 3; ++d) launch_weno_dir<double>(c, cq(qs), res, d, s, &c.launches);
+  launch_central_rk<double>(c, cq(qs), qn, o, res, res, dtn, dto, CRK_RIN | visc | CRK_UPDATE, s, &c.launches);
 }
 }  // namespace
 
@@ -435,18 +516,15 @@ cudaError_t adj_step(Ctx &c, Fields5<double> q, double dt, const double *lam_in,
   const AdjView v = adj_view(c);
   const int64_t N5 = 5 * (int64_t)c.g.n0 * c.g.n1 * c.g.n2;
   const double *a = c.plan.rk_a, *b = c.plan.rk_b;
-  const int visc = c.plan.visc == OSB_VISC_CONST ? CRK_VISC : 0;
   Fields5<double> res;
   for (int f = 0; f < 5; ++f) res.v[f] = static_cast<double *>(c.res[f]);
   // forward stage states q_1, q_2
   launch_halos<double>(c, q, s, &c.launches);
   k_adj_copy5<<<grid_blocks(c.g.numel), 256, 0, s>>>(c.g.numel, cq(q), v.O);
   ++c.launches;
-  launch_central_rk<double>(c, cq(q), v.Q1, v.O, res, res, dt * b[0], dt * a[0], CRK_SKEW | visc | CRK_UPDATE, s,
-                            &c.launches);
+  fwd_stage(c, q, v.Q1, v.O, res, dt * b[0], dt * a[0], s);
   launch_halos<double>(c, v.Q1, s, &c.launches);
-  launch_central_rk<double>(c, cq(v.Q1), v.Q2, v.O, res, res, dt * b[1], dt * a[1], CRK_SKEW | visc | CRK_UPDATE, s,
-                            &c.launches);
+  fwd_stage(c, v.Q1, v.Q2, v.O, res, dt * b[1], dt * a[1], s);
   launch_halos<double>(c, v.Q2, s, &c.launches);
   // reverse
   const dim3 grid((c.g.n0 + 127) / 128, c.g.n1, c.g.n2);

@@ -105,11 +105,106 @@ def test_gradient_matches_finite_differences():
     s.close()
 
 
-@pytest.mark.parametrize("plan", [tgv_plan(16, precision="mixed"), tgv_plan(16, conv="weno5js", Minf=1.25),
+@pytest.mark.parametrize("plan", [tgv_plan(16, precision="mixed"), tgv_plan(16, conv="weno5z", Minf=1.25),
+                                  tgv_plan(16, conv="teno5", Minf=1.25),
                                   tgv_plan(16).replace(bc=(("symmetry", "symmetry"),) * 3)])
 def test_adjoint_rejects_other_plans(plan):
     s = Solver(plan)
     s.init_tgv() if plan.bc[0][0] == "periodic" else None
     with pytest.raises(NotImplementedError):
         s.adjoint_residual(torch.zeros((5,) + s.shape, dtype=torch.float64, device=DEV))
+    s.close()
+
+
+# ---- WENO5-JS: the transposed characteristic flux difference (reverse mode through the Roe average,
+# the eigenvectors, the LLF splitting and the nonlinear weights) plus the viscous adjoint, against
+# central finite differences of the GPU's own FP64 residual and step ----
+
+def _weno_case(n, viscous=True):
+    """A Taylor-Green state with additive momentum noise.  The LLF wave speed max|u_D| over a window
+    is not differentiable where u_D vanishes on the whole window, which the unperturbed Taylor-Green
+    field does on its symmetry lines (u_1 = 0 wherever cos x = 0); there the adjoint takes a one-sided
+    derivative and central differences straddle the kink, so the checks use states without such
+    lines."""
+    plan = tgv_plan(n, conv="weno5js", Minf=1.25, visc="const" if viscous else "none")
+    q = perturbed_state(n, 5, Minf=1.25)
+    g = torch.Generator(device=DEV).manual_seed(8)
+    q[1:4] += 0.05 * q[0] * torch.randn(q[1:4].shape, generator=g, device=DEV, dtype=torch.float64)
+    return plan, q
+
+
+@pytest.mark.parametrize("n,viscous", [((16, 14, 12), True), ((12, 16, 14), False)])
+def test_weno_adjoint_residual_matches_finite_differences(n, viscous):
+    plan, q = _weno_case(n, viscous)
+    lam = torch.randn(q.shape, generator=torch.Generator(device=DEV).manual_seed(6), device=DEV, dtype=torch.float64)
+    s = Solver(plan)
+    s.set_state64(q)
+    adj = s.adjoint_residual(lam)
+    # a small step: the wave speeds are maxima over windows, and a step straddling two nearly equal
+    # candidates sees a kink the adjoint does not
+    h = 1e-7
+    for seed in range(3):
+        v = torch.randn(q.shape, generator=torch.Generator(device=DEV).manual_seed(10 + seed), device=DEV,
+                        dtype=torch.float64) * q.abs().mean(dim=(1, 2, 3), keepdim=True)
+        s.set_state64(q + h * v)
+        rp = s.residual().double()
+        s.set_state64(q - h * v)
+        rm = s.residual().double()
+        fd = float((lam * (rp - rm)).sum() / (2 * h))
+        ad = float((adj * v).sum())
+        assert abs(fd - ad) <= 1e-5 * abs(ad), (seed, fd, ad)
+    s.close()
+
+
+def test_weno_adjoint_step_matches_finite_differences():
+    n, dt = (14, 12, 16), 2e-3
+    plan, q = _weno_case(n)
+    lam = torch.randn(q.shape, generator=torch.Generator(device=DEV).manual_seed(7), device=DEV, dtype=torch.float64)
+    s = Solver(plan)
+    s.set_state64(q)
+    adj = s.adjoint_step(lam, dt)
+    assert torch.equal(s.state64(), q)
+    h = 1e-6
+    for seed in range(3):
+        v = torch.randn(q.shape, generator=torch.Generator(device=DEV).manual_seed(20 + seed), device=DEV,
+                        dtype=torch.float64) * q.abs().mean(dim=(1, 2, 3), keepdim=True)
+        s.set_state64(q + h * v)
+        s.step(1, dt)
+        qp = s.state64()
+        s.set_state64(q - h * v)
+        s.step(1, dt)
+        qm = s.state64()
+        fd = float((lam * (qp - qm)).sum() / (2 * h))
+        ad = float((adj * v).sum())
+        assert abs(fd - ad) <= 1e-6 * abs(ad), (seed, fd, ad)
+    s.close()
+
+
+def test_weno_rollout_gradient_matches_finite_differences():
+    """dJ/du0 of the kinetic energy after 12 WENO5-JS steps at Mach 1.25 through the checkpointed
+    Rollout (every 4 steps), against central differences of the forward solver."""
+    n, nsteps, dt, h = 16, 12, 2e-3, 1e-6
+    plan = tgv_plan(n, conv="weno5js", Minf=1.25)
+    s = Solver(plan)
+    p, rho, base = tgv_base(plan, s.device)
+    # additive noise: no window with u_D = 0 throughout (see _weno_case)
+    base = base + 0.05 * torch.randn(base.shape, generator=torch.Generator(device=DEV).manual_seed(9), device=DEV,
+                                     dtype=torch.float64)
+    v = base.clone().requires_grad_(True)
+    qT = Rollout.apply(state_from_velocity(v, p, rho, plan.gama), s, nsteps, dt, 4)
+    J = kinetic_energy(qT, plan.delta)
+    J.backward()
+    grad = v.grad.detach()
+
+    def J_of(vel):
+        s.set_state64(state_from_velocity(vel, p, rho, plan.gama))
+        s.step(nsteps, dt)
+        return float(kinetic_energy(s.state64(), plan.delta))
+
+    for seed in range(3):
+        d = torch.randn(base.shape, generator=torch.Generator(device=DEV).manual_seed(30 + seed), device=DEV,
+                        dtype=torch.float64)
+        fd = (J_of(base + h * d) - J_of(base - h * d)) / (2 * h)
+        ad = float((grad * d).sum())
+        assert abs(fd - ad) <= 1e-5 * abs(ad), (seed, fd, ad)
     s.close()
