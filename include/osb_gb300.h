@@ -220,9 +220,9 @@ int osb_autotune(osb_ctx *ctx, int reps, double *best_ms);
 int osb_probe(osb_ctx *ctx, int n, const int *what_ijk, double *host_out);
 
 /* Discrete adjoint of the time loop.  No counterpart in the reference.  FP64 3D plans with central
- * skew-symmetric or WENO5-JS fluxes (the latter differentiated through the characteristic projection
- * and the nonlinear weights) and periodic boundaries (viscous terms as the plan says); other plans get
- * OSB_EUNSUPPORTED.  Arrays are device FP64, dense interior [5][n2][n1][n0].
+ * skew-symmetric or characteristic fluxes (WENO5-JS, WENO5-Z, TENO5, TENO6: differentiated through the
+ * characteristic projection and the nonlinear weights; TENO weights held at the cut-off's selection)
+ * and periodic boundaries (viscous terms as the plan says); other plans get OSB_EUNSUPPORTED.  Arrays are device FP64, dense interior [5][n2][n1][n0].
  * osb_adjoint_residual: out = (dR/dq)^T lam at the bound state.
  * osb_adjoint_step: lam_out = (dPhi/dq)^T lam_in, Phi = one 2-register RK3 step of size dt from the
  * bound state, whose stage states are recomputed; the bound state itself is left unchanged.

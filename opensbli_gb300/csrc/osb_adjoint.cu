@@ -19,10 +19,12 @@
 //   s[D2_d u_c] = kappa_c (1 + delta_cd / 3) / Re,   s[D_{min(c,e)} D_{max(c,e)} u_e] = kappa_c / (3 Re),
 //   kappa_c = lambda_{1+c} + lambda_4 u_c.
 // The 2-register RK3 step (schemes/temporal/rk_sbli.py:117-124) is reversed stage by stage from the
-// recomputed stage states.  With WENO5-JS fluxes the convective part is replaced by the transpose of
-// the characteristic flux difference (k_adj_weno, the reverse mode of osb_adjoint_weno.cuh) and the
-// passes above carry the viscous and heat-flux terms only.  Periodic FP64 plans are accepted.
+// recomputed stage states.  With characteristic fluxes (WENO5-JS, WENO5-Z, TENO5, TENO6) the
+// convective part is replaced by the transpose of the flux difference (k_adj_weno, the reverse mode
+// of osb_adjoint_weno.cuh) and the passes above carry the viscous and heat-flux terms only.  Periodic
+// FP64 plans are accepted.
 #include <cstdio>
+#include <type_traits>
 
 #include "osb_adjoint_weno.cuh"
 #include "osb_common.cuh"
@@ -277,7 +279,7 @@ __global__ void k_adj_pass2(Grid g, Fields5<const double> q, Prim5 pr, FieldSet 
 //   F_bar(L) = (lambda_{L+1} [L+1 < n] - lambda_L [L >= 0]) / delta_D,
 // and its window's six points receive (dF/dQ)^T F_bar, folded back onto their periodic images.  One
 // thread per interface; the contributions of the six interfaces sharing a point meet in FP64 atomics.
-template <int D>
+template <int D, int SCH>
 __global__ void k_adj_weno(Grid g, Fields5<const double> q, FieldSet A, Phys ph, double *out, double scale) {
   const int nd = D == 0 ? g.n0 : D == 1 ? g.n1 : g.n2;
   const int na = D == 0 ? g.n1 : g.n0, nb = D == 2 ? g.n1 : g.n2;  // transverse extents
@@ -309,7 +311,7 @@ __global__ void k_adj_weno(Grid g, Fields5<const double> q, FieldSet A, Phys ph,
         Q[t][v] = q.v[v][nL + (int64_t)(t - 2) * sd];
         Qb[t][v] = 0.0;
       }
-    adjw::interface_flux_adj<D>(Q, Fb, ph.gama, Qb, nullptr, ph.weno_eps);
+    adjw::interface_flux_adj<D, SCH>(Q, Fb, ph.gama, Qb, nullptr, ph.weno_eps, ph.teno_ct);
 #pragma unroll
     for (int t = 0; t < 6; ++t) {
       const int c = ((L - 2 + t) % nd + nd) % nd;
@@ -457,12 +459,21 @@ void adj_rhs(Ctx &c, const AdjView &v, Fields5<double> qs, double *out, double s
   adj_halos(c, v.A.f, NA_HALO, s, &c.launches);
   k_adj_pass2<<<grid, 128, 0, s>>>(c.g, cq(qs), v.pr, v.A, ph, out, scale, conv);
   c.launches += 3;
-  if (!conv) {  // WENO5-JS fluxes: their transposes, added into out
+  if (!conv) {  // characteristic fluxes: their transposes, added into out
     const int64_t per = (int64_t)c.g.n0 * c.g.n1 * c.g.n2;
     const int nb = grid_blocks(per + per / 8 + 1);
-    k_adj_weno<0><<<nb, 128, 0, s>>>(c.g, cq(qs), v.A, ph, out, scale);
-    k_adj_weno<1><<<nb, 128, 0, s>>>(c.g, cq(qs), v.A, ph, out, scale);
-    k_adj_weno<2><<<nb, 128, 0, s>>>(c.g, cq(qs), v.A, ph, out, scale);
+    auto launch = [&](auto sch) {
+      constexpr int S = decltype(sch)::value;
+      k_adj_weno<0, S><<<nb, 128, 0, s>>>(c.g, cq(qs), v.A, ph, out, scale);
+      k_adj_weno<1, S><<<nb, 128, 0, s>>>(c.g, cq(qs), v.A, ph, out, scale);
+      k_adj_weno<2, S><<<nb, 128, 0, s>>>(c.g, cq(qs), v.A, ph, out, scale);
+    };
+    switch (c.plan.conv) {
+      case OSB_CONV_WENO5Z: launch(std::integral_constant<int, adjw::ADJ_Z>{}); break;
+      case OSB_CONV_TENO5: launch(std::integral_constant<int, adjw::ADJ_TENO5>{}); break;
+      case OSB_CONV_TENO6: launch(std::integral_constant<int, adjw::ADJ_TENO6>{}); break;
+      default: launch(std::integral_constant<int, adjw::ADJ_JS>{}); break;
+    }
     c.launches += 3;
   }
 }

@@ -1,11 +1,13 @@
-// osb_adjoint_weno.cuh -- reverse mode of the FP64 characteristic WENO5-JS interface flux
-// (osb_weno.cuh::interface_flux, FP64 branch, with point_prims): given the adjoint F_bar of the flux
-// F_{i+1/2}, the contributions (dF/dQ_t)^T F_bar to the six conserved vectors of its window.
+// osb_adjoint_weno.cuh -- reverse mode of the FP64 characteristic interface flux
+// (osb_weno.cuh::interface_flux, FP64 branch, with point_prims) for WENO5-JS, WENO5-Z, TENO5 and
+// TENO6: given the adjoint F_bar of the flux F_{i+1/2}, the contributions (dF/dQ_t)^T F_bar to the six
+// conserved vectors of its window.
 //
 // The forward quantities are recomputed in the same order and then swept backwards.  The LLF wave
 // speeds are maxima over the window: their derivative goes to the first point attaining the maximum
-// (the forward keeps the earlier of equal values), with the sign of the absolute value.  WENO5-JS
-// weights are smooth, so the nonlinear weights are differentiated exactly.
+// (the forward keeps the earlier of equal values), with the sign of the absolute value.  The WENO
+// weights are smooth and differentiated exactly; the TENO cut-off is a step function of the
+// indicators, so between switches the TENO weights are constants and only the candidates vary.
 // Plain C++ apart from the qualifiers, so the host compiler can check it against finite differences.
 #pragma once
 #include <math.h>
@@ -21,78 +23,175 @@ namespace adjw {
 
 constexpr double EPS_JS = 1e-6;
 
-// one WENO5-JS side (weno5_side<double, SCH_JS>): forward value
-OSB_ADJ_HD double side(const double f[5], double eps) {
+// Schemes, numbered as the flux kernels number them: WENO5-JS, WENO5-Z, TENO5, TENO6.
+enum { ADJ_JS = 0, ADJ_Z = 1, ADJ_TENO5 = 2, ADJ_TENO6 = 3 };
+
+// The nonlinear weights of one side as the FP64 flux kernels form them (osb_weno.cuh: weno5_side,
+// teno5_side, teno6_side).  f[0..5] run from the far upwind point to one past the far downwind one;
+// the 5-point schemes use f[0..4].  Returns the reconstruction; w[0..3] receive the weights of the
+// candidate differences (see below) and W their normaliser, so that
+//   y = p1 + (w[0] (-(t0 - t1)/12) + w[1] ((t2 - t1)/6) + w[2] ((-2 d1 + 5 d2 - 4 d3 + d4)/24)) / W.
+// WENO: w = (a0, a2, 0) and W = a0 + a1 + a2 depend smoothly on f; TENO: w and W are the cut-off's
+// selections of the optimal weights, constant between switches.
+template <int SCH>
+OSB_ADJ_HD double side_weights(const double f[6], bool plus, double eps, double ct, double w[3], double &W) {
   const double d0 = f[1] - f[0], d1 = f[2] - f[1], d2 = f[3] - f[2], d3 = f[4] - f[3];
   const double t0 = d3 - d2, t1 = d2 - d1, t2 = d1 - d0;
   const double s0 = d3 - 3.0 * d2, s1 = d1 + d2, s2 = 3.0 * d1 - d0;
   const double c13 = 13.0 / 48.0, c14 = 1.0 / 16.0;
-  const double e0 = c13 * t0 * t0 + c14 * s0 * s0 + eps, e1 = c13 * t1 * t1 + c14 * s1 * s1 + eps,
-               e2 = c13 * t2 * t2 + c14 * s2 * s2 + eps;
-  const double q0 = e0 * e0, q1 = e1 * e1, q2 = e2 * e2;
-  const double a0 = 0.3 * q1 * q2, a1 = 0.6 * q0 * q2, a2 = 0.1 * q0 * q1;
+  const double b0 = c13 * t0 * t0 + c14 * s0 * s0, b1 = c13 * t1 * t1 + c14 * s1 * s1,
+               b2 = c13 * t2 * t2 + c14 * s2 * s2;
+  w[2] = 0.0;
+  if (SCH == ADJ_JS || SCH == ADJ_Z) {
+    const double q0 = (b0 + eps) * (b0 + eps), q1 = (b1 + eps) * (b1 + eps), q2 = (b2 + eps) * (b2 + eps);
+    const double tt = SCH == ADJ_Z ? (b0 - b2) * (b0 - b2) : 0.0;
+    const double a0 = SCH == ADJ_Z ? 0.3 * (q0 + tt) * (q1 * q2) : 0.3 * q1 * q2;
+    const double a1 = SCH == ADJ_Z ? 0.6 * (q1 + tt) * (q0 * q2) : 0.6 * q0 * q2;
+    const double a2 = SCH == ADJ_Z ? 0.1 * (q2 + tt) * (q0 * q1) : 0.1 * q0 * q1;
+    w[0] = a0;
+    w[1] = a2;
+    W = a0 + a1 + a2;
+  } else {
+    // TENO: indicators central b1, downwind b0, upwind b2 (+ the four-point one for TENO6)
+    double m[4], tau;
+    int nr = 3;
+    double b4 = 0.0;
+    if (SCH == ADJ_TENO6) {
+      const double d4 = f[5] - f[4];
+      const double A = 11.0 * d2 - 7.0 * d3 + 2.0 * d4, B = 3.0 * d3 - 2.0 * d2 - d4, C = d2 - 2.0 * d3 + d4;
+      b4 = (1.0 / 144.0) * A * A + c13 * B * B + (plus ? (781.0 / 1440.0) * C : (781.0 / 2880.0) * C * C);
+      tau = fabs((1.0 / 6.0) * (b1 + b2) - (2.0 / 3.0) * b0 - b4);
+      nr = 4;
+    } else {
+      tau = fabs(b1 - b2);
+    }
+    const double bb[4] = {b1, b0, b2, b4};  // central, downwind, upwind, four-point
+    double mm = 0.0;
+    for (int r = 0; r < nr; ++r) {
+      m[r] = 1.0 + tau * (1.0 / (eps + bb[r]));
+      mm = fmax(mm, fabs(m[r]));
+    }
+    const double im = 1.0 / mm;
+    double q[4], qs = 0.0;
+    for (int r = 0; r < nr; ++r) {
+      const double n = m[r] * im;
+      q[r] = (n * n) * (n * n) * (n * n);
+    }
+    qs = nr == 4 ? (q[0] + q[1]) + (q[2] + q[3]) : q[0] + q[1] + q[2];
+    const double iq = 1.0 / qs;
+    const double dw5[3] = {11.0 / 20.0, 2.0 / 5.0, 1.0 / 20.0}, dw6[4] = {231.0 / 500.0, 3.0 / 10.0, 27.0 / 500.0, 23.0 / 125.0};
+    double wr[4];
+    for (int r = 0; r < nr; ++r) wr[r] = ct > q[r] * iq ? 0.0 : (nr == 4 ? dw6[r] : dw5[r]);
+    w[0] = wr[1];  // downwind
+    w[1] = wr[2];  // upwind
+    w[2] = nr == 4 ? wr[3] : 0.0;
+    W = nr == 4 ? (wr[0] + wr[1]) + (wr[2] + wr[3]) : wr[0] + wr[1] + wr[2];
+  }
   const double p1 = 0.5 * f[2] + d1 / 12.0 + d2 / 6.0;
-  return p1 + (-a0 * (t0 - t1) / 12.0 + a2 * (t2 - t1) / 6.0) / (a0 + a1 + a2);
+  const double c3 = SCH == ADJ_TENO6 ? (5.0 * d2 - 2.0 * d1 - 4.0 * d3 + (f[5] - f[4])) / 24.0 : 0.0;
+  return p1 + (w[0] * (-(t0 - t1) / 12.0) + w[1] * ((t2 - t1) / 6.0) + w[2] * c3) / W;
 }
 
-// its reverse: fb[k] += d(side)/df_k * yb
-OSB_ADJ_HD void side_adj(const double f[5], double yb, double eps, double fb[5]) {
+template <int SCH> OSB_ADJ_HD double side(const double f[6], bool plus, double eps, double ct) {
+  double w[3], W;
+  return side_weights<SCH>(f, plus, eps, ct, w, W);
+}
+
+// reverse of one side: fb[k] += d(side)/df_k * yb (TENO weights held at their selection)
+template <int SCH>
+OSB_ADJ_HD void side_adj(const double f[6], bool plus, double yb, double eps, double ct, double fb[6]) {
   const double d0 = f[1] - f[0], d1 = f[2] - f[1], d2 = f[3] - f[2], d3 = f[4] - f[3];
   const double t0 = d3 - d2, t1 = d2 - d1, t2 = d1 - d0;
-  const double s0 = d3 - 3.0 * d2, s1 = d1 + d2, s2 = 3.0 * d1 - d0;
-  const double c13 = 13.0 / 48.0, c14 = 1.0 / 16.0;
-  const double e0 = c13 * t0 * t0 + c14 * s0 * s0 + eps, e1 = c13 * t1 * t1 + c14 * s1 * s1 + eps,
-               e2 = c13 * t2 * t2 + c14 * s2 * s2 + eps;
-  const double q0 = e0 * e0, q1 = e1 * e1, q2 = e2 * e2;
-  const double a0 = 0.3 * q1 * q2, a1 = 0.6 * q0 * q2, a2 = 0.1 * q0 * q1;
   const double D0 = t0 - t1, D2 = t2 - t1;
-  const double iS = 1.0 / (a0 + a1 + a2);
-  const double N = -a0 * D0 / 12.0 + a2 * D2 / 6.0;
-  const double Nb = yb * iS, Sb = -yb * N * iS * iS;
-  const double a0b = Nb * (-D0 / 12.0) + Sb, a2b = Nb * (D2 / 6.0) + Sb, a1b = Sb;
-  const double D0b = Nb * (-a0 / 12.0), D2b = Nb * (a2 / 6.0);
-  const double q0b = a1b * 0.6 * q2 + a2b * 0.1 * q1;
-  const double q1b = a0b * 0.3 * q2 + a2b * 0.1 * q0;
-  const double q2b = a0b * 0.3 * q1 + a1b * 0.6 * q0;
-  const double b0b = 2.0 * e0 * q0b, b1b = 2.0 * e1 * q1b, b2b = 2.0 * e2 * q2b;
-  const double t0b = 2.0 * c13 * t0 * b0b + D0b, s0b = 2.0 * c14 * s0 * b0b;
-  const double t1b = 2.0 * c13 * t1 * b1b - D0b - D2b, s1b = 2.0 * c14 * s1 * b1b;
-  const double t2b = 2.0 * c13 * t2 * b2b + D2b, s2b = 2.0 * c14 * s2 * b2b;
-  const double d3b = s0b + t0b;
-  const double d2b = yb / 6.0 - 3.0 * s0b + s1b - t0b + t1b;
-  const double d1b = yb / 12.0 + s1b + 3.0 * s2b - t1b + t2b;
-  const double d0b = -s2b - t2b;
+  const double d4 = SCH == ADJ_TENO6 ? f[5] - f[4] : 0.0;
+  double w[3], W;
+  side_weights<SCH>(f, plus, eps, ct, w, W);
+  const double c3 = SCH == ADJ_TENO6 ? (5.0 * d2 - 2.0 * d1 - 4.0 * d3 + d4) / 24.0 : 0.0;
+  const double iW = 1.0 / W;
+  const double N = w[0] * (-D0 / 12.0) + w[1] * (D2 / 6.0) + w[2] * c3;
+  // y = p1 + N / W
+  double D0b = yb * iW * (-w[0] / 12.0), D2b = yb * iW * (w[1] / 6.0);
+  const double c3b = yb * iW * w[2];
+  double t0b = D0b, t1b = -D0b - D2b, t2b = D2b;
+  double d0b = 0, d1b = yb / 12.0, d2b = yb / 6.0, d3b = 0, d4b = 0;
+  d1b += -2.0 / 24.0 * c3b;
+  d2b += 5.0 / 24.0 * c3b;
+  d3b += -4.0 / 24.0 * c3b;
+  d4b += 1.0 / 24.0 * c3b;
+  if (SCH == ADJ_JS || SCH == ADJ_Z) {
+    // smooth weights: w0 = a0, w1 = a2, W = a0 + a1 + a2
+    const double s0 = d3 - 3.0 * d2, s1 = d1 + d2, s2 = 3.0 * d1 - d0;
+    const double c13 = 13.0 / 48.0, c14 = 1.0 / 16.0;
+    const double b0 = c13 * t0 * t0 + c14 * s0 * s0, b1 = c13 * t1 * t1 + c14 * s1 * s1,
+                 b2 = c13 * t2 * t2 + c14 * s2 * s2;
+    const double e0 = b0 + eps, e1 = b1 + eps, e2 = b2 + eps;
+    const double q0 = e0 * e0, q1 = e1 * e1, q2 = e2 * e2;
+    const double Wb = -yb * N * iW * iW;
+    const double a0b = yb * iW * (-D0 / 12.0) + Wb, a2b = yb * iW * (D2 / 6.0) + Wb, a1b = Wb;
+    double q0b, q1b, q2b, b0b = 0, b2b = 0;
+    if (SCH == ADJ_Z) {
+      const double tt = (b0 - b2) * (b0 - b2);
+      // a0 = 0.3 (q0 + tt) q1 q2, a1 = 0.6 (q1 + tt) q0 q2, a2 = 0.1 (q2 + tt) q0 q1
+      q0b = a0b * 0.3 * q1 * q2 + a1b * 0.6 * (q1 + tt) * q2 + a2b * 0.1 * (q2 + tt) * q1;
+      q1b = a0b * 0.3 * (q0 + tt) * q2 + a1b * 0.6 * q0 * q2 + a2b * 0.1 * (q2 + tt) * q0;
+      q2b = a0b * 0.3 * (q0 + tt) * q1 + a1b * 0.6 * (q1 + tt) * q0 + a2b * 0.1 * q0 * q1;
+      const double ttb = a0b * 0.3 * q1 * q2 + a1b * 0.6 * q0 * q2 + a2b * 0.1 * q0 * q1;
+      b0b += 2.0 * (b0 - b2) * ttb;
+      b2b -= 2.0 * (b0 - b2) * ttb;
+    } else {
+      q0b = a1b * 0.6 * q2 + a2b * 0.1 * q1;
+      q1b = a0b * 0.3 * q2 + a2b * 0.1 * q0;
+      q2b = a0b * 0.3 * q1 + a1b * 0.6 * q0;
+    }
+    b0b += 2.0 * e0 * q0b;
+    const double b1b = 2.0 * e1 * q1b;
+    b2b += 2.0 * e2 * q2b;
+    t0b += 2.0 * c13 * t0 * b0b;
+    t1b += 2.0 * c13 * t1 * b1b;
+    t2b += 2.0 * c13 * t2 * b2b;
+    const double s0b = 2.0 * c14 * s0 * b0b, s1b = 2.0 * c14 * s1 * b1b, s2b = 2.0 * c14 * s2 * b2b;
+    d3b += s0b;
+    d2b += -3.0 * s0b + s1b;
+    d1b += s1b + 3.0 * s2b;
+    d0b += -s2b;
+  }
+  // t0 = d3 - d2, t1 = d2 - d1, t2 = d1 - d0
+  d3b += t0b;
+  d2b += -t0b + t1b;
+  d1b += -t1b + t2b;
+  d0b += -t2b;
   fb[0] -= d0b;
   fb[1] += d0b - d1b;
   fb[2] += d1b - d2b + 0.5 * yb;
   fb[3] += d2b - d3b;
-  fb[4] += d3b;
+  fb[4] += d3b - d4b;
+  fb[5] += d4b;
 }
 
-// one characteristic row: forward reconstruction of f+- = cf +- lam cs, both sides
-OSB_ADJ_HD double recon(const double cf[6], const double cs[6], double lam, double eps) {
-  double fp[5], fm[5];
-#pragma unroll
-  for (int t = 0; t < 5; ++t) {
+// one characteristic row: the + side on f+ = cf + lam cs at points 0..5, the - side on
+// f- = cf - lam cs at points 5..0
+template <int SCH>
+OSB_ADJ_HD double recon(const double cf[6], const double cs[6], double lam, double eps, double ct) {
+  double fp[6], fm[6];
+  for (int t = 0; t < 6; ++t) {
     fp[t] = cf[t] + lam * cs[t];
     fm[t] = cf[5 - t] - lam * cs[5 - t];
   }
-  return side(fp, eps) + side(fm, eps);
+  return side<SCH>(fp, true, eps, ct) + side<SCH>(fm, false, eps, ct);
 }
 
 // its reverse: cfb, csb (6 points) and lamb accumulated
-OSB_ADJ_HD void recon_adj(const double cf[6], const double cs[6], double lam, double yb, double eps,
-                                          double cfb[6], double csb[6], double &lamb) {
-  double fp[5], fm[5], fpb[5] = {0, 0, 0, 0, 0}, fmb[5] = {0, 0, 0, 0, 0};
-#pragma unroll
-  for (int t = 0; t < 5; ++t) {
+template <int SCH>
+OSB_ADJ_HD void recon_adj(const double cf[6], const double cs[6], double lam, double yb, double eps, double ct,
+                          double cfb[6], double csb[6], double &lamb) {
+  double fp[6], fm[6], fpb[6] = {0, 0, 0, 0, 0, 0}, fmb[6] = {0, 0, 0, 0, 0, 0};
+  for (int t = 0; t < 6; ++t) {
     fp[t] = cf[t] + lam * cs[t];
     fm[t] = cf[5 - t] - lam * cs[5 - t];
   }
-  side_adj(fp, yb, eps, fpb);
-  side_adj(fm, yb, eps, fmb);
-#pragma unroll
-  for (int t = 0; t < 5; ++t) {
+  side_adj<SCH>(fp, true, yb, eps, ct, fpb);
+  side_adj<SCH>(fm, false, yb, eps, ct, fmb);
+  for (int t = 0; t < 6; ++t) {
     cfb[t] += fpb[t];
     csb[t] += lam * fpb[t];
     lamb += cs[t] * fpb[t];
@@ -104,9 +203,10 @@ OSB_ADJ_HD void recon_adj(const double cf[6], const double cs[6], double lam, do
 
 // Q[t][v]: conserved vectors of window points i-2 .. i+3 (interface between 2 and 3); Fb: adjoint of
 // the interface flux; Qb[t][v] += (dF/dQ_t)^T Fb.  F, if given, receives the forward flux.
-template <int D>
+template <int D, int SCH = ADJ_JS>
 OSB_ADJ_HD void interface_flux_adj(const double (&Q)[6][5], const double (&Fb)[5], double gama,
-                                            double (&Qb)[6][5], double *F = nullptr, double eps = EPS_JS) {
+                                            double (&Qb)[6][5], double *F = nullptr, double eps = EPS_JS,
+                                            double ct = 0.0) {
   constexpr int E1 = (D + 1) % 3, E2 = (D + 2) % 3;
   constexpr int e1 = 3 - E1 - D, e2 = 3 - E2 - D;
   const double gm1 = gama - 1.0, igm1 = 1.0 / gm1, S2 = 0.70710678118654752440;
@@ -168,8 +268,9 @@ OSB_ADJ_HD void interface_flux_adj(const double (&Q)[6][5], const double (&Fb)[5
     cf4[t] = bt * gF[t] - btA * hF[t];
     cs4[t] = bt * gQ[t] - btA * hQ[t];
   }
-  const double rE1 = recon(cfE1, csE1, lu, eps), rE2 = recon(cfE2, csE2, lu, eps);
-  const double rD = recon(cfD, csD, lu, eps), r3 = recon(cf3, cs3, lp, eps), r4 = recon(cf4, cs4, lm, eps);
+  const double rE1 = recon<SCH>(cfE1, csE1, lu, eps, ct), rE2 = recon<SCH>(cfE2, csE2, lu, eps, ct);
+  const double rD = recon<SCH>(cfD, csD, lu, eps, ct), r3 = recon<SCH>(cf3, cs3, lp, eps, ct),
+               r4 = recon<SCH>(cf4, cs4, lm, eps, ct);
   const double sac = r3 + r4, dac = r3 - r4, hh = (phi + a * a) * igm1;
   if (F) {
     F[0] = rD + al * sac;
@@ -219,11 +320,11 @@ OSB_ADJ_HD void interface_flux_adj(const double (&Q)[6][5], const double (&Fb)[5
   double cfE1b[6] = {}, csE1b[6] = {}, cfE2b[6] = {}, csE2b[6] = {}, cfDb[6] = {}, csDb[6] = {};
   double cf3b[6] = {}, cs3b[6] = {}, cf4b[6] = {}, cs4b[6] = {};
   double lub = 0, lpb = 0, lmb = 0;
-  recon_adj(cf4, cs4, lm, r4b, eps, cf4b, cs4b, lmb);
-  recon_adj(cf3, cs3, lp, r3b, eps, cf3b, cs3b, lpb);
-  recon_adj(cfD, csD, lu, rDb, eps, cfDb, csDb, lub);
-  recon_adj(cfE1, csE1, lu, rE1b, eps, cfE1b, csE1b, lub);
-  recon_adj(cfE2, csE2, lu, rE2b, eps, cfE2b, csE2b, lub);
+  recon_adj<SCH>(cf4, cs4, lm, r4b, eps, ct, cf4b, cs4b, lmb);
+  recon_adj<SCH>(cf3, cs3, lp, r3b, eps, ct, cf3b, cs3b, lpb);
+  recon_adj<SCH>(cfD, csD, lu, rDb, eps, ct, cfDb, csDb, lub);
+  recon_adj<SCH>(cfE1, csE1, lu, rE1b, eps, ct, cfE1b, csE1b, lub);
+  recon_adj<SCH>(cfE2, csE2, lu, rE2b, eps, ct, cfE2b, csE2b, lub);
   // ---- reverse: projections
   double btb = 0, btAb = 0, ia2b = 0, srb1 = 0, srb2 = 0;
   double udb[6] = {}, pb[6] = {}, atb[6] = {};

@@ -1083,8 +1083,8 @@ extern "C" {
 static int adjoint_check(osb_ctx *c) {
   if (!c) return OSB_EINVAL;
   const osb_plan_desc &p = c->plan;
-  if (p.ndim != 3 || c->mixed || (p.conv != OSB_CONV_CENTRAL_SKEW && p.conv != OSB_CONV_WENO5JS))
-    return set_err(c, OSB_EUNSUPPORTED, "adjoint: FP64 3D plans with central skew-symmetric or WENO5-JS fluxes only");
+  if (p.ndim != 3 || c->mixed || (p.conv != OSB_CONV_CENTRAL_SKEW && !char_fluxes(p)))
+    return set_err(c, OSB_EUNSUPPORTED, "adjoint: FP64 3D plans with central or characteristic fluxes only");
   for (int d = 0; d < 3; ++d)
     if (p.bc[d][0] != OSB_BC_PERIODIC || p.bc[d][1] != OSB_BC_PERIODIC)
       return set_err(c, OSB_EUNSUPPORTED, "adjoint: periodic boundaries only");

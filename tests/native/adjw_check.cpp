@@ -1,7 +1,7 @@
-// Checks the reverse mode of the FP64 characteristic WENO5-JS interface flux
+// Checks the reverse mode of the FP64 characteristic interface flux
 // (opensbli_gb300/csrc/osb_adjoint_weno.cuh) against central finite differences of its own forward
-// flux, for all three directions on random smooth windows and windows with a jump.  Prints the
-// worst relative error and the number of windows checked.
+// flux, for WENO5-JS, WENO5-Z, TENO5 and TENO6, all three directions, on random smooth windows and
+// windows with a jump.  Prints the worst relative error per scheme and the number of windows.
 #include <math.h>
 #include <stdio.h>
 
@@ -9,7 +9,7 @@
 
 #include "osb_adjoint_weno.cuh"
 
-template <int D> static double check(std::mt19937_64 &rng, bool jump) {
+template <int D, int SCH> static double check(std::mt19937_64 &rng, bool jump) {
   std::normal_distribution<double> N(0.0, 1.0);
   std::uniform_real_distribution<double> U(0.0, 1.0);
   const double g = 1.4;
@@ -31,9 +31,15 @@ template <int D> static double check(std::mt19937_64 &rng, bool jump) {
   double Fb[5];
   for (int v = 0; v < 5; ++v) Fb[v] = N(rng);
   double Qb[6][5] = {};
-  osb::adjw::interface_flux_adj<D>(Q, Fb, g, Qb);
+  // WENO5-Z is checked with eps = 1e-6: with the reference's 1e-14 its weights are so ill-conditioned
+  // on smooth windows that central differences cannot resolve them (the formula does not depend on eps)
+  const double eps = SCH >= 2 ? 1e-15 : 1e-6, ct = 1e-5;
+  osb::adjw::interface_flux_adj<D, SCH>(Q, Fb, g, Qb, nullptr, eps, ct);
+  // the smallest error over three steps: a TENO cut-off switch straddled by one step is not straddled
+  // by all three
+  double best = 1e300;
+  for (double h : {1e-5, 1e-6, 1e-7}) {
   double worst = 0, scale = 0;
-  const double h = 1e-6;
   double fd[6][5];
   for (int t = 0; t < 6; ++t)
     for (int v = 0; v < 5; ++v) {
@@ -43,8 +49,8 @@ template <int D> static double check(std::mt19937_64 &rng, bool jump) {
         for (int b = 0; b < 5; ++b) Qp[a][b] = Qm[a][b] = Q[a][b];
       Qp[t][v] += h;
       Qm[t][v] -= h;
-      osb::adjw::interface_flux_adj<D>(Qp, z, g, dummy, Fp);
-      osb::adjw::interface_flux_adj<D>(Qm, z, g, dummy, Fm);
+      osb::adjw::interface_flux_adj<D, SCH>(Qp, z, g, dummy, Fp, eps, ct);
+      osb::adjw::interface_flux_adj<D, SCH>(Qm, z, g, dummy, Fm, eps, ct);
       double s = 0;
       for (int k = 0; k < 5; ++k) s += (Fp[k] - Fm[k]) * Fb[k];
       fd[t][v] = s / (2 * h);
@@ -52,20 +58,29 @@ template <int D> static double check(std::mt19937_64 &rng, bool jump) {
     }
   for (int t = 0; t < 6; ++t)
     for (int v = 0; v < 5; ++v) worst = fmax(worst, fabs(fd[t][v] - Qb[t][v]));
-  return worst / scale;
+  best = fmin(best, worst / scale);
+  }
+  return best;
 }
 
-int main() {
-  std::mt19937_64 rng(7);
+template <int SCH> static double scheme(std::mt19937_64 &rng, int &n) {
   double worst = 0;
-  int n = 0;
   for (int k = 0; k < 300; ++k) {
     const bool jump = k % 4 == 3;
-    worst = fmax(worst, check<0>(rng, jump));
-    worst = fmax(worst, check<1>(rng, jump));
-    worst = fmax(worst, check<2>(rng, jump));
+    worst = fmax(worst, check<0, SCH>(rng, jump));
+    worst = fmax(worst, check<1, SCH>(rng, jump));
+    worst = fmax(worst, check<2, SCH>(rng, jump));
     n += 3;
   }
-  printf("%.3e %d\n", worst, n);
+  return worst;
+}
+
+// one line per scheme (WENO5-JS, WENO5-Z, TENO5, TENO6): worst relative error, windows checked
+int main() {
+  std::mt19937_64 rng(7);
+  int n = 0;
+  const double w[4] = {scheme<0>(rng, n), scheme<1>(rng, n), scheme<2>(rng, n), scheme<3>(rng, n)};
+  for (int s = 0; s < 4; ++s) printf("%d %.3e\n", s, w[s]);
+  printf("windows %d\n", n);
   return 0;
 }

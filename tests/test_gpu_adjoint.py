@@ -105,8 +105,8 @@ def test_gradient_matches_finite_differences():
     s.close()
 
 
-@pytest.mark.parametrize("plan", [tgv_plan(16, precision="mixed"), tgv_plan(16, conv="weno5z", Minf=1.25),
-                                  tgv_plan(16, conv="teno5", Minf=1.25),
+@pytest.mark.parametrize("plan", [tgv_plan(16, precision="mixed"), tgv_plan(16, conv="weno5js", Minf=1.25,
+                                                                       precision="mixed"),
                                   tgv_plan(16).replace(bc=(("symmetry", "symmetry"),) * 3)])
 def test_adjoint_rejects_other_plans(plan):
     s = Solver(plan)
@@ -120,13 +120,13 @@ def test_adjoint_rejects_other_plans(plan):
 # the eigenvectors, the LLF splitting and the nonlinear weights) plus the viscous adjoint, against
 # central finite differences of the GPU's own FP64 residual and step ----
 
-def _weno_case(n, viscous=True):
+def _weno_case(n, viscous=True, conv="weno5js"):
     """A Taylor-Green state with additive momentum noise.  The LLF wave speed max|u_D| over a window
     is not differentiable where u_D vanishes on the whole window, which the unperturbed Taylor-Green
     field does on its symmetry lines (u_1 = 0 wherever cos x = 0); there the adjoint takes a one-sided
     derivative and central differences straddle the kink, so the checks use states without such
     lines."""
-    plan = tgv_plan(n, conv="weno5js", Minf=1.25, visc="const" if viscous else "none")
+    plan = tgv_plan(n, conv=conv, Minf=1.25, visc="const" if viscous else "none")
     q = perturbed_state(n, 5, Minf=1.25)
     g = torch.Generator(device=DEV).manual_seed(8)
     q[1:4] += 0.05 * q[0] * torch.randn(q[1:4].shape, generator=g, device=DEV, dtype=torch.float64)
@@ -207,4 +207,29 @@ def test_weno_rollout_gradient_matches_finite_differences():
         fd = (J_of(base + h * d) - J_of(base - h * d)) / (2 * h)
         ad = float((grad * d).sum())
         assert abs(fd - ad) <= 1e-5 * abs(ad), (seed, fd, ad)
+    s.close()
+
+
+@pytest.mark.parametrize("conv,tol", [("weno5z", 1e-4), ("teno5", 1e-5), ("teno6", 1e-5)])
+def test_characteristic_adjoint_residual_matches_finite_differences(conv, tol):
+    """WENO5-Z (its eps = 1e-14 makes the weights too ill-conditioned on smooth data for central
+    differences to resolve them closely, hence the looser bar) and TENO5/TENO6 (weights constant between
+    cut-off switches; the smaller of two steps' errors, since a step may straddle a switch)."""
+    plan, q = _weno_case((14, 12, 16), True, conv)
+    lam = torch.randn(q.shape, generator=torch.Generator(device=DEV).manual_seed(11), device=DEV, dtype=torch.float64)
+    s = Solver(plan)
+    s.set_state64(q)
+    adj = s.adjoint_residual(lam)
+    for seed in range(3):
+        v = torch.randn(q.shape, generator=torch.Generator(device=DEV).manual_seed(40 + seed), device=DEV,
+                        dtype=torch.float64) * q.abs().mean(dim=(1, 2, 3), keepdim=True)
+        ad = float((adj * v).sum())
+        errs = []
+        for h in (1e-6, 1e-7):
+            s.set_state64(q + h * v)
+            rp = s.residual().double()
+            s.set_state64(q - h * v)
+            rm = s.residual().double()
+            errs.append(abs(float((lam * (rp - rm)).sum() / (2 * h)) - ad) / abs(ad))
+        assert min(errs) <= tol, (conv, seed, errs)
     s.close()
