@@ -25,7 +25,7 @@ def main():
     import torch
     from .plan import tgv_plan, tgv_cfl_dt
     from .runtime import Solver
-    M = 1.25 if a.conv.startswith("weno") else 0.1
+    M = 0.1 if a.conv == "central_skew" else 1.25
     plan = tgv_plan(a.n, conv=a.conv, Minf=M, precision=a.precision, use_graphs=not a.no_graphs)
     dt = tgv_cfl_dt(plan)
     s = Solver(plan)
