@@ -136,9 +136,12 @@ int osb_set_state64_padded(osb_ctx *ctx, int var, const double *dev_padded, int 
  * mirrored halos, SD111 = dD11/dxi1 (equation_types/metric.py:37-234, 315-332). */
 int osb_set_coordinate(osb_ctx *ctx, int axis, const double *dev_padded, int h);
 
-/* Set / read the FP64 master copy of variable `var` from / into a device array of n0*n1*n2 doubles
- * laid out [z][y][x] (interior only); setting also refreshes the bound state.  In FP64 mode the
- * master copy is the state itself; in mixed mode it is the FP64 RK accumulator. */
+/* Set / read the FP64 master copy of variable `var` from / into an array of n0*n1*n2 doubles laid
+ * out [z][y][x] (interior only); setting also refreshes the bound state.  In FP64 mode the master copy
+ * is the state itself; in mixed mode it is the FP64 RK accumulator.  The array may be device memory
+ * or page-locked host memory (cudaHostAlloc / cudaHostRegister), which the kernels then read or write
+ * over the host link without a staging copy; other host memory gets OSB_EINVAL.  Stream-ordered: a
+ * host array must stay valid until the stream has passed the call. */
 int osb_set_state64(osb_ctx *ctx, int var, const double *dev_interior);
 int osb_get_state64(osb_ctx *ctx, int var, double *dev_interior);
 

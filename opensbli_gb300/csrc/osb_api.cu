@@ -766,10 +766,27 @@ int osb_init_tgv(osb_ctx *c) {
   return cuda_err(c, cudaGetLastError(), "osb_init_tgv");
 }
 
+// The address a kernel may use for p: device and managed memory as they are, page-locked host
+// memory (cudaHostAlloc / cudaHostRegister, which unified addressing maps into the device's address
+// space) through its device pointer, so that the kernels read or write it over the host link without
+// a staging copy; nullptr for memory the device cannot reach (pageable host memory).
+static const void *device_access(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return p;
+  if (a.type == cudaMemoryTypeHost && a.devicePointer) return a.devicePointer;
+  return nullptr;
+}
+
 int osb_set_state64(osb_ctx *c, int var, const double *src) {
   if (!c) return OSB_EINVAL;
   if (int rc = check_bound(c)) return rc;
   if (var < 0 || var >= c->nvar || !src) return set_err(c, OSB_EINVAL, "bad var or pointer");
+  src = static_cast<const double *>(device_access(src));
+  if (!src) return set_err(c, OSB_EINVAL, "osb_set_state64: source is neither device nor page-locked host memory");
   const int nb = blocks_for((int64_t)c->g.n0 * c->g.n1 * c->g.n2);
   if (c->plan.ndim == 2) {
     if (c->mixed) k_set64<float><<<nb, 256, 0, c->stream>>>(c->g, src, (float *)c->qa[var], c->q64_2d[var]);
@@ -851,6 +868,8 @@ int osb_probe(osb_ctx *c, int n, const int *what_ijk, double *host_out) {
 int osb_get_state64(osb_ctx *c, int var, double *dst) {
   if (!c) return OSB_EINVAL;
   if (var < 0 || var >= c->nvar || !dst) return set_err(c, OSB_EINVAL, "bad var or pointer");
+  dst = const_cast<double *>(static_cast<const double *>(device_access(dst)));
+  if (!dst) return set_err(c, OSB_EINVAL, "osb_get_state64: destination is neither device nor page-locked host memory");
   if (!c->qold_valid) return set_err(c, OSB_EINVAL, "no state yet: call osb_init_tgv, osb_set_state64 or osb_step");
   const int nb = blocks_for((int64_t)c->g.n0 * c->g.n1 * c->g.n2);
   k_get64<<<nb, 256, 0, c->stream>>>(c->g, c->plan.ndim == 2 ? c->q64_2d[var] : c->qold[var], dst);

@@ -266,13 +266,25 @@ class Solver:
         self._check(self.lib.osb_init_tgv(self.ctx))
         self._out()
 
+    @staticmethod
+    def _pinned64(t):
+        return (isinstance(t, torch.Tensor) and t.device.type == "cpu" and t.dtype == torch.float64 and
+                t.is_contiguous() and t.is_pinned())
+
     def set_state64(self, q):
-        """q: FP64 tensor/array [nvar][z][y][x] (interior)."""
-        q = torch.as_tensor(q, dtype=torch.float64).to(self.device).contiguous()
+        """q: FP64 tensor/array [nvar][z][y][x] (interior).  A page-locked (pinned) host tensor is read by
+        the library's kernels over the host link without a staging copy; the call then waits for them,
+        so the buffer may be reused on return."""
+        pinned = self._pinned64(q)
+        if not pinned:
+            q = torch.as_tensor(q, dtype=torch.float64).to(self.device).contiguous()
         self._in()
         for v in range(self.layout.nvar):
             self._check(self.lib.osb_set_state64(self.ctx, v, ctypes.c_void_p(q[v].data_ptr())))
-        q.record_stream(self.stream)
+        if pinned:
+            self.stream.synchronize()
+        else:
+            q.record_stream(self.stream)
         self._out()
 
     def set_state64_padded(self, q, h):
@@ -335,12 +347,21 @@ class Solver:
         x.record_stream(self.stream)
         self._out()
 
-    def state64(self):
+    def state64(self, out=None):
+        """The FP64 state [nvar][z][y][x].  With `out` a page-locked (pinned) host tensor of that shape,
+        the kernels write it directly over the host link and the call waits for them."""
+        shape = (self.layout.nvar,) + self.shape
+        pinned = out is not None
+        if pinned and not (self._pinned64(out) and tuple(out.shape) == shape):
+            raise ValueError("out must be a contiguous pinned FP64 host tensor of shape %s" % (shape,))
         self._in()
-        with torch.cuda.stream(self.stream):
-            out = torch.empty((self.layout.nvar,) + self.shape, dtype=torch.float64, device=self.device)
+        if out is None:
+            with torch.cuda.stream(self.stream):
+                out = torch.empty(shape, dtype=torch.float64, device=self.device)
         for v in range(self.layout.nvar):
             self._check(self.lib.osb_get_state64(self.ctx, v, ctypes.c_void_p(out[v].data_ptr())))
+        if pinned:
+            self.stream.synchronize()
         self._out()
         return out
 

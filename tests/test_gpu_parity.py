@@ -167,3 +167,29 @@ def test_gpu_plan_errors_surface_as_exceptions():
     with pytest.raises(OSBError):
         s.step(1, -1.0)
     s.close()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_pinned_host_state_in_and_out_without_staging(precision):
+    """set_state64 from a pinned host tensor (read by the kernels over the host link) and
+    state64(out=pinned host tensor) give the same state as the device-array path; a pageable host
+    pointer handed to the C entry point directly is refused, not read."""
+    import ctypes
+    plan = tgv_plan(20, conv="weno5js", Minf=1.25, precision=precision)
+    q0 = O.tgv_init(oracle_cfg(plan, dt=2e-3))
+    host = torch.from_numpy(q0).pin_memory()
+    a = Solver(plan)
+    a.set_state64(torch.from_numpy(q0).cuda())
+    a.step(3, 2e-3)
+    ref = a.state64().cpu()
+    a.close()
+    b = Solver(plan)
+    b.set_state64(host)
+    b.step(3, 2e-3)
+    out = torch.empty_like(host).pin_memory()
+    got = b.state64(out=out)
+    assert got.data_ptr() == out.data_ptr() and torch.equal(out, ref)
+    pageable = torch.from_numpy(q0.copy())
+    rc = b.lib.osb_set_state64(b.ctx, 0, ctypes.c_void_p(pageable[0].data_ptr()))
+    assert rc != 0
+    b.close()
