@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-#define OSB_ABI_VERSION 3
+#define OSB_ABI_VERSION 4
 
 /* error codes */
 #define OSB_OK 0
@@ -53,6 +53,12 @@ extern "C" {
 #define OSB_BC_EXTRAPOLATION 3             /* extrapolation.py:8-58, order 0 (x0 side 1) */
 #define OSB_BC_ISOTHERMAL_WALL 4           /* isothermal_wall.py:11-88 (x1 side 0) */
 #define OSB_BC_DIRICHLET 5                 /* dirichlet.py:6-41 with a state switched at x0 (x1 side 1) */
+
+/* one-sided closures of the central derivatives at a face of a 2D block (opensblifunctions.py:523-534) */
+#define OSB_CLOSURE_REDUCED_ACCESS 0 /* reduced_access_scheme.py:6-83: first two points, 5-point stencils */
+#define OSB_CLOSURE_CARPENTER 1      /* Carpenter_scheme.py:6-102 (every face class's default): first
+                                      * derivatives at the first four points (6-point stencils), second
+                                      * derivatives as ReducedAccess */
 /* arithmetic: all FP64 (the reference's Double datatype, core/datatypes.py:2-13), or FP32 state
  * and flux arithmetic with the RK accumulator in FP64 */
 #define OSB_PREC_FP64 0
@@ -89,6 +95,8 @@ typedef struct osb_plan_desc {
    * on the interior (0 elsewhere).  teno_adaptive = 0 keeps the fixed teno_ct. */
   int teno_adaptive;
   double teno_a1, teno_a2, sensor_eps;
+  /* OSB_CLOSURE_* per axis and side of a 2D block (x0, x1; the third row is unused) */
+  int closure[3][2];
 } osb_plan_desc;
 
 /* Memory layout of every per-variable array: x fastest, interior point (i,j,k) at element

@@ -15,6 +15,9 @@
 // current).
 // Metrics (once, k2_metric_*): detJ = dx1/dxi1 with the closures, D11 = 1/detJ, halos mirrored about
 // the boundary points, SD111 = dD11/dxi1 (equation_types/metric.py:37-234, 315-332).
+#include <cmath>
+#include <utility>
+
 #include "osb_common.cuh"
 #include "osb_cvt.cuh"
 #include "osb_internal.h"
@@ -27,15 +30,40 @@ template <typename T> __device__ __forceinline__ T rcp2(T x);
 template <> __device__ __forceinline__ float rcp2<float>(float x) { return __fdividef(1.0f, x); }
 template <> __device__ __forceinline__ double rcp2<double>(double x) { return 1.0 / x; }
 
-// ---- one-sided closures of the ReducedAccess boundary scheme (reduced_access_scheme.py:34-83):
-// G(o) reads the function at offset o along the axis, k is the point's index, n the axis size.
-template <typename T, typename Gf> __device__ __forceinline__ T d1c(const Gf &G, int k, int n) {
-  if (k == 0) return T(-25.0 / 12.0) * G(0) + T(4) * G(1) - T(3) * G(2) + T(4.0 / 3.0) * G(3) - T(0.25) * G(4);
-  if (k == 1) return T(-0.25) * G(-1) - T(5.0 / 6.0) * G(0) + T(1.5) * G(1) - T(0.5) * G(2) + T(1.0 / 12.0) * G(3);
-  if (k == n - 1) return T(25.0 / 12.0) * G(0) - T(4) * G(-1) + T(3) * G(-2) - T(4.0 / 3.0) * G(-3) + T(0.25) * G(-4);
-  if (k == n - 2) return T(0.25) * G(1) + T(5.0 / 6.0) * G(0) - T(1.5) * G(-1) + T(0.5) * G(-2) - T(1.0 / 12.0) * G(-3);
+// ---- one-sided closures of the central first derivative.  G(o) reads the function at offset o
+// along the axis, k is the point's index, n the axis size, cl the axis's Carpenter faces (bit 0: side
+// 0, bit 1: side 1; the others are ReducedAccess).
+//  * ReducedAccess (reduced_access_scheme.py:34-83): the first two points of a face, 5-point stencils;
+//  * Carpenter (Carpenter_scheme.py:61-102): the first four points, weights c_carp[r][m] of f(m) at
+//    point r of a side-0 face, mirrored with the opposite sign on side 1.
+// A point within reach of both faces takes the side-0 closure (its condition comes first).
+__constant__ double c_carp_d[24];
+__constant__ float c_carp_f[24];
+template <typename T> __device__ __forceinline__ T carp_w(int i);
+template <> __device__ __forceinline__ double carp_w<double>(int i) { return c_carp_d[i]; }
+template <> __device__ __forceinline__ float carp_w<float>(int i) { return c_carp_f[i]; }
+
+template <typename T, typename Gf> __device__ __forceinline__ T d1c(const Gf &G, int k, int n, int cl) {
+  const int w0 = (cl & 1) ? 4 : 2, w1 = (cl & 2) ? 4 : 2;
+  if (k < w0 || n - 1 - k < w1) {
+    const bool s0 = k < w0;
+    if (s0 ? (cl & 1) : (cl & 2)) {
+      const int r = s0 ? k : n - 1 - k;
+      T v = T(0);
+#pragma unroll
+      for (int m = 0; m < 6; ++m) v += carp_w<T>(6 * r + m) * (s0 ? G(m - r) : G(r - m));
+      return s0 ? v : -v;
+    }
+    if (s0 && k == 0)
+      return T(-25.0 / 12.0) * G(0) + T(4) * G(1) - T(3) * G(2) + T(4.0 / 3.0) * G(3) - T(0.25) * G(4);
+    if (s0) return T(-0.25) * G(-1) - T(5.0 / 6.0) * G(0) + T(1.5) * G(1) - T(0.5) * G(2) + T(1.0 / 12.0) * G(3);
+    if (k == n - 1)
+      return T(25.0 / 12.0) * G(0) - T(4) * G(-1) + T(3) * G(-2) - T(4.0 / 3.0) * G(-3) + T(0.25) * G(-4);
+    return T(0.25) * G(1) + T(5.0 / 6.0) * G(0) - T(1.5) * G(-1) + T(0.5) * G(-2) - T(1.0 / 12.0) * G(-3);
+  }
   return T(1.0 / 12.0) * G(-2) - T(2.0 / 3.0) * G(-1) + T(2.0 / 3.0) * G(1) - T(1.0 / 12.0) * G(2);
 }
+// second derivative: the same two-point closure in both schemes (second_der_coefficients)
 template <typename T, typename Gf> __device__ __forceinline__ T d2c(const Gf &G, int k, int n) {
   if (k == 0)
     return T(35.0 / 12.0) * G(0) - T(26.0 / 3.0) * G(1) + T(9.5) * G(2) - T(14.0 / 3.0) * G(3) + T(11.0 / 12.0) * G(4);
@@ -55,11 +83,11 @@ __device__ __forceinline__ int64_t g2(const Grid &g, int i, int j) { return g.of
 // ---------------------------------------------------------------------------------------------
 // metrics
 // ---------------------------------------------------------------------------------------------
-__global__ void k2_metric_d11(Grid g, const double *x1, double *D11, double inv_d1) {
+__global__ void k2_metric_d11(Grid g, const double *x1, double *D11, double inv_d1, int cly) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.n0 || j >= g.n1) return;
   auto G = [&](int o) { return x1[g2(g, i, j + o)]; };
-  const double detJ = inv_d1 * d1c<double>(G, j, g.n1);
+  const double detJ = inv_d1 * d1c<double>(G, j, g.n1, cly);
   D11[g2(g, i, j)] = 1.0 / detJ;
 }
 
@@ -79,11 +107,11 @@ __global__ void k2_metric_halo(Grid g, double *D11, int axis, int hx, int hy) {
   }
 }
 
-__global__ void k2_metric_sd(Grid g, const double *D11, double *SD111, double inv_d1) {
+__global__ void k2_metric_sd(Grid g, const double *D11, double *SD111, double inv_d1, int cly) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
   if (i >= g.n0 || j >= g.n1) return;
   auto G = [&](int o) { return D11[g2(g, i, j + o)]; };
-  SD111[g2(g, i, j)] = inv_d1 * d1c<double>(G, j, g.n1);
+  SD111[g2(g, i, j)] = inv_d1 * d1c<double>(G, j, g.n1, cly);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -238,6 +266,7 @@ __constant__ double c_p10n[23] = {1e0,   1e-1,  1e-2,  1e-3,  1e-4,  1e-5,  1e-6
 
 struct Sensor2Args {
   double inv_d0, inv_d1, a1, a2, eps;
+  int clx, cly;  // Carpenter faces of x0 and x1 (d1c)
 };
 
 __device__ __forceinline__ float tanh_t(float x) { return tanhf(x); }
@@ -262,8 +291,8 @@ __global__ void k2_sensor_ct(Grid g, Prims<const T> pr, const double *D11, T *ct
     auto U0y = [&](int o) { return pr.u0[n + o * sy]; };
     auto U1y = [&](int o) { return pr.u1[n + o * sy]; };
     const T id0 = T(sa.inv_d0), id1 = T(sa.inv_d1);
-    const T l0 = id0 * d1c<T>(U0x, i, g.n0), l1 = id0 * d1c<T>(U1x, i, g.n0);
-    const T l2 = id1 * d1c<T>(U0y, j, g.n1), l3 = id1 * d1c<T>(U1y, j, g.n1);
+    const T l0 = id0 * d1c<T>(U0x, i, g.n0, sa.clx), l1 = id0 * d1c<T>(U1x, i, g.n0, sa.clx);
+    const T l2 = id1 * d1c<T>(U0y, j, g.n1, sa.cly), l3 = id1 * d1c<T>(U1y, j, g.n1, sa.cly);
     const T D = T(D11[n]);
     const T div = l0 + l3 * D, om = l1 - l2 * D;
     const T sw = T(0.5) - T(0.5) * tanh_t(T(250) * l0 + T(250) * l3 * D + T(2.5));
@@ -513,6 +542,7 @@ __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<con
 // ---------------------------------------------------------------------------------------------
 struct Visc2Args {
   double Re, kappa, inv_d0, inv_d1, dt, A, B;
+  int clx, cly;  // Carpenter faces of x0 and x1 (d1c)
 };
 
 template <typename T>
@@ -530,21 +560,21 @@ __global__ void __launch_bounds__(256) k2_visc_rk(Grid g, Prims<const T> pr, con
 #pragma unroll
   for (int k = 0; k < 2; ++k) {
     const T *f = uc[k];
-    gr[k][0] = id0 * d1c<T>([&](int o) { return X(f, o); }, i, g.n0);
-    const T fy = id1 * d1c<T>([&](int o) { return Y(f, o); }, j, g.n1);
+    gr[k][0] = id0 * d1c<T>([&](int o) { return X(f, o); }, i, g.n0, va.clx);
+    const T fy = id1 * d1c<T>([&](int o) { return Y(f, o); }, j, g.n1, va.cly);
     gr[k][1] = Dm * fy;
     h[k][0][0] = id0 * id0 * d2c<T>([&](int o) { return X(f, o); }, i, g.n0);
     h[k][1][1] = Dm * Dm * (id1 * id1 * d2c<T>([&](int o) { return Y(f, o); }, j, g.n1)) + Dm * S * fy;
     // d/dx0 of the row j+o, then d/dxi1 of that column (inner axis x0 over the extended x1 range)
     auto inner = [&](int o) {
-      return id0 * d1c<T>([&](int p) { return f[g2(g, i + p, j + o)]; }, i, g.n0);
+      return id0 * d1c<T>([&](int p) { return f[g2(g, i + p, j + o)]; }, i, g.n0, va.clx);
     };
-    h[k][0][1] = h[k][1][0] = Dm * (id1 * d1c<T>(inner, j, g.n1));
+    h[k][0][1] = h[k][1][0] = Dm * (id1 * d1c<T>(inner, j, g.n1, va.cly));
   }
-  const T mux = id0 * d1c<T>([&](int o) { return X(pr.mu, o); }, i, g.n0);
-  const T muy = Dm * id1 * d1c<T>([&](int o) { return Y(pr.mu, o); }, j, g.n1);
-  const T Tx = id0 * d1c<T>([&](int o) { return X(pr.T_, o); }, i, g.n0);
-  const T Tyx = id1 * d1c<T>([&](int o) { return Y(pr.T_, o); }, j, g.n1);
+  const T mux = id0 * d1c<T>([&](int o) { return X(pr.mu, o); }, i, g.n0, va.clx);
+  const T muy = Dm * id1 * d1c<T>([&](int o) { return Y(pr.mu, o); }, j, g.n1, va.cly);
+  const T Tx = id0 * d1c<T>([&](int o) { return X(pr.T_, o); }, i, g.n0, va.clx);
+  const T Tyx = id1 * d1c<T>([&](int o) { return Y(pr.T_, o); }, j, g.n1, va.cly);
   const T Ty = Dm * Tyx;
   const T Txx = id0 * id0 * d2c<T>([&](int o) { return X(pr.T_, o); }, i, g.n0);
   const T Tyy = Dm * Dm * (id1 * id1 * d2c<T>([&](int o) { return Y(pr.T_, o); }, j, g.n1)) + Dm * S * Tyx;
@@ -594,13 +624,63 @@ template <typename T> static Q4T<T> q4t(void *const *a) {
   return r;
 }
 
+// the Carpenter faces of one axis as d1c's bit mask
+static int closure_bits(const osb_plan_desc &p, int axis) {
+  return (p.closure[axis][0] == OSB_CLOSURE_CARPENTER ? 1 : 0) | (p.closure[axis][1] == OSB_CLOSURE_CARPENTER ? 2 : 0);
+}
+
+// The Carpenter first-derivative closure (Carpenter_scheme.py:90-102): weights = A^-1 B with the 4x4
+// block A and the 4x6 block B of the published boundary operator, free parameters R1 and R2 as the
+// reference sets them; solved once on the host (Gauss-Jordan, partial pivoting) and uploaded to the
+// constant tables c_carp_d / c_carp_f (the same values for every context).
+cudaError_t upload2_closure_weights() {
+  const double R1 = -(2177.0 * std::sqrt(295369.0) - 1166427.0) / 25488.0;
+  const double R2 = (66195.0 * std::sqrt(53.0) * std::sqrt(5573.0) - 35909375.0) / 101952.0;
+  const double a = 216.0 * R2 + 2160.0 * R1, b = 81.0 * R2 + 675.0 * R1, e = 864.0 * R2 + 6480.0 * R1;
+  const double f = 72.0 * R2 + 720.0 * R1, h = 108.0 * R2 + 756.0 * R1, u = 4104.0 * R2 + 32400.0 * R1;
+  const double w = 1836.0 * R2 + 14580.0 * R1, y = 216.0 * R2 + 1620.0 * R1, z = 108.0 * R2 + 810.0 * R1;
+  double M[4][10] = {
+      {-(a - 2125.0) / 12960.0, (b + 415.0) / 540.0, -(f + 445.0) / 1440.0, -(h + 421.0) / 1296.0,
+       -0.5, -(e + 305.0) / 4320.0, (y + 725.0) / 540.0, -(e + 3335.0) / 4320.0, 0.0, 0.0},
+      {(b + 415.0) / 540.0, -(u + 11225.0) / 4320.0, (w + 7295.0) / 2160.0, -(a + 655.0) / 4320.0,
+       (e + 305.0) / 4320.0, 0.0, -(e + 2315.0) / 1440.0, (z + 415.0) / 270.0, 0.0, 0.0},
+      {-(f + 445.0) / 1440.0, (w + 7295.0) / 2160.0, -(u + 12785.0) / 4320.0, (b + 335.0) / 540.0,
+       -(y + 725.0) / 540.0, (e + 2315.0) / 1440.0, 0.0, -(e + 785.0) / 4320.0, -1.0 / 12.0, 0.0},
+      {-(h + 421.0) / 1296.0, -(a + 655.0) / 4320.0, (b + 335.0) / 540.0, -(a - 12085.0) / 12960.0,
+       (e + 3335.0) / 4320.0, -(z + 415.0) / 270.0, (e + 785.0) / 4320.0, 0.0, 8.0 / 12.0, -1.0 / 12.0}};
+  for (int col = 0; col < 4; ++col) {
+    int piv = col;
+    for (int r = col + 1; r < 4; ++r)
+      if (std::fabs(M[r][col]) > std::fabs(M[piv][col])) piv = r;
+    for (int m = 0; m < 10; ++m) std::swap(M[col][m], M[piv][m]);
+    const double inv = 1.0 / M[col][col];
+    for (int m = 0; m < 10; ++m) M[col][m] *= inv;
+    for (int r = 0; r < 4; ++r) {
+      if (r == col) continue;
+      const double t = M[r][col];
+      for (int m = 0; m < 10; ++m) M[r][m] -= t * M[col][m];
+    }
+  }
+  double wd[24];
+  float wf[24];
+  for (int r = 0; r < 4; ++r)
+    for (int m = 0; m < 6; ++m) {
+      wd[6 * r + m] = M[r][4 + m];
+      wf[6 * r + m] = (float)M[r][4 + m];
+    }
+  cudaError_t err = cudaMemcpyToSymbol(c_carp_d, wd, sizeof(wd));
+  if (err == cudaSuccess) err = cudaMemcpyToSymbol(c_carp_f, wf, sizeof(wf));
+  return err;
+}
+
 void launch2_metrics(const Ctx &c, const double *x1, cudaStream_t s, int64_t *launches) {
   dim3 b(32, 8), gr((c.g.n0 + 31) / 32, (c.g.n1 + 7) / 8);
   const double inv_d1 = 1.0 / c.plan.delta[1];
-  k2_metric_d11<<<gr, b, 0, s>>>(c.g, x1, c.d11, inv_d1);
+  const int cly = closure_bits(c.plan, 1);
+  k2_metric_d11<<<gr, b, 0, s>>>(c.g, x1, c.d11, inv_d1, cly);
   k2_metric_halo<<<(c.g.n1 + 2 * c.hy2 + 127) / 128, 128, 0, s>>>(c.g, c.d11, 0, c.hx2, c.hy2);
   k2_metric_halo<<<(c.g.n0 + 2 * c.hx2 + 127) / 128, 128, 0, s>>>(c.g, c.d11, 1, c.hx2, c.hy2);
-  k2_metric_sd<<<gr, b, 0, s>>>(c.g, c.d11, c.sd111, inv_d1);
+  k2_metric_sd<<<gr, b, 0, s>>>(c.g, c.d11, c.sd111, inv_d1, cly);
   *launches += 4;
 }
 
@@ -653,7 +733,8 @@ template <typename T> void launch2_rhs(const Ctx &c, int update, double A, doubl
   const double eps = teno ? p.teno_eps : p.weno_eps;
   const T *ctp = nullptr;
   if (teno && p.teno_adaptive) {
-    Sensor2Args sa{1.0 / p.delta[0], 1.0 / p.delta[1], p.teno_a1, p.teno_a2, p.sensor_eps};
+    Sensor2Args sa{1.0 / p.delta[0], 1.0 / p.delta[1], p.teno_a1, p.teno_a2, p.sensor_eps, closure_bits(p, 0),
+                   closure_bits(p, 1)};
     dim3 gs((c.g.n0 + 2 + 31) / 32, (c.g.n1 + 2 + 7) / 8);
     k2_sensor_ct<T><<<gs, b, 0, s>>>(c.g, prc, c.d11, static_cast<T *>(c.ct2), sa);
     ctp = static_cast<const T *>(c.ct2);
@@ -683,6 +764,8 @@ template <typename T> void launch2_rhs(const Ctx &c, int update, double A, doubl
   va.dt = dt;
   va.A = A;
   va.B = B;
+  va.clx = closure_bits(p, 0);
+  va.cly = closure_bits(p, 1);
   dim3 gv((c.g.n0 + 31) / 32, (c.g.n1 + 7) / 8);
   k2_visc_rk<T><<<gv, b, 0, s>>>(c.g, prc, c.d11, c.sd111, q4t<const T>(c.res), q4(c.du2), q4(c.q64_2d), va, update);
   *launches += 4;
@@ -708,7 +791,8 @@ template <typename T> void launch2_cutoff(const Ctx &c, double *out, cudaStream_
   Prims<const T> prc{pr.u0, pr.u1, pr.p, pr.a, pr.T_, pr.mu};
   dim3 b(32, 8), gp((c.g.n0 + 8 + 31) / 32, (c.g.n1 + 8 + 7) / 8);
   k2_prims<T><<<gp, b, 0, s>>>(c.g, q4(c.q64_2d), q4t<float>(c.qa), pr, p.gama, p.Minf, p.SuthT / p.RefT);
-  Sensor2Args sa{1.0 / p.delta[0], 1.0 / p.delta[1], p.teno_a1, p.teno_a2, p.sensor_eps};
+  Sensor2Args sa{1.0 / p.delta[0], 1.0 / p.delta[1], p.teno_a1, p.teno_a2, p.sensor_eps, closure_bits(p, 0),
+                   closure_bits(p, 1)};
   dim3 gs((c.g.n0 + 2 + 31) / 32, (c.g.n1 + 2 + 7) / 8);
   k2_sensor_ct<T><<<gs, b, 0, s>>>(c.g, prc, c.d11, static_cast<T *>(c.ct2), sa);
   dim3 gi((c.g.n0 + 31) / 32, (c.g.n1 + 7) / 8);

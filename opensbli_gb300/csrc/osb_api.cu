@@ -59,6 +59,13 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
         return OSB_EINVAL;
       }
     }
+    for (int d = 0; d < 2; ++d)
+      for (int side = 0; side < 2; ++side)
+        if (p->closure[d][side] != OSB_CLOSURE_REDUCED_ACCESS && p->closure[d][side] != OSB_CLOSURE_CARPENTER) {
+          snprintf(why, n, "closure[%d][%d] = %d: OSB_CLOSURE_REDUCED_ACCESS or OSB_CLOSURE_CARPENTER", d, side,
+                   p->closure[d][side]);
+          return OSB_EINVAL;
+        }
     if (p->visc != OSB_VISC_SUTHERLAND) { snprintf(why, n, "2D blocks: Sutherland viscosity"); return OSB_EUNSUPPORTED; }
     if (p->rk != OSB_RK3_LS) { snprintf(why, n, "2D blocks: low-storage RK3"); return OSB_EUNSUPPORTED; }
     if (p->precision != OSB_PREC_FP64 && p->precision != OSB_PREC_MIXED) { snprintf(why, n, "precision %d", p->precision); return OSB_EINVAL; }
@@ -681,6 +688,7 @@ int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
     if (e == cudaSuccess) e = cudaMemset(c->sd111, 0, b64);
     c->red_blocks = 152 * 8;
     if (e == cudaSuccess) e = cudaMalloc(&c->red, (c->red_blocks + 1) * sizeof(double));
+    if (e == cudaSuccess) e = upload2_closure_weights();
     if (e != cudaSuccess) {
       fprintf(stderr, "osb_create: %s\n", cudaGetErrorString(e));
       osb_destroy(c);

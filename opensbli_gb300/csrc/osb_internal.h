@@ -94,6 +94,7 @@ template <typename T>
 void launch_central_rk(const Ctx &c, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold, Fields5<T> rin,
                        Fields5<T> rout, double dt_new, double dt_old, int mode, cudaStream_t s, int64_t *launches);
 
+cudaError_t upload2_closure_weights();
 void launch2_metrics(const Ctx &c, const double *x1, cudaStream_t s, int64_t *launches);
 void launch2_bcs(const Ctx &c, cudaStream_t s, int64_t *launches);
 void launch2_to_state(const Ctx &c, cudaStream_t s, int64_t *launches);

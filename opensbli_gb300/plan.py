@@ -74,6 +74,10 @@ class Plan:
     dirichlet_x_switch: float = 40.0
     Lx1: float = 115.0
     by: float = 5.0
+    # one-sided closure of the central first derivatives at each face of a 2D wall-bounded block,
+    # [axis][side]: "reduced_access" (boundary_conditions/reduced_access_scheme.py) or "carpenter"
+    # (boundary_conditions/Carpenter_scheme.py, the reference's default)
+    closure: Tuple[Tuple[str, str], ...] = (("reduced_access", "reduced_access"),) * 2
     name: str = ""
     kernels: List[str] = dataclasses.field(default_factory=list)  # the reference kernel names lowered
 
@@ -94,6 +98,8 @@ class Plan:
             if k in d:
                 d[k] = tuple(d[k])
         d["bc"] = tuple(tuple(x) for x in d["bc"])
+        if "closure" in d:
+            d["closure"] = tuple(tuple(x) for x in d["closure"])
         return cls(**d)
 
 
@@ -126,12 +132,14 @@ def tgv_cfl_dt(plan, cfl=0.5):
     return cfl * min(plan.delta) / float(s.max())
 
 
-def katzer_plan(n0=512, n1=256, precision="fp64", conv="teno5", dt=0.04, use_graphs=True, adaptive=False):
+def katzer_plan(n0=512, n1=256, precision="fp64", conv="teno5", dt=0.04, use_graphs=True, adaptive=False,
+                closure=(("reduced_access", "reduced_access"),) * 2):
     """2D laminar shock-wave/boundary-layer interaction (apps/katzer_SBLI/katzer_SBLI.py constants):
     Mach 2, Re = 950, Pr = 0.72, Twall = 1.67619431, Sutherland 110.4/288, TENO5 with C_T = 1e-5 and
     eps = 1e-15, domain [0, 400] x [0, 115] with x1 = 115 sinh(5 eta)/sinh(5), LS-RK3 (SSP).
     adaptive=True gives the script as published: the TENO cut-off adapted per interface by the
-    modified Ducros sensor (a1 = 10.5, a2 = 4.5, sensor epsilon 1e-12)."""
+    modified Ducros sensor (a1 = 10.5, a2 = 4.5, sensor epsilon 1e-12).  closure[axis][side] names
+    each face's one-sided derivative closure (the script sets ReducedAccess on all four)."""
     A, B = ls_rk3_ssp_coefficients()
     return Plan(ndim=2, n=(n0, n1, 1), delta=(400.0 / (n0 - 1), 115.0 / (n1 - 1), 1.0), conv=conv, visc="sutherland",
                 rk="ls_rk3", precision=precision,
@@ -139,4 +147,5 @@ def katzer_plan(n0=512, n1=256, precision="fp64", conv="teno5", dt=0.04, use_gra
                     ("periodic", "periodic")),
                 gama=1.4, Minf=2.0, Re=950.0, Pr=0.72, teno_ct=1e-5, teno_eps=1e-15, rk_a=A, rk_b=B, dt=dt,
                 use_graphs=use_graphs, ic="host", teno_adaptive=adaptive,
+                closure=tuple(tuple(c) for c in closure),
                 name="katzer_%s%s_%dx%d" % (conv, "_adaptive" if adaptive else "", n0, n1))

@@ -12,7 +12,7 @@ import torch
 
 from . import build as _build
 
-OSB_ABI_VERSION = 3
+OSB_ABI_VERSION = 4
 ERRORS = {
     -1: "invalid plan or argument",
     -2: "unsupported kernel pattern",
@@ -29,6 +29,7 @@ RK = {"rk3": 0, "ls_rk3": 1}
 BC = {"periodic": 0, "symmetry": 1, "inlet_pressure_extrapolate": 2, "extrapolation": 3, "isothermal_wall": 4,
       "dirichlet": 5}
 PREC = {"fp64": 0, "mixed": 1}
+CLOSURE = {"reduced_access": 0, "carpenter": 1}
 RED = {"ke": 0, "enstrophy": 1, "nancheck": 2}
 
 
@@ -62,6 +63,7 @@ class PlanDesc(ctypes.Structure):
         ("teno_a1", ctypes.c_double),
         ("teno_a2", ctypes.c_double),
         ("sensor_eps", ctypes.c_double),
+        ("closure", (ctypes.c_int * 2) * 3),
     ]
 
 
@@ -194,6 +196,9 @@ def make_plan_desc(plan):
     d.dirichlet_x_switch = plan.dirichlet_x_switch
     d.teno_adaptive = 1 if plan.teno_adaptive else 0
     d.teno_a1, d.teno_a2, d.sensor_eps = plan.teno_a1, plan.teno_a2, plan.sensor_eps
+    for a in range(len(plan.closure)):
+        for side in range(2):
+            d.closure[a][side] = CLOSURE[plan.closure[a][side]]
     return d
 
 

@@ -241,6 +241,7 @@ class GB300Writer:
         if any(b is None for pair in bcs for b in pair):
             found = sorted(n for n in names if "boundary dir" in n)
             raise NotImplementedError("2D boundary conditions: %s" % found)
+        closure = self._closures_2d()
         # the Dirichlet face: rho, rhou0, rhou1, rhoE = Piecewise((hi, x0 > xs), (lo, True))
         dk = self._kernels("Dirichlet boundary dir1 side1")[0]
         lo, hi, xs = {}, {}, None
@@ -265,7 +266,53 @@ class GB300Writer:
                     dirichlet_lo=tuple(lo[v] for v in order), dirichlet_hi=tuple(hi[v] for v in order),
                     dirichlet_x_switch=xs if xs is not None else 1e300, kernels=[n for n in names if n],
                     teno_adaptive=adaptive is not None,
-                    sensor_eps=adaptive if adaptive is not None else Plan.sensor_eps)
+                    sensor_eps=adaptive if adaptive is not None else Plan.sensor_eps, closure=closure)
+
+    def _closures_2d(self):
+        """The one-sided closure each face applies to the central derivatives of its direction
+        (opensblifunctions.py:523-534 wraps every central derivative in a Piecewise over the grid
+        index): ReducedAccess closes the first two points of a face (reduced_access_scheme.py:34-83),
+        Carpenter, the default of every face class, the first four (Carpenter_scheme.py:61-78).  Read
+        from the conditions of those Piecewise expressions in the algorithm's kernels."""
+        import sympy
+        from sympy import preorder_traversal
+        depth = {(d, side): 0 for d in range(2) for side in range(2)}
+        for k in self._kernels(""):
+            for e in k.equations:
+                for a in preorder_traversal(e.rhs):
+                    if not isinstance(a, sympy.Piecewise):
+                        continue
+                    for _, cond in a.args:
+                        if not isinstance(cond, sympy.Equality):
+                            continue
+                        # idx[d] == loc or idx[d] == block0npd - m, in either orientation
+                        e = sympy.expand(cond.lhs - cond.rhs)
+                        ix = [x for x in e.atoms(sympy.Indexed) if str(x.base) == "idx"]
+                        if len(ix) != 1:
+                            continue
+                        m = re.match(r"idx\[(\d)\]$", str(ix[0]))
+                        if not m or int(m.group(1)) > 1:
+                            continue
+                        d, k = int(m.group(1)), e.coeff(ix[0])
+                        if k not in (1, -1):
+                            continue
+                        r = sympy.expand(-(e - k * ix[0]) / k)
+                        if r.is_Integer:
+                            depth[(d, 0)] = max(depth[(d, 0)], int(r) + 1)
+                        elif {str(x) for x in r.free_symbols} == {"block0np%d" % d}:
+                            npd = next(iter(r.free_symbols))
+                            depth[(d, 1)] = max(depth[(d, 1)], int(npd - r))
+        kinds = {2: "reduced_access", 4: "carpenter"}
+        out = []
+        for d in range(2):
+            pair = []
+            for side in range(2):
+                if depth[(d, side)] not in kinds:
+                    raise NotImplementedError("face dir%d side%d: one-sided closure of %d points is not lowered"
+                                              % (d, side, depth[(d, side)]))
+                pair.append(kinds[depth[(d, side)]])
+            out.append(tuple(pair))
+        return tuple(out)
 
     def _adaptive_teno(self, teno):
         """Recognise the adaptive TENO cut-off (LLFTeno(formulation='adaptive'), schemes/spatial/

@@ -31,6 +31,7 @@ CASES = {
     "tgv_teno": "tgv_teno.py",
     "tgv_teno6": "tgv_teno6.py",
     "katzer_teno": "katzer_teno.py",
+    "katzer_carpenter": "katzer_carpenter.py",
     "katzer_adaptive": "ref:apps/katzer_SBLI/katzer_SBLI.py",
 }
 

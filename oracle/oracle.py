@@ -132,7 +132,11 @@ class Cfg2D(ctypes.Structure):
         ("teno_a1", ctypes.c_double),
         ("teno_a2", ctypes.c_double),
         ("sensor_eps", ctypes.c_double),
+        ("closure", (ctypes.c_int * 2) * 2),
     ]
+
+
+CLOSURES = {"reduced_access": 0, "carpenter": 1}
 
 
 def make_cfg2d(plan):
@@ -153,7 +157,17 @@ def make_cfg2d(plan):
     c.teno_a1 = getattr(plan, "teno_a1", 10.5)
     c.teno_a2 = getattr(plan, "teno_a2", 4.5)
     c.sensor_eps = getattr(plan, "sensor_eps", 1e-30)
+    for d in range(2):
+        for side in range(2):
+            c.closure[d][side] = CLOSURES[plan.closure[d][side]]
     return c
+
+
+def carpenter_d1():
+    """The oracle's Carpenter first-derivative closure weights, [4][6] (weight of f(m) at point r)."""
+    out = np.zeros(24)
+    lib().osbo2d_carpenter_d1(out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    return out.reshape(4, 6)
 
 
 def run2d(plan, q0_padded, nsteps):

@@ -55,6 +55,9 @@ typedef struct {
    * C_T = 10^-floor(a1 - a2 (1 - (1-theta)^4 (1+4 theta))) per interface; 0 selects the fixed teno_ct */
   int teno_adaptive;
   double teno_a1, teno_a2, sensor_eps;
+  /* one-sided closure of the central first derivatives at each face [axis][side]:
+   * 0 ReducedAccess (reduced_access_scheme.py), 1 Carpenter (Carpenter_scheme.py) */
+  int closure[2][2];
 } osbo2d_cfg;
 
 /* Advance q by nsteps LS-RK3 steps.  q holds [4][n1+8][n0+8]: rho, rhou0, rhou1, rhoE with a
@@ -64,6 +67,8 @@ int osbo2d_run(const osbo2d_cfg *cfg, double *q, int nsteps);
 /* Metric terms D11 and SD111 on the interior, [n1][n0]. */
 int osbo2d_cutoff(const osbo2d_cfg *cfg, const double *q, double *ct);
 int osbo2d_metrics(const osbo2d_cfg *cfg, double *D11, double *SD111);
+/* The Carpenter first-derivative closure weights, [4][6] row-major: weight of f(m) at point r. */
+void osbo2d_carpenter_d1(double *c24);
 
 #ifdef __cplusplus
 }

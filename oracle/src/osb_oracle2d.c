@@ -6,7 +6,7 @@
  * The kernel list restated here is the one TraditionalAlgorithmRK builds for a block with
  * MetricsEquation (stretched in x1), LLFTeno(5), Central(4), Sutherland viscosity, RungeKuttaLS(3,'SSP')
  * and the four boundary conditions InletPressureExtrapolateBC / ExtrapolationBC (x) and
- * IsothermalWallBC / DirichletBC (y), all with ReducedAccess closures
+ * IsothermalWallBC / DirichletBC (y), each face with the ReducedAccess or the Carpenter closure
  * (apps/katzer_SBLI/katzer_SBLI.py:32-126 with fixed-C_T TENO).  Order (algorithm.py:384-477):
  *   before the loop: coordinates, metric derivative, D11 = 1/(dx1/dxi1), metric halos, SD111
  *   iter { BCs; stage { CRs; TENO x; TENO y; TENO residual; viscous terms; LS-RK update; BCs } }
@@ -27,6 +27,7 @@ typedef struct {
   double *q[4], *du[4], *res[4];
   double *u0, *u1, *p, *a, *T, *mu, *theta;
   double *x1, *D11, *SD111, *flux[4];
+  double carp[4][6]; /* Carpenter first-derivative closure weights */
 } s2_t;
 
 static inline size_t I2(const s2_t *s, int i, int j) { return (size_t)(i + H) + (size_t)s->px * (size_t)(j + H); }
@@ -36,9 +37,12 @@ static double *alloc2(const s2_t *s) { return (double *)calloc(s->np, sizeof(dou
 #define N1 (s->c.n[1])
 #define FOR2(i0, i1, j0, j1) for (int j = (j0); j < (j1); ++j) for (int i = (i0); i < (i1); ++i)
 
+static void carpenter_d1(double c[4][6]);
+
 static void s2_init(s2_t *s, const osbo2d_cfg *cfg) {
   memset(s, 0, sizeof(*s));
   s->c = *cfg;
+  carpenter_d1(s->carp);
   s->px = cfg->n[0] + 2 * H;
   s->py = cfg->n[1] + 2 * H;
   s->np = (size_t)s->px * s->py;
@@ -60,24 +64,95 @@ static void s2_free(s2_t *s) {
 }
 
 /* ---------------------------------------------------------------------------------------------
- * 4th-order central derivatives in computational space with the ReducedAccess one-sided closures
- * at the first two and last two points of an axis (core/boundary_conditions/
- * reduced_access_scheme.py:34-83, applied through opensblifunctions.py:523-534).
+ * 4th-order central derivatives in computational space with one-sided closures at the faces
+ * (applied through opensblifunctions.py:523-534):
+ *  - ReducedAccess (core/boundary_conditions/reduced_access_scheme.py:34-83): first and second
+ *    derivatives at the first two and last two points, 5-point stencils;
+ *  - Carpenter (core/boundary_conditions/Carpenter_scheme.py:6-102, after the paper it cites,
+ *    doi:10.1006/jcph.1998.6114): first derivatives at the first four points from the 4x6 matrix
+ *    A^-1 B of the published boundary closure (free parameters R1, R2 as in the reference), mirrored
+ *    with the opposite sign on side 1; the second derivative uses the same two-point closure as
+ *    ReducedAccess.
  * ------------------------------------------------------------------------------------------- */
 static inline double F(const s2_t *s, const double *f, int i, int j) { return f[I2(s, i, j)]; }
+
+/* c[r][m]: weight of f(m) in the first derivative at point r of a side-0 face */
+static void carpenter_d1(double c[4][6]) {
+  const double R1 = -(2177.0 * sqrt(295369.0) - 1166427.0) / 25488.0;
+  const double R2 = (66195.0 * sqrt(53.0) * sqrt(5573.0) - 35909375.0) / 101952.0;
+  const double P = 216.0 * R2 + 2160.0 * R1, Q = 81.0 * R2 + 675.0 * R1, S = 864.0 * R2 + 6480.0 * R1;
+  /* A: the norm-matrix block of the closure (symmetric), B: the difference-operator block */
+  double A[4][10] = {
+      {-(P - 2125.0) / 12960.0, (Q + 415.0) / 540.0, -(72.0 * R2 + 720.0 * R1 + 445.0) / 1440.0,
+       -(108.0 * R2 + 756.0 * R1 + 421.0) / 1296.0},
+      {(Q + 415.0) / 540.0, -(4104.0 * R2 + 32400.0 * R1 + 11225.0) / 4320.0,
+       (1836.0 * R2 + 14580.0 * R1 + 7295.0) / 2160.0, -(P + 655.0) / 4320.0},
+      {-(72.0 * R2 + 720.0 * R1 + 445.0) / 1440.0, (1836.0 * R2 + 14580.0 * R1 + 7295.0) / 2160.0,
+       -(4104.0 * R2 + 32400.0 * R1 + 12785.0) / 4320.0, (Q + 335.0) / 540.0},
+      {-(108.0 * R2 + 756.0 * R1 + 421.0) / 1296.0, -(P + 655.0) / 4320.0, (Q + 335.0) / 540.0,
+       -(P - 12085.0) / 12960.0}};
+  const double B[4][6] = {
+      {-0.5, -(S + 305.0) / 4320.0, (216.0 * R2 + 1620.0 * R1 + 725.0) / 540.0, -(S + 3335.0) / 4320.0, 0.0, 0.0},
+      {(S + 305.0) / 4320.0, 0.0, -(S + 2315.0) / 1440.0, (108.0 * R2 + 810.0 * R1 + 415.0) / 270.0, 0.0, 0.0},
+      {-(216.0 * R2 + 1620.0 * R1 + 725.0) / 540.0, (S + 2315.0) / 1440.0, 0.0, -(S + 785.0) / 4320.0, -1.0 / 12.0,
+       0.0},
+      {(S + 3335.0) / 4320.0, -(108.0 * R2 + 810.0 * R1 + 415.0) / 270.0, (S + 785.0) / 4320.0, 0.0, 8.0 / 12.0,
+       -1.0 / 12.0}};
+  /* Gauss-Jordan elimination with partial pivoting on [A | B] */
+  for (int r = 0; r < 4; ++r)
+    for (int m = 0; m < 6; ++m) A[r][4 + m] = B[r][m];
+  for (int col = 0; col < 4; ++col) {
+    int piv = col;
+    for (int r = col + 1; r < 4; ++r)
+      if (fabs(A[r][col]) > fabs(A[piv][col])) piv = r;
+    for (int m = 0; m < 10; ++m) {
+      const double t = A[col][m];
+      A[col][m] = A[piv][m];
+      A[piv][m] = t;
+    }
+    const double inv = 1.0 / A[col][col];
+    for (int m = 0; m < 10; ++m) A[col][m] *= inv;
+    for (int r = 0; r < 4; ++r) {
+      if (r == col) continue;
+      const double f = A[r][col];
+      for (int m = 0; m < 10; ++m) A[r][m] -= f * A[col][m];
+    }
+  }
+  for (int r = 0; r < 4; ++r)
+    for (int m = 0; m < 6; ++m) c[r][m] = A[r][4 + m];
+}
 
 static double d1c(const s2_t *s, const double *f, int i, int j, int dir) {
   const int n = dir == 0 ? N0 : N1, k = dir == 0 ? i : j;
   const double inv = 1.0 / s->c.delta[dir];
+  const int c0 = s->c.closure[dir][0], c1 = s->c.closure[dir][1];
 #define G(o) (dir == 0 ? F(s, f, i + (o), j) : F(s, f, i, j + (o)))
+  /* the side-0 face's points take precedence (its condition comes first in the Piecewise) */
+  int side = -1, r = 0;
+  if (k < (c0 == 1 ? 4 : 2)) side = 0, r = k;
+  else if (n - 1 - k < (c1 == 1 ? 4 : 2)) side = 1, r = n - 1 - k;
+  const int carp = side >= 0 && (side == 0 ? c0 : c1) == 1;
   double v;
-  if (k == 0) v = -(25.0 / 12.0) * G(0) + 4.0 * G(1) - 3.0 * G(2) + (4.0 / 3.0) * G(3) - 0.25 * G(4);
-  else if (k == 1) v = -0.25 * G(-1) - (5.0 / 6.0) * G(0) + 1.5 * G(1) - 0.5 * G(2) + (1.0 / 12.0) * G(3);
-  else if (k == n - 1) v = (25.0 / 12.0) * G(0) - 4.0 * G(-1) + 3.0 * G(-2) - (4.0 / 3.0) * G(-3) + 0.25 * G(-4);
-  else if (k == n - 2) v = 0.25 * G(1) + (5.0 / 6.0) * G(0) - 1.5 * G(-1) + 0.5 * G(-2) - (1.0 / 12.0) * G(-3);
+  if (carp) {
+    /* side 0: point r reads f(0..5); side 1: point n-1-r reads f(n-1-m), sign reversed */
+    v = 0.0;
+    for (int m = 0; m < 6; ++m) v += s->carp[r][m] * (side == 0 ? G(m - r) : G(r - m));
+    if (side == 1) v = -v;
+  } else if (side == 0 && r == 0) v = -(25.0 / 12.0) * G(0) + 4.0 * G(1) - 3.0 * G(2) + (4.0 / 3.0) * G(3) - 0.25 * G(4);
+  else if (side == 0) v = -0.25 * G(-1) - (5.0 / 6.0) * G(0) + 1.5 * G(1) - 0.5 * G(2) + (1.0 / 12.0) * G(3);
+  else if (side == 1 && r == 0) v = (25.0 / 12.0) * G(0) - 4.0 * G(-1) + 3.0 * G(-2) - (4.0 / 3.0) * G(-3) + 0.25 * G(-4);
+  else if (side == 1) v = 0.25 * G(1) + (5.0 / 6.0) * G(0) - 1.5 * G(-1) + 0.5 * G(-2) - (1.0 / 12.0) * G(-3);
   else v = (1.0 / 12.0) * G(-2) - (2.0 / 3.0) * G(-1) + (2.0 / 3.0) * G(1) - (1.0 / 12.0) * G(2);
 #undef G
   return inv * v;
+}
+
+/* coefficient table of the Carpenter first-derivative closure (for the tests) */
+void osbo2d_carpenter_d1(double *c24) {
+  double c[4][6];
+  carpenter_d1(c);
+  for (int r = 0; r < 4; ++r)
+    for (int m = 0; m < 6; ++m) c24[6 * r + m] = c[r][m];
 }
 
 static double d2c(const s2_t *s, const double *f, int i, int j, int dir) {

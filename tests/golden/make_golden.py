@@ -45,6 +45,8 @@ CASES_2D = {
     "katzer_teno": ((64, 32), 20, {"dt": 0.01}),
     # the published script: TENO cut-off adapted by the modified Ducros sensor
     "katzer_adaptive": ((64, 32), 20, {"dt": 0.01}),
+    # Carpenter closures (the reference's default) on the outlet and the wall, ReducedAccess elsewhere
+    "katzer_carpenter": ((64, 32), 20, {"dt": 0.01}),
 }
 VARS_2D = ["rho", "rhou0", "rhou1", "rhoE"]
 

@@ -61,6 +61,19 @@ def test_query_layout_rejects_bad_plans(change, code):
     assert rc == code
 
 
+def test_query_layout_2d_closures():
+    from opensbli_gb300.plan import katzer_plan
+    carp = (("carpenter", "carpenter"),) * 2
+    assert layout(katzer_plan(64, 32, closure=carp))[0] == 0
+    d = runtime.make_plan_desc(katzer_plan(64, 32))
+    assert [list(r) for r in d.closure] == [[0, 0], [0, 0], [0, 0]]
+    d = runtime.make_plan_desc(katzer_plan(64, 32, closure=(("reduced_access", "carpenter"),) * 2))
+    assert [list(r) for r in d.closure][:2] == [[0, 1], [0, 1]]
+    d.closure[1][0] = 7
+    lay = runtime.Layout()
+    assert runtime.load().osb_query_layout(ctypes.byref(d), ctypes.byref(lay)) == -1
+
+
 def test_abi_version_mismatch():
     lib = runtime.load()
     d = runtime.make_plan_desc(tgv_plan(32))

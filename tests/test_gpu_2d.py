@@ -155,3 +155,40 @@ def test_gpu_2d_cutoff_needs_an_adaptive_plan():
     with pytest.raises(Exception):
         s.teno_cutoff()
     s.close()
+
+
+# ---- Carpenter closures (the reference's default; here on the outlet and the wall) ----
+
+def test_gpu_2d_carpenter_fp64_matches_reference_golden():
+    q0, x1, q_ref, n, steps, params = load_golden_2d("katzer_carpenter")
+    plan = golden_plan_2d("katzer_carpenter", n=n).replace(dt=params["dt"])
+    assert plan.closure == (("reduced_access", "carpenter"), ("carpenter", "reduced_access"))
+    q = run_gpu_2d(plan, q0, x1, steps, params["dt"])
+    ref = q_ref[:, 4:-4, 4:-4]
+    err = [float(np.abs(q[v] - ref[v]).max() / np.abs(ref[v]).max()) for v in range(4)]
+    assert max(err) <= 1e-12, err
+
+
+@pytest.mark.parametrize("closure", [(("carpenter", "reduced_access"), ("reduced_access", "carpenter")),
+                                     (("carpenter", "carpenter"), ("carpenter", "carpenter"))])
+def test_gpu_2d_carpenter_fp64_matches_oracle(closure):
+    """Every face combination the golden case does not hold, on a wider grid and a perturbed state."""
+    q0, x1, _, n, _, params = load_golden_2d("katzer_carpenter")
+    q0w, x1w = widen_2d(q0, 96), widen_2d(x1[None], 96)[0]
+    rng = np.random.default_rng(3)
+    q0w = q0w * (1.0 + 1e-3 * rng.standard_normal(q0w.shape))
+    plan = golden_plan_2d("katzer_carpenter", n=(96, n[1])).replace(dt=params["dt"], closure=closure)
+    q_or = O.run2d(plan, q0w, 10)
+    q = run_gpu_2d(plan, q0w, x1w, 10, params["dt"])
+    ref = q_or[:, 4:-4, 4:-4]
+    err = [float(np.abs(q[v] - ref[v]).max() / np.abs(ref[v]).max()) for v in range(4)]
+    assert max(err) <= 1e-12, err
+
+
+def test_gpu_2d_carpenter_mixed_close_to_fp64():
+    q0, x1, q_ref, n, steps, params = load_golden_2d("katzer_carpenter")
+    plan = golden_plan_2d("katzer_carpenter", n=n).replace(dt=params["dt"], precision="mixed")
+    qm = run_gpu_2d(plan, q0, x1, steps, params["dt"])
+    ref = q_ref[:, 4:-4, 4:-4]
+    l2 = [float(np.linalg.norm(qm[v] - ref[v]) / np.linalg.norm(ref[v])) for v in range(4)]
+    assert max(l2) < 1e-5, l2

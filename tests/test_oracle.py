@@ -71,12 +71,14 @@ def test_oracle_matches_reference_run(case, n, steps, extra):
     assert max(rel_err(q, q_ref)) < 1e-12
 
 
-@pytest.mark.parametrize("case", ["katzer_teno", "katzer_adaptive"])
+@pytest.mark.parametrize("case", ["katzer_teno", "katzer_adaptive", "katzer_carpenter"])
 def test_oracle_2d_matches_reference_golden(case):
     from helpers import load_golden_2d, golden_plan_2d, rel_err_2d
     q0, x1, q_ref, n, steps, params = load_golden_2d(case)
     plan = golden_plan_2d(case, n=n).replace(dt=params["dt"])
     assert plan.teno_adaptive == (case == "katzer_adaptive")
+    carp = (("reduced_access", "carpenter"), ("carpenter", "reduced_access"))
+    assert plan.closure == (carp if case == "katzer_carpenter" else (("reduced_access",) * 2,) * 2)
     q = O.run2d(plan, q0, steps)
     assert max(rel_err_2d(q, q_ref)) < 1e-12
     # halos too (the outlet and wall faces write them)
@@ -91,6 +93,31 @@ def test_oracle_adaptive_cutoff_changes_the_solution():
     plan = golden_plan_2d("katzer_adaptive", n=n).replace(dt=params["dt"], teno_adaptive=False)
     q = O.run2d(plan, q0, steps)
     assert max(rel_err_2d(q, q_ref)) > 1e-6
+
+
+def test_oracle_carpenter_closure_changes_the_solution():
+    """The Carpenter fixture is not reproduced with ReducedAccess closures on every face, so the
+    golden case pins the closure (on the wall and the outlet)."""
+    from helpers import load_golden_2d, golden_plan_2d, rel_err_2d
+    q0, x1, q_ref, n, steps, params = load_golden_2d("katzer_carpenter")
+    plan = golden_plan_2d("katzer_carpenter", n=n).replace(dt=params["dt"], closure=(("reduced_access",) * 2,) * 2)
+    q = O.run2d(plan, q0, steps)
+    assert max(rel_err_2d(q, q_ref)) > 1e-8
+
+
+def test_carpenter_closure_weights():
+    """The closure's first-derivative weights: consistent (rows sum to 0), exact for linear functions
+    (sum_m m c[r][m] = 1 at point r, offsets measured from the face), third order at the boundary point
+    (exact for m^2 and m^3), and the published boundary row f'(0) = (-11 f0 + 18 f1 - 9 f2 + 2 f3)/6."""
+    c = O.carpenter_d1()
+    m = np.arange(6.0)
+    for r in range(4):
+        assert abs(c[r].sum()) < 1e-14
+        assert abs((c[r] * (m - r)).sum() - 1.0) < 1e-13
+    for p in (2, 3):
+        assert abs((c[0] * m ** p).sum()) < 1e-12
+    assert np.allclose(c[0, :4], [-11.0 / 6.0, 3.0, -1.5, 1.0 / 3.0], atol=1e-13)
+    assert np.abs(c[0, 4:]).max() < 1e-13
 
 
 def test_oracle_2d_metrics_match_reference_coordinates():

@@ -48,7 +48,7 @@ def test_katzer_plan_matches_lowered_script():
     k = katzer_plan()
     g = golden_plan("katzer_teno")
     for f in ("ndim", "n", "conv", "visc", "rk", "bc", "gama", "Minf", "Re", "Pr", "Twall", "SuthT", "RefT", "teno_eps",
-              "teno_ct", "dirichlet_lo", "dirichlet_hi", "dirichlet_x_switch", "Lx1", "by"):
+              "teno_ct", "dirichlet_lo", "dirichlet_hi", "dirichlet_x_switch", "Lx1", "by", "closure"):
         assert getattr(k, f) == getattr(g, f), f
     assert np.allclose(k.rk_a, g.rk_a, atol=1e-15) and np.allclose(k.rk_b, g.rk_b, rtol=1e-15)
     assert np.allclose(k.delta[:2], g.delta[:2], rtol=1e-15)
@@ -67,6 +67,14 @@ def test_published_katzer_script_lowers_to_adaptive_teno():
     assert "ConstituentRelations evaluation" in g.kernels
 
 
+def test_carpenter_faces_lower_to_their_closure():
+    """Faces constructed without scheme= take the reference's default Carpenter closure; the writer
+    reads each face's closure from the derivative kernels' boundary conditions."""
+    g = golden_plan("katzer_carpenter")
+    assert g.closure == (("reduced_access", "carpenter"), ("carpenter", "reduced_access"))
+    assert golden_plan("katzer_teno").closure == (("reduced_access", "reduced_access"),) * 2
+
+
 def test_cfl_dt_tgv_weno():
     p = tgv_plan(256, conv="weno5js", Minf=1.25)
     dt = tgv_cfl_dt(p)
@@ -75,7 +83,7 @@ def test_cfl_dt_tgv_weno():
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
 @pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central",
-                                  "katzer_teno", "katzer_adaptive"])
+                                  "katzer_teno", "katzer_adaptive", "katzer_carpenter"])
 def test_writer_lowers_reference_script(case, tmp_path):
     r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case, "--out",
                         str(tmp_path), "--ref", REF], capture_output=True, text=True, timeout=900)
