@@ -253,8 +253,11 @@ __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> 
   }
 }
 
+// FP32: 384 threads per SM (168 registers with 4 lines per block): the two-lane side arithmetic
+// keeps both sides live at once and spilled at 128 registers; measured 4 % faster per step at 256^3
+// than the scalar sides at 512 threads.
 template <typename T, int DIR, bool ACCUM, int BY, int SCH>
-__global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 512 : 256) / (32 * BY))
+__global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 384 : 256) / (32 * BY))
     k_weno_march(Grid g, Fields5<const T> q, Fields5<T> res, Phys ph, int L) {
   weno_march_tile<T, DIR, ACCUM, BY, SCH>(g, q, res, ph, L, blockIdx.x, blockIdx.y, blockIdx.z);
 }

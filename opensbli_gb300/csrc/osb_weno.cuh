@@ -26,7 +26,9 @@
 // the candidate differences (p_r - p_1) only; in FP64,
 // where every division costs a Newton sequence on the slow FP64 pipe, the three alphas are scaled
 // by the common factor prod_s (eps+beta_s)^2, alpha_0 ~ d_0 (eps+beta_1)^2 (eps+beta_2)^2 etc., so
-// one exact division per side remains (the products stay far inside the FP64 range).
+// one exact division per side remains (the products stay far inside the FP64 range).  FP32 WENO-JS/Z
+// run both sides of a characteristic reconstruction in the two lanes of the f32x2 instructions
+// (weno5_pair12).
 #pragma once
 #include "osb_common.cuh"
 
@@ -98,6 +100,83 @@ template <typename T, int SCH> __device__ __forceinline__ T weno5_side(T f0, T f
     }
     return p1 + (T(-1.0 / 12.0) * a0 * D0 + T(1.0 / 6.0) * a2 * D2) * rcp_t(a0 + a1 + a2);
   }
+}
+
+// ---- two-lane FP32: the f32x2 instructions of sm_100 and later run both sides of one characteristic
+// reconstruction (+ side in the low lane, - side in the high lane) in one 64-bit register pair,
+// halving the instructions of the side arithmetic.  Each lane rounds as the scalar instruction does.
+struct F2 {
+  unsigned long long v;
+};
+__device__ __forceinline__ F2 f2(float lo, float hi) {
+  F2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_split(F2 x, float &lo, float &hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(x.v));
+}
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) {
+  F2 r;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) {
+  F2 r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+__device__ __forceinline__ F2 operator*(F2 a, F2 b) {
+  F2 r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+  return r;
+}
+// a * b + c, one rounding per lane
+__device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) {
+  F2 r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+  return r;
+}
+__device__ __forceinline__ F2 rcp2(F2 x) {
+  float a, b;
+  f2_split(x, a, b);
+  return f2(__fdividef(1.0f, a), __fdividef(1.0f, b));
+}
+
+// weno5_side (JS or Z) for both sides at once, FP32, returning 12x the reconstruction.  Rearranged
+// for few instructions and few constant registers, the same quantities as weno5_side:
+//   * indicators taken 16x (13/3 t^2 + s^2, with 16 eps): the weights depend on beta and eps only
+//     through ratios, so the common factor cancels;
+//   * alphas taken 10x: a = (3 r0, 6 r1, r2) with r = 1/(eps+beta)^2 (JS), a = (3 w0, 6 w1, w2) with
+//     w = 1 + tau^2 r (Z), so 12 (p0 - p1) a0 / sum a = -3 r0 D0 / sum and 12 (p2 - p1) a2 / sum
+//     = 2 r2 D2 / sum;
+//   * 12 p1 = 6 f2 + d1 + 2 d2.
+template <int SCH> __device__ __forceinline__ F2 weno5_pair12(F2 f0, F2 f1, F2 f2_, F2 f3, F2 f4, float eps) {
+  const F2 m3 = f2(-3.0f, -3.0f), p3 = f2(3.0f, 3.0f), p6 = f2(6.0f, 6.0f);
+  const F2 nd0 = f0 - f1, d1 = f2_ - f1, d2 = f3 - f2_, d3 = f4 - f3;
+  const F2 t0 = d3 - d2, t1 = d2 - d1, t2 = d1 + nd0;
+  const F2 s0 = fma2(m3, d2, d3), s1 = d1 + d2, s2 = fma2(p3, d1, nd0);
+  const F2 k13 = f2(13.0f / 3.0f, 13.0f / 3.0f), e16 = f2(16.0f * eps, 16.0f * eps);
+  const F2 e0 = fma2(k13 * t0, t0, s0 * s0) + e16;
+  const F2 e1 = fma2(k13 * t1, t1, s1 * s1) + e16;
+  const F2 e2 = fma2(k13 * t2, t2, s2 * s2) + e16;
+  const F2 r0 = rcp2(e0 * e0), r1 = rcp2(e1 * e1), r2 = rcp2(e2 * e2);
+  const F2 D0 = t0 - t1, D2 = t2 - t1;
+  const F2 x = fma2(p6, f2_, s1 + d2);
+  F2 w0, w2, sum;
+  if constexpr (SCH == SCH_Z) {
+    // the 16x indicators: tau and eps + beta carry the same factor
+    const F2 bd = e0 - e2, tt = bd * bd, one = f2(1.0f, 1.0f);
+    sum = fma2(tt, fma2(p3, r0, fma2(p6, r1, r2)), f2(10.0f, 10.0f));
+    w0 = fma2(tt, r0, one);
+    w2 = fma2(tt, r2, one);
+  } else {
+    sum = fma2(p3, r0, fma2(p6, r1, r2));
+    w0 = r0;
+    w2 = r2;
+  }
+  const F2 y = fma2(w2 + w2, D2, m3 * w0 * D0);
+  return fma2(y, rcp2(sum), x);
 }
 
 // One TENO5 side with a fixed cut-off (schemes/spatial/teno.py:57-213, 407-465), the same stencil
@@ -238,6 +317,16 @@ __device__ __forceinline__ void interface_flux_delta(const WPt<float> (&W)[6], c
     lam_m = max_t(lam_m, abs_t(W[t].a - W[t].ud));
   }
   auto recon = [&](const T (&cf)[6], const T (&cs)[6], T lam) -> T {
+    if constexpr (SCH == SCH_JS || SCH == SCH_Z) {
+      // + side f_k = cf[k] + lam cs[k] (points i-2..i+2), - side f_k = cf[5-k] - lam cs[5-k] (i+3..i-1)
+      const F2 pm = f2(lam, -lam);
+      F2 f[5];
+#pragma unroll
+      for (int k = 0; k < 5; ++k) f[k] = fma2(pm, f2(cs[k], cs[5 - k]), f2(cf[k], cf[5 - k]));
+      float rp, rm;
+      f2_split(weno5_pair12<SCH>(f[0], f[1], f[2], f[3], f[4], eps), rp, rm);
+      return (rp + rm) * (1.0f / 12.0f);
+    }
     T fp[6], fm[6];
 #pragma unroll
     for (int t = 0; t < 6; ++t) {
