@@ -325,7 +325,10 @@ __device__ __forceinline__ void interface_flux_delta(const WPt<float> (&W)[6], c
       for (int k = 0; k < 5; ++k) f[k] = fma2(pm, f2(cs[k], cs[5 - k]), f2(cf[k], cf[5 - k]));
       float rp, rm;
       f2_split(weno5_pair12<SCH>(f[0], f[1], f[2], f[3], f[4], eps), rp, rm);
-      return (rp + rm) * (1.0f / 12.0f);
+      // 1/12 as an FP32 hi/lo pair: FP32 1/12 alone is 3e-8 high and would scale every reconstructed
+      // flux the same way, a bias that grows in time
+      constexpr float c12 = 1.0f / 12.0f, c12_lo = (float)(1.0 / 12.0 - (double)(1.0f / 12.0f));
+      return mul_hl(rp + rm, c12, c12_lo);
     }
     T fp[6], fm[6];
 #pragma unroll

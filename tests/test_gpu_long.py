@@ -90,7 +90,7 @@ def test_katzer_fp64_matches_reference_500_steps():
 def test_mixed_weno_error_budget_128_500_steps():
     """Mixed path (FP32 state and arithmetic, FP64 RK register) against the FP64 path: Taylor-Green
     128^3, WENO5-JS + viscous, Minf 1.25, CFL 0.5, 500 steps (the same physical time as 1000 steps
-    at 256^3).  Measured 3.8e-8 .. 1.4e-7 relative L2; the bound leaves a factor of two.  Larger
+    at 256^3).  Measured 3.6e-8 .. 1.3e-7 relative L2; the bound leaves a factor of two.  Larger
     errors here mean FP32 rounding noise or a one-sided bias came back: the primitives rounded
     once, the difference-form characteristic flux, the differenced central stencils and the hi/lo
     FP32 constants are what keep it down."""
