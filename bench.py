@@ -94,13 +94,15 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def dist_init():
+def dist_init(backend="nccl"):
+    """One process per GPU (torchrun's RANK / WORLD_SIZE / LOCAL_RANK).  The ranks are independent
+    replicas: the only collectives are the barrier around the timed region and the max of the times."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
-        dist.init_process_group("nccl")
+        dist.init_process_group(backend)
     return world, rank, local
 
 
@@ -115,9 +117,16 @@ def max_over_ranks(x, world):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def aggregate_rate(units_per_rank, steps, t_max, world):
+    """Whole-job throughput of N replicas: every rank processes the same units per step; the job
+    time is the slowest rank's."""
+    return world * units_per_rank * steps / t_max
 
 
 # ------------------------------------------------------------------------------------------------
@@ -293,7 +302,7 @@ def own_arm(args, world, rank, local):
         t = time_steps(s, K, dt, torch)
     launches = s.launch_count()
     t = max_over_ranks(t, world)
-    value = world * cells * K / t
+    value = aggregate_rate(cells, K, t, world)
     q_head = s.state64()
 
     # ---- per-kernel-family timing (eager launches bracketed by CUDA events on the solver stream)
@@ -318,7 +327,7 @@ def own_arm(args, world, rank, local):
         s.state64(out=host_out)  # and write the result straight into pinned host memory
         torch.cuda.synchronize()
     t_e2e = max_over_ranks(time.perf_counter() - t0, world)
-    e2e_value = world * cells * e2e_steps / t_e2e
+    e2e_value = aggregate_rate(cells, e2e_steps, t_e2e, world)
     bytes_io = host_in.numel() * 8
     s.close()
     del s
@@ -553,7 +562,7 @@ def ensemble_arm(args, world, rank, local):
         t_loop += a.elapsed_time(b) / 1e3
         s.close()
     if rank == 0:
-        value = world * cells * K / t
+        value = aggregate_rate(cells, K, t, world)
         sizes = {}
         for p in plans:
             key = "%d^3 %s" % (p.n[0], "weno" if p.conv == "weno5js" else "central")
