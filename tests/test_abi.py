@@ -87,3 +87,21 @@ def test_solver_refuses_without_cuda(monkeypatch):
     monkeypatch.setattr(torch.cuda, "is_available", lambda: False)
     with pytest.raises(RuntimeError, match="CUDA"):
         runtime.Solver(tgv_plan(32))
+
+
+@pytest.mark.parametrize("cname,cls", [("osb_plan_desc", runtime.PlanDesc), ("osb_layout", runtime.Layout)])
+def test_ctypes_structs_match_the_header(cname, cls, tmp_path):
+    """Size and every field offset of the Python descriptors equal the C compiler's for the header."""
+    fields = [f[0] for f in cls._fields_]
+    src = ["#include <stddef.h>", "#include <stdio.h>", '#include "osb_gb300.h"', "int main(void) {",
+           '  printf("%%zu\\n", sizeof(%s));' % cname]
+    src += ['  printf("%%zu\\n", offsetof(%s, %s));' % (cname, f) for f in fields]
+    src += ["  return 0;", "}"]
+    c = tmp_path / "probe.c"
+    c.write_text("\n".join(src) + "\n")
+    exe = tmp_path / "probe"
+    import subprocess
+    subprocess.check_call(["gcc", "-std=c99", "-I", os.path.dirname(HEADER), str(c), "-o", str(exe)])
+    out = [int(x) for x in subprocess.check_output([str(exe)], text=True).split()]
+    assert out[0] == ctypes.sizeof(cls)
+    assert out[1:] == [getattr(cls, f).offset for f in fields]
