@@ -95,6 +95,7 @@ class GB300Writer:
         """Recognise the kernel families in alg.prg and build the Plan (all information comes from the
         algorithm tree, as for the OPSC writer)."""
         names = [n or "" for n in self.kernel_names]
+        self._check_kernel_families(names)
         ndim = self.block.ndim
         if ndim == 2:
             return self._lower_2d(precision, use_graphs)
@@ -188,6 +189,21 @@ class GB300Writer:
                     bc=tuple(tuple(p) for p in bcs), rk_a=coeff["rkold"], rk_b=coeff["rknew"],
                     weno_eps=1e-14 if conv == "weno5z" else 1e-6,  # WenoZ.eps / WenoJS.eps (weno.py)
                     use_graphs=use_graphs, ic="host", kernels=[n for n in names if n])
+
+    # The kernel families this writer lowers (by the computation names the reference gives them);
+    # anything else in the time loop (filters, other equation classes, user kernels) would be
+    # dropped silently, so it is refused.
+    _FAMILIES = re.compile(
+        r"^(CR\w+|ConstituentRelations evaluation|Convective (CD |residual|terms group)|Derivative evaluation CD |"
+        r"LLF(Weno|Teno)(_reconstruction_\d+_direction| Residual)|MetricsEquation|Viscous|Grid_based_initialisation|"
+        r"Save equations|Sub stage advancement|Temporal solution advancement|\w+ boundary dir\d side\d)")
+
+    @classmethod
+    def _check_kernel_families(cls, names):
+        other = sorted({n for n in names if n and not cls._FAMILIES.match(n)})
+        if other:
+            raise NotImplementedError("kernels outside the lowered families (filters, user-defined or other "
+                                      "equation classes are not lowered): %s" % other)
 
     def _rk_coefficients(self, names_expected):
         from sympy import preorder_traversal

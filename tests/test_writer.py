@@ -67,6 +67,18 @@ def test_published_katzer_script_lowers_to_adaptive_teno():
     assert "ConstituentRelations evaluation" in g.kernels
 
 
+def test_writer_refuses_kernels_outside_the_lowered_families():
+    """A WENO filter (filters/WENO_filter.py) or any other extra equation class adds kernels to the time
+    loop; lowering without them would change the solution, so the writer refuses."""
+    from opensbli_gb300.writer import GB300Writer
+    for case in ("tgv_central", "tgv_weno", "tgsym_central", "katzer_teno", "katzer_adaptive", "katzer_carpenter"):
+        GB300Writer._check_kernel_families(golden_plan(case).kernels)
+    names = golden_plan("tgv_central").kernels + ["Constituent Relations evaluation", "Shock sensor",
+                                                  "WENO reconstruction direction 0", "Non-linear filter application"]
+    with pytest.raises(NotImplementedError, match="Non-linear filter application"):
+        GB300Writer._check_kernel_families(names)
+
+
 def test_carpenter_faces_lower_to_their_closure():
     """Faces constructed without scheme= take the reference's default Carpenter closure; the writer
     reads each face's closure from the derivative kernels' boundary conditions."""
