@@ -272,6 +272,12 @@ class Solver:
         self._out()
 
     @staticmethod
+    def _check_shape(t, shape, what):
+        # the kernels index the array from the plan's sizes: a smaller array would be read past its end
+        if tuple(t.shape) != tuple(shape):
+            raise ValueError("%s of shape %s, the block needs %s" % (what, tuple(t.shape), tuple(shape)))
+
+    @staticmethod
     def _pinned64(t):
         return (isinstance(t, torch.Tensor) and t.device.type == "cpu" and t.dtype == torch.float64 and
                 t.is_contiguous() and t.is_pinned())
@@ -283,6 +289,7 @@ class Solver:
         pinned = self._pinned64(q)
         if not pinned:
             q = torch.as_tensor(q, dtype=torch.float64).to(self.device).contiguous()
+        self._check_shape(q, (self.layout.nvar,) + self.shape, "state")
         self._in()
         for v in range(self.layout.nvar):
             self._check(self.lib.osb_set_state64(self.ctx, v, ctypes.c_void_p(q[v].data_ptr())))
@@ -296,6 +303,7 @@ class Solver:
         """q: FP64 [nvar][...] including a halo of width h on every side (the initialisation kernel's
         range)."""
         q = torch.as_tensor(q, dtype=torch.float64).to(self.device).contiguous()
+        self._check_shape(q, (self.layout.nvar,) + tuple(k + 2 * int(h) for k in self.shape), "padded state")
         self._in()
         for v in range(self.layout.nvar):
             self._check(self.lib.osb_set_state64_padded(self.ctx, v, ctypes.c_void_p(q[v].data_ptr()), int(h)))
@@ -347,6 +355,7 @@ class Solver:
     def set_coordinate(self, x1, h=4):
         """2D blocks stretched in x1: the x1 coordinate, FP64 [n1+2h][n0+2h]; evaluates the metrics."""
         x = torch.as_tensor(x1, dtype=torch.float64).to(self.device).contiguous()
+        self._check_shape(x, tuple(k + 2 * int(h) for k in self.shape), "coordinate")
         self._in()
         self._check(self.lib.osb_set_coordinate(self.ctx, 1, ctypes.c_void_p(x.data_ptr()), int(h)))
         x.record_stream(self.stream)

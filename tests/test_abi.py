@@ -105,3 +105,12 @@ def test_ctypes_structs_match_the_header(cname, cls, tmp_path):
     out = [int(x) for x in subprocess.check_output([str(exe)], text=True).split()]
     assert out[0] == ctypes.sizeof(cls)
     assert out[1:] == [getattr(cls, f).offset for f in fields]
+
+
+def test_state_arrays_of_the_wrong_shape_are_refused():
+    """The kernels index caller arrays from the plan's sizes, so the host refuses a mismatched array
+    before any device access."""
+    import torch
+    runtime.Solver._check_shape(torch.zeros(5, 8, 8, 8), (5, 8, 8, 8), "state")
+    with pytest.raises(ValueError, match="the block needs"):
+        runtime.Solver._check_shape(torch.zeros(5, 8, 8, 7), (5, 8, 8, 8), "state")
