@@ -281,7 +281,9 @@ void osb_batch_destroy(osb_batch *batch);
  * OSB_NOALLOC_MAX_PLANES entries, resident on every device that loads the library until exit;
  * plans with more z-planes are rejected with OSB_ETOOLARGE.  The first call on a device, with that
  * device current, looks up the array's device address; make it before any stream capture.  All
- * calls share the array: calls that overlap on the GPU race and must be serialised. */
+ * calls share the array: calls that overlap on the GPU race and must be serialised.  3D plans only
+ * (2D plans get OSB_EUNSUPPORTED before any pointer is used); `stream` and `dev_out` must belong to
+ * the current device (otherwise OSB_EINVAL), because the scratch address is that device's. */
 #define OSB_NOALLOC_MAX_PLANES 2048
 int osb_reduce_noalloc(const osb_plan_desc *plan, void *const fields[5], int what, double *dev_out, void *stream);
 

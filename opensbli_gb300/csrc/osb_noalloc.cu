@@ -129,6 +129,12 @@ extern "C" int osb_reduce_noalloc(const osb_plan_desc *plan, void *const fields[
   osb_layout lay;
   int rc = osb_query_layout(plan, &lay);
   if (rc != OSB_OK) return rc;
+  // The kernels read five conserved arrays and, for the enstrophy, +-2 planes in z: 2D blocks have
+  // four arrays and no z-halo, so they are refused before any pointer is looked at (as osb_reduce does).
+  if (plan->ndim != 3) {
+    fprintf(stderr, "osb_reduce_noalloc: only 3D plans are supported (ndim = %d)\n", plan->ndim);
+    return OSB_EUNSUPPORTED;
+  }
   if (plan->n[2] > OSB_NOALLOC_MAX_PLANES) {
     fprintf(stderr, "osb_reduce_noalloc: %d z-planes exceed OSB_NOALLOC_MAX_PLANES (%d); use osb_reduce\n",
             plan->n[2], OSB_NOALLOC_MAX_PLANES);
@@ -140,6 +146,26 @@ extern "C" int osb_reduce_noalloc(const osb_plan_desc *plan, void *const fields[
   double *partials = nullptr;
   rc = partials_address(&partials);
   if (rc != OSB_OK) return rc;
+  // The scratch address belongs to the current device, so the stream and the output word must too.
+  {
+    int dev = -1, sdev = -1;
+    cudaGetDevice(&dev);
+    if (stream) {
+      cudaError_t e = cudaStreamGetDevice(static_cast<cudaStream_t>(stream), &sdev);
+      if (e != cudaSuccess || sdev != dev) {
+        cudaGetLastError();
+        fprintf(stderr, "osb_reduce_noalloc: the stream is not on the current device %d\n", dev);
+        return OSB_EINVAL;
+      }
+    }
+    cudaPointerAttributes pa;
+    cudaError_t e = cudaPointerGetAttributes(&pa, dev_out);
+    if (e != cudaSuccess || pa.type != cudaMemoryTypeDevice || pa.device != dev) {
+      cudaGetLastError();
+      fprintf(stderr, "osb_reduce_noalloc: dev_out is not device memory of the current device %d\n", dev);
+      return OSB_EINVAL;
+    }
+  }
 
   Grid g;
   g.n0 = plan->n[0];

@@ -2,7 +2,7 @@
 
 Test infrastructure (oracle).  Usage, from the repository root:
 
-    python oracle/gen/generate.py --case tgv_central [--ref /root/reference] [--out oracle/_ref]
+    python oracle/gen/generate.py --case tgv_central [--ref REFERENCE_TREE] [--out oracle/_ref]
 
 The reference generator (opensbli, read-only, imported from --ref) runs unmodified under the
 compatibility shims in compat.py.  Its OPSC writer (code_generation/opsc.py:250-282) writes
@@ -30,6 +30,7 @@ CASES = {
     "tgv_wenoz": "tgv_wenoz.py",
     "tgv_teno": "tgv_teno.py",
     "tgv_teno6": "tgv_teno6.py",
+    "tgv_filter": "tgv_filter.py",
     "katzer_teno": "katzer_teno.py",
     "katzer_carpenter": "katzer_carpenter.py",
     "katzer_adaptive": "ref:apps/katzer_SBLI/katzer_SBLI.py",
@@ -72,7 +73,9 @@ def run_case_inproc(case, ref):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", required=True, choices=sorted(CASES) + ["all"])
-    ap.add_argument("--ref", default="/root/reference")
+    from refpath import default_ref
+    ap.add_argument("--ref", default=default_ref(),
+                    help="reference tree (default: $OPENSBLI_REFERENCE, else ../reference beside the repository)")
     ap.add_argument("--out", default=os.path.join(REPO, "oracle", "_ref"))
     ap.add_argument("--inproc", action="store_true", help=argparse.SUPPRESS)
     a = ap.parse_args()

@@ -1,6 +1,6 @@
 """Lower a reference problem script with GB300Writer (test infrastructure).
 
-    python oracle/gen/lower_case.py --case tgv_central --out DIR [--ref /root/reference]
+    python oracle/gen/lower_case.py --case tgv_central --out DIR [--ref REFERENCE_TREE]
 
 Runs the case's problem script in this process with the reference generator imported from --ref
 (shims from compat.py), lets its OPSC call run as usual, hands the algorithm to
@@ -83,7 +83,9 @@ if __name__ == "__main__":
     ap = argparse.ArgumentParser()
     ap.add_argument("--case", required=True)
     ap.add_argument("--out", required=True)
-    ap.add_argument("--ref", default="/root/reference")
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from refpath import default_ref
+    ap.add_argument("--ref", default=default_ref())
     ap.add_argument("--n", type=int, default=None)
     a = ap.parse_args()
     p = lower(a.case, a.ref, a.out, a.n)

@@ -1,6 +1,6 @@
 """Regenerate the golden fixtures in tests/golden/ from the reference itself.
 
-Needs the reference tree (default /root/reference) and g++; run from the repository root:
+Needs the reference tree ($OPENSBLI_REFERENCE, else ../reference beside the repository) and g++; run from the repository root:
 
     python tests/golden/make_golden.py
 
@@ -25,6 +25,9 @@ sys.path.insert(0, REPO)
 
 from oracle import refrun  # noqa: E402
 
+sys.path.insert(0, os.path.join(REPO, "oracle", "gen"))
+from refpath import default_ref  # noqa: E402
+
 VARS = ["rho", "rhou0", "rhou1", "rhou2", "rhoE"]
 
 # case -> (grid points per axis, steps, run-time parameter overrides)
@@ -35,6 +38,8 @@ CASES = {
     "tgv_teno": (16, 10, {"dt": 2e-3, "Minf": 1.25}),
     "tgv_teno6": (16, 10, {"dt": 2e-3, "Minf": 1.25}),
     "tgsym_central": (17, 10, {"dt": 5e-3}),
+    # central skew-symmetric scheme with the WENO5 non-linear filter (constant sensor) after every step
+    "tgv_filter": (16, 10, {"dt": 3e-3, "Minf": 1.25}),
 }
 
 
@@ -86,8 +91,9 @@ def main2d(ref, only=None):
         print("wrote", case, fin["rho"].shape)
 
 
-def main(ref="/root/reference", only=None):
+def main(ref=None, only=None):
     """Regenerate every fixture, or only the case `only`."""
+    ref = ref or default_ref()
     if only is None:
         main2d(ref)
         katzer_profile(ref)
@@ -116,10 +122,11 @@ def main(ref="/root/reference", only=None):
         print("wrote", case, q.shape)
 
 
-def katzer_profile(ref="/root/reference", n1=256, n0=512):
+def katzer_profile(ref=None, n1=256, n0=512):
     """The reference's Katzer initial state on n1 = 256 rows (it is independent of x0): one padded
     column of rho, rhou0, rhou1, rhoE and x1 with a 4-point halo, for the 512 x 256 benchmark."""
     import tempfile
+    ref = ref or default_ref()
     case = "katzer_teno"
     if not refrun.available(case):
         subprocess.check_call([sys.executable, os.path.join(REPO, "oracle", "gen", "generate.py"), "--case", case,

@@ -100,3 +100,18 @@ def test_mixed_weno_error_budget_128_500_steps():
     qm = gpu_run(plan.replace(precision="mixed"), 500, dt)
     l2 = rel_l2(qm, q64)
     assert np.isfinite(qm).all() and max(l2) <= 3e-7, l2
+
+
+def test_mixed_weno_256_1000_steps_within_1e6():
+    """The headline accuracy bar: Taylor-Green 256^3, WENO5-JS + viscous, Minf 1.25, CFL 0.5, the full
+    1000 RK3 steps; the mixed path's relative L2 error against the FP64 path must stay within 1e-6 on
+    every conserved variable (Linf is reported in the message).  The FP64 run takes about five and a
+    half minutes on one GB300."""
+    plan = tgv_plan(256, conv="weno5js", Minf=1.25)
+    dt = tgv_cfl_dt(plan)
+    q64 = gpu_run(plan, 1000, dt)
+    qm = gpu_run(plan.replace(precision="mixed"), 1000, dt)
+    l2 = rel_l2(qm, q64)
+    linf = [float(np.abs(qm[v] - q64[v]).max() / np.abs(q64[v]).max()) for v in range(5)]
+    assert np.isfinite(qm).all() and np.isfinite(q64).all()
+    assert max(l2) <= 1e-6, ("L2", dict(zip(VARS, l2)), "Linf", dict(zip(VARS, linf)))

@@ -11,8 +11,11 @@ from opensbli_gb300.plan import Plan, tgv_plan, tgv_cfl_dt
 from opensbli_gb300.writer import _eval_c_expr
 from helpers import GOLDEN, golden_plan
 
-REF = "/root/reference"
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(REPO, "oracle", "gen"))
+from refpath import default_ref  # noqa: E402
+
+REF = default_ref()
 
 
 def test_plan_json_roundtrip():
