@@ -29,7 +29,9 @@
 namespace osb {
 
 namespace {
-enum { W_RHO = 0, W_RU0, W_RU1, W_RU2, W_E, W_P, W_A, W_UD, W_NF };
+enum { W_RHO = 0, W_RU0, W_RU1, W_RU2, W_E, W_P, W_A, W_UD, W_UDLO, W_PLO };
+// staged fields per point: FP32 also keeps u_D's and p's remainders for the double-float point flux
+template <typename T> __host__ __device__ constexpr int wnf() { return sizeof(T) == 4 ? 10 : 8; }
 
 // Tiles: 32 lines x 32 interfaces, four consecutive interfaces per thread, in every direction.
 // For x the shared arrays are [field][line][position] (lines are y rows of the block), otherwise
@@ -39,7 +41,8 @@ template <int DIR> struct WTile {
   static constexpr int FS = DIR == 0 ? TI + 1 : TA;  // row pitch of the flux array (x: padded)
 };
 
-template <typename T, int D, typename Pt> __device__ __forceinline__ void load_point(const Pt &P, int t, WPt<T> &w) {
+template <typename T, int D, typename Pt>
+__device__ __forceinline__ void load_point(const Pt &P, int t, WPt<T> &w, PtFlux &pf) {
   w.Q[0] = P(W_RHO, t);
   w.Q[1] = P(W_RU0, t);
   w.Q[2] = P(W_RU1, t);
@@ -48,6 +51,7 @@ template <typename T, int D, typename Pt> __device__ __forceinline__ void load_p
   w.ud = P(W_UD, t);
   w.p = P(W_P, t);
   w.a = P(W_A, t);
+  if constexpr (sizeof(T) == 4) point_flux_ff<D>(w.Q, w.ud, P(W_UDLO, t), w.p, P(W_PLO, t), pf);
 }
 }  // namespace
 
@@ -56,8 +60,10 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
   using Tl = WTile<DIR>;
   constexpr int TI = Tl::TI, TA = Tl::TA, NPT = TI + 5, FS = Tl::FS;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *sf = reinterpret_cast<T *>(smem_raw);   // [W_NF][TA][NPT] (DIR==0) or [W_NF][NPT][TA]
-  T *sflux = sf + W_NF * NPT * TA;           // [5][TA][FS] (DIR==0) or [5][TI][TA]
+  constexpr int NF = wnf<T>();
+  T *sf = reinterpret_cast<T *>(smem_raw);   // [NF][TA][NPT] (DIR==0) or [NF][NPT][TA]
+  T *sflux = sf + NF * NPT * TA;             // [5][TA][FS] (DIR==0) or [5][TI][TA]
+  T *sdf = sflux + 5 * (DIR == 0 ? TA * FS : TI * TA);  // FP32: F(left point) - F(point before), same layout
   const int tid = threadIdx.x;
   const int n[3] = {g.n0, g.n1, g.n2};
   const T gm1 = pick<T>(ph.gm1, ph.f_gm1), gama = pick<T>(ph.gama, ph.f_gama);
@@ -112,7 +118,12 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
       if (DIR == 0) { a = t / NPT; pos = t % NPT; }
       else { pos = t / TA; a = t % TA; }
       WPt<T> w;
-      point_prims<T, DIR>(r[l], gm1, gm1_lo, gama, w);
+      float lo2[2];
+      point_prims<T, DIR>(r[l], gm1, gm1_lo, gama, w, nullptr, lo2);
+      if constexpr (sizeof(T) == 4) {
+        sf[sidx(W_UDLO, pos, a)] = lo2[0];
+        sf[sidx(W_PLO, pos, a)] = lo2[1];
+      }
       sf[sidx(W_RHO, pos, a)] = w.Q[0];
       sf[sidx(W_RU0, pos, a)] = w.Q[1];
       sf[sidx(W_RU1, pos, a)] = w.Q[2];
@@ -132,16 +143,26 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
     auto P = [&](int f, int t) -> T { return sf[sidx(f, m0 + t, a)]; };
     if (a0 + a < na && d0 - 1 + m0 <= nd - 1) {
       WPt<T> W[6];
+      PtFlux fl_last, fl_new;
 #pragma unroll
-      for (int t = 0; t < 5; ++t) load_point<T, DIR>(P, t, W[t]);
+      for (int t = 0; t < 5; ++t) {
+        load_point<T, DIR>(P, t, W[t], fl_new);
+        if (t > 0) link_flux(W[t - 1], fl_last, fl_new);
+        fl_last = fl_new;
+      }
 #pragma unroll 1
       for (int w = 0; w < Tl::IPT; ++w) {
         if (d0 - 1 + m0 + w <= nd - 1) {
-          load_point<T, DIR>(P, w + 5, W[5]);
+          load_point<T, DIR>(P, w + 5, W[5], fl_new);
+          link_flux(W[4], fl_last, fl_new);
+          fl_last = fl_new;
           T fl[5];
           interface_flux<T, DIR, SCH>(W, gm1, igm1, eps, ct, fl);
 #pragma unroll
-          for (int v = 0; v < 5; ++v) sflux[fidx(v, m0 + w, a)] = fl[v];
+          for (int v = 0; v < 5; ++v) {
+            sflux[fidx(v, m0 + w, a)] = fl[v];
+            if constexpr (sizeof(T) == 4) sdf[fidx(v, m0 + w, a)] = W[1].dF[v];
+          }
         }
 #pragma unroll
         for (int t = 0; t < 5; ++t) W[t] = W[t + 1];
@@ -182,7 +203,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
     else { m = t / TA; a = t % TA; }
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
-      const T d = -mul_hl(sflux[fidx(v, m + 1, a)] - sflux[fidx(v, m, a)], idd, idd_lo);
+      T diff = sflux[fidx(v, m + 1, a)] - sflux[fidx(v, m, a)];
+      if constexpr (sizeof(T) == 4) diff = sdf[fidx(v, m + 1, a)] + diff;  // (F_i - F_{i-1}) + (G_i - G_{i-1})
+      const T d = -mul_hl(diff, idd, idd_lo);
       res.v[v][gi[l]] = ACCUM ? rv[l][v] + d : d;
     }
   }
@@ -210,6 +233,8 @@ __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> 
 
   // points c0-3 .. c0+1 fill the window; point c0+2 is the first one streamed in
   WPt<T> W[6];
+  PtFlux fl_last, fl_new;  // FP32: double-float fluxes of the newest window point and of the one added now
+  PtFlux *const pfl = sizeof(T) == 4 ? &fl_new : nullptr;
   {
     T r[5][5];
 #pragma unroll
@@ -217,7 +242,11 @@ __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> 
 #pragma unroll
       for (int v = 0; v < 5; ++v) r[t][v] = __ldg(q.v[v] + mline + (int64_t)(c0 - 3 + t) * sd);
 #pragma unroll
-    for (int t = 0; t < 5; ++t) point_prims<T, DIR>(r[t], gm1, gm1_lo, gama, W[t]);
+    for (int t = 0; t < 5; ++t) {
+      point_prims<T, DIR>(r[t], gm1, gm1_lo, gama, W[t], pfl);
+      if (t > 0) link_flux(W[t - 1], fl_last, fl_new);
+      fl_last = fl_new;
+    }
   }
   T nq[5];
 #pragma unroll
@@ -226,7 +255,9 @@ __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> 
   // interface c lies between cells c-1 and c and uses points c-3 .. c+2
 #pragma unroll 1
   for (int c = c0; c <= c1; ++c) {
-    point_prims<T, DIR>(nq, gm1, gm1_lo, gama, W[5]);
+    point_prims<T, DIR>(nq, gm1, gm1_lo, gama, W[5], pfl);
+    link_flux(W[4], fl_last, fl_new);
+    fl_last = fl_new;
     if (c < c1) {  // point c+3 <= nd+2 lies inside the halo
 #pragma unroll
       for (int v = 0; v < 5; ++v) nq[v] = __ldg(q.v[v] + mline + (int64_t)(c + 3) * sd);
@@ -242,7 +273,7 @@ __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> 
     if (c > c0) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        const T d = -mul_hl(F[v] - Fp[v], idd, idd_lo);
+        const T d = -mul_hl(flux_difference(W, v, F[v], Fp[v]), idd, idd_lo);
         res.v[v][mc] = ACCUM ? rv[v] + d : d;
       }
     }
@@ -337,6 +368,8 @@ __device__ __forceinline__ void weno_march_x_tile(const Grid &g, Fields5<const T
 
   WPt<T> W[6];
   T Fp[5];
+  PtFlux fl_last, fl_new;  // FP32: double-float fluxes of the previous and the new window point
+  PtFlux *const pfl = sizeof(T) == 4 ? &fl_new : nullptr;
   int xc = ((pfirst + 4) / XC) * XC - 4;  // chunk containing pfirst (pfirst + 4 >= 1)
   load_chunk(xc);
 #pragma unroll 1
@@ -353,7 +386,9 @@ __device__ __forceinline__ void weno_march_x_tile(const Grid &g, Fields5<const T
       T r[5];
 #pragma unroll
       for (int v = 0; v < 5; ++v) r[v] = qs[(v * 32 + lane) * QP + (p - xc)];
-      point_prims<T, 0>(r, gm1, gm1_lo, gama, W[5]);
+      point_prims<T, 0>(r, gm1, gm1_lo, gama, W[5], pfl);
+      if (p > pfirst) link_flux(W[4], fl_last, fl_new);
+      fl_last = fl_new;
       if (p >= c0 + 2) {  // window holds points c-3 .. c+2 of interface c = p - 2
         const int c = p - 2;
         T F[5] = {T(0), T(0), T(0), T(0), T(0)};  // rows past n1: defined, never stored
@@ -362,7 +397,8 @@ __device__ __forceinline__ void weno_march_x_tile(const Grid &g, Fields5<const T
           const int cc = c - 1;  // cell finished by this interface
           const int gs = ((cc + 4) / RG) * RG - 4, col = cc - gs;
 #pragma unroll
-          for (int v = 0; v < 5; ++v) rs[(v * 32 + lane) * RP + col] = -mul_hl(F[v] - Fp[v], idd, idd_lo);
+          for (int v = 0; v < 5; ++v)
+            rs[(v * 32 + lane) * RP + col] = -mul_hl(flux_difference(W, v, F[v], Fp[v]), idd, idd_lo);
           if (col == RG - 1 || cc == c1 - 1) flush(gs, c0, c1 - 1);
         }
 #pragma unroll
@@ -382,7 +418,9 @@ __global__ void __launch_bounds__(32 * BY, (sizeof(T) == 4 ? 384 : 256) / (32 * 
 
 template <typename T, int DIR> constexpr size_t tile_smem() {
   using Tl = WTile<DIR>;
-  return sizeof(T) * ((size_t)W_NF * (Tl::TI + 5) * Tl::TA + 5 * (DIR == 0 ? Tl::TA * Tl::FS : Tl::TI * Tl::TA));
+  // staged points, interface fluxes (FP32: their deviations G and the point-flux differences)
+  return sizeof(T) * ((size_t)wnf<T>() * (Tl::TI + 5) * Tl::TA +
+                      (sizeof(T) == 4 ? 2 : 1) * 5 * (DIR == 0 ? Tl::TA * Tl::FS : Tl::TI * Tl::TA));
 }
 
 template <typename T, int DIR, bool ACCUM, int SCH>

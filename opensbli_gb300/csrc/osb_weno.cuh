@@ -250,19 +250,68 @@ __device__ __forceinline__ T teno6_side(T f0, T f1, T f2, T f3, T f4, T f5, bool
 // F = (Q_{1+D}, Q_{1+c} u_D + delta_cD p, (p + Q_4) u_D), is folded into the projections below.
 template <typename T> struct WPt {
   T Q[5], ud, a, p;
+  // FP32 only: F(next point) - F(this point), each flux carried as a double-float sum (PtFlux), so
+  // the difference is rounded once relative to its own size; FP64 leaves it unused
+  T dF[5];
 };
+
+// FP32 physical flux of one point as an unevaluated sum h + l (double-float): h is the flux rounded
+// to FP32, l what that rounding and the rounding of u_D and p discarded.  The characteristic
+// projections act on flux differences between nearby points (O(delta)), so the FP32 rounding of
+// each point's flux (O(1)) would otherwise enter them as noise of relative size 2^-24 / delta.
+struct PtFlux {
+  float h[5], l[5];
+};
+
+// The double-float flux (Q_{1+D}, Q_{1+c} u_D + delta_cD p, (Q_4 + p) u_D) from u_D and p as hi/lo
+// pairs: products split by FMA (Dekker), sums by two-sum (Knuth).
+template <int D>
+__device__ __forceinline__ void point_flux_ff(const float (&r)[5], float ud, float ud_lo, float p, float p_lo,
+                                              PtFlux &pf) {
+  pf.h[0] = r[1 + D];
+  pf.l[0] = 0.0f;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    const float m = r[1 + c];
+    const float ph = __fmul_rn(m, ud);
+    const float pl = fmaf(m, ud, -ph) + m * ud_lo;
+    if (c == D) {
+      const float sh = __fadd_rn(ph, p), bv = __fsub_rn(sh, ph);
+      const float es = __fadd_rn(__fsub_rn(ph, __fsub_rn(sh, bv)), __fsub_rn(p, bv));
+      pf.h[1 + c] = sh;
+      pf.l[1 + c] = es + pl + p_lo;
+    } else {
+      pf.h[1 + c] = ph;
+      pf.l[1 + c] = pl;
+    }
+  }
+  const float sh = __fadd_rn(r[4], p), bv = __fsub_rn(sh, r[4]);
+  const float es = __fadd_rn(__fsub_rn(r[4], __fsub_rn(sh, bv)), __fsub_rn(p, bv));
+  const float h = __fmul_rn(sh, ud);
+  pf.h[4] = h;
+  pf.l[4] = fmaf(sh, ud, -h) + fmaf(es + p_lo, ud, sh * ud_lo);
+}
 
 // Primitive quantities of one point from its conserved vector.  1/rho is a correctly rounded
 // division: the velocity enters the physical flux directly, and a biased reciprocal would bias
 // every flux difference by the same relative amount, step after step.
 // In FP32, u_D and p are rounded once from their exact values (prims_f32).
+// With pf (FP32), also the point's double-float flux (point_flux_ff); lo2 (FP32, may be null)
+// receives u_D's and p's remainders, for kernels that stage points and form the flux later.
 template <typename T, int D>
-__device__ __forceinline__ void point_prims(const T (&r)[5], T gm1, T gm1_lo, T gama, WPt<T> &w) {
+__device__ __forceinline__ void point_prims(const T (&r)[5], T gm1, T gm1_lo, T gama, WPt<T> &w,
+                                            PtFlux *pf = nullptr, float *lo2 = nullptr) {
   T irho, p;
   if constexpr (sizeof(T) == 4) {
     float u[3], p_lo;
     prims_f32(r[0], r[1], r[2], r[3], r[4], gm1, gm1_lo, irho, u, p, p_lo);
     w.ud = u[D];
+    const float ud_lo = fmaf(-u[D], r[0], r[1 + D]) * irho;  // (m - u rho) exactly, over rho
+    if (pf) point_flux_ff<D>(r, u[D], ud_lo, p, p_lo, *pf);
+    if (lo2) {
+      lo2[0] = ud_lo;
+      lo2[1] = p_lo;
+    }
   } else {
     irho = T(1) / r[0];
     const T u0 = r[1] * irho, u1 = r[2] * irho, u2 = r[3] * irho;
@@ -276,13 +325,22 @@ __device__ __forceinline__ void point_prims(const T (&r)[5], T gm1, T gm1_lo, T 
   sqrt_rsqrt(gama * p * irho, w.a, ia);
 }
 
+// FP32: record F(next) - F(prev) at the earlier of two consecutive points (rounded once)
+__device__ __forceinline__ void link_flux(WPt<float> &prev, const PtFlux &fprev, const PtFlux &fnext) {
+#pragma unroll
+  for (int v = 0; v < 5; ++v) prev.dF[v] = __fsub_rn(fnext.h[v], fprev.h[v]) + __fsub_rn(fnext.l[v], fprev.l[v]);
+}
+__device__ __forceinline__ void link_flux(WPt<double> &, const PtFlux &, const PtFlux &) {}
+
 // FP32: the same flux in difference form about window point 2 (point i).  The reconstruction
 // reproduces constants (candidates are consistent, weights sum to one) and the splitting is linear,
 // so replacing every point's conserved vector Q_t and physical flux F_t by Q_t - Q_i and F_t - F_i
-// makes it return LEV.(F^ - F_i), and REV maps that to F_{i+1/2} - F_i (REV LEV = I).  The projections
-// then act on differences of neighbouring points instead of O(1) values: their FP32 rounding, which
-// otherwise dominates the flux differences that form the residual, shrinks with the differences.
-// F_{i+1/2} = F_i + (F_{i+1/2} - F_i) is rounded once.
+// makes it return LEV.(F^ - F_i), and REV maps that to G = F_{i+1/2} - F_i (REV LEV = I).  The
+// projections then act on differences of neighbouring points instead of O(1) values: their FP32
+// rounding, which otherwise dominates the flux differences that form the residual, shrinks with the
+// differences.  The flux differences F_t - F_i come from the window's consecutive-point differences
+// dF (double-float point fluxes, rounded once per difference) by prefix sums.  Returns G: the caller
+// forms F_{i+1/2} - F_{i-1/2} = (F_i - F_{i-1}) + (G_i - G_{i-1}) without ever rounding F_{i+1/2}.
 template <int D, int SCH>
 __device__ __forceinline__ void interface_flux_delta(const WPt<float> (&W)[6], const float gm1, const float igm1,
                                                      const float eps, const float ct, float out[5]) {
@@ -346,18 +404,19 @@ __device__ __forceinline__ void interface_flux_delta(const WPt<float> (&W)[6], c
       return weno5_side<T, SCH>(fp[0], fp[1], fp[2], fp[3], fp[4], eps) +
              weno5_side<T, SCH>(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
   };
-  // physical flux component v of point t: (Q_{1+D}, Q_{1+c} u_D + delta_cD p, (Q_4 + p) u_D)
-  auto flux = [&](int t, int v) -> T {
-    const WPt<T> &w = W[t];
-    if (v == 0) return w.Q[1 + D];
-    if (v == 4) return (w.Q[4] + w.p) * w.ud;
-    return v - 1 == D ? fmaf(w.Q[v], w.ud, w.p) : w.Q[v] * w.ud;
-  };
-  T F2[5];
+  // F_t - F_i for the six window points from the consecutive differences
+  T DF[6][5];
 #pragma unroll
-  for (int v = 0; v < 5; ++v) F2[v] = flux(2, v);
+  for (int v = 0; v < 5; ++v) {
+    DF[2][v] = T(0);
+    DF[3][v] = W[2].dF[v];
+    DF[4][v] = W[2].dF[v] + W[3].dF[v];
+    DF[5][v] = DF[4][v] + W[4].dF[v];
+    DF[1][v] = -W[1].dF[v];
+    DF[0][v] = -(W[1].dF[v] + W[0].dF[v]);
+  }
   auto dQ = [&](int t, int v) -> T { return t == 2 ? T(0) : W[t].Q[v] - W[2].Q[v]; };
-  auto dF = [&](int t, int v) -> T { return t == 2 ? T(0) : flux(t, v) - F2[v]; };
+  auto dF = [&](int t, int v) -> T { return DF[t][v]; };
 
   const T se1 = (D == (E1 + 1) % 3) ? T(1) : T(-1), se2 = (D == (E2 + 1) % 3) ? T(1) : T(-1);
   T rE1, rE2;
@@ -422,11 +481,13 @@ __device__ __forceinline__ void interface_flux_delta(const WPt<float> (&W)[6], c
   G[1 + e2] -= se2 * rho * rE2;
   G[4] -= se2 * rho * u[e2] * rE2;
 #pragma unroll
-  for (int v = 0; v < 5; ++v) out[v] = F2[v] + G[v];
+  for (int v = 0; v < 5; ++v) out[v] = G[v];
 }
 
 // Characteristic flux at the interface between window points 2 and 3 (points i and i+1).
-// ct: the TENO cut-off (unused by the WENO schemes).
+// ct: the TENO cut-off (unused by the WENO schemes).  FP64: out = F_{i+1/2}.  FP32: out = G =
+// F_{i+1/2} - F_i (interface_flux_delta); flux_difference below turns either into the cell's
+// F_{i+1/2} - F_{i-1/2}.
 template <typename T, int D, int SCH>
 __device__ __forceinline__ void interface_flux(const WPt<T> (&W)[6], const T gm1, const T igm1, const T eps,
                                                const T ct, T out[5]) {
@@ -548,6 +609,15 @@ __device__ __forceinline__ void interface_flux(const WPt<T> (&W)[6], const T gm1
   out[4] -= se1 * rho * u[e1] * rE1;
   out[1 + e2] -= se2 * rho * rE2;
   out[4] -= se2 * rho * u[e2] * rE2;
+}
+
+// F_{i+1/2} - F_{i-1/2} of variable v for the cell whose left interface flux (or its G) was `prev`
+// and right one `cur`; W is the window of the right interface (W[1], W[2] = points i-1, i).
+__device__ __forceinline__ float flux_difference(const WPt<float> (&W)[6], int v, float cur, float prev) {
+  return W[1].dF[v] + (cur - prev);
+}
+__device__ __forceinline__ double flux_difference(const WPt<double> (&)[6], int, double cur, double prev) {
+  return cur - prev;
 }
 
 }  // namespace osb
