@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-#define OSB_ABI_VERSION 4
+#define OSB_ABI_VERSION 5
 
 /* error codes */
 #define OSB_OK 0
@@ -59,6 +59,9 @@ extern "C" {
 #define OSB_CLOSURE_CARPENTER 1      /* Carpenter_scheme.py:6-102 (every face class's default): first
                                       * derivatives at the first four points (6-point stencils), second
                                       * derivatives as ReducedAccess */
+/* the WENO5 non-linear filter applied after every full time step (filters/WENO_filter.py:15-339) */
+#define OSB_FILTER_NONE 0
+#define OSB_FILTER_WENO5_CONSTANT 1 /* WENOFilter(block, 5, dissipation_sensor='Constant'): kappa = 1 */
 /* arithmetic: all FP64 (the reference's Double datatype, core/datatypes.py:2-13), or FP32 state
  * and flux arithmetic with the RK accumulator in FP64 */
 #define OSB_PREC_FP64 0
@@ -97,6 +100,10 @@ typedef struct osb_plan_desc {
   double teno_a1, teno_a2, sensor_eps;
   /* OSB_CLOSURE_* per axis and side of a 2D block (x0, x1; the third row is unused) */
   int closure[3][2];
+  /* OSB_FILTER_*: 3D blocks with periodic or symmetry faces (no wall faces, so the filter's Wall
+   * switch is 1 everywhere); filter_control is the generated code's shock_filter_control (1) */
+  int filter;
+  double filter_control;
 } osb_plan_desc;
 
 /* Memory layout of every per-variable array: x fastest, interior point (i,j,k) at element

@@ -77,6 +77,14 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
   }
   if (p->ndim != 3) { snprintf(why, n, "ndim %d: this library implements 2D and 3D blocks", p->ndim); return OSB_EUNSUPPORTED; }
   if (p->teno_adaptive) { snprintf(why, n, "adaptive TENO is implemented on 2D blocks"); return OSB_EUNSUPPORTED; }
+  if (p->filter != OSB_FILTER_NONE && p->filter != OSB_FILTER_WENO5_CONSTANT) {
+    snprintf(why, n, "filter %d: OSB_FILTER_NONE or OSB_FILTER_WENO5_CONSTANT", p->filter);
+    return OSB_EUNSUPPORTED;
+  }
+  if (p->filter != OSB_FILTER_NONE && !std::isfinite(p->filter_control)) {
+    snprintf(why, n, "filter_control must be finite");
+    return OSB_EINVAL;
+  }
   for (int d = 0; d < 3; ++d) {
     if (p->n[d] < 8 || p->n[d] > 4096) { snprintf(why, n, "n[%d] = %d out of range [8, 4096]", d, p->n[d]); return OSB_EINVAL; }
     if (!(p->delta[d] > 0)) { snprintf(why, n, "delta[%d] must be > 0", d); return OSB_EINVAL; }
@@ -355,6 +363,21 @@ template <typename T> void one_step(osb_ctx *c, int start, double dt, cudaStream
                            &c->launches);
     }
     cur ^= 1;
+  }
+  if (c->plan.filter != OSB_FILTER_NONE) {
+    // the WENO5 filter after the full step (the generated loop runs its kernels after the stage
+    // loop, algorithm.py:418-428 with filters/WENO_filter.py): halos of the new state, the filter's
+    // flux differences into the residual scratch, then q += dt * shock_filter_control * R
+    void **qs = cur == 0 ? c->qa : c->qb;
+    Fields5<T> r = fields<T>(c->res);
+    {
+      ProfScope ps(c, PF_HALO, s);
+      launch_halos<T>(*c, fields<T>(qs), s, &c->launches);
+    }
+    ProfScope ps(c, PF_OTHER, s);
+    for (int dir = 0; dir < 3; ++dir) launch_filter_dir<T>(*c, fields<const T>(qs), r, dir, s, &c->launches);
+    launch_filter_apply<T>(*c, fields<T>(qs), fields_d(c->qold), fields<const T>(c->res), dt * c->plan.filter_control,
+                           s, &c->launches);
   }
 }
 

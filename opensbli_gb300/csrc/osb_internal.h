@@ -89,6 +89,13 @@ template <typename T>
 void launch_weno_dir(const Ctx &c, Fields5<const T> q, Fields5<T> r, int dir, cudaStream_t s, int64_t *launches);
 template <typename T>
 void launch_weno_cfg(const Ctx &c, Fields5<const T> q, Fields5<T> r, int dir, WenoCfg w, cudaStream_t s);
+// the WENO5 non-linear filter: flux pass of one direction (x writes r, y and z accumulate), and the
+// update qold += dt_fc * r, q = qold (FP32 state rounded once)
+template <typename T>
+void launch_filter_dir(const Ctx &c, Fields5<const T> q, Fields5<T> r, int dir, cudaStream_t s, int64_t *launches);
+template <typename T>
+void launch_filter_apply(const Ctx &c, Fields5<T> q, Fields5<double> qold, Fields5<const T> r, double dt_fc,
+                         cudaStream_t s, int64_t *launches);
 
 template <typename T>
 void launch_central_rk(const Ctx &c, Fields5<const T> q, Fields5<T> qnew, Fields5<double> qold, Fields5<T> rin,

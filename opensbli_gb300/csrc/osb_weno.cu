@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
 #pragma unroll
           for (int v = 0; v < 5; ++v) {
             sflux[fidx(v, m0 + w, a)] = fl[v];
-            if constexpr (sizeof(T) == 4) sdf[fidx(v, m0 + w, a)] = W[1].dF[v];
+            if constexpr (sizeof(T) == 4 && SCH != SCH_FILTER) sdf[fidx(v, m0 + w, a)] = W[1].dF[v];
           }
         }
 #pragma unroll
@@ -204,7 +204,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
       T diff = sflux[fidx(v, m + 1, a)] - sflux[fidx(v, m, a)];
-      if constexpr (sizeof(T) == 4) diff = sdf[fidx(v, m + 1, a)] + diff;  // (F_i - F_{i-1}) + (G_i - G_{i-1})
+      if constexpr (sizeof(T) == 4 && SCH != SCH_FILTER)
+        diff = sdf[fidx(v, m + 1, a)] + diff;  // (F_i - F_{i-1}) + (G_i - G_{i-1})
       const T d = -mul_hl(diff, idd, idd_lo);
       res.v[v][gi[l]] = ACCUM ? rv[l][v] + d : d;
     }
@@ -273,7 +274,7 @@ __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> 
     if (c > c0) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        const T d = -mul_hl(flux_difference(W, v, F[v], Fp[v]), idd, idd_lo);
+        const T d = -mul_hl(flux_difference<SCH>(W, v, F[v], Fp[v]), idd, idd_lo);
         res.v[v][mc] = ACCUM ? rv[v] + d : d;
       }
     }
@@ -398,7 +399,7 @@ __device__ __forceinline__ void weno_march_x_tile(const Grid &g, Fields5<const T
           const int gs = ((cc + 4) / RG) * RG - 4, col = cc - gs;
 #pragma unroll
           for (int v = 0; v < 5; ++v)
-            rs[(v * 32 + lane) * RP + col] = -mul_hl(flux_difference(W, v, F[v], Fp[v]), idd, idd_lo);
+            rs[(v * 32 + lane) * RP + col] = -mul_hl(flux_difference<SCH>(W, v, F[v], Fp[v]), idd, idd_lo);
           if (col == RG - 1 || cc == c1 - 1) flush(gs, c0, c1 - 1);
         }
 #pragma unroll
@@ -575,6 +576,43 @@ void launch_batch_weno(const int4 *items, int nitems, int *counter, int parity, 
   }
 }
 
+// The filter's update of the interior (filters/WENO_filter.py:258-282, kappa = Wall = 1): the FP64
+// master copy takes q + dt * shock_filter_control * R, the bound state its value (FP32: rounded once)
+template <typename T>
+__global__ void k_filter_apply(Grid g, Fields5<T> q, Fields5<double> qold, Fields5<const T> r, double dt_fc) {
+  const int64_t N = (int64_t)g.n0 * g.n1 * g.n2;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.n0), j = (int)((t / g.n0) % g.n1), k = (int)(t / ((int64_t)g.n0 * g.n1));
+    const int64_t n = gidx(g, i, j, k);
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      const double x = dt_fc * (double)r.v[v][n] + qold.v[v][n];
+      qold.v[v][n] = x;
+      q.v[v][n] = (T)x;
+    }
+  }
+}
+
+template <typename T>
+void launch_filter_apply(const Ctx &c, Fields5<T> q, Fields5<double> qold, Fields5<const T> r, double dt_fc,
+                         cudaStream_t s, int64_t *launches) {
+  const int64_t N = (int64_t)c.g.n0 * c.g.n1 * c.g.n2;
+  int blocks = (int)((N + 255) / 256);
+  const int cap = c.num_sms * 8;
+  if (blocks > cap) blocks = cap;
+  k_filter_apply<T><<<blocks, 256, 0, s>>>(c.g, q, qold, r, dt_fc);
+  ++*launches;
+}
+
+// The WENO5 filter's flux passes: the same kernel shapes with the filter's interface flux
+template <typename T>
+void launch_filter_dir(const Ctx &c, Fields5<const T> q, Fields5<T> r, int dir, cudaStream_t s, int64_t *launches) {
+  if (dir == 0) launch_shape<T, 0, false, SCH_FILTER>(c, q, r, c.wcfg[0], s);
+  else if (dir == 1) launch_shape<T, 1, true, SCH_FILTER>(c, q, r, c.wcfg[1], s);
+  else launch_shape<T, 2, true, SCH_FILTER>(c, q, r, c.wcfg[2], s);
+  ++*launches;
+}
+
 template <typename T, int DIR, bool ACCUM> static void attr_dir() {
   cudaFuncSetAttribute(k_weno<T, DIR, ACCUM, SCH_JS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)tile_smem<T, DIR>());
@@ -583,6 +621,8 @@ template <typename T, int DIR, bool ACCUM> static void attr_dir() {
   cudaFuncSetAttribute(k_weno<T, DIR, ACCUM, SCH_TENO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)tile_smem<T, DIR>());
   cudaFuncSetAttribute(k_weno<T, DIR, ACCUM, SCH_TENO6>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)tile_smem<T, DIR>());
+  cudaFuncSetAttribute(k_weno<T, DIR, ACCUM, SCH_FILTER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)tile_smem<T, DIR>());
 }
 template <typename T> void setup_weno() {
@@ -604,6 +644,10 @@ template <typename T> void setup_weno() {
                        (int)march_x_smem<T, 4>());
   cudaFuncSetAttribute(k_weno_march_x<T, 8, SCH_TENO6>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)march_x_smem<T, 8>());
+  cudaFuncSetAttribute(k_weno_march_x<T, 4, SCH_FILTER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)march_x_smem<T, 4>());
+  cudaFuncSetAttribute(k_weno_march_x<T, 8, SCH_FILTER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)march_x_smem<T, 8>());
   attr_dir<T, 0, false>();
   attr_dir<T, 1, true>();
   attr_dir<T, 2, true>();
@@ -611,6 +655,14 @@ template <typename T> void setup_weno() {
 template void setup_weno<float>();
 template void setup_weno<double>();
 
+template void launch_filter_apply<float>(const Ctx &, Fields5<float>, Fields5<double>, Fields5<const float>, double,
+                                         cudaStream_t, int64_t *);
+template void launch_filter_apply<double>(const Ctx &, Fields5<double>, Fields5<double>, Fields5<const double>,
+                                          double, cudaStream_t, int64_t *);
+template void launch_filter_dir<float>(const Ctx &, Fields5<const float>, Fields5<float>, int, cudaStream_t,
+                                       int64_t *);
+template void launch_filter_dir<double>(const Ctx &, Fields5<const double>, Fields5<double>, int, cudaStream_t,
+                                        int64_t *);
 template void launch_weno_dir<float>(const Ctx &, Fields5<const float>, Fields5<float>, int, cudaStream_t, int64_t *);
 template void launch_weno_dir<double>(const Ctx &, Fields5<const double>, Fields5<double>, int, cudaStream_t,
                                       int64_t *);

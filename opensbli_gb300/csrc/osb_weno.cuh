@@ -46,7 +46,8 @@ __device__ __forceinline__ void sqrt_rsqrt(double x, double &s, double &is) {
 }
 
 // Schemes of the nonlinear weights
-enum { SCH_JS = 0, SCH_Z = 1, SCH_TENO = 2, SCH_TENO6 = 3 };
+// (SCH_FILTER: the characteristic flux of the WENO5 non-linear filter, filter_flux)
+enum { SCH_JS = 0, SCH_Z = 1, SCH_TENO = 2, SCH_TENO6 = 3, SCH_FILTER = 4 };
 
 // One WENO5 side.  f0..f4 are the five stencil values ordered from the far upwind point to the
 // far downwind one (for the right-going side: points i-2..i+2; for the left-going side the caller
@@ -484,34 +485,17 @@ __device__ __forceinline__ void interface_flux_delta(const WPt<float> (&W)[6], c
   for (int v = 0; v < 5; ++v) out[v] = G[v];
 }
 
-// Characteristic flux at the interface between window points 2 and 3 (points i and i+1).
-// ct: the TENO cut-off (unused by the WENO schemes).  FP64: out = F_{i+1/2}.  FP32: out = G =
-// F_{i+1/2} - F_i (interface_flux_delta); flux_difference below turns either into the cell's
-// F_{i+1/2} - F_{i-1/2}.
-template <typename T, int D, int SCH>
-__device__ __forceinline__ void interface_flux(const WPt<T> (&W)[6], const T gm1, const T igm1, const T eps,
-                                               const T ct, T out[5]) {
-  if constexpr (sizeof(T) == 4) {
-    interface_flux_delta<D, SCH>(W, gm1, igm1, eps, ct, out);
-    return;
-  }
+// The characteristic flux about the averaged interface state (rho, u, a; irho = 1/rho, ia = 1/a):
+// LEV/REV of the Euler eigensystem for the unit normal of direction D, CF = LEV.F and CS = LEV.Q at
+// the six window points, the LLF wave speeds over the window, recon(cf, cs, lam) per characteristic,
+// and REV back to conserved space.  Shared by the characteristic flux of the residual (Roe average,
+// FP64 arithmetic) and by the WENO filter (simple average, both precisions).
+template <typename T, int D, typename Recon>
+__device__ __forceinline__ void char_flux(const WPt<T> (&W)[6], const T gm1, const T igm1, const T rho, const T irho,
+                                          const T (&u)[3], const T a, const T ia, Recon recon, T out[5]) {
   constexpr int E1 = (D + 1) % 3, E2 = (D + 2) % 3;  // the two tangential axes (shear rows)
   constexpr int e1 = 3 - E1 - D, e2 = 3 - E2 - D;    // third axis of each shear row
-  // ---- Roe average of points 2 and 3
-  const T rl = W[2].Q[0], rr = W[3].Q[0];
-  T sl, sr, isl, isr;  // sqrt(rho) and 1/sqrt(rho) of both sides
-  sqrt_rsqrt(rl, sl, isl);
-  sqrt_rsqrt(rr, sr, isr);
-  const T rho = sl * sr;
-  const T inv_s = rcp_t(sl + sr);
-  T u[3];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) u[c] = inv_s * (W[2].Q[1 + c] * isl + W[3].Q[1 + c] * isr);
-  const T Hh = inv_s * ((W[2].p + W[2].Q[4]) * isl + (W[3].p + W[3].Q[4]) * isr);
   const T usq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
-  T a, ia;
-  sqrt_rsqrt(gm1 * (Hh - T(0.5) * usq), a, ia);
-  const T irho = isl * isr;
   const T phi = gm1 * T(0.5) * usq;
   const T bt = T(0.70710678118654752440) * irho * ia;  // 1/(sqrt(2) rho a)
   const T al = T(0.70710678118654752440) * rho * ia;   // rho/(sqrt(2) a)
@@ -525,23 +509,6 @@ __device__ __forceinline__ void interface_flux(const WPt<T> (&W)[6], const T gm1
     lam_p = max_t(lam_p, abs_t(W[t].ud + W[t].a));
     lam_m = max_t(lam_m, abs_t(W[t].a - W[t].ud));
   }
-  auto recon = [&](const T (&cf)[6], const T (&cs)[6], T lam) -> T {
-    T fp[6], fm[6];
-#pragma unroll
-    for (int t = 0; t < 6; ++t) {
-      fp[t] = cf[t] + lam * cs[t];
-      fm[t] = cf[t] - lam * cs[t];
-    }
-    if constexpr (SCH == SCH_TENO6)
-      return teno6_side<T>(fp[0], fp[1], fp[2], fp[3], fp[4], fp[5], true, eps, ct) +
-             teno6_side<T>(fm[5], fm[4], fm[3], fm[2], fm[1], fm[0], false, eps, ct);
-    else if constexpr (SCH == SCH_TENO)
-      return teno5_side<T>(fp[0], fp[1], fp[2], fp[3], fp[4], eps, ct) +
-             teno5_side<T>(fm[5], fm[4], fm[3], fm[2], fm[1], eps, ct);
-    else
-      return weno5_side<T, SCH>(fp[0], fp[1], fp[2], fp[3], fp[4], eps) +
-             weno5_side<T, SCH>(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
-  };
 
   // ---- shear rows: LEV_r . X = (s/rho)(u_e X_0 - X_{1+e}); for X = F: X_0 = Q_{1+D}, X_{1+e} = Q_{1+e} u_D
   const T se1 = (D == (E1 + 1) % 3) ? T(1) : T(-1), se2 = (D == (E2 + 1) % 3) ? T(1) : T(-1);
@@ -611,11 +578,116 @@ __device__ __forceinline__ void interface_flux(const WPt<T> (&W)[6], const T gm1
   out[4] -= se2 * rho * u[e2] * rE2;
 }
 
+// WENO5-JS side (weno5_side) that also reports the filter's weight sensor of that side,
+// sum_r |omega_r / d_r - 1|^4 / (9^4 + 2) (schemes/spatial/weno.py:436-452, sensor_theta = 4; d_r the
+// optimal weights, so 1/min(d) - 1 = 9)
+template <typename T> __device__ __forceinline__ T weno5_side_sensor(T f0, T f1, T f2, T f3, T f4, T eps, T &sens) {
+  const T d0 = f1 - f0, d1 = f2 - f1, d2 = f3 - f2, d3 = f4 - f3;
+  const T t0 = d3 - d2, t1 = d2 - d1, t2 = d1 - d0;
+  const T s0 = d3 - T(3) * d2, s1 = d1 + d2, s2 = T(3) * d1 - d0;
+  const T c13 = T(13.0 / 48.0), c14 = T(1.0 / 16.0);
+  const T e0 = c13 * t0 * t0 + c14 * s0 * s0 + eps;
+  const T e1 = c13 * t1 * t1 + c14 * s1 * s1 + eps;
+  const T e2 = c13 * t2 * t2 + c14 * s2 * s2 + eps;
+  const T q0 = e0 * e0, q1 = e1 * e1, q2 = e2 * e2;
+  // alphas over the common factor q0 q1 q2 (one division)
+  const T a0 = T(3.0 / 10.0) * (q1 * q2), a1 = T(3.0 / 5.0) * (q0 * q2), a2 = T(1.0 / 10.0) * (q0 * q1);
+  const T is = T(1) / (a0 + a1 + a2);
+  const T w0 = a0 * is, w1 = a1 * is, w2 = a2 * is;
+  const T x0 = T(10.0 / 3.0) * w0 - T(1), x1 = T(5.0 / 3.0) * w1 - T(1), x2 = T(10) * w2 - T(1);
+  sens = ((x0 * x0) * (x0 * x0) + (x1 * x1) * (x1 * x1) + (x2 * x2) * (x2 * x2)) * T(1.0 / 6563.0);
+  const T p1 = T(0.5) * f2 + T(1.0 / 12.0) * d1 + T(1.0 / 6.0) * d2;
+  return p1 + (T(-1.0 / 12.0) * w0 * (t0 - t1) + T(1.0 / 6.0) * w2 * (t2 - t1));
+}
+
+// Interface flux of the WENO5 non-linear filter (filters/WENO_filter.py:15-339 with the LLF WENO5-JS
+// scheme it builds, schemes/spatial/weno.py:474-483): the characteristic flux about the simple average
+// of rho, u and a over points i, i+1 (averaging.py SimpleAverage([0, 1])), whose reconstructed
+// characteristics are replaced by rj (Recon - central) with rj the larger of the two sides' weight
+// sensors and central = (CF_{i-2} - 8 CF_{i-1} + 37 CF_i + 37 CF_{i+1} - 8 CF_{i+2} + CF_{i+3}) / 60,
+// the 6th-order central interpolation of the characteristic fluxes (shock_capturing.py:399-412, 440-442).
+template <typename T, int D>
+__device__ __forceinline__ void filter_flux(const WPt<T> (&W)[6], const T gm1, const T igm1, T out[5]) {
+  const T eps = T(1e-6);  // the filter's LLFWeno is WENO-JS, whose epsilon is 1e-6 (weno.py:341-369)
+  const T rho = T(0.5) * (W[3].Q[0] + W[2].Q[0]);
+  const T ir2 = T(1) / W[2].Q[0], ir3 = T(1) / W[3].Q[0];
+  T u[3];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) u[c] = T(0.5) * (W[3].Q[1 + c] * ir3 + W[2].Q[1 + c] * ir2);
+  const T a = T(0.5) * (W[2].a + W[3].a);
+  const T ia = T(1) / a, irho = T(1) / rho;
+  auto recon = [&](const T (&cf)[6], const T (&cs)[6], T lam) -> T {
+    T fp[6], fm[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      fp[t] = cf[t] + lam * cs[t];
+      fm[t] = cf[t] - lam * cs[t];
+    }
+    T sp, sm;
+    const T rec = weno5_side_sensor<T>(fp[0], fp[1], fp[2], fp[3], fp[4], eps, sp) +
+                  weno5_side_sensor<T>(fm[5], fm[4], fm[3], fm[2], fm[1], eps, sm);
+    const T central = T(1.0 / 60.0) * ((cf[0] + cf[5]) - T(8) * (cf[1] + cf[4]) + T(37) * (cf[2] + cf[3]));
+    return max_t(sp, sm) * (rec - central);
+  };
+  char_flux<T, D>(W, gm1, igm1, rho, irho, u, a, ia, recon, out);
+}
+
+// Characteristic flux at the interface between window points 2 and 3 (points i and i+1), and for
+// SCH_FILTER the WENO filter's flux there.  ct: the TENO cut-off (unused by the other schemes).
+// FP64 and the filter: out = F_{i+1/2}.  Other FP32 schemes: out = G = F_{i+1/2} - F_i
+// (interface_flux_delta); flux_difference below turns either into the cell's F_{i+1/2} - F_{i-1/2}.
+template <typename T, int D, int SCH>
+__device__ __forceinline__ void interface_flux(const WPt<T> (&W)[6], const T gm1, const T igm1, const T eps,
+                                               const T ct, T out[5]) {
+  if constexpr (SCH == SCH_FILTER) {
+    filter_flux<T, D>(W, gm1, igm1, out);
+  } else if constexpr (sizeof(T) == 4) {
+    interface_flux_delta<D, SCH>(W, gm1, igm1, eps, ct, out);
+  } else {
+    // ---- Roe average of points 2 and 3
+    const T rl = W[2].Q[0], rr = W[3].Q[0];
+    T sl, sr, isl, isr;  // sqrt(rho) and 1/sqrt(rho) of both sides
+    sqrt_rsqrt(rl, sl, isl);
+    sqrt_rsqrt(rr, sr, isr);
+    const T rho = sl * sr;
+    const T inv_s = rcp_t(sl + sr);
+    T u[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) u[c] = inv_s * (W[2].Q[1 + c] * isl + W[3].Q[1 + c] * isr);
+    const T Hh = inv_s * ((W[2].p + W[2].Q[4]) * isl + (W[3].p + W[3].Q[4]) * isr);
+    const T usq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+    T a, ia;
+    sqrt_rsqrt(gm1 * (Hh - T(0.5) * usq), a, ia);
+    const T irho = isl * isr;
+    auto recon = [&](const T (&cf)[6], const T (&cs)[6], T lam) -> T {
+      T fp[6], fm[6];
+#pragma unroll
+      for (int t = 0; t < 6; ++t) {
+        fp[t] = cf[t] + lam * cs[t];
+        fm[t] = cf[t] - lam * cs[t];
+      }
+      if constexpr (SCH == SCH_TENO6)
+        return teno6_side<T>(fp[0], fp[1], fp[2], fp[3], fp[4], fp[5], true, eps, ct) +
+               teno6_side<T>(fm[5], fm[4], fm[3], fm[2], fm[1], fm[0], false, eps, ct);
+      else if constexpr (SCH == SCH_TENO)
+        return teno5_side<T>(fp[0], fp[1], fp[2], fp[3], fp[4], eps, ct) +
+               teno5_side<T>(fm[5], fm[4], fm[3], fm[2], fm[1], eps, ct);
+      else
+        return weno5_side<T, SCH>(fp[0], fp[1], fp[2], fp[3], fp[4], eps) +
+               weno5_side<T, SCH>(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
+    };
+    char_flux<T, D>(W, gm1, igm1, rho, irho, u, a, ia, recon, out);
+  }
+}
+
 // F_{i+1/2} - F_{i-1/2} of variable v for the cell whose left interface flux (or its G) was `prev`
 // and right one `cur`; W is the window of the right interface (W[1], W[2] = points i-1, i).
-__device__ __forceinline__ float flux_difference(const WPt<float> (&W)[6], int v, float cur, float prev) {
-  return W[1].dF[v] + (cur - prev);
+// (FP32 residual fluxes come as G; the filter's fluxes, and all FP64 ones, as the full flux)
+template <int SCH> __device__ __forceinline__ float flux_difference(const WPt<float> (&W)[6], int v, float cur, float prev) {
+  if constexpr (SCH == SCH_FILTER) return cur - prev;
+  else return W[1].dF[v] + (cur - prev);
 }
+template <int SCH>
 __device__ __forceinline__ double flux_difference(const WPt<double> (&)[6], int, double cur, double prev) {
   return cur - prev;
 }

@@ -78,6 +78,10 @@ class Plan:
     # [axis][side]: "reduced_access" (boundary_conditions/reduced_access_scheme.py) or "carpenter"
     # (boundary_conditions/Carpenter_scheme.py, the reference's default)
     closure: Tuple[Tuple[str, str], ...] = (("reduced_access", "reduced_access"),) * 2
+    # the WENO5 non-linear filter after every full step (filters/WENO_filter.py): "none" or
+    # "weno5_constant" (dissipation_sensor='Constant'); filter_control = shock_filter_control
+    filter: str = "none"
+    filter_control: float = 1.0
     name: str = ""
     kernels: List[str] = dataclasses.field(default_factory=list)  # the reference kernel names lowered
 

@@ -12,7 +12,7 @@ import torch
 
 from . import build as _build
 
-OSB_ABI_VERSION = 4
+OSB_ABI_VERSION = 5
 ERRORS = {
     -1: "invalid plan or argument",
     -2: "unsupported kernel pattern",
@@ -30,6 +30,7 @@ BC = {"periodic": 0, "symmetry": 1, "inlet_pressure_extrapolate": 2, "extrapolat
       "dirichlet": 5}
 PREC = {"fp64": 0, "mixed": 1}
 CLOSURE = {"reduced_access": 0, "carpenter": 1}
+FILTER = {"none": 0, "weno5_constant": 1}
 RED = {"ke": 0, "enstrophy": 1, "nancheck": 2}
 
 
@@ -64,6 +65,8 @@ class PlanDesc(ctypes.Structure):
         ("teno_a2", ctypes.c_double),
         ("sensor_eps", ctypes.c_double),
         ("closure", (ctypes.c_int * 2) * 3),
+        ("filter", ctypes.c_int),
+        ("filter_control", ctypes.c_double),
     ]
 
 
@@ -199,6 +202,8 @@ def make_plan_desc(plan):
     for a in range(len(plan.closure)):
         for side in range(2):
             d.closure[a][side] = CLOSURE[plan.closure[a][side]]
+    d.filter = FILTER[plan.filter]
+    d.filter_control = plan.filter_control
     return d
 
 

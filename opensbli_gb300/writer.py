@@ -185,10 +185,58 @@ class GB300Writer:
         other_bc = [n for n in names if "boundary dir" in n and not n.startswith("Symmetry")]
         if other_bc or any(b is None for pair in bcs for b in pair):
             raise NotImplementedError("unsupported boundary conditions: %s" % (other_bc or bcs))
+        filt, fc = self._weno_filter()
         return Plan(ndim=3, conv=conv, visc="const" if visc else "none", rk="rk3", precision=precision,
                     bc=tuple(tuple(p) for p in bcs), rk_a=coeff["rkold"], rk_b=coeff["rknew"],
                     weno_eps=1e-14 if conv == "weno5z" else 1e-6,  # WenoZ.eps / WenoJS.eps (weno.py)
-                    use_graphs=use_graphs, ic="host", kernels=[n for n in names if n])
+                    use_graphs=use_graphs, ic="host", kernels=[n for n in names if n], filter=filt,
+                    filter_control=fc)
+
+    def _weno_filter(self):
+        """Recognise the WENO5 non-linear filter (filters/WENO_filter.py:15-339) in the time loop: its
+        constituent relations, one reconstruction kernel per direction (LLFWeno(5, 'JS') with the simple
+        average, the weight sensor rj and the central subtraction, shock_capturing.py:399-442) and the
+        application kernel q += dt * shock_filter_control * Wall * kappa * R.  Returns (filter kind,
+        shock_filter_control).  Only the 'Constant' dissipation sensor (kappa = 1) is lowered; the
+        Ducros sensor's kernels are refused."""
+        recon = self._kernels("User kernel: WENO reconstruction direction")
+        app = self._kernels("User kernel: Non-linear filter application")
+        cr = self._kernels("User kernel: Constituent Relations evaluation")
+        if not recon and not app and not cr:
+            return "none", 1.0
+        if len(recon) != 3 or len(app) != 1 or len(cr) != 1:
+            raise NotImplementedError("WENO filter: one reconstruction kernel per direction, one constituent-"
+                                      "relation and one application kernel expected")
+        for k in recon:
+            lhs = self._lhs_names(k)
+            if not {"beta_0", "alpha_0", "omega_0", "rj0", "Recon_0"} <= lhs:
+                raise NotImplementedError("WENO filter: WENO5 reconstruction with the weight sensor expected in %s"
+                                          % k.computation_name)
+            if self._max_offset([k]) != 3:
+                raise NotImplementedError("WENO filter: 5th-order stencil expected in %s" % k.computation_name)
+            avg = [e for e in k.equations if str(e.lhs).startswith("AVG_") and str(e.lhs).endswith("_rho")]
+            if not avg or "sqrt" in str(avg[0].rhs):
+                raise NotImplementedError("WENO filter: the simple average expected in %s" % k.computation_name)
+            alpha0 = [e for e in k.equations if str(e.lhs) == "alpha_0"]
+            if not alpha0 or "Abs(" in str(alpha0[0].rhs):
+                raise NotImplementedError("WENO filter: WENO-JS weights expected in %s" % k.computation_name)
+        fc, kappa = None, False
+        from sympy import preorder_traversal
+        for e in app[0].equations:
+            for a in preorder_traversal(e.rhs):
+                if type(a).__name__ == "ConstantObject" and str(a) == "shock_filter_control":
+                    fc = float(a.value)
+                elif "kappa" in str(a) and type(a).__name__ in ("DataSet", "GridVariable"):
+                    kappa = True
+            if str(e.lhs) == "Wall" and str(e.rhs) != "1":
+                raise NotImplementedError("WENO filter next to wall faces is not lowered (3D periodic/symmetry "
+                                          "blocks only)")
+        if kappa or self._kernels("User kernel: Shock sensor"):
+            raise NotImplementedError("WENO filter with the Ducros dissipation sensor is not lowered "
+                                      "(dissipation_sensor='Constant' is)")
+        if fc is None:
+            raise NotImplementedError("WENO filter: shock_filter_control not found in the application kernel")
+        return "weno5_constant", fc
 
     # The kernel families this writer lowers (by the computation names the reference gives them);
     # anything else in the time loop (filters, other equation classes, user kernels) would be
@@ -196,7 +244,8 @@ class GB300Writer:
     _FAMILIES = re.compile(
         r"^(CR\w+|ConstituentRelations evaluation|Convective (CD |residual|terms group)|Derivative evaluation CD |"
         r"LLF(Weno|Teno)(_reconstruction_\d+_direction| Residual)|MetricsEquation|Viscous|Grid_based_initialisation|"
-        r"Save equations|Sub stage advancement|Temporal solution advancement|\w+ boundary dir\d side\d)")
+        r"Save equations|Sub stage advancement|Temporal solution advancement|\w+ boundary dir\d side\d|"
+        r"User kernel: (Constituent Relations evaluation|WENO reconstruction direction \d|Non-linear filter application))")
 
     @classmethod
     def _check_kernel_families(cls, names):
@@ -224,6 +273,8 @@ class GB300Writer:
         RungeKuttaLS(3), inlet/extrapolation faces in x0, isothermal wall/Dirichlet faces in x1."""
         import sympy
         names = [n or "" for n in self.kernel_names]
+        if any(n.startswith("User kernel:") for n in names):
+            raise NotImplementedError("the WENO filter is lowered on 3D blocks only")
         teno = self._kernels("LLFTeno_reconstruction_")
         weno = self._kernels("LLFWeno_reconstruction_")
         if bool(teno) == bool(weno) or len(teno or weno) != 2:

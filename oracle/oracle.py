@@ -35,7 +35,12 @@ class Cfg(ctypes.Structure):
         ("teno_ct", ctypes.c_double),
         ("teno_eps", ctypes.c_double),
         ("dt", ctypes.c_double),
+        ("filter", ctypes.c_int),
+        ("filter_control", ctypes.c_double),
     ]
+
+
+FILTER = {"none": 0, "weno5_constant": 1}
 
 
 def build(force=False):
@@ -63,7 +68,7 @@ def lib():
 
 
 def make_cfg(n, delta, gama=1.4, Minf=0.1, Re=1600.0, Pr=0.71, conv="central_skew", visc="const", rk="rk3",
-             bc="periodic", dt=5e-3, teno_ct=1e-5, teno_eps=1e-15):
+             bc="periodic", dt=5e-3, teno_ct=1e-5, teno_eps=1e-15, filter="none", filter_control=1.0):
     c = Cfg()
     c.ndim = len(n) if len(n) == 2 else 3
     nn = list(n) + [1] * (3 - len(n))
@@ -77,6 +82,7 @@ def make_cfg(n, delta, gama=1.4, Minf=0.1, Re=1600.0, Pr=0.71, conv="central_ske
         for s in range(2):
             c.bc[d][s] = BC[bc if isinstance(bc, str) else bc[d][s]]
     c.teno_ct, c.teno_eps, c.dt = teno_ct, teno_eps, dt
+    c.filter, c.filter_control = FILTER[filter], filter_control
     return c
 
 

@@ -133,7 +133,10 @@ static void bc_symmetry(st_t *s, int dir, int side, int depth) {
   }
 }
 
-static int halo_depth(const st_t *s) { return s->c.conv == OSBO_CONV_CENTRAL_SKEW ? 2 : 3; }
+/* exchanged depth: the central stencils reach 2 points, the characteristic fluxes (and the WENO filter) 3 */
+static int halo_depth(const st_t *s) {
+  return s->c.conv == OSBO_CONV_CENTRAL_SKEW && s->c.filter == OSBO_FILTER_NONE ? 2 : 3;
+}
 
 static void apply_bcs(st_t *s) {
   int depth = halo_depth(s);
@@ -306,7 +309,7 @@ static void residual_viscous(st_t *s) {
  * folds the 1/2 into the smoothness indicators (1/4 of Jiang-Shu's, expanded as products) and into
  * the candidate stencils (1/2 of the usual c_rj).  The expressions below keep that form and term
  * order.  fp = f at points i-2..i+2 (upwind side), fm = f at points i-1..i+3. */
-static double weno5_plus(const double f[5], int z) {
+static double weno5_plus_w(const double f[5], int z, double *w) {
   const double b0 = 0.5 * f[2] * ((5.0 / 3.0) * f[2] - (31.0 / 6.0) * f[3] + (11.0 / 6.0) * f[4]) +
                     0.5 * f[3] * ((25.0 / 6.0) * f[3] - (19.0 / 6.0) * f[4]) + (1.0 / 3.0) * f[4] * f[4];
   const double b1 = 0.5 * f[1] * ((2.0 / 3.0) * f[1] - (13.0 / 6.0) * f[2] + (5.0 / 6.0) * f[3]) +
@@ -326,11 +329,13 @@ static double weno5_plus(const double f[5], int z) {
     a2 = (1.0 / 10.0) / ((b2 + 1e-6) * (b2 + 1e-6));
   }
   const double inv = 1.0 / (a0 + a1 + a2);
+  if (w) { w[0] = a0 * inv; w[1] = a1 * inv; w[2] = a2 * inv; }
   return a0 * inv * ((1.0 / 6.0) * f[2] + (5.0 / 12.0) * f[3] - (1.0 / 12.0) * f[4]) +
          a1 * inv * (-(1.0 / 12.0) * f[1] + (5.0 / 12.0) * f[2] + (1.0 / 6.0) * f[3]) +
          a2 * inv * ((1.0 / 6.0) * f[0] - (7.0 / 12.0) * f[1] + (11.0 / 12.0) * f[2]);
 }
-static double weno5_minus(const double g[5], int z) {
+static double weno5_plus(const double f[5], int z) { return weno5_plus_w(f, z, NULL); }
+static double weno5_minus_w(const double g[5], int z, double *w) {
   /* g[0..4] = f at points i-1..i+3 (f1..f5 in the six-point numbering) */
   const double f1 = g[0], f2 = g[1], f3 = g[2], f4 = g[3], f5 = g[4];
   const double b0 = 0.5 * f3 * ((5.0 / 3.0) * f3 - (31.0 / 6.0) * f4 + (11.0 / 6.0) * f5) +
@@ -351,10 +356,13 @@ static double weno5_minus(const double g[5], int z) {
     a2 = (3.0 / 10.0) / ((b2 + 1e-6) * (b2 + 1e-6));
   }
   const double inv = 1.0 / (a0 + a1 + a2);
+  if (w) { w[0] = a0 * inv; w[1] = a1 * inv; w[2] = a2 * inv; }
   return a0 * inv * ((11.0 / 12.0) * f3 - (7.0 / 12.0) * f4 + (1.0 / 6.0) * f5) +
          a1 * inv * ((1.0 / 6.0) * f2 + (5.0 / 12.0) * f3 - (1.0 / 12.0) * f4) +
          a2 * inv * (-(1.0 / 12.0) * f1 + (5.0 / 12.0) * f2 + (1.0 / 6.0) * f3);
 }
+
+static double weno5_minus(const double g[5], int z) { return weno5_minus_w(g, z, NULL); }
 
 /* TENO5 (schemes/spatial/teno.py:57-213, 407-465) with fixed cut-off C_T on one side of the split
  * flux, f[0..4] ordered from the far upwind point to the far downwind one: smoothness indicators of
@@ -557,6 +565,107 @@ static void residual_weno(st_t *s) {
 }
 
 /* ---------------------------------------------------------------------------------------------
+ * WENO5 non-linear filter (filters/WENO_filter.py:15-339), applied after every full RK3 step with
+ * dissipation_sensor='Constant' (kappa = 1):
+ *   constituent relations of the filter (WENO_filter.py:134-168): inv_rho = 1/rho, u = rhou inv_rho,
+ *     p = (g-1)(rhoE - 0.5 |rhou|^2 inv_rho), a = sqrt(g p inv_rho), over the padded range;
+ *   per direction d, at interface i+1/2: the simple average of rho, u, a over points i, i+1
+ *     (SimpleAverage([0, 1]), schemes/spatial/averaging.py), the Euler eigensystem of that state,
+ *     CF = LEV.F with F = (rho u_d, rhou_c u_d + delta_cd p, (p + rhoE) u_d), CS = LEV.Q at i-2..i+3,
+ *     lambda as for the LLF flux, WENO5-JS on f = CF +- lambda CS (weno.py:341-369), the weight
+ *     sensor of each side r = sum_r |omega_r / d_r - 1|^4 / (9^4 + 2) (weno.py:436-452), rj = max of
+ *     the two sides, Recon = rj (Recon - (CF_0 - 8 CF_1 + 37 CF_2 + 37 CF_3 - 8 CF_4 + CF_5)/60)
+ *     (shock_capturing.py:399-412, 440-442), flux = REV.Recon;
+ *   q += dt * shock_filter_control * Wall * kappa * (-sum_d (flux_d[i] - flux_d[i-1]) / delta_d)
+ *     (WENO_filter.py:258-282), Wall = 1 away from wall faces (periodic blocks: everywhere).
+ * ------------------------------------------------------------------------------------------- */
+static double filter_side_sensor(const double w[3], const double inv_d[3]) {
+  double num = 0.0;
+  for (int r = 0; r < 3; ++r) num += pow(fabs(inv_d[r] * w[r] - 1.0), 4.0);
+  return num / (pow(9.0, 4.0) + 2.0);
+}
+
+static void weno_filter(st_t *s) {
+  const double g = s->c.gama;
+  int n[3] = {N0, N1, N2};
+  for (size_t m = 0; m < s->np; ++m) {
+    const double rho = s->q[0][m];
+    if (rho == 0.0) continue;
+    const double ir = 1.0 / rho;
+    for (int d = 0; d < 3; ++d) s->u[d][m] = s->q[1 + d][m] * ir;
+    const double p = (g - 1) * (s->q[4][m] - 0.5 * (s->q[1][m] * s->q[1][m] + s->q[2][m] * s->q[2][m] +
+                                                     s->q[3][m] * s->q[3][m]) * ir);
+    s->p[m] = p;
+    s->a[m] = sqrt(g * p * ir);
+  }
+  for (int v = 0; v < 5; ++v) FOR3(0, N0, 0, N1, 0, N2) s->res[v][IX(s, i, j, k)] = 0.0;
+  static const double inv_dp[3] = {10.0 / 3.0, 5.0 / 3.0, 10.0}, inv_dm[3] = {10.0, 5.0 / 3.0, 10.0 / 3.0};
+  for (int dir = 0; dir < 3; ++dir) {
+    const size_t o = stride(s, dir);
+    int lo[3] = {0, 0, 0}, hi[3] = {n[0], n[1], n[2]};
+    lo[dir] = -1;
+    FOR3(lo[0], hi[0], lo[1], hi[1], lo[2], hi[2]) {
+      const size_t c = IX(s, i, j, k);
+      const double ar = 0.5 * (s->q[0][c + o] + s->q[0][c]);
+      const double aa = 0.5 * (s->a[c] + s->a[c + o]);
+      double au[3];
+      for (int d = 0; d < 3; ++d) au[d] = 0.5 * (s->u[d][c + o] + s->u[d][c]);
+      double L[5][5], R[5][5];
+      eigensystem(dir, ar, au[0], au[1], au[2], aa, g, L, R);
+      double CF[5][6], CS[5][6];
+      double lam[5] = {0, 0, 0, 0, 0};
+      for (int t = 0; t < 6; ++t) {
+        const size_t m = c + (size_t)((long)(t - 2) * (long)o);
+        const double un = s->u[dir][m];
+        double F[5], Q[5];
+        for (int v = 0; v < 5; ++v) Q[v] = s->q[v][m];
+        F[0] = s->q[0][m] * un;
+        for (int d = 0; d < 3; ++d) F[1 + d] = s->q[1 + d][m] * un + (d == dir ? s->p[m] : 0.0);
+        F[4] = (s->p[m] + s->q[4][m]) * un;
+        for (int r = 0; r < 5; ++r) {
+          double cf = 0, cs = 0;
+          for (int v = 0; v < 5; ++v) {
+            cf += L[r][v] * F[v];
+            cs += L[r][v] * Q[v];
+          }
+          CF[r][t] = cf;
+          CS[r][t] = cs;
+        }
+        const double ev[5] = {fabs(un), fabs(un), fabs(un), fabs(un + s->a[m]), fabs(un - s->a[m])};
+        for (int r = 0; r < 5; ++r) lam[r] = fmax(lam[r], ev[r]);
+      }
+      double rec[5];
+      for (int r = 0; r < 5; ++r) {
+        double fp[5], fm[5], wp[3], wm[3];
+        for (int t = 0; t < 5; ++t) {
+          fp[t] = CF[r][t] + lam[r] * CS[r][t];
+          fm[t] = CF[r][t + 1] - lam[r] * CS[r][t + 1];
+        }
+        const double recon = weno5_plus_w(fp, 0, wp) + weno5_minus_w(fm, 0, wm);
+        const double rj = fmax(filter_side_sensor(wp, inv_dp), filter_side_sensor(wm, inv_dm));
+        const double central = (1.0 / 60.0) * (CF[r][0] - 8.0 * CF[r][1] + 37.0 * CF[r][2] + 37.0 * CF[r][3] -
+                                               8.0 * CF[r][4] + CF[r][5]);
+        rec[r] = rj * (recon - central);
+      }
+      for (int v = 0; v < 5; ++v) {
+        double fl = 0;
+        for (int r = 0; r < 5; ++r) fl += R[v][r] * rec[r];
+        s->flux[v][c] = fl;
+      }
+    }
+    FOR3(0, N0, 0, N1, 0, N2) {
+      const size_t c = IX(s, i, j, k);
+      for (int v = 0; v < 5; ++v) s->res[v][c] -= (s->flux[v][c] - s->flux[v][c - o]) / s->c.delta[dir];
+    }
+  }
+  const double scale = s->c.dt * s->c.filter_control;
+  for (int v = 0; v < 5; ++v) FOR3(0, N0, 0, N1, 0, N2) {
+      const size_t c = IX(s, i, j, k);
+      s->q[v][c] += scale * s->res[v][c];
+    }
+}
+
+/* ---------------------------------------------------------------------------------------------
  * Time advance: 2-register RK3 (schemes/temporal/rk_sbli.py:51-61, 117-133):
  *   save: qold = q
  *   stage s: q = qold + dt*rknew[s]*R ; qold = qold + dt*rkold[s]*R
@@ -643,6 +752,7 @@ int osbo_run(const osbo_cfg *cfg, double *q, int nsteps, double *ke) {
         }
       apply_bcs(&s);
     }
+    if (s.c.filter == OSBO_FILTER_WENO5_CONSTANT) weno_filter(&s);
     if (ke) ke[it + 1] = kinetic_energy(&s);
   }
   store_interior(&s, q, s.q);

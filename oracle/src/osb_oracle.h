@@ -18,6 +18,8 @@ enum { OSBO_CONV_CENTRAL_SKEW = 0, OSBO_CONV_WENO5JS = 1, OSBO_CONV_TENO5 = 2, O
 enum { OSBO_VISC_NONE = 0, OSBO_VISC_CONST = 1, OSBO_VISC_SUTHERLAND = 2 };
 enum { OSBO_RK3_2REG = 0, OSBO_RK3_LS_SSP = 1 };
 enum { OSBO_BC_PERIODIC = 0, OSBO_BC_SYMMETRY = 1 };
+/* the WENO5 non-linear filter after each full step (filters/WENO_filter.py), 3D periodic blocks */
+enum { OSBO_FILTER_NONE = 0, OSBO_FILTER_WENO5_CONSTANT = 1 };
 
 typedef struct {
   int ndim;        /* 2 or 3 */
@@ -28,6 +30,8 @@ typedef struct {
   int bc[3][2];    /* per axis, per side */
   double teno_ct, teno_eps;
   double dt;
+  int filter;             /* OSBO_FILTER_* */
+  double filter_control;  /* shock_filter_control (1 in the reference) */
 } osbo_cfg;
 
 /* Taylor-Green initial condition (apps/taylor_green_vortex/taylor_green_vortex.py:87-101) on the

@@ -32,7 +32,8 @@ def golden_plan(case, n=None, **kw):
 def oracle_cfg(plan, dt=None):
     bc = [[plan.bc[d][s] for s in range(2)] for d in range(3)]
     return O.make_cfg(plan.n, plan.delta, gama=plan.gama, Minf=plan.Minf, Re=plan.Re, Pr=plan.Pr, conv=plan.conv,
-                      visc=plan.visc, rk="rk3", bc=bc, dt=dt if dt is not None else (plan.dt or 1e-3))
+                      visc=plan.visc, rk="rk3", bc=bc, dt=dt if dt is not None else (plan.dt or 1e-3),
+                      filter=plan.filter, filter_control=plan.filter_control)
 
 
 def rel_err(a, b):

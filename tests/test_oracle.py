@@ -13,7 +13,7 @@ from oracle import oracle as O
 from oracle import refrun
 from helpers import load_golden, golden_plan, oracle_cfg, rel_err, rel_err_mom, WENOZ_TOL
 
-CASES = ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central"]
+CASES = ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central", "tgv_filter"]
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -54,6 +54,7 @@ def test_oracle_periodic_mass_conservation():
     ("tgv_wenoz", 12, 4, {"dt": 3e-3, "Minf": 1.25}),
     ("tgv_teno", 12, 4, {"dt": 3e-3, "Minf": 1.25}),
     ("tgv_teno6", 12, 4, {"dt": 3e-3, "Minf": 1.25}),
+    ("tgv_filter", 12, 6, {"dt": 3e-3, "Minf": 1.25}),
 ])
 def test_oracle_matches_reference_run(case, n, steps, extra):
     if not refrun.available(case):
@@ -137,3 +138,12 @@ def test_ls_rk3_coefficients_match_the_lowered_plan():
     A, B = ls_rk3_ssp_coefficients()
     p = golden_plan_2d()
     assert np.allclose(A, p.rk_a, rtol=0, atol=1e-15) and np.allclose(B, p.rk_b, rtol=1e-15)
+
+
+def test_oracle_filter_changes_the_state():
+    """The WENO filter case differs from the same scheme without the filter by far more than the
+    parity tolerance, so the golden comparison above pins the filter itself."""
+    q_ref, n, steps, params = load_golden("tgv_filter")
+    plan = golden_plan("tgv_filter", n=n).replace(Minf=params["Minf"])
+    q_nf = O.run(oracle_cfg(plan.replace(filter="none"), dt=params["dt"]), O.tgv_init(oracle_cfg(plan)), steps)
+    assert max(rel_err(q_nf, q_ref)) > 1e-6

@@ -71,15 +71,19 @@ def test_published_katzer_script_lowers_to_adaptive_teno():
 
 
 def test_writer_refuses_kernels_outside_the_lowered_families():
-    """A WENO filter (filters/WENO_filter.py) or any other extra equation class adds kernels to the time
-    loop; lowering without them would change the solution, so the writer refuses."""
+    """Extra equation classes add kernels to the time loop; lowering without them would change the
+    solution, so the writer refuses every kernel it does not lower.  The WENO filter with the constant
+    dissipation sensor is lowered; its Ducros variant adds a shock-sensor kernel and is refused."""
     from opensbli_gb300.writer import GB300Writer
-    for case in ("tgv_central", "tgv_weno", "tgsym_central", "katzer_teno", "katzer_adaptive", "katzer_carpenter"):
+    for case in ("tgv_central", "tgv_weno", "tgsym_central", "katzer_teno", "katzer_adaptive", "katzer_carpenter",
+                 "tgv_filter"):
         GB300Writer._check_kernel_families(golden_plan(case).kernels)
-    names = golden_plan("tgv_central").kernels + ["Constituent Relations evaluation", "Shock sensor",
-                                                  "WENO reconstruction direction 0", "Non-linear filter application"]
-    with pytest.raises(NotImplementedError, match="Non-linear filter application"):
+    assert "User kernel: Non-linear filter application" in golden_plan("tgv_filter").kernels
+    names = golden_plan("tgv_filter").kernels + ["User kernel: Shock sensor"]
+    with pytest.raises(NotImplementedError, match="Shock sensor"):
         GB300Writer._check_kernel_families(names)
+    with pytest.raises(NotImplementedError, match="User defined thing"):
+        GB300Writer._check_kernel_families(golden_plan("tgv_central").kernels + ["User defined thing"])
 
 
 def test_carpenter_faces_lower_to_their_closure():
@@ -98,7 +102,7 @@ def test_cfl_dt_tgv_weno():
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
 @pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central",
-                                  "katzer_teno", "katzer_adaptive", "katzer_carpenter"])
+                                  "katzer_teno", "katzer_adaptive", "katzer_carpenter", "tgv_filter"])
 def test_writer_lowers_reference_script(case, tmp_path):
     r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case, "--out",
                         str(tmp_path), "--ref", REF], capture_output=True, text=True, timeout=900)
