@@ -23,6 +23,7 @@ import re
 
 import numpy as np
 
+from . import physics_check
 from .plan import Plan
 
 _C_NAMES = {"M_PI": math.pi, "pi": math.pi}
@@ -186,6 +187,8 @@ class GB300Writer:
         if other_bc or any(b is None for pair in bcs for b in pair):
             raise NotImplementedError("unsupported boundary conditions: %s" % (other_bc or bcs))
         filt, fc = self._weno_filter()
+        # the equations behind the recognised kernels must be the physics the fused kernels implement
+        physics_check.check_algorithm(self.components, 3, viscous=bool(visc), skew=conv == "central_skew")
         return Plan(ndim=3, conv=conv, visc="const" if visc else "none", rk="rk3", precision=precision,
                     bc=tuple(tuple(p) for p in bcs), rk_a=coeff["rkold"], rk_b=coeff["rknew"],
                     weno_eps=1e-14 if conv == "weno5z" else 1e-6,  # WenoZ.eps / WenoJS.eps (weno.py)
@@ -326,6 +329,7 @@ class GB300Writer:
         order = ["rho", "rhou0", "rhou1", "rhoE"]
         if any(v not in lo for v in order):
             raise NotImplementedError("Dirichlet face must set rho, rhou0, rhou1, rhoE")
+        physics_check.check_algorithm(self.components, 2, viscous=True, sutherland=True, metric=True)
         return Plan(ndim=2, n=(64, 32, 1), delta=(1.0, 1.0, 1.0), conv="teno5" if teno else "weno5js",
                     visc="sutherland", rk="ls_rk3", precision=precision,
                     bc=(tuple(bcs[0]), tuple(bcs[1]), ("periodic", "periodic")),

@@ -126,3 +126,45 @@ def test_writer_lowers_reference_script(case, tmp_path):
     else:
         assert ic.shape == (5,) + tuple(reversed(p.n))
     assert np.isfinite(ic).all()
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
+@pytest.mark.parametrize("variant,what", [("bulk", "Viscous residual"), ("heat", "Viscous residual")])
+def test_writer_refuses_other_physics_with_the_same_kernel_names(variant, what, tmp_path):
+    """A script whose stress tensor carries a bulk-viscosity term, or whose heat-flux coefficient
+    differs, generates the same kernel names as the Taylor-Green WENO case; the writer evaluates the
+    equations behind them and refuses (opensbli_gb300/physics_check.py)."""
+    env = dict(os.environ, OSB_PHYSICS_VARIANT=variant)
+    r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case",
+                        "tgv_weno_modified", "--out", str(tmp_path), "--ref", REF], capture_output=True, text=True,
+                       timeout=900, env=env)
+    assert r.returncode != 0
+    assert "NotImplementedError" in r.stderr and what in r.stderr, r.stderr[-2000:]
+
+
+def test_physics_check_catches_a_changed_constituent_relation():
+    """Unit check of the constituent-relation comparison on a hand-made kernel list."""
+    import sympy
+    from opensbli_gb300 import physics_check as P
+
+    class DS(sympy.Symbol):  # stands in for the reference's DataSet (class name is what is checked)
+        pass
+    DS.__name__ = "DataSet"
+
+    class K:  # stands in for the reference's Kernel
+        def __init__(self, name, eqs):
+            self.computation_name, self.equations = name, eqs
+    K.__name__ = "Kernel"
+
+    def ds(name):
+        d = DS(name + "_B0")
+        d.base, d.indices = name + "_B0", (0, 0, 0)
+        return d
+    rho, m0, m1, m2, E = (ds(n) for n in ("rho", "rhou0", "rhou1", "rhou2", "rhoE"))
+    g = 1.4
+    good = [K("CRu%d" % c, [sympy.Eq(ds("u%d" % c), m / rho)]) for c, m in enumerate((m0, m1, m2))]
+    p_ok = K("CRp", [sympy.Eq(ds("p"), (g - 1) * (E - (m0 ** 2 + m1 ** 2 + m2 ** 2) / (2 * rho)))])
+    p_bad = K("CRp", [sympy.Eq(ds("p"), (g - 1) * (E - (m0 ** 2 + m1 ** 2) / (2 * rho)))])
+    P.PhysicsCheck(good + [p_ok], 3, viscous=False).check_constituent_relations()
+    with pytest.raises(NotImplementedError, match="constituent relation for p"):
+        P.PhysicsCheck(good + [p_bad], 3, viscous=False).check_constituent_relations()
