@@ -36,7 +36,11 @@ ALG_BYTES_STAGE = {"mixed": 5 * (2 * 4 + 2 * 8), "fp64": 5 * (2 * 8 + 2 * 8)}
 
 # DRAM bytes per cell per launch measured by ncu for the mixed WENO TGV kernels at 192^3 (state larger
 # than L2), used to scale the roofline's traffic figure to the benchmark's grid
-DRAM_BYTES_PER_CELL_WENO_MIXED = {"weno_x": 45.7, "weno_y": 57.9, "weno_z": 57.8, "central_rk": 147.3}
+DRAM_BYTES_PER_CELL_WENO_MIXED = {"weno_x": 46.0, "weno_y": 57.2, "weno_z": 57.4, "central_rk": 147.3}
+# thread-instructions per cell (one interface per cell and direction) executed by the same kernels in
+# the same capture (smsp__inst_executed x 32 / cells): the work that the FP32 issue rate bounds
+THREAD_INST_PER_CELL_WENO_MIXED = {"weno_x": 1302.0, "weno_y": 1171.0, "weno_z": 1163.0}
+SM_COUNT, SCHEDULERS_PER_SM, WARP = 152, 4, 32
 
 
 def load_peaks():
@@ -389,7 +393,19 @@ def own_arm(args, world, rank, local):
             traffic = DRAM_BYTES_PER_CELL_WENO_MIXED[dom] * cells / 1e9
             tsrc = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of the same kernel at 192^3, per cell, "
                     "times this launch's cells")
+        issue = None
+        if wl.name == "tgv_weno256" and head == "mixed" and dom in THREAD_INST_PER_CELL_WENO_MIXED:
+            # the instruction-issue roofline of the same kernel: one warp-instruction per scheduler per
+            # clock at the median SM clock sampled during the timed region
+            mhz = clk.summary().get("sm_mhz") or 2070.0
+            inst = THREAD_INST_PER_CELL_WENO_MIXED[dom] * cells
+            ach_i = inst / per_launch / 1e12
+            peak_i = SM_COUNT * SCHEDULERS_PER_SM * WARP * mhz * 1e6 / 1e12
+            issue = {"achieved": ach_i, "peak": peak_i, "unit": "T thread-instructions/s", "frac": ach_i / peak_i,
+                     "thread_inst_per_cell": THREAD_INST_PER_CELL_WENO_MIXED[dom], "sm_mhz": mhz,
+                     "source": "ncu smsp__inst_executed of the same kernel at 192^3, per cell"}
         roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "issue": issue,
                 "peak_kind": peak_kind, "traffic": traffic, "traffic_unit": "GB per launch",
                 "traffic_source": tsrc, "alg_bytes_per_cell": fam_bytes[dom],
                 "avg_launch_ms": per_launch * 1e3,
