@@ -352,10 +352,48 @@ template <typename T> __device__ __forceinline__ T t5_side(T f0, T f1, T f2, T f
 }
 
 enum { S2_RHO = 0, S2_RU0, S2_RU1, S2_E, S2_P, S2_A, S2_UD, S2_NF };
+// FP32 tiles also stage each point's double-float flux (hi, lo of 4 components)
+enum { S2_FH = S2_NF, S2_FL = S2_NF + 4 };
+template <typename T> __host__ __device__ constexpr int s2nf() { return sizeof(T) == 4 ? S2_NF + 8 : S2_NF; }
 
 template <typename T> struct W2 {
   T Q[4], ud, a, p;
 };
+
+// FP32 flux of one point along D, (Q_{1+D}, Q_{1+c} u_D + delta_cD p, (Q_3 + p) u_D), as a double-float
+// sum h + l: u_D and p come with their remainders (the division residual of u_D is exact, prims_f32
+// gives p_lo), products split by FMA, sums by two-sum.  The characteristic projections below act on
+// differences of these fluxes between nearby points, which FP32 rounding of the O(1) flux itself
+// would swamp.
+template <int D>
+__device__ __forceinline__ void point_flux2_ff(float rho, float m0, float m1, float E, float gm1, float gm1_lo,
+                                               float h[4], float l[4]) {
+  float ir, u[3], p, p_lo;
+  prims_f32(rho, m0, m1, 0.0f, E, gm1, gm1_lo, ir, u, p, p_lo);
+  const float m[2] = {m0, m1};
+  const float ud = u[D], ud_lo = fmaf(-ud, rho, m[D]) * ir;
+  h[0] = m[D];
+  l[0] = 0.0f;
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    const float ph = __fmul_rn(m[c], ud);
+    const float pl = fmaf(m[c], ud, -ph) + m[c] * ud_lo;
+    if (c == D) {
+      const float sh = __fadd_rn(ph, p), bv = __fsub_rn(sh, ph);
+      const float es = __fadd_rn(__fsub_rn(ph, __fsub_rn(sh, bv)), __fsub_rn(p, bv));
+      h[1 + c] = sh;
+      l[1 + c] = es + pl + p_lo;
+    } else {
+      h[1 + c] = ph;
+      l[1 + c] = pl;
+    }
+  }
+  const float sh = __fadd_rn(E, p), bv = __fsub_rn(sh, E);
+  const float es = __fadd_rn(__fsub_rn(E, __fsub_rn(sh, bv)), __fsub_rn(p, bv));
+  const float hh = __fmul_rn(sh, ud);
+  h[3] = hh;
+  l[3] = fmaf(sh, ud, -hh) + fmaf(es + p_lo, ud, sh * ud_lo);
+}
 
 // Characteristic flux between window points 2 and 3 along D (2D Euler eigensystem for a unit
 // normal, physical_models/euler_eigensystem.py:77-105; the block's metric is diagonal so the
@@ -445,6 +483,97 @@ __device__ __forceinline__ void flux2(const W2<T> (&W)[6], T gama, T eps, T ct, 
   out[3] -= s * rho * u[E] * r1;
 }
 
+// FP32: the same characteristic flux in difference form about window point 2 (point i): the
+// reconstructions reproduce constants (WENO and TENO candidates are consistent, the weights sum to
+// one) and the splitting is linear, so projecting Q_t - Q_i and F_t - F_i gives LEV.(F^ - F_i) and
+// REV maps it to G = F_{i+1/2} - F_i.  dF[t][v] = F_t - F_i from the double-float point fluxes.
+// Returns G; the caller differences (F_i - F_{i-1}) + (G_i - G_{i-1}).
+template <int D, bool TENO>
+__device__ __forceinline__ void flux2_delta(const W2<float> (&W)[6], const float (&dF)[6][4], float gama, float eps,
+                                            float ct, float out[4]) {
+  using T = float;
+  constexpr int E = 1 - D;
+  const T s = D == 0 ? T(1) : T(-1);
+  const T gm1 = gama - T(1);
+  const T rl = W[2].Q[0], rr = W[3].Q[0];
+  const T sl = sqrt_t(rl), sr = sqrt_t(rr);
+  const T rho = sqrt_t(rl * rr);
+  const T inv_s = T(1) / (sl + sr);
+  T u[2];
+#pragma unroll
+  for (int c = 0; c < 2; ++c) u[c] = inv_s * (sl * (W[2].Q[1 + c] / rl) + sr * (W[3].Q[1 + c] / rr));
+  const T Hh = inv_s * ((W[2].p + W[2].Q[3]) / sl + (W[3].p + W[3].Q[3]) / sr);
+  const T usq = u[0] * u[0] + u[1] * u[1];
+  const T a = sqrt_t(gm1 * (Hh - T(0.5) * usq));
+  const T ia = T(1) / a, irho = T(1) / rho;
+  const T phi = gm1 * T(0.5) * usq;
+  const T bt = T(0.70710678118654752440) * irho * ia, al = T(0.70710678118654752440) * rho * ia;
+  const T ia2 = ia * ia, btA = bt * a;
+  T lu = T(0), lp = T(0), lm = T(0);
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    lu = max_t(lu, abs_t(W[t].ud));
+    lp = max_t(lp, abs_t(W[t].ud + W[t].a));
+    lm = max_t(lm, abs_t(W[t].a - W[t].ud));
+  }
+  auto recon = [&](const T (&cf)[6], const T (&cs)[6], T lam) -> T {
+    T fp[6], fm[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      fp[t] = cf[t] + lam * cs[t];
+      fm[t] = cf[t] - lam * cs[t];
+    }
+    if (TENO)
+      return t5_side(fp[0], fp[1], fp[2], fp[3], fp[4], eps, ct) + t5_side(fm[5], fm[4], fm[3], fm[2], fm[1], eps, ct);
+    return w5_side(fp[0], fp[1], fp[2], fp[3], fp[4], eps) + w5_side(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
+  };
+  auto dQ = [&](int t, int v) -> T { return t == 2 ? T(0) : W[t].Q[v] - W[2].Q[v]; };
+  T r0, r1, r2, r3;
+  {
+    T cf[6], cs[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {  // shear row: (s/rho)(u_E X0 - X_{1+E})
+      cf[t] = s * irho * (u[E] * dF[t][0] - dF[t][1 + E]);
+      cs[t] = s * irho * (u[E] * dQ(t, 0) - dQ(t, 1 + E));
+    }
+    r1 = recon(cf, cs, lu);
+    T gQ[6], gF[6], hQ[6], hF[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      gQ[t] = phi * dQ(t, 0) - gm1 * (u[0] * dQ(t, 1) + u[1] * dQ(t, 2)) + gm1 * dQ(t, 3);
+      hQ[t] = dQ(t, 1 + D) - u[D] * dQ(t, 0);
+      gF[t] = phi * dF[t][0] - gm1 * (u[0] * dF[t][1] + u[1] * dF[t][2]) + gm1 * dF[t][3];
+      hF[t] = dF[t][1 + D] - u[D] * dF[t][0];
+    }
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = dF[t][0] - gF[t] * ia2;
+      cs[t] = dQ(t, 0) - gQ[t] * ia2;
+    }
+    r0 = recon(cf, cs, lu);
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = bt * gF[t] + btA * hF[t];
+      cs[t] = bt * gQ[t] + btA * hQ[t];
+    }
+    r2 = recon(cf, cs, lp);
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      cf[t] = bt * gF[t] - btA * hF[t];
+      cs[t] = bt * gQ[t] - btA * hQ[t];
+    }
+    r3 = recon(cf, cs, lm);
+  }
+  const T sac = r2 + r3, dac = r2 - r3;
+  const T hh = (phi + a * a) / gm1;
+  out[0] = r0 + al * sac;
+#pragma unroll
+  for (int c = 0; c < 2; ++c) out[1 + c] = u[c] * r0 + al * (u[c] * sac + (c == D ? a * dac : T(0)));
+  out[3] = (phi / gm1) * r0 + al * (hh * sac + u[D] * a * dac);
+  out[1 + E] -= s * rho * r1;
+  out[3] -= s * rho * u[E] * r1;
+}
+
 template <int D> struct T2Tile;
 template <> struct T2Tile<0> { static constexpr int TI = 64, TA = 4; };
 template <> struct T2Tile<1> { static constexpr int TI = 24, TA = 16; };  // static smem < 48 KB in FP64
@@ -458,8 +587,10 @@ __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<con
                                                const T *ctp) {
   using Tl = T2Tile<D>;
   constexpr int TI = Tl::TI, TA = Tl::TA, NPT = TI + 5;
-  __shared__ T sf[S2_NF][NPT][TA];
+  constexpr int NF = s2nf<T>();
+  __shared__ T sf[NF][NPT][TA];
   __shared__ T sfl[4][TI][TA];
+  __shared__ T sdf[sizeof(T) == 4 ? 4 : 1][TI][TA];  // FP32: F(left point) - F(the point before)
   const int tid = threadIdx.x;
   const int nd = D == 0 ? g.n0 : g.n1, na = D == 0 ? g.n1 : g.n0;
   const int d0 = (D == 0 ? blockIdx.x : blockIdx.y) * (TI - 1);
@@ -484,6 +615,16 @@ __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<con
     sf[S2_P][pos][a] = pr.p[m];
     sf[S2_A][pos][a] = pr.a[m];
     sf[S2_UD][pos][a] = D == 0 ? pr.u0[m] : pr.u1[m];
+    if constexpr (sizeof(T) == 4) {
+      const float gm1 = (float)(gama_d - 1.0), gm1_lo = (float)((gama_d - 1.0) - (double)gm1);
+      float h[4], l[4];
+      point_flux2_ff<D>(q.v[0][m], q.v[1][m], q.v[2][m], q.v[3][m], gm1, gm1_lo, h, l);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        sf[S2_FH + v][pos][a] = h[v];
+        sf[S2_FL + v][pos][a] = l[v];
+      }
+    }
   }
   __syncthreads();
   const T gama = T(gama_d), eps = T(eps_d), ct = T(ct_d);
@@ -510,7 +651,22 @@ __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<con
       ctl = ctp[g2(g, i, j)];
     }
     T fl[4];
-    flux2<T, D, TENO>(W, gama, eps, ctl, fl);
+    if constexpr (sizeof(T) == 4) {
+      // F_t - F_i of the window from the staged double-float fluxes, each rounded once
+      float dF[6][4];
+#pragma unroll
+      for (int k = 0; k < 6; ++k)
+#pragma unroll
+        for (int v = 0; v < 4; ++v)
+          dF[k][v] = k == 2 ? 0.0f
+                            : __fsub_rn(sf[S2_FH + v][m + k][a], sf[S2_FH + v][m + 2][a]) +
+                                  __fsub_rn(sf[S2_FL + v][m + k][a], sf[S2_FL + v][m + 2][a]);
+      flux2_delta<D, TENO>(W, dF, gama, eps, ctl, fl);
+#pragma unroll
+      for (int v = 0; v < 4; ++v) sdf[v][m][a] = -dF[1][v];  // F(point i) - F(point i-1)
+    } else {
+      flux2<T, D, TENO>(W, gama, eps, ctl, fl);
+    }
 #pragma unroll
     for (int v = 0; v < 4; ++v) sfl[v][m][a] = fl[v];
   }
@@ -530,7 +686,9 @@ __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<con
     const T sc_hi = T(sc), sc_lo = T(sc - (double)sc_hi);
 #pragma unroll
     for (int v = 0; v < 4; ++v) {
-      const T d = -mul_hl(sfl[v][m + 1][a] - sfl[v][m][a], sc_hi, sc_lo);
+      T diff = sfl[v][m + 1][a] - sfl[v][m][a];
+      if constexpr (sizeof(T) == 4) diff = sdf[v][m + 1][a] + diff;  // (F_i - F_{i-1}) + (G_i - G_{i-1})
+      const T d = -mul_hl(diff, sc_hi, sc_lo);
       if (D == 0) res.v[v][gi] = d;
       else res.v[v][gi] += d;
     }
