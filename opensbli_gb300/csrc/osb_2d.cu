@@ -21,6 +21,7 @@
 #include "osb_common.cuh"
 #include "osb_cvt.cuh"
 #include "osb_internal.h"
+#include "osb_weno.cuh"  // the WENO5-Z and TENO6 sides (weno5_side, teno6_side) and the SCH_* scheme codes
 
 namespace osb {
 
@@ -395,10 +396,27 @@ __device__ __forceinline__ void point_flux2_ff(float rho, float m0, float m1, fl
   l[3] = fmaf(sh, ud, -hh) + fmaf(es + p_lo, ud, sh * ud_lo);
 }
 
+// Both sides of one characteristic reconstruction (fp: CF + lambda CS, fm: CF - lambda CS at the six
+// window points): TENO5 (t5_side), WENO5-JS (w5_side), WENO5-Z (weno5_side, weno.py:283-331) or TENO6
+// (teno6_side, teno.py:94-192, 216-234, six points per side).
+template <typename T, int SCH>
+__device__ __forceinline__ T recon2(const T (&fp)[6], const T (&fm)[6], T eps, T ct) {
+  if constexpr (SCH == SCH_TENO)
+    return t5_side(fp[0], fp[1], fp[2], fp[3], fp[4], eps, ct) + t5_side(fm[5], fm[4], fm[3], fm[2], fm[1], eps, ct);
+  else if constexpr (SCH == SCH_TENO6)
+    return teno6_side<T>(fp[0], fp[1], fp[2], fp[3], fp[4], fp[5], true, eps, ct) +
+           teno6_side<T>(fm[5], fm[4], fm[3], fm[2], fm[1], fm[0], false, eps, ct);
+  else if constexpr (SCH == SCH_Z)
+    return weno5_side<T, SCH_Z>(fp[0], fp[1], fp[2], fp[3], fp[4], eps) +
+           weno5_side<T, SCH_Z>(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
+  else
+    return w5_side(fp[0], fp[1], fp[2], fp[3], fp[4], eps) + w5_side(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
+}
+
 // Characteristic flux between window points 2 and 3 along D (2D Euler eigensystem for a unit
 // normal, physical_models/euler_eigensystem.py:77-105; the block's metric is diagonal so the
 // eigensystem is Cartesian).  Dense rows share g = phi X0 - (g-1) u.X + (g-1) X3, h = X_{1+D} - u_D X0.
-template <typename T, int D, bool TENO>
+template <typename T, int D, int SCH>
 __device__ __forceinline__ void flux2(const W2<T> (&W)[6], T gama, T eps, T ct, T out[4]) {
   constexpr int E = 1 - D;
   const T s = D == 0 ? T(1) : T(-1);
@@ -431,9 +449,7 @@ __device__ __forceinline__ void flux2(const W2<T> (&W)[6], T gama, T eps, T ct, 
       fp[t] = cf[t] + lam * cs[t];
       fm[t] = cf[t] - lam * cs[t];
     }
-    if (TENO)
-      return t5_side(fp[0], fp[1], fp[2], fp[3], fp[4], eps, ct) + t5_side(fm[5], fm[4], fm[3], fm[2], fm[1], eps, ct);
-    return w5_side(fp[0], fp[1], fp[2], fp[3], fp[4], eps) + w5_side(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
+    return recon2<T, SCH>(fp, fm, eps, ct);
   };
   T r0, r1, r2, r3;
   {
@@ -488,7 +504,7 @@ __device__ __forceinline__ void flux2(const W2<T> (&W)[6], T gama, T eps, T ct, 
 // one) and the splitting is linear, so projecting Q_t - Q_i and F_t - F_i gives LEV.(F^ - F_i) and
 // REV maps it to G = F_{i+1/2} - F_i.  dF[t][v] = F_t - F_i from the double-float point fluxes.
 // Returns G; the caller differences (F_i - F_{i-1}) + (G_i - G_{i-1}).
-template <int D, bool TENO>
+template <int D, int SCH>
 __device__ __forceinline__ void flux2_delta(const W2<float> (&W)[6], const float (&dF)[6][4], float gama, float eps,
                                             float ct, float out[4]) {
   using T = float;
@@ -523,9 +539,7 @@ __device__ __forceinline__ void flux2_delta(const W2<float> (&W)[6], const float
       fp[t] = cf[t] + lam * cs[t];
       fm[t] = cf[t] - lam * cs[t];
     }
-    if (TENO)
-      return t5_side(fp[0], fp[1], fp[2], fp[3], fp[4], eps, ct) + t5_side(fm[5], fm[4], fm[3], fm[2], fm[1], eps, ct);
-    return w5_side(fp[0], fp[1], fp[2], fp[3], fp[4], eps) + w5_side(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
+    return recon2<T, SCH>(fp, fm, eps, ct);
   };
   auto dQ = [&](int t, int v) -> T { return t == 2 ? T(0) : W[t].Q[v] - W[2].Q[v]; };
   T r0, r1, r2, r3;
@@ -581,7 +595,7 @@ template <> struct T2Tile<1> { static constexpr int TI = 24, TA = 16; };  // sta
 // Interface fluxes along D for a tile and the flux difference -(F_i - F_{i-1})/delta (times D11 for
 // x1), written (D = 0) or accumulated (D = 1) into R.  TENO's cut-off is ct_d, or with ctp set the
 // per-point value at the interface's left point.
-template <typename T, int D, bool TENO>
+template <typename T, int D, int SCH>
 __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<const T> pr, const double *D11,
                                                Q4T<T> res, double gama_d, double eps_d, double ct_d, double inv_dd,
                                                const T *ctp) {
@@ -645,7 +659,7 @@ __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<con
       W[k].ud = sf[S2_UD][m + k][a];
     }
     T ctl = ct;
-    if (TENO && ctp) {
+    if (SCH == SCH_TENO && ctp) {
       int i, j;
       coord(d0 - 1 + m, a, i, j);
       ctl = ctp[g2(g, i, j)];
@@ -661,11 +675,11 @@ __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<con
           dF[k][v] = k == 2 ? 0.0f
                             : __fsub_rn(sf[S2_FH + v][m + k][a], sf[S2_FH + v][m + 2][a]) +
                                   __fsub_rn(sf[S2_FL + v][m + k][a], sf[S2_FL + v][m + 2][a]);
-      flux2_delta<D, TENO>(W, dF, gama, eps, ctl, fl);
+      flux2_delta<D, SCH>(W, dF, gama, eps, ctl, fl);
 #pragma unroll
       for (int v = 0; v < 4; ++v) sdf[v][m][a] = -dF[1][v];  // F(point i) - F(point i-1)
     } else {
-      flux2<T, D, TENO>(W, gama, eps, ctl, fl);
+      flux2<T, D, SCH>(W, gama, eps, ctl, fl);
     }
 #pragma unroll
     for (int v = 0; v < 4; ++v) sfl[v][m][a] = fl[v];
@@ -872,6 +886,21 @@ void launch2_to_state(const Ctx &c, cudaStream_t s, int64_t *launches) {
   ++*launches;
 }
 
+template <typename T, int D>
+static void launch2_flux(const Ctx &c, dim3 grid, Q4T<const T> q, Prims<const T> prc, Q4T<T> r, double eps,
+                         const T *ctp, cudaStream_t s) {
+  const osb_plan_desc &p = c.plan;
+  const double idd = 1.0 / p.delta[D];
+  if (p.conv == OSB_CONV_TENO5)
+    k2_flux<T, D, SCH_TENO><<<grid, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, idd, ctp);
+  else if (p.conv == OSB_CONV_TENO6)
+    k2_flux<T, D, SCH_TENO6><<<grid, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, idd, ctp);
+  else if (p.conv == OSB_CONV_WENO5Z)
+    k2_flux<T, D, SCH_Z><<<grid, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, idd, ctp);
+  else
+    k2_flux<T, D, SCH_JS><<<grid, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, idd, ctp);
+}
+
 template <typename T> void launch2_rhs(const Ctx &c, int update, double A, double B, double dt, cudaStream_t s,
                                        int64_t *launches) {
   const osb_plan_desc &p = c.plan;
@@ -887,7 +916,7 @@ template <typename T> void launch2_rhs(const Ctx &c, int update, double A, doubl
   dim3 b(32, 8), gp((c.g.n0 + 8 + 31) / 32, (c.g.n1 + 8 + 7) / 8);
   k2_prims<T><<<gp, b, 0, s>>>(c.g, q4(c.q64_2d), q4t<float>(c.qa), pr, p.gama, p.Minf, p.SuthT / p.RefT);
   Q4T<T> r = q4t<T>(c.res);
-  const bool teno = p.conv == OSB_CONV_TENO5;
+  const bool teno = p.conv == OSB_CONV_TENO5 || p.conv == OSB_CONV_TENO6;
   const double eps = teno ? p.teno_eps : p.weno_eps;
   const T *ctp = nullptr;
   if (teno && p.teno_adaptive) {
@@ -901,18 +930,12 @@ template <typename T> void launch2_rhs(const Ctx &c, int update, double A, doubl
   {
     using Tl = T2Tile<0>;
     dim3 gx((c.g.n0 + Tl::TI - 2) / (Tl::TI - 1), (c.g.n1 + Tl::TA - 1) / Tl::TA);
-    if (teno)
-      k2_flux<T, 0, true><<<gx, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, 1.0 / p.delta[0], ctp);
-    else
-      k2_flux<T, 0, false><<<gx, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, 1.0 / p.delta[0], ctp);
+    launch2_flux<T, 0>(c, gx, q, prc, r, eps, ctp, s);
   }
   {
     using Tl = T2Tile<1>;
     dim3 gy((c.g.n0 + Tl::TA - 1) / Tl::TA, (c.g.n1 + Tl::TI - 2) / (Tl::TI - 1));
-    if (teno)
-      k2_flux<T, 1, true><<<gy, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, 1.0 / p.delta[1], ctp);
-    else
-      k2_flux<T, 1, false><<<gy, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, 1.0 / p.delta[1], ctp);
+    launch2_flux<T, 1>(c, gy, q, prc, r, eps, ctp, s);
   }
   Visc2Args va;
   va.Re = p.Re;

@@ -51,7 +51,11 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
       snprintf(why, n, "2D blocks: boundary conditions must be inlet/extrapolation (x0) and isothermal wall/Dirichlet (x1)");
       return OSB_EUNSUPPORTED;
     }
-    if (p->conv != OSB_CONV_TENO5 && p->conv != OSB_CONV_WENO5JS) { snprintf(why, n, "2D blocks: TENO5 or WENO5-JS fluxes"); return OSB_EUNSUPPORTED; }
+    if (p->conv != OSB_CONV_TENO5 && p->conv != OSB_CONV_WENO5JS && p->conv != OSB_CONV_WENO5Z &&
+        p->conv != OSB_CONV_TENO6) {
+      snprintf(why, n, "2D blocks: TENO5, TENO6, WENO5-JS or WENO5-Z fluxes");
+      return OSB_EUNSUPPORTED;
+    }
     if (p->teno_adaptive) {
       if (p->conv != OSB_CONV_TENO5) { snprintf(why, n, "teno_adaptive needs TENO5 fluxes"); return OSB_EINVAL; }
       if (!(p->sensor_eps >= 0) || !std::isfinite(p->teno_a1) || !std::isfinite(p->teno_a2)) {

@@ -282,13 +282,28 @@ class GB300Writer:
         weno = self._kernels("LLFWeno_reconstruction_")
         if bool(teno) == bool(weno) or len(teno or weno) != 2:
             raise NotImplementedError("2D blocks: one LLFTeno or LLFWeno reconstruction per direction expected")
+        conv = None
         for k in teno:
             lhs = self._lhs_names(k)
             if not {"delta_0", "delta_1", "delta_2", "inv_omega_sum"} <= lhs:
                 raise NotImplementedError("TENO5 with a cut-off expected in %s" % k.computation_name)
-            if "delta_3" in lhs:
-                raise NotImplementedError("TENO6 on a 2D block is not lowered (3D blocks only)")
+            kconv = "teno6" if "delta_3" in lhs else "teno5"  # LLFTeno(6) adds a fourth candidate
+            if conv not in (None, kconv):
+                raise NotImplementedError("mixed TENO orders across directions")
+            conv = kconv
+        for k in weno:
+            lhs = self._lhs_names(k)
+            if not {"beta_0", "beta_1", "beta_2", "alpha_0", "omega_0", "inv_alpha_sum"} <= lhs:
+                raise NotImplementedError("WENO5 reconstruction expected in %s" % k.computation_name)
+            # WenoZ's alphas carry the global indicator |beta_0 - beta_2| (weno.py:283-331)
+            alpha0 = [e for e in k.equations if str(e.lhs) == "alpha_0"]
+            kconv = "weno5z" if alpha0 and "Abs(" in str(alpha0[0].rhs) else "weno5js"
+            if conv not in (None, kconv):
+                raise NotImplementedError("mixed WENO formulations across directions")
+            conv = kconv
         adaptive = self._adaptive_teno(teno) if teno else None
+        if adaptive is not None and conv != "teno5":
+            raise NotImplementedError("the adaptive cut-off is lowered for TENO5")
         if self._max_offset(teno or weno) != 3:
             raise NotImplementedError("5th-order reconstruction stencil expected")
         if not self._kernels("MetricsEquation") or not self._kernels("Metric boundary"):
@@ -330,7 +345,8 @@ class GB300Writer:
         if any(v not in lo for v in order):
             raise NotImplementedError("Dirichlet face must set rho, rhou0, rhou1, rhoE")
         physics_check.check_algorithm(self.components, 2, viscous=True, sutherland=True, metric=True)
-        return Plan(ndim=2, n=(64, 32, 1), delta=(1.0, 1.0, 1.0), conv="teno5" if teno else "weno5js",
+        return Plan(ndim=2, n=(64, 32, 1), delta=(1.0, 1.0, 1.0), conv=conv,
+                    weno_eps=1e-14 if conv == "weno5z" else 1e-6,  # WenoZ.eps / WenoJS.eps (weno.py)
                     visc="sutherland", rk="ls_rk3", precision=precision,
                     bc=(tuple(bcs[0]), tuple(bcs[1]), ("periodic", "periodic")),
                     rk_a=coeff["rkA"], rk_b=coeff["rkB"], use_graphs=use_graphs, ic="host",

@@ -34,6 +34,9 @@ CASES = {
     "tgv_weno_modified": "tgv_weno_modified.py",
     "katzer_teno": "katzer_teno.py",
     "katzer_carpenter": "katzer_carpenter.py",
+    "katzer_weno": "katzer_weno.py",
+    "katzer_wenoz": "katzer_wenoz.py",
+    "katzer_teno6": "katzer_teno6.py",
     "katzer_adaptive": "ref:apps/katzer_SBLI/katzer_SBLI.py",
 }
 

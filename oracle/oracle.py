@@ -139,6 +139,7 @@ class Cfg2D(ctypes.Structure):
         ("teno_a2", ctypes.c_double),
         ("sensor_eps", ctypes.c_double),
         ("closure", (ctypes.c_int * 2) * 2),
+        ("conv", ctypes.c_int),
     ]
 
 
@@ -166,6 +167,7 @@ def make_cfg2d(plan):
     for d in range(2):
         for side in range(2):
             c.closure[d][side] = CLOSURES[plan.closure[d][side]]
+    c.conv = CONV[plan.conv]
     return c
 
 

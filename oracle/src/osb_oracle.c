@@ -759,3 +759,8 @@ int osbo_run(const osbo_cfg *cfg, double *q, int nsteps, double *ke) {
   st_free(&s);
   return 0;
 }
+
+/* The reconstruction sides, shared with the 2D restatement (osb_oracle2d.c). */
+double osbo_side_weno5_plus(const double f[5], int z) { return weno5_plus(f, z); }
+double osbo_side_weno5_minus(const double g[5], int z) { return weno5_minus(g, z); }
+double osbo_side_teno6(const double g[6], int plus, double eps, double CT) { return teno6_side(g, plus, eps, CT); }

@@ -62,6 +62,9 @@ typedef struct {
   /* one-sided closure of the central first derivatives at each face [axis][side]:
    * 0 ReducedAccess (reduced_access_scheme.py), 1 Carpenter (Carpenter_scheme.py) */
   int closure[2][2];
+  /* characteristic scheme: OSBO_CONV_TENO5 (default 0 is read as TENO5), OSBO_CONV_WENO5JS,
+   * OSBO_CONV_WENO5Z or OSBO_CONV_TENO6 */
+  int conv;
 } osbo2d_cfg;
 
 /* Advance q by nsteps LS-RK3 steps.  q holds [4][n1+8][n0+8]: rho, rhou0, rhou1, rhoE with a

@@ -20,6 +20,11 @@
 
 #define H 5
 
+/* the 3D restatement's reconstruction sides (osb_oracle.c) */
+double osbo_side_weno5_plus(const double f[5], int z);
+double osbo_side_weno5_minus(const double g[5], int z);
+double osbo_side_teno6(const double g[6], int plus, double eps, double CT);
+
 typedef struct {
   osbo2d_cfg c;
   int px, py;
@@ -344,8 +349,8 @@ static double teno5_plus(const s2_t *s, const double f[5], double CT) {
          0.05 * d2 * iw * ((1.0 / 6.0) * f[0] - (7.0 / 12.0) * f[1] + (11.0 / 12.0) * f[2]);
 }
 
-/* Characteristic TENO fluxes in direction dir with Roe averaging and the 2D Euler eigensystem for a
- * unit normal (physical_models/euler_eigensystem.py:77-105; the block's metric is diagonal, so the
+/* Characteristic fluxes (TENO5, WENO5-JS, WENO5-Z or TENO6, as the configuration says) in direction
+ * dir with Roe averaging and the 2D Euler eigensystem for a unit normal (physical_models/euler_eigensystem.py:77-105; the block's metric is diagonal, so the
  * eigensystem is Cartesian and the metric enters the residual only). */
 static void teno_fluxes(s2_t *s, int dir) {
   const double g = s->c.gama;
@@ -401,13 +406,30 @@ static void teno_fluxes(s2_t *s, int dir) {
     }
     double rec[4];
     const double CT = teno_cutoff(s, c);
+    const int conv = s->c.conv;
     for (int r = 0; r < 4; ++r) {
       double fp[5], fm[5];
       for (int t = 0; t < 5; ++t) {
         fp[t] = CF[r][t] + lam[r] * CS[r][t];
         fm[t] = CF[r][5 - t] - lam[r] * CS[r][5 - t];
       }
-      rec[r] = teno5_plus(s, fp, CT) + teno5_plus(s, fm, CT);
+      if (conv == OSBO_CONV_WENO5JS || conv == OSBO_CONV_WENO5Z) {
+        /* weno.py:341-369 (JS) and 283-331 (Z): + side on points i-2..i+2, - side on i-1..i+3 */
+        double g[5];
+        for (int t = 0; t < 5; ++t) g[t] = CF[r][t + 1] - lam[r] * CS[r][t + 1];
+        const int z = conv == OSBO_CONV_WENO5Z;
+        rec[r] = osbo_side_weno5_plus(fp, z) + osbo_side_weno5_minus(g, z);
+      } else if (conv == OSBO_CONV_TENO6) {
+        /* teno.py:94-192, 216-234: both sides on the six points */
+        double gp[6], gm[6];
+        for (int t = 0; t < 6; ++t) {
+          gp[t] = CF[r][t] + lam[r] * CS[r][t];
+          gm[t] = CF[r][t] - lam[r] * CS[r][t];
+        }
+        rec[r] = osbo_side_teno6(gp, 1, s->c.teno_eps, CT) + osbo_side_teno6(gm, 0, s->c.teno_eps, CT);
+      } else {
+        rec[r] = teno5_plus(s, fp, CT) + teno5_plus(s, fm, CT);
+      }
     }
     /* REV columns (euler_eigensystem.py:90-92) */
     const double hh = (phi + a * a) / (g - 1);

@@ -52,6 +52,10 @@ CASES_2D = {
     "katzer_adaptive": ((64, 32), 20, {"dt": 0.01}),
     # Carpenter closures (the reference's default) on the outlet and the wall, ReducedAccess elsewhere
     "katzer_carpenter": ((64, 32), 20, {"dt": 0.01}),
+    # the other characteristic schemes on the 2D block
+    "katzer_weno": ((64, 32), 20, {"dt": 0.01}),
+    "katzer_wenoz": ((64, 32), 20, {"dt": 0.01}),
+    "katzer_teno6": ((64, 32), 20, {"dt": 0.01}),
 }
 VARS_2D = ["rho", "rhou0", "rhou1", "rhoE"]
 

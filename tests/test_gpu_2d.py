@@ -21,13 +21,36 @@ def run_gpu_2d(plan, q0_pad, x1_pad, steps, dt):
     return q
 
 
-def test_gpu_2d_fp64_matches_reference_golden():
-    q0, x1, q_ref, n, steps, params = load_golden_2d()
-    plan = golden_plan_2d(n=n).replace(dt=params["dt"])
+# WENO5-Z's eps = 1e-14 leaves its weights ill-conditioned where a characteristic field is flat: the
+# oracle itself matches the reference's generated code to 3e-11 on this fixture (1e-15 for the others)
+TOL_2D = {"katzer_teno": 1e-12, "katzer_weno": 1e-12, "katzer_teno6": 1e-12, "katzer_wenoz": 1e-9}
+
+
+@pytest.mark.parametrize("case", sorted(TOL_2D))
+def test_gpu_2d_fp64_matches_reference_golden(case):
+    q0, x1, q_ref, n, steps, params = load_golden_2d(case)
+    plan = golden_plan_2d(case, n=n).replace(dt=params["dt"])
     q = run_gpu_2d(plan, q0, x1, steps, params["dt"])
     ref = q_ref[:, 4:-4, 4:-4]
     err = [float(np.abs(q[v] - ref[v]).max() / np.abs(ref[v]).max()) for v in range(4)]
-    assert max(err) <= 1e-12, err
+    assert max(err) <= TOL_2D[case], err
+
+
+@pytest.mark.parametrize("case", ["katzer_weno", "katzer_wenoz", "katzer_teno6"])
+def test_gpu_2d_schemes_fp64_match_oracle_and_mixed_close(case):
+    """The other characteristic schemes on a wider block: FP64 against the oracle, mixed within 1e-5
+    (relative L2) of FP64 after 10 steps."""
+    q0, x1, _, n, _, params = load_golden_2d(case)
+    q0w, x1w = widen_2d(q0, 96), widen_2d(x1[None], 96)[0]
+    plan = golden_plan_2d(case, n=(96, n[1])).replace(dt=params["dt"])
+    q_or = O.run2d(plan, q0w, 10)
+    q = run_gpu_2d(plan, q0w, x1w, 10, params["dt"])
+    ref = q_or[:, 4:-4, 4:-4]
+    err = [float(np.abs(q[v] - ref[v]).max() / np.abs(ref[v]).max()) for v in range(4)]
+    assert max(err) <= TOL_2D[case], err
+    qm = run_gpu_2d(plan.replace(precision="mixed"), q0w, x1w, 10, params["dt"])
+    l2 = [float(np.linalg.norm(qm[v] - q[v]) / np.linalg.norm(q[v])) for v in range(4)]
+    assert max(l2) <= 1e-5, l2
 
 
 @pytest.mark.parametrize("n0,steps", [(70, 10), (130, 5)])

@@ -72,7 +72,8 @@ def test_oracle_matches_reference_run(case, n, steps, extra):
     assert max(rel_err(q, q_ref)) < 1e-12
 
 
-@pytest.mark.parametrize("case", ["katzer_teno", "katzer_adaptive", "katzer_carpenter"])
+@pytest.mark.parametrize("case", ["katzer_teno", "katzer_adaptive", "katzer_carpenter", "katzer_weno", "katzer_wenoz",
+                                  "katzer_teno6"])
 def test_oracle_2d_matches_reference_golden(case):
     from helpers import load_golden_2d, golden_plan_2d, rel_err_2d
     q0, x1, q_ref, n, steps, params = load_golden_2d(case)
@@ -81,9 +82,11 @@ def test_oracle_2d_matches_reference_golden(case):
     carp = (("reduced_access", "carpenter"), ("carpenter", "reduced_access"))
     assert plan.closure == (carp if case == "katzer_carpenter" else (("reduced_access",) * 2,) * 2)
     q = O.run2d(plan, q0, steps)
-    assert max(rel_err_2d(q, q_ref)) < 1e-12
+    # WENO5-Z (eps = 1e-14) amplifies rounding where a characteristic field is flat: 3e-11 here
+    tol = 1e-9 if case == "katzer_wenoz" else 1e-12
+    assert max(rel_err_2d(q, q_ref)) < tol
     # halos too (the outlet and wall faces write them)
-    assert float(np.abs(q - q_ref).max()) < 1e-10
+    assert float(np.abs(q - q_ref).max()) < 1e2 * tol
 
 
 def test_oracle_adaptive_cutoff_changes_the_solution():

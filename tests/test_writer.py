@@ -102,7 +102,8 @@ def test_cfl_dt_tgv_weno():
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
 @pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central",
-                                  "katzer_teno", "katzer_adaptive", "katzer_carpenter", "tgv_filter"])
+                                  "katzer_teno", "katzer_adaptive", "katzer_carpenter", "tgv_filter",
+                                  "katzer_weno", "katzer_wenoz", "katzer_teno6"])
 def test_writer_lowers_reference_script(case, tmp_path):
     r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case, "--out",
                         str(tmp_path), "--ref", REF], capture_output=True, text=True, timeout=900)
