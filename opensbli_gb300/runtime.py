@@ -384,6 +384,62 @@ class Solver:
         self._out()
         return out
 
+    def advance_host_states(self, inputs, outputs, dt, nsteps=1):
+        """Advance independent states held in page-locked host memory: outputs[k] = the state after
+        nsteps RK3 steps of size dt from inputs[k] (FP64 [nvar][z][y][x], contiguous pinned host
+        tensors; an input tensor may be listed more than once).  The jobs are pipelined over three
+        streams: while job k computes, the copy engines bring job k+1's state in and take job k-1's
+        result out, so the host link's time hides behind the kernels instead of adding to them.  The
+        solver's own state is left holding the last job's result.  Returns when every output has
+        been written."""
+        shape = (self.layout.nvar,) + self.shape
+        for t in list(inputs) + list(outputs):
+            if not (self._pinned64(t) and tuple(t.shape) == shape):
+                raise ValueError("inputs and outputs must be contiguous pinned FP64 host tensors of shape %s" %
+                                 (shape,))
+        if len(inputs) != len(outputs):
+            raise ValueError("one output per input")
+        if not hasattr(self, "_pipe"):
+            self._pipe = {
+                "in": [torch.empty(shape, dtype=torch.float64, device=self.device) for _ in range(2)],
+                "out": [torch.empty(shape, dtype=torch.float64, device=self.device) for _ in range(2)],
+                "h2d": torch.cuda.Stream(self.device), "d2h": torch.cuda.Stream(self.device)}
+        pp = self._pipe
+        ev = lambda: torch.cuda.Event()  # noqa: E731
+        loaded, consumed, computed, drained = [None, None], [None, None], [None, None], [None, None]
+        self._in()
+        pp["h2d"].wait_stream(self.stream)
+        pp["d2h"].wait_stream(self.stream)
+        for k, (src, dst) in enumerate(zip(inputs, outputs)):
+            slot = k % 2
+            with torch.cuda.stream(pp["h2d"]):
+                if consumed[slot] is not None:
+                    pp["h2d"].wait_event(consumed[slot])  # job k-2 has read this staging buffer
+                pp["in"][slot].copy_(src, non_blocking=True)
+                loaded[slot] = ev()
+                loaded[slot].record(pp["h2d"])
+            self.stream.wait_event(loaded[slot])
+            for v in range(self.layout.nvar):
+                self._check(self.lib.osb_set_state64(self.ctx, v, ctypes.c_void_p(pp["in"][slot][v].data_ptr())))
+            consumed[slot] = ev()
+            consumed[slot].record(self.stream)
+            self._check(self.lib.osb_step(self.ctx, int(nsteps), float(dt)))
+            if drained[slot] is not None:
+                self.stream.wait_event(drained[slot])  # job k-2's result has left this buffer
+            for v in range(self.layout.nvar):
+                self._check(self.lib.osb_get_state64(self.ctx, v, ctypes.c_void_p(pp["out"][slot][v].data_ptr())))
+            computed[slot] = ev()
+            computed[slot].record(self.stream)
+            with torch.cuda.stream(pp["d2h"]):
+                pp["d2h"].wait_event(computed[slot])
+                dst.copy_(pp["out"][slot], non_blocking=True)
+                drained[slot] = ev()
+                drained[slot].record(pp["d2h"])
+        pp["d2h"].synchronize()
+        pp["h2d"].synchronize()
+        self.stream.synchronize()
+        self._out()
+
     def teno_cutoff(self):
         """The adaptive TENO cut-off C_T of the current state, FP64 [n1][n0] (2D plans with
         teno_adaptive; the reference's TENO_B0 output field)."""

@@ -21,9 +21,11 @@ def run_gpu_2d(plan, q0_pad, x1_pad, steps, dt):
     return q
 
 
-# WENO5-Z's eps = 1e-14 leaves its weights ill-conditioned where a characteristic field is flat: the
-# oracle itself matches the reference's generated code to 3e-11 on this fixture (1e-15 for the others)
-TOL_2D = {"katzer_teno": 1e-12, "katzer_weno": 1e-12, "katzer_teno6": 1e-12, "katzer_wenoz": 1e-9}
+# Rounding sensitivity of the reference's own arithmetic on these fixtures (the oracle compiled with and
+# without FMA contraction, max-normalised difference after the 20 steps): TENO5 and WENO5-JS 1e-15,
+# TENO6 1.0e-12 (its sixth powers of (1 + tau/(eps + beta)) with eps = 1e-15 near the wall), WENO5-Z
+# 3e-11 (eps = 1e-14).  Each bar sits a few times above that floor.
+TOL_2D = {"katzer_teno": 1e-12, "katzer_weno": 1e-12, "katzer_teno6": 5e-12, "katzer_wenoz": 1e-9}
 
 
 @pytest.mark.parametrize("case", sorted(TOL_2D))
