@@ -31,6 +31,7 @@ CASES = {
     "tgv_teno": "tgv_teno.py",
     "tgv_teno6": "tgv_teno6.py",
     "tgv_filter": "tgv_filter.py",
+    "tgv_teno_adaptive": "tgv_teno_adaptive.py",
     "tgv_weno_modified": "tgv_weno_modified.py",
     "katzer_teno": "katzer_teno.py",
     "katzer_carpenter": "katzer_carpenter.py",
