@@ -91,8 +91,9 @@ typedef struct osb_plan_desc {
   double Twall, SuthT, RefT;
   double dirichlet_state[2][4];
   double dirichlet_x_switch;
-  /* TENO5 with the cut-off adapted per interface by the modified Ducros sensor (2D blocks;
-   * schemes/spatial/teno.py:430-443, schemes/spatial/shock_sensors.py:12-49): at the interface whose
+  /* TENO with the cut-off adapted per interface by the modified Ducros sensor (TENO5 on 2D blocks,
+   * TENO5 or TENO6 on 3D blocks; schemes/spatial/teno.py:430-443, schemes/spatial/shock_sensors.py:
+   * 12-49): at the interface whose
    * left point is P, C_T = 10^-floor(teno_a1 - teno_a2 (1 - (1 - theta)^4 (1 + 4 theta))) with
    * theta(P) = (1/2 - 1/2 tanh(2.5 + 250 div u)) (div u)^2 / (sensor_eps + (div u)^2 + |curl u|^2)
    * on the interior (0 elsewhere).  teno_adaptive = 0 keeps the fixed teno_ct. */
@@ -161,7 +162,8 @@ int osb_set_state64(osb_ctx *ctx, int var, const double *dev_interior);
 int osb_get_state64(osb_ctx *ctx, int var, double *dev_interior);
 
 /* Plans with teno_adaptive: evaluate the TENO cut-off C_T of the current state (after applying the
- * boundary conditions) into a device array of n0*n1 doubles laid out [x1][x0].  The reference
+ * boundary conditions) into a device array of n0*n1 doubles laid out [x1][x0] (2D blocks) or
+ * n0*n1*n2 doubles laid out [x2][x1][x0] (3D blocks).  The reference
  * stores the same field, TENO_B0, for output (StoreSome in apps/katzer_SBLI/katzer_SBLI.py);
  * values are 10^-k with k an integer. */
 int osb_teno_cutoff(osb_ctx *ctx, double *dev_out);

@@ -80,7 +80,16 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
     return OSB_OK;
   }
   if (p->ndim != 3) { snprintf(why, n, "ndim %d: this library implements 2D and 3D blocks", p->ndim); return OSB_EUNSUPPORTED; }
-  if (p->teno_adaptive) { snprintf(why, n, "adaptive TENO is implemented on 2D blocks"); return OSB_EUNSUPPORTED; }
+  if (p->teno_adaptive) {
+    if (p->conv != OSB_CONV_TENO5 && p->conv != OSB_CONV_TENO6) {
+      snprintf(why, n, "teno_adaptive needs TENO5 or TENO6 fluxes");
+      return OSB_EINVAL;
+    }
+    if (!(p->sensor_eps >= 0) || !std::isfinite(p->teno_a1) || !std::isfinite(p->teno_a2)) {
+      snprintf(why, n, "adaptive TENO: sensor_eps >= 0 and finite teno_a1, teno_a2");
+      return OSB_EINVAL;
+    }
+  }
   if (p->filter != OSB_FILTER_NONE && p->filter != OSB_FILTER_WENO5_CONSTANT) {
     snprintf(why, n, "filter %d: OSB_FILTER_NONE or OSB_FILTER_WENO5_CONSTANT", p->filter);
     return OSB_EUNSUPPORTED;
@@ -320,6 +329,10 @@ void prof_collect(osb_ctx *c) {
 // time loop
 // ---------------------------------------------------------------------------------------------
 template <typename T> void weno_all(osb_ctx *c, Fields5<const T> qc, Fields5<T> r, cudaStream_t s) {
+  if (c->plan.teno_adaptive) {
+    ProfScope ps(c, PF_OTHER, s);
+    launch_sensor_ct3<T>(*c, qc, s, &c->launches);
+  }
   for (int d = 0; d < 3; ++d) {
     ProfScope ps(c, PF_WENO_X + d, s);
     launch_weno_dir<T>(*c, qc, r, d, s, &c->launches);
@@ -741,6 +754,11 @@ int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
     if (e == cudaSuccess) e = cudaMemset(c->qold[v], 0, (size_t)c->g.numel * sizeof(double));
     if (e == cudaSuccess) e = cudaMemset(c->res[v], 0, bytes);
   }
+  if (e == cudaSuccess && plan->teno_adaptive) {
+    e = cudaMalloc(&c->ct2, bytes);
+    if (e == cudaSuccess) e = cudaMemset(c->ct2, 0, bytes);
+    c->ph.ctp = c->ct2;
+  }
   c->red_blocks = 152 * 8;
   if (e == cudaSuccess) e = cudaMalloc(&c->red, (c->red_blocks + 1) * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(int));
@@ -914,8 +932,20 @@ int osb_get_state64(osb_ctx *c, int var, double *dst) {
 int osb_teno_cutoff(osb_ctx *c, double *dev_out) {
   if (!c) return OSB_EINVAL;
   if (!dev_out) return set_err(c, OSB_EINVAL, "null output");
-  if (c->plan.ndim != 2 || !c->plan.teno_adaptive) return set_err(c, OSB_EINVAL, "plan has no adaptive TENO");
+  if (!c->plan.teno_adaptive) return set_err(c, OSB_EINVAL, "plan has no adaptive TENO");
   if (int rc = check_bound(c)) return rc;
+  if (c->plan.ndim == 3) {
+    if (!c->qold_valid) return set_err(c, OSB_EINVAL, "set the state first");
+    int64_t l = 0;
+    if (c->mixed) {
+      launch_halos<float>(*c, fields<float>(c->qa), c->stream, &l);
+      launch_cutoff3<float>(*c, fields<const float>(c->qa), dev_out, c->stream, &l);
+    } else {
+      launch_halos<double>(*c, fields<double>(c->qa), c->stream, &l);
+      launch_cutoff3<double>(*c, fields<const double>(c->qa), dev_out, c->stream, &l);
+    }
+    return cuda_err(c, cudaGetLastError(), "osb_teno_cutoff");
+  }
   if (!c->metrics_valid) return set_err(c, OSB_EINVAL, "2D block: call osb_set_coordinate first");
   if (!c->qold_valid) return set_err(c, OSB_EINVAL, "2D block: set the state first");
   int64_t l = 0;
@@ -1142,6 +1172,8 @@ static int adjoint_check(osb_ctx *c) {
   for (int d = 0; d < 3; ++d)
     if (p.bc[d][0] != OSB_BC_PERIODIC || p.bc[d][1] != OSB_BC_PERIODIC)
       return set_err(c, OSB_EUNSUPPORTED, "adjoint: periodic boundaries only");
+  if (p.teno_adaptive || p.filter != OSB_FILTER_NONE)
+    return set_err(c, OSB_EUNSUPPORTED, "adjoint: fixed TENO cut-off and no WENO filter");
   int rc = check_bound(c);
   if (rc) return rc;
   return cuda_err(c, adj_ensure(*c), "adjoint scratch allocation");

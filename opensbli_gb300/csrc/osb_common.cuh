@@ -43,6 +43,9 @@ struct Phys {
   // TENO cut-off C_T (weno_eps holds TENO's eps for TENO plans)
   double teno_ct;
   float f_teno_ct;
+  // adaptive TENO on 3D blocks: C_T per point (state precision, padded layout); the interface
+  // between cells c-1 and c takes the value at c-1.  Null for a fixed cut-off.
+  const void *ctp;
 };
 
 // the FP64 or FP32 copy of a plan constant

@@ -55,7 +55,7 @@ struct Ctx {
   double *q64_2d[4] = {};         // FP64 master state, padded (the bound arrays in FP64 mode)
   double *du2[4] = {};            // LS-RK register
   void *prim2[6] = {};            // u0, u1, p, a, T, mu (state precision, padded)
-  void *ct2 = nullptr;            // adaptive TENO: cut-off C_T per point (state precision, padded)
+  void *ct2 = nullptr;            // adaptive TENO (2D and 3D): cut-off C_T per point (state precision, padded)
   double *x1 = nullptr, *d11 = nullptr, *sd111 = nullptr;
   int metrics_valid = 0;
   std::string err;
@@ -89,6 +89,12 @@ template <typename T>
 void launch_weno_dir(const Ctx &c, Fields5<const T> q, Fields5<T> r, int dir, cudaStream_t s, int64_t *launches);
 template <typename T>
 void launch_weno_cfg(const Ctx &c, Fields5<const T> q, Fields5<T> r, int dir, WenoCfg w, cudaStream_t s);
+// adaptive TENO on 3D blocks: the cut-off C_T per point of the halo-filled state q into ct2
+// (read by the flux kernels through Phys::ctp), and its interior packed as FP64 [z][y][x]
+template <typename T>
+void launch_sensor_ct3(const Ctx &c, Fields5<const T> q, cudaStream_t s, int64_t *launches);
+template <typename T>
+void launch_cutoff3(const Ctx &c, Fields5<const T> q, double *out, cudaStream_t s, int64_t *launches);
 // the WENO5 non-linear filter: flux pass of one direction (x writes r, y and z accumulate), and the
 // update qold += dt_fc * r, q = qold (FP32 state rounded once)
 template <typename T>

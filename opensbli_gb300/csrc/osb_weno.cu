@@ -157,7 +157,15 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
           link_flux(W[4], fl_last, fl_new);
           fl_last = fl_new;
           T fl[5];
-          interface_flux<T, DIR, SCH>(W, gm1, igm1, eps, ct, fl);
+          T cti = ct;
+          if constexpr (SCH == SCH_TENO || SCH == SCH_TENO6) {
+            if (ph.ctp) {  // cut-off at the interface's left point, cell d0-1+m0+w
+              int i, j, k;
+              coords(m0 + w + 2, a, i, j, k);
+              cti = static_cast<const T *>(ph.ctp)[gidx(g, i, j, k)];
+            }
+          }
+          interface_flux<T, DIR, SCH>(W, gm1, igm1, eps, cti, fl);
 #pragma unroll
           for (int v = 0; v < 5; ++v) {
             sflux[fidx(v, m0 + w, a)] = fl[v];
@@ -270,7 +278,10 @@ __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> 
       for (int v = 0; v < 5; ++v) rv[v] = res.v[v][mc];
     }
     T F[5];
-    interface_flux<T, DIR, SCH>(W, gm1, igm1, eps, ct, F);
+    T cti = ct;
+    if constexpr (SCH == SCH_TENO || SCH == SCH_TENO6)
+      if (ph.ctp) cti = static_cast<const T *>(ph.ctp)[mline + (int64_t)(c - 1) * sd];
+    interface_flux<T, DIR, SCH>(W, gm1, igm1, eps, cti, F);
     if (c > c0) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
@@ -393,7 +404,12 @@ __device__ __forceinline__ void weno_march_x_tile(const Grid &g, Fields5<const T
       if (p >= c0 + 2) {  // window holds points c-3 .. c+2 of interface c = p - 2
         const int c = p - 2;
         T F[5] = {T(0), T(0), T(0), T(0), T(0)};  // rows past n1: defined, never stored
-        if (row_ok) interface_flux<T, 0, SCH>(W, gm1, igm1, eps, ct, F);
+        if (row_ok) {
+          T cti = ct;
+          if constexpr (SCH == SCH_TENO || SCH == SCH_TENO6)
+            if (ph.ctp) cti = static_cast<const T *>(ph.ctp)[gidx(g, c - 1, j0 + lane, k)];
+          interface_flux<T, 0, SCH>(W, gm1, igm1, eps, cti, F);
+        }
         if (c > c0) {
           const int cc = c - 1;  // cell finished by this interface
           const int gs = ((cc + 4) / RG) * RG - 4, col = cc - gs;
@@ -576,6 +592,88 @@ void launch_batch_weno(const int4 *items, int nitems, int *counter, int parity, 
   }
 }
 
+// ---------------------------------------------------------------------------------------------
+// adaptive TENO cut-off (schemes/spatial/teno.py:430-443) from the modified Ducros sensor
+// (schemes/spatial/shock_sensors.py:12-49)
+// ---------------------------------------------------------------------------------------------
+static __constant__ double c_p10n3[23] = {1e0,   1e-1,  1e-2,  1e-3,  1e-4,  1e-5,  1e-6,  1e-7,
+                                          1e-8,  1e-9,  1e-10, 1e-11, 1e-12, 1e-13, 1e-14, 1e-15,
+                                          1e-16, 1e-17, 1e-18, 1e-19, 1e-20, 1e-21, 1e-22};
+
+__device__ __forceinline__ float tanh_s(float x) { return tanhf(x); }
+__device__ __forceinline__ double tanh_s(double x) { return tanh(x); }
+
+// Over the points [-1, n_d] of every axis (the left points of all interfaces the flux kernels
+// form).  On the interior, with 4th-order central first derivatives of u_i = rhou_i / rho:
+//   theta = (1/2 - 1/2 tanh(250 div + 2.5)) div^2 / (eps + |curl u|^2 + div^2);
+// theta = 0 elsewhere (the sensor is evaluated on the interior only and the generated code never
+// fills its halos).  C_T = 10^-floor(a1 - a2 (1 - (1 - theta)^4 (1 + 4 theta))), the exponent
+// formed in FP64 in both precisions and the power taken from a table of correctly rounded 10^-k.
+template <typename T>
+__global__ void k_sensor_ct3(Grid g, Fields5<const T> q, T *ct, double i0, double i1, double i2, double a1,
+                             double a2, double seps) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x - 1, j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+  const int k = (int)blockIdx.z - 1;
+  if (i > g.n0 || j > g.n1) return;
+  const int64_t n = gidx(g, i, j, k);
+  double th = 0.0;
+  if (i >= 0 && i < g.n0 && j >= 0 && j < g.n1 && k >= 0 && k < g.n2) {
+    const int64_t st[3] = {1, g.sy, g.sz};
+    const T id[3] = {T(i0), T(i1), T(i2)};
+    T du[3][3];  // du[c][d] = d u_c / d x_d
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      T u[4][3];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        const int o = t < 2 ? t - 2 : t - 1;  // -2, -1, +1, +2
+        const int64_t m = n + o * st[d];
+        const T ir = T(1) / q.v[0][m];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) u[t][c] = q.v[1 + c][m] * ir;
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+        du[c][d] = id[d] * ((u[0][c] - u[3][c]) * T(1.0 / 12.0) + (u[2][c] - u[1][c]) * T(2.0 / 3.0));
+    }
+    const T div = du[0][0] + du[1][1] + du[2][2];
+    const T w0 = du[2][1] - du[1][2], w1 = du[0][2] - du[2][0], w2 = du[1][0] - du[0][1];
+    const T sw = T(0.5) - T(0.5) * tanh_s(T(250) * div + T(2.5));
+    th = (double)(sw * (div * div) / (T(seps) + w0 * w0 + w1 * w1 + w2 * w2 + div * div));
+  }
+  const double w = 1.0 - th;
+  const double e = floor(a1 - a2 * (1.0 - (w * w) * (w * w) * (4.0 * th + 1.0)));
+  ct[n] = T((e >= 0.0 && e <= 22.0) ? c_p10n3[(int)e] : pow(10.0, -e));
+}
+
+template <typename T>
+void launch_sensor_ct3(const Ctx &c, Fields5<const T> q, cudaStream_t s, int64_t *launches) {
+  const osb_plan_desc &p = c.plan;
+  dim3 b(32, 8), gs((c.g.n0 + 2 + 31) / 32, (c.g.n1 + 2 + 7) / 8, c.g.n2 + 2);
+  k_sensor_ct3<T><<<gs, b, 0, s>>>(c.g, q, static_cast<T *>(c.ct2), 1.0 / p.delta[0], 1.0 / p.delta[1],
+                                   1.0 / p.delta[2], p.teno_a1, p.teno_a2, p.sensor_eps);
+  ++*launches;
+}
+
+// The cut-off of the current state over the interior, FP64 [z][y][x] (the reference's TENO_B0).
+template <typename T> __global__ void k_pack_ct3(Grid g, const T *ct, double *out) {
+  const int64_t N = (int64_t)g.n0 * g.n1 * g.n2;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.n0), j = (int)((t / g.n0) % g.n1), k = (int)(t / ((int64_t)g.n0 * g.n1));
+    out[t] = (double)ct[gidx(g, i, j, k)];
+  }
+}
+
+template <typename T>
+void launch_cutoff3(const Ctx &c, Fields5<const T> q, double *out, cudaStream_t s, int64_t *launches) {
+  launch_sensor_ct3<T>(c, q, s, launches);
+  const int64_t N = (int64_t)c.g.n0 * c.g.n1 * c.g.n2;
+  int blocks = (int)((N + 255) / 256);
+  if (blocks > c.num_sms * 8) blocks = c.num_sms * 8;
+  k_pack_ct3<T><<<blocks, 256, 0, s>>>(c.g, static_cast<const T *>(c.ct2), out);
+  ++*launches;
+}
+
 // The filter's update of the interior (filters/WENO_filter.py:258-282, kappa = Wall = 1): the FP64
 // master copy takes q + dt * shock_filter_control * R, the bound state its value (FP32: rounded once)
 template <typename T>
@@ -663,6 +761,10 @@ template void launch_filter_dir<float>(const Ctx &, Fields5<const float>, Fields
                                        int64_t *);
 template void launch_filter_dir<double>(const Ctx &, Fields5<const double>, Fields5<double>, int, cudaStream_t,
                                         int64_t *);
+template void launch_sensor_ct3<float>(const Ctx &, Fields5<const float>, cudaStream_t, int64_t *);
+template void launch_sensor_ct3<double>(const Ctx &, Fields5<const double>, cudaStream_t, int64_t *);
+template void launch_cutoff3<float>(const Ctx &, Fields5<const float>, double *, cudaStream_t, int64_t *);
+template void launch_cutoff3<double>(const Ctx &, Fields5<const double>, double *, cudaStream_t, int64_t *);
 template void launch_weno_dir<float>(const Ctx &, Fields5<const float>, Fields5<float>, int, cudaStream_t, int64_t *);
 template void launch_weno_dir<double>(const Ctx &, Fields5<const double>, Fields5<double>, int, cudaStream_t,
                                       int64_t *);

@@ -26,7 +26,7 @@ import re
 
 import sympy
 
-_DERIV_NAMES = re.compile(r"^(Convective|Viscous|Derivative evaluation) (CD )+")
+_DERIV_NAMES = re.compile(r"^(Convective|Viscous|Derivative evaluation|ConstituentRelations) (CD )+")
 
 
 def _base(x):

@@ -441,8 +441,8 @@ class Solver:
         self._out()
 
     def teno_cutoff(self):
-        """The adaptive TENO cut-off C_T of the current state, FP64 [n1][n0] (2D plans with
-        teno_adaptive; the reference's TENO_B0 output field)."""
+        """The adaptive TENO cut-off C_T of the current state, FP64 [n1][n0] (2D) or [n2][n1][n0] (3D)
+        for plans with teno_adaptive (the reference's TENO_B0 output field)."""
         self._in()
         with torch.cuda.stream(self.stream):
             out = torch.empty(self.shape, dtype=torch.float64, device=self.device)

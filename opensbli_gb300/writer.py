@@ -110,9 +110,8 @@ class GB300Writer:
             raise NotImplementedError("expected exactly one convective discretisation (Central skew, LLFWeno or "
                                       "LLFTeno)")
         if teno:
-            # LLFTeno(5) with a fixed cut-off TENO_CT (teno.py:407-465); the adaptive cut-off needs the
-            # Ducros sensor, which this build evaluates on 2D blocks only
-            # LLFTeno(6) adds a fourth candidate stencil (delta_3, teno.py:94-105)
+            # LLFTeno(5) with a fixed or Ducros-adapted cut-off (teno.py:407-465); LLFTeno(6) adds a
+            # fourth candidate stencil (delta_3, teno.py:94-105)
             conv = "teno6" if all("delta_3" in self._lhs_names(k) for k in teno) else "teno5"
             if len(teno) != 3:
                 raise NotImplementedError("one LLFTeno reconstruction kernel per direction expected")
@@ -120,8 +119,6 @@ class GB300Writer:
                 lhs = self._lhs_names(k)
                 if not {"delta_0", "delta_1", "delta_2", "inv_omega_sum"} <= lhs:
                     raise NotImplementedError("TENO5 with a cut-off expected in %s" % k.computation_name)
-                if "TENO_CT" in lhs:
-                    raise NotImplementedError("adaptive TENO (Ducros sensor) on a 3D block is not lowered")
                 if self._max_offset([k]) != 3:
                     raise NotImplementedError("5th-order stencil expected in %s" % k.computation_name)
                 avg = [e for e in k.equations if str(e.lhs).endswith("_rho") and str(e.lhs).startswith("AVG_")]
@@ -187,13 +184,17 @@ class GB300Writer:
         if other_bc or any(b is None for pair in bcs for b in pair):
             raise NotImplementedError("unsupported boundary conditions: %s" % (other_bc or bcs))
         filt, fc = self._weno_filter()
+        adaptive = self._adaptive_teno(teno) if teno else None
+        if adaptive is None and self._kernels("ConstituentRelations CD"):
+            raise NotImplementedError("sensor derivative kernels without the adaptive TENO cut-off")
         # the equations behind the recognised kernels must be the physics the fused kernels implement
         physics_check.check_algorithm(self.components, 3, viscous=bool(visc), skew=conv == "central_skew")
         return Plan(ndim=3, conv=conv, visc="const" if visc else "none", rk="rk3", precision=precision,
                     bc=tuple(tuple(p) for p in bcs), rk_a=coeff["rkold"], rk_b=coeff["rknew"],
                     weno_eps=1e-14 if conv == "weno5z" else 1e-6,  # WenoZ.eps / WenoJS.eps (weno.py)
                     use_graphs=use_graphs, ic="host", kernels=[n for n in names if n], filter=filt,
-                    filter_control=fc)
+                    filter_control=fc, teno_adaptive=adaptive is not None,
+                    sensor_eps=adaptive if adaptive is not None else Plan.sensor_eps)
 
     def _weno_filter(self):
         """Recognise the WENO5 non-linear filter (filters/WENO_filter.py:15-339) in the time loop: its
@@ -245,7 +246,7 @@ class GB300Writer:
     # anything else in the time loop (filters, other equation classes, user kernels) would be
     # dropped silently, so it is refused.
     _FAMILIES = re.compile(
-        r"^(CR\w+|ConstituentRelations evaluation|Convective (CD |residual|terms group)|Derivative evaluation CD |"
+        r"^(CR\w+|ConstituentRelations (evaluation|CD )|Convective (CD |residual|terms group)|Derivative evaluation CD |"
         r"LLF(Weno|Teno)(_reconstruction_\d+_direction| Residual)|MetricsEquation|Viscous|Grid_based_initialisation|"
         r"Save equations|Sub stage advancement|Temporal solution advancement|\w+ boundary dir\d side\d|"
         r"User kernel: (Constituent Relations evaluation|WENO reconstruction direction \d|Non-linear filter application))")
@@ -441,8 +442,9 @@ class GB300Writer:
                 got = float(f.subs({th: t, a1: 10.5, a2: 4.5}))
                 if abs(got - want) > 1e-12 * want:
                     raise NotImplementedError("adaptive TENO: C_T formula not recognised")
-        # the sensor equation, with its derivative locals (GridVariables) classified by the variable
-        # and direction of their interior (default-branch) central stencil
+        # the sensor equation, with its velocity derivatives classified by the variable and direction
+        # of their interior (default-branch) central stencil: locals (GridVariables) of the sensor's
+        # kernel on 2D blocks, work arrays written by the "ConstituentRelations CD" kernels on 3D blocks
         locs, theta_eq = {}, None
         for k in self.components:
             if type(k).__name__ != "Kernel":
@@ -454,21 +456,35 @@ class GB300Writer:
                     theta_eq, kern = e, k
         if theta_eq is None:
             raise NotImplementedError("adaptive TENO: no kernel evaluates the sensor %s" % sensor)
-        for e in kern.equations:
-            if type(e.lhs).__name__ != "GridVariable" or not isinstance(e.rhs, sympy.Piecewise):
-                continue
-            body = e.rhs.args[-1][0]
+
+        def classify(rhs, what):
+            body = rhs.args[-1][0] if isinstance(rhs, sympy.Piecewise) else rhs
             ds = [a for a in sympy.preorder_traversal(body) if type(a).__name__ == "DataSet"]
             var = {str(a.base) for a in ds}
             dirs = {d for a in ds for d, i in enumerate(a.indices) if int(i) != 0}
             offs = sorted({int(i) for a in ds for i in a.indices if int(i) != 0})
             if len(var) != 1 or len(dirs) != 1 or offs != [-2, -1, 1, 2]:
-                raise NotImplementedError("adaptive TENO: sensor derivative %s not recognised" % e.lhs)
-            locs[e.lhs] = (var.pop(), dirs.pop())
+                raise NotImplementedError("adaptive TENO: sensor derivative %s not recognised" % what)
+            return var.pop(), dirs.pop()
+
+        for e in kern.equations:
+            if type(e.lhs).__name__ == "GridVariable" and isinstance(e.rhs, sympy.Piecewise):
+                locs[e.lhs] = classify(e.rhs, e.lhs)
+        nd = self.block.ndim
+        # work arrays: the last write before the sensor kernel, by a sensor-derivative kernel
+        written = {}
+        for k in self.components:
+            if k is kern:
+                break
+            if type(k).__name__ != "Kernel":
+                continue
+            for e in k.equations:
+                if hasattr(e.lhs, "base"):
+                    written[str(e.lhs.base)] = (k, e)
         sym = {}
-        for v in ("u0_B0", "u1_B0"):
-            for d in (0, 1):
-                sym[(v, d)] = sympy.Symbol("_osb_d_%s_%d" % (v, d))
+        for v in range(nd):
+            for d in range(nd):
+                sym[("u%d_B0" % v, d)] = sympy.Symbol("_osb_d_u%d_%d" % (v, d))
         D = sympy.Symbol("_osb_D11")
         reps, eps = {}, None
         for a in sympy.preorder_traversal(theta_eq.rhs):
@@ -479,24 +495,37 @@ class GB300Writer:
                 reps[a] = sym[locs[a]]
             elif t == "DataSet" and str(a.base) == "D11_B0" and all(int(i) == 0 for i in a.indices):
                 reps[a] = D
+            elif t == "DataSet":
+                w = written.get(str(a.base))
+                if (nd != 3 or w is None or any(int(i) != 0 for i in a.indices)
+                        or not (w[0].computation_name or "").startswith("ConstituentRelations CD")):
+                    raise NotImplementedError("adaptive TENO: sensor input %s not recognised" % a)
+                key = classify(w[1].rhs, a)
+                if key not in sym:
+                    raise NotImplementedError("adaptive TENO: sensor input %s is not a velocity derivative" % a)
+                reps[a] = sym[key]
             elif t == "ConstantObject" and str(a) == "epsilon":
                 eps = float(a.value)
                 reps[a] = sympy.Float(eps)
         g = theta_eq.rhs.xreplace(reps)
-        # the derivatives carry inv_0/inv_1 = 1/Delta; take Delta = 1 for the check
+        # the derivative locals carry inv_0/inv_1 = 1/Delta; take Delta = 1 for the check (the work
+        # arrays' stencils and spacing factors are checked with the other derivative kernels)
         g = g.subs({s_: 1 for s_ in g.free_symbols if str(s_) in ("inv_0", "inv_1")})
         if eps is None or g.free_symbols - set(sym.values()) - {D}:
             raise NotImplementedError("adaptive TENO: sensor formula not recognised")
-        # derivative locals are (f(+1)*8 - f(-1)*8 + f(-2) - f(+2))/12 etc.: the symbols stand for
-        # the stencil values, so compare against the reference form on random derivative values
+        # compare against the sensor the GPU kernel implements on random derivative values: D11 is
+        # the 2D block's metric factor d(xi1)/d(x1), 1 on the 3D Cartesian block
         rnd = random.Random(7)
         for _ in range(8):
             vals = {k_: rnd.uniform(-0.02, 0.02) for k_ in sym}
-            Dv = rnd.uniform(0.5, 2.0)
-            a_, b_ = vals[("u0_B0", 0)], vals[("u1_B0", 0)]
-            c_, d_ = vals[("u0_B0", 1)], vals[("u1_B0", 1)]
-            div, om = a_ + d_ * Dv, b_ - c_ * Dv
-            want = (0.5 - 0.5 * math.tanh(2.5 + 250.0 * div)) * div * div / (eps + div * div + om * om)
+            Dv = rnd.uniform(0.5, 2.0) if nd == 2 else 1.0
+            du = [[vals[("u%d_B0" % c, d)] * (Dv if d == 1 else 1.0) for d in range(nd)] for c in range(nd)]
+            div = sum(du[c][c] for c in range(nd))
+            if nd == 2:
+                om2 = (du[1][0] - du[0][1]) ** 2
+            else:
+                om2 = (du[2][1] - du[1][2]) ** 2 + (du[0][2] - du[2][0]) ** 2 + (du[1][0] - du[0][1]) ** 2
+            want = (0.5 - 0.5 * math.tanh(2.5 + 250.0 * div)) * div * div / (eps + div * div + om2)
             got = float(g.subs({**{sym[k_]: vals[k_] for k_ in sym}, D: Dv}))
             if abs(got - want) > 1e-12 * max(abs(want), 1e-300):
                 raise NotImplementedError("adaptive TENO: sensor formula not recognised")

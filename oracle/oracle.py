@@ -37,6 +37,10 @@ class Cfg(ctypes.Structure):
         ("dt", ctypes.c_double),
         ("filter", ctypes.c_int),
         ("filter_control", ctypes.c_double),
+        ("teno_adaptive", ctypes.c_int),
+        ("teno_a1", ctypes.c_double),
+        ("teno_a2", ctypes.c_double),
+        ("sensor_eps", ctypes.c_double),
     ]
 
 
@@ -62,13 +66,15 @@ def lib():
     global _lib
     if _lib is None:
         _lib = ctypes.CDLL(build())
-        for name in ("osbo_tgv_init", "osbo_run", "osbo_residual", "osbo2d_run", "osbo2d_metrics", "osbo2d_cutoff"):
+        for name in ("osbo_tgv_init", "osbo_run", "osbo_residual", "osbo_cutoff", "osbo2d_run", "osbo2d_metrics",
+                     "osbo2d_cutoff"):
             getattr(_lib, name).restype = ctypes.c_int
     return _lib
 
 
 def make_cfg(n, delta, gama=1.4, Minf=0.1, Re=1600.0, Pr=0.71, conv="central_skew", visc="const", rk="rk3",
-             bc="periodic", dt=5e-3, teno_ct=1e-5, teno_eps=1e-15, filter="none", filter_control=1.0):
+             bc="periodic", dt=5e-3, teno_ct=1e-5, teno_eps=1e-15, filter="none", filter_control=1.0,
+             teno_adaptive=False, teno_a1=10.5, teno_a2=4.5, sensor_eps=1e-12):
     c = Cfg()
     c.ndim = len(n) if len(n) == 2 else 3
     nn = list(n) + [1] * (3 - len(n))
@@ -83,6 +89,8 @@ def make_cfg(n, delta, gama=1.4, Minf=0.1, Re=1600.0, Pr=0.71, conv="central_ske
             c.bc[d][s] = BC[bc if isinstance(bc, str) else bc[d][s]]
     c.teno_ct, c.teno_eps, c.dt = teno_ct, teno_eps, dt
     c.filter, c.filter_control = FILTER[filter], filter_control
+    c.teno_adaptive = 1 if teno_adaptive else 0
+    c.teno_a1, c.teno_a2, c.sensor_eps = teno_a1, teno_a2, sensor_eps
     return c
 
 
@@ -114,6 +122,15 @@ def residual(c, q0):
     r = np.zeros_like(q)
     assert lib().osbo_residual(ctypes.byref(c), _ptr(q), _ptr(r)) == 0
     return r
+
+
+def cutoff(c, q0):
+    """Adaptive TENO cut-off C_T of the interior state q0 [5][n2][n1][n0] on a 3D block, laid out
+    [n2][n1][n0] (the reference's TENO_B0 field; osb_oracle.c ducros_sensor / teno_cutoff3)."""
+    q = np.ascontiguousarray(q0, dtype=np.float64)
+    ct = np.zeros(q.shape[1:], dtype=np.float64)
+    assert lib().osbo_cutoff(ctypes.byref(c), _ptr(q), _ptr(ct)) == 0
+    return ct
 
 
 class Cfg2D(ctypes.Structure):

@@ -30,6 +30,7 @@ typedef struct {
   double *u[3], *p, *T, *a; /* constituent relations */
   double *wk[6];    /* scratch for nested derivatives */
   double *flux[5];  /* interface fluxes (WENO/TENO) */
+  double *theta;    /* modified Ducros sensor (adaptive TENO), interior; 0 in the halos */
 } st_t;
 
 static inline size_t IX(const st_t *s, int i, int j, int k) {
@@ -59,6 +60,7 @@ static int st_init(st_t *s, const osbo_cfg *cfg) {
   s->T = alloc_pad(s);
   s->a = alloc_pad(s);
   for (int w = 0; w < 6; ++w) s->wk[w] = alloc_pad(s);
+  s->theta = alloc_pad(s);
   return 0;
 }
 
@@ -74,6 +76,7 @@ static void st_free(st_t *s) {
   free(s->T);
   free(s->a);
   for (int w = 0; w < 6; ++w) free(s->wk[w]);
+  free(s->theta);
 }
 
 #define N0 (s->c.n[0])
@@ -485,9 +488,35 @@ static void eigensystem(int dir, double rho, double u0, double u1, double u2, do
   R[4][4] = al * ((phi + a2) / (g - 1) - th * a);
 }
 
+/* Modified Ducros sensor on the interior (shock_sensors.py:12-49, the "ConstituentRelations CD" and
+ * "ConstituentRelations evaluation" kernels): 4th-order central first derivatives of u_i,
+ *   theta = (1/2 - 1/2 tanh(250 div + 2.5)) div^2 / (eps + |curl u|^2 + div^2);
+ * the halos keep 0, so the TENO interfaces whose left point is a halo point take C_T = 10^-floor(a1). */
+static void ducros_sensor(st_t *s) {
+  FOR3(0, N0, 0, N1, 0, N2) {
+    const size_t n = IX(s, i, j, k);
+    double du[3][3];
+    for (int c = 0; c < 3; ++c)
+      for (int d = 0; d < 3; ++d) du[c][d] = d1(s, s->u[c], n, d);
+    const double div = du[0][0] + du[1][1] + du[2][2];
+    const double w0 = du[2][1] - du[1][2], w1 = du[0][2] - du[2][0], w2 = du[1][0] - du[0][1];
+    s->theta[n] = (0.5 - 0.5 * tanh(250.0 * div + 2.5)) * (div * div) /
+                  (s->c.sensor_eps + w0 * w0 + w1 * w1 + w2 * w2 + div * div);
+  }
+}
+
+/* TENO cut-off at the interface whose left point is n: fixed, or adapted (teno.py:430-443):
+ * C_T = 10^-floor(a1 - a2 (1 - (1 - theta)^4 (4 theta + 1))) */
+static double teno_cutoff3(const st_t *s, size_t n) {
+  if (!s->c.teno_adaptive) return s->c.teno_ct;
+  const double th = s->theta[n];
+  return pow(10.0, -floor(s->c.teno_a1 - s->c.teno_a2 * (-pow(1 - th, 4) * (4 * th + 1) + 1)));
+}
+
 static void residual_weno(st_t *s) {
   const double g = s->c.gama;
   int n[3] = {N0, N1, N2};
+  if (s->c.teno_adaptive) ducros_sensor(s);
   for (int v = 0; v < 5; ++v)
     FOR3(0, N0, 0, N1, 0, N2) s->res[v][IX(s, i, j, k)] = 0.0;
   for (int dir = 0; dir < 3; ++dir) {
@@ -542,10 +571,10 @@ static void residual_weno(st_t *s) {
             gp[t] = CF[r][t] + lam[r] * CS[r][t];
             gm[t] = CF[r][t] - lam[r] * CS[r][t];
           }
-          rec[r] = teno6_side(gp, 1, s->c.teno_eps, s->c.teno_ct) + teno6_side(gm, 0, s->c.teno_eps, s->c.teno_ct);
+          rec[r] = teno6_side(gp, 1, s->c.teno_eps, teno_cutoff3(s, c)) + teno6_side(gm, 0, s->c.teno_eps, teno_cutoff3(s, c));
         } else if (s->c.conv == OSBO_CONV_TENO5) {
           const double fmr[5] = {fm[4], fm[3], fm[2], fm[1], fm[0]};  /* points i+3 .. i-1 */
-          rec[r] = teno5_side(fp, s->c.teno_eps, s->c.teno_ct) + teno5_side(fmr, s->c.teno_eps, s->c.teno_ct);
+          rec[r] = teno5_side(fp, s->c.teno_eps, teno_cutoff3(s, c)) + teno5_side(fmr, s->c.teno_eps, teno_cutoff3(s, c));
         } else {
           rec[r] = weno5_plus(fp, s->c.conv == OSBO_CONV_WENO5Z) + weno5_minus(fm, s->c.conv == OSBO_CONV_WENO5Z);
         }
@@ -728,6 +757,20 @@ int osbo_residual(const osbo_cfg *cfg, const double *q, double *r) {
   residual(&s);
   store_interior(&s, r, s.res);
   st_free(&s);
+  return 0;
+}
+
+int osbo_cutoff(const osbo_cfg *cfg, const double *q, double *ct) {
+  if (!cfg->teno_adaptive) return -1;
+  st_t st, *s = &st;
+  if (st_init(s, cfg)) return -1;
+  load_interior(s, q);
+  apply_bcs(s);
+  constituent(s);
+  ducros_sensor(s);
+  size_t m = 0;
+  FOR3(0, N0, 0, N1, 0, N2) ct[m++] = teno_cutoff3(s, IX(s, i, j, k));
+  st_free(s);
   return 0;
 }
 

@@ -32,6 +32,10 @@ typedef struct {
   double dt;
   int filter;             /* OSBO_FILTER_* */
   double filter_control;  /* shock_filter_control (1 in the reference) */
+  /* TENO cut-off adapted by the modified Ducros sensor (teno.py:430-443, shock_sensors.py:12-49):
+   * teno_adaptive = 1 with the constants a1, a2 and the sensor's epsilon; 0 keeps teno_ct */
+  int teno_adaptive;
+  double teno_a1, teno_a2, sensor_eps;
 } osbo_cfg;
 
 /* Taylor-Green initial condition (apps/taylor_green_vortex/taylor_green_vortex.py:87-101) on the
@@ -45,6 +49,9 @@ int osbo_run(const osbo_cfg *cfg, double *q, int nsteps, double *ke);
 /* One residual evaluation R(q) on the interior (the right-hand side of one RK stage), for
  * kernel-level parity tests.  r has the same layout as q. */
 int osbo_residual(const osbo_cfg *cfg, const double *q, double *r);
+/* adaptive TENO plans: the cut-off C_T at every interior point of the state q (after the boundary
+ * conditions), laid out like one variable of q (the reference's TENO_B0 field) */
+int osbo_cutoff(const osbo_cfg *cfg, const double *q, double *ct);
 
 /* ---- 2D curvilinear shock/boundary-layer path (TENO5, metrics, Sutherland, walls, LS-RK3) ---- */
 typedef struct {

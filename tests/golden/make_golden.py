@@ -40,6 +40,8 @@ CASES = {
     "tgsym_central": (17, 10, {"dt": 5e-3}),
     # central skew-symmetric scheme with the WENO5 non-linear filter (constant sensor) after every step
     "tgv_filter": (16, 10, {"dt": 3e-3, "Minf": 1.25}),
+    # TENO5 with the cut-off adapted by the modified Ducros sensor
+    "tgv_teno_adaptive": (16, 10, {"dt": 2e-3, "Minf": 1.25}),
 }
 
 

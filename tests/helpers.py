@@ -33,7 +33,9 @@ def oracle_cfg(plan, dt=None):
     bc = [[plan.bc[d][s] for s in range(2)] for d in range(3)]
     return O.make_cfg(plan.n, plan.delta, gama=plan.gama, Minf=plan.Minf, Re=plan.Re, Pr=plan.Pr, conv=plan.conv,
                       visc=plan.visc, rk="rk3", bc=bc, dt=dt if dt is not None else (plan.dt or 1e-3),
-                      filter=plan.filter, filter_control=plan.filter_control)
+                      filter=plan.filter, filter_control=plan.filter_control, teno_ct=plan.teno_ct,
+                      teno_eps=plan.teno_eps, teno_adaptive=plan.teno_adaptive, teno_a1=plan.teno_a1,
+                      teno_a2=plan.teno_a2, sensor_eps=plan.sensor_eps)
 
 
 def rel_err(a, b):

@@ -48,9 +48,14 @@ def test_query_layout_fp64_and_mixed():
     assert (lay.offset * 4) % 16 == 0 and (lay.stride_y * 4) % 16 == 0
 
 
+def test_query_layout_accepts_adaptive_teno_on_3d():
+    for conv in ("teno5", "teno6"):
+        assert layout(tgv_plan(64).replace(conv=conv, teno_adaptive=True))[0] == 0
+
+
 @pytest.mark.parametrize("change,code", [
     (dict(n=(4, 64, 64)), -1),                    # too small
-    (dict(conv="teno5", teno_adaptive=True), -2),  # adaptive TENO on a 3D block
+    (dict(conv="weno5js", teno_adaptive=True), -1),  # adaptive cut-off without TENO fluxes
     (dict(visc="sutherland"), -2),
     (dict(rk="ls_rk3"), -2),
     (dict(bc=(("periodic", "symmetry"),) + (("periodic", "periodic"),) * 2), -1),

@@ -161,8 +161,10 @@ def test_gpu_nancheck_flags_nonfinite_state():
 
 
 def test_gpu_plan_errors_surface_as_exceptions():
-    with pytest.raises(NotImplementedError):  # the Ducros sensor is evaluated on 2D blocks only
-        Solver(tgv_plan(32).replace(conv="teno5", teno_adaptive=True))
+    with pytest.raises(OSBError):  # the adaptive cut-off needs TENO fluxes
+        Solver(tgv_plan(32).replace(conv="weno5js", teno_adaptive=True))
+    with pytest.raises(NotImplementedError):  # Sutherland viscosity is implemented on 2D blocks
+        Solver(tgv_plan(32).replace(visc="sutherland"))
     s = Solver(tgv_plan(16))
     with pytest.raises(OSBError):
         s.step(1, -1.0)

@@ -13,7 +13,8 @@ from oracle import oracle as O
 from oracle import refrun
 from helpers import load_golden, golden_plan, oracle_cfg, rel_err, rel_err_mom, WENOZ_TOL
 
-CASES = ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central", "tgv_filter"]
+CASES = ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central", "tgv_filter",
+         "tgv_teno_adaptive"]
 
 
 @pytest.mark.parametrize("case", CASES)
@@ -55,6 +56,7 @@ def test_oracle_periodic_mass_conservation():
     ("tgv_teno", 12, 4, {"dt": 3e-3, "Minf": 1.25}),
     ("tgv_teno6", 12, 4, {"dt": 3e-3, "Minf": 1.25}),
     ("tgv_filter", 12, 6, {"dt": 3e-3, "Minf": 1.25}),
+    ("tgv_teno_adaptive", 12, 4, {"dt": 3e-3, "Minf": 1.25}),
 ])
 def test_oracle_matches_reference_run(case, n, steps, extra):
     if not refrun.available(case):

@@ -70,13 +70,24 @@ def test_published_katzer_script_lowers_to_adaptive_teno():
     assert "ConstituentRelations evaluation" in g.kernels
 
 
+def test_3d_sensor_kernels_lower_to_adaptive_teno():
+    """On 3D blocks the sensor's velocity derivatives are separate kernels ("ConstituentRelations CD
+    u_i x_j") writing work arrays that the sensor kernel reads; the writer follows them to the
+    adaptive cut-off, and the same TENO5 case without the sensor lowers to the fixed one."""
+    g = golden_plan("tgv_teno_adaptive")
+    assert g.teno_adaptive and g.conv == "teno5" and g.sensor_eps == 1e-12
+    assert (g.teno_a1, g.teno_a2) == (10.5, 4.5)
+    assert sum(k.startswith("ConstituentRelations CD u") for k in g.kernels) == 9
+    assert not golden_plan("tgv_teno").teno_adaptive
+
+
 def test_writer_refuses_kernels_outside_the_lowered_families():
     """Extra equation classes add kernels to the time loop; lowering without them would change the
     solution, so the writer refuses every kernel it does not lower.  The WENO filter with the constant
     dissipation sensor is lowered; its Ducros variant adds a shock-sensor kernel and is refused."""
     from opensbli_gb300.writer import GB300Writer
     for case in ("tgv_central", "tgv_weno", "tgsym_central", "katzer_teno", "katzer_adaptive", "katzer_carpenter",
-                 "tgv_filter"):
+                 "tgv_filter", "tgv_teno_adaptive"):
         GB300Writer._check_kernel_families(golden_plan(case).kernels)
     assert "User kernel: Non-linear filter application" in golden_plan("tgv_filter").kernels
     names = golden_plan("tgv_filter").kernels + ["User kernel: Shock sensor"]
@@ -103,7 +114,7 @@ def test_cfl_dt_tgv_weno():
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
 @pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central",
                                   "katzer_teno", "katzer_adaptive", "katzer_carpenter", "tgv_filter",
-                                  "katzer_weno", "katzer_wenoz", "katzer_teno6"])
+                                  "katzer_weno", "katzer_wenoz", "katzer_teno6", "tgv_teno_adaptive"])
 def test_writer_lowers_reference_script(case, tmp_path):
     r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case, "--out",
                         str(tmp_path), "--ref", REF], capture_output=True, text=True, timeout=900)
