@@ -67,8 +67,10 @@ def test_adaptive_cutoff_field_matches_oracle(precision):
     if precision == "fp64":
         assert np.array_equal(ct, ct_or), int((ct != ct_or).sum())
     else:
-        # FP32 sensor: a point whose exponent lies within rounding of an integer may take the next level
-        assert set(np.unique(ct)) <= set(np.unique(ct_or)) and (ct != ct_or).mean() < 1e-2
+        # the cut-off is held in the state precision (10^-k rounded to FP32), and the FP32 sensor may
+        # move a point whose exponent lies within rounding of an integer to the next level
+        ct_or32 = ct_or.astype(np.float32).astype(np.float64)
+        assert set(np.unique(ct)) <= set(np.unique(ct_or32)) and (ct != ct_or32).mean() < 1e-2
 
 
 @pytest.mark.parametrize("conv", ["teno5", "teno6"])
