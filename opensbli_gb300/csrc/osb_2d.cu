@@ -8,7 +8,8 @@
 //              also the FP32 working state
 //   k2_sensor_ct (adaptive TENO only): modified Ducros sensor theta and the cut-off C_T per point
 //   k2_flux<T, D, SCHEME> for D = x0, x1: interface fluxes + flux difference into R
-//   k2_visc_rk viscous/heat-flux terms + LS-RK3: du = A du + dt R, q += B du (FP64)
+//   k2_visc    viscous/heat-flux terms (shared-memory tiles), concurrent with the two flux kernels
+//   k2_rk      R = x fluxes + x1 fluxes + viscous terms; LS-RK3: du = A du + dt R, q += B du (FP64)
 //   k2_bc_x, k2_bc_y  the four face conditions on the FP64 master (inlet and outlet, then wall and
 //              top: the generated order where it matters)
 // A step starts with the face conditions and, mixed, ends with k2_to_state (the bound FP32 arrays
@@ -593,7 +594,7 @@ template <> struct T2Tile<0> { static constexpr int TI = 64, TA = 4; };
 template <> struct T2Tile<1> { static constexpr int TI = 24, TA = 16; };  // static smem < 48 KB in FP64
 
 // Interface fluxes along D for a tile and the flux difference -(F_i - F_{i-1})/delta (times D11 for
-// x1), written (D = 0) or accumulated (D = 1) into R.  TENO's cut-off is ct_d, or with ctp set the
+// x1), written into this direction's residual array.  TENO's cut-off is ct_d, or with ctp set the
 // per-point value at the interface's left point.
 template <typename T, int D, int SCH>
 __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<const T> pr, const double *D11,
@@ -702,9 +703,7 @@ __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<con
     for (int v = 0; v < 4; ++v) {
       T diff = sfl[v][m + 1][a] - sfl[v][m][a];
       if constexpr (sizeof(T) == 4) diff = sdf[v][m + 1][a] + diff;  // (F_i - F_{i-1}) + (G_i - G_{i-1})
-      const T d = -mul_hl(diff, sc_hi, sc_lo);
-      if (D == 0) res.v[v][gi] = d;
-      else res.v[v][gi] += d;
+      res.v[v][gi] = -mul_hl(diff, sc_hi, sc_lo);
     }
   }
 }
@@ -713,47 +712,75 @@ __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<con
 // viscous terms (stretched metric, closures) + LS-RK3 update
 // ---------------------------------------------------------------------------------------------
 struct Visc2Args {
-  double Re, kappa, inv_d0, inv_d1, dt, A, B;
+  double Re, kappa, inv_d0, inv_d1;
   int clx, cly;  // Carpenter faces of x0 and x1 (d1c)
 };
 
+template <typename T> struct Q3T {
+  T *v[3];
+};
+
+// Viscous terms of the momentum and energy equations at every interior point (the reference's
+// "Viscous" kernels: Newtonian stress and Fourier heat flux with Sutherland mu, d/dx1 = D11 d/dxi1 and
+// d2/dx1^2 = D11^2 d2/dxi1^2 + D11 SD111 d/dxi1, one-sided closures at the faces), into rv (momentum
+// 0, momentum 1, energy).  A 32 x 8 tile stages u0, u1, T and mu of its points and of the V2H points
+// around them in shared memory: the widest stencil, a one-sided closure or the nested x0/x1
+// derivative, reaches V2H = 5 points.  Points outside the padded arrays are neither staged nor read.
+constexpr int V2X = 32, V2Y = 8, V2H = 5;
 template <typename T>
-__global__ void __launch_bounds__(256) k2_visc_rk(Grid g, Prims<const T> pr, const double *D11, const double *SD111,
-                                                  Q4T<const T> res, Q4 du, Q4 q64, Visc2Args va, int update) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x, j = blockIdx.y * blockDim.y + threadIdx.y;
+__global__ void __launch_bounds__(V2X * V2Y, 2) k2_visc(Grid g, Prims<const T> pr, const double *D11,
+                                                        const double *SD111, Q3T<T> rv, Visc2Args va, int hx,
+                                                        int hy) {
+  constexpr int SX = V2X + 2 * V2H, SY = V2Y + 2 * V2H;
+  __shared__ T sm[4][SY][SX];  // u0, u1, T, mu
+  const int i0 = blockIdx.x * V2X, j0 = blockIdx.y * V2Y;
+  const int tid = threadIdx.y * V2X + threadIdx.x;
+  const T *src[4] = {pr.u0, pr.u1, pr.T_, pr.mu};
+  for (int t = tid; t < SX * SY; t += V2X * V2Y) {
+    const int li = t % SX, lj = t / SX;
+    const int gi = i0 - V2H + li, gj = j0 - V2H + lj;
+    if (gi < -hx || gi >= g.n0 + hx || gj < -hy || gj >= g.n1 + hy) continue;
+    const int64_t m = g2(g, gi, gj);
+#pragma unroll
+    for (int f = 0; f < 4; ++f) sm[f][lj][li] = src[f][m];
+  }
+  __syncthreads();
+  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
   if (i >= g.n0 || j >= g.n1) return;
+  const int li = threadIdx.x + V2H, lj = threadIdx.y + V2H;
   const int64_t c = g2(g, i, j);
   const T id0 = T(va.inv_d0), id1 = T(va.inv_d1), iRe = T(1.0 / va.Re);
-  const T Dm = T(D11[c]), S = T(SD111[c]), mu = pr.mu[c];
-  const T *uc[2] = {pr.u0, pr.u1};
-  auto X = [&](const T *f, int o) { return f[g2(g, i + o, j)]; };
-  auto Y = [&](const T *f, int o) { return f[g2(g, i, j + o)]; };
+  const T Dm = T(D11[c]), S = T(SD111[c]), mu = sm[3][lj][li];
   T gr[2][2], h[2][2][2];
 #pragma unroll
   for (int k = 0; k < 2; ++k) {
-    const T *f = uc[k];
-    gr[k][0] = id0 * d1c<T>([&](int o) { return X(f, o); }, i, g.n0, va.clx);
-    const T fy = id1 * d1c<T>([&](int o) { return Y(f, o); }, j, g.n1, va.cly);
+    auto X = [&](int o) { return sm[k][lj][li + o]; };
+    auto Y = [&](int o) { return sm[k][lj + o][li]; };
+    gr[k][0] = id0 * d1c<T>(X, i, g.n0, va.clx);
+    const T fy = id1 * d1c<T>(Y, j, g.n1, va.cly);
     gr[k][1] = Dm * fy;
-    h[k][0][0] = id0 * id0 * d2c<T>([&](int o) { return X(f, o); }, i, g.n0);
-    h[k][1][1] = Dm * Dm * (id1 * id1 * d2c<T>([&](int o) { return Y(f, o); }, j, g.n1)) + Dm * S * fy;
+    h[k][0][0] = id0 * id0 * d2c<T>(X, i, g.n0);
+    h[k][1][1] = Dm * Dm * (id1 * id1 * d2c<T>(Y, j, g.n1)) + Dm * S * fy;
     // d/dx0 of the row j+o, then d/dxi1 of that column (inner axis x0 over the extended x1 range)
     auto inner = [&](int o) {
-      return id0 * d1c<T>([&](int p) { return f[g2(g, i + p, j + o)]; }, i, g.n0, va.clx);
+      return id0 * d1c<T>([&](int p) { return sm[k][lj + o][li + p]; }, i, g.n0, va.clx);
     };
     h[k][0][1] = h[k][1][0] = Dm * (id1 * d1c<T>(inner, j, g.n1, va.cly));
   }
-  const T mux = id0 * d1c<T>([&](int o) { return X(pr.mu, o); }, i, g.n0, va.clx);
-  const T muy = Dm * id1 * d1c<T>([&](int o) { return Y(pr.mu, o); }, j, g.n1, va.cly);
-  const T Tx = id0 * d1c<T>([&](int o) { return X(pr.T_, o); }, i, g.n0, va.clx);
-  const T Tyx = id1 * d1c<T>([&](int o) { return Y(pr.T_, o); }, j, g.n1, va.cly);
+  auto XT = [&](int o) { return sm[2][lj][li + o]; };
+  auto YT = [&](int o) { return sm[2][lj + o][li]; };
+  auto Xmu = [&](int o) { return sm[3][lj][li + o]; };
+  auto Ymu = [&](int o) { return sm[3][lj + o][li]; };
+  const T mux = id0 * d1c<T>(Xmu, i, g.n0, va.clx);
+  const T muy = Dm * id1 * d1c<T>(Ymu, j, g.n1, va.cly);
+  const T Tx = id0 * d1c<T>(XT, i, g.n0, va.clx);
+  const T Tyx = id1 * d1c<T>(YT, j, g.n1, va.cly);
   const T Ty = Dm * Tyx;
-  const T Txx = id0 * id0 * d2c<T>([&](int o) { return X(pr.T_, o); }, i, g.n0);
-  const T Tyy = Dm * Dm * (id1 * id1 * d2c<T>([&](int o) { return Y(pr.T_, o); }, j, g.n1)) + Dm * S * Tyx;
+  const T Txx = id0 * id0 * d2c<T>(XT, i, g.n0);
+  const T Tyy = Dm * Dm * (id1 * id1 * d2c<T>(YT, j, g.n1)) + Dm * S * Tyx;
   const T div = gr[0][0] + gr[1][1];
   const T mug[2] = {mux, muy};
-  const T uu[2] = {pr.u0[c], pr.u1[c]};
-  T R[4] = {res.v[0][c], res.v[1][c], res.v[2][c], res.v[3][c]};
+  const T uu[2] = {sm[0][lj][li], sm[1][lj][li]};
   T e = T(va.kappa) * (mu * (Txx + Tyy) + mux * Tx + muy * Ty);
 #pragma unroll
   for (int a = 0; a < 2; ++a) {
@@ -763,22 +790,40 @@ __global__ void __launch_bounds__(256) k2_visc_rk(Grid g, Prims<const T> pr, con
     const T lap = h[a][0][0] + h[a][1][1];
     const T ddiv = h[0][a][0] + h[1][a][1];
     v += mu * iRe * (lap + ddiv * T(1.0 / 3.0));
-    R[1 + a] += v;
+    rv.v[a][c] = v;
     e += uu[a] * v;
 #pragma unroll
     for (int b = 0; b < 2; ++b) e += mu * iRe * (gr[a][b] + gr[b][a] - (a == b ? T(2.0 / 3.0) * div : T(0))) * gr[a][b];
   }
-  R[3] += e;
-  if (update) {
+  rv.v[2][c] = e;
+}
+
+// R = (x fluxes + x1 fluxes) + viscous terms at every interior point, then the LS-RK3 update
+// du = dt R + A du, q += B du in FP64 (update = 1), or R itself into du (update = 0: osb_residual).
+template <typename T>
+__global__ void k2_rk(Grid g, Q4T<const T> rx, Q4T<const T> ry, Q3T<const T> rv, Q4 du, Q4 q64, double dt, double A,
+                      double B, int update) {
+  const int64_t N = (int64_t)g.n0 * g.n1;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.n0), j = (int)(t / g.n0);
+    const int64_t c = g2(g, i, j);
+    T R[4];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) {
-      const double d = va.dt * to_f64(R[v]) + va.A * du.v[v][c];
-      du.v[v][c] = d;
-      q64.v[v][c] = va.B * d + q64.v[v][c];
+    for (int v = 0; v < 4; ++v) R[v] = rx.v[v][c] + ry.v[v][c];
+    R[1] += rv.v[0][c];
+    R[2] += rv.v[1][c];
+    R[3] += rv.v[2][c];
+    if (update) {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const double d = dt * to_f64(R[v]) + A * du.v[v][c];
+        du.v[v][c] = d;
+        q64.v[v][c] = B * d + q64.v[v][c];
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < 4; ++v) du.v[v][c] = to_f64(R[v]);
     }
-  } else {
-#pragma unroll
-    for (int v = 0; v < 4; ++v) du.v[v][c] = to_f64(R[v]);  // residual output mode: du holds R
   }
 }
 
@@ -927,6 +972,12 @@ template <typename T> void launch2_rhs(const Ctx &c, int update, double A, doubl
     ctp = static_cast<const T *>(c.ct2);
     ++*launches;
   }
+  // the x fluxes (this stream), the x1 fluxes and the viscous terms (side streams) read only the
+  // primitives and the state and write separate arrays, so they run concurrently: each alone leaves
+  // most of the GPU idle on a block of this size
+  cudaEventRecord(c.ev_fork2, s);
+  cudaStreamWaitEvent(c.side2[0], c.ev_fork2, 0);
+  cudaStreamWaitEvent(c.side2[1], c.ev_fork2, 0);
   {
     using Tl = T2Tile<0>;
     dim3 gx((c.g.n0 + Tl::TI - 2) / (Tl::TI - 1), (c.g.n1 + Tl::TA - 1) / Tl::TA);
@@ -935,21 +986,28 @@ template <typename T> void launch2_rhs(const Ctx &c, int update, double A, doubl
   {
     using Tl = T2Tile<1>;
     dim3 gy((c.g.n0 + Tl::TA - 1) / Tl::TA, (c.g.n1 + Tl::TI - 2) / (Tl::TI - 1));
-    launch2_flux<T, 1>(c, gy, q, prc, r, eps, ctp, s);
+    launch2_flux<T, 1>(c, gy, q, prc, q4t<T>(c.resy), eps, ctp, c.side2[0]);
   }
   Visc2Args va;
   va.Re = p.Re;
   va.kappa = 1.0 / ((p.gama - 1) * p.Minf * p.Minf * p.Pr * p.Re);
   va.inv_d0 = 1.0 / p.delta[0];
   va.inv_d1 = 1.0 / p.delta[1];
-  va.dt = dt;
-  va.A = A;
-  va.B = B;
   va.clx = closure_bits(p, 0);
   va.cly = closure_bits(p, 1);
-  dim3 gv((c.g.n0 + 31) / 32, (c.g.n1 + 7) / 8);
-  k2_visc_rk<T><<<gv, b, 0, s>>>(c.g, prc, c.d11, c.sd111, q4t<const T>(c.res), q4(c.du2), q4(c.q64_2d), va, update);
-  *launches += 4;
+  Q3T<T> rv{{static_cast<T *>(c.resv[0]), static_cast<T *>(c.resv[1]), static_cast<T *>(c.resv[2])}};
+  dim3 gv((c.g.n0 + V2X - 1) / V2X, (c.g.n1 + V2Y - 1) / V2Y);
+  k2_visc<T><<<gv, dim3(V2X, V2Y), 0, c.side2[1]>>>(c.g, prc, c.d11, c.sd111, rv, va, c.hx2, c.hy2);
+  cudaEventRecord(c.ev_join2[0], c.side2[0]);
+  cudaEventRecord(c.ev_join2[1], c.side2[1]);
+  cudaStreamWaitEvent(s, c.ev_join2[0], 0);
+  cudaStreamWaitEvent(s, c.ev_join2[1], 0);
+  Q3T<const T> rvc{{rv.v[0], rv.v[1], rv.v[2]}};
+  int nb = (int)(((int64_t)c.g.n0 * c.g.n1 + 255) / 256);
+  if (nb > c.num_sms * 4) nb = c.num_sms * 4;
+  k2_rk<T><<<nb, 256, 0, s>>>(c.g, q4t<const T>(c.res), q4t<const T>(c.resy), rvc, q4(c.du2), q4(c.q64_2d), dt, A, B,
+                              update);
+  *launches += 5;
 }
 
 // The adaptive TENO cut-off of the current working state over the interior, as FP64 [n1][n0]

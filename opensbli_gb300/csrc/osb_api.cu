@@ -721,6 +721,19 @@ int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
       e = cudaMalloc(&c->ct2, bytes);
       if (e == cudaSuccess) e = cudaMemset(c->ct2, 0, bytes);
     }
+    for (int v = 0; v < 4 && e == cudaSuccess; ++v) {
+      e = cudaMalloc(&c->resy[v], bytes);
+      if (e == cudaSuccess) e = cudaMemset(c->resy[v], 0, bytes);
+    }
+    for (int v = 0; v < 3 && e == cudaSuccess; ++v) {
+      e = cudaMalloc(&c->resv[v], bytes);
+      if (e == cudaSuccess) e = cudaMemset(c->resv[v], 0, bytes);
+    }
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+      e = cudaStreamCreateWithFlags(&c->side2[k], cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join2[k], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork2, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaMalloc(&c->x1, b64);
     if (e == cudaSuccess) e = cudaMalloc(&c->d11, b64);
     if (e == cudaSuccess) e = cudaMalloc(&c->sd111, b64);
@@ -1258,6 +1271,13 @@ void osb_destroy(osb_ctx *c) {
     cudaFree(c->du2[v]);
   }
   for (int k = 0; k < 6; ++k) cudaFree(c->prim2[k]);
+  for (int v = 0; v < 4; ++v) cudaFree(c->resy[v]);
+  for (int v = 0; v < 3; ++v) cudaFree(c->resv[v]);
+  for (int k = 0; k < 2; ++k) {
+    if (c->side2[k]) cudaStreamDestroy(c->side2[k]);
+    if (c->ev_join2[k]) cudaEventDestroy(c->ev_join2[k]);
+  }
+  if (c->ev_fork2) cudaEventDestroy(c->ev_fork2);
   cudaFree(c->ct2);
   cudaFree(c->x1);
   cudaFree(c->d11);

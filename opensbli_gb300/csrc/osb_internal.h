@@ -56,6 +56,12 @@ struct Ctx {
   double *du2[4] = {};            // LS-RK register
   void *prim2[6] = {};            // u0, u1, p, a, T, mu (state precision, padded)
   void *ct2 = nullptr;            // adaptive TENO (2D and 3D): cut-off C_T per point (state precision, padded)
+  // the stage's three right-hand-side parts, formed concurrently: x fluxes into res, x1 fluxes into
+  // resy, viscous terms (momentum 0, 1, energy) into resv; two side streams and fork/join events
+  void *resy[4] = {};
+  void *resv[3] = {};
+  cudaStream_t side2[2] = {nullptr, nullptr};
+  cudaEvent_t ev_fork2 = nullptr, ev_join2[2] = {nullptr, nullptr};
   double *x1 = nullptr, *d11 = nullptr, *sd111 = nullptr;
   int metrics_valid = 0;
   std::string err;
