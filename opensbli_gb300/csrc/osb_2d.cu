@@ -10,8 +10,8 @@
 //   k2_flux<T, D, SCHEME> for D = x0, x1: interface fluxes + flux difference into R
 //   k2_visc    viscous/heat-flux terms (shared-memory tiles), concurrent with the two flux kernels
 //   k2_rk      R = x fluxes + x1 fluxes + viscous terms; LS-RK3: du = A du + dt R, q += B du (FP64)
-//   k2_bc_x, k2_bc_y  the four face conditions on the FP64 master (inlet and outlet, then wall and
-//              top: the generated order where it matters)
+//   k2_bc      the four face conditions on the FP64 master, one launch (inlet and outlet, then wall
+//              and top: the generated order where it matters)
 // A step starts with the face conditions and, mixed, ends with k2_to_state (the bound FP32 arrays
 // current).
 // Metrics (once, k2_metric_*): detJ = dx1/dxi1 with the closures, D11 = 1/detJ, halos mirrored about
@@ -137,19 +137,23 @@ struct Dir2 {
   double lo[4], hi[4];
 };
 
-// The four faces in two launches.  The inlet and outlet touch disjoint columns (0, -1..-3 and
-// n0-2..n0+hx), the wall and the top face disjoint rows (-3..0 and n1-1..n1+hy); the generated order
-// (inlet, outlet, wall, top) only matters between the pairs: the wall reads the x-halo columns the
-// inlet and outlet wrote, and at the corners the later face wins.  One thread per row (x faces) or
-// column (y faces); small blocks spread the FP64 divisions over many SMs.
+// The four faces in one launch.  The inlet and outlet touch the columns -3..0 and n0-2..n0+hx (the
+// outlet reads n0-2), the wall and the top face the rows -3..3 and n1-1..n1+hy (the wall reads rows
+// 0..3); the generated order (inlet, outlet, wall, top) only matters where these meet: the wall reads
+// the x-halo columns the inlet and outlet wrote, the outlet must read column n0-2 before the wall
+// writes it, and at the corners the later face wins.  So block 0 applies the x faces of the rows
+// -3..3 and n1-1..n1+hy, then (after a barrier) the y faces of the columns -3..0 and n0-2..n0+hx;
+// the other blocks apply the x faces of the rows between and the y faces of the columns between,
+// which no other work item touches.  Each y-face column is three work items, one per wall halo
+// point, so the FP64 divisions of a column run in parallel.
 struct BC2Args {
   double gama, Minf, Twall, delta0, xs;
   int hx, hy;
   Dir2 st;
 };
-__global__ void __launch_bounds__(64) k2_bc_x(Grid g, Q4 q, BC2Args a) {
-  const int j = blockIdx.x * blockDim.x + threadIdx.x - 3;
-  if (j >= g.n1 + a.hy) return;
+
+// inlet (i = 0 and its halo) and outlet (i >= n0-1) of row j
+__device__ __forceinline__ void bc2_row(const Grid &g, const Q4 &q, const BC2Args &a, int j) {
   {  // inlet
     const int64_t b = g2(g, 0, j), m1 = g2(g, -1, j);
     const double rhob = q.v[0][b];
@@ -169,35 +173,56 @@ __global__ void __launch_bounds__(64) k2_bc_x(Grid g, Q4 q, BC2Args a) {
   }
 }
 
-__global__ void __launch_bounds__(64) k2_bc_y(Grid g, Q4 q, BC2Args a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x - 3;
-  if (i >= g.n0 + a.hx) return;
+// isothermal wall halo point -t of column i (t = 1 also sets the wall point itself and the
+// Dirichlet top face of the column)
+__device__ __forceinline__ void bc2_col(const Grid &g, const Q4 &q, const BC2Args &a, int i, int t) {
   const double M2 = a.Minf * a.Minf, gama = a.gama;
-  {  // isothermal wall
-    const int64_t w = g2(g, i, 0), a1 = g2(g, i, 1);
+  const int64_t w = g2(g, i, 0), a1 = g2(g, i, 1);
+  // the wall point after this face: zero momentum, energy from Twall; its pressure
+  // (gama-1) (rhoE - |rhou|^2 / (2 rho)) is exactly (gama-1) rhoE there
+  const double rw = q.v[0][w], ew = a.Twall * (1.0 / M2) * rw / (gama * (gama - 1.0));
+  const double Pw = (gama - 1) * ew;
+  const double Ta = M2 * gama * (gama - 1) *
+                    (-(0.5 * q.v[1][a1] * q.v[1][a1] + 0.5 * q.v[2][a1] * q.v[2][a1]) / q.v[0][a1] + q.v[3][a1]) /
+                    q.v[0][a1];
+  const int64_t m = g2(g, i, t), hh = g2(g, i, -t);
+  const double um0 = q.v[1][m] / q.v[0][m], um1 = q.v[2][m] / q.v[0][m];
+  const double Tt = (t + 1) * a.Twall - t * Ta;
+  const double rh = M2 * gama * Pw / Tt;
+  q.v[0][hh] = rh;
+  q.v[1][hh] = -rh * um0;
+  q.v[2][hh] = -rh * um1;
+  q.v[3][hh] = (1.0 / (gama - 1)) * Pw + 0.5 * rh * (um0 * um0 + um1 * um1);
+  if (t == 1) {
     q.v[1][w] = 0.0;
     q.v[2][w] = 0.0;
-    q.v[3][w] = a.Twall * (1.0 / M2) * q.v[0][w] / (gama * (gama - 1.0));
-    const double Pw = (gama - 1) * (-(0.5 * q.v[1][w] * q.v[1][w] + 0.5 * q.v[2][w] * q.v[2][w]) / q.v[0][w] + q.v[3][w]);
-    const double Ta = M2 * gama * (gama - 1) *
-                      (-(0.5 * q.v[1][a1] * q.v[1][a1] + 0.5 * q.v[2][a1] * q.v[2][a1]) / q.v[0][a1] + q.v[3][a1]) /
-                      q.v[0][a1];
-    for (int t = 1; t <= 3; ++t) {
-      const int64_t m = g2(g, i, t), hh = g2(g, i, -t);
-      const double um0 = q.v[1][m] / q.v[0][m], um1 = q.v[2][m] / q.v[0][m];
-      const double Tt = (t + 1) * a.Twall - t * Ta;
-      const double rh = M2 * gama * Pw / Tt;
-      q.v[0][hh] = rh;
-      q.v[1][hh] = -rh * um0;
-      q.v[2][hh] = -rh * um1;
-      q.v[3][hh] = (1.0 / (gama - 1)) * Pw + 0.5 * rh * (um0 * um0 + um1 * um1);
-    }
+    q.v[3][w] = ew;
+    const double x0 = a.delta0 * i;  // Dirichlet top face
+    for (int j = g.n1 - 1; j < g.n1 + a.hy; ++j)
+      for (int v = 0; v < 4; ++v) q.v[v][g2(g, i, j)] = x0 > a.xs ? a.st.hi[v] : a.st.lo[v];
   }
-  const double x0 = a.delta0 * i;  // Dirichlet top face
-  for (int j = g.n1 - 1; j < g.n1 + a.hy; ++j)
-    for (int v = 0; v < 4; ++v) q.v[v][g2(g, i, j)] = x0 > a.xs ? a.st.hi[v] : a.st.lo[v];
 }
 
+constexpr int BC2_THREADS = 128;
+__global__ void __launch_bounds__(BC2_THREADS) k2_bc(Grid g, Q4 q, BC2Args a, int row_blocks) {
+  const int tid = threadIdx.x;
+  if (blockIdx.x == 0) {
+    for (int j = -3 + tid; j < g.n1 + a.hy; j += BC2_THREADS)
+      if (j <= 3 || j >= g.n1 - 1) bc2_row(g, q, a, j);
+    __syncthreads();
+    for (int w = tid; w < 3 * (g.n0 + a.hx + 3); w += BC2_THREADS) {
+      const int i = w / 3 - 3;
+      if (i <= 0 || i >= g.n0 - 2) bc2_col(g, q, a, i, w % 3 + 1);
+    }
+  } else if ((int)blockIdx.x <= row_blocks) {
+    const int j = 4 + ((int)blockIdx.x - 1) * BC2_THREADS + tid;
+    if (j < g.n1 - 1) bc2_row(g, q, a, j);
+  } else {
+    const int w = ((int)blockIdx.x - 1 - row_blocks) * BC2_THREADS + tid;
+    const int i = 1 + w / 3;
+    if (i < g.n0 - 2) bc2_col(g, q, a, i, w % 3 + 1);
+  }
+}
 
 template <typename T> struct Q4T {
   T *v[4];
@@ -915,10 +940,11 @@ void launch2_bcs(const Ctx &c, cudaStream_t s, int64_t *launches) {
     a.st.lo[v] = p.dirichlet_state[0][v];
     a.st.hi[v] = p.dirichlet_state[1][v];
   }
-  const int ny = c.g.n1 + 3 + c.hy2, nx = c.g.n0 + 3 + c.hx2;
-  k2_bc_x<<<(ny + 63) / 64, 64, 0, s>>>(c.g, q4(c.q64_2d), a);
-  k2_bc_y<<<(nx + 63) / 64, 64, 0, s>>>(c.g, q4(c.q64_2d), a);
-  *launches += 2;
+  const int rows = c.g.n1 - 5 > 0 ? c.g.n1 - 5 : 0, cols = c.g.n0 - 3 > 0 ? c.g.n0 - 3 : 0;
+  const int row_blocks = (rows + BC2_THREADS - 1) / BC2_THREADS;
+  const int col_blocks = (3 * cols + BC2_THREADS - 1) / BC2_THREADS;
+  k2_bc<<<1 + row_blocks + col_blocks, BC2_THREADS, 0, s>>>(c.g, q4(c.q64_2d), a, row_blocks);
+  *launches += 1;
 }
 
 // Mixed: the FP32 working state from the FP64 master at every padded point (the right-hand side's
