@@ -599,6 +599,11 @@ void launch_batch_weno(const int4 *items, int nitems, int *counter, int parity, 
 static __constant__ double c_p10n3[23] = {1e0,   1e-1,  1e-2,  1e-3,  1e-4,  1e-5,  1e-6,  1e-7,
                                           1e-8,  1e-9,  1e-10, 1e-11, 1e-12, 1e-13, 1e-14, 1e-15,
                                           1e-16, 1e-17, 1e-18, 1e-19, 1e-20, 1e-21, 1e-22};
+// the same values rounded to FP32 (the FP32 state's cut-off)
+static __constant__ float c_p10n3f[23] = {
+    (float)1e0,   (float)1e-1,  (float)1e-2,  (float)1e-3,  (float)1e-4,  (float)1e-5,  (float)1e-6,  (float)1e-7,
+    (float)1e-8,  (float)1e-9,  (float)1e-10, (float)1e-11, (float)1e-12, (float)1e-13, (float)1e-14, (float)1e-15,
+    (float)1e-16, (float)1e-17, (float)1e-18, (float)1e-19, (float)1e-20, (float)1e-21, (float)1e-22};
 
 __device__ __forceinline__ float tanh_s(float x) { return tanhf(x); }
 __device__ __forceinline__ double tanh_s(double x) { return tanh(x); }
@@ -607,49 +612,94 @@ __device__ __forceinline__ double tanh_s(double x) { return tanh(x); }
 // form).  On the interior, with 4th-order central first derivatives of u_i = rhou_i / rho:
 //   theta = (1/2 - 1/2 tanh(250 div + 2.5)) div^2 / (eps + |curl u|^2 + div^2);
 // theta = 0 elsewhere (the sensor is evaluated on the interior only and the generated code never
-// fills its halos).  C_T = 10^-floor(a1 - a2 (1 - (1 - theta)^4 (1 + 4 theta))), the exponent
-// formed in FP64 in both precisions and the power taken from a table of correctly rounded 10^-k.
+// fills its halos).  C_T = 10^-floor(a1 - a2 (1 - (1 - theta)^4 (1 + 4 theta))), the exponent formed
+// in the state precision (FP64 arithmetic costs as much as the rest of this kernel on this GPU, and an
+// FP32 theta carries no more than FP32 accuracy into it) and the power taken from a table of
+// correctly rounded 10^-k.
+//
+// A block covers an x-y tile of SX x SY points and marches along z over SK planes.  u_i is formed once
+// per point (one division) into a ring of five planes of the tile and its two-point x-y margin in
+// shared memory; every derivative reads the ring.  Margin points outside [-2, n_d + 2) are never
+// read by an interior stencil and are not loaded.
+template <typename T> struct SensorTile {
+  static constexpr int SX = 32, SY = sizeof(T) == 4 ? 8 : 4, SK = 16;
+  static constexpr int PX = SX + 4, PY = SY + 4;  // plane of the ring: tile and margin
+};
+
 template <typename T>
-__global__ void k_sensor_ct3(Grid g, Fields5<const T> q, T *ct, double i0, double i1, double i2, double a1,
-                             double a2, double seps) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x - 1, j = blockIdx.y * blockDim.y + threadIdx.y - 1;
-  const int k = (int)blockIdx.z - 1;
-  if (i > g.n0 || j > g.n1) return;
-  const int64_t n = gidx(g, i, j, k);
-  double th = 0.0;
-  if (i >= 0 && i < g.n0 && j >= 0 && j < g.n1 && k >= 0 && k < g.n2) {
-    const int64_t st[3] = {1, g.sy, g.sz};
-    const T id[3] = {T(i0), T(i1), T(i2)};
-    T du[3][3];  // du[c][d] = d u_c / d x_d
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      T u[4][3];
-#pragma unroll
-      for (int t = 0; t < 4; ++t) {
-        const int o = t < 2 ? t - 2 : t - 1;  // -2, -1, +1, +2
-        const int64_t m = n + o * st[d];
+__global__ void __launch_bounds__(SensorTile<T>::SX * SensorTile<T>::SY)
+    k_sensor_ct3(Grid g, Fields5<const T> q, T *ct, double i0, double i1, double i2, double a1, double a2,
+                 double seps) {
+  using St = SensorTile<T>;
+  constexpr int SX = St::SX, SY = St::SY, SK = St::SK, PX = St::PX, PY = St::PY;
+  __shared__ T ring[5][3][PY][PX];
+  const int ti = threadIdx.x, tj = threadIdx.y, tid = tj * SX + ti;
+  const int ib = (int)blockIdx.x * SX - 1, jb = (int)blockIdx.y * SY - 1, kb = (int)blockIdx.z * SK - 1;
+  const int ke = min(kb + SK, g.n2 + 1);  // planes kb .. ke-1 of [-1, n2]
+  const T id[3] = {T(i0), T(i1), T(i2)};
+  // u of plane kk into ring slot (kk + 8) % 5 (kk >= -3)
+  auto load_plane = [&](int kk) {
+    const int slot = (kk + 8) % 5;
+    for (int t = tid; t < PX * PY; t += SX * SY) {
+      const int pi = t % PX, pj = t / PX;
+      const int ii = ib - 2 + pi, jj = jb - 2 + pj;
+      T u0 = T(0), u1 = T(0), u2 = T(0);
+      if (ii >= -2 && ii < g.n0 + 2 && jj >= -2 && jj < g.n1 + 2 && kk >= -2 && kk < g.n2 + 2) {
+        const int64_t m = gidx(g, ii, jj, kk);
         const T ir = T(1) / q.v[0][m];
-#pragma unroll
-        for (int c = 0; c < 3; ++c) u[t][c] = q.v[1 + c][m] * ir;
+        u0 = q.v[1][m] * ir;
+        u1 = q.v[2][m] * ir;
+        u2 = q.v[3][m] * ir;
       }
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-        du[c][d] = id[d] * ((u[0][c] - u[3][c]) * T(1.0 / 12.0) + (u[2][c] - u[1][c]) * T(2.0 / 3.0));
+      ring[slot][0][pj][pi] = u0;
+      ring[slot][1][pj][pi] = u1;
+      ring[slot][2][pj][pi] = u2;
     }
-    const T div = du[0][0] + du[1][1] + du[2][2];
-    const T w0 = du[2][1] - du[1][2], w1 = du[0][2] - du[2][0], w2 = du[1][0] - du[0][1];
-    const T sw = T(0.5) - T(0.5) * tanh_s(T(250) * div + T(2.5));
-    th = (double)(sw * (div * div) / (T(seps) + w0 * w0 + w1 * w1 + w2 * w2 + div * div));
+  };
+  for (int kk = kb - 2; kk < kb + 2; ++kk) load_plane(kk);
+  const int i = ib + ti, j = jb + tj;
+  for (int k = kb; k < ke; ++k) {
+    load_plane(k + 2);
+    __syncthreads();
+    if (i <= g.n0 && j <= g.n1) {
+      T th = T(0);
+      if (i >= 0 && i < g.n0 && j >= 0 && j < g.n1 && k >= 0 && k < g.n2) {
+        const int pi = ti + 2, pj = tj + 2, sc = (k + 8) % 5;
+        T du[3][3];  // du[c][d] = d u_c / d x_d
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          // values at offsets -2, -1, +1, +2 along each axis
+          const T x[4] = {ring[sc][c][pj][pi - 2], ring[sc][c][pj][pi - 1], ring[sc][c][pj][pi + 1],
+                          ring[sc][c][pj][pi + 2]};
+          const T y[4] = {ring[sc][c][pj - 2][pi], ring[sc][c][pj - 1][pi], ring[sc][c][pj + 1][pi],
+                          ring[sc][c][pj + 2][pi]};
+          const T z[4] = {ring[(k + 6) % 5][c][pj][pi], ring[(k + 7) % 5][c][pj][pi], ring[(k + 9) % 5][c][pj][pi],
+                          ring[(k + 10) % 5][c][pj][pi]};
+          du[c][0] = id[0] * ((x[0] - x[3]) * T(1.0 / 12.0) + (x[2] - x[1]) * T(2.0 / 3.0));
+          du[c][1] = id[1] * ((y[0] - y[3]) * T(1.0 / 12.0) + (y[2] - y[1]) * T(2.0 / 3.0));
+          du[c][2] = id[2] * ((z[0] - z[3]) * T(1.0 / 12.0) + (z[2] - z[1]) * T(2.0 / 3.0));
+        }
+        const T div = du[0][0] + du[1][1] + du[2][2];
+        const T w0 = du[2][1] - du[1][2], w1 = du[0][2] - du[2][0], w2 = du[1][0] - du[0][1];
+        const T sw = T(0.5) - T(0.5) * tanh_s(T(250) * div + T(2.5));
+        th = sw * (div * div) / (T(seps) + w0 * w0 + w1 * w1 + w2 * w2 + div * div);
+      }
+      const T w = T(1) - th;
+      const T e = floor(T(a1) - T(a2) * (T(1) - (w * w) * (w * w) * (T(4) * th + T(1))));
+      const int64_t n = gidx(g, i, j, k);
+      if (e >= T(0) && e <= T(22)) ct[n] = sizeof(T) == 4 ? T(c_p10n3f[(int)e]) : T(c_p10n3[(int)e]);
+      else ct[n] = T(pow(10.0, -(double)e));
+    }
+    __syncthreads();  // the next plane's load overwrites the slot of plane k - 2
   }
-  const double w = 1.0 - th;
-  const double e = floor(a1 - a2 * (1.0 - (w * w) * (w * w) * (4.0 * th + 1.0)));
-  ct[n] = T((e >= 0.0 && e <= 22.0) ? c_p10n3[(int)e] : pow(10.0, -e));
 }
 
 template <typename T>
 void launch_sensor_ct3(const Ctx &c, Fields5<const T> q, cudaStream_t s, int64_t *launches) {
+  using St = SensorTile<T>;
   const osb_plan_desc &p = c.plan;
-  dim3 b(32, 8), gs((c.g.n0 + 2 + 31) / 32, (c.g.n1 + 2 + 7) / 8, c.g.n2 + 2);
+  dim3 b(St::SX, St::SY);
+  dim3 gs((c.g.n0 + 2 + St::SX - 1) / St::SX, (c.g.n1 + 2 + St::SY - 1) / St::SY, (c.g.n2 + 2 + St::SK - 1) / St::SK);
   k_sensor_ct3<T><<<gs, b, 0, s>>>(c.g, q, static_cast<T *>(c.ct2), 1.0 / p.delta[0], 1.0 / p.delta[1],
                                    1.0 / p.delta[2], p.teno_a1, p.teno_a2, p.sensor_eps);
   ++*launches;
