@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-#define OSB_ABI_VERSION 5
+#define OSB_ABI_VERSION 6
 
 /* error codes */
 #define OSB_OK 0
@@ -84,12 +84,13 @@ typedef struct osb_plan_desc {
   double rk_a[3];    /* rk_sbli: rkold[]; rk_LS: A[] */
   double rk_b[3];    /* rk_sbli: rknew[]; rk_LS: B[] */
   int use_graphs;    /* capture one RK3 step as a CUDA graph */
-  /* 2D wall-bounded blocks (apps/katzer_SBLI/katzer_SBLI.py): isothermal wall temperature,
-   * Sutherland constants (mu = T^1.5 (1 + SuthT/RefT)/(T + SuthT/RefT)), and the Dirichlet face's
-   * two states: dirichlet_state[0] where x0 <= dirichlet_x_switch, [1] where x0 > it; rho, rhou0,
-   * rhou1, rhoE. */
+  /* wall-bounded blocks (2D: apps/katzer_SBLI/katzer_SBLI.py; 3D with a periodic x2:
+   * apps/transitional_SBLI/transitional_SBLI.py): isothermal wall temperature, Sutherland constants
+   * (mu = T^1.5 (1 + SuthT/RefT)/(T + SuthT/RefT)), and the Dirichlet face's two states:
+   * dirichlet_state[0] where x0 <= dirichlet_x_switch, [1] where x0 > it; the block's conserved
+   * variables in order (2D: rho, rhou0, rhou1, rhoE; 3D: rho, rhou0, rhou1, rhou2, rhoE). */
   double Twall, SuthT, RefT;
-  double dirichlet_state[2][4];
+  double dirichlet_state[2][5];
   double dirichlet_x_switch;
   /* TENO with the cut-off adapted per interface by the modified Ducros sensor (TENO5 on 2D blocks,
    * TENO5 or TENO6 on 3D blocks; schemes/spatial/teno.py:430-443, schemes/spatial/shock_sensors.py:

@@ -737,7 +737,7 @@ __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<con
 // viscous terms (stretched metric, closures) + LS-RK3 update
 // ---------------------------------------------------------------------------------------------
 struct Visc2Args {
-  double Re, kappa, inv_d0, inv_d1;
+  double Re, kappa, inv_d0, inv_d1, inv_d2;
   int clx, cly;  // Carpenter faces of x0 and x1 (d1c)
 };
 
@@ -1064,6 +1064,370 @@ template <typename T> void launch2_cutoff(const Ctx &c, double *out, cudaStream_
   k2_pack_ct<T><<<gi, b, 0, s>>>(c.g, static_cast<const T *>(c.ct2), out);
   *launches += 3;
 }
+
+// =============================================================================================
+// span-periodic 3D wall-bounded blocks: the configuration above with a periodic x2 axis
+// (apps/transitional_SBLI/transitional_SBLI.py without its body force, statistics and restart).
+// The FP64 master state is the context's RK register array (qold), the working state the bound
+// arrays (FP32 or FP64); the characteristic fluxes are the 3D flux kernels of osb_weno.cu, whose x1
+// sweep scales its flux difference by D11(j) (Phys::ysc_d / ysc_f).  Layout: the 3D one (halos 4,
+// 3, 3); the face conditions write the halo points the stencils read (the generated code also
+// writes row n1+3, which no stencil reads).
+// =============================================================================================
+struct Q5 {
+  double *v[5];
+};
+template <typename T> struct Q5T {
+  T *v[5];
+};
+
+// Metric terms of a block stretched in x1 (one block): D11(j) = 1/(dx1/dxi1) and SD111(j) =
+// dD11/dxi1 with the x1 closures (both read interior points only), and the x1 flux-difference scale
+// inv_delta1 D11(j) in FP64 and as an FP32 pair.
+__global__ void __launch_bounds__(256) k3w_metrics(int n1, const double *x1, double *D11, double *SD111, double *ysc_d,
+                                                   float2 *ysc_f, double inv_d1, int cly) {
+  for (int j = threadIdx.x; j < n1; j += blockDim.x) {
+    auto G = [&](int o) { return x1[j + o]; };
+    D11[j] = 1.0 / (inv_d1 * d1c<double>(G, j, n1, cly));
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < n1; j += blockDim.x) {
+    auto G = [&](int o) { return D11[j + o]; };
+    SD111[j] = inv_d1 * d1c<double>(G, j, n1, cly);
+    const double sc = inv_d1 * D11[j];
+    const float hi = (float)sc;
+    ysc_d[j] = sc;
+    ysc_f[j] = make_float2(hi, (float)(sc - (double)hi));
+  }
+}
+
+// The four faces of every interior x2 plane, one launch (blockIdx.y = plane), with the work split
+// of k2_bc: block 0 of a plane applies the x faces of the rows -3..3 and n1-1..n1+2, then the y faces
+// of the columns -3..0 and n0-2..n0+3; the other blocks the rows and columns between.
+struct BC3Args {
+  double gama, Minf, Twall, delta0, xs;
+  double lo[5], hi[5];
+};
+
+__device__ __forceinline__ void bc3_row(const Grid &g, const Q5 &q, const BC3Args &a, int j, int k) {
+  {  // inlet (inlet_pressure_extrapolate.py:11-66)
+    const int64_t b = gidx(g, 0, j, k), m1 = gidx(g, -1, j, k);
+    const double rhob = q.v[0][b];
+    const double ub0 = fabs(q.v[1][b] / rhob), ub1 = fabs(q.v[2][b] / rhob), ub2 = fabs(q.v[3][b] / rhob);
+    const double pb = (a.gama - 1) * (-0.5 * rhob * (ub0 * ub0 + ub1 * ub1 + ub2 * ub2) + q.v[4][b]);
+    const double ab = sqrt(a.gama * pb / rhob);
+    if (ub0 >= ab) {
+      for (int v = 0; v < 5; ++v) q.v[v][b] = q.v[v][m1];
+    } else {
+      const double e = q.v[4][b];
+      for (int t = 1; t <= 3; ++t) q.v[4][gidx(g, -t, j, k)] = e;
+    }
+  }
+  for (int v = 0; v < 5; ++v) {  // outlet (extrapolation.py:8-58)
+    const double val = q.v[v][gidx(g, g.n0 - 2, j, k)];
+    for (int t = 0; t <= 4; ++t) q.v[v][gidx(g, g.n0 - 1 + t, j, k)] = val;
+  }
+}
+
+__device__ __forceinline__ void bc3_col(const Grid &g, const Q5 &q, const BC3Args &a, int i, int t, int k) {
+  const double M2 = a.Minf * a.Minf, gama = a.gama;
+  const int64_t w = gidx(g, i, 0, k), a1 = gidx(g, i, 1, k);
+  // the wall point after this face: zero momentum, energy from Twall; its pressure
+  // (gama-1) (rhoE - |rhou|^2 / (2 rho)) is exactly (gama-1) rhoE there
+  const double rw = q.v[0][w], ew = a.Twall * (1.0 / M2) * rw / (gama * (gama - 1.0));
+  const double Pw = (gama - 1) * ew;
+  const double Ta = M2 * gama * (gama - 1) *
+                    (-(0.5 * q.v[1][a1] * q.v[1][a1] + 0.5 * q.v[2][a1] * q.v[2][a1] + 0.5 * q.v[3][a1] * q.v[3][a1]) /
+                         q.v[0][a1] + q.v[4][a1]) /
+                    q.v[0][a1];
+  const int64_t m = gidx(g, i, t, k), hh = gidx(g, i, -t, k);
+  const double um0 = q.v[1][m] / q.v[0][m], um1 = q.v[2][m] / q.v[0][m], um2 = q.v[3][m] / q.v[0][m];
+  const double Tt = (t + 1) * a.Twall - t * Ta;
+  const double rh = M2 * gama * Pw / Tt;
+  q.v[0][hh] = rh;
+  q.v[1][hh] = -rh * um0;
+  q.v[2][hh] = -rh * um1;
+  q.v[3][hh] = -rh * um2;
+  q.v[4][hh] = (1.0 / (gama - 1)) * Pw + 0.5 * rh * (um0 * um0 + um1 * um1 + um2 * um2);
+  if (t == 1) {
+    q.v[1][w] = 0.0;
+    q.v[2][w] = 0.0;
+    q.v[3][w] = 0.0;
+    q.v[4][w] = ew;
+    const double x0 = a.delta0 * i;  // Dirichlet top face
+    for (int j = g.n1 - 1; j < g.n1 + HY; ++j)
+      for (int v = 0; v < 5; ++v) q.v[v][gidx(g, i, j, k)] = x0 > a.xs ? a.hi[v] : a.lo[v];
+  }
+}
+
+__global__ void __launch_bounds__(BC2_THREADS) k3w_bc(Grid g, Q5 q, BC3Args a, int row_blocks) {
+  const int tid = threadIdx.x, k = blockIdx.y;
+  if (blockIdx.x == 0) {
+    for (int j = -3 + tid; j < g.n1 + HY; j += BC2_THREADS)
+      if (j <= 3 || j >= g.n1 - 1) bc3_row(g, q, a, j, k);
+    __syncthreads();
+    for (int w = tid; w < 3 * (g.n0 + HX + 3); w += BC2_THREADS) {
+      const int i = w / 3 - 3;
+      if (i <= 0 || i >= g.n0 - 2) bc3_col(g, q, a, i, w % 3 + 1, k);
+    }
+  } else if ((int)blockIdx.x <= row_blocks) {
+    const int j = 4 + ((int)blockIdx.x - 1) * BC2_THREADS + tid;
+    if (j < g.n1 - 1) bc3_row(g, q, a, j, k);
+  } else {
+    const int w = ((int)blockIdx.x - 1 - row_blocks) * BC2_THREADS + tid;
+    const int i = 1 + w / 3;
+    if (i < g.n0 - 2) bc3_col(g, q, a, i, w % 3 + 1, k);
+  }
+}
+
+// Periodic x2 (exchange.py:9-57): planes -3..-1 take n2-3..n2-1 and planes n2..n2+2 take 0..2,
+// whole padded x0-x1 planes.
+__global__ void k3w_wrap(Grid g, Q5 q) {
+  const int64_t plane = g.sz, N = plane * HZ;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 5 * N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int v = (int)(t / N);
+    const int64_t e = t % N, zo = e / plane, o = e % plane;  // zo = 0..HZ-1
+    double *f = q.v[v];
+    f[o + zo * plane] = f[o + (g.n2 + zo) * plane];                        // plane zo - HZ <- n2 + zo - HZ
+    f[o + (HZ + g.n2 + zo) * plane] = f[o + (HZ + zo) * plane];           // plane n2 + zo <- zo
+  }
+}
+
+// FP64 master -> working state over every padded point
+template <typename T> __global__ void k3w_to_state(int64_t numel, Q5 src, Q5T<T> dst) {
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < numel; t += (int64_t)gridDim.x * blockDim.x)
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      if constexpr (sizeof(T) == 4) dst.v[v][t] = cvt_f64_f32(src.v[v][t]);
+      else dst.v[v][t] = src.v[v][t];
+    }
+}
+
+// Viscous terms (momentum 0..2, energy) at every interior point, as k2_visc with the third
+// component and the periodic x2 derivatives: d/dx1 = D11 d/dxi1, d2/dx1^2 = D11^2 d2/dxi1^2 +
+// D11 SD111 d/dxi1, mixed derivatives nest first derivatives (the inner x0 or x2 derivative over the
+// extended range of the outer axis).  A 32 x 8 x-x1 tile stages u0, u1, u2, T and mu of the planes
+// k-2..k+2 and of V2H points around it in x0 and x1 in dynamic shared memory; the primitives are
+// formed from the working state as they are staged (FP32: u, p and T rounded once, prims_f32).
+template <typename T> constexpr size_t visc3_smem() {
+  return sizeof(T) * 5 * 5 * (size_t)(V2Y + 2 * V2H) * (V2X + 2 * V2H);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(V2X * V2Y) k3w_visc(Grid g, Q5T<const T> q, const double *D11, const double *SD111,
+                                                      Q5T<T> rv, Visc2Args va, double gama, double gM2, double suth,
+                                                      int clx, int cly) {
+  constexpr int SX = V2X + 2 * V2H, SY = V2Y + 2 * V2H, PL = SX * SY;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *sm = reinterpret_cast<T *>(smem_raw);  // [field u0 u1 u2 T mu][plane k-2..k+2][SY][SX]
+  auto S = [&](int f, int z, int y, int x) -> T & { return sm[((f * 5 + z) * SY + y) * SX + x]; };
+  const int i0 = blockIdx.x * V2X, j0 = blockIdx.y * V2Y, k = blockIdx.z;
+  const int tid = threadIdx.y * V2X + threadIdx.x;
+  const T S1 = T(suth);
+  for (int t = tid; t < 5 * PL; t += V2X * V2Y) {
+    const int z = t / PL, r = t % PL, li = r % SX, lj = r / SX;
+    const int gi = i0 - V2H + li, gj = j0 - V2H + lj, gk = k - 2 + z;
+    if (gi < -HX || gi >= g.n0 + HX || gj < -HY || gj >= g.n1 + HY) continue;
+    const int64_t m = gidx(g, gi, gj, gk);
+    T u[3], p, Tt;
+    const T rho = q.v[0][m];
+    if constexpr (sizeof(T) == 4) {
+      const float gm1 = (float)(gama - 1.0), gm1_lo = (float)((gama - 1.0) - (double)gm1);
+      float ir, p_lo;
+      prims_f32(rho, q.v[1][m], q.v[2][m], q.v[3][m], q.v[4][m], gm1, gm1_lo, ir, u, p, p_lo);
+      Tt = scaled_ratio_f32((float)gM2, p, p_lo, rho, ir);
+    } else {
+      const T ir = T(1) / rho;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) u[c] = q.v[1 + c][m] * ir;
+      p = (T(gama) - T(1)) * (q.v[4][m] - T(0.5) * rho * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]));
+      Tt = T(gM2) * p * ir;
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) S(c, z, lj, li) = u[c];
+    S(3, z, lj, li) = Tt;
+    S(4, z, lj, li) = (S1 + T(1)) * Tt * sqrt_t(Tt) / (S1 + Tt);
+  }
+  __syncthreads();
+  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+  if (i >= g.n0 || j >= g.n1) return;
+  const int li = threadIdx.x + V2H, lj = threadIdx.y + V2H;
+  const int64_t c = gidx(g, i, j, k);
+  const T id0 = T(va.inv_d0), id1 = T(va.inv_d1), id2 = T(va.inv_d2), iRe = T(1.0 / va.Re);
+  const T Dm = T(D11[j]), Sm = T(SD111[j]), mu = S(4, 2, lj, li);
+  const T c1 = T(1.0 / 12.0), c2 = T(2.0 / 3.0);
+  // central first derivative along x2 of the value at plane offset z (periodic: no closure)
+  auto dz1 = [&](auto &&F) { return id2 * (c1 * F(-2) - c2 * F(-1) + c2 * F(1) - c1 * F(2)); };
+  auto dz2 = [&](auto &&F) {
+    return id2 * id2 * (-c1 * F(-2) + T(4.0 / 3.0) * F(-1) - T(2.5) * F(0) + T(4.0 / 3.0) * F(1) - c1 * F(2));
+  };
+  T gr[3][3], h[3][3][3];
+#pragma unroll
+  for (int f = 0; f < 3; ++f) {
+    auto X = [&](int o) { return S(f, 2, lj, li + o); };
+    auto Y = [&](int o) { return S(f, 2, lj + o, li); };
+    auto Z = [&](int o) { return S(f, 2 + o, lj, li); };
+    gr[f][0] = id0 * d1c<T>(X, i, g.n0, clx);
+    const T fy = id1 * d1c<T>(Y, j, g.n1, cly);
+    gr[f][1] = Dm * fy;
+    gr[f][2] = dz1(Z);
+    h[f][0][0] = id0 * id0 * d2c<T>(X, i, g.n0);
+    h[f][1][1] = Dm * Dm * (id1 * id1 * d2c<T>(Y, j, g.n1)) + Dm * Sm * fy;
+    h[f][2][2] = dz2(Z);
+    // x0 derivative of row j+o / of plane k+o, then the outer derivative
+    auto inner_xy = [&](int o) { return id0 * d1c<T>([&](int p) { return S(f, 2, lj + o, li + p); }, i, g.n0, clx); };
+    auto inner_xz = [&](int o) { return id0 * d1c<T>([&](int p) { return S(f, 2 + o, lj, li + p); }, i, g.n0, clx); };
+    auto inner_zy = [&](int o) { return dz1([&](int p) { return S(f, 2 + p, lj + o, li); }); };
+    h[f][0][1] = h[f][1][0] = Dm * (id1 * d1c<T>(inner_xy, j, g.n1, cly));
+    h[f][0][2] = h[f][2][0] = dz1(inner_xz);
+    h[f][1][2] = h[f][2][1] = Dm * (id1 * d1c<T>(inner_zy, j, g.n1, cly));
+  }
+  auto XT = [&](int o) { return S(3, 2, lj, li + o); };
+  auto YT = [&](int o) { return S(3, 2, lj + o, li); };
+  auto ZT = [&](int o) { return S(3, 2 + o, lj, li); };
+  auto Xmu = [&](int o) { return S(4, 2, lj, li + o); };
+  auto Ymu = [&](int o) { return S(4, 2, lj + o, li); };
+  auto Zmu = [&](int o) { return S(4, 2 + o, lj, li); };
+  const T mug[3] = {id0 * d1c<T>(Xmu, i, g.n0, clx), Dm * id1 * d1c<T>(Ymu, j, g.n1, cly), dz1(Zmu)};
+  const T Tyx = id1 * d1c<T>(YT, j, g.n1, cly);
+  const T Tg[3] = {id0 * d1c<T>(XT, i, g.n0, clx), Dm * Tyx, dz1(ZT)};
+  const T Tlap = id0 * id0 * d2c<T>(XT, i, g.n0) + (Dm * Dm * (id1 * id1 * d2c<T>(YT, j, g.n1)) + Dm * Sm * Tyx) + dz2(ZT);
+  const T div = gr[0][0] + gr[1][1] + gr[2][2];
+  const T uu[3] = {S(0, 2, lj, li), S(1, 2, lj, li), S(2, 2, lj, li)};
+  T e = T(va.kappa) * (mu * Tlap + mug[0] * Tg[0] + mug[1] * Tg[1] + mug[2] * Tg[2]);
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    T v = T(0);
+#pragma unroll
+    for (int b = 0; b < 3; ++b) v += mug[b] * (gr[a][b] + gr[b][a] - (a == b ? T(2.0 / 3.0) * div : T(0))) * iRe;
+    const T lap = h[a][0][0] + h[a][1][1] + h[a][2][2];
+    const T ddiv = h[0][a][0] + h[1][a][1] + h[2][a][2];
+    v += mu * iRe * (lap + ddiv * T(1.0 / 3.0));
+    rv.v[a][c] = v;
+    e += uu[a] * v;
+#pragma unroll
+    for (int b = 0; b < 3; ++b) e += mu * iRe * (gr[a][b] + gr[b][a] - (a == b ? T(2.0 / 3.0) * div : T(0))) * gr[a][b];
+  }
+  rv.v[3][c] = e;
+}
+
+// R = fluxes + viscous terms at every interior point, then the LS-RK3 update of the FP64 master
+// (update = 1), or R itself into du (update = 0)
+template <typename T>
+__global__ void k3w_rk(Grid g, Q5T<const T> rf, Q5T<const T> rv, Q5 du, Q5 q64, double dt, double A, double B,
+                       int update) {
+  const int64_t N = (int64_t)g.n0 * g.n1 * g.n2;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.n0), j = (int)((t / g.n0) % g.n1), k = (int)(t / ((int64_t)g.n0 * g.n1));
+    const int64_t c = gidx(g, i, j, k);
+    T R[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) R[v] = rf.v[v][c];
+#pragma unroll
+    for (int v = 1; v < 5; ++v) R[v] += rv.v[v - 1][c];
+    if (update) {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        const double d = dt * to_f64(R[v]) + A * du.v[v][c];
+        du.v[v][c] = d;
+        q64.v[v][c] = B * d + q64.v[v][c];
+      }
+    } else {
+#pragma unroll
+      for (int v = 0; v < 5; ++v) du.v[v][c] = to_f64(R[v]);
+    }
+  }
+}
+
+static Q5 q5(double *const *a) {
+  Q5 r;
+  for (int v = 0; v < 5; ++v) r.v[v] = a[v];
+  return r;
+}
+template <typename T> static Q5T<T> q5t(void *const *a) {
+  Q5T<T> r;
+  for (int v = 0; v < 5; ++v) r.v[v] = static_cast<T *>(a[v]);
+  return r;
+}
+
+void launch3w_metrics(const Ctx &c, const double *x1_line, cudaStream_t s, int64_t *launches) {
+  k3w_metrics<<<1, 256, 0, s>>>(c.g.n1, x1_line, c.d11, c.sd111, c.ysc_d, c.ysc_f, 1.0 / c.plan.delta[1],
+                                closure_bits(c.plan, 1));
+  ++*launches;
+}
+
+// face conditions and the x2 wrap on the FP64 master, then the working state from it
+template <typename T> void launch3w_bcs(const Ctx &c, cudaStream_t s, int64_t *launches) {
+  const osb_plan_desc &p = c.plan;
+  BC3Args a;
+  a.gama = p.gama;
+  a.Minf = p.Minf;
+  a.Twall = p.Twall;
+  a.delta0 = p.delta[0];
+  a.xs = p.dirichlet_x_switch;
+  for (int v = 0; v < 5; ++v) {
+    a.lo[v] = p.dirichlet_state[0][v];
+    a.hi[v] = p.dirichlet_state[1][v];
+  }
+  const int rows = c.g.n1 - 5 > 0 ? c.g.n1 - 5 : 0, cols = c.g.n0 - 3 > 0 ? c.g.n0 - 3 : 0;
+  const int row_blocks = (rows + BC2_THREADS - 1) / BC2_THREADS;
+  const int col_blocks = (3 * cols + BC2_THREADS - 1) / BC2_THREADS;
+  k3w_bc<<<dim3(1 + row_blocks + col_blocks, c.g.n2), BC2_THREADS, 0, s>>>(c.g, q5(c.qold), a, row_blocks);
+  int nb = (int)((5 * c.g.sz * HZ + 255) / 256);
+  if (nb > c.num_sms * 8) nb = c.num_sms * 8;
+  k3w_wrap<<<nb, 256, 0, s>>>(c.g, q5(c.qold));
+  nb = (int)((c.g.numel + 255) / 256);
+  if (nb > c.num_sms * 8) nb = c.num_sms * 8;
+  k3w_to_state<T><<<nb, 256, 0, s>>>(c.g.numel, q5(c.qold), q5t<T>(c.qa));
+  *launches += 3;
+}
+
+// One stage's right-hand side: the x0, x1, x2 flux passes into res (this stream) and the viscous
+// terms into resv (a side stream) concurrently, then R and the LS-RK3 update (or R into du).
+template <typename T>
+void launch3w_rhs(const Ctx &c, int update, double A, double B, double dt, cudaStream_t s, int64_t *launches) {
+  const osb_plan_desc &p = c.plan;
+  Fields5<const T> q;
+  Fields5<T> r;
+  for (int v = 0; v < 5; ++v) {
+    q.v[v] = static_cast<const T *>(c.qa[v]);
+    r.v[v] = static_cast<T *>(c.res[v]);
+  }
+  cudaEventRecord(c.ev_fork2, s);
+  cudaStreamWaitEvent(c.side2[1], c.ev_fork2, 0);
+  for (int d = 0; d < 3; ++d) launch_weno_dir<T>(c, q, r, d, s, launches);
+  Visc2Args va;
+  va.Re = p.Re;
+  va.kappa = 1.0 / ((p.gama - 1) * p.Minf * p.Minf * p.Pr * p.Re);
+  va.inv_d0 = 1.0 / p.delta[0];
+  va.inv_d1 = 1.0 / p.delta[1];
+  va.inv_d2 = 1.0 / p.delta[2];
+  Q5T<T> rv{{static_cast<T *>(c.resv[0]), static_cast<T *>(c.resv[1]), static_cast<T *>(c.resv[2]),
+             static_cast<T *>(c.resv[3]), nullptr}};
+  dim3 gv((c.g.n0 + V2X - 1) / V2X, (c.g.n1 + V2Y - 1) / V2Y, c.g.n2);
+  k3w_visc<T><<<gv, dim3(V2X, V2Y), visc3_smem<T>(), c.side2[1]>>>(
+      c.g, q5t<const T>(c.qa), c.d11, c.sd111, rv, va, p.gama, p.gama * p.Minf * p.Minf, p.SuthT / p.RefT,
+      closure_bits(p, 0), closure_bits(p, 1));
+  cudaEventRecord(c.ev_join2[1], c.side2[1]);
+  cudaStreamWaitEvent(s, c.ev_join2[1], 0);
+  Q5T<const T> rf{{r.v[0], r.v[1], r.v[2], r.v[3], r.v[4]}};
+  Q5T<const T> rvc{{rv.v[0], rv.v[1], rv.v[2], rv.v[3], nullptr}};
+  int nb = (int)(((int64_t)c.g.n0 * c.g.n1 * c.g.n2 + 255) / 256);
+  if (nb > c.num_sms * 8) nb = c.num_sms * 8;
+  k3w_rk<T><<<nb, 256, 0, s>>>(c.g, rf, rvc, q5(c.du2), q5(c.qold), dt, A, B, update);
+  *launches += 2;
+}
+
+template <typename T> void setup3w() {
+  cudaFuncSetAttribute(k3w_visc<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)visc3_smem<T>());
+}
+
+template void setup3w<float>();
+template void setup3w<double>();
+template void launch3w_bcs<float>(const Ctx &, cudaStream_t, int64_t *);
+template void launch3w_bcs<double>(const Ctx &, cudaStream_t, int64_t *);
+template void launch3w_rhs<float>(const Ctx &, int, double, double, double, cudaStream_t, int64_t *);
+template void launch3w_rhs<double>(const Ctx &, int, double, double, double, cudaStream_t, int64_t *);
 
 template void launch2_cutoff<float>(const Ctx &, double *, cudaStream_t, int64_t *);
 template void launch2_cutoff<double>(const Ctx &, double *, cudaStream_t, int64_t *);

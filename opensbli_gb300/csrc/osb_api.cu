@@ -32,6 +32,9 @@ int cuda_err(osb_ctx *c, cudaError_t e, const char *where) {
   return set_err(c, OSB_ECUDA, buf);
 }
 
+// a span-periodic 3D wall-bounded block (the 2D shock/boundary-layer faces in x0 and x1)
+bool wall3(const osb_plan_desc &p) { return p.ndim == 3 && p.bc[1][0] == OSB_BC_ISOTHERMAL_WALL; }
+
 // the characteristic-flux schemes of the 3D kernels (WENO5-JS, WENO5-Z, TENO5)
 bool char_fluxes(const osb_plan_desc &p) {
   return p.conv == OSB_CONV_WENO5JS || p.conv == OSB_CONV_WENO5Z || p.conv == OSB_CONV_TENO5 ||
@@ -80,6 +83,40 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
     return OSB_OK;
   }
   if (p->ndim != 3) { snprintf(why, n, "ndim %d: this library implements 2D and 3D blocks", p->ndim); return OSB_EUNSUPPORTED; }
+  if (wall3(*p)) {
+    // span-periodic wall-bounded block: the 2D configuration's faces in x0 and x1, periodic x2
+    if (p->bc[0][0] != OSB_BC_INLET_PRESSURE_EXTRAPOLATE || p->bc[0][1] != OSB_BC_EXTRAPOLATION ||
+        p->bc[1][1] != OSB_BC_DIRICHLET || p->bc[2][0] != OSB_BC_PERIODIC || p->bc[2][1] != OSB_BC_PERIODIC) {
+      snprintf(why, n, "3D wall-bounded blocks: inlet/extrapolation (x0), isothermal wall/Dirichlet (x1), periodic x2");
+      return OSB_EUNSUPPORTED;
+    }
+    for (int d = 0; d < 3; ++d) {
+      if (p->n[d] < 8 || p->n[d] > 4096) { snprintf(why, n, "n[%d] = %d out of range [8, 4096]", d, p->n[d]); return OSB_EINVAL; }
+      if (!(p->delta[d] > 0)) { snprintf(why, n, "delta[%d] must be > 0", d); return OSB_EINVAL; }
+    }
+    if (p->conv != OSB_CONV_TENO5 && p->conv != OSB_CONV_WENO5JS && p->conv != OSB_CONV_WENO5Z &&
+        p->conv != OSB_CONV_TENO6) {
+      snprintf(why, n, "3D wall-bounded blocks: TENO5, TENO6, WENO5-JS or WENO5-Z fluxes");
+      return OSB_EUNSUPPORTED;
+    }
+    if (p->teno_adaptive) { snprintf(why, n, "3D wall-bounded blocks: fixed TENO cut-off"); return OSB_EUNSUPPORTED; }
+    if (p->filter != OSB_FILTER_NONE) { snprintf(why, n, "3D wall-bounded blocks: no WENO filter"); return OSB_EUNSUPPORTED; }
+    for (int d = 0; d < 2; ++d)
+      for (int side = 0; side < 2; ++side)
+        if (p->closure[d][side] != OSB_CLOSURE_REDUCED_ACCESS && p->closure[d][side] != OSB_CLOSURE_CARPENTER) {
+          snprintf(why, n, "closure[%d][%d] = %d: OSB_CLOSURE_REDUCED_ACCESS or OSB_CLOSURE_CARPENTER", d, side,
+                   p->closure[d][side]);
+          return OSB_EINVAL;
+        }
+    if (p->visc != OSB_VISC_SUTHERLAND) { snprintf(why, n, "3D wall-bounded blocks: Sutherland viscosity"); return OSB_EUNSUPPORTED; }
+    if (p->rk != OSB_RK3_LS) { snprintf(why, n, "3D wall-bounded blocks: low-storage RK3"); return OSB_EUNSUPPORTED; }
+    if (p->precision != OSB_PREC_FP64 && p->precision != OSB_PREC_MIXED) { snprintf(why, n, "precision %d", p->precision); return OSB_EINVAL; }
+    if (!(p->gama > 1.0) || !(p->Minf > 0) || !(p->Re > 0) || !(p->Pr > 0) || !(p->Twall > 0) || !(p->RefT > 0)) {
+      snprintf(why, n, "bad physical constants");
+      return OSB_EINVAL;
+    }
+    return OSB_OK;
+  }
   if (p->teno_adaptive) {
     if (p->conv != OSB_CONV_TENO5 && p->conv != OSB_CONV_TENO6) {
       snprintf(why, n, "teno_adaptive needs TENO5 or TENO6 fluxes");
@@ -450,6 +487,59 @@ template <typename T> int step_impl(osb_ctx *c, int nsteps, double dt) {
   return cuda_err(c, cudaGetLastError(), "osb_step launch");
 }
 
+// One LS-RK3 step on a span-periodic 3D wall-bounded block: face conditions (and the working state),
+// then per stage the right-hand side with the update du = A du + dt R, q += B du on the FP64 master
+// and the face conditions again (algorithm.py:384-477).
+template <typename T> void one_step3w(osb_ctx *c, double dt, cudaStream_t s) {
+  {
+    ProfScope ps(c, PF_HALO, s);
+    launch3w_bcs<T>(*c, s, &c->launches);
+  }
+  for (int st = 0; st < 3; ++st) {
+    {
+      ProfScope ps(c, PF_CENTRAL_RK, s);
+      launch3w_rhs<T>(*c, 1, c->plan.rk_a[st], c->plan.rk_b[st], dt, s, &c->launches);
+    }
+    ProfScope ps(c, PF_HALO, s);
+    launch3w_bcs<T>(*c, s, &c->launches);
+  }
+}
+
+template <typename T> int step3w_impl(osb_ctx *c, int nsteps, double dt) {
+  cudaStream_t s = c->stream;
+  c->launches = 0;
+  for (int it = 0; it < nsteps; ++it) {
+    if (c->plan.use_graphs && !c->prof_on && c->stream != nullptr) {
+      if (c->graph[0] && c->graph_dt[0] != dt) {
+        cudaGraphExecDestroy(c->graph[0]);
+        c->graph[0] = nullptr;
+      }
+      if (!c->graph[0]) {
+        cudaGraph_t gr;
+        int64_t l0 = c->launches;
+        cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return cuda_err(c, e, "cudaStreamBeginCapture");
+        one_step3w<T>(c, dt, s);
+        e = cudaStreamEndCapture(s, &gr);
+        if (e != cudaSuccess) return cuda_err(c, e, "cudaStreamEndCapture");
+        e = cudaGraphInstantiate(&c->graph[0], gr, 0);
+        cudaGraphDestroy(gr);
+        if (e != cudaSuccess) return cuda_err(c, e, "cudaGraphInstantiate");
+        c->graph_dt[0] = dt;
+        c->graph_launches = c->launches - l0;
+        c->launches = l0;
+      }
+      cudaError_t e = cudaGraphLaunch(c->graph[0], s);
+      if (e != cudaSuccess) return cuda_err(c, e, "cudaGraphLaunch");
+      c->launches += c->graph_launches;
+    } else {
+      one_step3w<T>(c, dt, s);
+    }
+  }
+  if (c->prof_on) prof_collect(c);
+  return cuda_err(c, cudaGetLastError(), "osb_step launch");
+}
+
 // One LS-RK3 step on a 2D block: boundary conditions, then per stage the right-hand side with the
 // update du = A du + dt R, q += B du, and the boundary conditions again (algorithm.py:384-477).
 template <typename T> void one_step2(osb_ctx *c, double dt, cudaStream_t s) {
@@ -527,7 +617,7 @@ __global__ void k_copy_padded(Grid g, const double *src, int h, double *dst) {
 }
 
 struct P4 {
-  const double *v[4];
+  const double *v[5];
 };
 template <typename T> __global__ void k_pack_d(Grid g, P4 src4, T *dst, int nvar) {
   const int64_t N = (int64_t)g.n0 * g.n1 * g.n2;
@@ -654,6 +744,17 @@ int osb_set_state64_padded(osb_ctx *c, int var, const double *src, int h) {
 
 int osb_set_coordinate(osb_ctx *c, int axis, const double *src, int h) {
   if (!c) return OSB_EINVAL;
+  if (wall3(c->plan)) {
+    // the x1 coordinate is a function of j alone: a line of n1 + 2h values
+    if (axis != 1) return set_err(c, OSB_EUNSUPPORTED, "coordinates: blocks stretched in x1 only");
+    if (!src || h < 0 || h > 4) return set_err(c, OSB_EINVAL, "coordinate line needs a halo of 0..4 points");
+    cudaError_t e = cudaMemcpyAsync(c->x1, src + h, (size_t)c->g.n1 * sizeof(double), cudaMemcpyDefault, c->stream);
+    if (e != cudaSuccess) return cuda_err(c, e, "osb_set_coordinate");
+    int64_t l = 0;
+    launch3w_metrics(*c, c->x1, c->stream, &l);
+    c->metrics_valid = 1;
+    return cuda_err(c, cudaGetLastError(), "osb_set_coordinate");
+  }
   if (c->plan.ndim != 2 || axis != 1) return set_err(c, OSB_EUNSUPPORTED, "coordinates: 2D blocks stretched in x1 only");
   if (!src || h < 4 || h > 4) return set_err(c, OSB_EINVAL, "coordinate array needs a 4-point halo");
   const int nb = blocks_for((int64_t)(c->g.n0 + 2 * h) * (c->g.n1 + 2 * h));
@@ -772,6 +873,36 @@ int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
     if (e == cudaSuccess) e = cudaMemset(c->ct2, 0, bytes);
     c->ph.ctp = c->ct2;
   }
+  if (e == cudaSuccess && wall3(*plan)) {
+    // LS-RK register, viscous terms, the x1 metric lines, a side stream for the viscous terms
+    const size_t b64 = (size_t)c->g.numel * sizeof(double), nl = (size_t)c->g.n1;
+    for (int v = 0; v < 5 && e == cudaSuccess; ++v) {
+      e = cudaMalloc(&c->du2[v], b64);
+      if (e == cudaSuccess) e = cudaMemset(c->du2[v], 0, b64);
+    }
+    for (int v = 0; v < 4 && e == cudaSuccess; ++v) {
+      e = cudaMalloc(&c->resv[v], bytes);
+      if (e == cudaSuccess) e = cudaMemset(c->resv[v], 0, bytes);
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&c->x1, nl * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&c->d11, nl * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&c->sd111, nl * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&c->ysc_d, nl * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&c->ysc_f, nl * sizeof(float2));
+    for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+      e = cudaStreamCreateWithFlags(&c->side2[k], cudaStreamNonBlocking);
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_join2[k], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork2, cudaEventDisableTiming);
+    c->ph.ysc_d = c->ysc_d;
+    c->ph.ysc_f = c->ysc_f;
+    if (e == cudaSuccess) {
+      if (c->mixed) setup3w<float>();
+      else setup3w<double>();
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = upload2_closure_weights();  // Carpenter closure tables of the derivatives
+  }
   c->red_blocks = 152 * 8;
   if (e == cudaSuccess) e = cudaMalloc(&c->red, (c->red_blocks + 1) * sizeof(double));
   if (e == cudaSuccess) e = cudaMalloc(&c->d_status, sizeof(int));
@@ -817,7 +948,8 @@ static int check_bound(osb_ctx *c) {
 int osb_init_tgv(osb_ctx *c) {
   if (!c) return OSB_EINVAL;
   if (int rc = check_bound(c)) return rc;
-  if (c->plan.ndim != 3) return set_err(c, OSB_EUNSUPPORTED, "the Taylor-Green initial condition is 3D");
+  if (c->plan.ndim != 3 || wall3(c->plan))
+    return set_err(c, OSB_EUNSUPPORTED, "the Taylor-Green initial condition is for periodic or symmetric 3D blocks");
   const int nb = blocks_for((int64_t)c->g.n0 * c->g.n1 * c->g.n2);
   const osb_plan_desc &p = c->plan;
   if (c->mixed)
@@ -864,7 +996,7 @@ int osb_set_state64(osb_ctx *c, int var, const double *src) {
   else k_set64<double><<<nb, 256, 0, c->stream>>>(c->g, src, (double *)c->qa[var], c->qold[var]);
   c->qold_valid = 1;
   c->cur = 0;
-  if (var == 4) {
+  if (var == 4 && !wall3(c->plan)) {  // wall-bounded blocks fill their halos at the start of a step
     int64_t l = 0;
     if (c->mixed) launch_halos<float>(*c, fields<float>(c->qa), c->stream, &l);
     else launch_halos<double>(*c, fields<double>(c->qa), c->stream, &l);
@@ -977,6 +1109,11 @@ int osb_step(osb_ctx *c, int nsteps, double dt) {
     if (!c->qold_valid) return set_err(c, OSB_EINVAL, "2D block: set the state first");
     return c->mixed ? step2_impl<float>(c, nsteps, dt) : step2_impl<double>(c, nsteps, dt);
   }
+  if (wall3(c->plan)) {
+    if (!c->metrics_valid) return set_err(c, OSB_EINVAL, "3D wall-bounded block: call osb_set_coordinate first");
+    if (!c->qold_valid) return set_err(c, OSB_EINVAL, "3D wall-bounded block: set the state first");
+    return c->mixed ? step3w_impl<float>(c, nsteps, dt) : step3w_impl<double>(c, nsteps, dt);
+  }
   return c->mixed ? step_impl<float>(c, nsteps, dt) : step_impl<double>(c, nsteps, dt);
 }
 
@@ -997,6 +1134,22 @@ int osb_residual(osb_ctx *c, void *dev_out) {
     } else {
       launch2_rhs<double>(*c, 0, 0.0, 0.0, 0.0, c->stream, &l);
       k_pack_d<double><<<nb, 256, 0, c->stream>>>(c->g, d, (double *)dev_out, 4);
+    }
+    return cuda_err(c, cudaGetLastError(), "osb_residual");
+  }
+  if (wall3(c->plan)) {
+    if (!c->metrics_valid) return set_err(c, OSB_EINVAL, "3D wall-bounded block: call osb_set_coordinate first");
+    int64_t l = 0;
+    P4 d;
+    for (int v = 0; v < 5; ++v) d.v[v] = c->du2[v];
+    if (c->mixed) {
+      launch3w_bcs<float>(*c, c->stream, &l);
+      launch3w_rhs<float>(*c, 0, 0.0, 0.0, 0.0, c->stream, &l);
+      k_pack_d<float><<<nb, 256, 0, c->stream>>>(c->g, d, (float *)dev_out, 5);
+    } else {
+      launch3w_bcs<double>(*c, c->stream, &l);
+      launch3w_rhs<double>(*c, 0, 0.0, 0.0, 0.0, c->stream, &l);
+      k_pack_d<double><<<nb, 256, 0, c->stream>>>(c->g, d, (double *)dev_out, 5);
     }
     return cuda_err(c, cudaGetLastError(), "osb_residual");
   }
@@ -1238,7 +1391,7 @@ int osb_get_central_shape(osb_ctx *c, int *ty) {
 int osb_autotune(osb_ctx *c, int reps, double *best_ms) {
   if (!c) return OSB_EINVAL;
   if (reps < 1) return set_err(c, OSB_EINVAL, "osb_autotune: reps must be >= 1");
-  if (c->plan.ndim != 3) {
+  if (c->plan.ndim != 3 || wall3(c->plan)) {  // the tuner times the periodic blocks' kernels
     for (int t = 0; t < OSB_TUNE_SLOTS && best_ms; ++t) best_ms[t] = 0.0;
     return OSB_OK;
   }
@@ -1266,13 +1419,14 @@ void osb_destroy(osb_ctx *c) {
   cudaFree(c->d_status);
   cudaFree(c->adj);
   cudaFree(c->probe_buf);
-  for (int v = 0; v < 4; ++v) {
+  for (int v = 0; v < 4; ++v)
     if (c->mixed) cudaFree(c->q64_2d[v]);
-    cudaFree(c->du2[v]);
-  }
+  for (int v = 0; v < 5; ++v) cudaFree(c->du2[v]);
   for (int k = 0; k < 6; ++k) cudaFree(c->prim2[k]);
   for (int v = 0; v < 4; ++v) cudaFree(c->resy[v]);
-  for (int v = 0; v < 3; ++v) cudaFree(c->resv[v]);
+  for (int v = 0; v < 4; ++v) cudaFree(c->resv[v]);
+  cudaFree(c->ysc_d);
+  cudaFree(c->ysc_f);
   for (int k = 0; k < 2; ++k) {
     if (c->side2[k]) cudaStreamDestroy(c->side2[k]);
     if (c->ev_join2[k]) cudaEventDestroy(c->ev_join2[k]);

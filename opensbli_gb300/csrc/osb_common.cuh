@@ -46,6 +46,10 @@ struct Phys {
   // adaptive TENO on 3D blocks: C_T per point (state precision, padded layout); the interface
   // between cells c-1 and c takes the value at c-1.  Null for a fixed cut-off.
   const void *ctp;
+  // blocks stretched in x1: the x1 flux difference of cell j is scaled by inv_delta1 D11(j), given
+  // per j in FP64 and as an FP32 pair (in place of inv_delta[1]).  Null on Cartesian blocks.
+  const double *ysc_d;
+  const float2 *ysc_f;
 };
 
 // the FP64 or FP32 copy of a plan constant

@@ -53,16 +53,19 @@ struct Ctx {
   int nvar = 5;
   int hx2 = 4, hy2 = 4;           // halos of the 2D layout
   double *q64_2d[4] = {};         // FP64 master state, padded (the bound arrays in FP64 mode)
-  double *du2[4] = {};            // LS-RK register
+  double *du2[5] = {};            // LS-RK register (2D and span-periodic 3D wall-bounded blocks)
   void *prim2[6] = {};            // u0, u1, p, a, T, mu (state precision, padded)
   void *ct2 = nullptr;            // adaptive TENO (2D and 3D): cut-off C_T per point (state precision, padded)
-  // the stage's three right-hand-side parts, formed concurrently: x fluxes into res, x1 fluxes into
-  // resy, viscous terms (momentum 0, 1, energy) into resv; two side streams and fork/join events
+  // the stage's right-hand-side parts, formed concurrently: 2D: x fluxes into res, x1 fluxes into
+  // resy, viscous terms (momentum 0, 1, energy) into resv; 3D wall-bounded: fluxes into res, viscous
+  // terms (momentum 0..2, energy) into resv; two side streams and fork/join events
   void *resy[4] = {};
-  void *resv[3] = {};
+  void *resv[4] = {};
   cudaStream_t side2[2] = {nullptr, nullptr};
   cudaEvent_t ev_fork2 = nullptr, ev_join2[2] = {nullptr, nullptr};
-  double *x1 = nullptr, *d11 = nullptr, *sd111 = nullptr;
+  double *x1 = nullptr, *d11 = nullptr, *sd111 = nullptr;  // 2D: padded arrays; 3D wall-bounded: lines in j
+  double *ysc_d = nullptr;        // 3D wall-bounded: inv_delta1 D11(j), FP64 and FP32 pair
+  float2 *ysc_f = nullptr;
   int metrics_valid = 0;
   std::string err;
   // per-kernel-family event timing (osb_profile); only used on the eager (non-graph) path
@@ -120,6 +123,14 @@ void launch2_to_state(const Ctx &c, cudaStream_t s, int64_t *launches);
 template <typename T> void launch2_cutoff(const Ctx &c, double *out, cudaStream_t s, int64_t *launches);
 template <typename T>
 void launch2_rhs(const Ctx &c, int update, double A, double B, double dt, cudaStream_t s, int64_t *launches);
+// span-periodic 3D wall-bounded blocks (osb_2d.cu): metrics from the x1 coordinate line, the face
+// conditions + x2 wrap on the FP64 master followed by the working state, one stage's right-hand side
+// with the LS-RK3 update (update = 1) or R into du2 (update = 0)
+void launch3w_metrics(const Ctx &c, const double *x1_line, cudaStream_t s, int64_t *launches);
+template <typename T> void launch3w_bcs(const Ctx &c, cudaStream_t s, int64_t *launches);
+template <typename T>
+void launch3w_rhs(const Ctx &c, int update, double A, double B, double dt, cudaStream_t s, int64_t *launches);
+template <typename T> void setup3w();
 
 // batched ensemble kernels (persistent, tile queue): items are int4 {instance, bx, by, bz}
 cudaError_t batch_table_upload_central(const void *src_dev, size_t bytes, cudaStream_t s);

@@ -41,6 +41,18 @@ template <int DIR> struct WTile {
   static constexpr int FS = DIR == 0 ? TI + 1 : TA;  // row pitch of the flux array (x: padded)
 };
 
+// 1/delta of the x1 flux difference at row j of a block stretched in x1 (inv_delta1 D11(j)) as the
+// pair the flux difference is multiplied by
+__device__ __forceinline__ void ysc_pair(const Phys &ph, int j, float &hi, float &lo) {
+  const float2 p = ph.ysc_f[j];
+  hi = p.x;
+  lo = p.y;
+}
+__device__ __forceinline__ void ysc_pair(const Phys &ph, int j, double &hi, double &lo) {
+  hi = ph.ysc_d[j];
+  lo = 0.0;
+}
+
 template <typename T, int D, typename Pt>
 __device__ __forceinline__ void load_point(const Pt &P, int t, WPt<T> &w, PtFlux &pf) {
   w.Q[0] = P(W_RHO, t);
@@ -209,12 +221,14 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 2 : 1) k_weno(Grid g, Fi
     int m, a;
     if (DIR == 0) { a = t / (TI - 1); m = t % (TI - 1); }
     else { m = t / TA; a = t % TA; }
+    T sh = idd, sl = idd_lo;
+    if (DIR == 1 && ph.ysc_d) ysc_pair(ph, d0 + m, sh, sl);
 #pragma unroll
     for (int v = 0; v < 5; ++v) {
       T diff = sflux[fidx(v, m + 1, a)] - sflux[fidx(v, m, a)];
       if constexpr (sizeof(T) == 4 && SCH != SCH_FILTER)
         diff = sdf[fidx(v, m + 1, a)] + diff;  // (F_i - F_{i-1}) + (G_i - G_{i-1})
-      const T d = -mul_hl(diff, idd, idd_lo);
+      const T d = -mul_hl(diff, sh, sl);
       res.v[v][gi[l]] = ACCUM ? rv[l][v] + d : d;
     }
   }
@@ -283,9 +297,11 @@ __device__ __forceinline__ void weno_march_tile(const Grid &g, Fields5<const T> 
       if (ph.ctp) cti = static_cast<const T *>(ph.ctp)[mline + (int64_t)(c - 1) * sd];
     interface_flux<T, DIR, SCH>(W, gm1, igm1, eps, cti, F);
     if (c > c0) {
+      T sh = idd, sl = idd_lo;
+      if (DIR == 1 && ph.ysc_d) ysc_pair(ph, c - 1, sh, sl);
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        const T d = -mul_hl(flux_difference<SCH>(W, v, F[v], Fp[v]), idd, idd_lo);
+        const T d = -mul_hl(flux_difference<SCH>(W, v, F[v], Fp[v]), sh, sl);
         res.v[v][mc] = ACCUM ? rv[v] + d : d;
       }
     }

@@ -136,6 +136,24 @@ def tgv_cfl_dt(plan, cfl=0.5):
     return cfl * min(plan.delta) / float(s.max())
 
 
+def sbli3d_plan(n0=128, n1=64, n2=16, precision="fp64", conv="teno5", dt=0.04, use_graphs=True, delta2=2.0,
+                closure=(("reduced_access", "reduced_access"),) * 2):
+    """3D span-periodic shock/boundary-layer block: the 2D configuration of katzer_plan with a periodic
+    x2 axis of spacing delta2 (apps/transitional_SBLI/transitional_SBLI.py's block without its body
+    force), the Dirichlet top face carrying rhou2 = 0."""
+    A, B = ls_rk3_ssp_coefficients()
+    lo, hi = Plan.dirichlet_lo, Plan.dirichlet_hi
+    return Plan(ndim=3, n=(n0, n1, n2), delta=(400.0 / (n0 - 1), 115.0 / (n1 - 1), delta2), conv=conv,
+                visc="sutherland", rk="ls_rk3", precision=precision,
+                bc=(("inlet_pressure_extrapolate", "extrapolation"), ("isothermal_wall", "dirichlet"),
+                    ("periodic", "periodic")),
+                gama=1.4, Minf=2.0, Re=950.0, Pr=0.72, teno_ct=1e-5, teno_eps=1e-15, rk_a=A, rk_b=B, dt=dt,
+                use_graphs=use_graphs, ic="host", closure=tuple(tuple(c) for c in closure),
+                weno_eps=1e-14 if conv == "weno5z" else 1e-6,  # WenoZ.eps / WenoJS.eps (weno.py)
+                dirichlet_lo=tuple(lo[:3]) + (0.0, lo[3]), dirichlet_hi=tuple(hi[:3]) + (0.0, hi[3]),
+                name="sbli3d_%s_%dx%dx%d" % (conv, n0, n1, n2))
+
+
 def katzer_plan(n0=512, n1=256, precision="fp64", conv="teno5", dt=0.04, use_graphs=True, adaptive=False,
                 closure=(("reduced_access", "reduced_access"),) * 2):
     """2D laminar shock-wave/boundary-layer interaction (apps/katzer_SBLI/katzer_SBLI.py constants):

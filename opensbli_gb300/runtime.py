@@ -12,7 +12,7 @@ import torch
 
 from . import build as _build
 
-OSB_ABI_VERSION = 5
+OSB_ABI_VERSION = 6
 ERRORS = {
     -1: "invalid plan or argument",
     -2: "unsupported kernel pattern",
@@ -58,7 +58,7 @@ class PlanDesc(ctypes.Structure):
         ("Twall", ctypes.c_double),
         ("SuthT", ctypes.c_double),
         ("RefT", ctypes.c_double),
-        ("dirichlet_state", (ctypes.c_double * 4) * 2),
+        ("dirichlet_state", (ctypes.c_double * 5) * 2),
         ("dirichlet_x_switch", ctypes.c_double),
         ("teno_adaptive", ctypes.c_int),
         ("teno_a1", ctypes.c_double),
@@ -193,7 +193,7 @@ def make_plan_desc(plan):
         d.rk_b[s] = plan.rk_b[s]
     d.use_graphs = 1 if plan.use_graphs else 0
     d.Twall, d.SuthT, d.RefT = plan.Twall, plan.SuthT, plan.RefT
-    for v in range(4):
+    for v in range(len(plan.dirichlet_lo)):
         d.dirichlet_state[0][v] = plan.dirichlet_lo[v]
         d.dirichlet_state[1][v] = plan.dirichlet_hi[v]
     d.dirichlet_x_switch = plan.dirichlet_x_switch
@@ -358,9 +358,13 @@ class Solver:
         self.set_state64(np.stack([a[sl] for a in arrays]))
 
     def set_coordinate(self, x1, h=4):
-        """2D blocks stretched in x1: the x1 coordinate, FP64 [n1+2h][n0+2h]; evaluates the metrics."""
+        """Blocks stretched in x1: the x1 coordinate, FP64 [n1+2h][n0+2h] on 2D blocks, the line
+        [n1+2h] (x1 depends on j alone) on 3D wall-bounded blocks; evaluates the metrics."""
         x = torch.as_tensor(x1, dtype=torch.float64).to(self.device).contiguous()
-        self._check_shape(x, tuple(k + 2 * int(h) for k in self.shape), "coordinate")
+        if self.plan.ndim == 3:
+            self._check_shape(x, (self.plan.n[1] + 2 * int(h),), "coordinate line")
+        else:
+            self._check_shape(x, tuple(k + 2 * int(h) for k in self.shape), "coordinate")
         self._in()
         self._check(self.lib.osb_set_coordinate(self.ctx, 1, ctypes.c_void_p(x.data_ptr()), int(h)))
         x.record_stream(self.stream)

@@ -39,6 +39,7 @@ CASES = {
     "katzer_wenoz": "katzer_wenoz.py",
     "katzer_teno6": "katzer_teno6.py",
     "katzer_adaptive": "ref:apps/katzer_SBLI/katzer_SBLI.py",
+    "sbli3d_teno": "sbli3d_teno.py",
 }
 
 

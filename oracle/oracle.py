@@ -48,7 +48,7 @@ FILTER = {"none": 0, "weno5_constant": 1}
 
 
 def build(force=False):
-    srcs = [os.path.join(HERE, "src", f) for f in ("osb_oracle.c", "osb_oracle2d.c")]
+    srcs = [os.path.join(HERE, "src", f) for f in ("osb_oracle.c", "osb_oracle2d.c", "osb_oracle3w.c")]
     deps = srcs + [os.path.join(HERE, "src", "osb_oracle.h")]
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(f) for f in deps):
         return LIB
@@ -67,7 +67,7 @@ def lib():
     if _lib is None:
         _lib = ctypes.CDLL(build())
         for name in ("osbo_tgv_init", "osbo_run", "osbo_residual", "osbo_cutoff", "osbo2d_run", "osbo2d_metrics",
-                     "osbo2d_cutoff"):
+                     "osbo2d_cutoff", "osbo3w_run", "osbo3w_residual"):
             getattr(_lib, name).restype = ctypes.c_int
     return _lib
 
@@ -220,3 +220,71 @@ def metrics2d(plan):
     S = np.zeros_like(D)
     assert lib().osbo2d_metrics(ctypes.byref(c), _ptr(D), _ptr(S)) == 0
     return D, S
+
+
+class Cfg3W(ctypes.Structure):
+    _fields_ = [
+        ("n", ctypes.c_int * 3),
+        ("delta", ctypes.c_double * 3),
+        ("gama", ctypes.c_double),
+        ("Minf", ctypes.c_double),
+        ("Re", ctypes.c_double),
+        ("Pr", ctypes.c_double),
+        ("Twall", ctypes.c_double),
+        ("SuthT", ctypes.c_double),
+        ("RefT", ctypes.c_double),
+        ("teno_eps", ctypes.c_double),
+        ("teno_ct", ctypes.c_double),
+        ("Lx1", ctypes.c_double),
+        ("by", ctypes.c_double),
+        ("rkA", ctypes.c_double * 3),
+        ("rkB", ctypes.c_double * 3),
+        ("dt", ctypes.c_double),
+        ("closure", (ctypes.c_int * 2) * 2),
+        ("conv", ctypes.c_int),
+        ("dirichlet", (ctypes.c_double * 5) * 2),
+        ("x_switch", ctypes.c_double),
+    ]
+
+
+def make_cfg3w(plan):
+    """Oracle configuration from a 3D wall-bounded Plan (span-periodic x2; osb_oracle3w.c)."""
+    c = Cfg3W()
+    for d in range(3):
+        c.n[d] = plan.n[d]
+        c.delta[d] = plan.delta[d]
+    c.gama, c.Minf, c.Re, c.Pr = plan.gama, plan.Minf, plan.Re, plan.Pr
+    c.Twall, c.SuthT, c.RefT = plan.Twall, plan.SuthT, plan.RefT
+    c.teno_eps, c.teno_ct = plan.teno_eps, plan.teno_ct
+    c.Lx1, c.by = plan.Lx1, plan.by
+    for s in range(3):
+        c.rkA[s] = plan.rk_a[s]
+        c.rkB[s] = plan.rk_b[s]
+    c.dt = plan.dt
+    for d in range(2):
+        for side in range(2):
+            c.closure[d][side] = CLOSURES[plan.closure[d][side]]
+    c.conv = CONV[plan.conv]
+    for v in range(5):
+        c.dirichlet[0][v] = plan.dirichlet_lo[v]
+        c.dirichlet[1][v] = plan.dirichlet_hi[v]
+    c.x_switch = plan.dirichlet_x_switch
+    return c
+
+
+def run3w(plan, q0_padded, nsteps):
+    """q0_padded: FP64 [5][n2+8][n1+8][n0+8] with a 4-point halo.  Returns the state after nsteps."""
+    c = make_cfg3w(plan)
+    q = np.ascontiguousarray(q0_padded, dtype=np.float64).copy()
+    assert q.shape == (5, plan.n[2] + 8, plan.n[1] + 8, plan.n[0] + 8)
+    assert lib().osbo3w_run(ctypes.byref(c), _ptr(q), int(nsteps)) == 0
+    return q
+
+
+def residual3w(plan, q0_padded):
+    """Right-hand side [5][n2][n1][n0] of a padded FP64 state (boundary conditions applied first)."""
+    c = make_cfg3w(plan)
+    q = np.ascontiguousarray(q0_padded, dtype=np.float64)
+    r = np.zeros((5, plan.n[2], plan.n[1], plan.n[0]))
+    assert lib().osbo3w_residual(ctypes.byref(c), _ptr(q), _ptr(r)) == 0
+    return r

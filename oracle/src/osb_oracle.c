@@ -807,3 +807,8 @@ int osbo_run(const osbo_cfg *cfg, double *q, int nsteps, double *ke) {
 double osbo_side_weno5_plus(const double f[5], int z) { return weno5_plus(f, z); }
 double osbo_side_weno5_minus(const double g[5], int z) { return weno5_minus(g, z); }
 double osbo_side_teno6(const double g[6], int plus, double eps, double CT) { return teno6_side(g, plus, eps, CT); }
+double osbo_side_teno5(const double f[5], double eps, double CT) { return teno5_side(f, eps, CT); }
+void osbo_eigensystem3(int dir, double rho, double u0, double u1, double u2, double a, double g, double L[5][5],
+                       double R[5][5]) {
+  eigensystem(dir, rho, u0, u1, u2, a, g, L, R);
+}

@@ -78,6 +78,30 @@ typedef struct {
  * 4-point halo on every side (the initial state must fill the halos as the script's
  * initialisation kernel does); it is overwritten with the final state, halos included. */
 int osbo2d_run(const osbo2d_cfg *cfg, double *q, int nsteps);
+/* ---- 3D span-periodic wall-bounded path: the 2D configuration above with a periodic x2 axis ---- */
+typedef struct {
+  int n[3];          /* interior points in x0, x1, x2 */
+  double delta[3];   /* computational spacing: Delta0block0, Delta1block0, Delta2block0 */
+  double gama, Minf, Re, Pr, Twall, SuthT, RefT;
+  double teno_eps, teno_ct;
+  double Lx1, by;    /* x1 = Lx1 sinh(by delta1 j / Lx1) / sinh(by) */
+  double rkA[3], rkB[3];
+  double dt;
+  int closure[2][2]; /* [axis 0, 1][side]: 0 ReducedAccess, 1 Carpenter */
+  int conv;          /* OSBO_CONV_TENO5 (0 read as TENO5), OSBO_CONV_WENO5JS, OSBO_CONV_WENO5Z, OSBO_CONV_TENO6 */
+  /* Dirichlet face (x1 side 1): state[1] where x0 = delta0 i > x_switch, state[0] elsewhere;
+   * rho, rhou0, rhou1, rhou2, rhoE */
+  double dirichlet[2][5];
+  double x_switch;
+} osbo3w_cfg;
+
+/* Advance q by nsteps LS-RK3 steps.  q holds [5][n2+8][n1+8][n0+8] with a 4-point halo on every side
+ * (the initial state fills the halos as the script's initialisation kernel does); it is overwritten
+ * with the final state, halos included. */
+int osbo3w_run(const osbo3w_cfg *cfg, double *q, int nsteps);
+/* The right-hand side of q (boundary conditions applied first) on the interior, [5][n2][n1][n0]. */
+int osbo3w_residual(const osbo3w_cfg *cfg, const double *q, double *r);
+
 /* Metric terms D11 and SD111 on the interior, [n1][n0]. */
 int osbo2d_cutoff(const osbo2d_cfg *cfg, const double *q, double *ct);
 int osbo2d_metrics(const osbo2d_cfg *cfg, double *D11, double *SD111);

@@ -61,6 +61,14 @@ CASES_2D = {
 }
 VARS_2D = ["rho", "rhou0", "rhou1", "rhoE"]
 
+# span-periodic 3D wall-bounded case: grid (n0, n1, n2), steps, overrides.  The fixture keeps the
+# reference's initial and final states with a 4-point halo and the x1 coordinate line (x1 depends on
+# j alone) with a 4-point halo.
+CASES_3W = {
+    "sbli3d_teno": ((32, 24, 8), 10, {"dt": 0.02}),
+}
+VARS_3W = ["rho", "rhou0", "rhou1", "rhou2", "rhoE"]
+
 
 def padded4(d, names):
     # dumps carry a 5-point halo; keep 4
@@ -97,14 +105,50 @@ def main2d(ref, only=None):
         print("wrote", case, fin["rho"].shape)
 
 
+def main3w(ref, only=None):
+    import tempfile
+    for case, ((n0, n1, n2), steps, extra) in CASES_3W.items():
+        if only is not None and case != only:
+            continue
+        if not refrun.available(case):
+            subprocess.check_call([sys.executable, os.path.join(REPO, "oracle", "gen", "generate.py"), "--case", case,
+                                   "--ref", ref])
+        base = dict(block0np0=n0, block0np1=n1, block0np2=n2)
+        base.update(extra)
+        d0 = tempfile.mkdtemp(prefix="osb_g0_")
+        refrun.run(case, dict(base, niter=0), VARS_3W + ["x1"], threads=4, outdir=d0)
+        ic = {v: refrun.load_dump(os.path.join(d0, "opensbli_output.%s_B0.bin" % v), interior=False)[1:-1, 1:-1, 1:-1]
+              for v in VARS_3W + ["x1"]}
+        d1 = tempfile.mkdtemp(prefix="osb_g1_")
+        refrun.run(case, dict(base, niter=steps), VARS_3W, threads=4, outdir=d1)
+        fin = {v: refrun.load_dump(os.path.join(d1, "opensbli_output.%s_B0.bin" % v), interior=False)[1:-1, 1:-1, 1:-1]
+               for v in VARS_3W}
+        np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % case), q0=np.stack([ic[v] for v in VARS_3W]),
+                            x1=ic["x1"][4, :, 4], q=np.stack([fin[v] for v in VARS_3W]), n=np.array([n0, n1, n2]),
+                            steps=steps, params=json.dumps(dict(base, niter=steps)))
+        out = os.path.join("/tmp", "osb_lower_%s" % case)
+        r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case,
+                            "--out", out, "--ref", ref], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        if r.returncode == 0:
+            with open(os.path.join(out, "plan.json")) as f:
+                plan = json.load(f)
+            with open(os.path.join(HERE, "plan_%s.json" % case), "w") as f:
+                json.dump(plan, f, indent=1)
+        print("wrote", case, fin["rho"].shape, "plan" if r.returncode == 0 else "(no plan: lowering failed)")
+
+
 def main(ref=None, only=None):
     """Regenerate every fixture, or only the case `only`."""
     ref = ref or default_ref()
     if only is None:
         main2d(ref)
+        main3w(ref)
         katzer_profile(ref)
     elif only in CASES_2D:
         main2d(ref, only)
+        return
+    elif only in CASES_3W:
+        main3w(ref, only)
         return
     for case, (n, steps, extra) in CASES.items():
         if only is not None and case != only:

@@ -5,6 +5,7 @@ where the reference tree and its generated sources are present the oracle is als
 fresh run of that code at other sizes.
 """
 import math
+import os
 
 import numpy as np
 import pytest
@@ -152,3 +153,41 @@ def test_oracle_filter_changes_the_state():
     plan = golden_plan("tgv_filter", n=n).replace(Minf=params["Minf"])
     q_nf = O.run(oracle_cfg(plan.replace(filter="none"), dt=params["dt"]), O.tgv_init(oracle_cfg(plan)), steps)
     assert max(rel_err(q_nf, q_ref)) > 1e-6
+
+
+def test_oracle_wall3d_matches_reference_golden():
+    """The span-periodic 3D wall-bounded restatement (osb_oracle3w.c) against the reference's generated
+    code: TENO5, 32 x 24 x 8 from a spanwise-perturbed similarity profile, 10 steps."""
+    import json
+    from opensbli_gb300.plan import sbli3d_plan
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_sbli3d_teno.npz"))
+    n = tuple(int(x) for x in d["n"])
+    params = json.loads(str(d["params"]))
+    plan = sbli3d_plan(*n, dt=params["dt"])
+    q = O.run3w(plan, d["q0"], int(d["steps"]))
+    inner = (slice(None), slice(4, -4), slice(4, -4), slice(4, -4))
+    ref = d["q"][inner]
+    err = [float(np.abs(q[inner][v] - ref[v]).max() / np.abs(ref[v]).max()) for v in range(5)]
+    assert max(err) < 1e-12, err
+    # the state moved: a wrong restatement could not pass by standing still
+    assert max(float(np.abs(ref[v] - d["q0"][inner][v]).max()) for v in range(5)) > 1e-2
+
+
+def test_oracle_wall3d_matches_reference_run():
+    """A longer run on another grid against the generated code itself, where its sources are present."""
+    from opensbli_gb300.plan import sbli3d_plan
+    case = "sbli3d_teno"
+    if not refrun.available(case):
+        pytest.skip("generated reference sources for %s not present" % case)
+    import tempfile
+    V = ["rho", "rhou0", "rhou1", "rhou2", "rhoE"]
+    base = dict(block0np0=24, block0np1=20, block0np2=6, dt=0.02)
+    d0 = tempfile.mkdtemp(prefix="osb_w0_")
+    refrun.run(case, dict(base, niter=0), V, threads=2, outdir=d0)
+    q0 = np.stack([refrun.load_dump(os.path.join(d0, "opensbli_output.%s_B0.bin" % v), interior=False)[1:-1, 1:-1, 1:-1]
+                   for v in V])
+    fields, _ = refrun.run(case, dict(base, niter=12), V, threads=2)
+    ref = np.stack([fields[v] for v in V])
+    q = O.run3w(sbli3d_plan(24, 20, 6, dt=0.02), q0, 12)[:, 4:-4, 4:-4, 4:-4]
+    err = [float(np.abs(q[v] - ref[v]).max() / np.abs(ref[v]).max()) for v in range(5)]
+    assert max(err) < 1e-12, err
