@@ -62,7 +62,7 @@ def _interior(expr):
 
 class PhysicsCheck:
     """Evaluate the kernels of `components` (alg.prg walked in program order) against the built-in
-    formulas of a 3D block with constant viscosity or a 2D block stretched in x1 with Sutherland
+    formulas of a 3D block with constant viscosity, or a 2D or 3D block stretched in x1 with Sutherland
     viscosity."""
 
     def __init__(self, components, ndim, viscous, sutherland=False, metric=False, skew=False):
@@ -332,7 +332,7 @@ class PhysicsCheck:
                 return c
             if i == 1 and j == 1:
                 return D11 ** 2 * c + D11 * SD * key((f, (1,)))
-            if j == 1:
+            if 1 in (i, j):  # mixed with x1: D11 times the computational derivative
                 return D11 * c
             return c
 

@@ -3,9 +3,12 @@
     python -m opensbli_gb300.profile_case --n 192 --conv weno5js --precision mixed --steps 1 [--no-graphs]
         [--shape 1:march4:48 --shape 2:march4:48] [--central-ty 16] [--adaptive] [--filter]
     python -m opensbli_gb300.profile_case --katzer 512 [--conv teno5|teno6|weno5js|weno5z] [--adaptive]
+    python -m opensbli_gb300.profile_case --sbli3d 256 --n2 64 [--conv ...]
 
 Runs the Taylor-Green vortex (or, with --katzer N0, the 2D shock/boundary-layer block N0 x 256 from
-the boundary-layer profile in tests/golden/katzer_ic_n256.npz) with the given scheme and precision
+the boundary-layer profile in tests/golden/katzer_ic_n256.npz, or with --sbli3d N0 the span-periodic
+3D block N0 x 256 x n2 from the same profile with a spanwise momentum 0.05 sin(2 pi k / n2)) with
+the given scheme and precision
 for --steps RK3 steps after --warmup steps and prints the wall time per step (not a benchmark
 number: bench.py is).
 """
@@ -28,11 +31,34 @@ def main():
     ap.add_argument("--adaptive", action="store_true", help="TENO cut-off adapted by the modified Ducros sensor")
     ap.add_argument("--filter", action="store_true", help="WENO5 non-linear filter after every step")
     ap.add_argument("--katzer", type=int, default=0, help="2D shock/boundary-layer block of this many x0 points")
+    ap.add_argument("--sbli3d", type=int, default=0, help="3D span-periodic block of this many x0 points")
+    ap.add_argument("--n2", type=int, default=32, help="--sbli3d: points along the periodic x2 axis")
     a = ap.parse_args()
     import torch
     from .plan import tgv_plan, tgv_cfl_dt
     from .runtime import Solver
-    if a.katzer:
+    if a.sbli3d:
+        import os
+        import numpy as np
+        from .plan import sbli3d_plan
+        n0, n1, n2 = a.sbli3d, 256, a.n2
+        a.conv = a.conv or "teno5"
+        plan = sbli3d_plan(n0, n1, n2, precision=a.precision, conv=a.conv, dt=0.04, use_graphs=not a.no_graphs)
+        dt = 0.04
+        ic = np.load(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests", "golden",
+                                  "katzer_ic_n%d.npz" % n1))
+        col = ic["q_col"][:, 1:-1]  # 3-point halo in x1
+        q = np.zeros((5, n2 + 6, n1 + 6, n0 + 6))
+        w = 0.05 * np.sin(2 * np.pi * np.arange(-3, n2 + 3) / n2)
+        for v, src in ((0, 0), (1, 1), (2, 2), (4, 3)):
+            q[v] = col[src][None, :, None]
+        q[3] = w[:, None, None] * np.ones((1, n1 + 6, n0 + 6))
+        q[4] += 0.5 * q[3] ** 2 / q[0]
+        s = Solver(plan)
+        s.set_coordinate(ic["x1_col"], 4)
+        s.set_state64_padded(q, 3)
+        a.n = n0
+    elif a.katzer:
         import os
         import numpy as np
         from .plan import katzer_plan

@@ -98,7 +98,7 @@ class GB300Writer:
         names = [n or "" for n in self.kernel_names]
         self._check_kernel_families(names)
         ndim = self.block.ndim
-        if ndim == 2:
+        if ndim == 2 or (ndim == 3 and any(n.startswith("IsothermalWall boundary") for n in names)):
             return self._lower_2d(precision, use_graphs)
         if ndim != 3:
             raise NotImplementedError("GB300Writer lowers 2D and 3D blocks (got ndim=%d)" % ndim)
@@ -274,15 +274,19 @@ class GB300Writer:
     def _lower_2d(self, precision, use_graphs):
         """2D wall-bounded blocks (apps/katzer_SBLI/katzer_SBLI.py with a fixed TENO cut-off): metrics
         stretched in x1, LLFTeno(5) or LLFWeno(5), Central(4) viscous terms with Sutherland viscosity,
-        RungeKuttaLS(3), inlet/extrapolation faces in x0, isothermal wall/Dirichlet faces in x1."""
+        RungeKuttaLS(3), inlet/extrapolation faces in x0, isothermal wall/Dirichlet faces in x1; and
+        the same block in 3D with a periodic x2 axis (apps/transitional_SBLI/transitional_SBLI.py's
+        block without its body force)."""
         import sympy
         names = [n or "" for n in self.kernel_names]
+        nd = self.block.ndim
         if any(n.startswith("User kernel:") for n in names):
             raise NotImplementedError("the WENO filter is lowered on 3D blocks only")
         teno = self._kernels("LLFTeno_reconstruction_")
         weno = self._kernels("LLFWeno_reconstruction_")
-        if bool(teno) == bool(weno) or len(teno or weno) != 2:
-            raise NotImplementedError("2D blocks: one LLFTeno or LLFWeno reconstruction per direction expected")
+        if bool(teno) == bool(weno) or len(teno or weno) != nd:
+            raise NotImplementedError("wall-bounded blocks: one LLFTeno or LLFWeno reconstruction per direction "
+                                      "expected")
         conv = None
         for k in teno:
             lhs = self._lhs_names(k)
@@ -303,8 +307,8 @@ class GB300Writer:
                 raise NotImplementedError("mixed WENO formulations across directions")
             conv = kconv
         adaptive = self._adaptive_teno(teno) if teno else None
-        if adaptive is not None and conv != "teno5":
-            raise NotImplementedError("the adaptive cut-off is lowered for TENO5")
+        if adaptive is not None and (conv != "teno5" or nd != 2):
+            raise NotImplementedError("the adaptive cut-off is lowered for TENO5 on 2D wall-bounded blocks")
         if self._max_offset(teno or weno) != 3:
             raise NotImplementedError("5th-order reconstruction stencil expected")
         if not self._kernels("MetricsEquation") or not self._kernels("Metric boundary"):
@@ -326,7 +330,13 @@ class GB300Writer:
                 bcs[d][side] = kind
         if any(b is None for pair in bcs for b in pair):
             found = sorted(n for n in names if "boundary dir" in n)
-            raise NotImplementedError("2D boundary conditions: %s" % found)
+            raise NotImplementedError("wall-bounded boundary conditions: %s" % found)
+        if nd == 3:
+            # x2 periodic: the exchanges of both sides and no boundary kernel on that axis
+            per = {c.side for c in self.components if type(c).__name__ == "ExchangeSelf" and c.direction == 2}
+            other = [n for n in names if "boundary dir" in n and n not in faces and not n.startswith("Metric boundary")]
+            if per != {"left", "right"} or other:
+                raise NotImplementedError("3D wall-bounded blocks: periodic x2 expected (found %s)" % (other or per))
         closure = self._closures_2d()
         # the Dirichlet face: rho, rhou0, rhou1, rhoE = Piecewise((hi, x0 > xs), (lo, True))
         dk = self._kernels("Dirichlet boundary dir1 side1")[0]
@@ -340,17 +350,18 @@ class GB300Writer:
                     raise NotImplementedError("Dirichlet face: state switched by x0 > value expected")
                 xs = float(cond.rhs)
                 hi[name], lo[name] = float(vhi), float(vlo)
-            elif name in ("rho", "rhou0", "rhou1", "rhoE"):
+            elif name in ("rho", "rhou0", "rhou1", "rhou2", "rhoE"):
                 hi[name] = lo[name] = float(rhs)
-        order = ["rho", "rhou0", "rhou1", "rhoE"]
+        order = ["rho", "rhou0", "rhou1"] + (["rhou2"] if nd == 3 else []) + ["rhoE"]
         if any(v not in lo for v in order):
-            raise NotImplementedError("Dirichlet face must set rho, rhou0, rhou1, rhoE")
-        physics_check.check_algorithm(self.components, 2, viscous=True, sutherland=True, metric=True)
-        return Plan(ndim=2, n=(64, 32, 1), delta=(1.0, 1.0, 1.0), conv=conv,
+            raise NotImplementedError("Dirichlet face must set %s" % ", ".join(order))
+        physics_check.check_algorithm(self.components, nd, viscous=True, sutherland=True, metric=True)
+        return Plan(ndim=nd, n=(64, 32, 1) if nd == 2 else (64, 32, 16), delta=(1.0, 1.0, 1.0), conv=conv,
                     weno_eps=1e-14 if conv == "weno5z" else 1e-6,  # WenoZ.eps / WenoJS.eps (weno.py)
                     visc="sutherland", rk="ls_rk3", precision=precision,
                     bc=(tuple(bcs[0]), tuple(bcs[1]), ("periodic", "periodic")),
                     rk_a=coeff["rkA"], rk_b=coeff["rkB"], use_graphs=use_graphs, ic="host",
+                    name="wall3d" if nd == 3 else Plan.name,
                     dirichlet_lo=tuple(lo[v] for v in order), dirichlet_hi=tuple(hi[v] for v in order),
                     dirichlet_x_switch=xs if xs is not None else 1e300, kernels=[n for n in names if n],
                     teno_adaptive=adaptive is not None,
@@ -578,7 +589,7 @@ class GB300Writer:
         consts.update({"gama": p.gama, "Minf": p.Minf, "Re": p.Re, "Pr": p.Pr})
         for d in range(3):
             consts["Delta%dblock0" % d] = p.delta[d]
-        if nd == 2:
+        if p.rk == "ls_rk3":  # wall-bounded blocks (2D, or 3D with a periodic x2)
             consts.update({"Lx1": p.Lx1, "by": p.by, "Twall": p.Twall, "SuthT": p.SuthT, "RefT": p.RefT})
         out = {}
         for eq in k.equations:
@@ -688,6 +699,11 @@ class GB300Writer:
             s.set_coordinate(f["x1"], 4)
             s.set_state64_padded(np.stack([f[v] for v in self.state_names()]), 4)
             coords = {k: f[k][4:-4, 4:-4] for k in ("x0", "x1") if k in f}
+        elif self.plan.rk == "ls_rk3":  # 3D wall-bounded: x1 is a function of j alone
+            f = self.initial_fields(halo=3)
+            s.set_coordinate(f["x1"][3, :, 3], 3)
+            s.set_state64_padded(np.stack([f[v] for v in self.state_names()]), 3)
+            coords = {k: f[k][3:-3, 3:-3, 3:-3] for k in ("x0", "x1", "x2") if k in f}
         else:
             s.set_state64(self.initial_state())
         ios = self.io_requests() if output_dir is not None else []

@@ -18,7 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 
 
-def lower(case, ref, out, n=None):
+def lower(case, ref, out, n=None, params=None):
     sys.path.insert(0, HERE)
     sys.path.insert(0, ref)
     sys.path.insert(0, REPO)
@@ -63,6 +63,8 @@ def lower(case, ref, out, n=None):
         for d in range(3):
             if "block0np%d" % d in consts:
                 vals[consts.index("block0np%d" % d)] = str(n if d == 0 else (n // 2 if w.plan.ndim == 2 else n))
+    for k, v in (params or {}).items():
+        vals[consts.index(k)] = v
     w.substitute_simulation_parameters(consts, vals)
     with open(os.path.join(out, "plan.json"), "w") as f:
         f.write(w.plan.to_json())
@@ -87,6 +89,7 @@ if __name__ == "__main__":
     from refpath import default_ref
     ap.add_argument("--ref", default=default_ref())
     ap.add_argument("--n", type=int, default=None)
+    ap.add_argument("--params", default="", help="name=value,... overrides of the script's simulation parameters")
     a = ap.parse_args()
-    p = lower(a.case, a.ref, a.out, a.n)
+    p = lower(a.case, a.ref, a.out, a.n, dict(kv.split("=", 1) for kv in a.params.split(",") if kv))
     print(p.to_json())

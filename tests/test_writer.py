@@ -81,13 +81,43 @@ def test_3d_sensor_kernels_lower_to_adaptive_teno():
     assert not golden_plan("tgv_teno").teno_adaptive
 
 
+def test_3d_wall_script_lowers_to_the_span_periodic_plan():
+    """The 3D shock/boundary-layer script (periodic x2) lowers to the same plan as sbli3d_plan, and the
+    writer's numpy evaluation of its initialisation kernel reproduces the reference's initial state
+    (halos included) on the fixture's grid."""
+    from opensbli_gb300.plan import sbli3d_plan
+    g = golden_plan("sbli3d_teno")
+    p = sbli3d_plan(*g.n)
+    assert g.replace(kernels=[], name="", niter=None) == p.replace(kernels=[], name="")
+    assert g.bc[2] == ("periodic", "periodic") and g.dirichlet_hi[3] == 0.0
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
+def test_3d_wall_initial_state_matches_reference(tmp_path):
+    import json
+    r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", "sbli3d_teno",
+                        "--out", str(tmp_path), "--ref", REF, "--params", "block0np0=32,block0np1=24,block0np2=8"],
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-3000:]
+    d = np.load(os.path.join(GOLDEN, "ref_sbli3d_teno.npz"))
+    ic = np.load(tmp_path / "ic.npy")
+    ref = d["q0"][:, 4:-4, 4:-4, 4:-4]
+    assert ic.shape == ref.shape
+    # the profile is a 50-coefficient polynomial in x1: numpy's evaluation and the generated C's round
+    # differently, and the polynomial's cancellation amplifies that to ~1e-9
+    assert np.abs(ic - ref).max() <= 1e-8 * np.abs(ref).max(), float(np.abs(ic - ref).max())
+    # the spanwise momentum (exact trigonometric values) agrees to rounding
+    assert np.abs(ic[3] - ref[3]).max() <= 1e-15
+    assert json.load(open(tmp_path / "plan.json"))["n"] == [32, 24, 8]
+
+
 def test_writer_refuses_kernels_outside_the_lowered_families():
     """Extra equation classes add kernels to the time loop; lowering without them would change the
     solution, so the writer refuses every kernel it does not lower.  The WENO filter with the constant
     dissipation sensor is lowered; its Ducros variant adds a shock-sensor kernel and is refused."""
     from opensbli_gb300.writer import GB300Writer
     for case in ("tgv_central", "tgv_weno", "tgsym_central", "katzer_teno", "katzer_adaptive", "katzer_carpenter",
-                 "tgv_filter", "tgv_teno_adaptive"):
+                 "tgv_filter", "tgv_teno_adaptive", "sbli3d_teno"):
         GB300Writer._check_kernel_families(golden_plan(case).kernels)
     assert "User kernel: Non-linear filter application" in golden_plan("tgv_filter").kernels
     names = golden_plan("tgv_filter").kernels + ["User kernel: Shock sensor"]
@@ -114,7 +144,8 @@ def test_cfl_dt_tgv_weno():
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
 @pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central",
                                   "katzer_teno", "katzer_adaptive", "katzer_carpenter", "tgv_filter",
-                                  "katzer_weno", "katzer_wenoz", "katzer_teno6", "tgv_teno_adaptive"])
+                                  "katzer_weno", "katzer_wenoz", "katzer_teno6", "tgv_teno_adaptive",
+                                  "sbli3d_teno"])
 def test_writer_lowers_reference_script(case, tmp_path):
     r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case, "--out",
                         str(tmp_path), "--ref", REF], capture_output=True, text=True, timeout=900)
