@@ -100,6 +100,10 @@ typedef struct osb_plan_desc {
    * on the interior (0 elsewhere).  teno_adaptive = 0 keeps the fixed teno_ct. */
   int teno_adaptive;
   double teno_a1, teno_a2, sensor_eps;
+  /* mixed precision on 2D blocks: an interface whose two points' pressures differ by more than this
+   * factor (a strong shock) forms its Roe average, eigenvectors and characteristic reconstruction in
+   * FP64 arithmetic; 0 keeps every interface in FP32.  Ignored by FP64 plans and by 3D blocks. */
+  double shock_fp64;
   /* OSB_CLOSURE_* per axis and side of a 2D block (x0, x1; the third row is unused) */
   int closure[3][2];
   /* OSB_FILTER_*: 3D blocks with periodic or symmetry faces (no wall faces, so the filter's Wall

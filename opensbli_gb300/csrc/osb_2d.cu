@@ -530,21 +530,27 @@ __device__ __forceinline__ void flux2(const W2<T> (&W)[6], T gama, T eps, T ct, 
 // one) and the splitting is linear, so projecting Q_t - Q_i and F_t - F_i gives LEV.(F^ - F_i) and
 // REV maps it to G = F_{i+1/2} - F_i.  dF[t][v] = F_t - F_i from the double-float point fluxes.
 // Returns G; the caller differences (F_i - F_{i-1}) + (G_i - G_{i-1}).
-template <int D, int SCH>
-__device__ __forceinline__ void flux2_delta(const W2<float> (&W)[6], const float (&dF)[6][4], float gama, float eps,
-                                            float ct, float out[4]) {
-  using T = float;
+// T = double: the same flux in FP64 arithmetic on the window's FP32 values (next to strong shocks),
+// rounded to FP32 once.
+template <typename T, int D, int SCH>
+__device__ __forceinline__ void flux2_delta(const W2<float> (&W)[6], const float (&dFf)[6][4], T gama, T eps, T ct,
+                                            float out[4]) {
+  T dF[6][4];
+#pragma unroll
+  for (int t = 0; t < 6; ++t)
+#pragma unroll
+    for (int v = 0; v < 4; ++v) dF[t][v] = T(dFf[t][v]);
   constexpr int E = 1 - D;
   const T s = D == 0 ? T(1) : T(-1);
   const T gm1 = gama - T(1);
-  const T rl = W[2].Q[0], rr = W[3].Q[0];
+  const T rl = T(W[2].Q[0]), rr = T(W[3].Q[0]);
   const T sl = sqrt_t(rl), sr = sqrt_t(rr);
   const T rho = sqrt_t(rl * rr);
   const T inv_s = T(1) / (sl + sr);
   T u[2];
 #pragma unroll
-  for (int c = 0; c < 2; ++c) u[c] = inv_s * (sl * (W[2].Q[1 + c] / rl) + sr * (W[3].Q[1 + c] / rr));
-  const T Hh = inv_s * ((W[2].p + W[2].Q[3]) / sl + (W[3].p + W[3].Q[3]) / sr);
+  for (int c = 0; c < 2; ++c) u[c] = inv_s * (sl * (T(W[2].Q[1 + c]) / rl) + sr * (T(W[3].Q[1 + c]) / rr));
+  const T Hh = inv_s * ((T(W[2].p) + T(W[2].Q[3])) / sl + (T(W[3].p) + T(W[3].Q[3])) / sr);
   const T usq = u[0] * u[0] + u[1] * u[1];
   const T a = sqrt_t(gm1 * (Hh - T(0.5) * usq));
   const T ia = T(1) / a, irho = T(1) / rho;
@@ -554,9 +560,9 @@ __device__ __forceinline__ void flux2_delta(const W2<float> (&W)[6], const float
   T lu = T(0), lp = T(0), lm = T(0);
 #pragma unroll
   for (int t = 0; t < 6; ++t) {
-    lu = max_t(lu, abs_t(W[t].ud));
-    lp = max_t(lp, abs_t(W[t].ud + W[t].a));
-    lm = max_t(lm, abs_t(W[t].a - W[t].ud));
+    lu = max_t(lu, abs_t(T(W[t].ud)));
+    lp = max_t(lp, abs_t(T(W[t].ud) + T(W[t].a)));
+    lm = max_t(lm, abs_t(T(W[t].a) - T(W[t].ud)));
   }
   auto recon = [&](const T (&cf)[6], const T (&cs)[6], T lam) -> T {
     T fp[6], fm[6];
@@ -567,7 +573,7 @@ __device__ __forceinline__ void flux2_delta(const W2<float> (&W)[6], const float
     }
     return recon2<T, SCH>(fp, fm, eps, ct);
   };
-  auto dQ = [&](int t, int v) -> T { return t == 2 ? T(0) : W[t].Q[v] - W[2].Q[v]; };
+  auto dQ = [&](int t, int v) -> T { return t == 2 ? T(0) : T(W[t].Q[v]) - T(W[2].Q[v]); };
   T r0, r1, r2, r3;
   {
     T cf[6], cs[6];
@@ -606,12 +612,15 @@ __device__ __forceinline__ void flux2_delta(const W2<float> (&W)[6], const float
   }
   const T sac = r2 + r3, dac = r2 - r3;
   const T hh = (phi + a * a) / gm1;
-  out[0] = r0 + al * sac;
+  T G[4];
+  G[0] = r0 + al * sac;
 #pragma unroll
-  for (int c = 0; c < 2; ++c) out[1 + c] = u[c] * r0 + al * (u[c] * sac + (c == D ? a * dac : T(0)));
-  out[3] = (phi / gm1) * r0 + al * (hh * sac + u[D] * a * dac);
-  out[1 + E] -= s * rho * r1;
-  out[3] -= s * rho * u[E] * r1;
+  for (int c = 0; c < 2; ++c) G[1 + c] = u[c] * r0 + al * (u[c] * sac + (c == D ? a * dac : T(0)));
+  G[3] = (phi / gm1) * r0 + al * (hh * sac + u[D] * a * dac);
+  G[1 + E] -= s * rho * r1;
+  G[3] -= s * rho * u[E] * r1;
+#pragma unroll
+  for (int v = 0; v < 4; ++v) out[v] = float(G[v]);
 }
 
 template <int D> struct T2Tile;
@@ -621,10 +630,13 @@ template <> struct T2Tile<1> { static constexpr int TI = 24, TA = 16; };  // sta
 // Interface fluxes along D for a tile and the flux difference -(F_i - F_{i-1})/delta (times D11 for
 // x1), written into this direction's residual array.  TENO's cut-off is ct_d, or with ctp set the
 // per-point value at the interface's left point.
-template <typename T, int D, int SCH>
+// SH (FP32 only): interfaces next to strong shocks (pressure ratio of points i, i+1 above `shock`)
+// form their flux in FP64 arithmetic; a separate instantiation, since the FP64 path raises the
+// kernel's registers from ~94 to ~160 and halves the resident blocks.
+template <typename T, int D, int SCH, bool SH = false>
 __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<const T> pr, const double *D11,
                                                Q4T<T> res, double gama_d, double eps_d, double ct_d, double inv_dd,
-                                               const T *ctp) {
+                                               const T *ctp, double shock) {
   using Tl = T2Tile<D>;
   constexpr int TI = Tl::TI, TA = Tl::TA, NPT = TI + 5;
   constexpr int NF = s2nf<T>();
@@ -701,7 +713,16 @@ __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<con
           dF[k][v] = k == 2 ? 0.0f
                             : __fsub_rn(sf[S2_FH + v][m + k][a], sf[S2_FH + v][m + 2][a]) +
                                   __fsub_rn(sf[S2_FL + v][m + k][a], sf[S2_FL + v][m + 2][a]);
-      flux2_delta<D, SCH>(W, dF, gama, eps, ctl, fl);
+      bool fp64 = false;
+      if constexpr (SH) {
+        const float pl = W[2].p, pr = W[3].p;
+        fp64 = fmaxf(pl, pr) > (float)shock * fminf(pl, pr);
+      }
+      if (fp64) {
+        if constexpr (SH) flux2_delta<double, D, SCH>(W, dF, gama_d, eps_d, ctp ? (double)ctl : ct_d, fl);
+      } else {
+        flux2_delta<float, D, SCH>(W, dF, gama, eps, ctl, fl);
+      }
 #pragma unroll
       for (int v = 0; v < 4; ++v) sdf[v][m][a] = -dF[1][v];  // F(point i) - F(point i-1)
     } else {
@@ -962,14 +983,19 @@ static void launch2_flux(const Ctx &c, dim3 grid, Q4T<const T> q, Prims<const T>
                          const T *ctp, cudaStream_t s) {
   const osb_plan_desc &p = c.plan;
   const double idd = 1.0 / p.delta[D];
+  // the FP64-next-to-shocks instantiation when the plan asks for it (FP32 state only)
+  const bool sh = sizeof(T) == 4 && p.shock_fp64 > 0.0;
+  auto launch = [&](auto plain, auto shock) {
+    (sh ? shock : plain)<<<grid, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, idd, ctp, p.shock_fp64);
+  };
   if (p.conv == OSB_CONV_TENO5)
-    k2_flux<T, D, SCH_TENO><<<grid, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, idd, ctp);
+    launch(k2_flux<T, D, SCH_TENO, false>, k2_flux<T, D, SCH_TENO, sizeof(T) == 4>);
   else if (p.conv == OSB_CONV_TENO6)
-    k2_flux<T, D, SCH_TENO6><<<grid, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, idd, ctp);
+    launch(k2_flux<T, D, SCH_TENO6, false>, k2_flux<T, D, SCH_TENO6, sizeof(T) == 4>);
   else if (p.conv == OSB_CONV_WENO5Z)
-    k2_flux<T, D, SCH_Z><<<grid, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, idd, ctp);
+    launch(k2_flux<T, D, SCH_Z, false>, k2_flux<T, D, SCH_Z, sizeof(T) == 4>);
   else
-    k2_flux<T, D, SCH_JS><<<grid, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, idd, ctp);
+    launch(k2_flux<T, D, SCH_JS, false>, k2_flux<T, D, SCH_JS, sizeof(T) == 4>);
 }
 
 template <typename T> void launch2_rhs(const Ctx &c, int update, double A, double B, double dt, cudaStream_t s,

@@ -44,6 +44,10 @@ bool char_fluxes(const osb_plan_desc &p) {
 int validate(const osb_plan_desc *p, char *why, size_t n) {
   if (!p) { snprintf(why, n, "null plan"); return OSB_EINVAL; }
   if (p->abi_version != OSB_ABI_VERSION) { snprintf(why, n, "abi_version %d != %d", p->abi_version, OSB_ABI_VERSION); return OSB_EINVAL; }
+  if (!(p->shock_fp64 == 0.0 || (p->shock_fp64 >= 1.0 && std::isfinite(p->shock_fp64)))) {
+    snprintf(why, n, "shock_fp64 = %g: 0 (off) or a pressure ratio >= 1", p->shock_fp64);
+    return OSB_EINVAL;
+  }
   if (p->ndim == 2) {
     for (int d = 0; d < 2; ++d) {
       if (p->n[d] < 8 || p->n[d] > 16384) { snprintf(why, n, "n[%d] = %d out of range [8, 16384]", d, p->n[d]); return OSB_EINVAL; }

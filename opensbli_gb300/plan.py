@@ -58,6 +58,9 @@ class Plan:
     teno_a1: float = 10.5
     teno_a2: float = 4.5
     sensor_eps: float = 1e-12
+    # mixed precision on 2D blocks: interfaces whose two points' pressures differ by more than this
+    # factor (strong shocks) form their characteristic flux in FP64 arithmetic; 0 keeps all in FP32
+    shock_fp64: float = 0.0
     rk_a: Tuple[float, float, float] = RK3_RKOLD
     rk_b: Tuple[float, float, float] = RK3_RKNEW
     use_graphs: bool = True

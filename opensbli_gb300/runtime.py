@@ -64,6 +64,7 @@ class PlanDesc(ctypes.Structure):
         ("teno_a1", ctypes.c_double),
         ("teno_a2", ctypes.c_double),
         ("sensor_eps", ctypes.c_double),
+        ("shock_fp64", ctypes.c_double),
         ("closure", (ctypes.c_int * 2) * 3),
         ("filter", ctypes.c_int),
         ("filter_control", ctypes.c_double),
@@ -199,6 +200,7 @@ def make_plan_desc(plan):
     d.dirichlet_x_switch = plan.dirichlet_x_switch
     d.teno_adaptive = 1 if plan.teno_adaptive else 0
     d.teno_a1, d.teno_a2, d.sensor_eps = plan.teno_a1, plan.teno_a2, plan.sensor_eps
+    d.shock_fp64 = plan.shock_fp64
     for a in range(len(plan.closure)):
         for side in range(2):
             d.closure[a][side] = CLOSURE[plan.closure[a][side]]
