@@ -104,6 +104,12 @@ typedef struct osb_plan_desc {
    * factor (a strong shock) forms its Roe average, eigenvectors and characteristic reconstruction in
    * FP64 arithmetic; 0 keeps every interface in FP32.  Ignored by FP64 plans and by 3D blocks. */
   double shock_fp64;
+  /* 3D wall-bounded blocks (apps/transitional_SBLI/transitional_SBLI.py): dirichlet_ke = 1 makes the
+   * Dirichlet face keep rhou2 and set rhoE = dirichlet_state[.][4] + rhou2^2/(2 rho); body_force =
+   * (A, xF, yF, bta, omega) adds BF = A exp(-((x0-xF)^2 + (x1-yF)^2)) cos(bta x2) sin(omega dt iter)
+   * to the continuity equation, iter counting the steps the context has taken (A = 0: none). */
+  int dirichlet_ke;
+  double body_force[5];
   /* OSB_CLOSURE_* per axis and side of a 2D block (x0, x1; the third row is unused) */
   int closure[3][2];
   /* OSB_FILTER_*: 3D blocks with periodic or symmetry faces (no wall faces, so the filter's Wall

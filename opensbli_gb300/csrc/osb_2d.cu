@@ -1133,6 +1133,7 @@ __global__ void __launch_bounds__(256) k3w_metrics(int n1, const double *x1, dou
 struct BC3Args {
   double gama, Minf, Twall, delta0, xs;
   double lo[5], hi[5];
+  int ke;  // Dirichlet face keeps rhou2 and sets rhoE = state + rhou2^2/(2 rho)
 };
 
 __device__ __forceinline__ void bc3_row(const Grid &g, const Q5 &q, const BC3Args &a, int j, int k) {
@@ -1181,8 +1182,16 @@ __device__ __forceinline__ void bc3_col(const Grid &g, const Q5 &q, const BC3Arg
     q.v[3][w] = 0.0;
     q.v[4][w] = ew;
     const double x0 = a.delta0 * i;  // Dirichlet top face
-    for (int j = g.n1 - 1; j < g.n1 + HY; ++j)
-      for (int v = 0; v < 5; ++v) q.v[v][gidx(g, i, j, k)] = x0 > a.xs ? a.hi[v] : a.lo[v];
+    const double *st = x0 > a.xs ? a.hi : a.lo;
+    for (int j = g.n1 - 1; j < g.n1 + HY; ++j) {
+      const int64_t m = gidx(g, i, j, k);
+      if (a.ke) {  // rho, rhou0, rhou1 set; rhoE from the face's rho and the local rhou2
+        for (int v = 0; v < 3; ++v) q.v[v][m] = st[v];
+        q.v[4][m] = st[4] + 0.5 * (q.v[3][m] * q.v[3][m]) / q.v[0][m];
+      } else {
+        for (int v = 0; v < 5; ++v) q.v[v][m] = st[v];
+      }
+    }
   }
 }
 
@@ -1339,9 +1348,15 @@ __global__ void __launch_bounds__(V2X * V2Y) k3w_visc(Grid g, Q5T<const T> q, co
 
 // R = fluxes + viscous terms at every interior point, then the LS-RK3 update of the FP64 master
 // (update = 1), or R itself into du (update = 0)
+// body force of the continuity equation: bf_xy[j][i] = A exp(-((x0-xF)^2 + (x1-yF)^2)), bf_z[k] =
+// cos(bta x2), *bf_t = sin(omega dt iter) of the current step (null bf_xy: none)
+struct BF3 {
+  const double *xy, *z, *t;
+};
+
 template <typename T>
 __global__ void k3w_rk(Grid g, Q5T<const T> rf, Q5T<const T> rv, Q5 du, Q5 q64, double dt, double A, double B,
-                       int update) {
+                       int update, BF3 bf) {
   const int64_t N = (int64_t)g.n0 * g.n1 * g.n2;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(t % g.n0), j = (int)((t / g.n0) % g.n1), k = (int)(t / ((int64_t)g.n0 * g.n1));
@@ -1351,6 +1366,7 @@ __global__ void k3w_rk(Grid g, Q5T<const T> rf, Q5T<const T> rv, Q5 du, Q5 q64, 
     for (int v = 0; v < 5; ++v) R[v] = rf.v[v][c];
 #pragma unroll
     for (int v = 1; v < 5; ++v) R[v] += rv.v[v - 1][c];
+    if (bf.xy) R[0] += T(bf.xy[(int64_t)j * g.n0 + i] * bf.z[k] * bf.t[0]);
     if (update) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
@@ -1362,6 +1378,68 @@ __global__ void k3w_rk(Grid g, Q5T<const T> rf, Q5T<const T> rv, Q5 du, Q5 q64, 
 #pragma unroll
       for (int v = 0; v < 5; ++v) du.v[v][c] = to_f64(R[v]);
     }
+  }
+}
+
+// Modified Ducros sensor of a wall-bounded block (shock_sensors.py:12-49 with the metric, as
+// generated for transitional_SBLI.py) and the adaptive TENO cut-off (teno.py:430-443) over the
+// points [-1, n_d] of every axis: on the interior, u_i = rhou_i/rho with the x0 and x1 closures and
+// d/dx1 = D11 d/dxi1, theta = (1/2 - 1/2 tanh(250 div + 2.5)) div^2 / (eps + |curl u|^2 + div^2);
+// theta = 0 elsewhere; C_T = 10^-floor(a1 - a2 (1 - (1 - theta)^4 (1 + 4 theta))) from the table of
+// correctly rounded powers (FP64 exponent, as the 2D kernel).
+template <typename T>
+__global__ void k3w_sensor(Grid g, Q5T<const T> q, const double *D11, T *ct, Sensor2Args sa, double inv_d2) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x - 1, j = blockIdx.y * blockDim.y + threadIdx.y - 1;
+  const int k = (int)blockIdx.z - 1;
+  if (i > g.n0 || j > g.n1) return;
+  const int64_t n = gidx(g, i, j, k);
+  double th = 0.0;
+  if (i >= 0 && i < g.n0 && j >= 0 && j < g.n1 && k >= 0 && k < g.n2) {
+    auto U = [&](int c, int di, int dj, int dk) {
+      const int64_t m = gidx(g, i + di, j + dj, k + dk);
+      return q.v[1 + c][m] / q.v[0][m];
+    };
+    const T id0 = T(sa.inv_d0), id1 = T(sa.inv_d1), id2 = T(inv_d2), Dm = T(D11[j]);
+    T du[3][3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      du[c][0] = id0 * d1c<T>([&](int o) { return U(c, o, 0, 0); }, i, g.n0, sa.clx);
+      du[c][1] = Dm * (id1 * d1c<T>([&](int o) { return U(c, 0, o, 0); }, j, g.n1, sa.cly));
+      du[c][2] = id2 * (T(1.0 / 12.0) * U(c, 0, 0, -2) - T(2.0 / 3.0) * U(c, 0, 0, -1) +
+                        T(2.0 / 3.0) * U(c, 0, 0, 1) - T(1.0 / 12.0) * U(c, 0, 0, 2));
+    }
+    const T div = du[0][0] + du[1][1] + du[2][2];
+    const T w0 = du[2][1] - du[1][2], w1 = du[0][2] - du[2][0], w2 = du[1][0] - du[0][1];
+    const T sw = T(0.5) - T(0.5) * tanh_t(T(250) * div + T(2.5));
+    th = (double)(sw * (div * div) / (T(sa.eps) + w0 * w0 + w1 * w1 + w2 * w2 + div * div));
+  }
+  const double w = 1.0 - th;
+  const double e = floor(sa.a1 - sa.a2 * (1.0 - (w * w) * (w * w) * (4.0 * th + 1.0)));
+  ct[n] = T((e >= 0.0 && e <= 22.0) ? c_p10n[(int)e] : pow(10.0, -e));
+}
+
+// the body-force tables of a block (once, after the coordinates): bf_xy and bf_z
+__global__ void k3w_bf_tables(Grid g, const double *x1, double delta0, double delta2, double A, double xF, double yF,
+                              double bta, double *xy, double *z) {
+  const int64_t N = (int64_t)g.n0 * g.n1;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N + g.n2; t += (int64_t)gridDim.x * blockDim.x) {
+    if (t < N) {
+      const int i = (int)(t % g.n0), j = (int)(t / g.n0);
+      const double x0 = delta0 * i, y = x1[j];
+      xy[t] = A * exp(-(x0 - xF) * (x0 - xF) - (y - yF) * (y - yF));
+    } else {
+      const int k = (int)(t - N);
+      z[k] = cos(bta * (delta2 * k));
+    }
+  }
+}
+
+// the body force's time factor sin(omega dt iter) at the start of a step (advance = 0), the step
+// count at its end (advance = 1)
+__global__ void k3w_tick(long long *iter, double *t, double omega_dt, int advance) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    if (advance) ++iter[0];
+    else t[0] = sin(omega_dt * (double)iter[0]);
   }
 }
 
@@ -1395,6 +1473,7 @@ template <typename T> void launch3w_bcs(const Ctx &c, cudaStream_t s, int64_t *l
     a.lo[v] = p.dirichlet_state[0][v];
     a.hi[v] = p.dirichlet_state[1][v];
   }
+  a.ke = p.dirichlet_ke;
   const int rows = c.g.n1 - 5 > 0 ? c.g.n1 - 5 : 0, cols = c.g.n0 - 3 > 0 ? c.g.n0 - 3 : 0;
   const int row_blocks = (rows + BC2_THREADS - 1) / BC2_THREADS;
   const int col_blocks = (3 * cols + BC2_THREADS - 1) / BC2_THREADS;
@@ -1419,6 +1498,13 @@ void launch3w_rhs(const Ctx &c, int update, double A, double B, double dt, cudaS
     q.v[v] = static_cast<const T *>(c.qa[v]);
     r.v[v] = static_cast<T *>(c.res[v]);
   }
+  if (p.teno_adaptive) {  // the cut-off of every interface from the sensor of the working state
+    Sensor2Args sa{1.0 / p.delta[0], 1.0 / p.delta[1], p.teno_a1, p.teno_a2, p.sensor_eps, closure_bits(p, 0),
+                   closure_bits(p, 1)};
+    dim3 b(32, 8), gs((c.g.n0 + 2 + 31) / 32, (c.g.n1 + 2 + 7) / 8, c.g.n2 + 2);
+    k3w_sensor<T><<<gs, b, 0, s>>>(c.g, q5t<const T>(c.qa), c.d11, static_cast<T *>(c.ct2), sa, 1.0 / p.delta[2]);
+    ++*launches;
+  }
   cudaEventRecord(c.ev_fork2, s);
   cudaStreamWaitEvent(c.side2[1], c.ev_fork2, 0);
   for (int d = 0; d < 3; ++d) launch_weno_dir<T>(c, q, r, d, s, launches);
@@ -1440,9 +1526,52 @@ void launch3w_rhs(const Ctx &c, int update, double A, double B, double dt, cudaS
   Q5T<const T> rvc{{rv.v[0], rv.v[1], rv.v[2], rv.v[3], nullptr}};
   int nb = (int)(((int64_t)c.g.n0 * c.g.n1 * c.g.n2 + 255) / 256);
   if (nb > c.num_sms * 8) nb = c.num_sms * 8;
-  k3w_rk<T><<<nb, 256, 0, s>>>(c.g, rf, rvc, q5(c.du2), q5(c.qold), dt, A, B, update);
+  const BF3 bf{c.bf_xy, c.bf_z, c.bf_t};
+  k3w_rk<T><<<nb, 256, 0, s>>>(c.g, rf, rvc, q5(c.du2), q5(c.qold), dt, A, B, update, bf);
   *launches += 2;
 }
+
+void launch3w_bf_tables(const Ctx &c, cudaStream_t s, int64_t *launches) {
+  if (!c.bf_xy) return;
+  const osb_plan_desc &p = c.plan;
+  const int64_t N = (int64_t)c.g.n0 * c.g.n1 + c.g.n2;
+  int nb = (int)((N + 255) / 256);
+  if (nb > c.num_sms * 8) nb = c.num_sms * 8;
+  k3w_bf_tables<<<nb, 256, 0, s>>>(c.g, c.x1, p.delta[0], p.delta[2], p.body_force[0], p.body_force[1],
+                                   p.body_force[2], p.body_force[3], c.bf_xy, c.bf_z);
+  ++*launches;
+}
+
+// advance = 0: the time factor of the current step (start of a step); 1: count the step (its end)
+void launch3w_tick(const Ctx &c, int advance, double dt, cudaStream_t s, int64_t *launches) {
+  if (!c.bf_xy) return;
+  k3w_tick<<<1, 32, 0, s>>>(c.d_iter, c.bf_t, c.plan.body_force[4] * dt, advance);
+  ++*launches;
+}
+
+// the adaptive cut-off of the current state over the interior, FP64 [z][y][x]
+template <typename T> __global__ void k3w_pack_ct(Grid g, const T *ct, double *out) {
+  const int64_t N = (int64_t)g.n0 * g.n1 * g.n2;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(t % g.n0), j = (int)((t / g.n0) % g.n1), k = (int)(t / ((int64_t)g.n0 * g.n1));
+    out[t] = (double)ct[gidx(g, i, j, k)];
+  }
+}
+
+template <typename T> void launch3w_cutoff(const Ctx &c, double *out, cudaStream_t s, int64_t *launches) {
+  const osb_plan_desc &p = c.plan;
+  launch3w_bcs<T>(c, s, launches);
+  Sensor2Args sa{1.0 / p.delta[0], 1.0 / p.delta[1], p.teno_a1, p.teno_a2, p.sensor_eps, closure_bits(p, 0),
+                 closure_bits(p, 1)};
+  dim3 b(32, 8), gs((c.g.n0 + 2 + 31) / 32, (c.g.n1 + 2 + 7) / 8, c.g.n2 + 2);
+  k3w_sensor<T><<<gs, b, 0, s>>>(c.g, q5t<const T>(c.qa), c.d11, static_cast<T *>(c.ct2), sa, 1.0 / p.delta[2]);
+  int nb = (int)(((int64_t)c.g.n0 * c.g.n1 * c.g.n2 + 255) / 256);
+  if (nb > c.num_sms * 8) nb = c.num_sms * 8;
+  k3w_pack_ct<T><<<nb, 256, 0, s>>>(c.g, static_cast<const T *>(c.ct2), out);
+  *launches += 2;
+}
+template void launch3w_cutoff<float>(const Ctx &, double *, cudaStream_t, int64_t *);
+template void launch3w_cutoff<double>(const Ctx &, double *, cudaStream_t, int64_t *);
 
 template <typename T> void setup3w() {
   cudaFuncSetAttribute(k3w_visc<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)visc3_smem<T>());

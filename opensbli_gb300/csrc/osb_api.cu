@@ -103,7 +103,14 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
       snprintf(why, n, "3D wall-bounded blocks: TENO5, TENO6, WENO5-JS or WENO5-Z fluxes");
       return OSB_EUNSUPPORTED;
     }
-    if (p->teno_adaptive) { snprintf(why, n, "3D wall-bounded blocks: fixed TENO cut-off"); return OSB_EUNSUPPORTED; }
+    if (p->teno_adaptive && ((p->conv != OSB_CONV_TENO5 && p->conv != OSB_CONV_TENO6) || !(p->sensor_eps >= 0) ||
+                             !std::isfinite(p->teno_a1) || !std::isfinite(p->teno_a2))) {
+      snprintf(why, n, "adaptive TENO: TENO5 or TENO6, sensor_eps >= 0 and finite teno_a1, teno_a2");
+      return OSB_EINVAL;
+    }
+    for (int k = 0; k < 5; ++k)
+      if (!std::isfinite(p->body_force[k])) { snprintf(why, n, "body_force[%d] must be finite", k); return OSB_EINVAL; }
+    if (p->dirichlet_ke != 0 && p->dirichlet_ke != 1) { snprintf(why, n, "dirichlet_ke: 0 or 1"); return OSB_EINVAL; }
     if (p->filter != OSB_FILTER_NONE) { snprintf(why, n, "3D wall-bounded blocks: no WENO filter"); return OSB_EUNSUPPORTED; }
     for (int d = 0; d < 2; ++d)
       for (int side = 0; side < 2; ++side)
@@ -495,6 +502,7 @@ template <typename T> int step_impl(osb_ctx *c, int nsteps, double dt) {
 // then per stage the right-hand side with the update du = A du + dt R, q += B du on the FP64 master
 // and the face conditions again (algorithm.py:384-477).
 template <typename T> void one_step3w(osb_ctx *c, double dt, cudaStream_t s) {
+  launch3w_tick(*c, 0, dt, s, &c->launches);  // body force: sin(omega dt iter) of this step
   {
     ProfScope ps(c, PF_HALO, s);
     launch3w_bcs<T>(*c, s, &c->launches);
@@ -507,6 +515,7 @@ template <typename T> void one_step3w(osb_ctx *c, double dt, cudaStream_t s) {
     ProfScope ps(c, PF_HALO, s);
     launch3w_bcs<T>(*c, s, &c->launches);
   }
+  launch3w_tick(*c, 1, dt, s, &c->launches);
 }
 
 template <typename T> int step3w_impl(osb_ctx *c, int nsteps, double dt) {
@@ -756,6 +765,7 @@ int osb_set_coordinate(osb_ctx *c, int axis, const double *src, int h) {
     if (e != cudaSuccess) return cuda_err(c, e, "osb_set_coordinate");
     int64_t l = 0;
     launch3w_metrics(*c, c->x1, c->stream, &l);
+    launch3w_bf_tables(*c, c->stream, &l);
     c->metrics_valid = 1;
     return cuda_err(c, cudaGetLastError(), "osb_set_coordinate");
   }
@@ -900,6 +910,16 @@ int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->ev_fork2, cudaEventDisableTiming);
     c->ph.ysc_d = c->ysc_d;
     c->ph.ysc_f = c->ysc_f;
+    if (e == cudaSuccess && plan->body_force[0] != 0.0) {
+      e = cudaMalloc(&c->bf_xy, (size_t)c->g.n0 * c->g.n1 * sizeof(double));
+      if (e == cudaSuccess) e = cudaMalloc(&c->bf_z, (size_t)c->g.n2 * sizeof(double));
+      if (e == cudaSuccess) e = cudaMalloc(&c->bf_t, sizeof(double));
+      if (e == cudaSuccess) e = cudaMalloc(&c->d_iter, sizeof(long long));
+      if (e == cudaSuccess) e = cudaMemset(c->bf_xy, 0, (size_t)c->g.n0 * c->g.n1 * sizeof(double));
+      if (e == cudaSuccess) e = cudaMemset(c->bf_z, 0, (size_t)c->g.n2 * sizeof(double));
+      if (e == cudaSuccess) e = cudaMemset(c->bf_t, 0, sizeof(double));
+      if (e == cudaSuccess) e = cudaMemset(c->d_iter, 0, sizeof(long long));
+    }
     if (e == cudaSuccess) {
       if (c->mixed) setup3w<float>();
       else setup3w<double>();
@@ -1083,6 +1103,14 @@ int osb_teno_cutoff(osb_ctx *c, double *dev_out) {
   if (!dev_out) return set_err(c, OSB_EINVAL, "null output");
   if (!c->plan.teno_adaptive) return set_err(c, OSB_EINVAL, "plan has no adaptive TENO");
   if (int rc = check_bound(c)) return rc;
+  if (wall3(c->plan)) {
+    if (!c->metrics_valid) return set_err(c, OSB_EINVAL, "3D wall-bounded block: call osb_set_coordinate first");
+    if (!c->qold_valid) return set_err(c, OSB_EINVAL, "set the state first");
+    int64_t l = 0;
+    if (c->mixed) launch3w_cutoff<float>(*c, dev_out, c->stream, &l);
+    else launch3w_cutoff<double>(*c, dev_out, c->stream, &l);
+    return cuda_err(c, cudaGetLastError(), "osb_teno_cutoff");
+  }
   if (c->plan.ndim == 3) {
     if (!c->qold_valid) return set_err(c, OSB_EINVAL, "set the state first");
     int64_t l = 0;
@@ -1431,6 +1459,10 @@ void osb_destroy(osb_ctx *c) {
   for (int v = 0; v < 4; ++v) cudaFree(c->resv[v]);
   cudaFree(c->ysc_d);
   cudaFree(c->ysc_f);
+  cudaFree(c->bf_xy);
+  cudaFree(c->bf_z);
+  cudaFree(c->bf_t);
+  cudaFree(c->d_iter);
   for (int k = 0; k < 2; ++k) {
     if (c->side2[k]) cudaStreamDestroy(c->side2[k]);
     if (c->ev_join2[k]) cudaEventDestroy(c->ev_join2[k]);

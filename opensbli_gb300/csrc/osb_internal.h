@@ -66,6 +66,10 @@ struct Ctx {
   double *x1 = nullptr, *d11 = nullptr, *sd111 = nullptr;  // 2D: padded arrays; 3D wall-bounded: lines in j
   double *ysc_d = nullptr;        // 3D wall-bounded: inv_delta1 D11(j), FP64 and FP32 pair
   float2 *ysc_f = nullptr;
+  // 3D wall-bounded body force: A exp(..) per (x0, x1) point, cos(bta x2) per plane, the step count
+  // and the current step's sin(omega dt iter) (device words, advanced inside the step's graph)
+  double *bf_xy = nullptr, *bf_z = nullptr, *bf_t = nullptr;
+  long long *d_iter = nullptr;
   int metrics_valid = 0;
   std::string err;
   // per-kernel-family event timing (osb_profile); only used on the eager (non-graph) path
@@ -131,6 +135,9 @@ template <typename T> void launch3w_bcs(const Ctx &c, cudaStream_t s, int64_t *l
 template <typename T>
 void launch3w_rhs(const Ctx &c, int update, double A, double B, double dt, cudaStream_t s, int64_t *launches);
 template <typename T> void setup3w();
+void launch3w_bf_tables(const Ctx &c, cudaStream_t s, int64_t *launches);
+void launch3w_tick(const Ctx &c, int advance, double dt, cudaStream_t s, int64_t *launches);
+template <typename T> void launch3w_cutoff(const Ctx &c, double *out, cudaStream_t s, int64_t *launches);
 
 // batched ensemble kernels (persistent, tile queue): items are int4 {instance, bx, by, bz}
 cudaError_t batch_table_upload_central(const void *src_dev, size_t bytes, cudaStream_t s);

@@ -61,6 +61,11 @@ class Plan:
     # mixed precision on 2D blocks: interfaces whose two points' pressures differ by more than this
     # factor (strong shocks) form their characteristic flux in FP64 arithmetic; 0 keeps all in FP32
     shock_fp64: float = 0.0
+    # 3D wall-bounded blocks: the Dirichlet face keeps rhou2 and sets rhoE = state + rhou2^2/(2 rho);
+    # body_force = (A, xF, yF, bta, omega) of BF = A exp(-((x0-xF)^2 + (x1-yF)^2)) cos(bta x2)
+    # sin(omega dt iter) in the continuity equation (apps/transitional_SBLI/transitional_SBLI.py)
+    dirichlet_ke: bool = False
+    body_force: Optional[Tuple[float, ...]] = None
     rk_a: Tuple[float, float, float] = RK3_RKOLD
     rk_b: Tuple[float, float, float] = RK3_RKNEW
     use_graphs: bool = True
@@ -101,8 +106,8 @@ class Plan:
     @classmethod
     def from_json(cls, s):
         d = json.loads(s)
-        for k in ("n", "delta", "rk_a", "rk_b", "dirichlet_lo", "dirichlet_hi"):
-            if k in d:
+        for k in ("n", "delta", "rk_a", "rk_b", "dirichlet_lo", "dirichlet_hi", "body_force"):
+            if d.get(k) is not None:
                 d[k] = tuple(d[k])
         d["bc"] = tuple(tuple(x) for x in d["bc"])
         if "closure" in d:
@@ -155,6 +160,28 @@ def sbli3d_plan(n0=128, n1=64, n2=16, precision="fp64", conv="teno5", dt=0.04, u
                 weno_eps=1e-14 if conv == "weno5z" else 1e-6,  # WenoZ.eps / WenoJS.eps (weno.py)
                 dirichlet_lo=tuple(lo[:3]) + (0.0, lo[3]), dirichlet_hi=tuple(hi[:3]) + (0.0, hi[3]),
                 name="sbli3d_%s_%dx%dx%d" % (conv, n0, n1, n2))
+
+
+def transitional_plan(n0=500, n1=200, n2=100, precision="fp64", dt=0.025, use_graphs=True):
+    """The block of apps/transitional_SBLI/transitional_SBLI.py: Mach 1.5, Re = 750, Pr = 0.72,
+    Twall = 1.38099733, Sutherland 110.4/202.17, domain 375 x 140 x 27.32 with x1 = 140 sinh(5 eta)/sinh(5),
+    TENO6 with the cut-off adapted by the Ducros sensor (a1 = 9.5, a2 = 3.5, sensor epsilon 1e-12,
+    TENO eps 1e-30), RungeKuttaLS(3), the shock generator's Dirichlet face switched at x0 = 20 (rhoE
+    carrying the local spanwise kinetic energy) and the body force A = 2.5e-3, xF = 20, yF = 4,
+    bta = 0.23, omega = 0.1011."""
+    g, M = 1.4, 1.5
+    pre = (1.0, 1.0, 0.004666540532088, 0.0, 1.293661681951063)  # the script's "%.15f" values
+    post = (1.091364590640748, 1.046223246979973, -0.045679092340368002, 0.0, 1.399487006243074)
+    return Plan(ndim=3, n=(n0, n1, n2), delta=(375.0 / (n0 - 1), 140.0 / (n1 - 1), 27.32 / n2), conv="teno6",
+                visc="sutherland", rk="ls_rk3", precision=precision,
+                bc=(("inlet_pressure_extrapolate", "extrapolation"), ("isothermal_wall", "dirichlet"),
+                    ("periodic", "periodic")),
+                gama=g, Minf=M, Re=750.0, Pr=0.72, Twall=1.3809973268575328, SuthT=110.4, RefT=202.17,
+                teno_ct=1e-5, teno_eps=1e-30, rk_a=(0.0, -5.0 / 9.0, -153.0 / 128.0),
+                rk_b=(1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0), dt=dt, use_graphs=use_graphs, ic="host",
+                teno_adaptive=True, teno_a1=9.5, teno_a2=3.5, sensor_eps=1e-12, Lx1=140.0, by=5.0,
+                dirichlet_lo=pre, dirichlet_hi=post, dirichlet_x_switch=20.0, dirichlet_ke=True,
+                body_force=(2.5e-3, 20.0, 4.0, 0.23, 0.1011), name="transitional_%dx%dx%d" % (n0, n1, n2))
 
 
 def katzer_plan(n0=512, n1=256, precision="fp64", conv="teno5", dt=0.04, use_graphs=True, adaptive=False,

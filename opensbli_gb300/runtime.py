@@ -65,6 +65,8 @@ class PlanDesc(ctypes.Structure):
         ("teno_a2", ctypes.c_double),
         ("sensor_eps", ctypes.c_double),
         ("shock_fp64", ctypes.c_double),
+        ("dirichlet_ke", ctypes.c_int),
+        ("body_force", ctypes.c_double * 5),
         ("closure", (ctypes.c_int * 2) * 3),
         ("filter", ctypes.c_int),
         ("filter_control", ctypes.c_double),
@@ -201,6 +203,9 @@ def make_plan_desc(plan):
     d.teno_adaptive = 1 if plan.teno_adaptive else 0
     d.teno_a1, d.teno_a2, d.sensor_eps = plan.teno_a1, plan.teno_a2, plan.sensor_eps
     d.shock_fp64 = plan.shock_fp64
+    d.dirichlet_ke = 1 if plan.dirichlet_ke else 0
+    for k, v in enumerate(plan.body_force or (0.0,) * 5):
+        d.body_force[k] = v
     for a in range(len(plan.closure)):
         for side in range(2):
             d.closure[a][side] = CLOSURE[plan.closure[a][side]]

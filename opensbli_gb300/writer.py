@@ -307,8 +307,8 @@ class GB300Writer:
                 raise NotImplementedError("mixed WENO formulations across directions")
             conv = kconv
         adaptive = self._adaptive_teno(teno) if teno else None
-        if adaptive is not None and (conv != "teno5" or nd != 2):
-            raise NotImplementedError("the adaptive cut-off is lowered for TENO5 on 2D wall-bounded blocks")
+        if adaptive is not None and conv not in (("teno5",) if nd == 2 else ("teno5", "teno6")):
+            raise NotImplementedError("the adaptive cut-off is lowered for TENO5 (2D) and TENO5/TENO6 (3D) blocks")
         if self._max_offset(teno or weno) != 3:
             raise NotImplementedError("5th-order reconstruction stencil expected")
         if not self._kernels("MetricsEquation") or not self._kernels("Metric boundary"):
@@ -338,9 +338,29 @@ class GB300Writer:
             if per != {"left", "right"} or other:
                 raise NotImplementedError("3D wall-bounded blocks: periodic x2 expected (found %s)" % (other or per))
         closure = self._closures_2d()
-        # the Dirichlet face: rho, rhou0, rhou1, rhoE = Piecewise((hi, x0 > xs), (lo, True))
+        # the Dirichlet face: rho, rhou0, rhou1 (, rhou2), rhoE = Piecewise((hi, x0 > xs), (lo, True)); on 3D
+        # blocks rhoE may instead be a constant plus the point's spanwise kinetic energy
+        # rhou2^2/(2 rho) with rhou2 left as it is (apps/transitional_SBLI/transitional_SBLI.py:110-116)
         dk = self._kernels("Dirichlet boundary dir1 side1")[0]
-        lo, hi, xs = {}, {}, None
+        lo, hi, xs, ke = {}, {}, None, False
+
+        def value(v, name):
+            nonlocal ke
+            ds = [a for a in sympy.preorder_traversal(v) if type(a).__name__ == "DataSet"]
+            if not ds:
+                return float(v)
+            names = {re.sub(r"_B0$", "", str(a.base)) for a in ds}
+            if nd != 3 or name != "rhoE" or names != {"rho", "rhou2"} or any(int(i) != 0 for a in ds for i in a.indices):
+                raise NotImplementedError("Dirichlet face: %s = %s is not lowered" % (name, v))
+            r2, rh = sympy.symbols("_osb_r2 _osb_rho")
+            f = v.xreplace({a: (r2 if str(a.base).startswith("rhou2") else rh) for a in ds})
+            c = float(f.subs({r2: 0, rh: 1}))
+            for tv, rv in ((0.37, 1.3), (-1.1, 0.6)):
+                if abs(float(f.subs({r2: tv, rh: rv})) - (c + 0.5 * tv * tv / rv)) > 1e-12:
+                    raise NotImplementedError("Dirichlet face: rhoE = %s is not const + rhou2^2/(2 rho)" % v)
+            ke = True
+            return c
+
         for e in dk.equations:
             name = re.sub(r"_B0$", "", str(getattr(e.lhs, "base", e.lhs)))
             rhs = e.rhs
@@ -349,13 +369,19 @@ class GB300Writer:
                 if not isinstance(cond, sympy.core.relational.StrictGreaterThan):
                     raise NotImplementedError("Dirichlet face: state switched by x0 > value expected")
                 xs = float(cond.rhs)
-                hi[name], lo[name] = float(vhi), float(vlo)
+                hi[name], lo[name] = value(vhi, name), value(vlo, name)
             elif name in ("rho", "rhou0", "rhou1", "rhou2", "rhoE"):
-                hi[name] = lo[name] = float(rhs)
+                hi[name] = lo[name] = value(rhs, name)
         order = ["rho", "rhou0", "rhou1"] + (["rhou2"] if nd == 3 else []) + ["rhoE"]
+        if ke:
+            if "rhou2" in lo:
+                raise NotImplementedError("Dirichlet face: rhou2 set with rhoE carrying its kinetic energy")
+            lo["rhou2"] = hi["rhou2"] = 0.0  # kept at the face, not set
         if any(v not in lo for v in order):
             raise NotImplementedError("Dirichlet face must set %s" % ", ".join(order))
-        physics_check.check_algorithm(self.components, nd, viscous=True, sutherland=True, metric=True)
+        bf = self._body_force() if nd == 3 else None
+        physics_check.check_algorithm(self.components, nd, viscous=True, sutherland=True, metric=True,
+                                      body_force=bf is not None)
         return Plan(ndim=nd, n=(64, 32, 1) if nd == 2 else (64, 32, 16), delta=(1.0, 1.0, 1.0), conv=conv,
                     weno_eps=1e-14 if conv == "weno5z" else 1e-6,  # WenoZ.eps / WenoJS.eps (weno.py)
                     visc="sutherland", rk="ls_rk3", precision=precision,
@@ -364,8 +390,62 @@ class GB300Writer:
                     name="wall3d" if nd == 3 else Plan.name,
                     dirichlet_lo=tuple(lo[v] for v in order), dirichlet_hi=tuple(hi[v] for v in order),
                     dirichlet_x_switch=xs if xs is not None else 1e300, kernels=[n for n in names if n],
+                    dirichlet_ke=ke, body_force=bf,
                     teno_adaptive=adaptive is not None,
                     sensor_eps=adaptive if adaptive is not None else Plan.sensor_eps, closure=closure)
+
+    _BF_CONSTS = ("A", "xF", "yF", "bta", "omega")
+
+    def _body_force(self):
+        """Recognise the body force of apps/transitional_SBLI/transitional_SBLI.py:80-89: a constituent
+        relation BF = A exp(-((x0-xF)^2 + (x1-yF)^2)) cos(bta x2) sin(omega dt iter) of the coordinate
+        arrays and the iteration number, added to the continuity equation's residual.  Returns None
+        without one, else (A, xF, yF, bta, omega) (values as far as the algorithm knows them; the
+        simulation parameters complete them)."""
+        import math
+        import random
+        import sympy
+        eqs = [(k, e) for k in self.components if type(k).__name__ == "Kernel" for e in k.equations
+               if str(getattr(e.lhs, "base", "")) == "BF_B0"]
+        if not eqs:
+            return None
+        if len(eqs) != 1:
+            raise NotImplementedError("body force: written more than once")
+        e = eqs[0][1]
+        syms = {}
+        it = sympy.preorder_traversal(e.rhs)
+        for a in it:
+            t = type(a).__name__
+            if t == "DataSet":
+                it.skip()  # not its shape constants
+                if any(int(i) != 0 for i in a.indices) or str(a.base) not in ("x0_B0", "x1_B0", "x2_B0"):
+                    raise NotImplementedError("body force reads %s" % a)
+                syms[a] = sympy.Symbol("_bf_" + str(a.base)[:2])
+            elif t == "ConstantObject":
+                if str(a) not in self._BF_CONSTS + ("dt",):
+                    raise NotImplementedError("body force constant %s" % a)
+                syms[a] = sympy.Symbol("_bf_" + str(a))
+            elif t == "Globalvariable":
+                if str(a) != "iter":
+                    raise NotImplementedError("body force reads %s" % a)
+                syms[a] = sympy.Symbol("_bf_iter")
+        f = e.rhs.xreplace(syms)
+        rnd = random.Random(11)
+        for _ in range(6):
+            v = {n: rnd.uniform(0.1, 2.0) for n in ("x0", "x1", "x2", "A", "xF", "yF", "bta", "omega", "dt")}
+            v["iter"] = float(rnd.randint(0, 50))
+            want = v["A"] * math.exp(-(v["x0"] - v["xF"]) ** 2 - (v["x1"] - v["yF"]) ** 2) * \
+                math.cos(v["bta"] * v["x2"]) * math.sin(v["omega"] * v["dt"] * v["iter"])
+            got = float(f.subs({sympy.Symbol("_bf_" + n): x for n, x in v.items()}))
+            if abs(got - want) > 1e-12 * max(1.0, abs(want)):
+                raise NotImplementedError("body force: formula not recognised")
+        # the continuity residual must add BF once (the generated residual kernel's "+ BF_B0")
+        adds = [k for k in self.components if type(k).__name__ == "Kernel" for q in k.equations
+                if str(getattr(q.lhs, "base", "")) == "Residual0_B0" and "BF_B0" in str(q.rhs)]
+        if len(adds) != 1:
+            raise NotImplementedError("body force: not added to the continuity equation exactly once")
+        vals = {str(a): getattr(a, "value", None) for a in syms if type(a).__name__ == "ConstantObject"}
+        return tuple(float(vals[k]) if isinstance(vals.get(k), (int, float)) else 0.0 for k in self._BF_CONSTS)
 
     def _closures_2d(self):
         """The one-sided closure each face applies to the central derivatives of its direction
@@ -479,7 +559,11 @@ class GB300Writer:
             return var.pop(), dirs.pop()
 
         for e in kern.equations:
-            if type(e.lhs).__name__ == "GridVariable" and isinstance(e.rhs, sympy.Piecewise):
+            # derivative locals: a closure Piecewise, or (periodic axes) a plain central stencil
+            if type(e.lhs).__name__ == "GridVariable" and (
+                    isinstance(e.rhs, sympy.Piecewise) or
+                    any(type(a).__name__ == "DataSet" and any(int(i) != 0 for i in a.indices)
+                        for a in sympy.preorder_traversal(e.rhs))):
                 locs[e.lhs] = classify(e.rhs, e.lhs)
         nd = self.block.ndim
         # work arrays: the last write before the sensor kernel, by a sensor-derivative kernel
@@ -525,11 +609,12 @@ class GB300Writer:
         if eps is None or g.free_symbols - set(sym.values()) - {D}:
             raise NotImplementedError("adaptive TENO: sensor formula not recognised")
         # compare against the sensor the GPU kernel implements on random derivative values: D11 is
-        # the 2D block's metric factor d(xi1)/d(x1), 1 on the 3D Cartesian block
+        # the metric factor d(xi1)/d(x1) of a block stretched in x1, 1 on a Cartesian block
         rnd = random.Random(7)
+        metric = D in g.free_symbols
         for _ in range(8):
             vals = {k_: rnd.uniform(-0.02, 0.02) for k_ in sym}
-            Dv = rnd.uniform(0.5, 2.0) if nd == 2 else 1.0
+            Dv = rnd.uniform(0.5, 2.0) if metric else 1.0
             du = [[vals[("u%d_B0" % c, d)] * (Dv if d == 1 else 1.0) for d in range(nd)] for c in range(nd)]
             div = sum(du[c][c] for c in range(nd))
             if nd == 2:
@@ -559,7 +644,9 @@ class GB300Writer:
                   niter=int(env["niter"]) if "niter" in env else p.niter)
         if nd == 3 and p.conv in ("teno5", "teno6"):
             kw.update(teno_eps=float(env.get("eps", p.teno_eps)), teno_ct=float(env.get("TENO_CT", p.teno_ct)))
-        if nd == 2:
+        if p.body_force is not None:
+            kw["body_force"] = tuple(float(env.get(k, v)) for k, v in zip(self._BF_CONSTS, p.body_force))
+        if p.rk == "ls_rk3":  # wall-bounded blocks
             kw.update(Twall=float(env.get("Twall", p.Twall)), SuthT=float(env.get("SuthT", p.SuthT)),
                       RefT=float(env.get("RefT", p.RefT)), teno_eps=float(env.get("eps", p.teno_eps)),
                       teno_ct=float(env.get("TENO_CT", p.teno_ct)), Lx1=float(env.get("Lx1", p.Lx1)),

@@ -40,6 +40,7 @@ CASES = {
     "katzer_teno6": "katzer_teno6.py",
     "katzer_adaptive": "ref:apps/katzer_SBLI/katzer_SBLI.py",
     "sbli3d_teno": "sbli3d_teno.py",
+    "transitional_sbli": "transitional_sbli.py",
 }
 
 

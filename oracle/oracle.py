@@ -244,6 +244,16 @@ class Cfg3W(ctypes.Structure):
         ("conv", ctypes.c_int),
         ("dirichlet", (ctypes.c_double * 5) * 2),
         ("x_switch", ctypes.c_double),
+        ("dirichlet_ke", ctypes.c_int),
+        ("bf_A", ctypes.c_double),
+        ("bf_xF", ctypes.c_double),
+        ("bf_yF", ctypes.c_double),
+        ("bf_bta", ctypes.c_double),
+        ("bf_omega", ctypes.c_double),
+        ("teno_adaptive", ctypes.c_int),
+        ("teno_a1", ctypes.c_double),
+        ("teno_a2", ctypes.c_double),
+        ("sensor_eps", ctypes.c_double),
     ]
 
 
@@ -269,6 +279,12 @@ def make_cfg3w(plan):
         c.dirichlet[0][v] = plan.dirichlet_lo[v]
         c.dirichlet[1][v] = plan.dirichlet_hi[v]
     c.x_switch = plan.dirichlet_x_switch
+    c.dirichlet_ke = 1 if getattr(plan, "dirichlet_ke", False) else 0
+    bf = getattr(plan, "body_force", None) or (0.0, 0.0, 0.0, 0.0, 0.0)
+    c.bf_A, c.bf_xF, c.bf_yF, c.bf_bta, c.bf_omega = bf
+    c.teno_adaptive = 1 if getattr(plan, "teno_adaptive", False) else 0
+    c.teno_a1, c.teno_a2 = getattr(plan, "teno_a1", 10.5), getattr(plan, "teno_a2", 4.5)
+    c.sensor_eps = getattr(plan, "sensor_eps", 1e-12)
     return c
 
 

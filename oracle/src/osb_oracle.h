@@ -93,6 +93,15 @@ typedef struct {
    * rho, rhou0, rhou1, rhou2, rhoE */
   double dirichlet[2][5];
   double x_switch;
+  /* dirichlet_ke = 1: the Dirichlet face keeps rhou2 and sets rhoE = dirichlet[.][4] + rhou2^2/(2 rho)
+   * with the face's rho (apps/transitional_SBLI/transitional_SBLI.py:110-116) */
+  int dirichlet_ke;
+  /* body force in the continuity equation (transitional_SBLI.py:80-89), 0 when bf_A = 0:
+   * BF = bf_A exp(-((x0-bf_xF)^2 + (x1-bf_yF)^2)) cos(bf_bta x2) sin(bf_omega dt iter) */
+  double bf_A, bf_xF, bf_yF, bf_bta, bf_omega;
+  /* TENO cut-off adapted by the metric-transformed Ducros sensor (0: the fixed teno_ct) */
+  int teno_adaptive;
+  double teno_a1, teno_a2, sensor_eps;
 } osbo3w_cfg;
 
 /* Advance q by nsteps LS-RK3 steps.  q holds [5][n2+8][n1+8][n0+8] with a 4-point halo on every side

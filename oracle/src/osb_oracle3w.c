@@ -39,6 +39,7 @@ typedef struct {
   double *q[5], *du[5], *res[5], *flux[5];
   double *u[3], *p, *a, *T, *mu;
   double *wk[3];                 /* inner x0 derivatives of u_i (nested derivatives) */
+  double *theta;                 /* Ducros sensor (adaptive TENO), interior; 0 elsewhere */
   double *wz[3];                 /* inner x2 derivatives of u_i */
   double x1[256 + 2 * H], D11[256 + 2 * H], SD111[256 + 2 * H]; /* functions of x1 only */
   double carp[4][6];
@@ -81,6 +82,7 @@ static int s3_init(s3_t *s, const osbo3w_cfg *cfg) {
     s->wz[d] = alloc3(s);
   }
   s->p = alloc3(s);
+  s->theta = alloc3(s);
   s->a = alloc3(s);
   s->T = alloc3(s);
   s->mu = alloc3(s);
@@ -100,6 +102,7 @@ static void s3_free(s3_t *s) {
     free(s->wz[d]);
   }
   free(s->p);
+  free(s->theta);
   free(s->a);
   free(s->T);
   free(s->mu);
@@ -247,7 +250,14 @@ static void apply_bcs(s3_t *s) {
     for (int j = N1 - 1; j < N1 + 4; ++j) /* DirichletBC, piecewise in x0 */
       for (int i = -3; i < N0 + 4; ++i) {
         const double x0 = s->c.delta[0] * i;
-        for (int v = 0; v < 5; ++v) s->q[v][I3(s, i, j, k)] = s->c.dirichlet[x0 > s->c.x_switch ? 1 : 0][v];
+        const double *st = s->c.dirichlet[x0 > s->c.x_switch ? 1 : 0];
+        const size_t m = I3(s, i, j, k);
+        if (s->c.dirichlet_ke) { /* rhou2 kept; rhoE from the face's rho and the local rhou2 */
+          for (int v = 0; v < 3; ++v) s->q[v][m] = st[v];
+          s->q[4][m] = st[4] + 0.5 * s->q[3][m] * s->q[3][m] / s->q[0][m];
+        } else {
+          for (int v = 0; v < 5; ++v) s->q[v][m] = st[v];
+        }
       }
   }
   for (int v = 0; v < 5; ++v) /* periodic x2 */
@@ -280,6 +290,45 @@ static void constituent(s3_t *s) {
   }
 }
 
+/* Modified Ducros sensor with the metric (shock_sensors.py:12-49 with metriceq, as generated for
+ * transitional_SBLI.py): on the interior, with the x0 and x1 closures and d/dx1 = D11 d/dxi1,
+ * theta = (1/2 - 1/2 tanh(250 div + 2.5)) div^2 / (eps + |curl u|^2 + div^2); 0 elsewhere. */
+static void ducros_sensor(s3_t *s) {
+  FOR3(0, N0, 0, N1, 0, N2) {
+    const size_t n = I3(s, i, j, k);
+    const double D = s->D11[j + H];
+    double du[3][3];
+    for (int c = 0; c < 3; ++c) {
+      du[c][0] = d1c(s, s->u[c], i, j, k, 0);
+      du[c][1] = D * d1c(s, s->u[c], i, j, k, 1);
+      du[c][2] = d1c(s, s->u[c], i, j, k, 2);
+    }
+    const double div = du[0][0] + du[1][1] + du[2][2];
+    const double w0 = du[2][1] - du[1][2], w1 = du[0][2] - du[2][0], w2 = du[1][0] - du[0][1];
+    s->theta[n] = (0.5 - 0.5 * tanh(250.0 * div + 2.5)) * (div * div) /
+                  (s->c.sensor_eps + w0 * w0 + w1 * w1 + w2 * w2 + div * div);
+  }
+}
+
+/* TENO cut-off at the interface whose left point is n (teno.py:430-443) */
+static double teno_cutoff(const s3_t *s, size_t n) {
+  if (!s->c.teno_adaptive) return s->c.teno_ct;
+  const double th = s->theta[n];
+  return pow(10.0, -floor(s->c.teno_a1 - s->c.teno_a2 * (-pow(1 - th, 4) * (4 * th + 1) + 1)));
+}
+
+/* Body force of the continuity equation at the iteration `it` (transitional_SBLI.py:80-89) */
+static void body_force(s3_t *s, int it) {
+  if (s->c.bf_A == 0.0) return;
+  const double st = sin(s->c.dt * s->c.bf_omega * it);
+  FOR3(0, N0, 0, N1, 0, N2) {
+    const double x0 = s->c.delta[0] * i, x1 = s->x1[j + H], x2 = s->c.delta[2] * k;
+    s->res[0][I3(s, i, j, k)] += s->c.bf_A * exp(-(x0 - s->c.bf_xF) * (x0 - s->c.bf_xF) -
+                                                 (x1 - s->c.bf_yF) * (x1 - s->c.bf_yF)) *
+                                 st * cos(s->c.bf_bta * x2);
+  }
+}
+
 /* Characteristic fluxes in direction dir (Roe average, the Cartesian 3D eigensystem: the block's
  * metric is diagonal and enters the residual only), TENO5 / WENO5-JS / WENO5-Z / TENO6, and the
  * residual R = -(F_i - F_{i-1})/delta0 - D11 (G_j - G_{j-1})/delta1 - (H_k - H_{k-1})/delta2
@@ -287,6 +336,7 @@ static void constituent(s3_t *s) {
 static void residual_flux(s3_t *s) {
   const double g = s->c.gama;
   const int n[3] = {N0, N1, N2};
+  if (s->c.teno_adaptive) ducros_sensor(s);
   for (int v = 0; v < 5; ++v) FOR3(0, N0, 0, N1, 0, N2) s->res[v][I3(s, i, j, k)] = 0.0;
   for (int dir = 0; dir < 3; ++dir) {
     const size_t o = dir == 0 ? 1 : dir == 1 ? (size_t)s->px : (size_t)s->px * s->py;
@@ -337,14 +387,15 @@ static void residual_flux(s3_t *s) {
             gp[t] = CF[r][t] + lam[r] * CS[r][t];
             gm[t] = CF[r][t] - lam[r] * CS[r][t];
           }
-          rec[r] = osbo_side_teno6(gp, 1, s->c.teno_eps, s->c.teno_ct) +
-                   osbo_side_teno6(gm, 0, s->c.teno_eps, s->c.teno_ct);
+          rec[r] = osbo_side_teno6(gp, 1, s->c.teno_eps, teno_cutoff(s, c)) +
+                   osbo_side_teno6(gm, 0, s->c.teno_eps, teno_cutoff(s, c));
         } else if (s->c.conv == OSBO_CONV_WENO5JS || s->c.conv == OSBO_CONV_WENO5Z) {
           const int z = s->c.conv == OSBO_CONV_WENO5Z;
           rec[r] = osbo_side_weno5_plus(fp, z) + osbo_side_weno5_minus(fm, z);
         } else {
           const double fmr[5] = {fm[4], fm[3], fm[2], fm[1], fm[0]}; /* points i+3 .. i-1 */
-          rec[r] = osbo_side_teno5(fp, s->c.teno_eps, s->c.teno_ct) + osbo_side_teno5(fmr, s->c.teno_eps, s->c.teno_ct);
+          rec[r] = osbo_side_teno5(fp, s->c.teno_eps, teno_cutoff(s, c)) +
+                   osbo_side_teno5(fmr, s->c.teno_eps, teno_cutoff(s, c));
         }
       }
       for (int v = 0; v < 5; ++v) {
@@ -433,6 +484,7 @@ int osbo3w_run(const osbo3w_cfg *cfg, double *q, int nsteps) {
     for (int stg = 0; stg < 3; ++stg) {
       constituent(s);
       residual_flux(s);
+      body_force(s, it);
       residual_viscous(s);
       /* RungeKuttaLS (rk_LS.py:155-166): du = A du + dt R; q = q + B du */
       for (int v = 0; v < 5; ++v) FOR3(0, N0, 0, N1, 0, N2) {
@@ -459,6 +511,7 @@ int osbo3w_residual(const osbo3w_cfg *cfg, const double *q, double *r) {
   apply_bcs(s);
   constituent(s);
   residual_flux(s);
+  body_force(s, 0);
   residual_viscous(s);
   size_t m = 0;
   for (int v = 0; v < 5; ++v) FOR3(0, N0, 0, N1, 0, N2) r[m++] = s->res[v][I3(s, i, j, k)];

@@ -66,6 +66,10 @@ VARS_2D = ["rho", "rhou0", "rhou1", "rhoE"]
 # j alone) with a 4-point halo.
 CASES_3W = {
     "sbli3d_teno": ((32, 24, 8), 10, {"dt": 0.02}),
+    # the transitional_SBLI block: adaptive TENO6 with the metric sensor, body force, Dirichlet face
+    # with the spanwise kinetic energy
+    # (forcing centred on a grid point of this coarse grid and 20x stronger, so that it shows)
+    "transitional_sbli": ((32, 24, 8), 20, {"dt": 0.2, "A": 0.05, "xF": 2 * 375.0 / 31}),
 }
 VARS_3W = ["rho", "rhou0", "rhou1", "rhou2", "rhoE"]
 

@@ -98,3 +98,61 @@ def test_wall3d_graph_matches_eager_and_mixed_error():
     ref = q_ref[INNER]
     l2 = [float(np.linalg.norm(qm[v] - ref[v]) / np.linalg.norm(ref[v])) for v in (0, 1, 2, 4)]
     assert np.isfinite(qm).all() and max(l2) <= 1e-5, l2
+
+
+# ---- the transitional_SBLI block: adaptive TENO6 with the metric-transformed Ducros sensor, body
+# force in the continuity equation, Dirichlet face carrying the spanwise kinetic energy ----
+
+def golden_tr():
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_transitional_sbli.npz"))
+    return d["q0"], d["x1"], d["q"], tuple(int(x) for x in d["n"]), int(d["steps"]), json.loads(str(d["params"]))
+
+
+def plan_tr(n, params):
+    """transitional_plan with the fixture's forcing (centred on a grid point, stronger than the app's)."""
+    from opensbli_gb300.plan import transitional_plan
+    return transitional_plan(*n, dt=params["dt"]).replace(body_force=(params["A"], params["xF"], 4.0, 0.23, 0.1011))
+
+
+def rel_err_mom(a, b):
+    """Max-normalised per variable, the three momenta on the largest momentum scale (rhou2 stays
+    near zero in this short run)."""
+    mom = max(float(np.abs(b[v]).max()) for v in (1, 2, 3))
+    return [float(np.abs(a[v] - b[v]).max() / (mom if v in (1, 2, 3) else np.abs(b[v]).max())) for v in range(5)]
+
+
+def test_transitional_fp64_matches_reference_golden():
+    q0, x1, q_ref, n, steps, params = golden_tr()
+    plan = plan_tr(n, params)
+    q = run_gpu(plan, q0, x1, steps, params["dt"])
+    err = rel_err_mom(q, q_ref[INNER])
+    assert max(err) <= 5e-12, err  # TENO6's rounding floor, as for the fixed cut-off
+
+
+def test_transitional_body_force_and_cutoff_field():
+    """Without the body force the state moves differently (the force is on); the cut-off field of the
+    state takes adapted levels 10^-k, k = 6 .. 9 (a1 = 9.5, a2 = 3.5)."""
+    q0, x1, q_ref, n, steps, params = golden_tr()
+    plan = plan_tr(n, params)
+    q_nobf = run_gpu(plan.replace(body_force=(0.0,) * 5), q0, x1, steps, params["dt"])
+    assert max(rel_err_mom(q_nobf, q_ref[INNER])) > 1e-3
+    s = Solver(plan)
+    s.set_coordinate(x1, 4)
+    s.set_state64_padded(q_ref[:, 1:-1, 1:-1, 1:-1], 3)
+    ct = s.teno_cutoff().cpu().numpy()
+    s.close()
+    levels = set(np.unique(ct))
+    assert levels <= {10.0 ** -k for k in range(6, 10)} and len(levels) >= 1, levels
+
+
+def test_transitional_graph_matches_eager_and_mixed_error():
+    q0, x1, q_ref, n, steps, params = golden_tr()
+    plan = plan_tr(n, params)
+    a = run_gpu(plan, q0, x1, 5, params["dt"])
+    b = run_gpu(plan.replace(use_graphs=False), q0, x1, 5, params["dt"])
+    assert np.array_equal(a, b)
+    qm = run_gpu(plan.replace(precision="mixed"), q0, x1, steps, params["dt"])
+    ref = q_ref[INNER]
+    l2 = [float(np.linalg.norm(qm[v] - ref[v]) / np.linalg.norm(ref[v])) for v in (0, 1, 2, 4)]
+    assert np.isfinite(qm).all() and max(l2) <= 1e-5, l2

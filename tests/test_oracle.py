@@ -191,3 +191,26 @@ def test_oracle_wall3d_matches_reference_run():
     q = O.run3w(sbli3d_plan(24, 20, 6, dt=0.02), q0, 12)[:, 4:-4, 4:-4, 4:-4]
     err = [float(np.abs(q[v] - ref[v]).max() / np.abs(ref[v]).max()) for v in range(5)]
     assert max(err) < 1e-12, err
+
+
+def test_oracle_transitional_matches_reference_golden():
+    """osb_oracle3w.c with the transitional_SBLI block's adaptive TENO6 (metric-transformed Ducros
+    sensor), body force and Dirichlet face against the reference's generated code: 32 x 24 x 8, 20
+    steps; the momenta on the largest momentum scale (rhou2 stays near zero this early)."""
+    import json
+    from opensbli_gb300.plan import transitional_plan
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_transitional_sbli.npz"))
+    n = tuple(int(x) for x in d["n"])
+    params = json.loads(str(d["params"]))
+    # the fixture's forcing is centred on a grid point and stronger than the app's (A, xF)
+    plan = transitional_plan(*n, dt=params["dt"]).replace(body_force=(params["A"], params["xF"], 4.0, 0.23, 0.1011))
+    q = O.run3w(plan, d["q0"], int(d["steps"]))
+    inner = (slice(None), slice(4, -4), slice(4, -4), slice(4, -4))
+    ref = d["q"][inner]
+    mom = max(float(np.abs(ref[v]).max()) for v in (1, 2, 3))
+    err = [float(np.abs(q[inner][v] - ref[v]).max() / (mom if v in (1, 2, 3) else np.abs(ref[v]).max()))
+           for v in range(5)]
+    assert max(err) < 1e-12, err
+    # without the body force the result differs: the oracle's force is the reference's
+    q0 = O.run3w(plan.replace(body_force=(0.0,) * 5), d["q0"], int(d["steps"]))
+    assert float(np.abs(q0[inner][0] - ref[0]).max()) > 1e-3

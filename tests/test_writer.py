@@ -92,6 +92,16 @@ def test_3d_wall_script_lowers_to_the_span_periodic_plan():
     assert g.bc[2] == ("periodic", "periodic") and g.dirichlet_hi[3] == 0.0
 
 
+def test_transitional_script_lowers_to_its_plan():
+    """The transitional_SBLI block lowers with its adaptive TENO6 cut-off (metric sensor), body force
+    and Dirichlet face carrying the spanwise kinetic energy, to the plan of transitional_plan."""
+    from opensbli_gb300.plan import transitional_plan
+    g = golden_plan("transitional_sbli")
+    p = transitional_plan(*g.n)
+    assert g.replace(kernels=[], name="", niter=None) == p.replace(kernels=[], name="")
+    assert g.teno_adaptive and g.conv == "teno6" and g.dirichlet_ke and g.body_force == (2.5e-3, 20.0, 4.0, 0.23, 0.1011)
+
+
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
 def test_3d_wall_initial_state_matches_reference(tmp_path):
     import json
@@ -117,7 +127,7 @@ def test_writer_refuses_kernels_outside_the_lowered_families():
     dissipation sensor is lowered; its Ducros variant adds a shock-sensor kernel and is refused."""
     from opensbli_gb300.writer import GB300Writer
     for case in ("tgv_central", "tgv_weno", "tgsym_central", "katzer_teno", "katzer_adaptive", "katzer_carpenter",
-                 "tgv_filter", "tgv_teno_adaptive", "sbli3d_teno"):
+                 "tgv_filter", "tgv_teno_adaptive", "sbli3d_teno", "transitional_sbli"):
         GB300Writer._check_kernel_families(golden_plan(case).kernels)
     assert "User kernel: Non-linear filter application" in golden_plan("tgv_filter").kernels
     names = golden_plan("tgv_filter").kernels + ["User kernel: Shock sensor"]
@@ -145,7 +155,7 @@ def test_cfl_dt_tgv_weno():
 @pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central",
                                   "katzer_teno", "katzer_adaptive", "katzer_carpenter", "tgv_filter",
                                   "katzer_weno", "katzer_wenoz", "katzer_teno6", "tgv_teno_adaptive",
-                                  "sbli3d_teno"])
+                                  "sbli3d_teno", "transitional_sbli"])
 def test_writer_lowers_reference_script(case, tmp_path):
     r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case, "--out",
                         str(tmp_path), "--ref", REF], capture_output=True, text=True, timeout=900)
