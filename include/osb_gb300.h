@@ -19,7 +19,7 @@
 extern "C" {
 #endif
 
-#define OSB_ABI_VERSION 6
+#define OSB_ABI_VERSION 7
 
 /* error codes */
 #define OSB_OK 0
@@ -38,10 +38,12 @@ extern "C" {
 #define OSB_CONV_TENO5 2
 #define OSB_CONV_WENO5Z 3   /* WENO5-Z weights (weno.py:283-331), 3D blocks */
 #define OSB_CONV_TENO6 4    /* LLFTeno(6), fixed cut-off (teno.py:94-192, 216-234), 3D blocks */
-/* viscous terms: none, constant viscosity (taylor_green_vortex.py:18-19), Sutherland (katzer_SBLI.py:25) */
+/* viscous terms: none, constant viscosity (taylor_green_vortex.py:18-19), Sutherland (katzer_SBLI.py:25),
+ * the power law mu = T^visc_exp (apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py:30) */
 #define OSB_VISC_NONE 0
 #define OSB_VISC_CONST 1
 #define OSB_VISC_SUTHERLAND 2
+#define OSB_VISC_POWER 3
 /* time integration: RungeKutta(3) 2-register (schemes/temporal/rk_sbli.py:51-61, 117-124),
  * RungeKuttaLS(3,'SSP') (schemes/temporal/rk_LS.py:71-101, 155-166) */
 #define OSB_RK3_2REG 0
@@ -51,7 +53,7 @@ extern "C" {
 #define OSB_BC_SYMMETRY 1
 #define OSB_BC_INLET_PRESSURE_EXTRAPOLATE 2 /* inlet_pressure_extrapolate.py:11-66 (x0 side 0) */
 #define OSB_BC_EXTRAPOLATION 3             /* extrapolation.py:8-58, order 0 (x0 side 1) */
-#define OSB_BC_ISOTHERMAL_WALL 4           /* isothermal_wall.py:11-88 (x1 side 0) */
+#define OSB_BC_ISOTHERMAL_WALL 4           /* isothermal_wall.py:11-88 (x1 side 0; side 1 on channel blocks) */
 #define OSB_BC_DIRICHLET 5                 /* dirichlet.py:6-41 with a state switched at x0 (x1 side 1) */
 
 /* one-sided closures of the central derivatives at a face of a 2D block (opensblifunctions.py:523-534) */
@@ -116,6 +118,12 @@ typedef struct osb_plan_desc {
    * switch is 1 everywhere); filter_control is the generated code's shock_filter_control (1) */
   int filter;
   double filter_control;
+  /* channel blocks (3D, periodic x0 and x2, isothermal walls on both x1 faces;
+   * apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py): visc_exp is the exponent of
+   * OSB_VISC_POWER; forcing = (c0, c1, c2) subtracts c_i from the momentum equations and c_j u_j from
+   * the energy equation (the script's constant pressure-gradient forcing; 0: none) */
+  double visc_exp;
+  double forcing[3];
 } osb_plan_desc;
 
 /* Memory layout of every per-variable array: x fastest, interior point (i,j,k) at element

@@ -31,10 +31,13 @@ namespace {
 template <typename T> __device__ __forceinline__ T rcp2(T x);
 template <> __device__ __forceinline__ float rcp2<float>(float x) { return __fdividef(1.0f, x); }
 template <> __device__ __forceinline__ double rcp2<double>(double x) { return 1.0 / x; }
+template <typename T> __device__ __forceinline__ T pow_t(T x, T y);
+template <> __device__ __forceinline__ float pow_t<float>(float x, float y) { return powf(x, y); }
+template <> __device__ __forceinline__ double pow_t<double>(double x, double y) { return pow(x, y); }
 
 // ---- one-sided closures of the central first derivative.  G(o) reads the function at offset o
 // along the axis, k is the point's index, n the axis size, cl the axis's Carpenter faces (bit 0: side
-// 0, bit 1: side 1; the others are ReducedAccess).
+// 0, bit 1: side 1; the others are ReducedAccess); bit 2 marks a periodic axis (central everywhere).
 //  * ReducedAccess (reduced_access_scheme.py:34-83): the first two points of a face, 5-point stencils;
 //  * Carpenter (Carpenter_scheme.py:61-102): the first four points, weights c_carp[r][m] of f(m) at
 //    point r of a side-0 face, mirrored with the opposite sign on side 1.
@@ -47,7 +50,7 @@ template <> __device__ __forceinline__ float carp_w<float>(int i) { return c_car
 
 template <typename T, typename Gf> __device__ __forceinline__ T d1c(const Gf &G, int k, int n, int cl) {
   const int w0 = (cl & 1) ? 4 : 2, w1 = (cl & 2) ? 4 : 2;
-  if (k < w0 || n - 1 - k < w1) {
+  if (!(cl & 4) && (k < w0 || n - 1 - k < w1)) {
     const bool s0 = k < w0;
     if (s0 ? (cl & 1) : (cl & 2)) {
       const int r = s0 ? k : n - 1 - k;
@@ -65,8 +68,10 @@ template <typename T, typename Gf> __device__ __forceinline__ T d1c(const Gf &G,
   }
   return T(1.0 / 12.0) * G(-2) - T(2.0 / 3.0) * G(-1) + T(2.0 / 3.0) * G(1) - T(1.0 / 12.0) * G(2);
 }
-// second derivative: the same two-point closure in both schemes (second_der_coefficients)
-template <typename T, typename Gf> __device__ __forceinline__ T d2c(const Gf &G, int k, int n) {
+// second derivative: the same two-point closure in both schemes (second_der_coefficients); none on a
+// periodic axis (cl bit 2)
+template <typename T, typename Gf> __device__ __forceinline__ T d2c(const Gf &G, int k, int n, int cl = 0) {
+  if (cl & 4) return T(-1.0 / 12.0) * G(-2) + T(4.0 / 3.0) * G(-1) - T(2.5) * G(0) + T(4.0 / 3.0) * G(1) - T(1.0 / 12.0) * G(2);
   if (k == 0)
     return T(35.0 / 12.0) * G(0) - T(26.0 / 3.0) * G(1) + T(9.5) * G(2) - T(14.0 / 3.0) * G(3) + T(11.0 / 12.0) * G(4);
   if (k == 1)
@@ -889,6 +894,7 @@ template <typename T> static Q4T<T> q4t(void *const *a) {
 
 // the Carpenter faces of one axis as d1c's bit mask
 static int closure_bits(const osb_plan_desc &p, int axis) {
+  if (p.bc[axis][0] == OSB_BC_PERIODIC) return 4;
   return (p.closure[axis][0] == OSB_CLOSURE_CARPENTER ? 1 : 0) | (p.closure[axis][1] == OSB_CLOSURE_CARPENTER ? 2 : 0);
 }
 
@@ -1133,10 +1139,13 @@ __global__ void __launch_bounds__(256) k3w_metrics(int n1, const double *x1, dou
 struct BC3Args {
   double gama, Minf, Twall, delta0, xs;
   double lo[5], hi[5];
-  int ke;  // Dirichlet face keeps rhou2 and sets rhoE = state + rhou2^2/(2 rho)
+  int ke;     // Dirichlet face keeps rhou2 and sets rhoE = state + rhou2^2/(2 rho)
+  int per0;   // channel: periodic x0 (no inlet and outlet faces)
+  int wall1;  // channel: isothermal wall on x1 side 1 (no Dirichlet face)
 };
 
 __device__ __forceinline__ void bc3_row(const Grid &g, const Q5 &q, const BC3Args &a, int j, int k) {
+  if (a.per0) return;
   {  // inlet (inlet_pressure_extrapolate.py:11-66)
     const int64_t b = gidx(g, 0, j, k), m1 = gidx(g, -1, j, k);
     const double rhob = q.v[0][b];
@@ -1156,9 +1165,13 @@ __device__ __forceinline__ void bc3_row(const Grid &g, const Q5 &q, const BC3Arg
   }
 }
 
-__device__ __forceinline__ void bc3_col(const Grid &g, const Q5 &q, const BC3Args &a, int i, int t, int k) {
+// One halo point of an isothermal wall (isothermal_wall.py:32-88) whose wall row is jw and whose
+// interior lies on the side sg (+1: side 0, -1: side 1) of it: the halo point jw - sg t mirrors the
+// point jw + sg t with T_t = (t+1) Twall - t T(jw + sg); t = 1 also sets the wall point.
+__device__ __forceinline__ void wall3_point(const Grid &g, const Q5 &q, const BC3Args &a, int i, int jw, int sg, int t,
+                                            int k) {
   const double M2 = a.Minf * a.Minf, gama = a.gama;
-  const int64_t w = gidx(g, i, 0, k), a1 = gidx(g, i, 1, k);
+  const int64_t w = gidx(g, i, jw, k), a1 = gidx(g, i, jw + sg, k);
   // the wall point after this face: zero momentum, energy from Twall; its pressure
   // (gama-1) (rhoE - |rhou|^2 / (2 rho)) is exactly (gama-1) rhoE there
   const double rw = q.v[0][w], ew = a.Twall * (1.0 / M2) * rw / (gama * (gama - 1.0));
@@ -1167,7 +1180,7 @@ __device__ __forceinline__ void bc3_col(const Grid &g, const Q5 &q, const BC3Arg
                     (-(0.5 * q.v[1][a1] * q.v[1][a1] + 0.5 * q.v[2][a1] * q.v[2][a1] + 0.5 * q.v[3][a1] * q.v[3][a1]) /
                          q.v[0][a1] + q.v[4][a1]) /
                     q.v[0][a1];
-  const int64_t m = gidx(g, i, t, k), hh = gidx(g, i, -t, k);
+  const int64_t m = gidx(g, i, jw + sg * t, k), hh = gidx(g, i, jw - sg * t, k);
   const double um0 = q.v[1][m] / q.v[0][m], um1 = q.v[2][m] / q.v[0][m], um2 = q.v[3][m] / q.v[0][m];
   const double Tt = (t + 1) * a.Twall - t * Ta;
   const double rh = M2 * gama * Pw / Tt;
@@ -1181,6 +1194,14 @@ __device__ __forceinline__ void bc3_col(const Grid &g, const Q5 &q, const BC3Arg
     q.v[2][w] = 0.0;
     q.v[3][w] = 0.0;
     q.v[4][w] = ew;
+  }
+}
+
+__device__ __forceinline__ void bc3_col(const Grid &g, const Q5 &q, const BC3Args &a, int i, int t, int k) {
+  wall3_point(g, q, a, i, 0, 1, t, k);
+  if (a.wall1) {  // the channel's second wall (rows n1-1 .. n1+2; the generated code's row n1+3 is never read)
+    wall3_point(g, q, a, i, g.n1 - 1, -1, t, k);
+  } else if (t == 1) {
     const double x0 = a.delta0 * i;  // Dirichlet top face
     const double *st = x0 > a.xs ? a.hi : a.lo;
     for (int j = g.n1 - 1; j < g.n1 + HY; ++j) {
@@ -1215,6 +1236,22 @@ __global__ void __launch_bounds__(BC2_THREADS) k3w_bc(Grid g, Q5 q, BC3Args a, i
   }
 }
 
+// Periodic x0 of a channel block (exchange.py:9-57) on the interior planes, after the wall faces
+// (which act on single x0 columns, so the order does not change a value): columns -4..-1 take
+// n0-4..n0-1 and columns n0..n0+3 take 0..3, every padded row.
+__global__ void k3w_wrapx(Grid g, Q5 q) {
+  const int rows = g.n1 + 2 * HY;
+  const int64_t N = (int64_t)rows * g.n2 * HX;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < 5 * N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int v = (int)(t / N);
+    const int64_t e = t % N;
+    const int x = (int)(e % HX), j = (int)((e / HX) % rows) - HY, k = (int)(e / ((int64_t)HX * rows));
+    double *f = q.v[v];
+    f[gidx(g, x - HX, j, k)] = f[gidx(g, g.n0 - HX + x, j, k)];
+    f[gidx(g, g.n0 + x, j, k)] = f[gidx(g, x, j, k)];
+  }
+}
+
 // Periodic x2 (exchange.py:9-57): planes -3..-1 take n2-3..n2-1 and planes n2..n2+2 take 0..2,
 // whole padded x0-x1 planes.
 __global__ void k3w_wrap(Grid g, Q5 q) {
@@ -1239,7 +1276,8 @@ template <typename T> __global__ void k3w_to_state(int64_t numel, Q5 src, Q5T<T>
 }
 
 // Viscous terms (momentum 0..2, energy) at every interior point, as k2_visc with the third
-// component and the periodic x2 derivatives: d/dx1 = D11 d/dxi1, d2/dx1^2 = D11^2 d2/dxi1^2 +
+// component and the periodic x2 derivatives (and x0 ones on channel blocks), mu from Sutherland's law
+// or, with vexp > 0, the power law T^vexp (turbulent_channel.py:30): d/dx1 = D11 d/dxi1, d2/dx1^2 = D11^2 d2/dxi1^2 +
 // D11 SD111 d/dxi1, mixed derivatives nest first derivatives (the inner x0 or x2 derivative over the
 // extended range of the outer axis).  A 32 x 8 x-x1 tile stages u0, u1, u2, T and mu of the planes
 // k-2..k+2 and of V2H points around it in x0 and x1 in dynamic shared memory; the primitives are
@@ -1251,7 +1289,7 @@ template <typename T> constexpr size_t visc3_smem() {
 template <typename T>
 __global__ void __launch_bounds__(V2X * V2Y) k3w_visc(Grid g, Q5T<const T> q, const double *D11, const double *SD111,
                                                       Q5T<T> rv, Visc2Args va, double gama, double gM2, double suth,
-                                                      int clx, int cly) {
+                                                      double vexp, int clx, int cly) {
   constexpr int SX = V2X + 2 * V2H, SY = V2Y + 2 * V2H, PL = SX * SY;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *sm = reinterpret_cast<T *>(smem_raw);  // [field u0 u1 u2 T mu][plane k-2..k+2][SY][SX]
@@ -1281,7 +1319,7 @@ __global__ void __launch_bounds__(V2X * V2Y) k3w_visc(Grid g, Q5T<const T> q, co
 #pragma unroll
     for (int c = 0; c < 3; ++c) S(c, z, lj, li) = u[c];
     S(3, z, lj, li) = Tt;
-    S(4, z, lj, li) = (S1 + T(1)) * Tt * sqrt_t(Tt) / (S1 + Tt);
+    S(4, z, lj, li) = vexp > 0.0 ? pow_t(Tt, T(vexp)) : (S1 + T(1)) * Tt * sqrt_t(Tt) / (S1 + Tt);
   }
   __syncthreads();
   const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
@@ -1306,7 +1344,7 @@ __global__ void __launch_bounds__(V2X * V2Y) k3w_visc(Grid g, Q5T<const T> q, co
     const T fy = id1 * d1c<T>(Y, j, g.n1, cly);
     gr[f][1] = Dm * fy;
     gr[f][2] = dz1(Z);
-    h[f][0][0] = id0 * id0 * d2c<T>(X, i, g.n0);
+    h[f][0][0] = id0 * id0 * d2c<T>(X, i, g.n0, clx);
     h[f][1][1] = Dm * Dm * (id1 * id1 * d2c<T>(Y, j, g.n1)) + Dm * Sm * fy;
     h[f][2][2] = dz2(Z);
     // x0 derivative of row j+o / of plane k+o, then the outer derivative
@@ -1326,7 +1364,7 @@ __global__ void __launch_bounds__(V2X * V2Y) k3w_visc(Grid g, Q5T<const T> q, co
   const T mug[3] = {id0 * d1c<T>(Xmu, i, g.n0, clx), Dm * id1 * d1c<T>(Ymu, j, g.n1, cly), dz1(Zmu)};
   const T Tyx = id1 * d1c<T>(YT, j, g.n1, cly);
   const T Tg[3] = {id0 * d1c<T>(XT, i, g.n0, clx), Dm * Tyx, dz1(ZT)};
-  const T Tlap = id0 * id0 * d2c<T>(XT, i, g.n0) + (Dm * Dm * (id1 * id1 * d2c<T>(YT, j, g.n1)) + Dm * Sm * Tyx) + dz2(ZT);
+  const T Tlap = id0 * id0 * d2c<T>(XT, i, g.n0, clx) + (Dm * Dm * (id1 * id1 * d2c<T>(YT, j, g.n1)) + Dm * Sm * Tyx) + dz2(ZT);
   const T div = gr[0][0] + gr[1][1] + gr[2][2];
   const T uu[3] = {S(0, 2, lj, li), S(1, 2, lj, li), S(2, 2, lj, li)};
   T e = T(va.kappa) * (mu * Tlap + mug[0] * Tg[0] + mug[1] * Tg[1] + mug[2] * Tg[2]);
@@ -1353,10 +1391,16 @@ __global__ void __launch_bounds__(V2X * V2Y) k3w_visc(Grid g, Q5T<const T> q, co
 struct BF3 {
   const double *xy, *z, *t;
 };
+// the channel's constant forcing c_j (turbulent_channel.py:15-16): -c_i in the momentum equations,
+// -c_j u_j in the energy equation, u_j from the FP64 state the stage started from (on = 0: none)
+struct Force3 {
+  double c[3];
+  int on;
+};
 
 template <typename T>
 __global__ void k3w_rk(Grid g, Q5T<const T> rf, Q5T<const T> rv, Q5 du, Q5 q64, double dt, double A, double B,
-                       int update, BF3 bf) {
+                       int update, BF3 bf, Force3 fo) {
   const int64_t N = (int64_t)g.n0 * g.n1 * g.n2;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(t % g.n0), j = (int)((t / g.n0) % g.n1), k = (int)(t / ((int64_t)g.n0 * g.n1));
@@ -1367,16 +1411,25 @@ __global__ void k3w_rk(Grid g, Q5T<const T> rf, Q5T<const T> rv, Q5 du, Q5 q64, 
 #pragma unroll
     for (int v = 1; v < 5; ++v) R[v] += rv.v[v - 1][c];
     if (bf.xy) R[0] += T(bf.xy[(int64_t)j * g.n0 + i] * bf.z[k] * bf.t[0]);
+    double Rd[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) Rd[v] = to_f64(R[v]);
+    if (fo.on) {
+      const double ir = 1.0 / q64.v[0][c];
+      Rd[4] -= fo.c[0] * (q64.v[1][c] * ir) + fo.c[1] * (q64.v[2][c] * ir) + fo.c[2] * (q64.v[3][c] * ir);
+#pragma unroll
+      for (int d = 0; d < 3; ++d) Rd[1 + d] -= fo.c[d];
+    }
     if (update) {
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        const double d = dt * to_f64(R[v]) + A * du.v[v][c];
+        const double d = dt * Rd[v] + A * du.v[v][c];
         du.v[v][c] = d;
         q64.v[v][c] = B * d + q64.v[v][c];
       }
     } else {
 #pragma unroll
-      for (int v = 0; v < 5; ++v) du.v[v][c] = to_f64(R[v]);
+      for (int v = 0; v < 5; ++v) du.v[v][c] = Rd[v];
     }
   }
 }
@@ -1460,7 +1513,8 @@ void launch3w_metrics(const Ctx &c, const double *x1_line, cudaStream_t s, int64
   ++*launches;
 }
 
-// face conditions and the x2 wrap on the FP64 master, then the working state from it
+// face conditions (and the x0 wrap of a channel block) and the x2 wrap on the FP64 master, then the
+// working state from it
 template <typename T> void launch3w_bcs(const Ctx &c, cudaStream_t s, int64_t *launches) {
   const osb_plan_desc &p = c.plan;
   BC3Args a;
@@ -1474,11 +1528,20 @@ template <typename T> void launch3w_bcs(const Ctx &c, cudaStream_t s, int64_t *l
     a.hi[v] = p.dirichlet_state[1][v];
   }
   a.ke = p.dirichlet_ke;
-  const int rows = c.g.n1 - 5 > 0 ? c.g.n1 - 5 : 0, cols = c.g.n0 - 3 > 0 ? c.g.n0 - 3 : 0;
+  a.per0 = p.bc[0][0] == OSB_BC_PERIODIC;
+  a.wall1 = p.bc[1][1] == OSB_BC_ISOTHERMAL_WALL;
+  const int rows = (c.g.n1 - 5 > 0 && !a.per0) ? c.g.n1 - 5 : 0, cols = c.g.n0 - 3 > 0 ? c.g.n0 - 3 : 0;
   const int row_blocks = (rows + BC2_THREADS - 1) / BC2_THREADS;
   const int col_blocks = (3 * cols + BC2_THREADS - 1) / BC2_THREADS;
   k3w_bc<<<dim3(1 + row_blocks + col_blocks, c.g.n2), BC2_THREADS, 0, s>>>(c.g, q5(c.qold), a, row_blocks);
-  int nb = (int)((5 * c.g.sz * HZ + 255) / 256);
+  int nb;
+  if (a.per0) {
+    nb = (int)((5 * (int64_t)(c.g.n1 + 2 * HY) * c.g.n2 * HX + 255) / 256);
+    if (nb > c.num_sms * 8) nb = c.num_sms * 8;
+    k3w_wrapx<<<nb, 256, 0, s>>>(c.g, q5(c.qold));
+    ++*launches;
+  }
+  nb = (int)((5 * c.g.sz * HZ + 255) / 256);
   if (nb > c.num_sms * 8) nb = c.num_sms * 8;
   k3w_wrap<<<nb, 256, 0, s>>>(c.g, q5(c.qold));
   nb = (int)((c.g.numel + 255) / 256);
@@ -1519,7 +1582,7 @@ void launch3w_rhs(const Ctx &c, int update, double A, double B, double dt, cudaS
   dim3 gv((c.g.n0 + V2X - 1) / V2X, (c.g.n1 + V2Y - 1) / V2Y, c.g.n2);
   k3w_visc<T><<<gv, dim3(V2X, V2Y), visc3_smem<T>(), c.side2[1]>>>(
       c.g, q5t<const T>(c.qa), c.d11, c.sd111, rv, va, p.gama, p.gama * p.Minf * p.Minf, p.SuthT / p.RefT,
-      closure_bits(p, 0), closure_bits(p, 1));
+      p.visc == OSB_VISC_POWER ? p.visc_exp : 0.0, closure_bits(p, 0), closure_bits(p, 1));
   cudaEventRecord(c.ev_join2[1], c.side2[1]);
   cudaStreamWaitEvent(s, c.ev_join2[1], 0);
   Q5T<const T> rf{{r.v[0], r.v[1], r.v[2], r.v[3], r.v[4]}};
@@ -1527,7 +1590,9 @@ void launch3w_rhs(const Ctx &c, int update, double A, double B, double dt, cudaS
   int nb = (int)(((int64_t)c.g.n0 * c.g.n1 * c.g.n2 + 255) / 256);
   if (nb > c.num_sms * 8) nb = c.num_sms * 8;
   const BF3 bf{c.bf_xy, c.bf_z, c.bf_t};
-  k3w_rk<T><<<nb, 256, 0, s>>>(c.g, rf, rvc, q5(c.du2), q5(c.qold), dt, A, B, update, bf);
+  const Force3 fo{{p.forcing[0], p.forcing[1], p.forcing[2]},
+                  p.forcing[0] != 0.0 || p.forcing[1] != 0.0 || p.forcing[2] != 0.0};
+  k3w_rk<T><<<nb, 256, 0, s>>>(c.g, rf, rvc, q5(c.du2), q5(c.qold), dt, A, B, update, bf, fo);
   *launches += 2;
 }
 

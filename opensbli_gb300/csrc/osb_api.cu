@@ -34,6 +34,8 @@ int cuda_err(osb_ctx *c, cudaError_t e, const char *where) {
 
 // a span-periodic 3D wall-bounded block (the 2D shock/boundary-layer faces in x0 and x1)
 bool wall3(const osb_plan_desc &p) { return p.ndim == 3 && p.bc[1][0] == OSB_BC_ISOTHERMAL_WALL; }
+// the channel form of a 3D wall-bounded block: periodic x0, isothermal walls on both x1 faces
+bool channel3(const osb_plan_desc &p) { return wall3(p) && p.bc[0][0] == OSB_BC_PERIODIC; }
 
 // the characteristic-flux schemes of the 3D kernels (WENO5-JS, WENO5-Z, TENO5)
 bool char_fluxes(const osb_plan_desc &p) {
@@ -47,6 +49,10 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
   if (!(p->shock_fp64 == 0.0 || (p->shock_fp64 >= 1.0 && std::isfinite(p->shock_fp64)))) {
     snprintf(why, n, "shock_fp64 = %g: 0 (off) or a pressure ratio >= 1", p->shock_fp64);
     return OSB_EINVAL;
+  }
+  if (!wall3(*p) && (p->forcing[0] != 0 || p->forcing[1] != 0 || p->forcing[2] != 0)) {
+    snprintf(why, n, "forcing: 3D wall-bounded blocks only");
+    return OSB_EUNSUPPORTED;
   }
   if (p->ndim == 2) {
     for (int d = 0; d < 2; ++d) {
@@ -88,10 +94,15 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
   }
   if (p->ndim != 3) { snprintf(why, n, "ndim %d: this library implements 2D and 3D blocks", p->ndim); return OSB_EUNSUPPORTED; }
   if (wall3(*p)) {
-    // span-periodic wall-bounded block: the 2D configuration's faces in x0 and x1, periodic x2
-    if (p->bc[0][0] != OSB_BC_INLET_PRESSURE_EXTRAPOLATE || p->bc[0][1] != OSB_BC_EXTRAPOLATION ||
-        p->bc[1][1] != OSB_BC_DIRICHLET || p->bc[2][0] != OSB_BC_PERIODIC || p->bc[2][1] != OSB_BC_PERIODIC) {
-      snprintf(why, n, "3D wall-bounded blocks: inlet/extrapolation (x0), isothermal wall/Dirichlet (x1), periodic x2");
+    // span-periodic wall-bounded block: the 2D configuration's faces in x0 and x1, or the channel's
+    // periodic x0 and isothermal walls on both x1 faces; periodic x2
+    const bool sbli = p->bc[0][0] == OSB_BC_INLET_PRESSURE_EXTRAPOLATE && p->bc[0][1] == OSB_BC_EXTRAPOLATION &&
+                      p->bc[1][1] == OSB_BC_DIRICHLET;
+    const bool chan = p->bc[0][0] == OSB_BC_PERIODIC && p->bc[0][1] == OSB_BC_PERIODIC &&
+                      p->bc[1][1] == OSB_BC_ISOTHERMAL_WALL;
+    if (!(sbli || chan) || p->bc[2][0] != OSB_BC_PERIODIC || p->bc[2][1] != OSB_BC_PERIODIC) {
+      snprintf(why, n, "3D wall-bounded blocks: inlet/extrapolation (x0) with isothermal wall/Dirichlet (x1), or "
+                       "periodic x0 with isothermal walls on both x1 faces; periodic x2");
       return OSB_EUNSUPPORTED;
     }
     for (int d = 0; d < 3; ++d) {
@@ -119,7 +130,16 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
                    p->closure[d][side]);
           return OSB_EINVAL;
         }
-    if (p->visc != OSB_VISC_SUTHERLAND) { snprintf(why, n, "3D wall-bounded blocks: Sutherland viscosity"); return OSB_EUNSUPPORTED; }
+    if (p->visc != OSB_VISC_SUTHERLAND && p->visc != OSB_VISC_POWER) {
+      snprintf(why, n, "3D wall-bounded blocks: Sutherland or power-law viscosity");
+      return OSB_EUNSUPPORTED;
+    }
+    if (p->visc == OSB_VISC_POWER && !(p->visc_exp > 0 && p->visc_exp < 8)) {
+      snprintf(why, n, "visc_exp must lie in (0, 8)");
+      return OSB_EINVAL;
+    }
+    for (int k = 0; k < 3; ++k)
+      if (!std::isfinite(p->forcing[k])) { snprintf(why, n, "forcing[%d] must be finite", k); return OSB_EINVAL; }
     if (p->rk != OSB_RK3_LS) { snprintf(why, n, "3D wall-bounded blocks: low-storage RK3"); return OSB_EUNSUPPORTED; }
     if (p->precision != OSB_PREC_FP64 && p->precision != OSB_PREC_MIXED) { snprintf(why, n, "precision %d", p->precision); return OSB_EINVAL; }
     if (!(p->gama > 1.0) || !(p->Minf > 0) || !(p->Re > 0) || !(p->Pr > 0) || !(p->Twall > 0) || !(p->RefT > 0)) {

@@ -66,6 +66,13 @@ class Plan:
     # sin(omega dt iter) in the continuity equation (apps/transitional_SBLI/transitional_SBLI.py)
     dirichlet_ke: bool = False
     body_force: Optional[Tuple[float, ...]] = None
+    # channel blocks (apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py): visc="power" takes
+    # mu = T^visc_exp; forcing = (c0, c1, c2) subtracts c_i from the momentum equations and c_j u_j
+    # from the energy equation; x1_grid="tanh" clusters x1 at both walls (used by the oracle)
+    visc_exp: float = 0.7
+    forcing: Optional[Tuple[float, ...]] = None
+    x1_grid: str = "sinh"           # sinh: Lx1 sinh(by eta)/sinh(by) | tanh: -tanh(stretch (1-2eta))/tanh(stretch)
+    stretch: float = 1.7
     rk_a: Tuple[float, float, float] = RK3_RKOLD
     rk_b: Tuple[float, float, float] = RK3_RKNEW
     use_graphs: bool = True
@@ -106,7 +113,7 @@ class Plan:
     @classmethod
     def from_json(cls, s):
         d = json.loads(s)
-        for k in ("n", "delta", "rk_a", "rk_b", "dirichlet_lo", "dirichlet_hi", "body_force"):
+        for k in ("n", "delta", "rk_a", "rk_b", "dirichlet_lo", "dirichlet_hi", "body_force", "forcing"):
             if d.get(k) is not None:
                 d[k] = tuple(d[k])
         d["bc"] = tuple(tuple(x) for x in d["bc"])
@@ -182,6 +189,23 @@ def transitional_plan(n0=500, n1=200, n2=100, precision="fp64", dt=0.025, use_gr
                 teno_adaptive=True, teno_a1=9.5, teno_a2=3.5, sensor_eps=1e-12, Lx1=140.0, by=5.0,
                 dirichlet_lo=pre, dirichlet_hi=post, dirichlet_x_switch=20.0, dirichlet_ke=True,
                 body_force=(2.5e-3, 20.0, 4.0, 0.23, 0.1011), name="transitional_%dx%dx%d" % (n0, n1, n2))
+
+
+def channel_plan(n0=129, n1=129, n2=129, precision="fp64", dt=2e-4, use_graphs=True, conv="teno6"):
+    """The block of apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py (statistics off):
+    Re = 190.71, Minf = 0.0955, Pr = 0.7, gama = 1.4, Twall = 1, mu = T^0.7, the forcing c = (-1, 0, 0),
+    domain 4 pi x 2 x 4 pi/3 periodic in x0 and x2 with isothermal walls on both x1 faces (Carpenter
+    closures), x1 = -tanh(1.7 (1 - 2 eta))/tanh(1.7), LLFTeno(6) with C_T = 1e-7 and eps = 1e-15,
+    RungeKuttaLS(3, 'SSP'); 129^3 points and dt = 2e-4 as the script sets them."""
+    A, B = ls_rk3_ssp_coefficients()
+    carp = (("carpenter", "carpenter"),) * 2
+    return Plan(ndim=3, n=(n0, n1, n2), delta=(4 * math.pi / n0, 2.0 / (n1 - 1), (4 * math.pi / 3) / n2), conv=conv,
+                visc="power", visc_exp=0.7, rk="ls_rk3", precision=precision,
+                bc=(("periodic", "periodic"), ("isothermal_wall", "isothermal_wall"), ("periodic", "periodic")),
+                gama=1.4, Minf=0.0955, Re=190.71, Pr=0.7, Twall=1.0, teno_ct=1e-7, teno_eps=1e-15,
+                weno_eps=1e-14 if conv == "weno5z" else 1e-6, rk_a=A, rk_b=B, dt=dt, use_graphs=use_graphs,
+                ic="host", closure=carp, forcing=(-1.0, 0.0, 0.0), x1_grid="tanh", stretch=1.7,
+                name="channel_%s_%dx%dx%d" % (conv, n0, n1, n2))
 
 
 def katzer_plan(n0=512, n1=256, precision="fp64", conv="teno5", dt=0.04, use_graphs=True, adaptive=False,

@@ -12,7 +12,7 @@ import torch
 
 from . import build as _build
 
-OSB_ABI_VERSION = 6
+OSB_ABI_VERSION = 7
 ERRORS = {
     -1: "invalid plan or argument",
     -2: "unsupported kernel pattern",
@@ -24,7 +24,7 @@ ERRORS = {
 }
 
 CONV = {"central_skew": 0, "weno5js": 1, "teno5": 2, "weno5z": 3, "teno6": 4}
-VISC = {"none": 0, "const": 1, "sutherland": 2}
+VISC = {"none": 0, "const": 1, "sutherland": 2, "power": 3}
 RK = {"rk3": 0, "ls_rk3": 1}
 BC = {"periodic": 0, "symmetry": 1, "inlet_pressure_extrapolate": 2, "extrapolation": 3, "isothermal_wall": 4,
       "dirichlet": 5}
@@ -70,6 +70,8 @@ class PlanDesc(ctypes.Structure):
         ("closure", (ctypes.c_int * 2) * 3),
         ("filter", ctypes.c_int),
         ("filter_control", ctypes.c_double),
+        ("visc_exp", ctypes.c_double),
+        ("forcing", ctypes.c_double * 3),
     ]
 
 
@@ -211,6 +213,9 @@ def make_plan_desc(plan):
             d.closure[a][side] = CLOSURE[plan.closure[a][side]]
     d.filter = FILTER[plan.filter]
     d.filter_control = plan.filter_control
+    d.visc_exp = plan.visc_exp
+    for k, v in enumerate(plan.forcing or (0.0,) * 3):
+        d.forcing[k] = v
     return d
 
 

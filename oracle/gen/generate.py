@@ -41,6 +41,7 @@ CASES = {
     "katzer_adaptive": "ref:apps/katzer_SBLI/katzer_SBLI.py",
     "sbli3d_teno": "sbli3d_teno.py",
     "transitional_sbli": "transitional_sbli.py",
+    "channel_teno": "channel_teno.py",
 }
 
 

@@ -254,6 +254,12 @@ class Cfg3W(ctypes.Structure):
         ("teno_a1", ctypes.c_double),
         ("teno_a2", ctypes.c_double),
         ("sensor_eps", ctypes.c_double),
+        ("periodic0", ctypes.c_int),
+        ("wall1", ctypes.c_int),
+        ("grid_tanh", ctypes.c_int),
+        ("stretch", ctypes.c_double),
+        ("visc_pow", ctypes.c_double),
+        ("force", ctypes.c_double * 3),
     ]
 
 
@@ -275,9 +281,10 @@ def make_cfg3w(plan):
         for side in range(2):
             c.closure[d][side] = CLOSURES[plan.closure[d][side]]
     c.conv = CONV[plan.conv]
-    for v in range(5):
-        c.dirichlet[0][v] = plan.dirichlet_lo[v]
-        c.dirichlet[1][v] = plan.dirichlet_hi[v]
+    if plan.bc[1][1] == "dirichlet":
+        for v in range(5):
+            c.dirichlet[0][v] = plan.dirichlet_lo[v]
+            c.dirichlet[1][v] = plan.dirichlet_hi[v]
     c.x_switch = plan.dirichlet_x_switch
     c.dirichlet_ke = 1 if getattr(plan, "dirichlet_ke", False) else 0
     bf = getattr(plan, "body_force", None) or (0.0, 0.0, 0.0, 0.0, 0.0)
@@ -285,6 +292,13 @@ def make_cfg3w(plan):
     c.teno_adaptive = 1 if getattr(plan, "teno_adaptive", False) else 0
     c.teno_a1, c.teno_a2 = getattr(plan, "teno_a1", 10.5), getattr(plan, "teno_a2", 4.5)
     c.sensor_eps = getattr(plan, "sensor_eps", 1e-12)
+    c.periodic0 = 1 if plan.bc[0][0] == "periodic" else 0
+    c.wall1 = 1 if plan.bc[1][1] == "isothermal_wall" else 0
+    c.grid_tanh = 1 if plan.x1_grid == "tanh" else 0
+    c.stretch = plan.stretch
+    c.visc_pow = plan.visc_exp if plan.visc == "power" else 0.0
+    for d, f in enumerate(plan.forcing or (0.0, 0.0, 0.0)):
+        c.force[d] = f
     return c
 
 

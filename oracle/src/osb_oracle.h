@@ -102,6 +102,14 @@ typedef struct {
   /* TENO cut-off adapted by the metric-transformed Ducros sensor (0: the fixed teno_ct) */
   int teno_adaptive;
   double teno_a1, teno_a2, sensor_eps;
+  /* channel blocks (apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py): periodic0 = 1
+   * makes x0 periodic (no inlet or outlet face), wall1 = 1 puts an isothermal wall on x1 side 1 (no
+   * Dirichlet face), grid_tanh = 1 takes x1 = -tanh(stretch (1 - 2 j/(n1-1))) / tanh(stretch),
+   * visc_pow > 0 takes mu = T^visc_pow (0: Sutherland), force = c_j of the momentum (-c_i) and energy
+   * (-c_j u_j) equations */
+  int periodic0, wall1, grid_tanh;
+  double stretch, visc_pow;
+  double force[3];
 } osbo3w_cfg;
 
 /* Advance q by nsteps LS-RK3 steps.  q holds [5][n2+8][n1+8][n0+8] with a 4-point halo on every side

@@ -1,7 +1,9 @@
 /* osb_oracle3w.c -- CPU restatement (FP64) of the generated per-timestep algorithm for a 3D
  * span-periodic wall-bounded block: the 2D shock/boundary-layer configuration of osb_oracle2d.c with
- * a periodic x2 axis (apps/transitional_SBLI/transitional_SBLI.py without its body force, statistics
- * and restart).
+ * a periodic x2 axis (apps/transitional_SBLI/transitional_SBLI.py without its statistics and
+ * restart), and the channel configuration (apps/channel_flow/compressible_TCF_TENO/
+ * turbulent_channel.py without its statistics): periodic x0, isothermal walls on both x1 faces,
+ * mu = T^0.7 and the constant forcing of the momentum and energy equations.
  *
  * TEST INFRASTRUCTURE ONLY (the parity oracle).  See osb_oracle.h.
  *
@@ -9,9 +11,11 @@
  *   before the loop: coordinates, metric derivative, D11 = 1/(dx1/dxi1), metric halos, SD111
  *   iter { BCs; stage { CRs; fluxes x0, x1, x2; flux residual; viscous terms; LS-RK update; BCs } }
  *   BCs = inlet (x0 side 0), outlet (x0 side 1), isothermal wall (x1 side 0), Dirichlet (x1 side 1),
- *         then the periodic exchange of x2 (exchange.py:9-57).
+ *         then the periodic exchange of x2 (exchange.py:9-57);
+ *   channel: the periodic exchange of x0, isothermal walls on both x1 faces, the exchange of x2.
  * The faces are pointwise in x2, so applying them to the interior planes and then wrapping the x2
- * halos gives what the generated code gives by applying them over the x2 halo range as well.
+ * halos gives what the generated code gives by applying them over the x2 halo range as well; the
+ * wall faces are pointwise in x0 too, so wrapping x0 after them equals wrapping it before.
  * Arrays carry a 5-point halo; the state exchanged with callers carries a 4-point halo.
  */
 #include <math.h>
@@ -61,7 +65,7 @@ static double *alloc3(const s3_t *s) { return (double *)calloc(s->np, sizeof(dou
 static int s3_init(s3_t *s, const osbo3w_cfg *cfg) {
   memset(s, 0, sizeof(*s));
   s->c = *cfg;
-  if (cfg->n[1] > 256 || cfg->n[2] < 4) return -1;
+  if (cfg->n[1] > 256 || cfg->n[2] < 4 || (cfg->periodic0 && cfg->n[0] < H)) return -1;
   double c24[24];
   osbo2d_carpenter_d1(c24);
   for (int r = 0; r < 4; ++r)
@@ -113,8 +117,10 @@ static void s3_free(s3_t *s) {
  * osb_oracle2d.c: ReducedAccess, reduced_access_scheme.py:34-83, or Carpenter,
  * Carpenter_scheme.py:6-102); x2 is periodic, every point takes the central stencil.
  * ------------------------------------------------------------------------------------------- */
+static int periodic_axis(const s3_t *s, int dir) { return dir == 2 || (dir == 0 && s->c.periodic0); }
+
 static double d1_stencil(const s3_t *s, int dir, int kk, int n, double (*G)(const void *, int), const void *ctx) {
-  if (dir == 2)
+  if (periodic_axis(s, dir))
     return (1.0 / 12.0) * G(ctx, -2) - (2.0 / 3.0) * G(ctx, -1) + (2.0 / 3.0) * G(ctx, 1) - (1.0 / 12.0) * G(ctx, 2);
   const int c0 = s->c.closure[dir][0], c1 = s->c.closure[dir][1];
   int side = -1, r = 0;
@@ -139,17 +145,20 @@ static double d1_stencil(const s3_t *s, int dir, int kk, int n, double (*G)(cons
   return v;
 }
 
-static double d2_stencil(int dir, int kk, int n, double (*G)(const void *, int), const void *ctx) {
-  if (dir != 2 && kk == 0)
+static double d2_stencil(const s3_t *s, int dir, int kk, int n, double (*G)(const void *, int), const void *ctx) {
+  if (periodic_axis(s, dir))
+    return -(1.0 / 12.0) * G(ctx, -2) + (4.0 / 3.0) * G(ctx, -1) - 2.5 * G(ctx, 0) + (4.0 / 3.0) * G(ctx, 1) -
+           (1.0 / 12.0) * G(ctx, 2);
+  if (kk == 0)
     return (35.0 / 12.0) * G(ctx, 0) - (26.0 / 3.0) * G(ctx, 1) + 9.5 * G(ctx, 2) - (14.0 / 3.0) * G(ctx, 3) +
            (11.0 / 12.0) * G(ctx, 4);
-  if (dir != 2 && kk == 1)
+  if (kk == 1)
     return (11.0 / 12.0) * G(ctx, -1) - (5.0 / 3.0) * G(ctx, 0) + 0.5 * G(ctx, 1) + (1.0 / 3.0) * G(ctx, 2) -
            (1.0 / 12.0) * G(ctx, 3);
-  if (dir != 2 && kk == n - 1)
+  if (kk == n - 1)
     return (35.0 / 12.0) * G(ctx, 0) - (26.0 / 3.0) * G(ctx, -1) + 9.5 * G(ctx, -2) - (14.0 / 3.0) * G(ctx, -3) +
            (11.0 / 12.0) * G(ctx, -4);
-  if (dir != 2 && kk == n - 2)
+  if (kk == n - 2)
     return (11.0 / 12.0) * G(ctx, 1) - (5.0 / 3.0) * G(ctx, 0) + 0.5 * G(ctx, -1) + (1.0 / 3.0) * G(ctx, -2) -
            (1.0 / 12.0) * G(ctx, -3);
   return -(1.0 / 12.0) * G(ctx, -2) + (4.0 / 3.0) * G(ctx, -1) - 2.5 * G(ctx, 0) + (4.0 / 3.0) * G(ctx, 1) -
@@ -180,19 +189,22 @@ static double d1c(const s3_t *s, const double *f, int i, int j, int k, int dir) 
 static double d2c(const s3_t *s, const double *f, int i, int j, int k, int dir) {
   const pt_t p = {s, f, i, j, k, dir};
   const int n = dir == 0 ? N0 : dir == 1 ? N1 : N2, kk = dir == 0 ? i : dir == 1 ? j : k;
-  return (1.0 / (s->c.delta[dir] * s->c.delta[dir])) * d2_stencil(dir, kk, n, G3, &p);
+  return (1.0 / (s->c.delta[dir] * s->c.delta[dir])) * d2_stencil(s, dir, kk, n, G3, &p);
 }
 
 /* ---------------------------------------------------------------------------------------------
  * Metrics (equation_types/metric.py:37-234, 315-332), stretched in x1 only, so functions of j:
- * x1(j) = Lx1 sinh(by delta1 j / Lx1) / sinh(by), D11 = 1/(dx1/dxi1) with the x1 closures, halos
- * mirrored about the boundary points, SD111 = dD11/dxi1.
+ * x1(j) = Lx1 sinh(by delta1 j / Lx1) / sinh(by) (or the channel's tanh clustering), D11 =
+ * 1/(dx1/dxi1) with the x1 closures, halos mirrored about the boundary points, SD111 = dD11/dxi1.
  * ------------------------------------------------------------------------------------------- */
 static double G1(const void *ctx, int o) { return ((const double *)ctx)[o]; }
 
 static void metrics(s3_t *s) {
   const double Lx1 = s->c.Lx1, by = s->c.by, d1 = s->c.delta[1];
-  for (int j = -3; j < N1 + 4; ++j) s->x1[j + H] = sinh(d1 * by * (1.0 / Lx1) * j) / ((1.0 / Lx1) * sinh(by));
+  for (int j = -3; j < N1 + 4; ++j)
+    s->x1[j + H] = s->c.grid_tanh /* turbulent_channel.py:167-170, Ly = 2 */
+                       ? 0.5 * 2.0 * (1.0 - tanh(s->c.stretch * (1.0 - 2.0 * (j / (N1 - 1.0)))) / tanh(s->c.stretch)) - 1.0
+                       : sinh(d1 * by * (1.0 / Lx1) * j) / ((1.0 / Lx1) * sinh(by));
   double wk[256 + 2 * H];
   for (int j = 0; j < N1; ++j) wk[j + H] = (1.0 / d1) * d1_stencil(s, 1, j, N1, G1, &s->x1[j + H]);
   for (int j = 0; j < N1; ++j) s->D11[j + H] = 1.0 / wk[j + H];
@@ -208,7 +220,7 @@ static void metrics(s3_t *s) {
 static void apply_bcs(s3_t *s) {
   const double g = s->c.gama, M = s->c.Minf, Tw = s->c.Twall;
   for (int k = 0; k < N2; ++k) {
-    for (int j = -3; j < N1 + 4; ++j) { /* InletPressureExtrapolateBC (inlet_pressure_extrapolate.py:11-66) */
+    for (int j = -3; j < N1 + 4 && !s->c.periodic0; ++j) { /* InletPressureExtrapolateBC (inlet_pressure_extrapolate.py:11-66) */
       const size_t b = I3(s, 0, j, k);
       const double rhob = s->q[0][b];
       const double ub0 = fabs(s->q[1][b] / rhob), ub1 = fabs(s->q[2][b] / rhob), ub2 = fabs(s->q[3][b] / rhob);
@@ -220,7 +232,7 @@ static void apply_bcs(s3_t *s) {
         for (int t = 1; t <= 3; ++t) s->q[4][I3(s, -t, j, k)] = s->q[4][b];
       }
     }
-    for (int j = -3; j < N1 + 4; ++j) /* ExtrapolationBC order 0 (extrapolation.py:8-58) */
+    for (int j = -3; j < N1 + 4 && !s->c.periodic0; ++j) /* ExtrapolationBC order 0 (extrapolation.py:8-58) */
       for (int v = 0; v < 5; ++v) {
         const double val = s->q[v][I3(s, N0 - 2, j, k)];
         for (int t = 0; t <= 4; ++t) s->q[v][I3(s, N0 - 1 + t, j, k)] = val;
@@ -247,7 +259,27 @@ static void apply_bcs(s3_t *s) {
         s->q[4][h] = (1.0 / (g - 1)) * Pw + 0.5 * rh * (um[0] * um[0] + um[1] * um[1] + um[2] * um[2]);
       }
     }
-    for (int j = N1 - 1; j < N1 + 4; ++j) /* DirichletBC, piecewise in x0 */
+    for (int i = -3; i < N0 + 4 && s->c.wall1; ++i) { /* IsothermalWallBC on side 1 (isothermal_wall.py:32-88) */
+      const int jw = N1 - 1;
+      const size_t w = I3(s, i, jw, k), a1 = I3(s, i, jw - 1, k);
+      for (int c = 1; c <= 3; ++c) s->q[c][w] = 0.0;
+      s->q[4][w] = Tw * (1.0 / (M * M)) * s->q[0][w] / (g * (g - 1.0));
+      const double Pw = (g - 1) * s->q[4][w];
+      const double Ta = M * M * g * (g - 1) *
+                        (-(0.5 * s->q[1][a1] * s->q[1][a1] + 0.5 * s->q[2][a1] * s->q[2][a1] +
+                           0.5 * s->q[3][a1] * s->q[3][a1]) / s->q[0][a1] + s->q[4][a1]) /
+                        s->q[0][a1];
+      for (int t = 1; t <= 4; ++t) {
+        const size_t m = I3(s, i, jw - t, k), h = I3(s, i, jw + t, k);
+        const double um[3] = {s->q[1][m] / s->q[0][m], s->q[2][m] / s->q[0][m], s->q[3][m] / s->q[0][m]};
+        const double Tt = (t + 1) * Tw - t * Ta;
+        const double rh = M * M * g * Pw / Tt;
+        s->q[0][h] = rh;
+        for (int c = 0; c < 3; ++c) s->q[1 + c][h] = -rh * um[c];
+        s->q[4][h] = (1.0 / (g - 1)) * Pw + 0.5 * rh * (um[0] * um[0] + um[1] * um[1] + um[2] * um[2]);
+      }
+    }
+    for (int j = N1 - 1; j < N1 + 4 && !s->c.wall1; ++j) /* DirichletBC, piecewise in x0 */
       for (int i = -3; i < N0 + 4; ++i) {
         const double x0 = s->c.delta[0] * i;
         const double *st = s->c.dirichlet[x0 > s->c.x_switch ? 1 : 0];
@@ -260,6 +292,14 @@ static void apply_bcs(s3_t *s) {
         }
       }
   }
+  if (s->c.periodic0) /* periodic x0 */
+    for (int v = 0; v < 5; ++v)
+      for (int k = 0; k < N2; ++k)
+        for (int j = -H; j < N1 + H; ++j)
+          for (int i = -H; i < 0; ++i) {
+            s->q[v][I3(s, i, j, k)] = s->q[v][I3(s, i + N0, j, k)];
+            s->q[v][I3(s, N0 - 1 - i, j, k)] = s->q[v][I3(s, -1 - i, j, k)];
+          }
   for (int v = 0; v < 5; ++v) /* periodic x2 */
     for (int k = -H; k < 0; ++k)
       for (int j = -H; j < N1 + H; ++j)
@@ -270,7 +310,7 @@ static void apply_bcs(s3_t *s) {
 }
 
 /* Constituent relations (transitional_SBLI.py:33-38): u_i, p, a over -3..n+4 in x0, x1 and the x2
- * halos; T and mu (Sutherland) over -2..n+2. */
+ * halos; T and mu (Sutherland, or the power law) over -2..n+2. */
 static void constituent(s3_t *s) {
   const double g = s->c.gama, M = s->c.Minf, ST = s->c.SuthT / s->c.RefT;
   FOR3(-3, N0 + 4, -3, N1 + 4, -3, N2 + 3) {
@@ -286,7 +326,8 @@ static void constituent(s3_t *s) {
   FOR3(-2, N0 + 2, -2, N1 + 2, -2, N2 + 2) {
     const size_t n = I3(s, i, j, k);
     s->T[n] = M * M * g * s->p[n] / s->q[0][n];
-    s->mu[n] = (ST + 1.0) * pow(s->T[n], 1.5) / (ST + s->T[n]);
+    s->mu[n] = s->c.visc_pow > 0.0 ? pow(s->T[n], s->c.visc_pow) /* turbulent_channel.py:30 */
+                                    : (ST + 1.0) * pow(s->T[n], 1.5) / (ST + s->T[n]);
   }
 }
 
@@ -326,6 +367,18 @@ static void body_force(s3_t *s, int it) {
     s->res[0][I3(s, i, j, k)] += s->c.bf_A * exp(-(x0 - s->c.bf_xF) * (x0 - s->c.bf_xF) -
                                                  (x1 - s->c.bf_yF) * (x1 - s->c.bf_yF)) *
                                  st * cos(s->c.bf_bta * x2);
+  }
+}
+
+/* The channel's constant forcing (turbulent_channel.py:15-16): -c_i in the momentum equations,
+ * -c_j u_j in the energy equation. */
+static void forcing(s3_t *s) {
+  const double *f = s->c.force;
+  if (f[0] == 0.0 && f[1] == 0.0 && f[2] == 0.0) return;
+  FOR3(0, N0, 0, N1, 0, N2) {
+    const size_t c = I3(s, i, j, k);
+    for (int d = 0; d < 3; ++d) s->res[1 + d][c] -= f[d];
+    s->res[4][c] -= f[0] * s->u[0][c] + f[1] * s->u[1][c] + f[2] * s->u[2][c];
   }
 }
 
@@ -484,6 +537,7 @@ int osbo3w_run(const osbo3w_cfg *cfg, double *q, int nsteps) {
     for (int stg = 0; stg < 3; ++stg) {
       constituent(s);
       residual_flux(s);
+      forcing(s);
       body_force(s, it);
       residual_viscous(s);
       /* RungeKuttaLS (rk_LS.py:155-166): du = A du + dt R; q = q + B du */
@@ -511,6 +565,7 @@ int osbo3w_residual(const osbo3w_cfg *cfg, const double *q, double *r) {
   apply_bcs(s);
   constituent(s);
   residual_flux(s);
+  forcing(s);
   body_force(s, 0);
   residual_viscous(s);
   size_t m = 0;

@@ -70,6 +70,8 @@ CASES_3W = {
     # with the spanwise kinetic energy
     # (forcing centred on a grid point of this coarse grid and 20x stronger, so that it shows)
     "transitional_sbli": ((32, 24, 8), 20, {"dt": 0.2, "A": 0.05, "xF": 2 * 375.0 / 31}),
+    # the compressible_TCF_TENO channel block (statistics off) at the script's dt
+    "channel_teno": ((32, 24, 16), 40, {"dt": 2e-4}),
 }
 VARS_3W = ["rho", "rhou0", "rhou1", "rhou2", "rhoE"]
 

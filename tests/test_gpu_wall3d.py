@@ -159,3 +159,65 @@ def test_transitional_graph_matches_eager_and_mixed_error():
     mom = float(np.linalg.norm(ref[1]))
     l2 = [float(np.linalg.norm(qm[v] - ref[v]) / (mom if v in (1, 2, 3) else np.linalg.norm(ref[v]))) for v in range(5)]
     assert np.isfinite(qm).all() and max(l2) <= 1e-5, l2
+
+
+# ---- the channel block (apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py, statistics
+# off): periodic x0 and x2, isothermal walls on both x1 faces, mu = T^0.7, the constant forcing
+# c = (-1, 0, 0), tanh-clustered x1, TENO6 with C_T = 1e-7, Carpenter closures ----
+
+def golden_ch():
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_channel_teno.npz"))
+    return d["q0"], d["x1"], d["q"], tuple(int(x) for x in d["n"]), int(d["steps"]), json.loads(str(d["params"]))
+
+
+def test_channel_fp64_matches_reference_golden():
+    from opensbli_gb300.plan import channel_plan
+    q0, x1, q_ref, n, steps, params = golden_ch()
+    q = run_gpu(channel_plan(*n, dt=params["dt"]), q0, x1, steps, params["dt"])
+    err = rel_err(q, q_ref[INNER])
+    assert max(err) <= 5e-12, err  # TENO6's rounding floor, as on the other wall-bounded blocks
+
+
+@pytest.mark.parametrize("conv,closure,shapes", [
+    ("teno5", "carpenter", (("tile", 32), ("tile", 32), ("tile", 32))),
+    ("weno5js", "reduced_access", (("march8", 16), ("march8", 24), ("march8", 20))),
+])
+def test_channel_fp64_matches_oracle(conv, closure, shapes):
+    from opensbli_gb300.plan import channel_plan
+    q0, x1, _, n, _, params = golden_ch()
+    plan = channel_plan(*n, dt=params["dt"], conv=conv).replace(closure=((closure, closure),) * 2)
+    q_or = O.run3w(plan, q0, 4)[INNER]
+    q = run_gpu(plan, q0, x1, 4, params["dt"], shapes)
+    err = rel_err(q, q_or)
+    assert max(err) <= 1e-12, err
+
+
+def test_channel_residual_matches_oracle():
+    """The right-hand side (fluxes, viscous terms with mu = T^0.7, forcing) on the interior."""
+    from opensbli_gb300.plan import channel_plan
+    q0, x1, _, n, _, params = golden_ch()
+    plan = channel_plan(*n, dt=params["dt"])
+    r_or = O.residual3w(plan, q0)
+    s = Solver(plan)
+    s.set_coordinate(x1, 4)
+    s.set_state64_padded(q0[:, 1:-1, 1:-1, 1:-1], 3)
+    r = s.residual().cpu().numpy()
+    s.close()
+    scale = [np.abs(r_or[v]).max() for v in range(5)]
+    err = [float(np.abs(r[v] - r_or[v]).max() / scale[v]) for v in range(5)]
+    assert max(err) <= 1e-11, err
+
+
+def test_channel_graph_matches_eager_and_mixed_error():
+    from opensbli_gb300.plan import channel_plan
+    q0, x1, q_ref, n, steps, params = golden_ch()
+    plan = channel_plan(*n, dt=params["dt"])
+    a = run_gpu(plan, q0, x1, 5, params["dt"])
+    b = run_gpu(plan.replace(use_graphs=False), q0, x1, 5, params["dt"])
+    assert np.array_equal(a, b)
+    qm = run_gpu(plan.replace(precision="mixed"), q0, x1, steps, params["dt"])
+    ref = q_ref[INNER]
+    mom = float(np.linalg.norm(ref[1]))
+    l2 = [float(np.linalg.norm(qm[v] - ref[v]) / (mom if v in (1, 2, 3) else np.linalg.norm(ref[v]))) for v in range(5)]
+    assert np.isfinite(qm).all() and max(l2) <= 1e-5, l2

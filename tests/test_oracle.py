@@ -214,3 +214,31 @@ def test_oracle_transitional_matches_reference_golden():
     # without the body force the result differs: the oracle's force is the reference's
     q0 = O.run3w(plan.replace(body_force=(0.0,) * 5), d["q0"], int(d["steps"]))
     assert float(np.abs(q0[inner][0] - ref[0]).max()) > 1e-3
+
+
+def test_oracle_channel_matches_reference_golden():
+    """osb_oracle3w.c with the channel block of apps/channel_flow/compressible_TCF_TENO (periodic x0 and
+    x2, isothermal walls on both x1 faces, mu = T^0.7, the forcing c = (-1, 0, 0), tanh-clustered x1,
+    TENO6) against the reference's generated code: 32 x 24 x 16, 40 steps at the script's dt."""
+    import json
+    from opensbli_gb300.plan import channel_plan
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_channel_teno.npz"))
+    n = tuple(int(x) for x in d["n"])
+    params = json.loads(str(d["params"]))
+    plan = channel_plan(*n, dt=params["dt"])
+    # the coordinate line of the fixture is the plan's tanh clustering
+    j = np.arange(-4, n[1] + 4)
+    x1 = -np.tanh(plan.stretch * (1 - 2 * j / (n[1] - 1))) / np.tanh(plan.stretch)
+    assert np.abs(x1 - d["x1"]).max() < 1e-15
+    q = O.run3w(plan, d["q0"], int(d["steps"]))
+    inner = (slice(None), slice(4, -4), slice(4, -4), slice(4, -4))
+    ref = d["q"][inner]
+    err = [float(np.abs(q[inner][v] - ref[v]).max() / np.abs(ref[v]).max()) for v in range(5)]
+    assert max(err) < 1e-12, err
+    assert min(float(np.abs(ref[v] - d["q0"][inner][v]).max() / np.abs(ref[v]).max()) for v in range(5)) > 1e-2
+    # the forcing enters the right-hand side as -c_i and -c_j u_j
+    r1 = O.residual3w(plan, d["q0"])
+    r0 = O.residual3w(plan.replace(forcing=(0.0, 0.0, 0.0)), d["q0"])
+    q0 = d["q0"][inner]
+    assert np.abs((r1[1] - r0[1]) - 1.0).max() < 1e-12
+    assert np.abs((r1[4] - r0[4]) - q0[1] / q0[0]).max() < 1e-10 * np.abs(q0[1] / q0[0]).max()
