@@ -65,10 +65,11 @@ class PhysicsCheck:
     formulas of a 3D block with constant viscosity, or a 2D or 3D block stretched in x1 with Sutherland
     viscosity."""
 
-    def __init__(self, components, ndim, viscous, sutherland=False, metric=False, skew=False, body_force=False):
+    def __init__(self, components, ndim, viscous, sutherland=False, metric=False, skew=False, body_force=False,
+                 visc_exp=None, forcing=False):
         self.components = [c for c in components if type(c).__name__ == "Kernel"]
         self.ndim, self.viscous, self.sutherland, self.metric, self.skew = ndim, viscous, sutherland, metric, skew
-        self.body_force = body_force
+        self.body_force, self.visc_exp, self.forcing = body_force, visc_exp, forcing
         self.rnd = random.Random(2024)
         self.delta = (0.37, 0.53, 0.61)  # test spacings for the 1/delta factors
         self.consts = {"gama": 1.4, "Minf": 0.7, "Re": 950.0, "Pr": 0.72, "SuthT": 110.4, "RefT": 288.0}
@@ -112,7 +113,10 @@ class PhysicsCheck:
         out["T"] = g * M * M * p / rho
         out["a"] = math.sqrt(g * p / rho)
         S = self.consts["SuthT"] / self.consts["RefT"]
-        out["mu"] = out["T"] ** 1.5 * (1 + S) / (out["T"] + S)
+        if self.visc_exp is not None:  # the power law (turbulent_channel.py:30)
+            out["mu"] = out["T"] ** self.visc_exp
+        else:
+            out["mu"] = out["T"] ** 1.5 * (1 + S) / (out["T"] + S)
         return out
 
     def _random_state(self):
@@ -397,7 +401,10 @@ class PhysicsCheck:
                     else:
                         self._fail("characteristic residual reads %s" % a)
                 elif t == "ConstantObject":
-                    reps[a] = sympy.Float(self._const_value(a), 30)
+                    if self.forcing and re.fullmatch(r"c[0-2]", str(a)):
+                        reps[a] = sympy.Symbol("_c%s" % str(a)[1])  # the channel's forcing constants
+                    else:
+                        reps[a] = sympy.Float(self._const_value(a), 30)
                 else:
                     self._fail("characteristic residual reads the local %s" % a)
             # every flux array appears at i and at i-1 along one axis, one array per axis
@@ -419,6 +426,13 @@ class PhysicsCheck:
                         (pts["D11"] if (self.metric and d == 1) else 1) for d in range(self.ndim))
             if lhs == "Residual0" and sympy.Symbol("_bf") in got.free_symbols:
                 want = want + sympy.Symbol("_bf")
+            if self.forcing:  # -c_i (momentum i), -c_j u_j (energy): turbulent_channel.py:15-16
+                c = [sympy.Symbol("_c%d" % j) for j in range(self.ndim)]
+                r = int(lhs[len("Residual"):])
+                if 1 <= r <= self.ndim:
+                    want = want - c[r - 1]
+                elif r == self.ndim + 1:
+                    want = want - sum(c[j] * pts["u%d" % j] for j in range(self.ndim))
             for trial in range(3):
                 vals = {s: sympy.Float(self.rnd.uniform(-2, 2), 30) for s in got.free_symbols | want.free_symbols}
                 a, b = float(got.xreplace(vals)), float(want.xreplace(vals))
@@ -426,11 +440,14 @@ class PhysicsCheck:
                     self._fail("characteristic residual %s is not -sum_d dF_d/dx_d" % lhs)
 
 
-def check_algorithm(components, ndim, viscous, sutherland=False, metric=False, skew=False, body_force=False):
+def check_algorithm(components, ndim, viscous, sutherland=False, metric=False, skew=False, body_force=False,
+                    visc_exp=None, forcing=False):
     """Raise NotImplementedError unless the algorithm's constituent relations, derivative stencils and
     residual kernels are the ones the fused kernels implement (see the module docstring).  body_force:
-    the continuity residual may add the BF array (recognised by the writer)."""
+    the continuity residual may add the BF array (recognised by the writer); visc_exp: mu = T^visc_exp
+    instead of Sutherland's law; forcing: the characteristic residual subtracts the constants c_i
+    (momentum) and c_j u_j (energy)."""
     pc = PhysicsCheck(components, ndim, viscous, sutherland=sutherland, metric=metric, skew=skew,
-                      body_force=body_force)
+                      body_force=body_force, visc_exp=visc_exp, forcing=forcing)
     pc.check_constituent_relations()
     pc.check_residuals()

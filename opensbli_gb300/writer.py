@@ -314,7 +314,10 @@ class GB300Writer:
         if not self._kernels("MetricsEquation") or not self._kernels("Metric boundary"):
             raise NotImplementedError("2D blocks: metric terms expected")
         if not any(n.startswith("CRmu") for n in names):
-            raise NotImplementedError("2D blocks: Sutherland viscosity (CRmu) expected")
+            raise NotImplementedError("wall-bounded blocks: a viscosity relation (CRmu) expected")
+        visc_exp = self._power_law_viscosity()
+        if visc_exp is not None and nd != 3:
+            raise NotImplementedError("2D blocks: Sutherland viscosity")
         coeff = self._rk_coefficients(["Temporal solution advancement"])
         if set(coeff) != {"rkA", "rkB"}:
             raise NotImplementedError("RungeKuttaLS(3) coefficients rkA/rkB expected")
@@ -323,25 +326,38 @@ class GB300Writer:
             "Extrapolation boundary dir0 side1": ("extrapolation", 0, 1),
             "IsothermalWall boundary dir1 side0": ("isothermal_wall", 1, 0),
             "Dirichlet boundary dir1 side1": ("dirichlet", 1, 1),
+            "IsothermalWall boundary dir1 side1": ("isothermal_wall", 1, 1),
         }
         bcs = [[None, None], [None, None]]
         for kname, (kind, d, side) in faces.items():
             if self._kernels(kname):
+                if bcs[d][side] is not None:
+                    raise NotImplementedError("two boundary conditions on face dir%d side%d" % (d, side))
                 bcs[d][side] = kind
-        if any(b is None for pair in bcs for b in pair):
+        # a periodic x0 (the channel, apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py): the
+        # exchanges of both sides and no boundary kernel on that axis
+        per0 = {c.side for c in self.components if type(c).__name__ == "ExchangeSelf" and c.direction == 0}
+        if nd == 3 and per0 == {"left", "right"} and bcs[0] == [None, None]:
+            bcs[0] = ["periodic", "periodic"]
+        known = ([["inlet_pressure_extrapolate", "extrapolation"], ["isothermal_wall", "dirichlet"]],
+                 [["periodic", "periodic"], ["isothermal_wall", "isothermal_wall"]])
+        if bcs not in known or (bcs == known[1] and nd != 3):
             found = sorted(n for n in names if "boundary dir" in n)
             raise NotImplementedError("wall-bounded boundary conditions: %s" % found)
+        channel = bcs == known[1]
+        if channel and visc_exp is None:
+            raise NotImplementedError("channel blocks: the power-law viscosity expected")
         if nd == 3:
             # x2 periodic: the exchanges of both sides and no boundary kernel on that axis
             per = {c.side for c in self.components if type(c).__name__ == "ExchangeSelf" and c.direction == 2}
             other = [n for n in names if "boundary dir" in n and n not in faces and not n.startswith("Metric boundary")]
             if per != {"left", "right"} or other:
                 raise NotImplementedError("3D wall-bounded blocks: periodic x2 expected (found %s)" % (other or per))
-        closure = self._closures_2d()
+        closure = self._closures_2d(periodic0=channel)
         # the Dirichlet face: rho, rhou0, rhou1 (, rhou2), rhoE = Piecewise((hi, x0 > xs), (lo, True)); on 3D
         # blocks rhoE may instead be a constant plus the point's spanwise kinetic energy
         # rhou2^2/(2 rho) with rhou2 left as it is (apps/transitional_SBLI/transitional_SBLI.py:110-116)
-        dk = self._kernels("Dirichlet boundary dir1 side1")[0]
+        dk = self._kernels("Dirichlet boundary dir1 side1")
         lo, hi, xs, ke = {}, {}, None, False
 
         def value(v, name):
@@ -361,7 +377,7 @@ class GB300Writer:
             ke = True
             return c
 
-        for e in dk.equations:
+        for e in (dk[0].equations if dk else []):
             name = re.sub(r"_B0$", "", str(getattr(e.lhs, "base", e.lhs)))
             rhs = e.rhs
             if isinstance(rhs, sympy.Piecewise) and len(rhs.args) == 2:
@@ -377,24 +393,65 @@ class GB300Writer:
             if "rhou2" in lo:
                 raise NotImplementedError("Dirichlet face: rhou2 set with rhoE carrying its kinetic energy")
             lo["rhou2"] = hi["rhou2"] = 0.0  # kept at the face, not set
-        if any(v not in lo for v in order):
+        if dk and any(v not in lo for v in order):
             raise NotImplementedError("Dirichlet face must set %s" % ", ".join(order))
         bf = self._body_force() if nd == 3 else None
+        forcing = self._forcing(teno or weno) if nd == 3 else None
         physics_check.check_algorithm(self.components, nd, viscous=True, sutherland=True, metric=True,
-                                      body_force=bf is not None)
+                                      body_force=bf is not None, visc_exp=visc_exp, forcing=forcing is not None)
+        extra = {}
+        if channel:  # the coordinate line comes from the script's grid equations (initial_fields)
+            extra = dict(visc_exp=visc_exp, forcing=forcing, x1_grid="tanh")
+        else:
+            extra = dict(dirichlet_lo=tuple(lo[v] for v in order), dirichlet_hi=tuple(hi[v] for v in order),
+                         dirichlet_x_switch=xs if xs is not None else 1e300)
         return Plan(ndim=nd, n=(64, 32, 1) if nd == 2 else (64, 32, 16), delta=(1.0, 1.0, 1.0), conv=conv,
                     weno_eps=1e-14 if conv == "weno5z" else 1e-6,  # WenoZ.eps / WenoJS.eps (weno.py)
-                    visc="sutherland", rk="ls_rk3", precision=precision,
+                    visc="power" if channel else "sutherland", rk="ls_rk3", precision=precision,
                     bc=(tuple(bcs[0]), tuple(bcs[1]), ("periodic", "periodic")),
                     rk_a=coeff["rkA"], rk_b=coeff["rkB"], use_graphs=use_graphs, ic="host",
-                    name="wall3d" if nd == 3 else Plan.name,
-                    dirichlet_lo=tuple(lo[v] for v in order), dirichlet_hi=tuple(hi[v] for v in order),
-                    dirichlet_x_switch=xs if xs is not None else 1e300, kernels=[n for n in names if n],
-                    dirichlet_ke=ke, body_force=bf,
+                    name=("channel" if channel else "wall3d") if nd == 3 else Plan.name,
+                    kernels=[n for n in names if n], dirichlet_ke=ke, body_force=bf, **extra,
                     teno_adaptive=adaptive is not None,
                     sensor_eps=adaptive if adaptive is not None else Plan.sensor_eps, closure=closure)
 
     _BF_CONSTS = ("A", "xF", "yF", "bta", "omega")
+
+    def _power_law_viscosity(self):
+        """The viscosity relation of the CRmu kernel: None for Sutherland's law (katzer_SBLI.py:25,
+        checked with the other relations), else the exponent a of mu = T^a
+        (apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py:30)."""
+        import sympy
+        eqs = [e for k in self._kernels("CRmu") for e in k.equations if str(getattr(e.lhs, "base", "")) == "mu_B0"]
+        if len(eqs) != 1:
+            raise NotImplementedError("viscosity: one relation for mu expected")
+        r = eqs[0].rhs
+        if isinstance(r, sympy.Pow) and type(r.base).__name__ == "DataSet" and str(r.base.base) == "T_B0" and \
+                all(int(i) == 0 for i in r.base.indices) and r.exp.is_number:
+            return float(r.exp)
+        return None
+
+    def _forcing(self, reconstruction):
+        """The constant forcing of turbulent_channel.py:15-16 (- KD(_i,_j) c_j in the momentum
+        equations, - Dot(c_j, u_j) in the energy equation): the constants c0, c1, c2 of the
+        characteristic residual kernel (their form is checked by physics_check).  Returns None without
+        them, else their values as far as the algorithm knows them (the simulation parameters complete
+        them)."""
+        import sympy
+        found = {}
+        for k in self._kernels(""):
+            if not re.match(r"LLF(Weno|Teno) Residual", (k.computation_name or "").strip()):
+                continue
+            for e in k.equations:
+                for a in sympy.preorder_traversal(e.rhs):
+                    if type(a).__name__ == "ConstantObject" and re.fullmatch(r"c[0-2]", str(a)):
+                        found[int(str(a)[1])] = a
+        if not found:
+            return None
+        if len(found) != self.block.ndim:
+            raise NotImplementedError("forcing: constants %s" % sorted("c%d" % d for d in found))
+        vals = [getattr(found[d], "value", None) for d in range(3)]
+        return tuple(float(v) if isinstance(v, (int, float)) else 0.0 for v in vals)
 
     def _body_force(self):
         """Recognise the body force of apps/transitional_SBLI/transitional_SBLI.py:80-89: a constituent
@@ -447,7 +504,7 @@ class GB300Writer:
         vals = {str(a): getattr(a, "value", None) for a in syms if type(a).__name__ == "ConstantObject"}
         return tuple(float(vals[k]) if isinstance(vals.get(k), (int, float)) else 0.0 for k in self._BF_CONSTS)
 
-    def _closures_2d(self):
+    def _closures_2d(self, periodic0=False):
         """The one-sided closure each face applies to the central derivatives of its direction
         (opensblifunctions.py:523-534 wraps every central derivative in a Piecewise over the grid
         index): ReducedAccess closes the first two points of a face (reduced_access_scheme.py:34-83),
@@ -484,6 +541,11 @@ class GB300Writer:
         kinds = {2: "reduced_access", 4: "carpenter"}
         out = []
         for d in range(2):
+            if d == 0 and periodic0:  # no closure on a periodic axis (the field is unused there)
+                if depth[(0, 0)] or depth[(0, 1)]:
+                    raise NotImplementedError("periodic x0 with one-sided derivative closures")
+                out.append(("carpenter", "carpenter"))
+                continue
             pair = []
             for side in range(2):
                 if depth[(d, side)] not in kinds:
@@ -646,6 +708,10 @@ class GB300Writer:
             kw.update(teno_eps=float(env.get("eps", p.teno_eps)), teno_ct=float(env.get("TENO_CT", p.teno_ct)))
         if p.body_force is not None:
             kw["body_force"] = tuple(float(env.get(k, v)) for k, v in zip(self._BF_CONSTS, p.body_force))
+        if p.forcing is not None:
+            kw["forcing"] = tuple(float(env.get("c%d" % d, v)) for d, v in enumerate(p.forcing))
+        if p.x1_grid == "tanh":
+            kw["stretch"] = float(env.get("stretch", p.stretch))
         if p.rk == "ls_rk3":  # wall-bounded blocks
             kw.update(Twall=float(env.get("Twall", p.Twall)), SuthT=float(env.get("SuthT", p.SuthT)),
                       RefT=float(env.get("RefT", p.RefT)), teno_eps=float(env.get("eps", p.teno_eps)),

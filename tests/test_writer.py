@@ -102,6 +102,32 @@ def test_transitional_script_lowers_to_its_plan():
     assert g.teno_adaptive and g.conv == "teno6" and g.dirichlet_ke and g.body_force == (2.5e-3, 20.0, 4.0, 0.23, 0.1011)
 
 
+def test_channel_script_lowers_to_its_plan():
+    """The channel script (compressible_TCF_TENO, statistics off) lowers with periodic x0, isothermal
+    walls on both x1 faces, the power-law viscosity and the constant forcing, to channel_plan's plan."""
+    from opensbli_gb300.plan import channel_plan
+    g = golden_plan("channel_teno")
+    p = channel_plan(*g.n)
+    assert g.replace(kernels=[], name="", niter=None) == p.replace(kernels=[], name="")
+    assert g.visc == "power" and g.visc_exp == 0.7 and g.forcing == (-1.0, 0.0, 0.0)
+    assert g.bc[0] == ("periodic", "periodic") and g.bc[1] == ("isothermal_wall", "isothermal_wall")
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
+def test_channel_initial_state_matches_reference(tmp_path):
+    """The channel's initial condition (laminar/log profile with sinusoidal perturbations) and its
+    tanh-clustered coordinates, evaluated by the writer, against the generated code's."""
+    r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", "channel_teno",
+                        "--out", str(tmp_path), "--ref", REF, "--params", "block0np0=32,block0np1=24,block0np2=16"],
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-3000:]
+    d = np.load(os.path.join(GOLDEN, "ref_channel_teno.npz"))
+    ic = np.load(tmp_path / "ic.npy")
+    ref = d["q0"][:, 4:-4, 4:-4, 4:-4]
+    assert ic.shape == ref.shape
+    assert np.abs(ic - ref).max() <= 1e-13 * np.abs(ref).max(), float(np.abs(ic - ref).max())
+
+
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
 def test_3d_wall_initial_state_matches_reference(tmp_path):
     import json
@@ -127,7 +153,7 @@ def test_writer_refuses_kernels_outside_the_lowered_families():
     dissipation sensor is lowered; its Ducros variant adds a shock-sensor kernel and is refused."""
     from opensbli_gb300.writer import GB300Writer
     for case in ("tgv_central", "tgv_weno", "tgsym_central", "katzer_teno", "katzer_adaptive", "katzer_carpenter",
-                 "tgv_filter", "tgv_teno_adaptive", "sbli3d_teno", "transitional_sbli"):
+                 "tgv_filter", "tgv_teno_adaptive", "sbli3d_teno", "transitional_sbli", "channel_teno"):
         GB300Writer._check_kernel_families(golden_plan(case).kernels)
     assert "User kernel: Non-linear filter application" in golden_plan("tgv_filter").kernels
     names = golden_plan("tgv_filter").kernels + ["User kernel: Shock sensor"]
@@ -155,7 +181,7 @@ def test_cfl_dt_tgv_weno():
 @pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central",
                                   "katzer_teno", "katzer_adaptive", "katzer_carpenter", "tgv_filter",
                                   "katzer_weno", "katzer_wenoz", "katzer_teno6", "tgv_teno_adaptive",
-                                  "sbli3d_teno", "transitional_sbli"])
+                                  "sbli3d_teno", "transitional_sbli", "channel_teno"])
 def test_writer_lowers_reference_script(case, tmp_path):
     r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case, "--out",
                         str(tmp_path), "--ref", REF], capture_output=True, text=True, timeout=900)
