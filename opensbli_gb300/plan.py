@@ -208,6 +208,39 @@ def channel_plan(n0=129, n1=129, n2=129, precision="fp64", dt=2e-4, use_graphs=T
                 name="channel_%s_%dx%dx%d" % (conv, n0, n1, n2))
 
 
+def channel_initial_state(plan, halo=3):
+    """The initial state of apps/channel_flow/compressible_TCF_TENO/turbulent_channel.py:167-199 on a
+    channel_plan block, halos included: x1 = -tanh(stretch (1 - 2 j/(n1-1)))/tanh(stretch), the mean
+    velocity (1 - |x1|) Re where that is below 10 and 2.5 log((1 - |x1|) Re) + 5.5 elsewhere, plus the
+    script's sinusoidal perturbations of amplitude 0.1 (2.5 log(Re) + 5.5); rho = 1, p = 1/(gama Minf^2).
+    The box lengths are n0 delta0 (4 pi) and n2 delta2 (4 pi / 3).  Returns (q, x1): FP64
+    [5][n2+2h][n1+2h][n0+2h] and the coordinate line [n1+2h]."""
+    import numpy as np
+    n0, n1, n2 = plan.n
+    h = int(halo)
+    lx, lz = n0 * plan.delta[0], n2 * plan.delta[2]
+    j = np.arange(-h, n1 + h, dtype=np.float64)
+    y1 = -np.tanh(plan.stretch * (1.0 - 2.0 * j / (n1 - 1.0))) / np.tanh(plan.stretch)
+    x = (np.arange(-h, n0 + h) * plan.delta[0])[None, None, :]
+    y = y1[None, :, None]
+    z = (np.arange(-h, n2 + h) * plan.delta[2])[:, None, None]
+    Re, b, kv = plan.Re, 5.5, 2.5
+    wall = (1.0 - np.abs(y)) * Re
+    with np.errstate(invalid="ignore", divide="ignore"):
+        ubar = np.where(wall < 10.0, wall, kv * np.log(wall) + b)
+    amp = 0.1 * (kv * np.log(Re) + b)
+    sx, sy, sz = np.sin(4.0 * np.pi * x / lx), np.sin(np.pi * y), np.sin(2.0 * np.pi * z / lz)
+    cx, cy, cz = np.cos(4.0 * np.pi * x / lx), 1.0 + np.cos(np.pi * y), np.cos(2.0 * np.pi * z / lz)
+    u = ubar + amp * (lx / 2.0) * cx * sy * sz
+    v = -amp * sx * cy * sz
+    w = -amp * (lz / 2.0) * sx * sy * cz
+    shape = (n2 + 2 * h, n1 + 2 * h, n0 + 2 * h)
+    u, v, w = (np.broadcast_to(a, shape) for a in (u, v, w))
+    p = 1.0 / (plan.gama * plan.Minf ** 2)
+    q = np.stack([np.ones(shape), u, v, w, p / (plan.gama - 1.0) + 0.5 * (u * u + v * v + w * w)])
+    return np.ascontiguousarray(q), y1
+
+
 def katzer_plan(n0=512, n1=256, precision="fp64", conv="teno5", dt=0.04, use_graphs=True, adaptive=False,
                 closure=(("reduced_access", "reduced_access"),) * 2):
     """2D laminar shock-wave/boundary-layer interaction (apps/katzer_SBLI/katzer_SBLI.py constants):

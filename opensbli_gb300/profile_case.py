@@ -4,10 +4,12 @@
         [--shape 1:march4:48 --shape 2:march4:48] [--central-ty 16] [--adaptive] [--filter]
     python -m opensbli_gb300.profile_case --katzer 512 [--conv teno5|teno6|weno5js|weno5z] [--adaptive]
     python -m opensbli_gb300.profile_case --sbli3d 256 --n2 64 [--conv ...]
+    python -m opensbli_gb300.profile_case --channel 129 [--conv ...]
 
 Runs the Taylor-Green vortex (or, with --katzer N0, the 2D shock/boundary-layer block N0 x 256 from
 the boundary-layer profile in tests/golden/katzer_ic_n256.npz, or with --sbli3d N0 the span-periodic
-3D block N0 x 256 x n2 from the same profile with a spanwise momentum 0.05 sin(2 pi k / n2)) with
+3D block N0 x 256 x n2 from the same profile with a spanwise momentum 0.05 sin(2 pi k / n2), or with
+--channel N the N^3 channel block of compressible_TCF_TENO from its initial condition) with
 the given scheme and precision
 for --steps RK3 steps after --warmup steps and prints the wall time per step (not a benchmark
 number: bench.py is).
@@ -33,11 +35,23 @@ def main():
     ap.add_argument("--katzer", type=int, default=0, help="2D shock/boundary-layer block of this many x0 points")
     ap.add_argument("--sbli3d", type=int, default=0, help="3D span-periodic block of this many x0 points")
     ap.add_argument("--n2", type=int, default=32, help="--sbli3d: points along the periodic x2 axis")
+    ap.add_argument("--channel", type=int, default=0, help="the N^3 channel block (turbulent_channel.py)")
     a = ap.parse_args()
     import torch
     from .plan import tgv_plan, tgv_cfl_dt
     from .runtime import Solver
-    if a.sbli3d:
+    if a.channel:
+        from .plan import channel_plan, channel_initial_state
+        a.conv = a.conv or "teno6"
+        plan = channel_plan(a.channel, a.channel, a.channel, precision=a.precision, conv=a.conv,
+                            use_graphs=not a.no_graphs)
+        dt = plan.dt
+        q, x1 = channel_initial_state(plan, halo=3)
+        s = Solver(plan)
+        s.set_coordinate(x1, 3)
+        s.set_state64_padded(q, 3)
+        a.n = a.channel
+    elif a.sbli3d:
         import os
         import numpy as np
         from .plan import sbli3d_plan

@@ -42,6 +42,7 @@ CASES = {
     "sbli3d_teno": "sbli3d_teno.py",
     "transitional_sbli": "transitional_sbli.py",
     "channel_teno": "channel_teno.py",
+    "shock_reflection": "ref:apps/inviscid_shock_reflection/inviscid_shock.py",
 }
 
 

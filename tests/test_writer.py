@@ -113,6 +113,17 @@ def test_channel_script_lowers_to_its_plan():
     assert g.bc[0] == ("periodic", "periodic") and g.bc[1] == ("isothermal_wall", "isothermal_wall")
 
 
+def test_channel_initial_state_helper_matches_reference():
+    """plan.channel_initial_state (the script's initial condition restated with numpy, for drivers that
+    run without the reference) against the generated code's initial state, halos included."""
+    from opensbli_gb300.plan import channel_plan, channel_initial_state
+    d = np.load(os.path.join(GOLDEN, "ref_channel_teno.npz"))
+    q, x1 = channel_initial_state(channel_plan(*(int(x) for x in d["n"])), halo=4)
+    assert np.abs(x1 - d["x1"]).max() <= 1e-15
+    err = [float(np.abs(q[v] - d["q0"][v]).max() / np.abs(d["q0"][v]).max()) for v in range(5)]
+    assert max(err) <= 1e-13, err
+
+
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
 def test_channel_initial_state_matches_reference(tmp_path):
     """The channel's initial condition (laminar/log profile with sinusoidal perturbations) and its
