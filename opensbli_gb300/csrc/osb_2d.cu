@@ -155,11 +155,19 @@ struct BC2Args {
   double gama, Minf, Twall, delta0, xs;
   int hx, hy;
   Dir2 st;
+  // Euler blocks: Dirichlet x0 faces (constant states f0 on side 0, f1 on side 1) instead of the inlet
+  // and the outlet; symmetry x1 faces instead of the wall (side 0) and the Dirichlet face (side 1)
+  int dir0, dir1, sym0, sym1;
+  double f0[4], f1[4];
 };
 
-// inlet (i = 0 and its halo) and outlet (i >= n0-1) of row j
+// inlet (i = 0 and its halo) and outlet (i >= n0-1) of row j, or the Dirichlet x0 faces
+// (dirichlet.py:6-41: the boundary point and the halo take the face's state)
 __device__ __forceinline__ void bc2_row(const Grid &g, const Q4 &q, const BC2Args &a, int j) {
-  {  // inlet
+  if (a.dir0) {
+    for (int i = -3; i <= 0; ++i)
+      for (int v = 0; v < 4; ++v) q.v[v][g2(g, i, j)] = a.f0[v];
+  } else {  // inlet
     const int64_t b = g2(g, 0, j), m1 = g2(g, -1, j);
     const double rhob = q.v[0][b];
     const double ub0 = fabs(q.v[1][b] / rhob), ub1 = fabs(q.v[2][b] / rhob);
@@ -172,15 +180,44 @@ __device__ __forceinline__ void bc2_row(const Grid &g, const Q4 &q, const BC2Arg
       for (int t = 1; t <= 3; ++t) q.v[3][g2(g, -t, j)] = e;
     }
   }
-  for (int v = 0; v < 4; ++v) {  // outlet
-    const double val = q.v[v][g2(g, g.n0 - 2, j)];
-    for (int t = 0; t <= a.hx; ++t) q.v[v][g2(g, g.n0 - 1 + t, j)] = val;
+  if (a.dir1) {
+    for (int t = 0; t <= a.hx; ++t)
+      for (int v = 0; v < 4; ++v) q.v[v][g2(g, g.n0 - 1 + t, j)] = a.f1[v];
+  } else {
+    for (int v = 0; v < 4; ++v) {  // outlet
+      const double val = q.v[v][g2(g, g.n0 - 2, j)];
+      for (int t = 0; t <= a.hx; ++t) q.v[v][g2(g, g.n0 - 1 + t, j)] = val;
+    }
   }
+}
+
+// SymmetryBC (symmetry.py) of column i on an x1 face whose boundary row is jb, the interior on the
+// side sg: the halo point jb - sg t mirrors jb + sg t with the normal momentum reversed; the boundary
+// point keeps its values.
+__device__ __forceinline__ void sym2_point(const Grid &g, const Q4 &q, int i, int jb, int sg, int t) {
+  const int64_t h = g2(g, i, jb - sg * t), m = g2(g, i, jb + sg * t);
+  q.v[0][h] = q.v[0][m];
+  q.v[1][h] = q.v[1][m];
+  q.v[2][h] = -q.v[2][m];
+  q.v[3][h] = q.v[3][m];
 }
 
 // isothermal wall halo point -t of column i (t = 1 also sets the wall point itself and the
 // Dirichlet top face of the column)
 __device__ __forceinline__ void bc2_col(const Grid &g, const Q4 &q, const BC2Args &a, int i, int t) {
+  if (a.sym0) {
+    sym2_point(g, q, i, 0, 1, t);
+    if (t == 1) {
+      if (a.sym1) {
+        for (int u = 1; u <= a.hy; ++u) sym2_point(g, q, i, g.n1 - 1, -1, u);
+      } else {
+        const double x0 = a.delta0 * i;  // Dirichlet top face
+        for (int j = g.n1 - 1; j < g.n1 + a.hy; ++j)
+          for (int v = 0; v < 4; ++v) q.v[v][g2(g, i, j)] = x0 > a.xs ? a.st.hi[v] : a.st.lo[v];
+      }
+    }
+    return;
+  }
   const double M2 = a.Minf * a.Minf, gama = a.gama;
   const int64_t w = g2(g, i, 0), a1 = g2(g, i, 1);
   // the wall point after this face: zero momentum, energy from Twall; its pressure
@@ -447,21 +484,39 @@ __device__ __forceinline__ T recon2(const T (&fp)[6], const T (&fm)[6], T eps, T
 // Characteristic flux between window points 2 and 3 along D (2D Euler eigensystem for a unit
 // normal, physical_models/euler_eigensystem.py:77-105; the block's metric is diagonal so the
 // eigensystem is Cartesian).  Dense rows share g = phi X0 - (g-1) u.X + (g-1) X3, h = X_{1+D} - u_D X0.
+// The state of the characteristic system at the interface between the points l and r (conserved
+// ql, qr, pressures and sound speeds): RoeAverage (averaging.py:62-114; rho = sqrt(rho_l rho_r), u
+// and H weighted by sqrt(rho), a from H) or, with simple, SimpleAverage (averaging.py:31-59: the
+// arithmetic means of rho, u = rhou/rho and a).
+template <typename T>
+__device__ __forceinline__ void avg2(const T (&ql)[4], const T (&qr)[4], T pl, T pr, T al, T ar, T gm1, bool simple,
+                                     T &rho, T (&u)[2], T &a) {
+  const T rl = ql[0], rr = qr[0];
+  if (simple) {
+    rho = T(0.5) * (rl + rr);
+#pragma unroll
+    for (int c = 0; c < 2; ++c) u[c] = T(0.5) * (qr[1 + c] / rr + ql[1 + c] / rl);
+    a = T(0.5) * (al + ar);
+    return;
+  }
+  const T sl = sqrt_t(rl), sr = sqrt_t(rr);
+  rho = sqrt_t(rl * rr);
+  const T inv_s = T(1) / (sl + sr);
+#pragma unroll
+  for (int c = 0; c < 2; ++c) u[c] = inv_s * (sl * (ql[1 + c] / rl) + sr * (qr[1 + c] / rr));
+  const T Hh = inv_s * ((pl + ql[3]) / sl + (pr + qr[3]) / sr);
+  a = sqrt_t(gm1 * (Hh - T(0.5) * (u[0] * u[0] + u[1] * u[1])));
+}
+
 template <typename T, int D, int SCH>
-__device__ __forceinline__ void flux2(const W2<T> (&W)[6], T gama, T eps, T ct, T out[4]) {
+__device__ __forceinline__ void flux2(const W2<T> (&W)[6], T gama, T eps, T ct, T out[4], bool simple) {
   constexpr int E = 1 - D;
   const T s = D == 0 ? T(1) : T(-1);
   const T gm1 = gama - T(1);
   const T rl = W[2].Q[0], rr = W[3].Q[0];
-  const T sl = sqrt_t(rl), sr = sqrt_t(rr);
-  const T rho = sqrt_t(rl * rr);
-  const T inv_s = T(1) / (sl + sr);
-  T u[2];
-#pragma unroll
-  for (int c = 0; c < 2; ++c) u[c] = inv_s * (sl * (W[2].Q[1 + c] / rl) + sr * (W[3].Q[1 + c] / rr));
-  const T Hh = inv_s * ((W[2].p + W[2].Q[3]) / sl + (W[3].p + W[3].Q[3]) / sr);
+  T rho, u[2], a;
+  avg2(W[2].Q, W[3].Q, W[2].p, W[3].p, W[2].a, W[3].a, gm1, simple, rho, u, a);
   const T usq = u[0] * u[0] + u[1] * u[1];
-  const T a = sqrt_t(gm1 * (Hh - T(0.5) * usq));
   const T ia = T(1) / a, irho = T(1) / rho;
   const T phi = gm1 * T(0.5) * usq;
   const T bt = T(0.70710678118654752440) * irho * ia, al = T(0.70710678118654752440) * rho * ia;
@@ -539,7 +594,7 @@ __device__ __forceinline__ void flux2(const W2<T> (&W)[6], T gama, T eps, T ct, 
 // rounded to FP32 once.
 template <typename T, int D, int SCH>
 __device__ __forceinline__ void flux2_delta(const W2<float> (&W)[6], const float (&dFf)[6][4], T gama, T eps, T ct,
-                                            float out[4]) {
+                                            float out[4], bool simple) {
   T dF[6][4];
 #pragma unroll
   for (int t = 0; t < 6; ++t)
@@ -548,16 +603,13 @@ __device__ __forceinline__ void flux2_delta(const W2<float> (&W)[6], const float
   constexpr int E = 1 - D;
   const T s = D == 0 ? T(1) : T(-1);
   const T gm1 = gama - T(1);
-  const T rl = T(W[2].Q[0]), rr = T(W[3].Q[0]);
-  const T sl = sqrt_t(rl), sr = sqrt_t(rr);
-  const T rho = sqrt_t(rl * rr);
-  const T inv_s = T(1) / (sl + sr);
-  T u[2];
-#pragma unroll
-  for (int c = 0; c < 2; ++c) u[c] = inv_s * (sl * (T(W[2].Q[1 + c]) / rl) + sr * (T(W[3].Q[1 + c]) / rr));
-  const T Hh = inv_s * ((T(W[2].p) + T(W[2].Q[3])) / sl + (T(W[3].p) + T(W[3].Q[3])) / sr);
+  T rho, u[2], a;
+  {
+    const T ql[4] = {T(W[2].Q[0]), T(W[2].Q[1]), T(W[2].Q[2]), T(W[2].Q[3])};
+    const T qr[4] = {T(W[3].Q[0]), T(W[3].Q[1]), T(W[3].Q[2]), T(W[3].Q[3])};
+    avg2(ql, qr, T(W[2].p), T(W[3].p), T(W[2].a), T(W[3].a), gm1, simple, rho, u, a);
+  }
   const T usq = u[0] * u[0] + u[1] * u[1];
-  const T a = sqrt_t(gm1 * (Hh - T(0.5) * usq));
   const T ia = T(1) / a, irho = T(1) / rho;
   const T phi = gm1 * T(0.5) * usq;
   const T bt = T(0.70710678118654752440) * irho * ia, al = T(0.70710678118654752440) * rho * ia;
@@ -641,7 +693,7 @@ template <> struct T2Tile<1> { static constexpr int TI = 24, TA = 16; };  // sta
 template <typename T, int D, int SCH, bool SH = false>
 __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<const T> pr, const double *D11,
                                                Q4T<T> res, double gama_d, double eps_d, double ct_d, double inv_dd,
-                                               const T *ctp, double shock) {
+                                               const T *ctp, double shock, int simple) {
   using Tl = T2Tile<D>;
   constexpr int TI = Tl::TI, TA = Tl::TA, NPT = TI + 5;
   constexpr int NF = s2nf<T>();
@@ -724,14 +776,14 @@ __global__ void __launch_bounds__(256) k2_flux(Grid g, Q4T<const T> q, Prims<con
         fp64 = fmaxf(pl, pr) > (float)shock * fminf(pl, pr);
       }
       if (fp64) {
-        if constexpr (SH) flux2_delta<double, D, SCH>(W, dF, gama_d, eps_d, ctp ? (double)ctl : ct_d, fl);
+        if constexpr (SH) flux2_delta<double, D, SCH>(W, dF, gama_d, eps_d, ctp ? (double)ctl : ct_d, fl, simple);
       } else {
-        flux2_delta<float, D, SCH>(W, dF, gama, eps, ctl, fl);
+        flux2_delta<float, D, SCH>(W, dF, gama, eps, ctl, fl, simple);
       }
 #pragma unroll
       for (int v = 0; v < 4; ++v) sdf[v][m][a] = -dF[1][v];  // F(point i) - F(point i-1)
     } else {
-      flux2<T, D, SCH>(W, gama, eps, ctl, fl);
+      flux2<T, D, SCH>(W, gama, eps, ctl, fl, simple);
     }
 #pragma unroll
     for (int v = 0; v < 4; ++v) sfl[v][m][a] = fl[v];
@@ -861,9 +913,11 @@ __global__ void k2_rk(Grid g, Q4T<const T> rx, Q4T<const T> ry, Q3T<const T> rv,
     T R[4];
 #pragma unroll
     for (int v = 0; v < 4; ++v) R[v] = rx.v[v][c] + ry.v[v][c];
-    R[1] += rv.v[0][c];
-    R[2] += rv.v[1][c];
-    R[3] += rv.v[2][c];
+    if (rv.v[0]) {  // viscous terms (none on Euler blocks)
+      R[1] += rv.v[0][c];
+      R[2] += rv.v[1][c];
+      R[3] += rv.v[2][c];
+    }
     if (update) {
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
@@ -966,7 +1020,13 @@ void launch2_bcs(const Ctx &c, cudaStream_t s, int64_t *launches) {
   for (int v = 0; v < 4; ++v) {
     a.st.lo[v] = p.dirichlet_state[0][v];
     a.st.hi[v] = p.dirichlet_state[1][v];
+    a.f0[v] = p.dirichlet_x0[0][v];
+    a.f1[v] = p.dirichlet_x0[1][v];
   }
+  a.dir0 = p.bc[0][0] == OSB_BC_DIRICHLET;
+  a.dir1 = p.bc[0][1] == OSB_BC_DIRICHLET;
+  a.sym0 = p.bc[1][0] == OSB_BC_SYMMETRY;
+  a.sym1 = p.bc[1][1] == OSB_BC_SYMMETRY;
   const int rows = c.g.n1 - 5 > 0 ? c.g.n1 - 5 : 0, cols = c.g.n0 - 3 > 0 ? c.g.n0 - 3 : 0;
   const int row_blocks = (rows + BC2_THREADS - 1) / BC2_THREADS;
   const int col_blocks = (3 * cols + BC2_THREADS - 1) / BC2_THREADS;
@@ -992,7 +1052,8 @@ static void launch2_flux(const Ctx &c, dim3 grid, Q4T<const T> q, Prims<const T>
   // the FP64-next-to-shocks instantiation when the plan asks for it (FP32 state only)
   const bool sh = sizeof(T) == 4 && p.shock_fp64 > 0.0;
   auto launch = [&](auto plain, auto shock) {
-    (sh ? shock : plain)<<<grid, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, idd, ctp, p.shock_fp64);
+    (sh ? shock : plain)<<<grid, 256, 0, s>>>(c.g, q, prc, c.d11, r, p.gama, eps, p.teno_ct, idd, ctp, p.shock_fp64,
+                                              p.averaging == OSB_AVG_SIMPLE);
   };
   if (p.conv == OSB_CONV_TENO5)
     launch(k2_flux<T, D, SCH_TENO, false>, k2_flux<T, D, SCH_TENO, sizeof(T) == 4>);
@@ -1053,9 +1114,13 @@ template <typename T> void launch2_rhs(const Ctx &c, int update, double A, doubl
   va.inv_d1 = 1.0 / p.delta[1];
   va.clx = closure_bits(p, 0);
   va.cly = closure_bits(p, 1);
-  Q3T<T> rv{{static_cast<T *>(c.resv[0]), static_cast<T *>(c.resv[1]), static_cast<T *>(c.resv[2])}};
-  dim3 gv((c.g.n0 + V2X - 1) / V2X, (c.g.n1 + V2Y - 1) / V2Y);
-  k2_visc<T><<<gv, dim3(V2X, V2Y), 0, c.side2[1]>>>(c.g, prc, c.d11, c.sd111, rv, va, c.hx2, c.hy2);
+  const bool visc = p.visc != OSB_VISC_NONE;
+  Q3T<T> rv{{nullptr, nullptr, nullptr}};
+  if (visc) {
+    rv = Q3T<T>{{static_cast<T *>(c.resv[0]), static_cast<T *>(c.resv[1]), static_cast<T *>(c.resv[2])}};
+    dim3 gv((c.g.n0 + V2X - 1) / V2X, (c.g.n1 + V2Y - 1) / V2Y);
+    k2_visc<T><<<gv, dim3(V2X, V2Y), 0, c.side2[1]>>>(c.g, prc, c.d11, c.sd111, rv, va, c.hx2, c.hy2);
+  }
   cudaEventRecord(c.ev_join2[0], c.side2[0]);
   cudaEventRecord(c.ev_join2[1], c.side2[1]);
   cudaStreamWaitEvent(s, c.ev_join2[0], 0);
@@ -1065,7 +1130,7 @@ template <typename T> void launch2_rhs(const Ctx &c, int update, double A, doubl
   if (nb > c.num_sms * 4) nb = c.num_sms * 4;
   k2_rk<T><<<nb, 256, 0, s>>>(c.g, q4t<const T>(c.res), q4t<const T>(c.resy), rvc, q4(c.du2), q4(c.q64_2d), dt, A, B,
                               update);
-  *launches += 5;
+  *launches += visc ? 5 : 4;
 }
 
 // The adaptive TENO cut-off of the current working state over the interior, as FP64 [n1][n0]
@@ -1279,109 +1344,125 @@ template <typename T> __global__ void k3w_to_state(int64_t numel, Q5 src, Q5T<T>
 // component and the periodic x2 derivatives (and x0 ones on channel blocks), mu from Sutherland's law
 // or, with vexp > 0, the power law T^vexp (turbulent_channel.py:30): d/dx1 = D11 d/dxi1, d2/dx1^2 = D11^2 d2/dxi1^2 +
 // D11 SD111 d/dxi1, mixed derivatives nest first derivatives (the inner x0 or x2 derivative over the
-// extended range of the outer axis).  A 32 x 8 x-x1 tile stages u0, u1, u2, T and mu of the planes
-// k-2..k+2 and of V2H points around it in x0 and x1 in dynamic shared memory; the primitives are
-// formed from the working state as they are staged (FP32: u, p and T rounded once, prims_f32).
+// extended range of the outer axis).  A block marches a 32 x 8 x-x1 tile through kz planes in x2: a
+// ring of five planes in dynamic shared memory holds u0, u1, u2, T and mu of the planes k-2..k+2 with
+// V2H points around the tile in x0 and x1, one plane staged per step; the primitives are formed from
+// the working state as they are staged (FP32: u, p and T rounded once, prims_f32).
+constexpr int VISC3_KZ = 8;  // x2 planes per block of the viscous kernel
 template <typename T> constexpr size_t visc3_smem() {
   return sizeof(T) * 5 * 5 * (size_t)(V2Y + 2 * V2H) * (V2X + 2 * V2H);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(V2X * V2Y) k3w_visc(Grid g, Q5T<const T> q, const double *D11, const double *SD111,
+__global__ void __launch_bounds__(V2X * V2Y, sizeof(T) == 4 ? 3 : 1) k3w_visc(Grid g, Q5T<const T> q, const double *D11, const double *SD111,
                                                       Q5T<T> rv, Visc2Args va, double gama, double gM2, double suth,
-                                                      double vexp, int clx, int cly) {
+                                                      double vexp, int clx, int cly, int kz) {
   constexpr int SX = V2X + 2 * V2H, SY = V2Y + 2 * V2H, PL = SX * SY;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *sm = reinterpret_cast<T *>(smem_raw);  // [field u0 u1 u2 T mu][plane k-2..k+2][SY][SX]
-  auto S = [&](int f, int z, int y, int x) -> T & { return sm[((f * 5 + z) * SY + y) * SX + x]; };
-  const int i0 = blockIdx.x * V2X, j0 = blockIdx.y * V2Y, k = blockIdx.z;
+  T *sm = reinterpret_cast<T *>(smem_raw);  // [field u0 u1 u2 T mu][ring slot: plane mod 5][SY][SX]
+  auto R = [&](int f, int slot, int y, int x) -> T & { return sm[((f * 5 + slot) * SY + y) * SX + x]; };
+  const int i0 = blockIdx.x * V2X, j0 = blockIdx.y * V2Y, k0 = (int)blockIdx.z * kz;
+  const int k1 = k0 + kz < g.n2 ? k0 + kz : g.n2;
   const int tid = threadIdx.y * V2X + threadIdx.x;
   const T S1 = T(suth);
-  for (int t = tid; t < 5 * PL; t += V2X * V2Y) {
-    const int z = t / PL, r = t % PL, li = r % SX, lj = r / SX;
-    const int gi = i0 - V2H + li, gj = j0 - V2H + lj, gk = k - 2 + z;
-    if (gi < -HX || gi >= g.n0 + HX || gj < -HY || gj >= g.n1 + HY) continue;
-    const int64_t m = gidx(g, gi, gj, gk);
-    T u[3], p, Tt;
-    const T rho = q.v[0][m];
-    if constexpr (sizeof(T) == 4) {
-      const float gm1 = (float)(gama - 1.0), gm1_lo = (float)((gama - 1.0) - (double)gm1);
-      float ir, p_lo;
-      prims_f32(rho, q.v[1][m], q.v[2][m], q.v[3][m], q.v[4][m], gm1, gm1_lo, ir, u, p, p_lo);
-      Tt = scaled_ratio_f32((float)gM2, p, p_lo, rho, ir);
-    } else {
-      const T ir = T(1) / rho;
+  auto stage = [&](int gk) {  // plane gk (>= -2) into ring slot (gk + 5) mod 5
+    const int slot = (gk + 5) % 5;
+    for (int t = tid; t < PL; t += V2X * V2Y) {
+      const int r = t, li = r % SX, lj = r / SX;
+      const int gi = i0 - V2H + li, gj = j0 - V2H + lj;
+      if (gi < -HX || gi >= g.n0 + HX || gj < -HY || gj >= g.n1 + HY) continue;
+      const int64_t m = gidx(g, gi, gj, gk);
+      T u[3], p, Tt;
+      const T rho = q.v[0][m];
+      if constexpr (sizeof(T) == 4) {
+        const float gm1 = (float)(gama - 1.0), gm1_lo = (float)((gama - 1.0) - (double)gm1);
+        float ir, p_lo;
+        prims_f32(rho, q.v[1][m], q.v[2][m], q.v[3][m], q.v[4][m], gm1, gm1_lo, ir, u, p, p_lo);
+        Tt = scaled_ratio_f32((float)gM2, p, p_lo, rho, ir);
+      } else {
+        const T ir = T(1) / rho;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) u[c] = q.v[1 + c][m] * ir;
-      p = (T(gama) - T(1)) * (q.v[4][m] - T(0.5) * rho * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]));
-      Tt = T(gM2) * p * ir;
+        for (int c = 0; c < 3; ++c) u[c] = q.v[1 + c][m] * ir;
+        p = (T(gama) - T(1)) * (q.v[4][m] - T(0.5) * rho * (u[0] * u[0] + u[1] * u[1] + u[2] * u[2]));
+        Tt = T(gM2) * p * ir;
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) R(c, slot, lj, li) = u[c];
+      R(3, slot, lj, li) = Tt;
+      R(4, slot, lj, li) = vexp > 0.0 ? pow_t(Tt, T(vexp)) : (S1 + T(1)) * Tt * sqrt_t(Tt) / (S1 + Tt);
     }
-#pragma unroll
-    for (int c = 0; c < 3; ++c) S(c, z, lj, li) = u[c];
-    S(3, z, lj, li) = Tt;
-    S(4, z, lj, li) = vexp > 0.0 ? pow_t(Tt, T(vexp)) : (S1 + T(1)) * Tt * sqrt_t(Tt) / (S1 + Tt);
-  }
-  __syncthreads();
-  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
-  if (i >= g.n0 || j >= g.n1) return;
-  const int li = threadIdx.x + V2H, lj = threadIdx.y + V2H;
-  const int64_t c = gidx(g, i, j, k);
-  const T id0 = T(va.inv_d0), id1 = T(va.inv_d1), id2 = T(va.inv_d2), iRe = T(1.0 / va.Re);
-  const T Dm = T(D11[j]), Sm = T(SD111[j]), mu = S(4, 2, lj, li);
-  const T c1 = T(1.0 / 12.0), c2 = T(2.0 / 3.0);
-  // central first derivative along x2 of the value at plane offset z (periodic: no closure)
-  auto dz1 = [&](auto &&F) { return id2 * (c1 * F(-2) - c2 * F(-1) + c2 * F(1) - c1 * F(2)); };
-  auto dz2 = [&](auto &&F) {
-    return id2 * id2 * (-c1 * F(-2) + T(4.0 / 3.0) * F(-1) - T(2.5) * F(0) + T(4.0 / 3.0) * F(1) - c1 * F(2));
   };
-  T gr[3][3], h[3][3][3];
+  for (int gk = k0 - 2; gk < k0 + 2; ++gk) stage(gk);
+  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+  const int li = threadIdx.x + V2H, lj = threadIdx.y + V2H;
+  for (int k = k0; k < k1; ++k) {
+    stage(k + 2);
+    __syncthreads();
+    int sl[5];
 #pragma unroll
-  for (int f = 0; f < 3; ++f) {
-    auto X = [&](int o) { return S(f, 2, lj, li + o); };
-    auto Y = [&](int o) { return S(f, 2, lj + o, li); };
-    auto Z = [&](int o) { return S(f, 2 + o, lj, li); };
-    gr[f][0] = id0 * d1c<T>(X, i, g.n0, clx);
-    const T fy = id1 * d1c<T>(Y, j, g.n1, cly);
-    gr[f][1] = Dm * fy;
-    gr[f][2] = dz1(Z);
-    h[f][0][0] = id0 * id0 * d2c<T>(X, i, g.n0, clx);
-    h[f][1][1] = Dm * Dm * (id1 * id1 * d2c<T>(Y, j, g.n1)) + Dm * Sm * fy;
-    h[f][2][2] = dz2(Z);
-    // x0 derivative of row j+o / of plane k+o, then the outer derivative
-    auto inner_xy = [&](int o) { return id0 * d1c<T>([&](int p) { return S(f, 2, lj + o, li + p); }, i, g.n0, clx); };
-    auto inner_xz = [&](int o) { return id0 * d1c<T>([&](int p) { return S(f, 2 + o, lj, li + p); }, i, g.n0, clx); };
-    auto inner_zy = [&](int o) { return dz1([&](int p) { return S(f, 2 + p, lj + o, li); }); };
-    h[f][0][1] = h[f][1][0] = Dm * (id1 * d1c<T>(inner_xy, j, g.n1, cly));
-    h[f][0][2] = h[f][2][0] = dz1(inner_xz);
-    h[f][1][2] = h[f][2][1] = Dm * (id1 * d1c<T>(inner_zy, j, g.n1, cly));
+    for (int z = 0; z < 5; ++z) sl[z] = (k + z + 3) % 5;  // slot of plane k - 2 + z
+    auto S = [&](int f, int z, int y, int x) -> T & { return R(f, sl[z], y, x); };
+    if (i < g.n0 && j < g.n1) {
+      const int64_t c = gidx(g, i, j, k);
+      const T id0 = T(va.inv_d0), id1 = T(va.inv_d1), id2 = T(va.inv_d2), iRe = T(1.0 / va.Re);
+      const T Dm = T(D11[j]), Sm = T(SD111[j]), mu = S(4, 2, lj, li);
+      const T c1 = T(1.0 / 12.0), c2 = T(2.0 / 3.0);
+      // central first derivative along x2 of the value at plane offset z (periodic: no closure)
+      auto dz1 = [&](auto &&F) { return id2 * (c1 * F(-2) - c2 * F(-1) + c2 * F(1) - c1 * F(2)); };
+      auto dz2 = [&](auto &&F) {
+        return id2 * id2 * (-c1 * F(-2) + T(4.0 / 3.0) * F(-1) - T(2.5) * F(0) + T(4.0 / 3.0) * F(1) - c1 * F(2));
+      };
+      T gr[3][3], h[3][3][3];
+#pragma unroll
+      for (int f = 0; f < 3; ++f) {
+        auto X = [&](int o) { return S(f, 2, lj, li + o); };
+        auto Y = [&](int o) { return S(f, 2, lj + o, li); };
+        auto Z = [&](int o) { return S(f, 2 + o, lj, li); };
+        gr[f][0] = id0 * d1c<T>(X, i, g.n0, clx);
+        const T fy = id1 * d1c<T>(Y, j, g.n1, cly);
+        gr[f][1] = Dm * fy;
+        gr[f][2] = dz1(Z);
+        h[f][0][0] = id0 * id0 * d2c<T>(X, i, g.n0, clx);
+        h[f][1][1] = Dm * Dm * (id1 * id1 * d2c<T>(Y, j, g.n1)) + Dm * Sm * fy;
+        h[f][2][2] = dz2(Z);
+        // x0 derivative of row j+o / of plane k+o, then the outer derivative
+        auto inner_xy = [&](int o) { return id0 * d1c<T>([&](int p) { return S(f, 2, lj + o, li + p); }, i, g.n0, clx); };
+        auto inner_xz = [&](int o) { return id0 * d1c<T>([&](int p) { return S(f, 2 + o, lj, li + p); }, i, g.n0, clx); };
+        auto inner_zy = [&](int o) { return dz1([&](int p) { return S(f, 2 + p, lj + o, li); }); };
+        h[f][0][1] = h[f][1][0] = Dm * (id1 * d1c<T>(inner_xy, j, g.n1, cly));
+        h[f][0][2] = h[f][2][0] = dz1(inner_xz);
+        h[f][1][2] = h[f][2][1] = Dm * (id1 * d1c<T>(inner_zy, j, g.n1, cly));
+      }
+      auto XT = [&](int o) { return S(3, 2, lj, li + o); };
+      auto YT = [&](int o) { return S(3, 2, lj + o, li); };
+      auto ZT = [&](int o) { return S(3, 2 + o, lj, li); };
+      auto Xmu = [&](int o) { return S(4, 2, lj, li + o); };
+      auto Ymu = [&](int o) { return S(4, 2, lj + o, li); };
+      auto Zmu = [&](int o) { return S(4, 2 + o, lj, li); };
+      const T mug[3] = {id0 * d1c<T>(Xmu, i, g.n0, clx), Dm * id1 * d1c<T>(Ymu, j, g.n1, cly), dz1(Zmu)};
+      const T Tyx = id1 * d1c<T>(YT, j, g.n1, cly);
+      const T Tg[3] = {id0 * d1c<T>(XT, i, g.n0, clx), Dm * Tyx, dz1(ZT)};
+      const T Tlap = id0 * id0 * d2c<T>(XT, i, g.n0, clx) + (Dm * Dm * (id1 * id1 * d2c<T>(YT, j, g.n1)) + Dm * Sm * Tyx) + dz2(ZT);
+      const T div = gr[0][0] + gr[1][1] + gr[2][2];
+      const T uu[3] = {S(0, 2, lj, li), S(1, 2, lj, li), S(2, 2, lj, li)};
+      T e = T(va.kappa) * (mu * Tlap + mug[0] * Tg[0] + mug[1] * Tg[1] + mug[2] * Tg[2]);
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        T v = T(0);
+#pragma unroll
+        for (int b = 0; b < 3; ++b) v += mug[b] * (gr[a][b] + gr[b][a] - (a == b ? T(2.0 / 3.0) * div : T(0))) * iRe;
+        const T lap = h[a][0][0] + h[a][1][1] + h[a][2][2];
+        const T ddiv = h[0][a][0] + h[1][a][1] + h[2][a][2];
+        v += mu * iRe * (lap + ddiv * T(1.0 / 3.0));
+        rv.v[a][c] = v;
+        e += uu[a] * v;
+#pragma unroll
+        for (int b = 0; b < 3; ++b) e += mu * iRe * (gr[a][b] + gr[b][a] - (a == b ? T(2.0 / 3.0) * div : T(0))) * gr[a][b];
+      }
+      rv.v[3][c] = e;
+    }
+    __syncthreads();  // before the next plane overwrites the slot of plane k - 2
   }
-  auto XT = [&](int o) { return S(3, 2, lj, li + o); };
-  auto YT = [&](int o) { return S(3, 2, lj + o, li); };
-  auto ZT = [&](int o) { return S(3, 2 + o, lj, li); };
-  auto Xmu = [&](int o) { return S(4, 2, lj, li + o); };
-  auto Ymu = [&](int o) { return S(4, 2, lj + o, li); };
-  auto Zmu = [&](int o) { return S(4, 2 + o, lj, li); };
-  const T mug[3] = {id0 * d1c<T>(Xmu, i, g.n0, clx), Dm * id1 * d1c<T>(Ymu, j, g.n1, cly), dz1(Zmu)};
-  const T Tyx = id1 * d1c<T>(YT, j, g.n1, cly);
-  const T Tg[3] = {id0 * d1c<T>(XT, i, g.n0, clx), Dm * Tyx, dz1(ZT)};
-  const T Tlap = id0 * id0 * d2c<T>(XT, i, g.n0, clx) + (Dm * Dm * (id1 * id1 * d2c<T>(YT, j, g.n1)) + Dm * Sm * Tyx) + dz2(ZT);
-  const T div = gr[0][0] + gr[1][1] + gr[2][2];
-  const T uu[3] = {S(0, 2, lj, li), S(1, 2, lj, li), S(2, 2, lj, li)};
-  T e = T(va.kappa) * (mu * Tlap + mug[0] * Tg[0] + mug[1] * Tg[1] + mug[2] * Tg[2]);
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    T v = T(0);
-#pragma unroll
-    for (int b = 0; b < 3; ++b) v += mug[b] * (gr[a][b] + gr[b][a] - (a == b ? T(2.0 / 3.0) * div : T(0))) * iRe;
-    const T lap = h[a][0][0] + h[a][1][1] + h[a][2][2];
-    const T ddiv = h[0][a][0] + h[1][a][1] + h[2][a][2];
-    v += mu * iRe * (lap + ddiv * T(1.0 / 3.0));
-    rv.v[a][c] = v;
-    e += uu[a] * v;
-#pragma unroll
-    for (int b = 0; b < 3; ++b) e += mu * iRe * (gr[a][b] + gr[b][a] - (a == b ? T(2.0 / 3.0) * div : T(0))) * gr[a][b];
-  }
-  rv.v[3][c] = e;
 }
 
 // R = fluxes + viscous terms at every interior point, then the LS-RK3 update of the FP64 master
@@ -1579,10 +1660,11 @@ void launch3w_rhs(const Ctx &c, int update, double A, double B, double dt, cudaS
   va.inv_d2 = 1.0 / p.delta[2];
   Q5T<T> rv{{static_cast<T *>(c.resv[0]), static_cast<T *>(c.resv[1]), static_cast<T *>(c.resv[2]),
              static_cast<T *>(c.resv[3]), nullptr}};
-  dim3 gv((c.g.n0 + V2X - 1) / V2X, (c.g.n1 + V2Y - 1) / V2Y, c.g.n2);
+  const int kz = VISC3_KZ;
+  dim3 gv((c.g.n0 + V2X - 1) / V2X, (c.g.n1 + V2Y - 1) / V2Y, (c.g.n2 + kz - 1) / kz);
   k3w_visc<T><<<gv, dim3(V2X, V2Y), visc3_smem<T>(), c.side2[1]>>>(
       c.g, q5t<const T>(c.qa), c.d11, c.sd111, rv, va, p.gama, p.gama * p.Minf * p.Minf, p.SuthT / p.RefT,
-      p.visc == OSB_VISC_POWER ? p.visc_exp : 0.0, closure_bits(p, 0), closure_bits(p, 1));
+      p.visc == OSB_VISC_POWER ? p.visc_exp : 0.0, closure_bits(p, 0), closure_bits(p, 1), kz);
   cudaEventRecord(c.ev_join2[1], c.side2[1]);
   cudaStreamWaitEvent(s, c.ev_join2[1], 0);
   Q5T<const T> rf{{r.v[0], r.v[1], r.v[2], r.v[3], r.v[4]}};
