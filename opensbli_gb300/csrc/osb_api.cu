@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "osb_common.cuh"
 #include "osb_internal.h"
@@ -50,6 +51,10 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
     snprintf(why, n, "shock_fp64 = %g: 0 (off) or a pressure ratio >= 1", p->shock_fp64);
     return OSB_EINVAL;
   }
+  if (p->ndim == 3 && (p->averaging != OSB_AVG_ROE || p->cartesian != 0)) {
+    snprintf(why, n, "3D blocks: Roe averaging, cartesian = 0");
+    return OSB_EUNSUPPORTED;
+  }
   if (!wall3(*p) && (p->forcing[0] != 0 || p->forcing[1] != 0 || p->forcing[2] != 0)) {
     snprintf(why, n, "forcing: 3D wall-bounded blocks only");
     return OSB_EUNSUPPORTED;
@@ -59,9 +64,35 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
       if (p->n[d] < 8 || p->n[d] > 16384) { snprintf(why, n, "n[%d] = %d out of range [8, 16384]", d, p->n[d]); return OSB_EINVAL; }
       if (!(p->delta[d] > 0)) { snprintf(why, n, "delta[%d] must be > 0", d); return OSB_EINVAL; }
     }
-    if (p->bc[0][0] != OSB_BC_INLET_PRESSURE_EXTRAPOLATE || p->bc[0][1] != OSB_BC_EXTRAPOLATION ||
-        p->bc[1][0] != OSB_BC_ISOTHERMAL_WALL || p->bc[1][1] != OSB_BC_DIRICHLET) {
+    if (p->averaging != OSB_AVG_ROE && p->averaging != OSB_AVG_SIMPLE) {
+      snprintf(why, n, "averaging %d: OSB_AVG_ROE or OSB_AVG_SIMPLE", p->averaging);
+      return OSB_EINVAL;
+    }
+    if (p->visc == OSB_VISC_NONE) {
+      // Euler block (inviscid_shock_reflection.py): Cartesian, Dirichlet/inlet and Dirichlet/extrapolation
+      // x0 faces, a symmetry face at x1 = 0, a Dirichlet or symmetry face at the top
+      const int *b0 = p->bc[0], *b1 = p->bc[1];
+      const bool ok = (b0[0] == OSB_BC_INLET_PRESSURE_EXTRAPOLATE || b0[0] == OSB_BC_DIRICHLET) &&
+                      (b0[1] == OSB_BC_EXTRAPOLATION || b0[1] == OSB_BC_DIRICHLET) && b1[0] == OSB_BC_SYMMETRY &&
+                      (b1[1] == OSB_BC_DIRICHLET || b1[1] == OSB_BC_SYMMETRY);
+      if (!ok) {
+        snprintf(why, n, "2D Euler blocks: inlet or Dirichlet / extrapolation or Dirichlet (x0), symmetry / Dirichlet or "
+                         "symmetry (x1)");
+        return OSB_EUNSUPPORTED;
+      }
+      if (p->cartesian != 1) { snprintf(why, n, "2D Euler blocks: Cartesian (cartesian = 1)"); return OSB_EUNSUPPORTED; }
+      for (int side = 0; side < 2; ++side)
+        for (int v = 0; v < 4; ++v)
+          if (!std::isfinite(p->dirichlet_x0[side][v])) {
+            snprintf(why, n, "dirichlet_x0 must be finite");
+            return OSB_EINVAL;
+          }
+    } else if (p->bc[0][0] != OSB_BC_INLET_PRESSURE_EXTRAPOLATE || p->bc[0][1] != OSB_BC_EXTRAPOLATION ||
+               p->bc[1][0] != OSB_BC_ISOTHERMAL_WALL || p->bc[1][1] != OSB_BC_DIRICHLET) {
       snprintf(why, n, "2D blocks: boundary conditions must be inlet/extrapolation (x0) and isothermal wall/Dirichlet (x1)");
+      return OSB_EUNSUPPORTED;
+    } else if (p->cartesian != 0) {
+      snprintf(why, n, "2D viscous blocks: metrics stretched in x1 (cartesian = 0)");
       return OSB_EUNSUPPORTED;
     }
     if (p->conv != OSB_CONV_TENO5 && p->conv != OSB_CONV_WENO5JS && p->conv != OSB_CONV_WENO5Z &&
@@ -83,7 +114,10 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
                    p->closure[d][side]);
           return OSB_EINVAL;
         }
-    if (p->visc != OSB_VISC_SUTHERLAND) { snprintf(why, n, "2D blocks: Sutherland viscosity"); return OSB_EUNSUPPORTED; }
+    if (p->visc != OSB_VISC_SUTHERLAND && p->visc != OSB_VISC_NONE) {
+      snprintf(why, n, "2D blocks: Sutherland viscosity or none");
+      return OSB_EUNSUPPORTED;
+    }
     if (p->rk != OSB_RK3_LS) { snprintf(why, n, "2D blocks: low-storage RK3"); return OSB_EUNSUPPORTED; }
     if (p->precision != OSB_PREC_FP64 && p->precision != OSB_PREC_MIXED) { snprintf(why, n, "precision %d", p->precision); return OSB_EINVAL; }
     if (!(p->gama > 1.0) || !(p->Minf > 0) || !(p->Re > 0) || !(p->Pr > 0) || !(p->Twall > 0) || !(p->RefT > 0)) {
@@ -790,6 +824,7 @@ int osb_set_coordinate(osb_ctx *c, int axis, const double *src, int h) {
     return cuda_err(c, cudaGetLastError(), "osb_set_coordinate");
   }
   if (c->plan.ndim != 2 || axis != 1) return set_err(c, OSB_EUNSUPPORTED, "coordinates: 2D blocks stretched in x1 only");
+  if (c->plan.cartesian) return set_err(c, OSB_EINVAL, "Cartesian 2D block: no coordinate to set");
   if (!src || h < 4 || h > 4) return set_err(c, OSB_EINVAL, "coordinate array needs a 4-point halo");
   const int nb = blocks_for((int64_t)(c->g.n0 + 2 * h) * (c->g.n1 + 2 * h));
   k_copy_padded<<<nb, 256, 0, c->stream>>>(c->g, src, h, c->x1);
@@ -874,6 +909,11 @@ int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
     if (e == cudaSuccess) e = cudaMalloc(&c->sd111, b64);
     if (e == cudaSuccess) e = cudaMemset(c->d11, 0, b64);
     if (e == cudaSuccess) e = cudaMemset(c->sd111, 0, b64);
+    if (e == cudaSuccess && plan->cartesian) {  // no metric terms: D11 = 1, SD111 = 0
+      std::vector<double> ones((size_t)c->g.numel, 1.0);
+      e = cudaMemcpy(c->d11, ones.data(), b64, cudaMemcpyHostToDevice);
+      c->metrics_valid = 1;
+    }
     c->red_blocks = 152 * 8;
     if (e == cudaSuccess) e = cudaMalloc(&c->red, (c->red_blocks + 1) * sizeof(double));
     if (e == cudaSuccess) e = upload2_closure_weights();

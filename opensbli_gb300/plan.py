@@ -72,7 +72,12 @@ class Plan:
     visc_exp: float = 0.7
     forcing: Optional[Tuple[float, ...]] = None
     x1_grid: str = "sinh"           # sinh: Lx1 sinh(by eta)/sinh(by) | tanh: -tanh(stretch (1-2eta))/tanh(stretch)
-    stretch: float = 1.7
+    stretch: float = 1.7            # | uniform: a Cartesian 2D block (no metric terms)
+    # 2D Euler blocks (apps/inviscid_shock_reflection/inviscid_shock.py): the average the characteristic
+    # system is built from ("roe" | "simple", averaging.py) and the constant states of Dirichlet x0
+    # faces (side 0, side 1; rho, rhou0, rhou1, rhoE)
+    averaging: str = "roe"
+    dirichlet_x0: Optional[Tuple[Tuple[float, ...], ...]] = None
     rk_a: Tuple[float, float, float] = RK3_RKOLD
     rk_b: Tuple[float, float, float] = RK3_RKNEW
     use_graphs: bool = True
@@ -117,6 +122,8 @@ class Plan:
             if d.get(k) is not None:
                 d[k] = tuple(d[k])
         d["bc"] = tuple(tuple(x) for x in d["bc"])
+        if d.get("dirichlet_x0") is not None:
+            d["dirichlet_x0"] = tuple(tuple(x) for x in d["dirichlet_x0"])
         if "closure" in d:
             d["closure"] = tuple(tuple(x) for x in d["closure"])
         return cls(**d)
@@ -239,6 +246,30 @@ def channel_initial_state(plan, halo=3):
     p = 1.0 / (plan.gama * plan.Minf ** 2)
     q = np.stack([np.ones(shape), u, v, w, p / (plan.gama - 1.0) + 0.5 * (u * u + v * v + w * w)])
     return np.ascontiguousarray(q), y1
+
+
+def shock_reflection_plan(n0=457, n1=255, precision="fp64", dt=0.1, use_graphs=True, conv="weno5z",
+                          averaging="simple"):
+    """The 2D inviscid shock reflection of apps/inviscid_shock_reflection/inviscid_shock.py: Euler
+    equations at Mach 2 (gama = 1.4) on 350 x 115 with a uniform grid, LLFWeno(5, 'Z') with
+    SimpleAverage, RungeKuttaLS(3); a Dirichlet inlet (the free stream) at x0 = 0, extrapolation at the
+    outlet, a symmetry face at x1 = 0 and the shock generator's Dirichlet face at x1 = 115 (post-shock
+    state where x0 >= 40; pressures as the script formats them, "%f").  457 x 255 and dt = 0.1 as the
+    script sets them."""
+    g, M = 1.4, 2.0
+
+    def state(d, u0, u1, p):  # the generated code's rhoE = p/(gama-1) + d |u|^2 / 2
+        return (d, d * u0, d * u1, (1.0 / (g - 1.0)) * p + 0.5 * d * (u0 ** 2 + u1 ** 2))
+    free = state(1.0, 1.0, 0.0, 1.0 * (1.0 / g) * (1.0 / M ** 2))
+    pre = state(1.0, 1.0, 0.0, float("%f" % (1.0 / (1.4 * 4.0))))
+    post = state(1.129734572, 0.9667023804242755, -0.052106102140246795, float("%f" % (1.0 / (1.4 * 4.0) * 1.18646663)))
+    return Plan(ndim=2, n=(n0, n1, 1), delta=(350.0 / (n0 - 1), 115.0 / (n1 - 1), 1.0), conv=conv, visc="none",
+                rk="ls_rk3", precision=precision, averaging=averaging,
+                bc=(("dirichlet", "extrapolation"), ("symmetry", "dirichlet"), ("periodic", "periodic")),
+                gama=g, Minf=M, weno_eps=1e-14 if conv == "weno5z" else 1e-6, rk_a=(0.0, -5.0 / 9.0, -153.0 / 128.0),
+                rk_b=(1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0), dt=dt, use_graphs=use_graphs, ic="host",
+                x1_grid="uniform", dirichlet_x0=(free, free), dirichlet_lo=pre, dirichlet_hi=post,
+                dirichlet_x_switch=math.nextafter(40.0, 0.0), name="shock_reflection_%s_%dx%d" % (conv, n0, n1))
 
 
 def katzer_plan(n0=512, n1=256, precision="fp64", conv="teno5", dt=0.04, use_graphs=True, adaptive=False,

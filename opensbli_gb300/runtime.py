@@ -12,7 +12,7 @@ import torch
 
 from . import build as _build
 
-OSB_ABI_VERSION = 7
+OSB_ABI_VERSION = 8
 ERRORS = {
     -1: "invalid plan or argument",
     -2: "unsupported kernel pattern",
@@ -25,6 +25,7 @@ ERRORS = {
 
 CONV = {"central_skew": 0, "weno5js": 1, "teno5": 2, "weno5z": 3, "teno6": 4}
 VISC = {"none": 0, "const": 1, "sutherland": 2, "power": 3}
+AVG = {"roe": 0, "simple": 1}
 RK = {"rk3": 0, "ls_rk3": 1}
 BC = {"periodic": 0, "symmetry": 1, "inlet_pressure_extrapolate": 2, "extrapolation": 3, "isothermal_wall": 4,
       "dirichlet": 5}
@@ -72,6 +73,9 @@ class PlanDesc(ctypes.Structure):
         ("filter_control", ctypes.c_double),
         ("visc_exp", ctypes.c_double),
         ("forcing", ctypes.c_double * 3),
+        ("averaging", ctypes.c_int),
+        ("cartesian", ctypes.c_int),
+        ("dirichlet_x0", (ctypes.c_double * 5) * 2),
     ]
 
 
@@ -216,6 +220,11 @@ def make_plan_desc(plan):
     d.visc_exp = plan.visc_exp
     for k, v in enumerate(plan.forcing or (0.0,) * 3):
         d.forcing[k] = v
+    d.averaging = AVG[plan.averaging]
+    d.cartesian = 1 if plan.x1_grid == "uniform" else 0
+    for side, st in enumerate(plan.dirichlet_x0 or ()):
+        for v, x in enumerate(st):
+            d.dirichlet_x0[side][v] = x
     return d
 
 

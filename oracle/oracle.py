@@ -157,6 +157,12 @@ class Cfg2D(ctypes.Structure):
         ("sensor_eps", ctypes.c_double),
         ("closure", (ctypes.c_int * 2) * 2),
         ("conv", ctypes.c_int),
+        ("euler", ctypes.c_int),
+        ("simple_avg", ctypes.c_int),
+        ("bc", (ctypes.c_int * 2) * 2),
+        ("face0", (ctypes.c_double * 4) * 2),
+        ("top", (ctypes.c_double * 4) * 2),
+        ("x_switch", ctypes.c_double),
     ]
 
 
@@ -185,7 +191,32 @@ def make_cfg2d(plan):
         for side in range(2):
             c.closure[d][side] = CLOSURES[plan.closure[d][side]]
     c.conv = CONV[plan.conv]
+    # Euler blocks: Cartesian x1, no viscous terms, the faces and states of the plan
+    c.euler = 1 if plan.visc == "none" else 0
+    c.simple_avg = 1 if plan.averaging == "simple" else 0
+    kinds = {"dirichlet": 1, "symmetry": 2}
+    for d in range(2):
+        for side in range(2):
+            c.bc[d][side] = kinds.get(plan.bc[d][side], 0) if c.euler else 0
+    for side, st in enumerate(plan.dirichlet_x0 or ()):
+        for v in range(4):
+            c.face0[side][v] = st[v]
+    if c.euler and plan.bc[1][1] == "dirichlet":
+        for v in range(4):
+            c.top[0][v] = plan.dirichlet_lo[v]
+            c.top[1][v] = plan.dirichlet_hi[v]
+        c.x_switch = plan.dirichlet_x_switch
     return c
+
+
+def residual2d(plan, q0_padded):
+    """Right-hand side [4][n1][n0] of a padded FP64 state (boundary conditions applied first)."""
+    c = make_cfg2d(plan)
+    q = np.ascontiguousarray(q0_padded, dtype=np.float64)
+    assert q.shape == (4, plan.n[1] + 8, plan.n[0] + 8)
+    r = np.zeros((4, plan.n[1], plan.n[0]))
+    assert lib().osbo2d_residual(ctypes.byref(c), _ptr(q), _ptr(r)) == 0
+    return r
 
 
 def carpenter_d1():

@@ -72,12 +72,27 @@ typedef struct {
   /* characteristic scheme: OSBO_CONV_TENO5 (default 0 is read as TENO5), OSBO_CONV_WENO5JS,
    * OSBO_CONV_WENO5Z or OSBO_CONV_TENO6 */
   int conv;
+  /* 2D Euler blocks (apps/inviscid_shock_reflection/inviscid_shock.py): euler = 1 drops the viscous
+   * terms and the metric (x1 uniform, D11 = 1).  bc[axis][side]: OSBO_BC2_DEFAULT (the shock/boundary-
+   * layer face of that side: inlet, extrapolation, isothermal wall, the script's Dirichlet top),
+   * OSBO_BC2_DIRICHLET or OSBO_BC2_SYMMETRY; face0[side] is the constant state of a Dirichlet x0
+   * face, top[0] / top[1] the states of a Dirichlet x1 side-1 face where x0 <= x_switch / x0 >
+   * x_switch (rho, rhou0, rhou1, rhoE).  simple_avg = 1: the characteristic system at an interface
+   * from the arithmetic means of rho, u and a (SimpleAverage, averaging.py:31-59). */
+  int euler, simple_avg;
+  int bc[2][2];
+  double face0[2][4], top[2][4], x_switch;
 } osbo2d_cfg;
+#define OSBO_BC2_DEFAULT 0
+#define OSBO_BC2_DIRICHLET 1
+#define OSBO_BC2_SYMMETRY 2
 
 /* Advance q by nsteps LS-RK3 steps.  q holds [4][n1+8][n0+8]: rho, rhou0, rhou1, rhoE with a
  * 4-point halo on every side (the initial state must fill the halos as the script's
  * initialisation kernel does); it is overwritten with the final state, halos included. */
 int osbo2d_run(const osbo2d_cfg *cfg, double *q, int nsteps);
+/* The right-hand side of q (boundary conditions applied first) on the interior, [4][n1][n0]. */
+int osbo2d_residual(const osbo2d_cfg *cfg, const double *q, double *r);
 /* ---- 3D span-periodic wall-bounded path: the 2D configuration above with a periodic x2 axis ---- */
 typedef struct {
   int n[3];          /* interior points in x0, x1, x2 */

@@ -185,6 +185,13 @@ static double d2c(const s2_t *s, const double *f, int i, int j, int dir) {
  *   detJ = dx1/dxi1, D11 = 1/detJ, halos mirrored about the boundary points, SD111 = dD11/dxi1.
  * ------------------------------------------------------------------------------------------- */
 static void metrics(s2_t *s) {
+  if (s->c.euler) { /* no metric kernels in a Cartesian block: d/dx1 = d/dxi1 */
+    FOR2(-H, N0 + H, -H, N1 + H) {
+      s->D11[I2(s, i, j)] = 1.0;
+      s->SD111[I2(s, i, j)] = 0.0;
+    }
+    return;
+  }
   const double Lx1 = s->c.Lx1, by = s->c.by, d1 = s->c.delta[1];
   FOR2(-3, N0 + 4, -3, N1 + 4) s->x1[I2(s, i, j)] = sinh(d1 * by * (1.0 / Lx1) * j) / ((1.0 / Lx1) * sinh(by));
   double *wk = alloc2(s);
@@ -275,11 +282,47 @@ static void bc_top(s2_t *s) {
     }
 }
 
+/* DirichletBC on an x0 face (dirichlet.py:6-41): the boundary point and the halo take the constant
+ * state of the face (side 0: i = -3..0; side 1: i = n0-1..n0+3). */
+static void bc_dirichlet_x0(s2_t *s, int side) {
+  const double *st = s->c.face0[side];
+  const int i0 = side == 0 ? -3 : N0 - 1, i1 = side == 0 ? 1 : N0 + 4;
+  for (int j = -3; j < N1 + 4; ++j)
+    for (int i = i0; i < i1; ++i)
+      for (int v = 0; v < 4; ++v) s->q[v][I2(s, i, j)] = st[v];
+}
+
+/* SymmetryBC on an x1 face (symmetry.py): halo point t mirrors the interior point t away from the
+ * boundary point, the normal momentum reversed; the boundary point keeps its values. */
+static void bc_symmetry_x1(s2_t *s, int side) {
+  const int jb = side == 0 ? 0 : N1 - 1, sg = side == 0 ? 1 : -1, nt = side == 0 ? 3 : 4;
+  for (int i = -3; i < N0 + 4; ++i)
+    for (int t = 1; t <= nt; ++t) {
+      const size_t h = I2(s, i, jb - sg * t), m = I2(s, i, jb + sg * t);
+      for (int v = 0; v < 4; ++v) s->q[v][h] = v == 2 ? -s->q[v][m] : s->q[v][m];
+    }
+}
+
+/* DirichletBC on x1 side 1 with a state switched at x0 (the shock generator of an Euler block) */
+static void bc_top_states(s2_t *s) {
+  for (int j = N1 - 1; j < N1 + 4; ++j)
+    for (int i = -3; i < N0 + 4; ++i) {
+      const double x0 = s->c.delta[0] * i;
+      for (int v = 0; v < 4; ++v) s->q[v][I2(s, i, j)] = s->c.top[x0 > s->c.x_switch ? 1 : 0][v];
+    }
+}
+
 static void apply_bcs(s2_t *s) {
-  bc_inlet(s);
-  bc_outlet(s);
-  bc_wall(s);
-  bc_top(s);
+  const int(*b)[2] = s->c.bc;
+  if (b[0][0] == OSBO_BC2_DIRICHLET) bc_dirichlet_x0(s, 0);
+  else bc_inlet(s);
+  if (b[0][1] == OSBO_BC2_DIRICHLET) bc_dirichlet_x0(s, 1);
+  else bc_outlet(s);
+  if (b[1][0] == OSBO_BC2_SYMMETRY) bc_symmetry_x1(s, 0);
+  else bc_wall(s);
+  if (b[1][1] == OSBO_BC2_SYMMETRY) bc_symmetry_x1(s, 1);
+  else if (b[1][1] == OSBO_BC2_DIRICHLET) bc_top_states(s);
+  else bc_top(s);
 }
 
 /* ---------------------------------------------------------------------------------------------
@@ -361,13 +404,19 @@ static void teno_fluxes(s2_t *s, int dir) {
   FOR2(lo0, N0, lo1, N1) {
     const size_t c = I2(s, i, j);
     const double rl = s->q[0][c], rr = s->q[0][c + o];
-    const double sl = sqrt(rl), sr = sqrt(rr);
-    const double rho = sqrt(rl * rr), inv = 1.0 / (sl + sr);
     const double uL[2] = {s->u0[c], s->u1[c]}, uR[2] = {s->u0[c + o], s->u1[c + o]};
-    double u[2];
-    for (int k = 0; k < 2; ++k) u[k] = inv * (sl * uL[k] + sr * uR[k]);
-    const double Hh = inv * ((s->p[c] + s->q[3][c]) / sl + (s->p[c + o] + s->q[3][c + o]) / sr);
-    const double a = sqrt((g - 1) * (Hh - 0.5 * (u[0] * u[0] + u[1] * u[1])));
+    double u[2], rho, a;
+    if (s->c.simple_avg) { /* SimpleAverage (averaging.py:31-59) */
+      rho = 0.5 * (rl + rr);
+      for (int k = 0; k < 2; ++k) u[k] = 0.5 * (uL[k] + uR[k]);
+      a = 0.5 * (s->a[c] + s->a[c + o]);
+    } else { /* RoeAverage (averaging.py:62-114) */
+      const double sl = sqrt(rl), sr = sqrt(rr), inv = 1.0 / (sl + sr);
+      rho = sqrt(rl * rr);
+      for (int k = 0; k < 2; ++k) u[k] = inv * (sl * uL[k] + sr * uR[k]);
+      const double Hh = inv * ((s->p[c] + s->q[3][c]) / sl + (s->p[c + o] + s->q[3][c + o]) / sr);
+      a = sqrt((g - 1) * (Hh - 0.5 * (u[0] * u[0] + u[1] * u[1])));
+    }
     const double phi = (g - 1) * 0.5 * (u[0] * u[0] + u[1] * u[1]);
     const double bt = 1.0 / (rho * a * sqrt(2.0)), al = rho / (a * sqrt(2.0));
     double L[4][4];
@@ -534,7 +583,7 @@ int osbo2d_run(const osbo2d_cfg *cfg, double *q, int nsteps) {
       constituent(&s);
       if (cfg->teno_adaptive) sensor(&s);
       residual_teno(&s);
-      residual_viscous(&s);
+      if (!cfg->euler) residual_viscous(&s);
       /* RungeKuttaLS (rk_LS.py:155-166): du = A du + dt R; q = q + B du */
       for (int v = 0; v < 4; ++v)
         for (int j = 0; j < cfg->n[1]; ++j)
@@ -550,6 +599,30 @@ int osbo2d_run(const osbo2d_cfg *cfg, double *q, int nsteps) {
     for (int j = -hp; j < cfg->n[1] + hp; ++j)
       for (int i = -hp; i < cfg->n[0] + hp; ++i)
         q[((size_t)v * pyo + (size_t)(j + hp)) * pxo + (size_t)(i + hp)] = s.q[v][I2(&s, i, j)];
+  s2_free(&s);
+  return 0;
+}
+
+/* The right-hand side of a padded state (boundary conditions applied first) on the interior,
+ * [4][n1][n0]. */
+int osbo2d_residual(const osbo2d_cfg *cfg, const double *q, double *r) {
+  s2_t s;
+  s2_init(&s, cfg);
+  const int hp = 4, pxo = cfg->n[0] + 2 * hp, pyo = cfg->n[1] + 2 * hp;
+  for (int v = 0; v < 4; ++v)
+    for (int j = -hp; j < cfg->n[1] + hp; ++j)
+      for (int i = -hp; i < cfg->n[0] + hp; ++i)
+        s.q[v][I2(&s, i, j)] = q[((size_t)v * pyo + (size_t)(j + hp)) * pxo + (size_t)(i + hp)];
+  metrics(&s);
+  apply_bcs(&s);
+  constituent(&s);
+  if (cfg->teno_adaptive) sensor(&s);
+  residual_teno(&s);
+  if (!cfg->euler) residual_viscous(&s);
+  size_t m = 0;
+  for (int v = 0; v < 4; ++v)
+    for (int j = 0; j < cfg->n[1]; ++j)
+      for (int i = 0; i < cfg->n[0]; ++i) r[m++] = s.res[v][I2(&s, i, j)];
   s2_free(&s);
   return 0;
 }

@@ -58,6 +58,9 @@ CASES_2D = {
     "katzer_weno": ((64, 32), 20, {"dt": 0.01}),
     "katzer_wenoz": ((64, 32), 20, {"dt": 0.01}),
     "katzer_teno6": ((64, 32), 20, {"dt": 0.01}),
+    # the inviscid shock reflection (Euler, WENO5-Z with SimpleAverage, Dirichlet inlet, symmetry
+    # face, the shock generator's Dirichlet top), dt at CFL ~0.4 so that the shock moves
+    "shock_reflection": ((64, 32), 30, {"dt": 1.0}),
 }
 VARS_2D = ["rho", "rhou0", "rhou1", "rhoE"]
 
