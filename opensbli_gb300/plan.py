@@ -268,7 +268,7 @@ def shock_reflection_plan(n0=457, n1=255, precision="fp64", dt=0.1, use_graphs=T
                 bc=(("dirichlet", "extrapolation"), ("symmetry", "dirichlet"), ("periodic", "periodic")),
                 gama=g, Minf=M, weno_eps=1e-14 if conv == "weno5z" else 1e-6, rk_a=(0.0, -5.0 / 9.0, -153.0 / 128.0),
                 rk_b=(1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0), dt=dt, use_graphs=use_graphs, ic="host",
-                x1_grid="uniform", dirichlet_x0=(free, free), dirichlet_lo=pre, dirichlet_hi=post,
+                x1_grid="uniform", dirichlet_x0=(free, (0.0, 0.0, 0.0, 0.0)), dirichlet_lo=pre, dirichlet_hi=post,
                 dirichlet_x_switch=math.nextafter(40.0, 0.0), name="shock_reflection_%s_%dx%d" % (conv, n0, n1))
 
 

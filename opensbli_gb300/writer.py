@@ -62,9 +62,9 @@ class GB300Writer:
         self.components = _walk(algorithm.prg, [])
         self.kernel_names = [getattr(c, "computation_name", None) for c in self.components
                              if type(c).__name__ == "Kernel"]
+        self.values = {}
         self.plan = self._lower(precision, use_graphs)
         self.ic_kernel = self._find_kernel("Grid_based_initialisation")
-        self.values = {}
 
     # ------------------------------------------------------------------ recognition
     def _find_kernel(self, prefix):
@@ -311,6 +311,13 @@ class GB300Writer:
             raise NotImplementedError("the adaptive cut-off is lowered for TENO5 (2D) and TENO5/TENO6 (3D) blocks")
         if self._max_offset(teno or weno) != 3:
             raise NotImplementedError("5th-order reconstruction stencil expected")
+        averaging = self._averaging(teno or weno)
+        # a 2D Euler block (apps/inviscid_shock_reflection/inviscid_shock.py): no viscous kernels, no metric
+        euler = nd == 2 and not any(n.startswith(("CRmu", "CRT", "Viscous")) for n in names)
+        if euler:
+            if self._kernels("MetricsEquation") or self._kernels("Metric boundary"):
+                raise NotImplementedError("2D Euler blocks: Cartesian grids only")
+            return self._lower_euler2d(precision, use_graphs, conv, averaging, names)
         if not self._kernels("MetricsEquation") or not self._kernels("Metric boundary"):
             raise NotImplementedError("2D blocks: metric terms expected")
         if not any(n.startswith("CRmu") for n in names):
@@ -318,6 +325,8 @@ class GB300Writer:
         visc_exp = self._power_law_viscosity()
         if visc_exp is not None and nd != 3:
             raise NotImplementedError("2D blocks: Sutherland viscosity")
+        if averaging != "roe":
+            raise NotImplementedError("wall-bounded blocks: the Roe average expected")
         coeff = self._rk_coefficients(["Temporal solution advancement"])
         if set(coeff) != {"rkA", "rkB"}:
             raise NotImplementedError("RungeKuttaLS(3) coefficients rkA/rkB expected")
@@ -416,6 +425,146 @@ class GB300Writer:
                     sensor_eps=adaptive if adaptive is not None else Plan.sensor_eps, closure=closure)
 
     _BF_CONSTS = ("A", "xF", "yF", "bta", "omega")
+
+    def _averaging(self, reconstruction):
+        """The average the characteristic system is built from, read from the reconstruction kernels'
+        AVG_*_rho equations: "roe" (sqrt(rho_l rho_r), averaging.py:62-114) or "simple" ((rho_l +
+        rho_r)/2, averaging.py:31-59); both checked numerically."""
+        import sympy
+        kinds = set()
+        for k in reconstruction:
+            avg = [e for e in k.equations if re.match(r"AVG_\d+_rho$", str(e.lhs))]
+            if len(avg) != 1:
+                raise NotImplementedError("averaged density expected in %s" % k.computation_name)
+            ds = [a for a in sympy.preorder_traversal(avg[0].rhs) if type(a).__name__ == "DataSet"]
+            if len(ds) != 2 or {str(a.base) for a in ds} != {"rho_B0"}:
+                raise NotImplementedError("averaged density of %s reads %s" % (k.computation_name, ds))
+            val = float(avg[0].rhs.xreplace({ds[0]: sympy.Float(1.3), ds[1]: sympy.Float(0.7)}))
+            if abs(val - 1.0) < 1e-14:
+                kinds.add("simple")
+            elif abs(val - (1.3 * 0.7) ** 0.5) < 1e-14:
+                kinds.add("roe")
+            else:
+                raise NotImplementedError("average of %s not recognised" % k.computation_name)
+        if len(kinds) != 1:
+            raise NotImplementedError("one average for every direction expected")
+        return kinds.pop()
+
+    def _face_states(self, kname, consts):
+        """Evaluate a Dirichlet face kernel (dirichlet.py:6-41) as the generated code does, in equation
+        order with its locals, the constants in `consts`, and x0 a free variable.  Returns (lo, hi, xs):
+        the states (rho, rhou0, rhou1, rhoE) where x0 <= xs and where x0 > xs (xs = 1e300: one state)."""
+        import math
+        import sympy
+        ks = self._kernels(kname)  # the face is applied before the loop and after every stage
+        if not ks or any(k.equations != ks[0].equations for k in ks):
+            raise NotImplementedError("one %s kernel expected" % kname)
+        x = sympy.Symbol("_osb_x0")
+        env, out, thresholds = {}, {}, set()
+        for e in ks[0].equations:
+            reps = {}
+            it = sympy.preorder_traversal(e.rhs)
+            for a in it:
+                t = type(a).__name__
+                if t == "DataSet":
+                    it.skip()  # not its shape constants
+                    if str(a.base) != "x0_B0" or any(int(i) != 0 for i in a.indices):
+                        raise NotImplementedError("Dirichlet face reads %s" % a)
+                    reps[a] = x
+                elif t == "ConstantObject":
+                    if str(a) not in consts:
+                        raise NotImplementedError("Dirichlet face constant %s" % a)
+                    reps[a] = sympy.Float(consts[str(a)], 30)
+                elif isinstance(a, sympy.Symbol):  # the kernel's locals (GridVariables)
+                    if str(a) not in env:
+                        raise NotImplementedError("Dirichlet face: %s used before it is set" % a)
+                    reps[a] = env[str(a)]
+            v = e.rhs.xreplace(reps)
+            for r in sympy.preorder_traversal(v):
+                if isinstance(r, sympy.core.relational.Relational) and r.free_symbols == {x}:
+                    sol = sympy.solve(sympy.Eq(r.lhs, r.rhs), x)
+                    thresholds.update(float(t) for t in sol)
+            if type(e.lhs).__name__ == "GridVariable":
+                env[str(e.lhs)] = v
+            else:
+                out[re.sub(r"_B0$", "", str(getattr(e.lhs, "base", e.lhs)))] = v
+        order = ["rho", "rhou0", "rhou1", "rhoE"]
+        if set(out) != set(order):
+            raise NotImplementedError("%s sets %s" % (kname, sorted(out)))
+
+        def at(xv):
+            return tuple(float(out[n].subs(x, xv)) for n in order)
+        if not thresholds:
+            st = at(0.0)
+            return st, st, 1e300
+        if len(thresholds) != 1:
+            raise NotImplementedError("%s: one switch location expected" % kname)
+        c = thresholds.pop()
+        lo, hi, mid = at(c - 1.0), at(c + 1.0), at(c)
+        if mid not in (lo, hi) or any(at(xv) != lo for xv in (c - 5.0, c - 100.0)) or \
+                any(at(xv) != hi for xv in (c + 5.0, c + 100.0)):
+            raise NotImplementedError("%s: a state switched at one x0 location expected" % kname)
+        # the kernels compare x0 > xs: a switch that includes c itself moves xs just below it
+        return lo, hi, (c if mid == lo else math.nextafter(c, -math.inf))
+
+    def _lower_euler2d(self, precision, use_graphs, conv, averaging, names):
+        """A 2D Euler block (apps/inviscid_shock_reflection/inviscid_shock.py): Cartesian, no viscous terms,
+        LLFWeno/LLFTeno with the Roe or the simple average, RungeKuttaLS(3); a Dirichlet or inlet face at
+        x0 = 0, a Dirichlet or extrapolation face at the outlet, a symmetry face at x1 = 0 and a Dirichlet
+        (possibly switched at one x0) or symmetry face at the top.  The faces' states depend on the
+        simulation's constants; they are evaluated again by substitute_simulation_parameters."""
+        coeff = self._rk_coefficients(["Temporal solution advancement"])
+        if set(coeff) != {"rkA", "rkB"}:
+            raise NotImplementedError("RungeKuttaLS(3) coefficients rkA/rkB expected")
+        faces = {
+            "InletPressureExtrapolate boundary dir0 side0": ("inlet_pressure_extrapolate", 0, 0),
+            "Dirichlet boundary dir0 side0": ("dirichlet", 0, 0),
+            "Extrapolation boundary dir0 side1": ("extrapolation", 0, 1),
+            "Dirichlet boundary dir0 side1": ("dirichlet", 0, 1),
+            "Symmetry boundary dir1 side0": ("symmetry", 1, 0),
+            "Dirichlet boundary dir1 side1": ("dirichlet", 1, 1),
+            "Symmetry boundary dir1 side1": ("symmetry", 1, 1),
+        }
+        bcs = [[None, None], [None, None]]
+        for kname, (kind, d, side) in faces.items():
+            if self._kernels(kname):
+                if bcs[d][side] is not None:
+                    raise NotImplementedError("two boundary conditions on face dir%d side%d" % (d, side))
+                bcs[d][side] = kind
+        other = sorted(n for n in names if "boundary dir" in n and n not in faces)
+        if other or bcs[1][0] != "symmetry" or None in bcs[0] or bcs[1][1] is None:
+            raise NotImplementedError("2D Euler block boundary conditions: %s" %
+                                      (other or sorted(n for n in names if "boundary dir" in n)))
+        physics_check.check_algorithm(self.components, 2, viscous=False, metric=False)
+        self._euler_faces = bcs
+        plan = Plan(ndim=2, n=(64, 32, 1), delta=(1.0, 1.0, 1.0), conv=conv,
+                    weno_eps=1e-14 if conv == "weno5z" else 1e-6,  # WenoZ.eps / WenoJS.eps (weno.py)
+                    visc="none", rk="ls_rk3", precision=precision, averaging=averaging, x1_grid="uniform",
+                    bc=(tuple(bcs[0]), tuple(bcs[1]), ("periodic", "periodic")),
+                    rk_a=coeff["rkA"], rk_b=coeff["rkB"], use_graphs=use_graphs, ic="host", name="euler2d",
+                    kernels=[n for n in names if n])
+        return self._euler_states(plan)
+
+    def _euler_states(self, plan):
+        """The Dirichlet states of a 2D Euler block's faces with the plan's constants."""
+        consts = {"gama": plan.gama, "Minf": plan.Minf}
+        consts.update({k: v for k, v in self.values.items() if isinstance(v, (int, float))})
+        b = self._euler_faces
+        kw = {}
+        x0 = []
+        for side in range(2):
+            if b[0][side] == "dirichlet":
+                lo, hi, xs = self._face_states("Dirichlet boundary dir0 side%d" % side, consts)
+                if xs != 1e300:
+                    raise NotImplementedError("Dirichlet x0 face: a constant state expected")
+                x0.append(lo)
+            else:
+                x0.append((0.0, 0.0, 0.0, 0.0))
+        kw["dirichlet_x0"] = tuple(x0)
+        if b[1][1] == "dirichlet":
+            lo, hi, xs = self._face_states("Dirichlet boundary dir1 side1", consts)
+            kw.update(dirichlet_lo=lo, dirichlet_hi=hi, dirichlet_x_switch=xs)
+        return plan.replace(**kw)
 
     def _power_law_viscosity(self):
         """The viscosity relation of the CRmu kernel: None for Sutherland's law (katzer_SBLI.py:25,
@@ -719,6 +868,8 @@ class GB300Writer:
                       by=float(env.get("by", p.by)), teno_a1=float(env.get("teno_a1", p.teno_a1)),
                       teno_a2=float(env.get("teno_a2", p.teno_a2)))
         self.plan = p.replace(**kw)
+        if p.visc == "none" and p.ndim == 2:  # the Dirichlet states of a 2D Euler block use gama and Minf
+            self.plan = self._euler_states(self.plan)
         return self.plan
 
     # ------------------------------------------------------------------ initial condition
@@ -849,7 +1000,8 @@ class GB300Writer:
         coords = {}
         if self.plan.ndim == 2:
             f = self.initial_fields(halo=4)
-            s.set_coordinate(f["x1"], 4)
+            if self.plan.x1_grid != "uniform":
+                s.set_coordinate(f["x1"], 4)
             s.set_state64_padded(np.stack([f[v] for v in self.state_names()]), 4)
             coords = {k: f[k][4:-4, 4:-4] for k in ("x0", "x1") if k in f}
         elif self.plan.rk == "ls_rk3":  # 3D wall-bounded: x1 is a function of j alone

@@ -102,6 +102,26 @@ def test_transitional_script_lowers_to_its_plan():
     assert g.teno_adaptive and g.conv == "teno6" and g.dirichlet_ke and g.body_force == (2.5e-3, 20.0, 4.0, 0.23, 0.1011)
 
 
+def test_shock_reflection_script_lowers_to_its_plan():
+    """The inviscid shock reflection lowers to a Cartesian 2D Euler block with WENO5-Z, the simple
+    average, a Dirichlet inlet, a symmetry face and the shock generator's Dirichlet face switched at
+    x0 >= 40; the face states evaluated from the script's kernels equal shock_reflection_plan's to the
+    last bit or two (high-precision evaluation against the generated code's double arithmetic)."""
+    import math
+    from opensbli_gb300.plan import shock_reflection_plan
+    g = golden_plan("shock_reflection")
+    p = shock_reflection_plan(*g.n[:2])
+    states = ("dirichlet_x0", "dirichlet_lo", "dirichlet_hi")
+    assert g.replace(kernels=[], name="", niter=None, **{k: None for k in states}) == \
+        p.replace(kernels=[], name="", **{k: None for k in states})
+    flat = lambda v: [x for t in v for x in (t if isinstance(t, tuple) else (t,))]
+    for k in states:
+        a, b = flat(getattr(g, k)), flat(getattr(p, k))
+        assert len(a) == len(b) and all(math.isclose(x, y, rel_tol=1e-15, abs_tol=0) for x, y in zip(a, b)), k
+    assert g.visc == "none" and g.averaging == "simple" and g.conv == "weno5z" and g.x1_grid == "uniform"
+    assert g.dirichlet_x_switch == math.nextafter(40.0, 0.0)
+
+
 def test_channel_script_lowers_to_its_plan():
     """The channel script (compressible_TCF_TENO, statistics off) lowers with periodic x0, isothermal
     walls on both x1 faces, the power-law viscosity and the constant forcing, to channel_plan's plan."""
@@ -164,7 +184,8 @@ def test_writer_refuses_kernels_outside_the_lowered_families():
     dissipation sensor is lowered; its Ducros variant adds a shock-sensor kernel and is refused."""
     from opensbli_gb300.writer import GB300Writer
     for case in ("tgv_central", "tgv_weno", "tgsym_central", "katzer_teno", "katzer_adaptive", "katzer_carpenter",
-                 "tgv_filter", "tgv_teno_adaptive", "sbli3d_teno", "transitional_sbli", "channel_teno"):
+                 "tgv_filter", "tgv_teno_adaptive", "sbli3d_teno", "transitional_sbli", "channel_teno",
+                 "shock_reflection"):
         GB300Writer._check_kernel_families(golden_plan(case).kernels)
     assert "User kernel: Non-linear filter application" in golden_plan("tgv_filter").kernels
     names = golden_plan("tgv_filter").kernels + ["User kernel: Shock sensor"]
@@ -192,7 +213,7 @@ def test_cfl_dt_tgv_weno():
 @pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central",
                                   "katzer_teno", "katzer_adaptive", "katzer_carpenter", "tgv_filter",
                                   "katzer_weno", "katzer_wenoz", "katzer_teno6", "tgv_teno_adaptive",
-                                  "sbli3d_teno", "transitional_sbli", "channel_teno"])
+                                  "sbli3d_teno", "transitional_sbli", "channel_teno", "shock_reflection"])
 def test_writer_lowers_reference_script(case, tmp_path):
     r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case, "--out",
                         str(tmp_path), "--ref", REF], capture_output=True, text=True, timeout=900)
