@@ -43,6 +43,8 @@ CASES = {
     "transitional_sbli": "transitional_sbli.py",
     "channel_teno": "channel_teno.py",
     "shock_reflection": "ref:apps/inviscid_shock_reflection/inviscid_shock.py",
+    "sod": "ref:apps/Sod_shock_tube/Sod_shock_tube.py",
+    "shu_osher": "ref:apps/shu_osher/shu_osher.py",
 }
 
 
