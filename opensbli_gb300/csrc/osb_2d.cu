@@ -481,9 +481,6 @@ __device__ __forceinline__ T recon2(const T (&fp)[6], const T (&fm)[6], T eps, T
     return w5_side(fp[0], fp[1], fp[2], fp[3], fp[4], eps) + w5_side(fm[5], fm[4], fm[3], fm[2], fm[1], eps);
 }
 
-// Characteristic flux between window points 2 and 3 along D (2D Euler eigensystem for a unit
-// normal, physical_models/euler_eigensystem.py:77-105; the block's metric is diagonal so the
-// eigensystem is Cartesian).  Dense rows share g = phi X0 - (g-1) u.X + (g-1) X3, h = X_{1+D} - u_D X0.
 // The state of the characteristic system at the interface between the points l and r (conserved
 // ql, qr, pressures and sound speeds): RoeAverage (averaging.py:62-114; rho = sqrt(rho_l rho_r), u
 // and H weighted by sqrt(rho), a from H) or, with simple, SimpleAverage (averaging.py:31-59: the
@@ -508,6 +505,9 @@ __device__ __forceinline__ void avg2(const T (&ql)[4], const T (&qr)[4], T pl, T
   a = sqrt_t(gm1 * (Hh - T(0.5) * (u[0] * u[0] + u[1] * u[1])));
 }
 
+// Characteristic flux between window points 2 and 3 along D (2D Euler eigensystem for a unit
+// normal, physical_models/euler_eigensystem.py:77-105; the block's metric is diagonal so the
+// eigensystem is Cartesian).  Dense rows share g = phi X0 - (g-1) u.X + (g-1) X3, h = X_{1+D} - u_D X0.
 template <typename T, int D, int SCH>
 __device__ __forceinline__ void flux2(const W2<T> (&W)[6], T gama, T eps, T ct, T out[4], bool simple) {
   constexpr int E = 1 - D;
@@ -1736,5 +1736,131 @@ template void launch2_cutoff<double>(const Ctx &, double *, cudaStream_t, int64_
 
 template void launch2_rhs<float>(const Ctx &, int, double, double, double, cudaStream_t, int64_t *);
 template void launch2_rhs<double>(const Ctx &, int, double, double, double, cudaStream_t, int64_t *);
+
+// =============================================================================================
+// 1D Euler blocks (apps/Sod_shock_tube/Sod_shock_tube.py, apps/shu_osher/shu_osher.py): FP64, the
+// three conserved arrays (rho, rhou0, rhoE) on the 2D layout with a single row.  Per stage one thread
+// per interface forms the characteristic flux from the six points around it and the reference's 1D
+// eigensystem (physical_models/euler_eigensystem.py:57-76: waves u-a, u, u+a, REV = [[1,1,1],
+// [u-a,u,u+a],[H-ua,u^2/2,H+ua]], H = a^2/(gama-1) + u^2/2, LEV its inverse) at the Roe or simple
+// average; a second launch differences the fluxes and applies the LS-RK3 update.  The blocks of these
+// apps hold a few hundred to a few thousand points, so the step is launch-bound: it is one graph.
+// =============================================================================================
+struct Euler1Args {
+  double gama, eps, ct;
+  int simple;
+};
+
+template <int SCH> __global__ void __launch_bounds__(128) k1_flux(Grid g, Q4 q, Q4 flux, Euler1Args a) {
+  const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x) - 1;  // the interface i + 1/2, i = -1 .. n0-1
+  if (i >= g.n0) return;
+  const double gm1 = a.gama - 1.0;
+  double Q[6][3], u[6], p[6], c[6];
+#pragma unroll
+  for (int t = 0; t < 6; ++t) {
+    const int64_t m = g2(g, i + t - 2, 0);
+#pragma unroll
+    for (int v = 0; v < 3; ++v) Q[t][v] = q.v[v][m];
+    u[t] = Q[t][1] / Q[t][0];
+    p[t] = gm1 * (Q[t][2] - 0.5 * Q[t][0] * u[t] * u[t]);
+    c[t] = sqrt(a.gama * p[t] / Q[t][0]);
+  }
+  double ua, aa;
+  if (a.simple) {  // SimpleAverage (averaging.py:31-59)
+    ua = 0.5 * (u[2] + u[3]);
+    aa = 0.5 * (c[2] + c[3]);
+  } else {  // RoeAverage (averaging.py:62-114)
+    const double sl = sqrt(Q[2][0]), sr = sqrt(Q[3][0]), inv = 1.0 / (sl + sr);
+    ua = inv * (sl * u[2] + sr * u[3]);
+    const double Hh = inv * ((p[2] + Q[2][2]) / sl + (p[3] + Q[3][2]) / sr);
+    aa = sqrt(gm1 * (Hh - 0.5 * ua * ua));
+  }
+  const double ia = 1.0 / aa, Hs = aa * aa / gm1 + 0.5 * ua * ua;
+  const double L[3][3] = {{0.25 * ua * ia * (gm1 * ua * ia + 2.0), -0.5 * ia * (gm1 * ua * ia + 1.0), 0.5 * gm1 * ia * ia},
+                          {1.0 - 0.5 * gm1 * ua * ua * ia * ia, gm1 * ua * ia * ia, -gm1 * ia * ia},
+                          {0.25 * ua * ia * (gm1 * ua * ia - 2.0), -0.5 * ia * (gm1 * ua * ia - 1.0), 0.5 * gm1 * ia * ia}};
+  double rec[3];
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+    double cf[6], cs[6], lam = 0.0;
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      const double F0 = Q[t][1], F1 = Q[t][1] * u[t] + p[t], F2 = (p[t] + Q[t][2]) * u[t];
+      cf[t] = L[r][0] * F0 + L[r][1] * F1 + L[r][2] * F2;
+      cs[t] = L[r][0] * Q[t][0] + L[r][1] * Q[t][1] + L[r][2] * Q[t][2];
+      lam = fmax(lam, fabs(r == 0 ? c[t] - u[t] : r == 1 ? u[t] : c[t] + u[t]));
+    }
+    double fp[6], fm[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) {
+      fp[t] = cf[t] + lam * cs[t];
+      fm[t] = cf[t] - lam * cs[t];
+    }
+    rec[r] = recon2<double, SCH>(fp, fm, a.eps, a.ct);
+  }
+  const int64_t n = g2(g, i, 0);
+  flux.v[0][n] = rec[0] + rec[1] + rec[2];
+  flux.v[1][n] = (ua - aa) * rec[0] + ua * rec[1] + (ua + aa) * rec[2];
+  flux.v[2][n] = (Hs - ua * aa) * rec[0] + 0.5 * ua * ua * rec[1] + (Hs + ua * aa) * rec[2];
+}
+
+// R = -(F_i - F_{i-1}) / delta0 and the LS-RK3 update (update = 1), or R into du (update = 0)
+__global__ void k1_rk(Grid g, Q4 flux, Q4 du, Q4 q, double inv_d0, double dt, double A, double B, int update) {
+  const int i = (int)(blockIdx.x * blockDim.x + threadIdx.x);
+  if (i >= g.n0) return;
+  const int64_t n = g2(g, i, 0);
+#pragma unroll
+  for (int v = 0; v < 3; ++v) {
+    const double R = -(flux.v[v][n] - flux.v[v][n - 1]) * inv_d0;
+    if (update) {
+      const double d = dt * R + A * du.v[v][n];
+      du.v[v][n] = d;
+      q.v[v][n] = B * d + q.v[v][n];
+    } else {
+      du.v[v][n] = R;
+    }
+  }
+}
+
+// DirichletBC (dirichlet.py:6-41) at both ends: points -3..0 and n0-1..n0+3 take the faces' states;
+// side 1 may instead extrapolate point n0-2 (extrapolation.py:8-58)
+struct Faces1 {
+  double f0[3], f1[3];
+};
+__global__ void k1_bc(Grid g, Q4 q, Faces1 f, int extrap1) {
+  const int t = threadIdx.x;
+  if (t < 4) {
+    for (int v = 0; v < 3; ++v) q.v[v][g2(g, t - 3, 0)] = f.f0[v];
+  } else if (t < 9) {
+    const int i = g.n0 - 1 + (t - 4);
+    for (int v = 0; v < 3; ++v) q.v[v][g2(g, i, 0)] = extrap1 ? q.v[v][g2(g, g.n0 - 2, 0)] : f.f1[v];
+  }
+}
+
+void launch1_bcs(const Ctx &c, cudaStream_t s, int64_t *launches) {
+  Faces1 f;
+  for (int v = 0; v < 3; ++v) {
+    f.f0[v] = c.plan.dirichlet_x0[0][v];
+    f.f1[v] = c.plan.dirichlet_x0[1][v];
+  }
+  k1_bc<<<1, 32, 0, s>>>(c.g, q4(c.q64_2d), f, c.plan.bc[0][1] == OSB_BC_EXTRAPOLATION);
+  ++*launches;
+}
+
+void launch1_rhs(const Ctx &c, int update, double A, double B, double dt, cudaStream_t s, int64_t *launches) {
+  const osb_plan_desc &p = c.plan;
+  const bool teno = p.conv == OSB_CONV_TENO5 || p.conv == OSB_CONV_TENO6;
+  const Euler1Args a{p.gama, teno ? p.teno_eps : p.weno_eps, p.teno_ct, p.averaging == OSB_AVG_SIMPLE};
+  const int nb = (c.g.n0 + 1 + 127) / 128;
+  const Q4 q = q4(c.q64_2d);
+  Q4 fl;  // the interface fluxes (the residual arrays of the context, FP64 for these blocks)
+  for (int v = 0; v < 4; ++v) fl.v[v] = static_cast<double *>(c.res[v]);
+  if (p.conv == OSB_CONV_TENO5) k1_flux<SCH_TENO><<<nb, 128, 0, s>>>(c.g, q, fl, a);
+  else if (p.conv == OSB_CONV_TENO6) k1_flux<SCH_TENO6><<<nb, 128, 0, s>>>(c.g, q, fl, a);
+  else if (p.conv == OSB_CONV_WENO5Z) k1_flux<SCH_Z><<<nb, 128, 0, s>>>(c.g, q, fl, a);
+  else k1_flux<SCH_JS><<<nb, 128, 0, s>>>(c.g, q, fl, a);
+  k1_rk<<<(c.g.n0 + 127) / 128, 128, 0, s>>>(c.g, fl, q4(c.du2), q, 1.0 / p.delta[0], dt, A, B, update);
+  *launches += 2;
+}
 
 }  // namespace osb

@@ -59,6 +59,36 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
     snprintf(why, n, "forcing: 3D wall-bounded blocks only");
     return OSB_EUNSUPPORTED;
   }
+  if (p->ndim == 1) {
+    // 1D Euler block (Sod_shock_tube.py, shu_osher.py): Dirichlet faces (side 1 may extrapolate), FP64
+    if (p->n[0] < 8 || p->n[0] > (1 << 24)) { snprintf(why, n, "n[0] = %d out of range [8, 2^24]", p->n[0]); return OSB_EINVAL; }
+    if (!(p->delta[0] > 0)) { snprintf(why, n, "delta[0] must be > 0"); return OSB_EINVAL; }
+    if (p->bc[0][0] != OSB_BC_DIRICHLET || (p->bc[0][1] != OSB_BC_DIRICHLET && p->bc[0][1] != OSB_BC_EXTRAPOLATION)) {
+      snprintf(why, n, "1D blocks: a Dirichlet face at x0 = 0, a Dirichlet or extrapolation face at the end");
+      return OSB_EUNSUPPORTED;
+    }
+    if (p->conv != OSB_CONV_TENO5 && p->conv != OSB_CONV_WENO5JS && p->conv != OSB_CONV_WENO5Z &&
+        p->conv != OSB_CONV_TENO6) {
+      snprintf(why, n, "1D blocks: TENO5, TENO6, WENO5-JS or WENO5-Z fluxes");
+      return OSB_EUNSUPPORTED;
+    }
+    if (p->teno_adaptive || p->filter != OSB_FILTER_NONE || p->shock_fp64 != 0.0) {
+      snprintf(why, n, "1D blocks: fixed TENO cut-off, no filter");
+      return OSB_EUNSUPPORTED;
+    }
+    if (p->visc != OSB_VISC_NONE) { snprintf(why, n, "1D blocks: Euler equations (no viscosity)"); return OSB_EUNSUPPORTED; }
+    if (p->rk != OSB_RK3_LS) { snprintf(why, n, "1D blocks: low-storage RK3"); return OSB_EUNSUPPORTED; }
+    if (p->precision != OSB_PREC_FP64) { snprintf(why, n, "1D blocks: FP64"); return OSB_EUNSUPPORTED; }
+    if (p->averaging != OSB_AVG_ROE && p->averaging != OSB_AVG_SIMPLE) {
+      snprintf(why, n, "averaging %d: OSB_AVG_ROE or OSB_AVG_SIMPLE", p->averaging);
+      return OSB_EINVAL;
+    }
+    for (int side = 0; side < 2; ++side)
+      for (int v = 0; v < 3; ++v)
+        if (!std::isfinite(p->dirichlet_x0[side][v])) { snprintf(why, n, "dirichlet_x0 must be finite"); return OSB_EINVAL; }
+    if (!(p->gama > 1.0)) { snprintf(why, n, "bad physical constants"); return OSB_EINVAL; }
+    return OSB_OK;
+  }
   if (p->ndim == 2) {
     for (int d = 0; d < 2; ++d) {
       if (p->n[d] < 8 || p->n[d] > 16384) { snprintf(why, n, "n[%d] = %d out of range [8, 16384]", d, p->n[d]); return OSB_EINVAL; }
@@ -126,7 +156,7 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
     }
     return OSB_OK;
   }
-  if (p->ndim != 3) { snprintf(why, n, "ndim %d: this library implements 2D and 3D blocks", p->ndim); return OSB_EUNSUPPORTED; }
+  if (p->ndim != 3) { snprintf(why, n, "ndim %d: this library implements 1D, 2D and 3D blocks", p->ndim); return OSB_EUNSUPPORTED; }
   if (wall3(*p)) {
     // span-periodic wall-bounded block: the 2D configuration's faces in x0 and x1, or the channel's
     // periodic x0 and isothermal walls on both x1 faces; periodic x2
@@ -230,6 +260,18 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
 
 Grid make_grid(const osb_plan_desc *p) {
   Grid g;
+  if (p->ndim == 1) {  // one row with a 4-point x halo
+    g.n0 = p->n[0];
+    g.n1 = 1;
+    g.n2 = 1;
+    int64_t px = p->n[0] + 8;
+    px = (px + 7) / 8 * 8;
+    g.sy = px;
+    g.sz = px;
+    g.off0 = 4;
+    g.numel = px;
+    return g;
+  }
   if (p->ndim == 2) {  // x fastest, 4-point halo on every side, one plane
     g.n0 = p->n[0];
     g.n1 = p->n[1];
@@ -610,6 +652,14 @@ template <typename T> int step3w_impl(osb_ctx *c, int nsteps, double dt) {
 // One LS-RK3 step on a 2D block: boundary conditions, then per stage the right-hand side with the
 // update du = A du + dt R, q += B du, and the boundary conditions again (algorithm.py:384-477).
 template <typename T> void one_step2(osb_ctx *c, double dt, cudaStream_t s) {
+  if (c->plan.ndim == 1) {  // 1D Euler block (FP64): faces, then per stage fluxes + update and faces
+    launch1_bcs(*c, s, &c->launches);
+    for (int st = 0; st < 3; ++st) {
+      launch1_rhs(*c, 1, c->plan.rk_a[st], c->plan.rk_b[st], dt, s, &c->launches);
+      launch1_bcs(*c, s, &c->launches);
+    }
+    return;
+  }
   {
     ProfScope ps(c, PF_HALO, s);
     launch2_bcs(*c, s, &c->launches);
@@ -663,10 +713,11 @@ template <typename T> int step2_impl(osb_ctx *c, int nsteps, double dt) {
 }
 
 template <typename T> __global__ void k_set64_padded(Grid g, const double *src, int h, T *q, double *q64) {
-  const int w = g.n0 + 2 * h, hgt = g.n1 + 2 * h, dep = g.n2 == 1 ? 1 : g.n2 + 2 * h;
+  // a 1D block (n1 = 1) has no x1 halo, a 2D block (n2 = 1) no x2 halo
+  const int w = g.n0 + 2 * h, hgt = g.n1 == 1 ? 1 : g.n1 + 2 * h, dep = g.n2 == 1 ? 1 : g.n2 + 2 * h;
   const int64_t N = (int64_t)w * hgt * dep;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
-    const int i = (int)(t % w) - h, j = (int)((t / w) % hgt) - h;
+    const int i = (int)(t % w) - h, j = g.n1 == 1 ? 0 : (int)((t / w) % hgt) - h;
     const int k = g.n2 == 1 ? 0 : (int)(t / ((int64_t)w * hgt)) - h;
     const int64_t n = gidx(g, i, j, k);
     q64[n] = src[t];
@@ -697,16 +748,20 @@ template <typename T> __global__ void k_pack_d(Grid g, P4 src4, T *dst, int nvar
 struct D4 {
   const double *v[4];
 };
-__global__ void k_reduce2(Grid g, D4 q, int what, double *partial) {
+__global__ void k_reduce2(Grid g, D4 q, int what, double *partial, int nvar) {
+  // 2D blocks (rho, rhou0, rhou1, rhoE) and 1D blocks (rho, rhou0, rhoE)
   const int64_t N = (int64_t)g.n0 * g.n1;
   double acc = 0.0;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(t % g.n0), j = (int)(t / g.n0);
     const int64_t n = gidx(g, i, j, 0);
-    if (what == OSB_RED_KE) acc += 0.5 * (q.v[1][n] * q.v[1][n] + q.v[2][n] * q.v[2][n]) / q.v[0][n];
-    else
-      for (int v = 0; v < 4; ++v)
+    if (what == OSB_RED_KE) {
+      const double m1 = nvar == 4 ? q.v[2][n] : 0.0;
+      acc += 0.5 * (q.v[1][n] * q.v[1][n] + m1 * m1) / q.v[0][n];
+    } else {
+      for (int v = 0; v < nvar; ++v)
         if (!isfinite(q.v[v][n])) acc = 1.0;
+    }
   }
   const double s = block_sum(acc);
   if (threadIdx.x == 0) partial[blockIdx.x] = (what == OSB_RED_NANCHECK) ? (s > 0 ? 1.0 : 0.0) : s;
@@ -797,10 +852,11 @@ static int check_bound(osb_ctx *c);
 int osb_set_state64_padded(osb_ctx *c, int var, const double *src, int h) {
   if (!c) return OSB_EINVAL;
   if (int rc = check_bound(c)) return rc;
-  const int hmax = c->plan.ndim == 2 ? 4 : HY;
+  const int hmax = c->plan.ndim <= 2 ? 4 : HY;
   if (var < 0 || var >= c->nvar || !src || h < 1 || h > hmax) return set_err(c, OSB_EINVAL, "bad var, pointer or halo");
-  double *m = c->plan.ndim == 2 ? c->q64_2d[var] : c->qold[var];
-  const int64_t N = (int64_t)(c->g.n0 + 2 * h) * (c->g.n1 + 2 * h) * (c->plan.ndim == 2 ? 1 : c->g.n2 + 2 * h);
+  double *m = c->plan.ndim <= 2 ? c->q64_2d[var] : c->qold[var];
+  const int64_t N = (int64_t)(c->g.n0 + 2 * h) * (c->plan.ndim == 1 ? 1 : c->g.n1 + 2 * h) *
+                    (c->plan.ndim <= 2 ? 1 : c->g.n2 + 2 * h);
   const int nb = blocks_for(N);
   if (c->mixed) k_set64_padded<float><<<nb, 256, 0, c->stream>>>(c->g, src, h, (float *)c->qa[var], m);
   else k_set64_padded<double><<<nb, 256, 0, c->stream>>>(c->g, src, h, (double *)c->qa[var], m);
@@ -845,9 +901,9 @@ int osb_query_layout(const osb_plan_desc *plan, osb_layout *out) {
   out->stride_y = g.sy;
   out->stride_z = g.sz;
   out->halo[0] = HX;
-  out->halo[1] = plan->ndim == 2 ? 4 : HY;
-  out->halo[2] = plan->ndim == 2 ? 0 : HZ;
-  out->nvar = plan->ndim == 2 ? 4 : 5;
+  out->halo[1] = plan->ndim == 1 ? 0 : plan->ndim == 2 ? 4 : HY;
+  out->halo[2] = plan->ndim <= 2 ? 0 : HZ;
+  out->nvar = plan->ndim + 2;
   out->state_bytes = plan->precision == OSB_PREC_MIXED ? 4 : 8;
   return OSB_OK;
 }
@@ -870,10 +926,10 @@ int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
   c->ph = plan_phys(plan);
   const size_t bytes = (size_t)c->g.numel * c->elem;
   cudaError_t e = cudaSuccess;
-  if (plan->ndim == 2) {
-    c->nvar = 4;
+  if (plan->ndim <= 2) {  // 2D blocks, and 1D blocks on the same storage
+    c->nvar = plan->ndim + 2;
     const size_t b64 = (size_t)c->g.numel * sizeof(double);
-    for (int v = 0; v < 4 && e == cudaSuccess; ++v) {
+    for (int v = 0; v < c->nvar && e == cudaSuccess; ++v) {
       if (c->mixed) {
         e = cudaMalloc(&c->q64_2d[v], b64);
         if (e == cudaSuccess) e = cudaMemset(c->q64_2d[v], 0, b64);
@@ -909,7 +965,7 @@ int osb_create(const osb_plan_desc *plan, osb_ctx **out) {
     if (e == cudaSuccess) e = cudaMalloc(&c->sd111, b64);
     if (e == cudaSuccess) e = cudaMemset(c->d11, 0, b64);
     if (e == cudaSuccess) e = cudaMemset(c->sd111, 0, b64);
-    if (e == cudaSuccess && plan->cartesian) {  // no metric terms: D11 = 1, SD111 = 0
+    if (e == cudaSuccess && (plan->cartesian || plan->ndim == 1)) {  // no metric terms: D11 = 1, SD111 = 0
       std::vector<double> ones((size_t)c->g.numel, 1.0);
       e = cudaMemcpy(c->d11, ones.data(), b64, cudaMemcpyHostToDevice);
       c->metrics_valid = 1;
@@ -1006,7 +1062,7 @@ int osb_bind_field(osb_ctx *c, int var, void *dev_ptr) {
   if (var < 0 || var >= c->nvar) return set_err(c, OSB_EINVAL, "var out of range");
   if (!dev_ptr || ((uintptr_t)dev_ptr % 32) != 0) return set_err(c, OSB_EINVAL, "device pointer null or not 32-byte aligned");
   c->qa[var] = dev_ptr;
-  if (c->plan.ndim == 2 && !c->mixed) c->q64_2d[var] = static_cast<double *>(dev_ptr);
+  if (c->plan.ndim <= 2 && !c->mixed) c->q64_2d[var] = static_cast<double *>(dev_ptr);
   c->qold_valid = 0;
   c->cur = 0;
   if (c->plan.ndim == 3) encode_state_maps(*c, 0);
@@ -1070,7 +1126,7 @@ int osb_set_state64(osb_ctx *c, int var, const double *src) {
   src = static_cast<const double *>(device_access(src));
   if (!src) return set_err(c, OSB_EINVAL, "osb_set_state64: source is neither device nor page-locked host memory");
   const int nb = blocks_for((int64_t)c->g.n0 * c->g.n1 * c->g.n2);
-  if (c->plan.ndim == 2) {
+  if (c->plan.ndim <= 2) {
     if (c->mixed) k_set64<float><<<nb, 256, 0, c->stream>>>(c->g, src, (float *)c->qa[var], c->q64_2d[var]);
     else k_set64<double><<<nb, 256, 0, c->stream>>>(c->g, src, (double *)c->qa[var], c->q64_2d[var]);
     c->qold_valid = 1;
@@ -1122,11 +1178,12 @@ int osb_probe(osb_ctx *c, int n, const int *what_ijk, double *host_out) {
   if (n == 0) return OSB_OK;
   if (n > OSB_PROBE_MAX) return set_err(c, OSB_ETOOLARGE, "osb_probe: too many probes");
   if (!c->qold_valid) return set_err(c, OSB_EINVAL, "no state yet: call osb_init_tgv, osb_set_state64 or osb_step");
-  const int n2 = c->plan.ndim == 2 ? 1 : c->g.n2;
+  const int n2 = c->plan.ndim <= 2 ? 1 : c->g.n2;
   for (int t = 0; t < n; ++t) {
     const int w = what_ijk[4 * t], i = what_ijk[4 * t + 1], j = what_ijk[4 * t + 2], k = what_ijk[4 * t + 3];
     const bool ok_w = (w >= 0 && w < c->nvar) || (w >= OSB_PROBE_U0 && w <= OSB_PROBE_T &&
-                                                   (w != OSB_PROBE_U2 || c->plan.ndim == 3));
+                                                   (w != OSB_PROBE_U2 || c->plan.ndim == 3) &&
+                                                   (w != OSB_PROBE_U1 || c->plan.ndim >= 2));
     if (!ok_w || i < 0 || i >= c->g.n0 || j < 0 || j >= c->g.n1 || k < 0 || k >= n2)
       return set_err(c, OSB_EINVAL, "osb_probe: quantity or index out of range");
   }
@@ -1137,7 +1194,7 @@ int osb_probe(osb_ctx *c, int n, const int *what_ijk, double *host_out) {
   double *out = reinterpret_cast<double *>(req + 4 * OSB_PROBE_MAX);
   e = cudaMemcpyAsync(req, what_ijk, sizeof(int) * 4 * n, cudaMemcpyHostToDevice, c->stream);
   Fields5<double> m;
-  for (int v = 0; v < 5; ++v) m.v[v] = v < c->nvar ? (c->plan.ndim == 2 ? c->q64_2d[v] : c->qold[v]) : nullptr;
+  for (int v = 0; v < 5; ++v) m.v[v] = v < c->nvar ? (c->plan.ndim <= 2 ? c->q64_2d[v] : c->qold[v]) : nullptr;
   if (e == cudaSuccess) {
     k_probe<<<(n + 127) / 128, 128, 0, c->stream>>>(c->g, m, c->nvar, n, req, out, c->ph.gm1, c->ph.gM2);
     e = cudaGetLastError();
@@ -1154,7 +1211,7 @@ int osb_get_state64(osb_ctx *c, int var, double *dst) {
   if (!dst) return set_err(c, OSB_EINVAL, "osb_get_state64: destination is neither device nor page-locked host memory");
   if (!c->qold_valid) return set_err(c, OSB_EINVAL, "no state yet: call osb_init_tgv, osb_set_state64 or osb_step");
   const int nb = blocks_for((int64_t)c->g.n0 * c->g.n1 * c->g.n2);
-  k_get64<<<nb, 256, 0, c->stream>>>(c->g, c->plan.ndim == 2 ? c->q64_2d[var] : c->qold[var], dst);
+  k_get64<<<nb, 256, 0, c->stream>>>(c->g, c->plan.ndim <= 2 ? c->q64_2d[var] : c->qold[var], dst);
   return cuda_err(c, cudaGetLastError(), "osb_get_state64");
 }
 
@@ -1163,6 +1220,7 @@ int osb_teno_cutoff(osb_ctx *c, double *dev_out) {
   if (!dev_out) return set_err(c, OSB_EINVAL, "null output");
   if (!c->plan.teno_adaptive) return set_err(c, OSB_EINVAL, "plan has no adaptive TENO");
   if (int rc = check_bound(c)) return rc;
+  if (c->plan.ndim == 1) return set_err(c, OSB_EUNSUPPORTED, "osb_teno_cutoff: 1D blocks have a fixed cut-off");
   if (wall3(c->plan)) {
     if (!c->metrics_valid) return set_err(c, OSB_EINVAL, "3D wall-bounded block: call osb_set_coordinate first");
     if (!c->qold_valid) return set_err(c, OSB_EINVAL, "set the state first");
@@ -1196,9 +1254,9 @@ int osb_step(osb_ctx *c, int nsteps, double dt) {
   if (!c) return OSB_EINVAL;
   if (int rc = check_bound(c)) return rc;
   if (nsteps < 0 || !(dt > 0)) return set_err(c, OSB_EINVAL, "nsteps >= 0 and dt > 0 required");
-  if (c->plan.ndim == 2) {
+  if (c->plan.ndim <= 2) {  // one_step2 steps 1D blocks too
     if (!c->metrics_valid) return set_err(c, OSB_EINVAL, "2D block: call osb_set_coordinate first");
-    if (!c->qold_valid) return set_err(c, OSB_EINVAL, "2D block: set the state first");
+    if (!c->qold_valid) return set_err(c, OSB_EINVAL, "set the state first");
     return c->mixed ? step2_impl<float>(c, nsteps, dt) : step2_impl<double>(c, nsteps, dt);
   }
   if (wall3(c->plan)) {
@@ -1214,6 +1272,15 @@ int osb_residual(osb_ctx *c, void *dev_out) {
   if (int rc = check_bound(c)) return rc;
   if (!dev_out) return set_err(c, OSB_EINVAL, "null output");
   const int nb = blocks_for((int64_t)c->g.n0 * c->g.n1 * c->g.n2);
+  if (c->plan.ndim == 1) {
+    int64_t l = 0;
+    launch1_bcs(*c, c->stream, &l);
+    launch1_rhs(*c, 0, 0.0, 0.0, 0.0, c->stream, &l);
+    P4 d;
+    for (int v = 0; v < 3; ++v) d.v[v] = c->du2[v];
+    k_pack_d<double><<<nb, 256, 0, c->stream>>>(c->g, d, (double *)dev_out, 3);
+    return cuda_err(c, cudaGetLastError(), "osb_residual");
+  }
   if (c->plan.ndim == 2) {
     if (!c->metrics_valid) return set_err(c, OSB_EINVAL, "2D block: call osb_set_coordinate first");
     int64_t l = 0;
@@ -1264,11 +1331,11 @@ int osb_reduce(osb_ctx *c, int what, double *out) {
   const int64_t N = (int64_t)c->g.n0 * c->g.n1 * c->g.n2;
   int nb = blocks_for(N);
   if (nb > c->red_blocks) nb = c->red_blocks;
-  if (c->plan.ndim == 2) {
+  if (c->plan.ndim <= 2) {
     if (what == OSB_RED_ENSTROPHY) return set_err(c, OSB_EUNSUPPORTED, "enstrophy: 3D blocks");
     D4 q2;
     for (int v = 0; v < 4; ++v) q2.v[v] = c->q64_2d[v];
-    k_reduce2<<<nb, RED_THREADS, 0, c->stream>>>(c->g, q2, what, c->red);
+    k_reduce2<<<nb, RED_THREADS, 0, c->stream>>>(c->g, q2, what, c->red, c->nvar);
     k_reduce_final<<<1, RED_THREADS, 0, c->stream>>>(c->red, nb, what, 1.0 / (double)N, c->red + c->red_blocks);
     double h = 0;
     cudaError_t e = cudaMemcpyAsync(&h, c->red + c->red_blocks, sizeof(double), cudaMemcpyDeviceToHost, c->stream);

@@ -272,6 +272,43 @@ def shock_reflection_plan(n0=457, n1=255, precision="fp64", dt=0.1, use_graphs=T
                 dirichlet_x_switch=math.nextafter(40.0, 0.0), name="shock_reflection_%s_%dx%d" % (conv, n0, n1))
 
 
+def _euler1d_state(g, d, u0, p):
+    """rho, rhou0, rhoE as the generated 1D face kernels form them: rhoE = d u0^2 / 2 + p / (gama - 1)."""
+    return (d, d * u0, 0.5 * d * u0 ** 2 + p / (g - 1.0))
+
+
+def sod_plan(n0=200, precision="fp64", dt=2e-4, use_graphs=True, conv="teno5", averaging="roe"):
+    """The Sod shock tube of apps/Sod_shock_tube/Sod_shock_tube.py: 1D Euler, gama = 1.4, [0, 1] with
+    n0 points, LLFTeno(5) with RoeAverage (C_T = 1e-5, eps = 1e-16), RungeKuttaLS(3), Dirichlet faces
+    holding the left (1, 0, 1) and right (0.125, 0, 0.1) states (rho, u, p); 200 points and dt = 2e-4
+    as the script sets them."""
+    g = 1.4
+    return Plan(ndim=1, n=(n0, 1, 1), delta=(1.0 / (n0 - 1), 1.0, 1.0), conv=conv, visc="none", rk="ls_rk3",
+                precision=precision, averaging=averaging, bc=(("dirichlet", "dirichlet"),) + (("periodic", "periodic"),) * 2,
+                gama=g, teno_ct=1e-5, teno_eps=1e-16, weno_eps=1e-14 if conv == "weno5z" else 1e-6,
+                rk_a=(0.0, -5.0 / 9.0, -153.0 / 128.0), rk_b=(1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0), dt=dt,
+                use_graphs=use_graphs, ic="host", x1_grid="uniform",
+                dirichlet_x0=(_euler1d_state(g, 1.0, 0.0, 1.0), _euler1d_state(g, 0.125, 0.0, 0.1)),
+                name="sod_%s_%d" % (conv, n0))
+
+
+def shu_osher_plan(n0=3200, precision="fp64", dt=2e-4, use_graphs=True, conv="weno5z", averaging="roe"):
+    """The Shu-Osher shock/entropy-wave interaction of apps/shu_osher/shu_osher.py: 1D Euler, gama = 1.4,
+    [-5, 5] with n0 points, LLFWeno(5, 'Z') with RoeAverage, RungeKuttaLS(3), Dirichlet faces holding
+    the post-shock state (3.857143, 2.629369, 10.33333) and (1 + 0.2 sin(25), 0, 1) (rho, u, p); 3200
+    points and dt = 2e-4 as the script sets them."""
+    import math as m
+    g = 1.4
+    return Plan(ndim=1, n=(n0, 1, 1), delta=(10.0 / (n0 - 1), 1.0, 1.0), conv=conv, visc="none", rk="ls_rk3",
+                precision=precision, averaging=averaging, bc=(("dirichlet", "dirichlet"),) + (("periodic", "periodic"),) * 2,
+                gama=g, Minf=0.1, teno_ct=1e-5, teno_eps=1e-15, weno_eps=1e-14 if conv == "weno5z" else 1e-6,
+                rk_a=(0.0, -5.0 / 9.0, -153.0 / 128.0), rk_b=(1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0), dt=dt,
+                use_graphs=use_graphs, ic="host", x1_grid="uniform",
+                dirichlet_x0=(_euler1d_state(g, 3.857143, 2.629369, 10.33333),
+                              _euler1d_state(g, 1.0 + 0.2 * m.sin(5 * 5.0), 0.0, 1.0)),
+                name="shu_osher_%s_%d" % (conv, n0))
+
+
 def katzer_plan(n0=512, n1=256, precision="fp64", conv="teno5", dt=0.04, use_graphs=True, adaptive=False,
                 closure=(("reduced_access", "reduced_access"),) * 2):
     """2D laminar shock-wave/boundary-layer interaction (apps/katzer_SBLI/katzer_SBLI.py constants):

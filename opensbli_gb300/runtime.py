@@ -271,6 +271,8 @@ class Solver:
 
     @property
     def shape(self):
+        if self.plan.ndim == 1:
+            return (self.plan.n[0],)
         if self.plan.ndim == 2:
             return (self.plan.n[1], self.plan.n[0])
         return (self.plan.n[2], self.plan.n[1], self.plan.n[0])
@@ -278,6 +280,8 @@ class Solver:
     def interior(self, var):
         """View of the interior of bound variable `var` as [z][y][x] ([y][x] in 2D), state precision."""
         lay = self.layout
+        if self.plan.ndim == 1:
+            return torch.as_strided(self.fields[var], self.shape, (1,), lay.offset)
         if self.plan.ndim == 2:
             return torch.as_strided(self.fields[var], self.shape, (lay.stride_y, 1), lay.offset)
         n0, n1, n2 = self.plan.n

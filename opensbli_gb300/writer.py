@@ -26,7 +26,8 @@ import numpy as np
 from . import physics_check
 from .plan import Plan
 
-_C_NAMES = {"M_PI": math.pi, "pi": math.pi}
+_C_NAMES = {"M_PI": math.pi, "pi": math.pi, "ceil": math.ceil, "floor": math.floor, "sqrt": math.sqrt,
+            "sin": math.sin, "cos": math.cos, "exp": math.exp, "log": math.log, "pow": math.pow, "fabs": abs}
 
 
 def _eval_c_expr(expr, env):
@@ -98,7 +99,7 @@ class GB300Writer:
         names = [n or "" for n in self.kernel_names]
         self._check_kernel_families(names)
         ndim = self.block.ndim
-        if ndim == 2 or (ndim == 3 and any(n.startswith("IsothermalWall boundary") for n in names)):
+        if ndim in (1, 2) or (ndim == 3 and any(n.startswith("IsothermalWall boundary") for n in names)):
             return self._lower_2d(precision, use_graphs)
         if ndim != 3:
             raise NotImplementedError("GB300Writer lowers 2D and 3D blocks (got ndim=%d)" % ndim)
@@ -313,11 +314,13 @@ class GB300Writer:
             raise NotImplementedError("5th-order reconstruction stencil expected")
         averaging = self._averaging(teno or weno)
         # a 2D Euler block (apps/inviscid_shock_reflection/inviscid_shock.py): no viscous kernels, no metric
-        euler = nd == 2 and not any(n.startswith(("CRmu", "CRT", "Viscous")) for n in names)
+        euler = nd <= 2 and not any(n.startswith(("CRmu", "CRT", "Viscous")) for n in names)
         if euler:
             if self._kernels("MetricsEquation") or self._kernels("Metric boundary"):
-                raise NotImplementedError("2D Euler blocks: Cartesian grids only")
+                raise NotImplementedError("Euler blocks: Cartesian grids only")
             return self._lower_euler2d(precision, use_graphs, conv, averaging, names)
+        if nd == 1:
+            raise NotImplementedError("1D blocks: the Euler equations")
         if not self._kernels("MetricsEquation") or not self._kernels("Metric boundary"):
             raise NotImplementedError("2D blocks: metric terms expected")
         if not any(n.startswith("CRmu") for n in names):
@@ -450,7 +453,7 @@ class GB300Writer:
             raise NotImplementedError("one average for every direction expected")
         return kinds.pop()
 
-    def _face_states(self, kname, consts):
+    def _face_states(self, kname, consts, nd=2):
         """Evaluate a Dirichlet face kernel (dirichlet.py:6-41) as the generated code does, in equation
         order with its locals, the constants in `consts`, and x0 a free variable.  Returns (lo, hi, xs):
         the states (rho, rhou0, rhou1, rhoE) where x0 <= xs and where x0 > xs (xs = 1e300: one state)."""
@@ -472,13 +475,19 @@ class GB300Writer:
                         raise NotImplementedError("Dirichlet face reads %s" % a)
                     reps[a] = x
                 elif t == "ConstantObject":
-                    if str(a) not in consts:
-                        raise NotImplementedError("Dirichlet face constant %s" % a)
-                    reps[a] = sympy.Float(consts[str(a)], 30)
-                elif isinstance(a, sympy.Symbol):  # the kernel's locals (GridVariables)
-                    if str(a) not in env:
-                        raise NotImplementedError("Dirichlet face: %s used before it is set" % a)
-                    reps[a] = env[str(a)]
+                    if str(a) in consts:  # others (a grid spacing of an unused local) stay symbols
+                        reps[a] = sympy.Float(consts[str(a)], 30)
+                elif t == "GridVariable" or (isinstance(a, sympy.Symbol) and t == "Symbol"):
+                    # the kernel's locals, else a constant the generated code reads by name (a script
+                    # that parses "gama" without declaring it a ConstantObject); the generated code
+                    # initialises every local to 0.0, so one read before it is set reads 0
+                    # (shu_osher.py's outlet face reads u0 so)
+                    if str(a) in env:
+                        reps[a] = env[str(a)]
+                    elif str(a) in consts and t == "Symbol":
+                        reps[a] = sympy.Float(consts[str(a)], 30)
+                    else:
+                        reps[a] = sympy.Float(0)
             v = e.rhs.xreplace(reps)
             for r in sympy.preorder_traversal(v):
                 if isinstance(r, sympy.core.relational.Relational) and r.free_symbols == {x}:
@@ -488,9 +497,12 @@ class GB300Writer:
                 env[str(e.lhs)] = v
             else:
                 out[re.sub(r"_B0$", "", str(getattr(e.lhs, "base", e.lhs)))] = v
-        order = ["rho", "rhou0", "rhou1", "rhoE"]
+        order = ["rho", "rhou0", "rhou1", "rhoE"] if nd == 2 else ["rho", "rhou0", "rhoE"]
         if set(out) != set(order):
             raise NotImplementedError("%s sets %s" % (kname, sorted(out)))
+        for n_ in order:
+            if out[n_].free_symbols - {x}:
+                raise NotImplementedError("%s: %s depends on %s" % (kname, n_, out[n_].free_symbols - {x}))
 
         def at(xv):
             return tuple(float(out[n].subs(x, xv)) for n in order)
@@ -525,6 +537,7 @@ class GB300Writer:
             "Dirichlet boundary dir1 side1": ("dirichlet", 1, 1),
             "Symmetry boundary dir1 side1": ("symmetry", 1, 1),
         }
+        nd = self.block.ndim
         bcs = [[None, None], [None, None]]
         for kname, (kind, d, side) in faces.items():
             if self._kernels(kname):
@@ -532,17 +545,22 @@ class GB300Writer:
                     raise NotImplementedError("two boundary conditions on face dir%d side%d" % (d, side))
                 bcs[d][side] = kind
         other = sorted(n for n in names if "boundary dir" in n and n not in faces)
-        if other or bcs[1][0] != "symmetry" or None in bcs[0] or bcs[1][1] is None:
+        if nd == 1:  # 1D (Sod_shock_tube.py, shu_osher.py): a Dirichlet face at x0 = 0
+            if other or bcs[0][0] != "dirichlet" or bcs[0][1] not in ("dirichlet", "extrapolation"):
+                raise NotImplementedError("1D Euler block boundary conditions: %s" %
+                                          (other or sorted(n for n in names if "boundary dir" in n)))
+            bcs[1] = ["periodic", "periodic"]
+        elif other or bcs[1][0] != "symmetry" or None in bcs[0] or bcs[1][1] is None:
             raise NotImplementedError("2D Euler block boundary conditions: %s" %
                                       (other or sorted(n for n in names if "boundary dir" in n)))
-        physics_check.check_algorithm(self.components, 2, viscous=False, metric=False)
+        physics_check.check_algorithm(self.components, nd, viscous=False, metric=False)
         self._euler_faces = bcs
-        plan = Plan(ndim=2, n=(64, 32, 1), delta=(1.0, 1.0, 1.0), conv=conv,
+        plan = Plan(ndim=nd, n=(64, 32, 1) if nd == 2 else (64, 1, 1), delta=(1.0, 1.0, 1.0), conv=conv,
                     weno_eps=1e-14 if conv == "weno5z" else 1e-6,  # WenoZ.eps / WenoJS.eps (weno.py)
                     visc="none", rk="ls_rk3", precision=precision, averaging=averaging, x1_grid="uniform",
                     bc=(tuple(bcs[0]), tuple(bcs[1]), ("periodic", "periodic")),
-                    rk_a=coeff["rkA"], rk_b=coeff["rkB"], use_graphs=use_graphs, ic="host", name="euler2d",
-                    kernels=[n for n in names if n])
+                    rk_a=coeff["rkA"], rk_b=coeff["rkB"], use_graphs=use_graphs, ic="host",
+                    name="euler%dd" % nd, kernels=[n for n in names if n])
         return self._euler_states(plan)
 
     def _euler_states(self, plan):
@@ -550,16 +568,17 @@ class GB300Writer:
         consts = {"gama": plan.gama, "Minf": plan.Minf}
         consts.update({k: v for k, v in self.values.items() if isinstance(v, (int, float))})
         b = self._euler_faces
+        nd = plan.ndim
         kw = {}
         x0 = []
         for side in range(2):
             if b[0][side] == "dirichlet":
-                lo, hi, xs = self._face_states("Dirichlet boundary dir0 side%d" % side, consts)
+                lo, hi, xs = self._face_states("Dirichlet boundary dir0 side%d" % side, consts, nd)
                 if xs != 1e300:
                     raise NotImplementedError("Dirichlet x0 face: a constant state expected")
                 x0.append(lo)
             else:
-                x0.append((0.0, 0.0, 0.0, 0.0))
+                x0.append((0.0,) * (nd + 2))
         kw["dirichlet_x0"] = tuple(x0)
         if b[1][1] == "dirichlet":
             lo, hi, xs = self._face_states("Dirichlet boundary dir1 side1", consts)
@@ -868,7 +887,7 @@ class GB300Writer:
                       by=float(env.get("by", p.by)), teno_a1=float(env.get("teno_a1", p.teno_a1)),
                       teno_a2=float(env.get("teno_a2", p.teno_a2)))
         self.plan = p.replace(**kw)
-        if p.visc == "none" and p.ndim == 2:  # the Dirichlet states of a 2D Euler block use gama and Minf
+        if p.visc == "none" and p.ndim <= 2:  # the Dirichlet states of an Euler block use gama and Minf
             self.plan = self._euler_states(self.plan)
         return self.plan
 
@@ -928,7 +947,8 @@ class GB300Writer:
         return out
 
     def state_names(self):
-        return ["rho", "rhou0", "rhou1", "rhoE"] if self.plan.ndim == 2 else ["rho", "rhou0", "rhou1", "rhou2", "rhoE"]
+        return {1: ["rho", "rhou0", "rhoE"], 2: ["rho", "rhou0", "rhou1", "rhoE"]}.get(
+            self.plan.ndim, ["rho", "rhou0", "rhou1", "rhou2", "rhoE"])
 
     def initial_state(self, halo=0):
         """FP64 initial conserved state [nvar][...] from the script's initialisation kernel."""
@@ -998,7 +1018,11 @@ class GB300Writer:
         from . import monitor as mon
         s = self.solver(device)
         coords = {}
-        if self.plan.ndim == 2:
+        if self.plan.ndim == 1:
+            f = self.initial_fields(halo=4)
+            s.set_state64_padded(np.stack([f[v] for v in self.state_names()]), 4)
+            coords = {k: f[k][4:-4] for k in ("x0",) if k in f}
+        elif self.plan.ndim == 2:
             f = self.initial_fields(halo=4)
             if self.plan.x1_grid != "uniform":
                 s.set_coordinate(f["x1"], 4)

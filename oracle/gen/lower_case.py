@@ -68,7 +68,10 @@ def lower(case, ref, out, n=None, params=None):
     w.substitute_simulation_parameters(consts, vals)
     with open(os.path.join(out, "plan.json"), "w") as f:
         f.write(w.plan.to_json())
-    if w.plan.ndim == 2:
+    if w.plan.ndim == 1:
+        f = w.initial_fields(halo=4)
+        np.save(os.path.join(out, "ic.npy"), np.stack([f[v] for v in w.state_names()]))
+    elif w.plan.ndim == 2:
         f = w.initial_fields(halo=4)
         np.save(os.path.join(out, "ic.npy"), np.stack([f[v] for v in w.state_names()]))
         np.save(os.path.join(out, "x1.npy"), f["x1"])

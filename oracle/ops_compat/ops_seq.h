@@ -82,6 +82,8 @@ typedef struct ops_halo_group_core { int n; ops_halo *h; } *ops_halo_group;
 static int osb_xdim[128], osb_ydim[128];
 #if defined(OPS_3D)
 #define OSB_ACC(n, x, y, z) ((x) + osb_xdim[n] * (y) + osb_xdim[n] * osb_ydim[n] * (z))
+#elif defined(OPS_1D)
+#define OSB_ACC(n, x) (x)
 #else
 #define OSB_ACC(n, x, y) ((x) + osb_xdim[n] * (y))
 #endif

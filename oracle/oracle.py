@@ -48,7 +48,7 @@ FILTER = {"none": 0, "weno5_constant": 1}
 
 
 def build(force=False):
-    srcs = [os.path.join(HERE, "src", f) for f in ("osb_oracle.c", "osb_oracle2d.c", "osb_oracle3w.c")]
+    srcs = [os.path.join(HERE, "src", f) for f in ("osb_oracle.c", "osb_oracle1d.c", "osb_oracle2d.c", "osb_oracle3w.c")]
     deps = srcs + [os.path.join(HERE, "src", "osb_oracle.h")]
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(f) for f in deps):
         return LIB
@@ -251,6 +251,58 @@ def metrics2d(plan):
     S = np.zeros_like(D)
     assert lib().osbo2d_metrics(ctypes.byref(c), _ptr(D), _ptr(S)) == 0
     return D, S
+
+
+class Cfg1D(ctypes.Structure):
+    _fields_ = [
+        ("n0", ctypes.c_int),
+        ("delta0", ctypes.c_double),
+        ("gama", ctypes.c_double),
+        ("conv", ctypes.c_int),
+        ("teno_eps", ctypes.c_double),
+        ("teno_ct", ctypes.c_double),
+        ("simple_avg", ctypes.c_int),
+        ("rkA", ctypes.c_double * 3),
+        ("rkB", ctypes.c_double * 3),
+        ("dt", ctypes.c_double),
+        ("bc1", ctypes.c_int),
+        ("face", (ctypes.c_double * 3) * 2),
+    ]
+
+
+def make_cfg1d(plan):
+    """Oracle configuration from a 1D Plan (osb_oracle1d.c)."""
+    c = Cfg1D()
+    c.n0, c.delta0, c.gama = plan.n[0], plan.delta[0], plan.gama
+    c.conv = CONV[plan.conv]
+    c.teno_eps, c.teno_ct = plan.teno_eps, plan.teno_ct
+    c.simple_avg = 1 if plan.averaging == "simple" else 0
+    for s in range(3):
+        c.rkA[s] = plan.rk_a[s]
+        c.rkB[s] = plan.rk_b[s]
+    c.dt = plan.dt
+    c.bc1 = 1 if plan.bc[0][1] == "extrapolation" else 0
+    for side, st in enumerate(plan.dirichlet_x0 or ()):
+        for v in range(3):
+            c.face[side][v] = st[v]
+    return c
+
+
+def run1d(plan, q0_padded, nsteps):
+    """q0_padded: FP64 [3][n0+8] with a 4-point halo.  Returns the state after nsteps."""
+    c = make_cfg1d(plan)
+    q = np.ascontiguousarray(q0_padded, dtype=np.float64).copy()
+    assert q.shape == (3, plan.n[0] + 8)
+    assert lib().osbo1d_run(ctypes.byref(c), _ptr(q), int(nsteps)) == 0
+    return q
+
+
+def residual1d(plan, q0_padded):
+    c = make_cfg1d(plan)
+    q = np.ascontiguousarray(q0_padded, dtype=np.float64)
+    r = np.zeros((3, plan.n[0]))
+    assert lib().osbo1d_residual(ctypes.byref(c), _ptr(q), _ptr(r)) == 0
+    return r
 
 
 class Cfg3W(ctypes.Structure):

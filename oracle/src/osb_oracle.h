@@ -93,6 +93,22 @@ typedef struct {
 int osbo2d_run(const osbo2d_cfg *cfg, double *q, int nsteps);
 /* The right-hand side of q (boundary conditions applied first) on the interior, [4][n1][n0]. */
 int osbo2d_residual(const osbo2d_cfg *cfg, const double *q, double *r);
+/* ---- 1D Euler blocks (apps/Sod_shock_tube, apps/shu_osher) ---- */
+typedef struct {
+  int n0;
+  double delta0, gama;
+  int conv;          /* OSBO_CONV_TENO5 (0), OSBO_CONV_WENO5JS, OSBO_CONV_WENO5Z, OSBO_CONV_TENO6 */
+  double teno_eps, teno_ct;
+  int simple_avg;    /* 1: SimpleAverage, 0: RoeAverage */
+  double rkA[3], rkB[3];
+  double dt;
+  int bc1;           /* side 1: 0 Dirichlet (face[1]), 1 extrapolation; side 0 is Dirichlet (face[0]) */
+  double face[2][3]; /* rho, rhou0, rhoE */
+} osbo1d_cfg;
+/* Advance q [3][n0+8] (4-point halo) by nsteps LS-RK3 steps, in place. */
+int osbo1d_run(const osbo1d_cfg *cfg, double *q, int nsteps);
+/* The right-hand side [3][n0] of q (boundary conditions applied first). */
+int osbo1d_residual(const osbo1d_cfg *cfg, const double *q, double *r);
 /* ---- 3D span-periodic wall-bounded path: the 2D configuration above with a periodic x2 axis ---- */
 typedef struct {
   int n[3];          /* interior points in x0, x1, x2 */

@@ -64,6 +64,13 @@ CASES_2D = {
 }
 VARS_2D = ["rho", "rhou0", "rhou1", "rhoE"]
 
+# 1D Euler case: n0, steps, overrides; the fixture keeps the initial and final states with a 4-point halo
+CASES_1D = {
+    "sod": (200, 200, {"dt": 2e-4}),
+    "shu_osher": (400, 200, {"dt": 2e-3}),
+}
+VARS_1D = ["rho", "rhou0", "rhoE"]
+
 # span-periodic 3D wall-bounded case: grid (n0, n1, n2), steps, overrides.  The fixture keeps the
 # reference's initial and final states with a 4-point halo and the x1 coordinate line (x1 depends on
 # j alone) with a 4-point halo.
@@ -114,6 +121,38 @@ def main2d(ref, only=None):
         print("wrote", case, fin["rho"].shape)
 
 
+def main1d(ref, only=None):
+    import tempfile
+    for case, (n0, steps, extra) in CASES_1D.items():
+        if only is not None and case != only:
+            continue
+        if not refrun.available(case):
+            subprocess.check_call([sys.executable, os.path.join(REPO, "oracle", "gen", "generate.py"), "--case", case,
+                                   "--ref", ref])
+        base = dict(block0np0=n0)
+        base.update(extra)
+        d0 = tempfile.mkdtemp(prefix="osb_g0_")
+        refrun.run(case, dict(base, niter=0), VARS_1D, threads=2, outdir=d0)
+        ic = {v: refrun.load_dump(os.path.join(d0, "opensbli_output.%s_B0.bin" % v), interior=False).reshape(-1)[1:-1]
+              for v in VARS_1D}
+        d1 = tempfile.mkdtemp(prefix="osb_g1_")
+        refrun.run(case, dict(base, niter=steps), VARS_1D, threads=2, outdir=d1)
+        fin = {v: refrun.load_dump(os.path.join(d1, "opensbli_output.%s_B0.bin" % v), interior=False).reshape(-1)[1:-1]
+               for v in VARS_1D}
+        np.savez_compressed(os.path.join(HERE, "ref_%s.npz" % case), q0=np.stack([ic[v] for v in VARS_1D]),
+                            q=np.stack([fin[v] for v in VARS_1D]), n=np.array([n0]), steps=steps,
+                            params=json.dumps(dict(base, niter=steps)))
+        out = os.path.join("/tmp", "osb_lower_%s" % case)
+        r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case,
+                            "--out", out, "--ref", ref], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
+        if r.returncode == 0:
+            with open(os.path.join(out, "plan.json")) as f:
+                plan = json.load(f)
+            with open(os.path.join(HERE, "plan_%s.json" % case), "w") as f:
+                json.dump(plan, f, indent=1)
+        print("wrote", case, fin["rho"].shape, "plan" if r.returncode == 0 else "(no plan: lowering failed)")
+
+
 def main3w(ref, only=None):
     import tempfile
     for case, ((n0, n1, n2), steps, extra) in CASES_3W.items():
@@ -150,6 +189,7 @@ def main(ref=None, only=None):
     """Regenerate every fixture, or only the case `only`."""
     ref = ref or default_ref()
     if only is None:
+        main1d(ref)
         main2d(ref)
         main3w(ref)
         katzer_profile(ref)
@@ -158,6 +198,9 @@ def main(ref=None, only=None):
         return
     elif only in CASES_3W:
         main3w(ref, only)
+        return
+    elif only in CASES_1D:
+        main1d(ref, only)
         return
     for case, (n, steps, extra) in CASES.items():
         if only is not None and case != only:

@@ -263,3 +263,21 @@ def test_oracle_shock_reflection_matches_reference_golden():
     assert max(err(O.run2d(plan, d["q0"], int(d["steps"])))) < 1e-7
     assert min(err(O.run2d(plan.replace(averaging="roe"), d["q0"], int(d["steps"])))) > 1e-6
     assert max(float(np.abs(ref[v] - d["q0"][inner][v]).max() / np.abs(ref[v]).max()) for v in range(4)) > 0.1
+
+
+@pytest.mark.parametrize("case,tol", [("sod", 1e-13), ("shu_osher", 1e-7)])
+def test_oracle_euler1d_matches_reference_golden(case, tol):
+    """osb_oracle1d.c (the reference's 1D eigensystem) against the generated code of
+    apps/Sod_shock_tube (TENO5, 200 points, 200 steps) and apps/shu_osher (WENO5-Z, 400 points, 200
+    steps at dt = 2e-3; WENO-Z's rounding floor, 3.7e-9).  The simple average is 3e-4 .. 4e-3 away, so
+    the fixtures pin the Roe average."""
+    import json
+    from opensbli_gb300.plan import sod_plan, shu_osher_plan
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_%s.npz" % case))
+    params = json.loads(str(d["params"]))
+    plan = {"sod": sod_plan, "shu_osher": shu_osher_plan}[case](int(d["n"][0]), dt=params["dt"])
+    inner = (slice(None), slice(4, -4))
+    ref = d["q"][inner]
+    err = lambda q: [float(np.abs(q[inner][v] - ref[v]).max() / np.abs(ref[v]).max()) for v in range(3)]
+    assert max(err(O.run1d(plan, d["q0"], int(d["steps"])))) < tol
+    assert min(err(O.run1d(plan.replace(averaging="simple"), d["q0"], int(d["steps"])))) > 1e-4

@@ -122,6 +122,18 @@ def test_shock_reflection_script_lowers_to_its_plan():
     assert g.dirichlet_x_switch == math.nextafter(40.0, 0.0)
 
 
+@pytest.mark.parametrize("case", ["sod", "shu_osher"])
+def test_euler1d_scripts_lower_to_their_plans(case):
+    """The Sod shock tube (TENO5) and the Shu-Osher problem (WENO5-Z) lower to 1D Euler blocks with
+    Roe averaging and Dirichlet faces whose states the writer evaluates from the face kernels (the
+    Shu-Osher outlet kernel reads its u0 before setting it: 0, as the generated code's locals start)."""
+    from opensbli_gb300.plan import sod_plan, shu_osher_plan
+    g = golden_plan(case)
+    p = {"sod": sod_plan, "shu_osher": shu_osher_plan}[case](g.n[0])
+    assert g.replace(kernels=[], name="", niter=None) == p.replace(kernels=[], name="")
+    assert g.ndim == 1 and g.visc == "none" and g.averaging == "roe"
+
+
 def test_channel_script_lowers_to_its_plan():
     """The channel script (compressible_TCF_TENO, statistics off) lowers with periodic x0, isothermal
     walls on both x1 faces, the power-law viscosity and the constant forcing, to channel_plan's plan."""
@@ -185,7 +197,7 @@ def test_writer_refuses_kernels_outside_the_lowered_families():
     from opensbli_gb300.writer import GB300Writer
     for case in ("tgv_central", "tgv_weno", "tgsym_central", "katzer_teno", "katzer_adaptive", "katzer_carpenter",
                  "tgv_filter", "tgv_teno_adaptive", "sbli3d_teno", "transitional_sbli", "channel_teno",
-                 "shock_reflection"):
+                 "shock_reflection", "sod", "shu_osher"):
         GB300Writer._check_kernel_families(golden_plan(case).kernels)
     assert "User kernel: Non-linear filter application" in golden_plan("tgv_filter").kernels
     names = golden_plan("tgv_filter").kernels + ["User kernel: Shock sensor"]
@@ -213,7 +225,8 @@ def test_cfl_dt_tgv_weno():
 @pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central",
                                   "katzer_teno", "katzer_adaptive", "katzer_carpenter", "tgv_filter",
                                   "katzer_weno", "katzer_wenoz", "katzer_teno6", "tgv_teno_adaptive",
-                                  "sbli3d_teno", "transitional_sbli", "channel_teno", "shock_reflection"])
+                                  "sbli3d_teno", "transitional_sbli", "channel_teno", "shock_reflection", "sod",
+                                  "shu_osher"])
 def test_writer_lowers_reference_script(case, tmp_path):
     r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case, "--out",
                         str(tmp_path), "--ref", REF], capture_output=True, text=True, timeout=900)
@@ -227,12 +240,15 @@ def test_writer_lowers_reference_script(case, tmp_path):
     io = json.load(open(tmp_path / "io.json"))
     writes = [r for r in io if r["kind"] == "write"]
     assert len(writes) == 1 and writes[0]["at_end"]
-    conserved = ["rho_B0", "rhou0_B0", "rhou1_B0"] + (["rhou2_B0"] if p.ndim == 3 else []) + ["rhoE_B0"]
+    conserved = ["rho_B0", "rhou0_B0"] + (["rhou1_B0"] if p.ndim >= 2 else []) + \
+        (["rhou2_B0"] if p.ndim == 3 else []) + ["rhoE_B0"]
     assert writes[0]["arrays"][:len(conserved)] == conserved
     if case == "katzer_adaptive":
         assert writes[0]["arrays"][len(conserved):] == ["x0_B0", "x1_B0", "D11_B0", "TENO_B0"]
     ic = np.load(tmp_path / "ic.npy")
-    if p.ndim == 2:
+    if p.ndim == 1:
+        assert ic.shape == (3, p.n[0] + 8)
+    elif p.ndim == 2:
         assert ic.shape == (4, p.n[1] + 8, p.n[0] + 8)  # 4-point halo: the initialisation kernel fills halos
     else:
         assert ic.shape == (5,) + tuple(reversed(p.n))
