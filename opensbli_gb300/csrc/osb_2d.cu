@@ -245,6 +245,34 @@ __device__ __forceinline__ void bc2_col(const Grid &g, const Q4 &q, const BC2Arg
   }
 }
 
+// The periodic exchange of axis d of a doubly periodic 2D block (exchange.py:9-57): the hx (hy) halo
+// points of every padded row (column) take the interior points one period away.
+__global__ void k2_wrap(Grid g, Q4 q, int d, int hx, int hy) {
+  const int h = d == 0 ? hx : hy, len = d == 0 ? g.n1 + 2 * hy : g.n0 + 2 * hx, n = d == 0 ? g.n0 : g.n1;
+  const int64_t N = (int64_t)4 * len * h;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int v = (int)(t / ((int64_t)len * h)), r = (int)(t % ((int64_t)len * h));
+    const int a = r / h - (d == 0 ? hy : hx), k = r % h + 1;  // the row (column) and the halo depth
+    double *f = q.v[v];
+    if (d == 0) {
+      f[g2(g, -k, a)] = f[g2(g, n - k, a)];
+      f[g2(g, n - 1 + k, a)] = f[g2(g, k - 1, a)];
+    } else {
+      f[g2(g, a, -k)] = f[g2(g, a, n - k)];
+      f[g2(g, a, n - 1 + k)] = f[g2(g, a, k - 1)];
+    }
+  }
+}
+
+// "Save equations" of the two-register RK3: qold (the context's RK register) = q on the interior
+__global__ void k2_save(Grid g, Q4 q, Q4 qold, int nv) {
+  const int64_t N = (int64_t)g.n0 * g.n1;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = g2(g, (int)(t % g.n0), (int)(t / g.n0));
+    for (int v = 0; v < nv; ++v) qold.v[v][c] = q.v[v][c];
+  }
+}
+
 constexpr int BC2_THREADS = 128;
 __global__ void __launch_bounds__(BC2_THREADS) k2_bc(Grid g, Q4 q, BC2Args a, int row_blocks) {
   const int tid = threadIdx.x;
@@ -905,7 +933,7 @@ __global__ void __launch_bounds__(V2X * V2Y, 2) k2_visc(Grid g, Prims<const T> p
 // du = dt R + A du, q += B du in FP64 (update = 1), or R itself into du (update = 0: osb_residual).
 template <typename T>
 __global__ void k2_rk(Grid g, Q4T<const T> rx, Q4T<const T> ry, Q3T<const T> rv, Q4 du, Q4 q64, double dt, double A,
-                      double B, int update) {
+                      double B, int update, int rk2) {
   const int64_t N = (int64_t)g.n0 * g.n1;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(t % g.n0), j = (int)(t / g.n0);
@@ -918,7 +946,14 @@ __global__ void k2_rk(Grid g, Q4T<const T> rx, Q4T<const T> ry, Q3T<const T> rv,
       R[2] += rv.v[1][c];
       R[3] += rv.v[2][c];
     }
-    if (update) {
+    if (update && rk2) {  // RungeKutta(3), two registers (rk_sbli.py:117-124): du holds qold
+#pragma unroll
+      for (int v = 0; v < 4; ++v) {
+        const double r = to_f64(R[v]), old = du.v[v][c];
+        q64.v[v][c] = dt * B * r + old;
+        du.v[v][c] = dt * A * r + old;
+      }
+    } else if (update) {
 #pragma unroll
       for (int v = 0; v < 4; ++v) {
         const double d = dt * to_f64(R[v]) + A * du.v[v][c];
@@ -1007,8 +1042,25 @@ void launch2_metrics(const Ctx &c, const double *x1, cudaStream_t s, int64_t *la
   *launches += 4;
 }
 
+void launch2_save(const Ctx &c, cudaStream_t s, int64_t *launches) {
+  int nb = (int)(((int64_t)c.g.n0 * c.g.n1 + 255) / 256);
+  if (nb > c.num_sms * 4) nb = c.num_sms * 4;
+  k2_save<<<nb, 256, 0, s>>>(c.g, q4(c.q64_2d), q4(c.du2), 4);
+  ++*launches;
+}
+
 void launch2_bcs(const Ctx &c, cudaStream_t s, int64_t *launches) {
   const osb_plan_desc &p = c.plan;
+  if (p.bc[0][0] == OSB_BC_PERIODIC) {  // a doubly periodic block: x0, then x1 (corners from the x0 images)
+    for (int d = 0; d < 2; ++d) {
+      const int64_t N = (int64_t)4 * (d == 0 ? c.g.n1 + 2 * c.hy2 : c.g.n0 + 2 * c.hx2) * (d == 0 ? c.hx2 : c.hy2);
+      int nb = (int)((N + 255) / 256);
+      if (nb > c.num_sms * 4) nb = c.num_sms * 4;
+      k2_wrap<<<nb, 256, 0, s>>>(c.g, q4(c.q64_2d), d, c.hx2, c.hy2);
+    }
+    *launches += 2;
+    return;
+  }
   BC2Args a;
   a.gama = p.gama;
   a.Minf = p.Minf;
@@ -1129,7 +1181,7 @@ template <typename T> void launch2_rhs(const Ctx &c, int update, double A, doubl
   int nb = (int)(((int64_t)c.g.n0 * c.g.n1 + 255) / 256);
   if (nb > c.num_sms * 4) nb = c.num_sms * 4;
   k2_rk<T><<<nb, 256, 0, s>>>(c.g, q4t<const T>(c.res), q4t<const T>(c.resy), rvc, q4(c.du2), q4(c.q64_2d), dt, A, B,
-                              update);
+                              update, p.rk == OSB_RK3_2REG);
   *launches += visc ? 5 : 4;
 }
 

@@ -102,12 +102,15 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
       // Euler block (inviscid_shock_reflection.py): Cartesian, Dirichlet/inlet and Dirichlet/extrapolation
       // x0 faces, a symmetry face at x1 = 0, a Dirichlet or symmetry face at the top
       const int *b0 = p->bc[0], *b1 = p->bc[1];
-      const bool ok = (b0[0] == OSB_BC_INLET_PRESSURE_EXTRAPOLATE || b0[0] == OSB_BC_DIRICHLET) &&
-                      (b0[1] == OSB_BC_EXTRAPOLATION || b0[1] == OSB_BC_DIRICHLET) && b1[0] == OSB_BC_SYMMETRY &&
-                      (b1[1] == OSB_BC_DIRICHLET || b1[1] == OSB_BC_SYMMETRY);
+      const bool periodic = b0[0] == OSB_BC_PERIODIC && b0[1] == OSB_BC_PERIODIC && b1[0] == OSB_BC_PERIODIC &&
+                            b1[1] == OSB_BC_PERIODIC;  // euler_wave.py
+      const bool ok = periodic ||
+                      ((b0[0] == OSB_BC_INLET_PRESSURE_EXTRAPOLATE || b0[0] == OSB_BC_DIRICHLET) &&
+                       (b0[1] == OSB_BC_EXTRAPOLATION || b0[1] == OSB_BC_DIRICHLET) && b1[0] == OSB_BC_SYMMETRY &&
+                       (b1[1] == OSB_BC_DIRICHLET || b1[1] == OSB_BC_SYMMETRY));
       if (!ok) {
-        snprintf(why, n, "2D Euler blocks: inlet or Dirichlet / extrapolation or Dirichlet (x0), symmetry / Dirichlet or "
-                         "symmetry (x1)");
+        snprintf(why, n, "2D Euler blocks: periodic on both axes, or inlet or Dirichlet / extrapolation or Dirichlet "
+                         "(x0), symmetry / Dirichlet or symmetry (x1)");
         return OSB_EUNSUPPORTED;
       }
       if (p->cartesian != 1) { snprintf(why, n, "2D Euler blocks: Cartesian (cartesian = 1)"); return OSB_EUNSUPPORTED; }
@@ -148,7 +151,10 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
       snprintf(why, n, "2D blocks: Sutherland viscosity or none");
       return OSB_EUNSUPPORTED;
     }
-    if (p->rk != OSB_RK3_LS) { snprintf(why, n, "2D blocks: low-storage RK3"); return OSB_EUNSUPPORTED; }
+    if (p->rk != OSB_RK3_LS && !(p->rk == OSB_RK3_2REG && p->visc == OSB_VISC_NONE)) {
+      snprintf(why, n, "2D blocks: low-storage RK3 (2D Euler blocks also the two-register RK3)");
+      return OSB_EUNSUPPORTED;
+    }
     if (p->precision != OSB_PREC_FP64 && p->precision != OSB_PREC_MIXED) { snprintf(why, n, "precision %d", p->precision); return OSB_EINVAL; }
     if (!(p->gama > 1.0) || !(p->Minf > 0) || !(p->Re > 0) || !(p->Pr > 0) || !(p->Twall > 0) || !(p->RefT > 0)) {
       snprintf(why, n, "bad physical constants");
@@ -664,6 +670,7 @@ template <typename T> void one_step2(osb_ctx *c, double dt, cudaStream_t s) {
     ProfScope ps(c, PF_HALO, s);
     launch2_bcs(*c, s, &c->launches);
   }
+  if (c->plan.rk == OSB_RK3_2REG) launch2_save(*c, s, &c->launches);  // qold = q
   for (int st = 0; st < 3; ++st) {
     {
       ProfScope ps(c, PF_CENTRAL_RK, s);

@@ -125,6 +125,7 @@ void launch2_metrics(const Ctx &c, const double *x1, cudaStream_t s, int64_t *la
 void launch1_bcs(const Ctx &c, cudaStream_t s, int64_t *launches);
 void launch1_rhs(const Ctx &c, int update, double A, double B, double dt, cudaStream_t s, int64_t *launches);
 void launch2_bcs(const Ctx &c, cudaStream_t s, int64_t *launches);
+void launch2_save(const Ctx &c, cudaStream_t s, int64_t *launches);
 void launch2_to_state(const Ctx &c, cudaStream_t s, int64_t *launches);
 template <typename T> void launch2_cutoff(const Ctx &c, double *out, cudaStream_t s, int64_t *launches);
 template <typename T>

@@ -272,6 +272,17 @@ def shock_reflection_plan(n0=457, n1=255, precision="fp64", dt=0.1, use_graphs=T
                 dirichlet_x_switch=math.nextafter(40.0, 0.0), name="shock_reflection_%s_%dx%d" % (conv, n0, n1))
 
 
+def euler_wave_plan(n0=400, n1=400, precision="fp64", dt=1e-3, use_graphs=True, conv="weno5z", averaging="simple"):
+    """The 2D Euler density wave of apps/euler_wave/euler_wave.py: gama = 1.4 on the doubly periodic
+    [0, 2)^2 (delta = 2/n), LLFWeno(5, 'Z') with SimpleAverage, RungeKutta(3) (two registers); the
+    initial state rho = 1 + 0.2 sin(pi (x0 + x1)), u = (1, -0.5), p = 1 is advected unchanged by the
+    Euler equations.  400 x 400 and dt = 1e-3 as the script sets them."""
+    return Plan(ndim=2, n=(n0, n1, 1), delta=(2.0 / n0, 2.0 / n1, 1.0), conv=conv, visc="none", rk="rk3",
+                precision=precision, averaging=averaging, bc=(("periodic", "periodic"),) * 3, gama=1.4,
+                weno_eps=1e-14 if conv == "weno5z" else 1e-6, dt=dt, use_graphs=use_graphs, ic="host",
+                x1_grid="uniform", name="euler_wave_%s_%dx%d" % (conv, n0, n1))
+
+
 def _euler1d_state(g, d, u0, p):
     """rho, rhou0, rhoE as the generated 1D face kernels form them: rhoE = d u0^2 / 2 + p / (gama - 1)."""
     return (d, d * u0, 0.5 * d * u0 ** 2 + p / (g - 1.0))

@@ -526,8 +526,13 @@ class GB300Writer:
         (possibly switched at one x0) or symmetry face at the top.  The faces' states depend on the
         simulation's constants; they are evaluated again by substitute_simulation_parameters."""
         coeff = self._rk_coefficients(["Temporal solution advancement"])
-        if set(coeff) != {"rkA", "rkB"}:
-            raise NotImplementedError("RungeKuttaLS(3) coefficients rkA/rkB expected")
+        if set(coeff) == {"rkA", "rkB"}:
+            rk, rk_a, rk_b = "ls_rk3", coeff["rkA"], coeff["rkB"]
+        else:  # RungeKutta(3) with two registers (euler_wave.py)
+            coeff = self._rk_coefficients(["Sub stage advancement", "Temporal solution advancement"])
+            if set(coeff) != {"rkold", "rknew"} or len(coeff["rkold"]) != 3:
+                raise NotImplementedError("RungeKuttaLS(3) or RungeKutta(3) coefficients expected")
+            rk, rk_a, rk_b = "rk3", coeff["rkold"], coeff["rknew"]
         faces = {
             "InletPressureExtrapolate boundary dir0 side0": ("inlet_pressure_extrapolate", 0, 0),
             "Dirichlet boundary dir0 side0": ("dirichlet", 0, 0),
@@ -545,7 +550,11 @@ class GB300Writer:
                     raise NotImplementedError("two boundary conditions on face dir%d side%d" % (d, side))
                 bcs[d][side] = kind
         other = sorted(n for n in names if "boundary dir" in n and n not in faces)
-        if nd == 1:  # 1D (Sod_shock_tube.py, shu_osher.py): a Dirichlet face at x0 = 0
+        exch = {(c.direction, c.side) for c in self.components if type(c).__name__ == "ExchangeSelf"}
+        if nd == 2 and bcs == [[None, None], [None, None]] and not other and \
+                exch == {(d, side) for d in range(2) for side in ("left", "right")}:
+            bcs = [["periodic", "periodic"], ["periodic", "periodic"]]  # doubly periodic (euler_wave.py)
+        elif nd == 1:  # 1D (Sod_shock_tube.py, shu_osher.py): a Dirichlet face at x0 = 0
             if other or bcs[0][0] != "dirichlet" or bcs[0][1] not in ("dirichlet", "extrapolation"):
                 raise NotImplementedError("1D Euler block boundary conditions: %s" %
                                           (other or sorted(n for n in names if "boundary dir" in n)))
@@ -557,9 +566,9 @@ class GB300Writer:
         self._euler_faces = bcs
         plan = Plan(ndim=nd, n=(64, 32, 1) if nd == 2 else (64, 1, 1), delta=(1.0, 1.0, 1.0), conv=conv,
                     weno_eps=1e-14 if conv == "weno5z" else 1e-6,  # WenoZ.eps / WenoJS.eps (weno.py)
-                    visc="none", rk="ls_rk3", precision=precision, averaging=averaging, x1_grid="uniform",
+                    visc="none", rk=rk, precision=precision, averaging=averaging, x1_grid="uniform",
                     bc=(tuple(bcs[0]), tuple(bcs[1]), ("periodic", "periodic")),
-                    rk_a=coeff["rkA"], rk_b=coeff["rkB"], use_graphs=use_graphs, ic="host",
+                    rk_a=rk_a, rk_b=rk_b, use_graphs=use_graphs, ic="host",
                     name="euler%dd" % nd, kernels=[n for n in names if n])
         return self._euler_states(plan)
 
@@ -579,7 +588,7 @@ class GB300Writer:
                 x0.append(lo)
             else:
                 x0.append((0.0,) * (nd + 2))
-        kw["dirichlet_x0"] = tuple(x0)
+        kw["dirichlet_x0"] = tuple(x0) if "dirichlet" in b[0] else None
         if b[1][1] == "dirichlet":
             lo, hi, xs = self._face_states("Dirichlet boundary dir1 side1", consts)
             kw.update(dirichlet_lo=lo, dirichlet_hi=hi, dirichlet_x_switch=xs)

@@ -45,6 +45,8 @@ CASES = {
     "shock_reflection": "ref:apps/inviscid_shock_reflection/inviscid_shock.py",
     "sod": "ref:apps/Sod_shock_tube/Sod_shock_tube.py",
     "shu_osher": "ref:apps/shu_osher/shu_osher.py",
+    "euler_wave": "ref:apps/euler_wave/euler_wave.py",
+    "kelvin_helmholtz": "ref:apps/kelvin_helmholtz/kelvin_helmholtz.py",
 }
 
 

@@ -163,6 +163,7 @@ class Cfg2D(ctypes.Structure):
         ("face0", (ctypes.c_double * 4) * 2),
         ("top", (ctypes.c_double * 4) * 2),
         ("x_switch", ctypes.c_double),
+        ("rk2reg", ctypes.c_int),
     ]
 
 
@@ -194,7 +195,8 @@ def make_cfg2d(plan):
     # Euler blocks: Cartesian x1, no viscous terms, the faces and states of the plan
     c.euler = 1 if plan.visc == "none" else 0
     c.simple_avg = 1 if plan.averaging == "simple" else 0
-    kinds = {"dirichlet": 1, "symmetry": 2}
+    kinds = {"dirichlet": 1, "symmetry": 2, "periodic": 3}
+    c.rk2reg = 1 if plan.rk == "rk3" else 0
     for d in range(2):
         for side in range(2):
             c.bc[d][side] = kinds.get(plan.bc[d][side], 0) if c.euler else 0

@@ -312,8 +312,29 @@ static void bc_top_states(s2_t *s) {
     }
 }
 
+/* The periodic exchange of axis d (exchange.py:9-57): the halo points take the interior points one
+ * period away, every row (column) of the padded block. */
+static void bc_periodic(s2_t *s, int d) {
+  for (int v = 0; v < 4; ++v)
+    for (int a = -H; a < (d == 0 ? N1 : N0) + H; ++a)
+      for (int t = 1; t <= H; ++t) {
+        if (d == 0) {
+          s->q[v][I2(s, -t, a)] = s->q[v][I2(s, N0 - t, a)];
+          s->q[v][I2(s, N0 - 1 + t, a)] = s->q[v][I2(s, t - 1, a)];
+        } else {
+          s->q[v][I2(s, a, -t)] = s->q[v][I2(s, a, N1 - t)];
+          s->q[v][I2(s, a, N1 - 1 + t)] = s->q[v][I2(s, a, t - 1)];
+        }
+      }
+}
+
 static void apply_bcs(s2_t *s) {
   const int(*b)[2] = s->c.bc;
+  if (b[0][0] == OSBO_BC2_PERIODIC) { /* a doubly periodic Euler block (euler_wave.py) */
+    bc_periodic(s, 0);
+    bc_periodic(s, 1);
+    return;
+  }
   if (b[0][0] == OSBO_BC2_DIRICHLET) bc_dirichlet_x0(s, 0);
   else bc_inlet(s);
   if (b[0][1] == OSBO_BC2_DIRICHLET) bc_dirichlet_x0(s, 1);
@@ -579,18 +600,26 @@ int osbo2d_run(const osbo2d_cfg *cfg, double *q, int nsteps) {
   metrics(&s);
   for (int it = 0; it < nsteps; ++it) {
     apply_bcs(&s);
+    if (cfg->rk2reg) /* "Save equations": qold = q (the RK register du holds qold) */
+      for (int v = 0; v < 4; ++v)
+        for (int j = 0; j < cfg->n[1]; ++j)
+          for (int i = 0; i < cfg->n[0]; ++i) s.du[v][I2(&s, i, j)] = s.q[v][I2(&s, i, j)];
     for (int st = 0; st < 3; ++st) {
       constituent(&s);
       if (cfg->teno_adaptive) sensor(&s);
       residual_teno(&s);
       if (!cfg->euler) residual_viscous(&s);
-      /* RungeKuttaLS (rk_LS.py:155-166): du = A du + dt R; q = q + B du */
       for (int v = 0; v < 4; ++v)
         for (int j = 0; j < cfg->n[1]; ++j)
           for (int i = 0; i < cfg->n[0]; ++i) {
             const size_t c = I2(&s, i, j);
-            s.du[v][c] = cfg->dt * s.res[v][c] + cfg->rkA[st] * s.du[v][c];
-            s.q[v][c] = cfg->rkB[st] * s.du[v][c] + s.q[v][c];
+            if (cfg->rk2reg) { /* rk_sbli.py:117-124: sub stage, then the temporal register */
+              s.q[v][c] = cfg->dt * cfg->rkB[st] * s.res[v][c] + s.du[v][c];
+              s.du[v][c] = cfg->dt * cfg->rkA[st] * s.res[v][c] + s.du[v][c];
+            } else { /* RungeKuttaLS (rk_LS.py:155-166): du = A du + dt R; q = q + B du */
+              s.du[v][c] = cfg->dt * s.res[v][c] + cfg->rkA[st] * s.du[v][c];
+              s.q[v][c] = cfg->rkB[st] * s.du[v][c] + s.q[v][c];
+            }
           }
       apply_bcs(&s);
     }

@@ -61,6 +61,8 @@ CASES_2D = {
     # the inviscid shock reflection (Euler, WENO5-Z with SimpleAverage, Dirichlet inlet, symmetry
     # face, the shock generator's Dirichlet top), dt at CFL ~0.4 so that the shock moves
     "shock_reflection": ((64, 32), 30, {"dt": 1.0}),
+    # the doubly periodic Euler density wave (WENO5-Z, simple average, two-register RK3)
+    "euler_wave": ((32, 24), 40, {"dt": 5e-3}),
 }
 VARS_2D = ["rho", "rhou0", "rhou1", "rhoE"]
 

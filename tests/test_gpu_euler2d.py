@@ -9,6 +9,8 @@ Dirichlet face at the top, a Cartesian grid and no viscous terms.
 * FP64 GPU vs the oracle for WENO5-JS and TENO5 with SimpleAverage and for WENO5-JS with the Roe
   average <= 1e-12 on a wider block; the right-hand side <= 1e-11.
 * Graph replay and eager launches give bitwise equal states; mixed precision within 1e-5 (relative L2).
+* The doubly periodic density wave of apps/euler_wave/euler_wave.py (two-register RungeKutta(3)):
+  FP64 vs its golden fixture and vs the oracle <= 1e-12, graph = eager, mixed within 1e-5.
 """
 import json
 import os
@@ -103,3 +105,35 @@ def test_cartesian_block_takes_no_coordinate():
     with pytest.raises(OSBError, match="Cartesian"):
         s.set_coordinate(np.zeros((40, 72)), 4)
     s.close()
+
+
+# ---- the doubly periodic Euler density wave (apps/euler_wave/euler_wave.py): WENO5-Z, the simple
+# average, RungeKutta(3) with two registers ----
+
+def test_euler_wave_fp64_matches_reference_golden_and_oracle():
+    from opensbli_gb300.plan import euler_wave_plan
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_euler_wave.npz"))
+    n = tuple(int(x) for x in d["n"])
+    params = json.loads(str(d["params"]))
+    plan = euler_wave_plan(*n, dt=params["dt"])
+    q = run_gpu(plan, d["q0"], int(d["steps"]))
+    err = rel_err(q, d["q"][INNER])
+    assert max(err) <= 1e-12, err
+    for conv in ("weno5js", "teno5"):
+        p2 = plan.replace(conv=conv, weno_eps=1e-6)
+        q_or = O.run2d(p2, d["q0"], 20)[INNER]
+        assert max(rel_err(run_gpu(p2, d["q0"], 20), q_or)) <= 1e-12
+
+
+def test_euler_wave_graph_matches_eager_and_mixed_error():
+    from opensbli_gb300.plan import euler_wave_plan
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_euler_wave.npz"))
+    n = tuple(int(x) for x in d["n"])
+    plan = euler_wave_plan(*n, dt=json.loads(str(d["params"]))["dt"])
+    a = run_gpu(plan, d["q0"], 6)
+    b = run_gpu(plan.replace(use_graphs=False), d["q0"], 6)
+    assert np.array_equal(a, b)
+    qm = run_gpu(plan.replace(precision="mixed"), d["q0"], int(d["steps"]))
+    ref = d["q"][INNER]
+    l2 = [float(np.linalg.norm(qm[v] - ref[v]) / np.linalg.norm(ref[v])) for v in range(4)]
+    assert np.isfinite(qm).all() and max(l2) <= 1e-5, l2

@@ -122,6 +122,15 @@ def test_shock_reflection_script_lowers_to_its_plan():
     assert g.dirichlet_x_switch == math.nextafter(40.0, 0.0)
 
 
+def test_euler_wave_script_lowers_to_its_plan():
+    """The doubly periodic Euler wave lowers with its exchanges on both axes and RungeKutta(3)'s two
+    registers (rkold, rknew) to euler_wave_plan's plan."""
+    from opensbli_gb300.plan import euler_wave_plan
+    g = golden_plan("euler_wave")
+    assert g.replace(kernels=[], name="", niter=None) == euler_wave_plan(*g.n[:2]).replace(kernels=[], name="")
+    assert g.rk == "rk3" and g.bc[:2] == (("periodic", "periodic"),) * 2
+
+
 @pytest.mark.parametrize("case", ["sod", "shu_osher"])
 def test_euler1d_scripts_lower_to_their_plans(case):
     """The Sod shock tube (TENO5) and the Shu-Osher problem (WENO5-Z) lower to 1D Euler blocks with
@@ -197,7 +206,7 @@ def test_writer_refuses_kernels_outside_the_lowered_families():
     from opensbli_gb300.writer import GB300Writer
     for case in ("tgv_central", "tgv_weno", "tgsym_central", "katzer_teno", "katzer_adaptive", "katzer_carpenter",
                  "tgv_filter", "tgv_teno_adaptive", "sbli3d_teno", "transitional_sbli", "channel_teno",
-                 "shock_reflection", "sod", "shu_osher"):
+                 "shock_reflection", "sod", "shu_osher", "euler_wave"):
         GB300Writer._check_kernel_families(golden_plan(case).kernels)
     assert "User kernel: Non-linear filter application" in golden_plan("tgv_filter").kernels
     names = golden_plan("tgv_filter").kernels + ["User kernel: Shock sensor"]
@@ -226,7 +235,7 @@ def test_cfl_dt_tgv_weno():
                                   "katzer_teno", "katzer_adaptive", "katzer_carpenter", "tgv_filter",
                                   "katzer_weno", "katzer_wenoz", "katzer_teno6", "tgv_teno_adaptive",
                                   "sbli3d_teno", "transitional_sbli", "channel_teno", "shock_reflection", "sod",
-                                  "shu_osher"])
+                                  "shu_osher", "euler_wave"])
 def test_writer_lowers_reference_script(case, tmp_path):
     r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case, "--out",
                         str(tmp_path), "--ref", REF], capture_output=True, text=True, timeout=900)
