@@ -47,6 +47,7 @@ CASES = {
     "shu_osher": "ref:apps/shu_osher/shu_osher.py",
     "euler_wave": "ref:apps/euler_wave/euler_wave.py",
     "kelvin_helmholtz": "ref:apps/kelvin_helmholtz/kelvin_helmholtz.py",
+    "viscous_shock_tube": "ref:apps/viscous_shock_tube/viscous_shock_tube.py",
 }
 
 
