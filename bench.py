@@ -270,6 +270,38 @@ def workload(name, n=None):
         return Workload(name, plan, 0.04, init, cfg, "katzer_adaptive" if adaptive else "katzer_teno",
                         dict(block0np0=n0, block0np1=n1, dt=0.04),
                         {"mixed": 4 * (2 * 4 + 2 * 8) + 4, "fp64": 4 * (2 * 8 + 2 * 8) + 8})
+    if name == "channel129":
+        from opensbli_gb300.plan import channel_plan, channel_initial_state
+        n = n or 129
+        plan = channel_plan(n, n, n)
+        q, x1 = channel_initial_state(plan, halo=3)
+
+        def init(s):
+            s.set_coordinate(x1, 3)
+            s.set_state64_padded(q, 3)
+        cfg = {"workload": "compressible turbulent channel %d^3 (compressible_TCF_TENO, statistics off): TENO6 "
+                           "(C_T=1e-7), periodic x0/x2, isothermal walls on both x1 faces, x1 tanh-clustered (1.7), "
+                           "mu=T^0.7, forcing c=(-1,0,0), LS-RK3 SSP, Re=190.71, Minf=0.0955, dt=2e-4" % n,
+               "grid": [n, n, n], "dt": plan.dt, "precision": "mixed",
+               "l2": "inputs larger than L2 (state %.0f MB FP32 + %.0f MB FP64 master and register)" %
+                     (5 * n ** 3 * 4 / 1e6, 2 * 5 * n ** 3 * 8 / 1e6)}
+        return Workload(name, plan, plan.dt, init, cfg, "channel_teno", dict(block0np0=n, block0np1=n, block0np2=n,
+                        dt=plan.dt), {"mixed": 5 * (2 * 4 + 2 * 8), "fp64": 5 * (2 * 8 + 2 * 8)})
+    if name == "shock_reflection":
+        from opensbli_gb300.plan import shock_reflection_plan
+        n0, n1 = (n or 457), 255
+        plan = shock_reflection_plan(n0, n1)
+        g = plan.gama
+        free = np.array(plan.dirichlet_x0[0])
+        q = np.ascontiguousarray(np.broadcast_to(free[:, None, None], (4, n1 + 8, n0 + 8)))
+        cfg = {"workload": "2D inviscid shock reflection %dx%d (inviscid_shock.py): Euler, WENO5-Z with the simple "
+                           "average, Dirichlet inlet, extrapolation, symmetry face, shock-generator top face, "
+                           "LS-RK3, Mach 2, gama=%g, dt=0.1" % (n0, n1, g),
+               "grid": [n0, n1], "dt": plan.dt, "precision": "mixed",
+               "l2": "inputs smaller than L2 (%.0f MB state)" % (4 * n0 * n1 * 8 / 1e6)}
+        return Workload(name, plan, plan.dt, lambda s: s.set_state64_padded(q, 4), cfg, "shock_reflection",
+                        dict(block0np0=n0, block0np1=n1, dt=plan.dt),
+                        {"mixed": 4 * (2 * 4 + 2 * 8), "fp64": 4 * (2 * 8 + 2 * 8)})
     raise SystemExit("unknown config %s" % name)
 
 
@@ -613,7 +645,7 @@ def main():
     ap.add_argument("--impl", default="own", choices=["own", "reference"])
     ap.add_argument("--config", default="tgv_weno256",
                     choices=["tgv_weno256", "tgv_central64", "katzer512", "katzer512_adaptive", "tgv_adjoint128",
-                             "tgv_batch96"])
+                             "tgv_batch96", "channel129", "shock_reflection"])
     ap.add_argument("--precision", default=None, choices=["mixed", "fp64"], help="tgv_batch96: precision")
     ap.add_argument("--adj-steps", type=int, default=None, help="tgv_adjoint128: RK3 steps to T=2 (default 800)")
     ap.add_argument("--fd-dirs", type=int, default=16, help="tgv_adjoint128: finite-difference directions")
