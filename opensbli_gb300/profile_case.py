@@ -5,6 +5,7 @@
     python -m opensbli_gb300.profile_case --katzer 512 [--conv teno5|teno6|weno5js|weno5z] [--adaptive]
     python -m opensbli_gb300.profile_case --sbli3d 256 --n2 64 [--conv ...]
     python -m opensbli_gb300.profile_case --channel 129 [--conv ...]
+    python -m opensbli_gb300.profile_case --shock-reflection 457 [--conv ...]
 
 Runs the Taylor-Green vortex (or, with --katzer N0, the 2D shock/boundary-layer block N0 x 256 from
 the boundary-layer profile in tests/golden/katzer_ic_n256.npz, or with --sbli3d N0 the span-periodic
@@ -36,11 +37,24 @@ def main():
     ap.add_argument("--sbli3d", type=int, default=0, help="3D span-periodic block of this many x0 points")
     ap.add_argument("--n2", type=int, default=32, help="--sbli3d: points along the periodic x2 axis")
     ap.add_argument("--channel", type=int, default=0, help="the N^3 channel block (turbulent_channel.py)")
+    ap.add_argument("--shock-reflection", type=int, default=0,
+                    help="the 2D inviscid shock reflection of this many x0 points (inviscid_shock.py)")
     a = ap.parse_args()
     import torch
     from .plan import tgv_plan, tgv_cfl_dt
     from .runtime import Solver
-    if a.channel:
+    if a.shock_reflection:
+        import numpy as np
+        from .plan import shock_reflection_plan
+        a.conv = a.conv or "weno5z"
+        plan = shock_reflection_plan(a.shock_reflection, 255, precision=a.precision, conv=a.conv,
+                                     use_graphs=not a.no_graphs)
+        dt = plan.dt
+        free = np.array(plan.dirichlet_x0[0])  # the free stream everywhere, as the script starts
+        s = Solver(plan)
+        s.set_state64_padded(np.ascontiguousarray(np.broadcast_to(free[:, None, None], (4, 255 + 8, plan.n[0] + 8))), 4)
+        a.n = plan.n[0]
+    elif a.channel:
         from .plan import channel_plan, channel_initial_state
         a.conv = a.conv or "teno6"
         plan = channel_plan(a.channel, a.channel, a.channel, precision=a.precision, conv=a.conv,
