@@ -230,12 +230,20 @@ def test_cfl_dt_tgv_weno():
     assert 1e-3 < dt < 1e-2
 
 
+# Every script the writer lowers; the default CPU run re-lowers one of each block kind (the reference
+# generator takes ~15 s per script), OSB_ALL_SCRIPTS=1 all of them.  The golden plans of the others
+# are still checked against the plan constructors above.
+ALL_SCRIPTS = ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central", "katzer_teno",
+               "katzer_adaptive", "katzer_carpenter", "tgv_filter", "katzer_weno", "katzer_wenoz", "katzer_teno6",
+               "tgv_teno_adaptive", "sbli3d_teno", "transitional_sbli", "channel_teno", "shock_reflection", "sod",
+               "shu_osher", "euler_wave"]
+SCRIPTS = ALL_SCRIPTS if os.environ.get("OSB_ALL_SCRIPTS") == "1" else \
+    ["tgv_weno", "tgv_filter", "katzer_adaptive", "transitional_sbli", "channel_teno", "shock_reflection", "sod",
+     "euler_wave"]
+
+
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
-@pytest.mark.parametrize("case", ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central",
-                                  "katzer_teno", "katzer_adaptive", "katzer_carpenter", "tgv_filter",
-                                  "katzer_weno", "katzer_wenoz", "katzer_teno6", "tgv_teno_adaptive",
-                                  "sbli3d_teno", "transitional_sbli", "channel_teno", "shock_reflection", "sod",
-                                  "shu_osher", "euler_wave"])
+@pytest.mark.parametrize("case", SCRIPTS)
 def test_writer_lowers_reference_script(case, tmp_path):
     r = subprocess.run([sys.executable, os.path.join(REPO, "oracle", "gen", "lower_case.py"), "--case", case, "--out",
                         str(tmp_path), "--ref", REF], capture_output=True, text=True, timeout=900)
