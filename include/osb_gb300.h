@@ -55,12 +55,15 @@ extern "C" {
 #define OSB_BC_EXTRAPOLATION 3             /* extrapolation.py:8-58, order 0 (x0 side 1) */
 #define OSB_BC_ISOTHERMAL_WALL 4           /* isothermal_wall.py:11-88 (x1 side 0; side 1 on channel blocks) */
 #define OSB_BC_DIRICHLET 5                 /* dirichlet.py:6-41 with a state switched at x0 (x1 side 1) */
+#define OSB_BC_ADIABATIC_WALL 6            /* adiabatic_wall.py (2D: x0 faces and x1 side 0) */
 
 /* the average the characteristic system of an interface is built from (2D blocks; 3D blocks: Roe) */
 #define OSB_AVG_ROE 0    /* RoeAverage (schemes/spatial/averaging.py:62-114) */
 #define OSB_AVG_SIMPLE 1 /* SimpleAverage (averaging.py:31-59): arithmetic means of rho, u_i and a */
 /* one-sided closures of the central derivatives at a face of a 2D block (opensblifunctions.py:523-534) */
 #define OSB_CLOSURE_REDUCED_ACCESS 0 /* reduced_access_scheme.py:6-83: first two points, 5-point stencils */
+#define OSB_CLOSURE_NONE 2           /* a symmetry face of a Cartesian viscous block: central stencils
+                                      * over its mirrored halos (2D) */
 #define OSB_CLOSURE_CARPENTER 1      /* Carpenter_scheme.py:6-102 (every face class's default): first
                                       * derivatives at the first four points (6-point stencils), second
                                       * derivatives as ReducedAccess */
@@ -127,7 +130,9 @@ typedef struct osb_plan_desc {
    * the energy equation (the script's constant pressure-gradient forcing; 0: none) */
   double visc_exp;
   double forcing[3];
-  /* 2D Euler blocks (OSB_VISC_NONE; apps/inviscid_shock_reflection/inviscid_shock.py): averaging is
+  /* 2D Cartesian viscous blocks (apps/viscous_shock_tube/viscous_shock_tube.py): OSB_VISC_CONST (mu = 1),
+   * cartesian = 1, adiabatic walls on both x0 faces and x1 side 0, a symmetry face at x1 side 1.
+   * 2D Euler blocks (OSB_VISC_NONE; apps/inviscid_shock_reflection/inviscid_shock.py): averaging is
    * OSB_AVG_*; cartesian = 1 takes x1 uniform (no metric terms; osb_set_coordinate is not called);
    * dirichlet_x0[side] is the constant state (rho, rhou0, rhou1, rhoE) of an OSB_BC_DIRICHLET x0 face.
    * Faces: x0 OSB_BC_INLET_PRESSURE_EXTRAPOLATE or OSB_BC_DIRICHLET (side 0), OSB_BC_EXTRAPOLATION or

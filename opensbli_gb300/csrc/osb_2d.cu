@@ -37,7 +37,8 @@ template <> __device__ __forceinline__ double pow_t<double>(double x, double y) 
 
 // ---- one-sided closures of the central first derivative.  G(o) reads the function at offset o
 // along the axis, k is the point's index, n the axis size, cl the axis's Carpenter faces (bit 0: side
-// 0, bit 1: side 1; the others are ReducedAccess); bit 2 marks a periodic axis (central everywhere).
+// 0, bit 1: side 1; the others are ReducedAccess); bit 2 marks a periodic axis (central everywhere),
+// bits 3 and 4 a side 0 / side 1 without a closure (a symmetry face: central over its mirrored halos).
 //  * ReducedAccess (reduced_access_scheme.py:34-83): the first two points of a face, 5-point stencils;
 //  * Carpenter (Carpenter_scheme.py:61-102): the first four points, weights c_carp[r][m] of f(m) at
 //    point r of a side-0 face, mirrored with the opposite sign on side 1.
@@ -49,7 +50,7 @@ template <> __device__ __forceinline__ double carp_w<double>(int i) { return c_c
 template <> __device__ __forceinline__ float carp_w<float>(int i) { return c_carp_f[i]; }
 
 template <typename T, typename Gf> __device__ __forceinline__ T d1c(const Gf &G, int k, int n, int cl) {
-  const int w0 = (cl & 1) ? 4 : 2, w1 = (cl & 2) ? 4 : 2;
+  const int w0 = (cl & 8) ? 0 : (cl & 1) ? 4 : 2, w1 = (cl & 16) ? 0 : (cl & 2) ? 4 : 2;
   if (!(cl & 4) && (k < w0 || n - 1 - k < w1)) {
     const bool s0 = k < w0;
     if (s0 ? (cl & 1) : (cl & 2)) {
@@ -71,14 +72,14 @@ template <typename T, typename Gf> __device__ __forceinline__ T d1c(const Gf &G,
 // second derivative: the same two-point closure in both schemes (second_der_coefficients); none on a
 // periodic axis (cl bit 2)
 template <typename T, typename Gf> __device__ __forceinline__ T d2c(const Gf &G, int k, int n, int cl = 0) {
-  if (cl & 4) return T(-1.0 / 12.0) * G(-2) + T(4.0 / 3.0) * G(-1) - T(2.5) * G(0) + T(4.0 / 3.0) * G(1) - T(1.0 / 12.0) * G(2);
-  if (k == 0)
+  const bool s0 = !(cl & 12), s1 = !(cl & 20);  // side 0 / side 1 closed
+  if (k == 0 && s0)
     return T(35.0 / 12.0) * G(0) - T(26.0 / 3.0) * G(1) + T(9.5) * G(2) - T(14.0 / 3.0) * G(3) + T(11.0 / 12.0) * G(4);
-  if (k == 1)
+  if (k == 1 && s0)
     return T(11.0 / 12.0) * G(-1) - T(5.0 / 3.0) * G(0) + T(0.5) * G(1) + T(1.0 / 3.0) * G(2) - T(1.0 / 12.0) * G(3);
-  if (k == n - 1)
+  if (k == n - 1 && s1)
     return T(35.0 / 12.0) * G(0) - T(26.0 / 3.0) * G(-1) + T(9.5) * G(-2) - T(14.0 / 3.0) * G(-3) + T(11.0 / 12.0) * G(-4);
-  if (k == n - 2)
+  if (k == n - 2 && s1)
     return T(11.0 / 12.0) * G(1) - T(5.0 / 3.0) * G(0) + T(0.5) * G(-1) + T(1.0 / 3.0) * G(-2) - T(1.0 / 12.0) * G(-3);
   return T(-1.0 / 12.0) * G(-2) + T(4.0 / 3.0) * G(-1) - T(2.5) * G(0) + T(4.0 / 3.0) * G(1) - T(1.0 / 12.0) * G(2);
 }
@@ -147,7 +148,8 @@ struct Dir2 {
 // 0..3); the generated order (inlet, outlet, wall, top) only matters where these meet: the wall reads
 // the x-halo columns the inlet and outlet wrote, the outlet must read column n0-2 before the wall
 // writes it, and at the corners the later face wins.  So block 0 applies the x faces of the rows
-// -3..3 and n1-1..n1+hy, then (after a barrier) the y faces of the columns -3..0 and n0-2..n0+hx;
+// -3..3 and n1-5..n1+hy (a symmetry top face reads rows n1-5..n1-2), then (after a barrier) the y
+// faces of the columns -3..0 and n0-2..n0+hx;
 // the other blocks apply the x faces of the rows between and the y faces of the columns between,
 // which no other work item touches.  Each y-face column is three work items, one per wall halo
 // point, so the FP64 divisions of a column run in parallel.
@@ -159,11 +161,48 @@ struct BC2Args {
   // and the outlet; symmetry x1 faces instead of the wall (side 0) and the Dirichlet face (side 1)
   int dir0, dir1, sym0, sym1;
   double f0[4], f1[4];
+  // viscous_shock_tube.py: adiabatic walls on the x0 faces and on x1 side 0
+  int adi0, adi1, adiy0;
 };
+
+// AdiabaticWallBC (adiabatic_wall.py, as generated for viscous_shock_tube.py) on one line across a face
+// whose boundary point is b (index along the face normal) and interior lies on the side sg: zero
+// momentum at b, T_w = (18 T_1 - 9 T_2 + 2 T_3)/11 over the first three interior points, rhoE_w =
+// rho_w T_w / (gama Minf^2 (gama-1)); halo t mirrors interior t, rho and rhoE even, momentum odd
+// (t = 1..nt; the other threads of the face write only halo points, which this point never reads).
+template <typename At>
+__device__ __forceinline__ void adia2_line(const Q4 &q, const BC2Args &a, At at, int bnd, int sg, int t0, int t1) {
+  for (int t = t0; t <= t1; ++t) {
+    const int64_t h = at(bnd - sg * t), m = at(bnd + sg * t);
+    q.v[0][h] = q.v[0][m];
+    q.v[1][h] = -q.v[1][m];
+    q.v[2][h] = -q.v[2][m];
+    q.v[3][h] = q.v[3][m];
+  }
+  if (t0 == 1) {
+    const double gm1 = a.gama - 1.0, gM2 = a.gama * a.Minf * a.Minf;
+    double T[4];
+    for (int k = 1; k <= 3; ++k) {
+      const int64_t m = at(bnd + sg * k);
+      const double r = q.v[0][m];
+      T[k] = gM2 * gm1 * (q.v[3][m] - 0.5 * (q.v[1][m] * q.v[1][m] + q.v[2][m] * q.v[2][m]) / r) / r;
+    }
+    const int64_t w = at(bnd);
+    q.v[1][w] = 0.0;
+    q.v[2][w] = 0.0;
+    q.v[3][w] = (18.0 / 11.0 * T[1] - 9.0 / 11.0 * T[2] + 2.0 / 11.0 * T[3]) * q.v[0][w] / (gM2 * gm1);
+  }
+}
 
 // inlet (i = 0 and its halo) and outlet (i >= n0-1) of row j, or the Dirichlet x0 faces
 // (dirichlet.py:6-41: the boundary point and the halo take the face's state)
 __device__ __forceinline__ void bc2_row(const Grid &g, const Q4 &q, const BC2Args &a, int j) {
+  if (a.adi0) {  // both x0 faces adiabatic (the 4-point halo of side 1 as generated)
+    auto at = [&](int i) { return g2(g, i, j); };
+    adia2_line(q, a, at, 0, 1, 1, 3);
+    adia2_line(q, a, at, g.n0 - 1, -1, 1, 4);
+    return;
+  }
   if (a.dir0) {
     for (int i = -3; i <= 0; ++i)
       for (int v = 0; v < 4; ++v) q.v[v][g2(g, i, j)] = a.f0[v];
@@ -205,6 +244,13 @@ __device__ __forceinline__ void sym2_point(const Grid &g, const Q4 &q, int i, in
 // isothermal wall halo point -t of column i (t = 1 also sets the wall point itself and the
 // Dirichlet top face of the column)
 __device__ __forceinline__ void bc2_col(const Grid &g, const Q4 &q, const BC2Args &a, int i, int t) {
+  if (a.adiy0) {  // adiabatic wall at x1 = 0 (halo point t), symmetry face at the top (with t = 1)
+    auto at = [&](int j) { return g2(g, i, j); };
+    adia2_line(q, a, at, 0, 1, t, t);  // t = 1 also sets the wall point
+    if (t == 1)
+      for (int u = 1; u <= a.hy; ++u) sym2_point(g, q, i, g.n1 - 1, -1, u);
+    return;
+  }
   if (a.sym0) {
     sym2_point(g, q, i, 0, 1, t);
     if (t == 1) {
@@ -278,7 +324,7 @@ __global__ void __launch_bounds__(BC2_THREADS) k2_bc(Grid g, Q4 q, BC2Args a, in
   const int tid = threadIdx.x;
   if (blockIdx.x == 0) {
     for (int j = -3 + tid; j < g.n1 + a.hy; j += BC2_THREADS)
-      if (j <= 3 || j >= g.n1 - 1) bc2_row(g, q, a, j);
+      if (j <= 3 || j >= g.n1 - 5) bc2_row(g, q, a, j);
     __syncthreads();
     for (int w = tid; w < 3 * (g.n0 + a.hx + 3); w += BC2_THREADS) {
       const int i = w / 3 - 3;
@@ -286,7 +332,7 @@ __global__ void __launch_bounds__(BC2_THREADS) k2_bc(Grid g, Q4 q, BC2Args a, in
     }
   } else if ((int)blockIdx.x <= row_blocks) {
     const int j = 4 + ((int)blockIdx.x - 1) * BC2_THREADS + tid;
-    if (j < g.n1 - 1) bc2_row(g, q, a, j);
+    if (j < g.n1 - 5) bc2_row(g, q, a, j);
   } else {
     const int w = ((int)blockIdx.x - 1 - row_blocks) * BC2_THREADS + tid;
     const int i = 1 + w / 3;
@@ -349,7 +395,7 @@ __global__ void k2_prims(Grid g, Q4 q64, Q4T<float> qs, Prims<T> pr, double gama
   pr.a[n] = sqrt_t(gm * p * ir);
   const T S = T(suth);
   pr.T_[n] = Tt;
-  pr.mu[n] = (S + T(1)) * Tt * sqrt_t(Tt) / (S + Tt);
+  pr.mu[n] = suth < 0.0 ? T(1) : (S + T(1)) * Tt * sqrt_t(Tt) / (S + Tt);  // suth < 0: constant mu = 1
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -890,8 +936,8 @@ __global__ void __launch_bounds__(V2X * V2Y, 2) k2_visc(Grid g, Prims<const T> p
     gr[k][0] = id0 * d1c<T>(X, i, g.n0, va.clx);
     const T fy = id1 * d1c<T>(Y, j, g.n1, va.cly);
     gr[k][1] = Dm * fy;
-    h[k][0][0] = id0 * id0 * d2c<T>(X, i, g.n0);
-    h[k][1][1] = Dm * Dm * (id1 * id1 * d2c<T>(Y, j, g.n1)) + Dm * S * fy;
+    h[k][0][0] = id0 * id0 * d2c<T>(X, i, g.n0, va.clx);
+    h[k][1][1] = Dm * Dm * (id1 * id1 * d2c<T>(Y, j, g.n1, va.cly)) + Dm * S * fy;
     // d/dx0 of the row j+o, then d/dxi1 of that column (inner axis x0 over the extended x1 range)
     auto inner = [&](int o) {
       return id0 * d1c<T>([&](int p) { return sm[k][lj + o][li + p]; }, i, g.n0, va.clx);
@@ -907,8 +953,8 @@ __global__ void __launch_bounds__(V2X * V2Y, 2) k2_visc(Grid g, Prims<const T> p
   const T Tx = id0 * d1c<T>(XT, i, g.n0, va.clx);
   const T Tyx = id1 * d1c<T>(YT, j, g.n1, va.cly);
   const T Ty = Dm * Tyx;
-  const T Txx = id0 * id0 * d2c<T>(XT, i, g.n0);
-  const T Tyy = Dm * Dm * (id1 * id1 * d2c<T>(YT, j, g.n1)) + Dm * S * Tyx;
+  const T Txx = id0 * id0 * d2c<T>(XT, i, g.n0, va.clx);
+  const T Tyy = Dm * Dm * (id1 * id1 * d2c<T>(YT, j, g.n1, va.cly)) + Dm * S * Tyx;
   const T div = gr[0][0] + gr[1][1];
   const T mug[2] = {mux, muy};
   const T uu[2] = {sm[0][lj][li], sm[1][lj][li]};
@@ -984,7 +1030,8 @@ template <typename T> static Q4T<T> q4t(void *const *a) {
 // the Carpenter faces of one axis as d1c's bit mask
 static int closure_bits(const osb_plan_desc &p, int axis) {
   if (p.bc[axis][0] == OSB_BC_PERIODIC) return 4;
-  return (p.closure[axis][0] == OSB_CLOSURE_CARPENTER ? 1 : 0) | (p.closure[axis][1] == OSB_CLOSURE_CARPENTER ? 2 : 0);
+  return (p.closure[axis][0] == OSB_CLOSURE_CARPENTER ? 1 : 0) | (p.closure[axis][1] == OSB_CLOSURE_CARPENTER ? 2 : 0) |
+         (p.closure[axis][0] == OSB_CLOSURE_NONE ? 8 : 0) | (p.closure[axis][1] == OSB_CLOSURE_NONE ? 16 : 0);
 }
 
 // The Carpenter first-derivative closure (Carpenter_scheme.py:90-102): weights = A^-1 B with the 4x4
@@ -1079,7 +1126,11 @@ void launch2_bcs(const Ctx &c, cudaStream_t s, int64_t *launches) {
   a.dir1 = p.bc[0][1] == OSB_BC_DIRICHLET;
   a.sym0 = p.bc[1][0] == OSB_BC_SYMMETRY;
   a.sym1 = p.bc[1][1] == OSB_BC_SYMMETRY;
-  const int rows = c.g.n1 - 5 > 0 ? c.g.n1 - 5 : 0, cols = c.g.n0 - 3 > 0 ? c.g.n0 - 3 : 0;
+  a.adi0 = p.bc[0][0] == OSB_BC_ADIABATIC_WALL;
+  a.adi1 = p.bc[0][1] == OSB_BC_ADIABATIC_WALL;
+  a.adiy0 = p.bc[1][0] == OSB_BC_ADIABATIC_WALL;
+  // rows 4 .. n1-6 to the other blocks: block 0 takes the rows a top symmetry face reads (n1-5 ..)
+  const int rows = c.g.n1 - 9 > 0 ? c.g.n1 - 9 : 0, cols = c.g.n0 - 3 > 0 ? c.g.n0 - 3 : 0;
   const int row_blocks = (rows + BC2_THREADS - 1) / BC2_THREADS;
   const int col_blocks = (3 * cols + BC2_THREADS - 1) / BC2_THREADS;
   k2_bc<<<1 + row_blocks + col_blocks, BC2_THREADS, 0, s>>>(c.g, q4(c.q64_2d), a, row_blocks);
@@ -1130,7 +1181,8 @@ template <typename T> void launch2_rhs(const Ctx &c, int update, double A, doubl
   Prims<const T> prc{pr.u0, pr.u1, pr.p, pr.a, pr.T_, pr.mu};
   Q4T<const T> q = q4t<const T>(c.qa);
   dim3 b(32, 8), gp((c.g.n0 + 8 + 31) / 32, (c.g.n1 + 8 + 7) / 8);
-  k2_prims<T><<<gp, b, 0, s>>>(c.g, q4(c.q64_2d), q4t<float>(c.qa), pr, p.gama, p.Minf, p.SuthT / p.RefT);
+  k2_prims<T><<<gp, b, 0, s>>>(c.g, q4(c.q64_2d), q4t<float>(c.qa), pr, p.gama, p.Minf,
+                                p.visc == OSB_VISC_CONST ? -1.0 : p.SuthT / p.RefT);
   Q4T<T> r = q4t<T>(c.res);
   const bool teno = p.conv == OSB_CONV_TENO5 || p.conv == OSB_CONV_TENO6;
   const double eps = teno ? p.teno_eps : p.weno_eps;

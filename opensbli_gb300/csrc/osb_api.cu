@@ -120,6 +120,13 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
             snprintf(why, n, "dirichlet_x0 must be finite");
             return OSB_EINVAL;
           }
+    } else if (p->visc == OSB_VISC_CONST) {
+      // Cartesian viscous block (viscous_shock_tube.py): adiabatic walls, a symmetry top face, mu = 1
+      if (p->bc[0][0] != OSB_BC_ADIABATIC_WALL || p->bc[0][1] != OSB_BC_ADIABATIC_WALL ||
+          p->bc[1][0] != OSB_BC_ADIABATIC_WALL || p->bc[1][1] != OSB_BC_SYMMETRY || p->cartesian != 1) {
+        snprintf(why, n, "2D constant-viscosity blocks: Cartesian, adiabatic walls (x0, x1 side 0), symmetry top");
+        return OSB_EUNSUPPORTED;
+      }
     } else if (p->bc[0][0] != OSB_BC_INLET_PRESSURE_EXTRAPOLATE || p->bc[0][1] != OSB_BC_EXTRAPOLATION ||
                p->bc[1][0] != OSB_BC_ISOTHERMAL_WALL || p->bc[1][1] != OSB_BC_DIRICHLET) {
       snprintf(why, n, "2D blocks: boundary conditions must be inlet/extrapolation (x0) and isothermal wall/Dirichlet (x1)");
@@ -141,14 +148,17 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
       }
     }
     for (int d = 0; d < 2; ++d)
-      for (int side = 0; side < 2; ++side)
-        if (p->closure[d][side] != OSB_CLOSURE_REDUCED_ACCESS && p->closure[d][side] != OSB_CLOSURE_CARPENTER) {
-          snprintf(why, n, "closure[%d][%d] = %d: OSB_CLOSURE_REDUCED_ACCESS or OSB_CLOSURE_CARPENTER", d, side,
-                   p->closure[d][side]);
+      for (int side = 0; side < 2; ++side) {
+        const int cl = p->closure[d][side];
+        const bool none_ok = cl == OSB_CLOSURE_NONE && p->bc[d][side] == OSB_BC_SYMMETRY && p->visc == OSB_VISC_CONST;
+        if (cl != OSB_CLOSURE_REDUCED_ACCESS && cl != OSB_CLOSURE_CARPENTER && !none_ok) {
+          snprintf(why, n, "closure[%d][%d] = %d: OSB_CLOSURE_REDUCED_ACCESS or OSB_CLOSURE_CARPENTER (NONE on the "
+                           "symmetry face of a constant-viscosity block)", d, side, cl);
           return OSB_EINVAL;
         }
-    if (p->visc != OSB_VISC_SUTHERLAND && p->visc != OSB_VISC_NONE) {
-      snprintf(why, n, "2D blocks: Sutherland viscosity or none");
+      }
+    if (p->visc != OSB_VISC_SUTHERLAND && p->visc != OSB_VISC_NONE && p->visc != OSB_VISC_CONST) {
+      snprintf(why, n, "2D blocks: Sutherland or constant viscosity, or none");
       return OSB_EUNSUPPORTED;
     }
     if (p->rk != OSB_RK3_LS && !(p->rk == OSB_RK3_2REG && p->visc == OSB_VISC_NONE)) {

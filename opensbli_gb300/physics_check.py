@@ -72,7 +72,8 @@ class PhysicsCheck:
         self.body_force, self.visc_exp, self.forcing = body_force, visc_exp, forcing
         self.rnd = random.Random(2024)
         self.delta = (0.37, 0.53, 0.61)  # test spacings for the 1/delta factors
-        self.consts = {"gama": 1.4, "Minf": 0.7, "Re": 950.0, "Pr": 0.72, "SuthT": 110.4, "RefT": 288.0}
+        # test values; mu is a script's constant viscosity, which the kernels implement as 1
+        self.consts = {"gama": 1.4, "Minf": 0.7, "Re": 950.0, "Pr": 0.72, "SuthT": 110.4, "RefT": 288.0, "mu": 1.0}
 
     # ------------------------------------------------------------------ helpers
     def _fail(self, what):

@@ -283,6 +283,23 @@ def euler_wave_plan(n0=400, n1=400, precision="fp64", dt=1e-3, use_graphs=True, 
                 x1_grid="uniform", name="euler_wave_%s_%dx%d" % (conv, n0, n1))
 
 
+def viscous_shock_tube_plan(n0=500, n1=250, precision="fp64", dt=5e-6, use_graphs=True, conv="teno5"):
+    """The 2D viscous shock tube of apps/viscous_shock_tube/viscous_shock_tube.py: Navier-Stokes with the
+    constant viscosity mu = 1, Re = 200, Pr = 0.73, Minf = 1, gama = 1.4 on [0, 1] x [0, 0.5] (uniform),
+    LLFTeno(5) with RoeAverage (C_T = 1e-6, eps = 1e-15), StoreSome central derivatives, RungeKuttaLS(3),
+    adiabatic walls at x0 = 0, x0 = 1 and x1 = 0 with ReducedAccess closures and a symmetry face at x1 =
+    0.5, whose derivatives stay central over its mirrored halos; 500 x 250 and dt = 5e-6 as the script
+    sets them."""
+    return Plan(ndim=2, n=(n0, n1, 1), delta=(1.0 / (n0 - 1), 0.5 / (n1 - 1), 1.0), conv=conv, visc="const",
+                rk="ls_rk3", precision=precision, bc=(("adiabatic_wall", "adiabatic_wall"),
+                                                      ("adiabatic_wall", "symmetry"), ("periodic", "periodic")),
+                gama=1.4, Minf=1.0, Re=200.0, Pr=0.73, teno_ct=1e-6, teno_eps=1e-15,
+                weno_eps=1e-14 if conv == "weno5z" else 1e-6, rk_a=(0.0, -5.0 / 9.0, -153.0 / 128.0),
+                rk_b=(1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0), dt=dt, use_graphs=use_graphs, ic="host", x1_grid="uniform",
+                closure=(("reduced_access", "reduced_access"), ("reduced_access", "none")),
+                name="viscous_shock_tube_%dx%d" % (n0, n1))
+
+
 def _euler1d_state(g, d, u0, p):
     """rho, rhou0, rhoE as the generated 1D face kernels form them: rhoE = d u0^2 / 2 + p / (gama - 1)."""
     return (d, d * u0, 0.5 * d * u0 ** 2 + p / (g - 1.0))

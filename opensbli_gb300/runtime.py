@@ -28,9 +28,9 @@ VISC = {"none": 0, "const": 1, "sutherland": 2, "power": 3}
 AVG = {"roe": 0, "simple": 1}
 RK = {"rk3": 0, "ls_rk3": 1}
 BC = {"periodic": 0, "symmetry": 1, "inlet_pressure_extrapolate": 2, "extrapolation": 3, "isothermal_wall": 4,
-      "dirichlet": 5}
+      "dirichlet": 5, "adiabatic_wall": 6}
 PREC = {"fp64": 0, "mixed": 1}
-CLOSURE = {"reduced_access": 0, "carpenter": 1}
+CLOSURE = {"reduced_access": 0, "carpenter": 1, "none": 2}
 FILTER = {"none": 0, "weno5_constant": 1}
 RED = {"ke": 0, "enstrophy": 1, "nancheck": 2}
 

@@ -321,6 +321,8 @@ class GB300Writer:
             return self._lower_euler2d(precision, use_graphs, conv, averaging, names)
         if nd == 1:
             raise NotImplementedError("1D blocks: the Euler equations")
+        if nd == 2 and not self._kernels("MetricsEquation") and not self._kernels("Metric boundary"):
+            return self._lower_viscous2d_cartesian(precision, use_graphs, conv, averaging, names)
         if not self._kernels("MetricsEquation") or not self._kernels("Metric boundary"):
             raise NotImplementedError("2D blocks: metric terms expected")
         if not any(n.startswith("CRmu") for n in names):
@@ -519,6 +521,33 @@ class GB300Writer:
         # the kernels compare x0 > xs: a switch that includes c itself moves xs just below it
         return lo, hi, (c if mid == lo else math.nextafter(c, -math.inf))
 
+    def _lower_viscous2d_cartesian(self, precision, use_graphs, conv, averaging, names):
+        """A Cartesian 2D Navier-Stokes block with a constant viscosity (apps/viscous_shock_tube/
+        viscous_shock_tube.py): LLFTeno/LLFWeno with the Roe average, central viscous terms, RungeKuttaLS(3),
+        adiabatic walls at both x0 faces and at x1 = 0, a symmetry face at the top (each face's closure
+        read from the derivative kernels).  mu is the script's constant; the kernels implement mu = 1,
+        which substitute_simulation_parameters checks."""
+        if any(n.startswith("CRmu") for n in names):
+            raise NotImplementedError("Cartesian viscous blocks: a constant viscosity expected")
+        if averaging != "roe":
+            raise NotImplementedError("Cartesian viscous blocks: the Roe average expected")
+        coeff = self._rk_coefficients(["Temporal solution advancement"])
+        if set(coeff) != {"rkA", "rkB"}:
+            raise NotImplementedError("RungeKuttaLS(3) coefficients rkA/rkB expected")
+        faces = {"AdiabaticWall boundary dir0 side0", "AdiabaticWall boundary dir0 side1",
+                 "AdiabaticWall boundary dir1 side0", "Symmetry boundary dir1 side1"}
+        found = {n for n in names if "boundary dir" in n}
+        if found != faces:
+            raise NotImplementedError("Cartesian viscous block boundary conditions: %s" % sorted(found))
+        closure = self._closures_2d()
+        physics_check.check_algorithm(self.components, 2, viscous=True, sutherland=False, metric=False)
+        return Plan(ndim=2, n=(64, 32, 1), delta=(1.0, 1.0, 1.0), conv=conv,
+                    weno_eps=1e-14 if conv == "weno5z" else 1e-6,  # WenoZ.eps / WenoJS.eps (weno.py)
+                    visc="const", rk="ls_rk3", precision=precision, x1_grid="uniform",
+                    bc=(("adiabatic_wall", "adiabatic_wall"), ("adiabatic_wall", "symmetry"), ("periodic", "periodic")),
+                    rk_a=coeff["rkA"], rk_b=coeff["rkB"], use_graphs=use_graphs, ic="host", closure=closure,
+                    name="viscous2d", kernels=[n for n in names if n])
+
     def _lower_euler2d(self, precision, use_graphs, conv, averaging, names):
         """A 2D Euler block (apps/inviscid_shock_reflection/inviscid_shock.py): Cartesian, no viscous terms,
         LLFWeno/LLFTeno with the Roe or the simple average, RungeKuttaLS(3); a Dirichlet or inlet face at
@@ -715,7 +744,7 @@ class GB300Writer:
                         elif {str(x) for x in r.free_symbols} == {"block0np%d" % d}:
                             npd = next(iter(r.free_symbols))
                             depth[(d, 1)] = max(depth[(d, 1)], int(npd - r))
-        kinds = {2: "reduced_access", 4: "carpenter"}
+        kinds = {0: "none", 2: "reduced_access", 4: "carpenter"}  # none: a symmetry face's mirrored halos
         out = []
         for d in range(2):
             if d == 0 and periodic0:  # no closure on a periodic axis (the field is unused there)
@@ -896,6 +925,9 @@ class GB300Writer:
                       by=float(env.get("by", p.by)), teno_a1=float(env.get("teno_a1", p.teno_a1)),
                       teno_a2=float(env.get("teno_a2", p.teno_a2)))
         self.plan = p.replace(**kw)
+        if p.visc == "const" and p.ndim == 2 and float(env.get("mu", 1.0)) != 1.0:
+            raise NotImplementedError("Cartesian viscous blocks: the kernels implement mu = 1, the script sets %s"
+                                      % env.get("mu"))
         if p.visc == "none" and p.ndim <= 2:  # the Dirichlet states of an Euler block use gama and Minf
             self.plan = self._euler_states(self.plan)
         return self.plan

@@ -227,6 +227,18 @@ static void ops_par_loop(void (*kernel)(P...), const char *name, ops_block block
   }
 }
 
+/* ops_NaNcheck: stop the run when a double dat holds a NaN anywhere (the generated code calls it every
+ * few iterations when the script asks for print_iteration_ops(NaN_check=...)) */
+static inline void ops_NaNcheck(ops_dat d) {
+  const size_t n = (size_t)d->pad[0] * d->pad[1] * d->pad[2];
+  const double *v = (const double *)d->data;
+  for (size_t k = 0; k < n; ++k)
+    if (v[k] != v[k]) {
+      fprintf(stderr, "ops_NaNcheck: NaN in a dat\n");
+      exit(1);
+    }
+}
+
 /* ---------- halos ---------- */
 static inline ops_halo ops_decl_halo(ops_dat from, ops_dat to, int *iter, int *from_base, int *to_base, int *from_dir,
                                      int *to_dir) {

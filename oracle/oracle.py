@@ -164,10 +164,12 @@ class Cfg2D(ctypes.Structure):
         ("top", (ctypes.c_double * 4) * 2),
         ("x_switch", ctypes.c_double),
         ("rk2reg", ctypes.c_int),
+        ("cartesian", ctypes.c_int),
+        ("visc_const", ctypes.c_int),
     ]
 
 
-CLOSURES = {"reduced_access": 0, "carpenter": 1}
+CLOSURES = {"reduced_access": 0, "carpenter": 1, "none": 2}
 
 
 def make_cfg2d(plan):
@@ -195,11 +197,13 @@ def make_cfg2d(plan):
     # Euler blocks: Cartesian x1, no viscous terms, the faces and states of the plan
     c.euler = 1 if plan.visc == "none" else 0
     c.simple_avg = 1 if plan.averaging == "simple" else 0
-    kinds = {"dirichlet": 1, "symmetry": 2, "periodic": 3}
+    kinds = {"dirichlet": 1, "symmetry": 2, "periodic": 3, "adiabatic_wall": 4}
     c.rk2reg = 1 if plan.rk == "rk3" else 0
+    c.cartesian = 1 if plan.x1_grid == "uniform" else 0
+    c.visc_const = 1 if plan.visc == "const" else 0
     for d in range(2):
         for side in range(2):
-            c.bc[d][side] = kinds.get(plan.bc[d][side], 0) if c.euler else 0
+            c.bc[d][side] = kinds.get(plan.bc[d][side], 0) if (c.euler or c.cartesian) else 0
     for side, st in enumerate(plan.dirichlet_x0 or ()):
         for v in range(4):
             c.face0[side][v] = st[v]

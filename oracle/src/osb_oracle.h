@@ -85,11 +85,15 @@ typedef struct {
   /* rk2reg = 1: RungeKutta(3) with two registers (rk_sbli.py:51-61, 117-124): at the step's start
    * qold = q; per stage q = qold + rkB dt R, then qold += rkA dt R (rkA = rkold, rkB = rknew) */
   int rk2reg;
+  /* Cartesian viscous blocks (apps/viscous_shock_tube/viscous_shock_tube.py): cartesian = 1 takes D11 = 1
+   * with the viscous terms kept; visc_const = 1 takes mu = 1 (the script's constant mu) */
+  int cartesian, visc_const;
 } osbo2d_cfg;
 #define OSBO_BC2_DEFAULT 0
 #define OSBO_BC2_DIRICHLET 1
 #define OSBO_BC2_SYMMETRY 2
 #define OSBO_BC2_PERIODIC 3 /* periodic.py / exchange.py:9-57 (both sides of the axis) */
+#define OSBO_BC2_ADIABATIC 4 /* adiabatic_wall.py: no slip, zero wall-normal temperature gradient */
 
 /* Advance q by nsteps LS-RK3 steps.  q holds [4][n1+8][n0+8]: rho, rhou0, rhou1, rhoE with a
  * 4-point halo on every side (the initial state must fill the halos as the script's

@@ -133,9 +133,10 @@ static double d1c(const s2_t *s, const double *f, int i, int j, int dir) {
   const int c0 = s->c.closure[dir][0], c1 = s->c.closure[dir][1];
 #define G(o) (dir == 0 ? F(s, f, i + (o), j) : F(s, f, i, j + (o)))
   /* the side-0 face's points take precedence (its condition comes first in the Piecewise) */
+  /* closure 2: none (a symmetry face, whose mirrored halos the central stencil reads) */
   int side = -1, r = 0;
-  if (k < (c0 == 1 ? 4 : 2)) side = 0, r = k;
-  else if (n - 1 - k < (c1 == 1 ? 4 : 2)) side = 1, r = n - 1 - k;
+  if (k < (c0 == 1 ? 4 : c0 == 2 ? 0 : 2)) side = 0, r = k;
+  else if (n - 1 - k < (c1 == 1 ? 4 : c1 == 2 ? 0 : 2)) side = 1, r = n - 1 - k;
   const int carp = side >= 0 && (side == 0 ? c0 : c1) == 1;
   double v;
   if (carp) {
@@ -165,13 +166,14 @@ static double d2c(const s2_t *s, const double *f, int i, int j, int dir) {
   const double inv = 1.0 / (s->c.delta[dir] * s->c.delta[dir]);
 #define G(o) (dir == 0 ? F(s, f, i + (o), j) : F(s, f, i, j + (o)))
   double v;
-  if (k == 0)
+  const int open0 = s->c.closure[dir][0] != 2, open1 = s->c.closure[dir][1] != 2; /* 2: no closure */
+  if (k == 0 && open0)
     v = (35.0 / 12.0) * G(0) - (26.0 / 3.0) * G(1) + 9.5 * G(2) - (14.0 / 3.0) * G(3) + (11.0 / 12.0) * G(4);
-  else if (k == 1)
+  else if (k == 1 && open0)
     v = (11.0 / 12.0) * G(-1) - (5.0 / 3.0) * G(0) + 0.5 * G(1) + (1.0 / 3.0) * G(2) - (1.0 / 12.0) * G(3);
-  else if (k == n - 1)
+  else if (k == n - 1 && open1)
     v = (35.0 / 12.0) * G(0) - (26.0 / 3.0) * G(-1) + 9.5 * G(-2) - (14.0 / 3.0) * G(-3) + (11.0 / 12.0) * G(-4);
-  else if (k == n - 2)
+  else if (k == n - 2 && open1)
     v = (11.0 / 12.0) * G(1) - (5.0 / 3.0) * G(0) + 0.5 * G(-1) + (1.0 / 3.0) * G(-2) - (1.0 / 12.0) * G(-3);
   else
     v = -(1.0 / 12.0) * G(-2) + (4.0 / 3.0) * G(-1) - 2.5 * G(0) + (4.0 / 3.0) * G(1) - (1.0 / 12.0) * G(2);
@@ -185,7 +187,7 @@ static double d2c(const s2_t *s, const double *f, int i, int j, int dir) {
  *   detJ = dx1/dxi1, D11 = 1/detJ, halos mirrored about the boundary points, SD111 = dD11/dxi1.
  * ------------------------------------------------------------------------------------------- */
 static void metrics(s2_t *s) {
-  if (s->c.euler) { /* no metric kernels in a Cartesian block: d/dx1 = d/dxi1 */
+  if (s->c.euler || s->c.cartesian) { /* no metric kernels in a Cartesian block: d/dx1 = d/dxi1 */
     FOR2(-H, N0 + H, -H, N1 + H) {
       s->D11[I2(s, i, j)] = 1.0;
       s->SD111[I2(s, i, j)] = 0.0;
@@ -328,8 +330,43 @@ static void bc_periodic(s2_t *s, int d) {
       }
 }
 
+/* AdiabaticWallBC (adiabatic_wall.py, as generated for viscous_shock_tube.py) on the face of axis d,
+ * side `side`, every line across it: zero momentum at the wall point, the wall temperature from the
+ * one-sided zero-gradient formula T_w = (18 T_1 - 9 T_2 + 2 T_3)/11 over the first three interior
+ * points and rhoE_w = rho_w T_w / (gama Minf^2 (gama-1)); halo point t mirrors interior point t with
+ * rho and rhoE even and the momentum odd (t = 1..3 on side 0, 1..4 on side 1). */
+static void bc_adiabatic(s2_t *s, int d, int side) {
+  const double g = s->c.gama, M2 = s->c.Minf * s->c.Minf;
+  const int n = d == 0 ? N0 : N1, len = d == 0 ? N1 : N0, bnd = side == 0 ? 0 : n - 1;
+  const int sg = side == 0 ? 1 : -1, nt = side == 0 ? 3 : 4;
+  for (int a = -3; a < len + 4; ++a) {
+#define AT(k) (d == 0 ? I2(s, (k), a) : I2(s, a, (k)))
+    for (int t = 1; t <= nt; ++t) s->q[0][AT(bnd - sg * t)] = s->q[0][AT(bnd + sg * t)];
+    s->q[1][AT(bnd)] = 0.0;
+    s->q[2][AT(bnd)] = 0.0;
+    for (int t = 1; t <= nt; ++t)
+      for (int v = 1; v <= 2; ++v) s->q[v][AT(bnd - sg * t)] = -s->q[v][AT(bnd + sg * t)];
+    double T[4];
+    for (int k = 1; k <= 3; ++k) {
+      const size_t m = AT(bnd + sg * k);
+      const double p = (g - 1) * (s->q[3][m] - 0.5 * (s->q[1][m] * s->q[1][m] + s->q[2][m] * s->q[2][m]) / s->q[0][m]);
+      T[k] = g * M2 * p / s->q[0][m];
+    }
+    s->q[3][AT(bnd)] = (18.0 / 11.0 * T[1] - 9.0 / 11.0 * T[2] + 2.0 / 11.0 * T[3]) * s->q[0][AT(bnd)] / (g * M2 * (g - 1));
+    for (int t = 1; t <= nt; ++t) s->q[3][AT(bnd - sg * t)] = s->q[3][AT(bnd + sg * t)];
+#undef AT
+  }
+}
+
 static void apply_bcs(s2_t *s) {
   const int(*b)[2] = s->c.bc;
+  if (b[0][0] == OSBO_BC2_ADIABATIC) { /* viscous_shock_tube.py: adiabatic walls and a symmetry top */
+    bc_adiabatic(s, 0, 0);
+    bc_adiabatic(s, 0, 1);
+    bc_adiabatic(s, 1, 0);
+    bc_symmetry_x1(s, 1);
+    return;
+  }
   if (b[0][0] == OSBO_BC2_PERIODIC) { /* a doubly periodic Euler block (euler_wave.py) */
     bc_periodic(s, 0);
     bc_periodic(s, 1);
@@ -364,7 +401,7 @@ static void constituent(s2_t *s) {
   FOR2(-2, N0 + 2, -2, N1 + 2) {
     const size_t n = I2(s, i, j);
     s->T[n] = M * M * g * s->p[n] / s->q[0][n];
-    s->mu[n] = (ST + 1.0) * pow(s->T[n], 1.5) / (ST + s->T[n]);
+    s->mu[n] = s->c.visc_const ? 1.0 : (ST + 1.0) * pow(s->T[n], 1.5) / (ST + s->T[n]);
   }
 }
 

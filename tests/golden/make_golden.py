@@ -63,6 +63,8 @@ CASES_2D = {
     "shock_reflection": ((64, 32), 30, {"dt": 1.0}),
     # the doubly periodic Euler density wave (WENO5-Z, simple average, two-register RK3)
     "euler_wave": ((32, 24), 40, {"dt": 5e-3}),
+    # the viscous shock tube: adiabatic walls on three faces, a symmetry face, constant mu, Cartesian
+    "viscous_shock_tube": ((48, 24), 40, {"dt": 1e-3}),
 }
 VARS_2D = ["rho", "rhou0", "rhou1", "rhoE"]
 

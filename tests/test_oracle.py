@@ -300,3 +300,24 @@ def test_oracle_euler_wave_matches_reference_golden():
     # the low-storage scheme with the same coefficients is a different method: the fixture pins the registers
     q2 = O.run2d(plan.replace(rk="ls_rk3"), d["q0"], int(d["steps"]))
     assert max(float(np.abs(q2[inner][v] - ref[v]).max() / np.abs(ref[v]).max()) for v in range(4)) > 1e-6
+
+
+def test_oracle_viscous_shock_tube_matches_reference_golden():
+    """osb_oracle2d.c as the Cartesian viscous block of apps/viscous_shock_tube/viscous_shock_tube.py
+    (adiabatic walls on three faces, a symmetry top, mu = 1, TENO5) against the generated code: 48 x 24,
+    40 steps at dt = 1e-3 (the state moves 43-100 %).  The wall temperature formula is pinned: with the
+    walls' energy taken from the first interior point instead, the result moves by far more."""
+    import json
+    from opensbli_gb300.plan import viscous_shock_tube_plan
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_viscous_shock_tube.npz"))
+    n = tuple(int(x) for x in d["n"])
+    plan = viscous_shock_tube_plan(*n, dt=json.loads(str(d["params"]))["dt"])
+    inner = (slice(None), slice(4, -4), slice(4, -4))
+    ref = d["q"][inner]
+    mom = max(float(np.abs(ref[1]).max()), float(np.abs(ref[2]).max()))
+    q = O.run2d(plan, d["q0"], int(d["steps"]))
+    err = [float(np.abs(q[inner][v] - ref[v]).max() / (mom if v in (1, 2) else np.abs(ref[v]).max())) for v in range(4)]
+    assert max(err) < 1e-13, err
+    # the viscous terms matter: the same block without them is far away
+    q2 = O.run2d(plan.replace(visc="none"), d["q0"], int(d["steps"]))
+    assert max(float(np.abs(q2[inner][v] - ref[v]).max()) / mom for v in (1, 2)) > 1e-4

@@ -122,6 +122,16 @@ def test_shock_reflection_script_lowers_to_its_plan():
     assert g.dirichlet_x_switch == math.nextafter(40.0, 0.0)
 
 
+def test_viscous_shock_tube_script_lowers_to_its_plan():
+    """The viscous shock tube lowers to a Cartesian 2D block with the constant viscosity, adiabatic walls
+    on three faces (ReducedAccess) and a symmetry top face without a one-sided closure."""
+    from opensbli_gb300.plan import viscous_shock_tube_plan
+    g = golden_plan("viscous_shock_tube")
+    p = viscous_shock_tube_plan(*g.n[:2])
+    assert g.replace(kernels=[], name="", niter=None) == p.replace(kernels=[], name="")
+    assert g.visc == "const" and g.closure[1] == ("reduced_access", "none")
+
+
 def test_euler_wave_script_lowers_to_its_plan():
     """The doubly periodic Euler wave lowers with its exchanges on both axes and RungeKutta(3)'s two
     registers (rkold, rknew) to euler_wave_plan's plan."""
@@ -206,7 +216,7 @@ def test_writer_refuses_kernels_outside_the_lowered_families():
     from opensbli_gb300.writer import GB300Writer
     for case in ("tgv_central", "tgv_weno", "tgsym_central", "katzer_teno", "katzer_adaptive", "katzer_carpenter",
                  "tgv_filter", "tgv_teno_adaptive", "sbli3d_teno", "transitional_sbli", "channel_teno",
-                 "shock_reflection", "sod", "shu_osher", "euler_wave"):
+                 "shock_reflection", "sod", "shu_osher", "euler_wave", "viscous_shock_tube"):
         GB300Writer._check_kernel_families(golden_plan(case).kernels)
     assert "User kernel: Non-linear filter application" in golden_plan("tgv_filter").kernels
     names = golden_plan("tgv_filter").kernels + ["User kernel: Shock sensor"]
@@ -236,10 +246,10 @@ def test_cfl_dt_tgv_weno():
 ALL_SCRIPTS = ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central", "katzer_teno",
                "katzer_adaptive", "katzer_carpenter", "tgv_filter", "katzer_weno", "katzer_wenoz", "katzer_teno6",
                "tgv_teno_adaptive", "sbli3d_teno", "transitional_sbli", "channel_teno", "shock_reflection", "sod",
-               "shu_osher", "euler_wave"]
+               "shu_osher", "euler_wave", "viscous_shock_tube"]
 SCRIPTS = ALL_SCRIPTS if os.environ.get("OSB_ALL_SCRIPTS") == "1" else \
     ["tgv_weno", "tgv_filter", "katzer_adaptive", "transitional_sbli", "channel_teno", "shock_reflection", "sod",
-     "euler_wave"]
+     "euler_wave", "viscous_shock_tube"]
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
