@@ -163,6 +163,8 @@ struct BC2Args {
   double f0[4], f1[4];
   // viscous_shock_tube.py: adiabatic walls on the x0 faces and on x1 side 0
   int adi0, adi1, adiy0;
+  // laminar_channel.py: periodic x0 (wrapped after the faces) and an isothermal wall on x1 side 1
+  int per0, wall1;
 };
 
 // AdiabaticWallBC (adiabatic_wall.py, as generated for viscous_shock_tube.py) on one line across a face
@@ -197,6 +199,7 @@ __device__ __forceinline__ void adia2_line(const Q4 &q, const BC2Args &a, At at,
 // inlet (i = 0 and its halo) and outlet (i >= n0-1) of row j, or the Dirichlet x0 faces
 // (dirichlet.py:6-41: the boundary point and the halo take the face's state)
 __device__ __forceinline__ void bc2_row(const Grid &g, const Q4 &q, const BC2Args &a, int j) {
+  if (a.per0) return;  // the x0 exchange follows the faces (k2_wrap)
   if (a.adi0) {  // both x0 faces adiabatic (the 4-point halo of side 1 as generated)
     auto at = [&](int i) { return g2(g, i, j); };
     adia2_line(q, a, at, 0, 1, 1, 3);
@@ -281,10 +284,36 @@ __device__ __forceinline__ void bc2_col(const Grid &g, const Q4 &q, const BC2Arg
   q.v[1][hh] = -rh * um0;
   q.v[2][hh] = -rh * um1;
   q.v[3][hh] = (1.0 / (gama - 1)) * Pw + 0.5 * rh * (um0 * um0 + um1 * um1);
+  if (a.wall1) {  // the channel's second wall: row n1-1, halo rows n1..n1+3 (t = 1..3 here, 4 with t = 1)
+    const int jw = g.n1 - 1;
+    const int64_t w1 = g2(g, i, jw), b1 = g2(g, i, jw - 1);
+    const double ew1 = a.Twall * (1.0 / M2) * q.v[0][w1] / (gama * (gama - 1.0)), Pw1 = (gama - 1) * ew1;
+    const double Tb = M2 * gama * (gama - 1) *
+                      (-(0.5 * q.v[1][b1] * q.v[1][b1] + 0.5 * q.v[2][b1] * q.v[2][b1]) / q.v[0][b1] + q.v[3][b1]) /
+                      q.v[0][b1];
+    const int us[2] = {t, t == 1 ? 4 : 0};
+    for (int k = 0; k < 2; ++k) {
+      const int u = us[k];
+      if (!u) continue;
+      const int64_t m1 = g2(g, i, jw - u), h1 = g2(g, i, jw + u);
+      const double v0 = q.v[1][m1] / q.v[0][m1], v1 = q.v[2][m1] / q.v[0][m1];
+      const double Tu = (u + 1) * a.Twall - u * Tb, rh1 = M2 * gama * Pw1 / Tu;
+      q.v[0][h1] = rh1;
+      q.v[1][h1] = -rh1 * v0;
+      q.v[2][h1] = -rh1 * v1;
+      q.v[3][h1] = (1.0 / (gama - 1)) * Pw1 + 0.5 * rh1 * (v0 * v0 + v1 * v1);
+    }
+    if (t == 1) {
+      q.v[1][w1] = 0.0;
+      q.v[2][w1] = 0.0;
+      q.v[3][w1] = ew1;
+    }
+  }
   if (t == 1) {
     q.v[1][w] = 0.0;
     q.v[2][w] = 0.0;
     q.v[3][w] = ew;
+    if (a.wall1) return;
     const double x0 = a.delta0 * i;  // Dirichlet top face
     for (int j = g.n1 - 1; j < g.n1 + a.hy; ++j)
       for (int v = 0; v < 4; ++v) q.v[v][g2(g, i, j)] = x0 > a.xs ? a.st.hi[v] : a.st.lo[v];
@@ -893,6 +922,64 @@ struct Visc2Args {
   int clx, cly;  // Carpenter faces of x0 and x1 (d1c)
 };
 
+// Central skew-symmetric convective terms of a Cartesian 2D block (laminar_channel.py's Skew(...), the
+// form of the Taylor-Green script, parsing.py:75-111) with the faces' derivative closures:
+//   R_rho = -sum_d skew(rho, d), R_rhou_i = -sum_d skew(rhou_i, d) - dp/dx_i,
+//   R_rhoE = -sum_d skew(rhoE, d) - sum_d d(p u_d)/dx_d,  skew(phi, d) = (d(phi u_d) + u_d dphi + phi du_d)/2.
+// A 32 x 8 tile stages rho, rhou0, rhou1, rhoE, u0, u1 and p with a 5-point margin in shared memory.
+struct Skew2Args {
+  double inv_d0, inv_d1;
+  int clx, cly;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(256) k2_skew(Grid g, Q4T<const T> q, const T *u0, const T *u1, const T *pr, Q4T<T> r,
+                                               Skew2Args sa) {
+  constexpr int TX = 32, TY = 8, HM = 5, SX = TX + 2 * HM, SY = TY + 2 * HM;
+  __shared__ T sm[7][SY][SX];  // rho rhou0 rhou1 rhoE u0 u1 p
+  const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY, tid = threadIdx.y * TX + threadIdx.x;
+  for (int t = tid; t < SX * SY; t += TX * TY) {
+    const int li = t % SX, lj = t / SX, gi = i0 - HM + li, gj = j0 - HM + lj;
+    if (gi < -4 || gi >= g.n0 + 4 || gj < -4 || gj >= g.n1 + 4) continue;
+    const int64_t m = g2(g, gi, gj);
+#pragma unroll
+    for (int v = 0; v < 4; ++v) sm[v][lj][li] = q.v[v][m];
+    sm[4][lj][li] = u0[m];
+    sm[5][lj][li] = u1[m];
+    sm[6][lj][li] = pr[m];
+  }
+  __syncthreads();
+  const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+  if (i >= g.n0 || j >= g.n1) return;
+  const int li = threadIdx.x + HM, lj = threadIdx.y + HM;
+  auto D = [&](int d, auto &&F) {  // first derivative along d of F(offset) at the point
+    return d == 0 ? T(sa.inv_d0) * d1c<T>([&](int o) { return F(0, o); }, i, g.n0, sa.clx)
+                  : T(sa.inv_d1) * d1c<T>([&](int o) { return F(1, o); }, j, g.n1, sa.cly);
+  };
+  auto at = [&](int f, int d, int o) -> T { return d == 0 ? sm[f][lj][li + o] : sm[f][lj + o][li]; };
+  T R[4];
+#pragma unroll
+  for (int v = 0; v < 4; ++v) {
+    T acc = T(0);
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      const T dprod = D(d, [&](int dd, int o) { return at(v, dd, o) * at(4 + dd, dd, o); });
+      const T dphi = D(d, [&](int dd, int o) { return at(v, dd, o); });
+      const T du = D(d, [&](int dd, int o) { return at(4 + dd, dd, o); });
+      acc += T(0.5) * (dprod + sm[4 + d][lj][li] * dphi + sm[v][lj][li] * du);
+    }
+    R[v] = -acc;
+  }
+#pragma unroll
+  for (int d = 0; d < 2; ++d) {
+    R[1 + d] -= D(d, [&](int dd, int o) { return at(6, dd, o); });
+    R[3] -= D(d, [&](int dd, int o) { return at(6, dd, o) * at(4 + dd, dd, o); });
+  }
+  const int64_t c = g2(g, i, j);
+#pragma unroll
+  for (int v = 0; v < 4; ++v) r.v[v][c] = R[v];
+}
+
 template <typename T> struct Q3T {
   T *v[3];
 };
@@ -979,18 +1066,24 @@ __global__ void __launch_bounds__(V2X * V2Y, 2) k2_visc(Grid g, Prims<const T> p
 // du = dt R + A du, q += B du in FP64 (update = 1), or R itself into du (update = 0: osb_residual).
 template <typename T>
 __global__ void k2_rk(Grid g, Q4T<const T> rx, Q4T<const T> ry, Q3T<const T> rv, Q4 du, Q4 q64, double dt, double A,
-                      double B, int update, int rk2) {
+                      double B, int update, int rk2, double f0, double f1) {
   const int64_t N = (int64_t)g.n0 * g.n1;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < N; t += (int64_t)gridDim.x * blockDim.x) {
     const int i = (int)(t % g.n0), j = (int)(t / g.n0);
     const int64_t c = g2(g, i, j);
     T R[4];
 #pragma unroll
-    for (int v = 0; v < 4; ++v) R[v] = rx.v[v][c] + ry.v[v][c];
+    for (int v = 0; v < 4; ++v) R[v] = ry.v[0] ? rx.v[v][c] + ry.v[v][c] : rx.v[v][c];  // ry: x1 fluxes
     if (rv.v[0]) {  // viscous terms (none on Euler blocks)
       R[1] += rv.v[0][c];
       R[2] += rv.v[1][c];
       R[3] += rv.v[2][c];
+    }
+    if (f0 != 0.0 || f1 != 0.0) {  // the channel's forcing c_j (laminar_channel.py): -c_i, -c_j u_j
+      const double ir = 1.0 / q64.v[0][c];
+      R[1] -= T(f0);
+      R[2] -= T(f1);
+      R[3] -= T(f0 * (q64.v[1][c] * ir) + f1 * (q64.v[2][c] * ir));
     }
     if (update && rk2) {  // RungeKutta(3), two registers (rk_sbli.py:117-124): du holds qold
 #pragma unroll
@@ -1098,7 +1191,7 @@ void launch2_save(const Ctx &c, cudaStream_t s, int64_t *launches) {
 
 void launch2_bcs(const Ctx &c, cudaStream_t s, int64_t *launches) {
   const osb_plan_desc &p = c.plan;
-  if (p.bc[0][0] == OSB_BC_PERIODIC) {  // a doubly periodic block: x0, then x1 (corners from the x0 images)
+  if (p.bc[0][0] == OSB_BC_PERIODIC && p.bc[1][0] == OSB_BC_PERIODIC) {  // doubly periodic: x0, then x1
     for (int d = 0; d < 2; ++d) {
       const int64_t N = (int64_t)4 * (d == 0 ? c.g.n1 + 2 * c.hy2 : c.g.n0 + 2 * c.hx2) * (d == 0 ? c.hx2 : c.hy2);
       int nb = (int)((N + 255) / 256);
@@ -1129,12 +1222,21 @@ void launch2_bcs(const Ctx &c, cudaStream_t s, int64_t *launches) {
   a.adi0 = p.bc[0][0] == OSB_BC_ADIABATIC_WALL;
   a.adi1 = p.bc[0][1] == OSB_BC_ADIABATIC_WALL;
   a.adiy0 = p.bc[1][0] == OSB_BC_ADIABATIC_WALL;
+  a.per0 = p.bc[0][0] == OSB_BC_PERIODIC;
+  a.wall1 = p.bc[1][1] == OSB_BC_ISOTHERMAL_WALL;
   // rows 4 .. n1-6 to the other blocks: block 0 takes the rows a top symmetry face reads (n1-5 ..)
   const int rows = c.g.n1 - 9 > 0 ? c.g.n1 - 9 : 0, cols = c.g.n0 - 3 > 0 ? c.g.n0 - 3 : 0;
   const int row_blocks = (rows + BC2_THREADS - 1) / BC2_THREADS;
   const int col_blocks = (3 * cols + BC2_THREADS - 1) / BC2_THREADS;
   k2_bc<<<1 + row_blocks + col_blocks, BC2_THREADS, 0, s>>>(c.g, q4(c.q64_2d), a, row_blocks);
   *launches += 1;
+  if (a.per0) {  // the x0 exchange after the walls, which act on single x0 columns
+    const int64_t N = (int64_t)4 * (c.g.n1 + 2 * c.hy2) * c.hx2;
+    int nb = (int)((N + 255) / 256);
+    if (nb > c.num_sms * 4) nb = c.num_sms * 4;
+    k2_wrap<<<nb, 256, 0, s>>>(c.g, q4(c.q64_2d), 0, c.hx2, c.hy2);
+    *launches += 1;
+  }
 }
 
 // Mixed: the FP32 working state from the FP64 master at every padded point (the right-hand side's
@@ -1201,15 +1303,21 @@ template <typename T> void launch2_rhs(const Ctx &c, int update, double A, doubl
   cudaEventRecord(c.ev_fork2, s);
   cudaStreamWaitEvent(c.side2[0], c.ev_fork2, 0);
   cudaStreamWaitEvent(c.side2[1], c.ev_fork2, 0);
-  {
-    using Tl = T2Tile<0>;
-    dim3 gx((c.g.n0 + Tl::TI - 2) / (Tl::TI - 1), (c.g.n1 + Tl::TA - 1) / Tl::TA);
-    launch2_flux<T, 0>(c, gx, q, prc, r, eps, ctp, s);
-  }
-  {
-    using Tl = T2Tile<1>;
-    dim3 gy((c.g.n0 + Tl::TA - 1) / Tl::TA, (c.g.n1 + Tl::TI - 2) / (Tl::TI - 1));
-    launch2_flux<T, 1>(c, gy, q, prc, q4t<T>(c.resy), eps, ctp, c.side2[0]);
+  const bool skew = p.conv == OSB_CONV_CENTRAL_SKEW;
+  if (skew) {  // central skew-symmetric convective terms (laminar_channel.py), Cartesian
+    const Skew2Args sa{1.0 / p.delta[0], 1.0 / p.delta[1], closure_bits(p, 0), closure_bits(p, 1)};
+    k2_skew<T><<<dim3((c.g.n0 + 31) / 32, (c.g.n1 + 7) / 8), dim3(32, 8), 0, s>>>(c.g, q, pr.u0, pr.u1, pr.p, r, sa);
+  } else {
+    {
+      using Tl = T2Tile<0>;
+      dim3 gx((c.g.n0 + Tl::TI - 2) / (Tl::TI - 1), (c.g.n1 + Tl::TA - 1) / Tl::TA);
+      launch2_flux<T, 0>(c, gx, q, prc, r, eps, ctp, s);
+    }
+    {
+      using Tl = T2Tile<1>;
+      dim3 gy((c.g.n0 + Tl::TA - 1) / Tl::TA, (c.g.n1 + Tl::TI - 2) / (Tl::TI - 1));
+      launch2_flux<T, 1>(c, gy, q, prc, q4t<T>(c.resy), eps, ctp, c.side2[0]);
+    }
   }
   Visc2Args va;
   va.Re = p.Re;
@@ -1232,9 +1340,11 @@ template <typename T> void launch2_rhs(const Ctx &c, int update, double A, doubl
   Q3T<const T> rvc{{rv.v[0], rv.v[1], rv.v[2]}};
   int nb = (int)(((int64_t)c.g.n0 * c.g.n1 + 255) / 256);
   if (nb > c.num_sms * 4) nb = c.num_sms * 4;
-  k2_rk<T><<<nb, 256, 0, s>>>(c.g, q4t<const T>(c.res), q4t<const T>(c.resy), rvc, q4(c.du2), q4(c.q64_2d), dt, A, B,
-                              update, p.rk == OSB_RK3_2REG);
-  *launches += visc ? 5 : 4;
+  Q4T<const T> ryc = q4t<const T>(c.resy);
+  if (skew) ryc.v[0] = nullptr;  // the skew kernel writes the whole convective residual into res
+  k2_rk<T><<<nb, 256, 0, s>>>(c.g, q4t<const T>(c.res), ryc, rvc, q4(c.du2), q4(c.q64_2d), dt, A, B, update,
+                              p.rk == OSB_RK3_2REG, p.forcing[0], p.forcing[1]);
+  *launches += 2 + (skew ? 1 : 2) + (visc ? 1 : 0);
 }
 
 // The adaptive TENO cut-off of the current working state over the interior, as FP64 [n1][n0]

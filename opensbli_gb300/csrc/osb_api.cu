@@ -55,7 +55,8 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
     snprintf(why, n, "3D blocks: Roe averaging, cartesian = 0");
     return OSB_EUNSUPPORTED;
   }
-  if (!wall3(*p) && (p->forcing[0] != 0 || p->forcing[1] != 0 || p->forcing[2] != 0)) {
+  const bool chan2 = p->ndim == 2 && p->conv == OSB_CONV_CENTRAL_SKEW;  // laminar_channel.py
+  if (!wall3(*p) && !chan2 && (p->forcing[0] != 0 || p->forcing[1] != 0 || p->forcing[2] != 0)) {
     snprintf(why, n, "forcing: 3D wall-bounded blocks only");
     return OSB_EUNSUPPORTED;
   }
@@ -127,18 +128,38 @@ int validate(const osb_plan_desc *p, char *why, size_t n) {
         snprintf(why, n, "2D constant-viscosity blocks: Cartesian, adiabatic walls (x0, x1 side 0), symmetry top");
         return OSB_EUNSUPPORTED;
       }
-    } else if (p->bc[0][0] != OSB_BC_INLET_PRESSURE_EXTRAPOLATE || p->bc[0][1] != OSB_BC_EXTRAPOLATION ||
-               p->bc[1][0] != OSB_BC_ISOTHERMAL_WALL || p->bc[1][1] != OSB_BC_DIRICHLET) {
+    } else if (!chan2 && (p->bc[0][0] != OSB_BC_INLET_PRESSURE_EXTRAPOLATE || p->bc[0][1] != OSB_BC_EXTRAPOLATION ||
+                          p->bc[1][0] != OSB_BC_ISOTHERMAL_WALL || p->bc[1][1] != OSB_BC_DIRICHLET)) {
       snprintf(why, n, "2D blocks: boundary conditions must be inlet/extrapolation (x0) and isothermal wall/Dirichlet (x1)");
       return OSB_EUNSUPPORTED;
-    } else if (p->cartesian != 0) {
+    } else if (!chan2 && p->cartesian != 0) {
       snprintf(why, n, "2D viscous blocks: metrics stretched in x1 (cartesian = 0)");
       return OSB_EUNSUPPORTED;
     }
     if (p->conv != OSB_CONV_TENO5 && p->conv != OSB_CONV_WENO5JS && p->conv != OSB_CONV_WENO5Z &&
-        p->conv != OSB_CONV_TENO6) {
-      snprintf(why, n, "2D blocks: TENO5, TENO6, WENO5-JS or WENO5-Z fluxes");
+        p->conv != OSB_CONV_TENO6 && !chan2) {
+      snprintf(why, n, "2D blocks: TENO5, TENO6, WENO5-JS or WENO5-Z fluxes (central skew on channel blocks)");
       return OSB_EUNSUPPORTED;
+    }
+    if (chan2) {  // Cartesian, periodic x0, isothermal walls on both x1 faces, Sutherland, forcing
+      if (p->bc[0][0] != OSB_BC_PERIODIC || p->bc[0][1] != OSB_BC_PERIODIC || p->bc[1][0] != OSB_BC_ISOTHERMAL_WALL ||
+          p->bc[1][1] != OSB_BC_ISOTHERMAL_WALL || p->cartesian != 1 || p->visc != OSB_VISC_SUTHERLAND ||
+          p->rk != OSB_RK3_LS || p->forcing[2] != 0 || !std::isfinite(p->forcing[0]) || !std::isfinite(p->forcing[1])) {
+        snprintf(why, n, "2D central-skew blocks: the laminar channel (Cartesian, periodic x0, isothermal walls on both "
+                         "x1 faces, Sutherland, LS-RK3, finite forcing c0, c1)");
+        return OSB_EUNSUPPORTED;
+      }
+      for (int side = 0; side < 2; ++side)
+        if (p->closure[1][side] != OSB_CLOSURE_REDUCED_ACCESS && p->closure[1][side] != OSB_CLOSURE_CARPENTER) {
+          snprintf(why, n, "closure[1][%d]: OSB_CLOSURE_REDUCED_ACCESS or OSB_CLOSURE_CARPENTER", side);
+          return OSB_EINVAL;
+        }
+      if (!(p->gama > 1.0) || !(p->Minf > 0) || !(p->Re > 0) || !(p->Pr > 0) || !(p->Twall > 0) || !(p->RefT > 0)) {
+        snprintf(why, n, "bad physical constants");
+        return OSB_EINVAL;
+      }
+      if (p->precision != OSB_PREC_FP64 && p->precision != OSB_PREC_MIXED) { snprintf(why, n, "precision"); return OSB_EINVAL; }
+      return OSB_OK;
     }
     if (p->teno_adaptive) {
       if (p->conv != OSB_CONV_TENO5) { snprintf(why, n, "teno_adaptive needs TENO5 fluxes"); return OSB_EINVAL; }

@@ -300,6 +300,21 @@ def viscous_shock_tube_plan(n0=500, n1=250, precision="fp64", dt=5e-6, use_graph
                 name="viscous_shock_tube_%dx%d" % (n0, n1))
 
 
+def laminar_channel_plan(n0=16, n1=64, precision="fp64", dt=2e-4, use_graphs=True):
+    """The 2D laminar channel of apps/channel_flow/laminar_2D/laminar_channel.py: central skew-symmetric
+    convective terms (Skew) with StoreSome central viscous terms, Sutherland viscosity (110.4/273),
+    Re = 90, Minf = 0.1, Pr = 0.72, the forcing c = (-1, 0), periodic x0 of length 2 pi, isothermal
+    walls (Twall = 1) at x1 = -1 and x1 = 1 with Carpenter closures, a uniform grid, RungeKuttaLS(3);
+    16 x 64 and dt = 2e-4 as the script sets them."""
+    return Plan(ndim=2, n=(n0, n1, 1), delta=(2 * math.pi / n0, 2.0 / (n1 - 1), 1.0), conv="central_skew",
+                visc="sutherland", rk="ls_rk3", precision=precision,
+                bc=(("periodic", "periodic"), ("isothermal_wall", "isothermal_wall"), ("periodic", "periodic")),
+                gama=1.4, Minf=0.1, Re=90.0, Pr=0.72, Twall=1.0, SuthT=110.4, RefT=273.0,
+                rk_a=(0.0, -5.0 / 9.0, -153.0 / 128.0), rk_b=(1.0 / 3.0, 15.0 / 16.0, 8.0 / 15.0), dt=dt,
+                use_graphs=use_graphs, ic="host", x1_grid="uniform", forcing=(-1.0, 0.0),
+                closure=(("none", "none"), ("carpenter", "carpenter")), name="laminar_channel_%dx%d" % (n0, n1))
+
+
 def _euler1d_state(g, d, u0, p):
     """rho, rhou0, rhoE as the generated 1D face kernels form them: rhoE = d u0^2 / 2 + p / (gama - 1)."""
     return (d, d * u0, 0.5 * d * u0 ** 2 + p / (g - 1.0))

@@ -48,6 +48,7 @@ CASES = {
     "euler_wave": "ref:apps/euler_wave/euler_wave.py",
     "kelvin_helmholtz": "ref:apps/kelvin_helmholtz/kelvin_helmholtz.py",
     "viscous_shock_tube": "ref:apps/viscous_shock_tube/viscous_shock_tube.py",
+    "laminar_channel": "ref:apps/channel_flow/laminar_2D/laminar_channel.py",
 }
 
 

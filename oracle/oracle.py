@@ -166,6 +166,8 @@ class Cfg2D(ctypes.Structure):
         ("rk2reg", ctypes.c_int),
         ("cartesian", ctypes.c_int),
         ("visc_const", ctypes.c_int),
+        ("skew", ctypes.c_int),
+        ("force", ctypes.c_double * 2),
     ]
 
 
@@ -204,6 +206,11 @@ def make_cfg2d(plan):
     for d in range(2):
         for side in range(2):
             c.bc[d][side] = kinds.get(plan.bc[d][side], 0) if (c.euler or c.cartesian) else 0
+    if c.cartesian and plan.bc[1][1] == "isothermal_wall":
+        c.bc[1][1] = 5  # the channel's second wall
+    c.skew = 1 if plan.conv == "central_skew" else 0
+    for d, f in enumerate((plan.forcing or (0.0, 0.0))[:2]):
+        c.force[d] = f
     for side, st in enumerate(plan.dirichlet_x0 or ()):
         for v in range(4):
             c.face0[side][v] = st[v]

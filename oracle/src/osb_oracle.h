@@ -88,12 +88,18 @@ typedef struct {
   /* Cartesian viscous blocks (apps/viscous_shock_tube/viscous_shock_tube.py): cartesian = 1 takes D11 = 1
    * with the viscous terms kept; visc_const = 1 takes mu = 1 (the script's constant mu) */
   int cartesian, visc_const;
+  /* the laminar channel (apps/channel_flow/laminar_2D/laminar_channel.py): skew = 1 takes the central
+   * skew-symmetric convective terms instead of the characteristic fluxes, force = c_j subtracted from the
+   * momentum (c_i) and energy (c_j u_j) equations */
+  int skew;
+  double force[2];
 } osbo2d_cfg;
 #define OSBO_BC2_DEFAULT 0
 #define OSBO_BC2_DIRICHLET 1
 #define OSBO_BC2_SYMMETRY 2
 #define OSBO_BC2_PERIODIC 3 /* periodic.py / exchange.py:9-57 (both sides of the axis) */
 #define OSBO_BC2_ADIABATIC 4 /* adiabatic_wall.py: no slip, zero wall-normal temperature gradient */
+#define OSBO_BC2_WALL 5      /* isothermal_wall.py on x1 side 1 (the channel's second wall) */
 
 /* Advance q by nsteps LS-RK3 steps.  q holds [4][n1+8][n0+8]: rho, rhou0, rhou1, rhoE with a
  * 4-point halo on every side (the initial state must fill the halos as the script's

@@ -358,8 +358,41 @@ static void bc_adiabatic(s2_t *s, int d, int side) {
   }
 }
 
+/* IsothermalWallBC on x1 side 1 (isothermal_wall.py:32-88): bc_wall mirrored about row n1-1, halo
+ * rows n1..n1+3 */
+static void bc_wall_top(s2_t *s) {
+  const double g = s->c.gama, M = s->c.Minf, Tw = s->c.Twall;
+  const int jw = N1 - 1;
+  for (int i = -3; i < N0 + 4; ++i) {
+    const size_t w = I2(s, i, jw), a1 = I2(s, i, jw - 1);
+    s->q[1][w] = 0.0;
+    s->q[2][w] = 0.0;
+    s->q[3][w] = Tw * (1.0 / (M * M)) * s->q[0][w] / (g * (g - 1.0));
+    const double Pw = (g - 1) * s->q[3][w];
+    const double Ta = M * M * g * (g - 1) *
+                      (-(0.5 * s->q[1][a1] * s->q[1][a1] + 0.5 * s->q[2][a1] * s->q[2][a1]) / s->q[0][a1] + s->q[3][a1]) /
+                      s->q[0][a1];
+    for (int t = 1; t <= 4; ++t) {
+      const size_t m = I2(s, i, jw - t), h = I2(s, i, jw + t);
+      const double um0 = s->q[1][m] / s->q[0][m], um1 = s->q[2][m] / s->q[0][m];
+      const double Tt = (t + 1) * Tw - t * Ta;
+      const double rh = M * M * g * Pw / Tt;
+      s->q[0][h] = rh;
+      s->q[1][h] = -rh * um0;
+      s->q[2][h] = -rh * um1;
+      s->q[3][h] = (1.0 / (g - 1)) * Pw + 0.5 * rh * (um0 * um0 + um1 * um1);
+    }
+  }
+}
+
 static void apply_bcs(s2_t *s) {
   const int(*b)[2] = s->c.bc;
+  if (b[0][0] == OSBO_BC2_PERIODIC && b[1][0] != OSBO_BC2_PERIODIC) { /* laminar_channel.py */
+    bc_periodic(s, 0);
+    bc_wall(s);
+    bc_wall_top(s);
+    return;
+  }
   if (b[0][0] == OSBO_BC2_ADIABATIC) { /* viscous_shock_tube.py: adiabatic walls and a symmetry top */
     bc_adiabatic(s, 0, 0);
     bc_adiabatic(s, 0, 1);
@@ -567,6 +600,40 @@ static void residual_teno(s2_t *s) {
   }
 }
 
+/* Central skew-symmetric convective terms (laminar_channel.py's Skew(...); the same form as the
+ * Taylor-Green script, parsing.py:75-111) on a Cartesian block with the derivative closures of the
+ * faces, and the forcing c_j:
+ *   R_rho = -sum_j skew(rho, j), R_rhou_i = -sum_j skew(rhou_i, j) - dp/dx_i - c_i,
+ *   R_rhoE = -sum_j skew(rhoE, j) - sum_j d(p u_j)/dx_j - c_j u_j,
+ *   skew(phi, j) = (d(phi u_j)/dx_j + u_j dphi/dx_j + phi du_j/dx_j) / 2. */
+static void residual_skew(s2_t *s) {
+  double *prod = alloc2(s);
+  const double *U[2] = {s->u0, s->u1};
+  const double *phi[4] = {s->q[0], s->q[1], s->q[2], s->q[3]};
+  for (int v = 0; v < 4; ++v) FOR2(0, N0, 0, N1) s->res[v][I2(s, i, j)] = 0.0;
+  for (int v = 0; v < 4; ++v)
+    for (int d = 0; d < 2; ++d) {
+      FOR2(-H, N0 + H, -H, N1 + H) prod[I2(s, i, j)] = phi[v][I2(s, i, j)] * U[d][I2(s, i, j)];
+      FOR2(0, N0, 0, N1) {
+        const size_t c = I2(s, i, j);
+        const double sk = 0.5 * (d1c(s, prod, i, j, d) + U[d][c] * d1c(s, phi[v], i, j, d) + phi[v][c] * d1c(s, U[d], i, j, d));
+        s->res[v][c] -= sk;
+      }
+    }
+  for (int d = 0; d < 2; ++d) {
+    FOR2(0, N0, 0, N1) s->res[1 + d][I2(s, i, j)] -= d1c(s, s->p, i, j, d);
+    FOR2(-H, N0 + H, -H, N1 + H) prod[I2(s, i, j)] = s->p[I2(s, i, j)] * U[d][I2(s, i, j)];
+    FOR2(0, N0, 0, N1) s->res[3][I2(s, i, j)] -= d1c(s, prod, i, j, d);
+  }
+  FOR2(0, N0, 0, N1) {
+    const size_t c = I2(s, i, j);
+    s->res[1][c] -= s->c.force[0];
+    s->res[2][c] -= s->c.force[1];
+    s->res[3][c] -= s->c.force[0] * s->u0[c] + s->c.force[1] * s->u1[c];
+  }
+  free(prod);
+}
+
 /* Viscous and heat-flux terms with Sutherland viscosity in the stretched metric
  * (katzer_SBLI.py:12-14; metric.py:72-234): d/dx0 = d/dxi0, d/dx1 = D11 d/dxi1,
  * d2/dx1^2 = D11^2 d2/dxi1^2 + D11 SD111 d/dxi1, d2/dx0dx1 = D11 d/dxi1 (d/dxi0) (inner derivative
@@ -644,7 +711,8 @@ int osbo2d_run(const osbo2d_cfg *cfg, double *q, int nsteps) {
     for (int st = 0; st < 3; ++st) {
       constituent(&s);
       if (cfg->teno_adaptive) sensor(&s);
-      residual_teno(&s);
+      if (cfg->skew) residual_skew(&s);
+      else residual_teno(&s);
       if (!cfg->euler) residual_viscous(&s);
       for (int v = 0; v < 4; ++v)
         for (int j = 0; j < cfg->n[1]; ++j)
@@ -683,7 +751,8 @@ int osbo2d_residual(const osbo2d_cfg *cfg, const double *q, double *r) {
   apply_bcs(&s);
   constituent(&s);
   if (cfg->teno_adaptive) sensor(&s);
-  residual_teno(&s);
+  if (cfg->skew) residual_skew(&s);
+  else residual_teno(&s);
   if (!cfg->euler) residual_viscous(&s);
   size_t m = 0;
   for (int v = 0; v < 4; ++v)

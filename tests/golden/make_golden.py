@@ -65,6 +65,8 @@ CASES_2D = {
     "euler_wave": ((32, 24), 40, {"dt": 5e-3}),
     # the viscous shock tube: adiabatic walls on three faces, a symmetry face, constant mu, Cartesian
     "viscous_shock_tube": ((48, 24), 40, {"dt": 1e-3}),
+    # the laminar channel: skew-symmetric central convection, walls on both x1 faces, forcing
+    "laminar_channel": ((16, 32), 40, {"dt": 2e-3}),
 }
 VARS_2D = ["rho", "rhou0", "rhou1", "rhoE"]
 

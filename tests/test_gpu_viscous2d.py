@@ -79,3 +79,37 @@ def test_viscous_shock_tube_residual_graph_and_mixed():
     mom = float(np.linalg.norm(ref[1]))
     l2 = [float(np.linalg.norm(qm[v] - ref[v]) / (mom if v in (1, 2) else np.linalg.norm(ref[v]))) for v in range(4)]
     assert np.isfinite(qm).all() and max(l2) <= 1e-5, l2
+
+
+# ---- the laminar channel (apps/channel_flow/laminar_2D/laminar_channel.py): central skew-symmetric
+# convective terms, Sutherland viscosity, periodic x0, isothermal walls on both x1 faces, forcing ----
+
+def test_laminar_channel_fp64_matches_reference_golden_and_oracle():
+    from opensbli_gb300.plan import laminar_channel_plan
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_laminar_channel.npz"))
+    n = tuple(int(x) for x in d["n"])
+    plan = laminar_channel_plan(*n, dt=json.loads(str(d["params"]))["dt"])
+    q = run_gpu(plan, d["q0"], int(d["steps"]))
+    assert max(rel_err_mom(q, d["q"][INNER])) <= 1e-12, rel_err_mom(q, d["q"][INNER])
+    p2 = plan.replace(closure=(("none", "none"), ("reduced_access", "reduced_access")))
+    assert max(rel_err_mom(run_gpu(p2, d["q0"], 20), O.run2d(p2, d["q0"], 20)[INNER])) <= 1e-12
+    r_or = O.residual2d(plan, d["q"])
+    s = Solver(plan)
+    s.set_state64_padded(d["q"], 4)
+    r = s.residual().cpu().numpy()
+    s.close()
+    mom = max(np.abs(r_or[1]).max(), np.abs(r_or[2]).max())
+    assert max(float(np.abs(r[v] - r_or[v]).max() / (mom if v in (1, 2) else np.abs(r_or[v]).max())) for v in range(4)) <= 1e-11
+
+
+def test_laminar_channel_graph_and_mixed():
+    from opensbli_gb300.plan import laminar_channel_plan
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_laminar_channel.npz"))
+    n = tuple(int(x) for x in d["n"])
+    plan = laminar_channel_plan(*n, dt=json.loads(str(d["params"]))["dt"])
+    assert np.array_equal(run_gpu(plan, d["q0"], 6), run_gpu(plan.replace(use_graphs=False), d["q0"], 6))
+    qm = run_gpu(plan.replace(precision="mixed"), d["q0"], int(d["steps"]))
+    ref = d["q"][INNER]
+    mom = float(np.linalg.norm(ref[1]))
+    l2 = [float(np.linalg.norm(qm[v] - ref[v]) / (mom if v in (1, 2) else np.linalg.norm(ref[v]))) for v in range(4)]
+    assert np.isfinite(qm).all() and max(l2) <= 1e-5, l2

@@ -321,3 +321,21 @@ def test_oracle_viscous_shock_tube_matches_reference_golden():
     # the viscous terms matter: the same block without them is far away
     q2 = O.run2d(plan.replace(visc="none"), d["q0"], int(d["steps"]))
     assert max(float(np.abs(q2[inner][v] - ref[v]).max()) / mom for v in (1, 2)) > 1e-4
+
+
+def test_oracle_laminar_channel_matches_reference_golden():
+    """osb_oracle2d.c with the central skew-symmetric convective terms, Sutherland viscosity, periodic x0,
+    isothermal walls on both x1 faces and the forcing (apps/channel_flow/laminar_2D/laminar_channel.py)
+    against the generated code: 16 x 32, 40 steps at dt = 2e-3; without the forcing it is far away."""
+    import json
+    from opensbli_gb300.plan import laminar_channel_plan
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "ref_laminar_channel.npz"))
+    n = tuple(int(x) for x in d["n"])
+    plan = laminar_channel_plan(*n, dt=json.loads(str(d["params"]))["dt"])
+    inner = (slice(None), slice(4, -4), slice(4, -4))
+    ref = d["q"][inner]
+    mom = max(float(np.abs(ref[1]).max()), float(np.abs(ref[2]).max()))
+    err = lambda q: [float(np.abs(q[inner][v] - ref[v]).max() / (mom if v in (1, 2) else np.abs(ref[v]).max()))
+                     for v in range(4)]
+    assert max(err(O.run2d(plan, d["q0"], int(d["steps"])))) < 1e-13
+    assert max(err(O.run2d(plan.replace(forcing=(0.0, 0.0)), d["q0"], int(d["steps"])))) > 1e-3
