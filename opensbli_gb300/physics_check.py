@@ -190,7 +190,11 @@ class PhysicsCheck:
         checked = set()
         for k in self.components:
             cn = (k.computation_name or "").strip()
-            if cn.startswith("Convective terms group"):
+            if cn == "Convective terms":
+                # the convective terms with their derivatives evaluated locally (laminar_channel.py)
+                self._check_central_residual("Convective residual", k, meaning, products)
+                checked.add("Convective residual")
+            elif cn.startswith("Convective terms group"):
                 for e in k.equations:
                     factors = []
                     for f in sympy.Mul.make_args(e.rhs):
@@ -224,6 +228,8 @@ class PhysicsCheck:
         body = _interior(rhs)
         ds = _datasets(body)
         bases = {_base(a) for a in ds}
+        if len(bases) == 2:  # a stencil applied to the product of two arrays (laminar_channel.py's d(p u_j))
+            return self._classify_product_derivative(cn, body, ds, sorted(bases))
         if len(bases) != 1:
             self._fail("derivative %s reads %s" % (cn, sorted(bases)))
         axes = {d for a in ds for d, i in enumerate(a.indices) if int(i) != 0}
@@ -260,6 +266,37 @@ class PhysicsCheck:
                 self._fail("derivative %s nests more than two first derivatives" % cn)
             return (inner[0], tuple(sorted(inner[1] + (d,))))
         return ((base,), (d,) * order)
+
+    def _classify_product_derivative(self, cn, body, ds, bases):
+        """sum_o w_o f(o) g(o) along one axis, checked bilinear at random values, with the 4th-order
+        central first-derivative weights: the derivative of the product f g."""
+        axes = {d for a in ds for d, i in enumerate(a.indices) if int(i) != 0}
+        if len(axes) != 1:
+            self._fail("derivative %s is not along one axis" % cn)
+        d = axes.pop()
+        invs = [c for c in _constants(body) if str(c).startswith("inv_")]
+        if len(invs) != 1:
+            self._fail("derivative %s: one 1/delta factor expected" % cn)
+        offs = sorted({int(a.indices[d]) for a in ds})
+        w = {}
+        for o in offs:  # f = delta(o), g = 1
+            reps = {a: sympy.Integer(1 if (_base(a) == bases[1] or int(a.indices[d]) == o) and
+                                     (_base(a) == bases[1] or _base(a) == bases[0]) and
+                                     (_base(a) != bases[0] or int(a.indices[d]) == o) else 0) for a in ds}
+            reps[invs[0]] = sympy.Integer(1)
+            w[o] = sympy.nsimplify(body.xreplace(reps))
+        for trial in range(3):
+            vals = {(b, o): self.rnd.uniform(0.5, 1.5) for b in bases for o in offs}
+            reps = {a: sympy.Float(vals[(_base(a), int(a.indices[d]))], 30) for a in ds}
+            reps[invs[0]] = sympy.Integer(1)
+            got = float(body.xreplace(reps))
+            want = sum(float(w[o]) * vals[(bases[0], o)] * vals[(bases[1], o)] for o in offs)
+            if abs(got - want) > 1e-12 * max(1.0, abs(want)):
+                self._fail("derivative %s is not a stencil of the product %s" % (cn, bases))
+        mom = [sympy.nsimplify(sum(w[o] * sympy.Integer(o) ** k for o in offs)) for k in range(5)]
+        if mom != [0, 1, 0, 0, 0]:
+            self._fail("derivative %s: weights are not 4th-order central (moments %s)" % (cn, mom))
+        return (tuple(bases), (d,))
 
     def _point_symbols(self):
         names = ["rho", "rhoE", "p", "T", "mu", "D11", "SD111"] + ["rhou%d" % c for c in range(self.ndim)] + \
@@ -300,7 +337,10 @@ class PhysicsCheck:
                     else:
                         self._fail("%s reads %s" % (cn, b))
                 elif t == "ConstantObject":
-                    reps[a] = sympy.Float(self._const_value(a), 30)
+                    if self.forcing and re.fullmatch(r"c[0-2]", str(a)):
+                        reps[a] = sympy.Symbol("_c%s" % str(a)[1])
+                    else:
+                        reps[a] = sympy.Float(self._const_value(a), 30)
                 else:
                     if a not in local:
                         self._fail("%s reads the local %s" % (cn, a))
@@ -309,7 +349,8 @@ class PhysicsCheck:
         want = self._builtin_residual(cn, pts, key_symbol)
         if set(got) != set(want):
             self._fail("%s sets residuals %s, the kernels %s" % (cn, sorted(got), sorted(want)))
-        syms = list(pts.values()) + list(dsym.values())
+        syms = list(pts.values()) + list(dsym.values()) + \
+            ([sympy.Symbol("_c%d" % k) for k in range(self.ndim)] if self.forcing else [])
         for trial in range(3):
             vals = {s: sympy.Float(self.rnd.uniform(0.3, 1.7) * self.rnd.choice((-1, 1)), 30) for s in syms}
             for v in ("rho", "p", "T", "mu", "D11"):
@@ -352,6 +393,10 @@ class PhysicsCheck:
                 R[1 + i] = -sum(skew("rhou%d" % i, j) for j in range(nd)) - d1(("p",), i)
             R[1 + nd] = -sum(skew("rhoE", j) for j in range(nd)) - sum(d1(tuple(sorted(("p", "u%d" % j))), j)
                                                                         for j in range(nd))
+            if self.forcing:  # -c_i (momentum i), -c_j u_j (energy): the channels' constant forcing
+                for i in range(nd):
+                    R[1 + i] = R[1 + i] - sympy.Symbol("_c%d" % i)
+                R[1 + nd] = R[1 + nd] - sum(sympy.Symbol("_c%d" % j) * u[j] for j in range(nd))
             return R
         mu = pts["mu"] if self.sutherland else sympy.Integer(1)
         kT = 1.0 / ((g - 1) * M * M * Pr * Re)

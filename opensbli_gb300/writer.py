@@ -247,7 +247,7 @@ class GB300Writer:
     # anything else in the time loop (filters, other equation classes, user kernels) would be
     # dropped silently, so it is refused.
     _FAMILIES = re.compile(
-        r"^(CR\w+|ConstituentRelations (evaluation|CD )|Convective (CD |residual|terms group)|Derivative evaluation CD |"
+        r"^(CR\w+|ConstituentRelations (evaluation|CD )|Convective (CD |residual|terms group|terms$)|Derivative evaluation CD |"
         r"LLF(Weno|Teno)(_reconstruction_\d+_direction| Residual)|MetricsEquation|Viscous|Grid_based_initialisation|"
         r"Save equations|Sub stage advancement|Temporal solution advancement|\w+ boundary dir\d side\d|"
         r"User kernel: (Constituent Relations evaluation|WENO reconstruction direction \d|Non-linear filter application))")
@@ -285,6 +285,8 @@ class GB300Writer:
             raise NotImplementedError("the WENO filter is lowered on 3D blocks only")
         teno = self._kernels("LLFTeno_reconstruction_")
         weno = self._kernels("LLFWeno_reconstruction_")
+        if nd == 2 and not teno and not weno and self._kernels("Convective terms"):
+            return self._lower_skew2d(precision, use_graphs, names)
         if bool(teno) == bool(weno) or len(teno or weno) != nd:
             raise NotImplementedError("wall-bounded blocks: one LLFTeno or LLFWeno reconstruction per direction "
                                       "expected")
@@ -520,6 +522,42 @@ class GB300Writer:
             raise NotImplementedError("%s: a state switched at one x0 location expected" % kname)
         # the kernels compare x0 > xs: a switch that includes c itself moves xs just below it
         return lo, hi, (c if mid == lo else math.nextafter(c, -math.inf))
+
+    def _lower_skew2d(self, precision, use_graphs, names):
+        """The 2D laminar channel (apps/channel_flow/laminar_2D/laminar_channel.py): central skew-symmetric
+        convective terms (one "Convective terms" kernel), central viscous terms with Sutherland's law on a
+        Cartesian grid, the constant forcing c_j, periodic x0, isothermal walls on both x1 faces,
+        RungeKuttaLS(3)."""
+        import sympy
+        if self._kernels("MetricsEquation") or self._kernels("Metric boundary"):
+            raise NotImplementedError("2D central-skew blocks: Cartesian grids only")
+        if not any(n.startswith("CRmu") for n in names) or self._power_law_viscosity() is not None:
+            raise NotImplementedError("2D central-skew blocks: Sutherland viscosity expected")
+        coeff = self._rk_coefficients(["Temporal solution advancement"])
+        if set(coeff) != {"rkA", "rkB"}:
+            raise NotImplementedError("RungeKuttaLS(3) coefficients rkA/rkB expected")
+        found = {n for n in names if "boundary dir" in n}
+        exch = {(c.direction, c.side) for c in self.components if type(c).__name__ == "ExchangeSelf"}
+        if found != {"IsothermalWall boundary dir1 side0", "IsothermalWall boundary dir1 side1"} or \
+                exch != {(0, "left"), (0, "right")}:
+            raise NotImplementedError("2D central-skew block boundary conditions: %s" % sorted(found))
+        forcing = {}
+        for k in self._kernels("Convective terms"):
+            for e in k.equations:
+                for a in sympy.preorder_traversal(e.rhs):
+                    if type(a).__name__ == "ConstantObject" and re.fullmatch(r"c[0-1]", str(a)):
+                        forcing[int(str(a)[1])] = a
+        closure = self._closures_2d(periodic0=True)
+        physics_check.check_algorithm(self.components, 2, viscous=True, sutherland=True, metric=False, skew=True,
+                                      forcing=bool(forcing))
+        vals = [getattr(forcing.get(d), "value", None) for d in range(2)]
+        return Plan(ndim=2, n=(64, 32, 1), delta=(1.0, 1.0, 1.0), conv="central_skew", visc="sutherland",
+                    rk="ls_rk3", precision=precision, x1_grid="uniform",
+                    bc=(("periodic", "periodic"), ("isothermal_wall", "isothermal_wall"), ("periodic", "periodic")),
+                    rk_a=coeff["rkA"], rk_b=coeff["rkB"], use_graphs=use_graphs, ic="host",
+                    closure=(("none", "none"), closure[1]),
+                    forcing=tuple(float(v) if isinstance(v, (int, float)) else 0.0 for v in vals) if forcing else None,
+                    name="channel2d", kernels=[n for n in names if n])
 
     def _lower_viscous2d_cartesian(self, precision, use_graphs, conv, averaging, names):
         """A Cartesian 2D Navier-Stokes block with a constant viscosity (apps/viscous_shock_tube/

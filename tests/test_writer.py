@@ -122,6 +122,15 @@ def test_shock_reflection_script_lowers_to_its_plan():
     assert g.dirichlet_x_switch == math.nextafter(40.0, 0.0)
 
 
+def test_laminar_channel_script_lowers_to_its_plan():
+    """The 2D laminar channel lowers with its skew-symmetric convective terms (one kernel, derivatives of
+    products formed inline, checked by the physics check), forcing, periodic x0 and walls on both x1 faces."""
+    from opensbli_gb300.plan import laminar_channel_plan
+    g = golden_plan("laminar_channel")
+    assert g.replace(kernels=[], name="", niter=None) == laminar_channel_plan(*g.n[:2]).replace(kernels=[], name="")
+    assert g.conv == "central_skew" and g.forcing == (-1.0, 0.0)
+
+
 def test_viscous_shock_tube_script_lowers_to_its_plan():
     """The viscous shock tube lowers to a Cartesian 2D block with the constant viscosity, adiabatic walls
     on three faces (ReducedAccess) and a symmetry top face without a one-sided closure."""
@@ -216,7 +225,7 @@ def test_writer_refuses_kernels_outside_the_lowered_families():
     from opensbli_gb300.writer import GB300Writer
     for case in ("tgv_central", "tgv_weno", "tgsym_central", "katzer_teno", "katzer_adaptive", "katzer_carpenter",
                  "tgv_filter", "tgv_teno_adaptive", "sbli3d_teno", "transitional_sbli", "channel_teno",
-                 "shock_reflection", "sod", "shu_osher", "euler_wave", "viscous_shock_tube"):
+                 "shock_reflection", "sod", "shu_osher", "euler_wave", "viscous_shock_tube", "laminar_channel"):
         GB300Writer._check_kernel_families(golden_plan(case).kernels)
     assert "User kernel: Non-linear filter application" in golden_plan("tgv_filter").kernels
     names = golden_plan("tgv_filter").kernels + ["User kernel: Shock sensor"]
@@ -246,10 +255,10 @@ def test_cfl_dt_tgv_weno():
 ALL_SCRIPTS = ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", "tgsym_central", "katzer_teno",
                "katzer_adaptive", "katzer_carpenter", "tgv_filter", "katzer_weno", "katzer_wenoz", "katzer_teno6",
                "tgv_teno_adaptive", "sbli3d_teno", "transitional_sbli", "channel_teno", "shock_reflection", "sod",
-               "shu_osher", "euler_wave", "viscous_shock_tube"]
+               "shu_osher", "euler_wave", "viscous_shock_tube", "laminar_channel"]
 SCRIPTS = ALL_SCRIPTS if os.environ.get("OSB_ALL_SCRIPTS") == "1" else \
     ["tgv_weno", "tgv_filter", "katzer_adaptive", "transitional_sbli", "channel_teno", "shock_reflection", "sod",
-     "euler_wave", "viscous_shock_tube"]
+     "euler_wave", "viscous_shock_tube", "laminar_channel", "tgv_central"]
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
