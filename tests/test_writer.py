@@ -257,8 +257,7 @@ ALL_SCRIPTS = ["tgv_central", "tgv_weno", "tgv_wenoz", "tgv_teno", "tgv_teno6", 
                "tgv_teno_adaptive", "sbli3d_teno", "transitional_sbli", "channel_teno", "shock_reflection", "sod",
                "shu_osher", "euler_wave", "viscous_shock_tube", "laminar_channel"]
 SCRIPTS = ALL_SCRIPTS if os.environ.get("OSB_ALL_SCRIPTS") == "1" else \
-    ["tgv_weno", "tgv_filter", "katzer_adaptive", "transitional_sbli", "channel_teno", "shock_reflection", "sod",
-     "euler_wave", "viscous_shock_tube", "laminar_channel", "tgv_central"]
+    ["tgv_weno", "katzer_adaptive", "channel_teno", "shock_reflection", "sod", "laminar_channel"]
 
 
 @pytest.mark.skipif(not os.path.isdir(os.path.join(REF, "opensbli")), reason="reference tree not present")
