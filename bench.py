@@ -15,6 +15,12 @@ own instance (one per GPU, no exchange) and value = total cell-updates / max tim
 Reference arm (--impl reference): the reference generator's own C output for this problem
 (oracle/_ref/tgv_weno, compiled with the OPS-API stand-in and OpenMP on all host cores), timed by
 its own "Total Wall time" over K steps after a W-step warm-up run.
+
+Other workloads (--config): tgv_central64 (the central Taylor-Green case), katzer512 and
+katzer512_adaptive (the 2D shock/boundary-layer block), channel129 (the compressible_TCF_TENO channel,
+129^3), shock_reflection (the 2D inviscid shock reflection, 457 x 255), tgv_adjoint128 (the discrete
+adjoint) and tgv_batch96 (an ensemble of 96 blocks); each with the reference's generated C for the
+same problem as its host-core arm where one exists.
 """
 import argparse
 import json
